@@ -1,0 +1,158 @@
+/*
+ * mrfmap_gb300.h -- C ABI of the GB300 MRFMap hot path (libmrfmap_gb300.so).
+ *
+ * One map = one occupancy volume of 8^3-voxel bricks plus the posed depth
+ * views added to it.  Every call is ordered on the map's own CUDA stream;
+ * calls that hand results to host memory block until they are ready.
+ * Plain pointers and sizes only: poses are 16 floats, row-major 4x4
+ * camera-to-world in metres (camera x right, y down, z forward); depth
+ * images are rows*cols floats, row-major, row 0 at the top, metres, with
+ * NaN / <= 0 meaning "no return".
+ *
+ * Each entry point cites the reference interface it replaces
+ * (paths inside the MRFMap project).
+ */
+#ifndef MRFMAP_GB300_H
+#define MRFMAP_GB300_H
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define MRF_API __attribute__((visibility("default")))
+#else
+#define MRF_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  MRF_OK = 0,
+  MRF_ERR_INVALID = 1,   /* bad argument */
+  MRF_ERR_CUDA = 2,      /* CUDA runtime error (mrf_last_error has text) */
+  MRF_ERR_OOM = 3,       /* device allocation failed */
+  MRF_ERR_CAPACITY = 4,  /* a 32-bit index range would overflow */
+  MRF_ERR_DEVICE = 5,    /* a kernel raised its error flag (bounds) */
+  MRF_ERR_STATE = 6      /* call not valid in the map's state */
+} mrf_status;
+
+/* brick activation policy */
+#define MRF_ACT_ENDPOINT 0 /* bricks around measured endpoints, 1-voxel halo */
+#define MRF_ACT_FULL_RAY 1 /* plus every brick a ray crosses up to d+3 sigma */
+
+/* mrf_infer flags */
+#define MRF_JACOBI 1        /* all cameras from one snapshot per iteration */
+#define MRF_INCREMENTAL 2   /* keep per-camera messages across calls */
+#define MRF_FIX_PRE_RESET 4 /* carry Pre-pass visibility across all bricks */
+#define MRF_ASYNC 8         /* enqueue only; do not wait for completion */
+
+/* Mirrors gvdb_params_t (include/mrfmap/GVDBParams.h:11-28). */
+typedef struct mrf_params {
+  float res;                /* voxel edge (m) */
+  float dims[3];            /* volume extent (m); x,y centred, z from 0 */
+  float fx, fy, cx, cy;     /* pinhole intrinsics K */
+  int rows, cols;           /* image size */
+  float prior;              /* occupancy prior */
+  int max_iters;            /* BP iterations when mrf_infer gets iters <= 0 */
+  int lookup_n;             /* 3: sigma(z)=p0+p1 z+p2 z^2, 2: linear */
+  const float* sigma_lut;   /* ceil(rows/20)*ceil(cols/20)*lookup_n floats */
+  const float* bias_lut;    /* same layout; per 20x20-pixel tile */
+  float occ_thresh;
+  float acc_thresh;
+  int activation;           /* MRF_ACT_* */
+  int reserved[7];
+} mrf_params;
+
+typedef struct mrf_map mrf_map;
+
+typedef struct mrf_stats {
+  int64_t n_views;
+  int64_t n_bricks;
+  int64_t n_rays;          /* rays with at least one incidence */
+  int64_t n_inc_pre;       /* incidences traversed by the Pre pass */
+  int64_t n_inc_post;      /* ray->voxel messages per iteration (N_inc) */
+  int64_t n_pairs;         /* (camera, voxel) pairs (N_cv) */
+  int64_t n_pairs_active;  /* pairs with cumulative length > 0.1 */
+  int64_t n_vox_touched;   /* distinct voxels with a message (N_vox) */
+  int64_t iters_done;      /* iterations run by the last mrf_infer */
+  int64_t kernel_launches; /* kernels launched by the last mrf_infer */
+  double build_ms;         /* last incidence-list build */
+  double infer_ms;         /* last mrf_infer, device time */
+} mrf_stats;
+
+/* Map construction: GVDBInference(...) + GVDBMRFMap::gpuAllocate
+ * (src/GVDBInference.cpp:20-37, src/GVDBMRFMap.cpp:23-93). */
+MRF_API mrf_status mrf_create(const mrf_params* params, mrf_map** out);
+MRF_API void mrf_destroy(mrf_map* map);
+/* Text of the last error raised on this thread. */
+MRF_API const char* mrf_last_error(void);
+
+/* GVDBInference::add_camera_with_depth (src/GVDBInference.cpp:58-64):
+ * uploads and cleans the depth image (src/GVDBImage.cpp:13-60) and
+ * activates bricks (src/GVDBCamera.cpp:70-112). */
+MRF_API mrf_status mrf_add_view(mrf_map* map, const float* pose, const float* depth_host,
+                        int* view_id);
+/* Same, with the depth image already in device memory. */
+MRF_API mrf_status mrf_add_view_device(mrf_map* map, const float* pose, const float* depth_dev,
+                               int* view_id);
+/* GVDBInference::set_pose (src/GVDBInference.cpp:66-82): moves a view and
+ * activates bricks for its new pose. */
+MRF_API mrf_status mrf_set_pose(mrf_map* map, int view_id, const float* pose);
+
+/* GVDBInference::perform_inference_ids (src/GVDBInference.cpp:100-178):
+ * zeroes the messages of the cameras in ids (unless MRF_INCREMENTAL) and
+ * runs iters BP iterations over every camera. ids == NULL -> all cameras. */
+MRF_API mrf_status mrf_infer(mrf_map* map, const int* ids, int n_ids, int iters, int flags);
+/* Extension: log-odds back to the prior, beliefs to 0, messages to 0. */
+MRF_API mrf_status mrf_reset_state(mrf_map* map);
+
+/* GVDBInference::get_likelihood_image / compute_likelihood
+ * (src/GVDBInference.cpp:180-193).  out_img (rows*cols, host) may be NULL. */
+MRF_API mrf_status mrf_likelihood_view(mrf_map* map, int view_id, float* out_img, float* out_sum);
+/* GVDBInference::get_likelihood_image_at_pose (src/GVDBInference.cpp:195-240)
+ * and GVDBMapLikelihoodEstimator::get_likelihood_image_at_pose
+ * (src/GVDBMapLikelihoodEstimator.cpp:294-314); host buffers. */
+MRF_API mrf_status mrf_likelihood(mrf_map* map, const float* pose, const float* depth_host,
+                          float* out_img, float* out_sum);
+/* Same with device buffers: depth_dev in, out_img_dev (may be NULL) and
+ * out_sum_dev (one float) out; stream-ordered, does not block. */
+MRF_API mrf_status mrf_likelihood_device(mrf_map* map, const float* pose, const float* depth_dev,
+                                 float* out_img_dev, float* out_sum_dev);
+
+/* GVDBMRFMap::get_occupied_bricks(0) (src/GVDBMRFMap.cpp:137-152). */
+MRF_API mrf_status mrf_num_bricks(mrf_map* map, int64_t* n_bricks);
+/* centres: n*3 floats, brick centres in voxel units (the reference's GVDB
+ * world frame); beliefs: n*512 floats, element (x*8+y)*8+z
+ * (GVDBMRFMap::get_alphas, src/GVDBMRFMap.cpp:154-208).  Either may be NULL.
+ * n must equal mrf_num_bricks (else MRF_ERR_INVALID, as the reference throws). */
+MRF_API mrf_status mrf_read_bricks(mrf_map* map, float* centres, float* beliefs, int64_t n);
+/* Extension: total log-odds per voxel, same layout. */
+MRF_API mrf_status mrf_read_logodds(mrf_map* map, float* logodds, int64_t n);
+/* Upper-level node centres (GVDBMRFMap::get_occupied_bricks(lev>0)). */
+MRF_API mrf_status mrf_num_nodes(mrf_map* map, int level, int64_t* n);
+MRF_API mrf_status mrf_read_nodes(mrf_map* map, int level, float* centres, int64_t n);
+
+/* GVDBMapLikelihoodEstimator::load_map (src/GVDBMapLikelihoodEstimator.cpp:168-240):
+ * points n*3 in voxel units, occupancies n floats written into the belief
+ * field after activating the bricks around each point. */
+MRF_API mrf_status mrf_load_map(mrf_map* map, const float* points, const float* occupancies,
+                        int64_t n);
+
+/* Introspection of one view's incidence lists (after building them):
+ * meta rows*cols*5 ints per pixel {n_pre, n_post, r0, rinf, inf_gate};
+ * vox / len / mu: the view's incidences in ray order (pixel-major), at most
+ * cap entries; *n_inc receives the count.  Any output may be NULL. */
+MRF_API mrf_status mrf_view_incidences(mrf_map* map, int view_id, int* meta, uint32_t* vox, float* len,
+                               float* mu, int64_t cap, int64_t* n_inc);
+
+/* Device pointers of the map state (for zero-copy consumers and benches). */
+MRF_API mrf_status mrf_device_beliefs(mrf_map* map, const float** beliefs, int64_t* n_voxels);
+MRF_API mrf_status mrf_stats_get(mrf_map* map, mrf_stats* out);
+/* The CUDA stream the map enqueues on (cudaStream_t as void*). */
+MRF_API mrf_status mrf_get_stream(mrf_map* map, void** stream);
+MRF_API mrf_status mrf_synchronize(mrf_map* map);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,513 @@
+// mrf_build.cu -- per-keyframe work that runs once per brick-set change:
+// depth clean-up, brick activation, the 3D-DDA traversal that emits each
+// ray's incidence list, and the (camera, voxel) pair / CSR construction.
+//
+// Reference behaviour restated here (paths inside the MRFMap project):
+//   depth clean-up            src/GVDBImage.cpp:32-40
+//   endpoint back-projection  src/GVDBImage.cpp:48-56, src/GVDBCamera.cpp:70-100
+//   activation radius 1       src/GVDBMRFMap.cpp:117-135
+//   per-brick stop rules      src/cuda/gvdbkernels.cu:568, 816, 1035
+//   infinity-term gate        src/cuda/gvdbkernels.cu:1196-1208
+//   Pre-pass visibility reset src/cuda/gvdbkernels.cu:708-715
+#include <cub/cub.cuh>
+
+#include "mrf_geometry.cuh"
+#include "mrf_internal.h"
+
+namespace mrf {
+
+namespace {
+
+constexpr int kThreads = 256;
+
+inline unsigned grid_for(int64_t n, int t = kThreads) {
+  int64_t b = (n + t - 1) / t;
+  return (unsigned)(b < 1 ? 1 : b);
+}
+
+__global__ void k_clean_depth(const float* __restrict__ in, float* __restrict__ out, int rows,
+                              int cols) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= rows * cols) return;
+  float d = in[i];
+  float v = isfinite(d) ? d : -1.0f;
+  if (rows == 480 && cols == 848) {
+    int x = i % cols, y = i / cols;
+    if (x < 24 || x >= cols - 24 || y < 20 || y >= rows - 20) v = -1.0f;
+  }
+  out[i] = v;
+}
+
+__device__ __forceinline__ int floordiv8(int v) { return v >= 0 ? v / 8 : -((-v + 7) / 8); }
+
+__device__ __forceinline__ void mark_point(const Geom& g, float px, float py, float pz,
+                                           uint8_t* flags) {
+  int lo[3], hi[3];
+  float pv[3] = {px, py, pz};
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    int vi = (int)floorf(pv[a]);
+    lo[a] = max(floordiv8(vi - 1), 0);
+    hi[a] = min(floordiv8(vi + 1), g.NB[a] - 1);
+  }
+  for (int bx = lo[0]; bx <= hi[0]; ++bx)
+    for (int by = lo[1]; by <= hi[1]; ++by)
+      for (int bz = lo[2]; bz <= hi[2]; ++bz)
+        flags[((int64_t)bx * g.NB[1] + by) * g.NB[2] + bz] = 1;
+}
+
+__global__ void k_activate(Geom g, Pose P, const float* __restrict__ depth, int policy,
+                           uint8_t* __restrict__ flags) {
+  int pix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix >= g.rows * g.cols) return;
+  float d = depth[pix];
+  if (!(d > 0.0f)) return;
+  int x = pix % g.cols, y = pix / g.cols;
+  // back-projection with fx on both axes and integer pixel coordinates
+  float f = fd(d, g.fx);
+  float X = fm(f, fs((float)x, g.cx));
+  float Y = fm(f, fs((float)y, g.cy));
+  float pv[3];
+  bool inside = true;
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    float pw = fa(fa(fa(fm(P.m[a * 4 + 0], X), fm(P.m[a * 4 + 1], Y)), fm(P.m[a * 4 + 2], d)),
+                  P.m[a * 4 + 3]);
+    pv[a] = fa(fm(pw, g.inv_res), g.off[a]);
+    if (!(pv[a] >= 0.0f && pv[a] < g.hi[a])) inside = false;
+  }
+  if (inside) mark_point(g, pv[0], pv[1], pv[2], flags);
+  if (policy == 1) {
+    const float* sg = lut_at(g, g.sigma, x, y);
+    float lim = fa(d, fm(3.0f, poly_f(sg, g.lookup_n, d)));
+    Ray ray;
+    ray_setup(g, P, x, y, ray);
+    Dda r;
+    if (dda_init(r, g, ray)) {
+      int vx, vy, vz;
+      float l, tin, te;
+      int64_t cur = -1;
+      while (dda_next(r, g, vx, vy, vz, l, tin, te)) {
+        if (fm(tin, ray.mult) >= lim) break;
+        int64_t lin = brick_lin(g, vx, vy, vz);
+        if (lin != cur) {
+          flags[lin] = 1;
+          cur = lin;
+        }
+      }
+    }
+  }
+}
+
+__global__ void k_activate_points(Geom g, const float* __restrict__ pts, int64_t n,
+                                  uint8_t* __restrict__ flags) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float px = pts[3 * i], py = pts[3 * i + 1], pz = pts[3 * i + 2];
+  if (!(px >= 0.0f && py >= 0.0f && pz >= 0.0f && px < (float)g.E[0] && py < (float)g.E[1] &&
+        pz < (float)g.E[2]))
+    return;
+  mark_point(g, px, py, pz, flags);
+}
+
+__global__ void k_new_indicator(const uint8_t* __restrict__ flags, const int* __restrict__ slot,
+                                int* __restrict__ ind, int64_t n) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  ind[i] = (flags[i] && slot[i] < 0) ? 1 : 0;
+}
+
+__global__ void k_assign_slots(Geom g, const int* __restrict__ ind, const int* __restrict__ scan,
+                               int nb_base, int* __restrict__ slot, int* __restrict__ coord,
+                               int64_t n) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || !ind[i]) return;
+  int s = nb_base + scan[i];
+  slot[i] = s;
+  int bz = (int)(i % g.NB[2]);
+  int by = (int)((i / g.NB[2]) % g.NB[1]);
+  int bx = (int)(i / ((int64_t)g.NB[2] * g.NB[1]));
+  coord[3 * s + 0] = bx;
+  coord[3 * s + 1] = by;
+  coord[3 * s + 2] = bz;
+}
+
+__global__ void k_fill_new_voxels(float* L, float* belief, int64_t v0, int64_t v1, float lp) {
+  int64_t i = v0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= v1) return;
+  L[i] = lp;
+  belief[i] = 0.0f;
+}
+
+// set_channel_kernel (gvdbkernels.cu:1040-1064): write occupancies of points
+// (voxel units) into the belief field
+__global__ void k_set_points(Geom g, const float* __restrict__ pts, const float* __restrict__ occ,
+                             int64_t n, float* __restrict__ belief) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float px = pts[3 * i], py = pts[3 * i + 1], pz = pts[3 * i + 2];
+  if (!(px >= 0.0f && py >= 0.0f && pz >= 0.0f && px < (float)g.E[0] && py < (float)g.E[1] &&
+        pz < (float)g.E[2]))
+    return;
+  int vx = (int)floorf(px), vy = (int)floorf(py), vz = (int)floorf(pz);
+  int s = g.brick_slot[brick_lin(g, vx, vy, vz)];
+  if (s < 0) return;
+  belief[(int64_t)s * kBrickVox + voxel_local(vx, vy, vz)] = occ[i];
+}
+
+// One thread per pixel walks the DDA through the active bricks.  Runs of
+// voxels in one brick end with the reference's per-brick stop tests; the
+// count pass and the emit pass execute the identical loop.
+template <bool EMIT>
+__global__ void __launch_bounds__(kThreads)
+    k_trace(Geom g, Pose P, const float* __restrict__ depth, uint32_t* __restrict__ counts,
+            const uint32_t* __restrict__ pix_off, uint32_t inc_base, RayMeta* __restrict__ meta,
+            uint32_t* __restrict__ inc_vox, float* __restrict__ inc_len,
+            float* __restrict__ inc_mu, int* __restrict__ err) {
+  int pix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix >= g.rows * g.cols) return;
+  float d = depth[pix];
+  int count = 0, n_pre = -1, n_post = -1, r0 = -1, run_start = 0;
+  bool gate = false;
+  uint32_t base = EMIT ? pix_off[pix] : 0;
+  if (d > 0.0f) {
+    int x = pix % g.cols, y = pix / g.cols;
+    const float* sg = lut_at(g, g.sigma, x, y);
+    const float* bs = lut_at(g, g.bias, x, y);
+    const int n = g.lookup_n;
+    Ray ray;
+    ray_setup(g, P, x, y, ray);
+    Dda r;
+    if (dda_init(r, g, ray)) {
+      int64_t cur = -1;
+      int slot = -1;
+      bool run_open = false;
+      float s_last = 0.0f;
+      int vx, vy, vz;
+      float l, tin, te;
+      while (dda_next(r, g, vx, vy, vz, l, tin, te)) {
+        int64_t lin = brick_lin(g, vx, vy, vz);
+        if (lin != cur) {
+          if (run_open) {
+            run_open = false;
+            float lhs = fa(s_last, poly_f(bs, n, s_last));
+            float rhs = fa(d, fm(3.0f, poly_f(sg, n, s_last)));
+            if (n_post < 0 && lhs >= rhs) n_post = count;
+            if (lhs > rhs) {
+              n_pre = count;
+              break;
+            }
+          }
+          cur = lin;
+          slot = g.brick_slot[lin];
+        }
+        if (slot < 0) continue;
+        if (count >= kMaxRayLen) {
+          atomicOr(err, 1);
+          break;
+        }
+        float s = fm(te, ray.mult);
+        if (!run_open) run_start = count;
+        if (EMIT) {
+          uint32_t k = base + (uint32_t)count;
+          inc_vox[k] = (uint32_t)slot * kBrickVox + voxel_local(vx, vy, vz);
+          inc_len[k] = l;
+          bool z = potential_is_zero(sg, bs, n, s, d);
+          inc_mu[k] = z ? 0.0f : potential(sg, bs, n, s, d);
+          if (r0 < 0 && !z) r0 = run_start;
+        }
+        run_open = true;
+        s_last = s;
+        ++count;
+      }
+      if (n_pre < 0 && run_open) {
+        float lhs = fa(s_last, poly_f(bs, n, s_last));
+        float rhs = fa(d, fm(3.0f, poly_f(sg, n, s_last)));
+        if (n_post < 0 && lhs >= rhs) n_post = count;
+        if (lhs > rhs) n_pre = count;
+      }
+      if (n_pre < 0) {
+        n_pre = count;
+        if (count > 0) gate = d > fa(s_last, poly_f(bs, n, s_last));
+      }
+    }
+  }
+  if (n_pre < 0) n_pre = count;
+  if (n_post < 0) n_post = count;
+  if (!EMIT) {
+    counts[pix] = (uint32_t)n_pre;
+  } else {
+    RayMeta m;
+    m.off = inc_base + base;
+    m.n_pre = (uint16_t)n_pre;
+    m.n_post = (uint16_t)n_post;
+    m.r0 = (uint16_t)(r0 >= 0 ? r0 : n_pre);
+    m.rinf = (uint16_t)(r0 >= 0 ? r0 : run_start);
+    m.flags = gate ? 1u : 0u;
+    meta[pix] = m;
+  }
+}
+
+__global__ void k_first_touch(const uint32_t* __restrict__ vox, uint32_t n, uint32_t* first) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  atomicMin(&first[vox[i]], i);
+}
+
+__global__ void k_flag_first(const uint32_t* __restrict__ vox, uint32_t n,
+                             const uint32_t* __restrict__ first, uint32_t* __restrict__ flag) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  flag[i] = first[vox[i]] == i ? 1u : 0u;
+}
+
+__global__ void k_pair_assign(const uint32_t* __restrict__ vox, uint32_t n,
+                              const uint32_t* __restrict__ flag, const uint32_t* __restrict__ scan,
+                              uint32_t pair_base, uint32_t* __restrict__ pair_vox, uint32_t* first) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || !flag[i]) return;
+  uint32_t p = pair_base + scan[i];
+  pair_vox[p] = vox[i];
+  first[vox[i]] = p;
+}
+
+__global__ void k_inc_pair(const uint32_t* __restrict__ vox, uint32_t n,
+                           const uint32_t* __restrict__ first, uint32_t* __restrict__ inc_pair) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  inc_pair[i] = first[vox[i]];
+}
+
+__global__ void k_reset_first(const uint32_t* __restrict__ pair_vox, uint32_t np, uint32_t* first) {
+  uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= np) return;
+  first[pair_vox[p]] = 0xFFFFFFFFu;
+}
+
+// sort keys: local pair id for incidences that receive a message, npairs
+// (sorted last) for Pre-only incidences
+__global__ void k_sort_keys(const RayMeta* __restrict__ meta, int nrays, uint32_t inc_base,
+                            const uint32_t* __restrict__ inc_pair, uint32_t pair_base,
+                            uint32_t npairs, uint32_t* __restrict__ keys,
+                            uint32_t* __restrict__ vals) {
+  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrays) return;
+  RayMeta m = meta[r];
+  uint32_t o = m.off - inc_base;
+  for (int i = 0; i < m.n_pre; ++i) {
+    uint32_t k = o + (uint32_t)i;
+    keys[k] = i < m.n_post ? inc_pair[m.off + i] - pair_base : npairs;
+    vals[k] = k;
+  }
+}
+
+__global__ void k_seg_bounds(const uint32_t* __restrict__ skeys, uint32_t n, uint32_t npairs,
+                             uint32_t* __restrict__ seg) {
+  uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p > npairs) return;
+  uint32_t lo = 0, hi = n;
+  while (lo < hi) {
+    uint32_t mid = lo + ((hi - lo) >> 1);
+    if (skeys[mid] < p) lo = mid + 1;
+    else hi = mid;
+  }
+  seg[p] = lo;
+}
+
+// cumulative length per pair: fp32, summed in increasing incidence order
+// (the order the cumulative-length pass visits them, pixel-major)
+__global__ void k_pair_init(const uint32_t* __restrict__ seg_local,
+                            const uint32_t* __restrict__ perm_local, uint32_t inc_base,
+                            uint32_t npairs, const float* __restrict__ inc_len, uint32_t perm_base,
+                            uint32_t pair_base, uint32_t* __restrict__ seg, float* __restrict__ cum) {
+  uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p > npairs) return;
+  seg[pair_base + p] = perm_base + seg_local[p];
+  if (p == npairs) return;
+  float c = 0.0f;
+  for (uint32_t k = seg_local[p]; k < seg_local[p + 1]; ++k) c += inc_len[inc_base + perm_local[k]];
+  cum[pair_base + p] = c;
+}
+
+__global__ void k_perm_copy(const uint32_t* __restrict__ perm_local, uint32_t n, uint32_t inc_base,
+                            uint32_t* __restrict__ perm) {
+  uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  perm[k] = inc_base + perm_local[k];
+}
+
+__global__ void k_iota(uint32_t* out, uint32_t n) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) out[i] = i;
+}
+
+}  // namespace
+
+cudaError_t launch_clean_depth(const float* in, float* out, int rows, int cols, cudaStream_t s) {
+  k_clean_depth<<<grid_for((int64_t)rows * cols), kThreads, 0, s>>>(in, out, rows, cols);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_activate(const Geom& g, const Pose& P, const float* depth, int policy,
+                            uint8_t* flags, cudaStream_t s) {
+  k_activate<<<grid_for((int64_t)g.rows * g.cols, 128), 128, 0, s>>>(g, P, depth, policy, flags);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_activate_points(const Geom& g, const float* pts, int64_t n, uint8_t* flags,
+                                   cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_activate_points<<<grid_for(n), kThreads, 0, s>>>(g, pts, n, flags);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_new_indicator(const uint8_t* flags, const int* slot, int* ind, int64_t n,
+                                 cudaStream_t s) {
+  k_new_indicator<<<grid_for(n), kThreads, 0, s>>>(flags, slot, ind, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_assign_slots2(const Geom& g, const int* ind, const int* scan, int nb_base,
+                                 int* brick_slot, int* brick_coord, int64_t n, cudaStream_t s) {
+  k_assign_slots<<<grid_for(n), kThreads, 0, s>>>(g, ind, scan, nb_base, brick_slot, brick_coord, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fill_new_voxels(float* L, float* belief, int64_t v0, int64_t v1, float lp,
+                                   cudaStream_t s) {
+  if (v1 <= v0) return cudaSuccess;
+  k_fill_new_voxels<<<grid_for(v1 - v0), kThreads, 0, s>>>(L, belief, v0, v1, lp);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_set_points(const Geom& g, const float* pts, const float* occ, int64_t n,
+                              float* belief, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_set_points<<<grid_for(n), kThreads, 0, s>>>(g, pts, occ, n, belief);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_trace_count(const Geom& g, const Pose& P, const float* depth, uint32_t* counts,
+                               int* err, cudaStream_t s) {
+  k_trace<false><<<grid_for((int64_t)g.rows * g.cols), kThreads, 0, s>>>(
+      g, P, depth, counts, nullptr, 0, nullptr, nullptr, nullptr, nullptr, err);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_trace_emit(const Geom& g, const Pose& P, const float* depth,
+                              const uint32_t* pix_off, uint32_t inc_base, RayMeta* meta,
+                              uint32_t* inc_vox, float* inc_len, float* inc_mu, int* err,
+                              cudaStream_t s) {
+  k_trace<true><<<grid_for((int64_t)g.rows * g.cols), kThreads, 0, s>>>(
+      g, P, depth, nullptr, pix_off, inc_base, meta, inc_vox, inc_len, inc_mu, err);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_first_touch(const uint32_t* inc_vox, uint32_t n, uint32_t* first, cudaStream_t s) {
+  if (!n) return cudaSuccess;
+  k_first_touch<<<grid_for(n), kThreads, 0, s>>>(inc_vox, n, first);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_flag_first(const uint32_t* inc_vox, uint32_t n, const uint32_t* first,
+                              uint32_t* flag, cudaStream_t s) {
+  if (!n) return cudaSuccess;
+  k_flag_first<<<grid_for(n), kThreads, 0, s>>>(inc_vox, n, first, flag);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pair_assign(const uint32_t* inc_vox, uint32_t n, const uint32_t* flag,
+                               const uint32_t* scan, uint32_t pair_base, uint32_t* pair_vox,
+                               uint32_t* first, cudaStream_t s) {
+  if (!n) return cudaSuccess;
+  k_pair_assign<<<grid_for(n), kThreads, 0, s>>>(inc_vox, n, flag, scan, pair_base, pair_vox, first);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_inc_pair(const uint32_t* inc_vox, uint32_t n, const uint32_t* first,
+                            uint32_t* inc_pair, cudaStream_t s) {
+  if (!n) return cudaSuccess;
+  k_inc_pair<<<grid_for(n), kThreads, 0, s>>>(inc_vox, n, first, inc_pair);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_reset_first(const uint32_t* pair_vox, uint32_t npairs, uint32_t* first,
+                               cudaStream_t s) {
+  if (!npairs) return cudaSuccess;
+  k_reset_first<<<grid_for(npairs), kThreads, 0, s>>>(pair_vox, npairs, first);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sort_keys(const RayMeta* meta, int nrays, uint32_t inc_base,
+                             const uint32_t* inc_pair, uint32_t pair_base, uint32_t npairs,
+                             uint32_t* keys, uint32_t* vals, cudaStream_t s) {
+  if (nrays <= 0) return cudaSuccess;
+  k_sort_keys<<<grid_for(nrays), kThreads, 0, s>>>(meta, nrays, inc_base, inc_pair, pair_base,
+                                                   npairs, keys, vals);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_seg_bounds(const uint32_t* skeys, uint32_t n, uint32_t npairs, uint32_t* seg,
+                              cudaStream_t s) {
+  k_seg_bounds<<<grid_for((int64_t)npairs + 1), kThreads, 0, s>>>(skeys, n, npairs, seg);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pair_init2(const uint32_t* seg_local, const uint32_t* perm_local,
+                              uint32_t inc_base, uint32_t npairs, const float* inc_len,
+                              uint32_t perm_base, uint32_t pair_base, uint32_t* seg, float* cum,
+                              cudaStream_t s) {
+  k_pair_init<<<grid_for((int64_t)npairs + 1), kThreads, 0, s>>>(
+      seg_local, perm_local, inc_base, npairs, inc_len, perm_base, pair_base, seg, cum);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_perm_copy(const uint32_t* perm_local, uint32_t n, uint32_t inc_base,
+                             uint32_t* perm, cudaStream_t s) {
+  if (!n) return cudaSuccess;
+  k_perm_copy<<<grid_for(n), kThreads, 0, s>>>(perm_local, n, inc_base, perm);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_iota(uint32_t* out, uint32_t n, cudaStream_t s) {
+  if (!n) return cudaSuccess;
+  k_iota<<<grid_for(n), kThreads, 0, s>>>(out, n);
+  return cudaGetLastError();
+}
+
+size_t scan_temp_bytes(uint32_t n) {
+  size_t b = 0;
+  cub::DeviceScan::ExclusiveSum(nullptr, b, (const uint32_t*)nullptr, (uint32_t*)nullptr, (int)n);
+  return b;
+}
+
+cudaError_t exclusive_scan_u32(void* tmp, size_t tmp_bytes, const uint32_t* in, uint32_t* out,
+                               uint32_t n, cudaStream_t s) {
+  return cub::DeviceScan::ExclusiveSum(tmp, tmp_bytes, in, out, (int)n, s);
+}
+
+size_t scan_temp_bytes_i32(int64_t n) {
+  size_t b = 0;
+  cub::DeviceScan::ExclusiveSum(nullptr, b, (const int*)nullptr, (int*)nullptr, (int)n);
+  return b;
+}
+
+cudaError_t exclusive_scan_i32(void* tmp, size_t tmp_bytes, const int* in, int* out, int64_t n,
+                               cudaStream_t s) {
+  return cub::DeviceScan::ExclusiveSum(tmp, tmp_bytes, in, out, (int)n, s);
+}
+
+size_t sort_temp_bytes(uint32_t n, int bits) {
+  size_t b = 0;
+  cub::DeviceRadixSort::SortPairs(nullptr, b, (const uint32_t*)nullptr, (uint32_t*)nullptr,
+                                  (const uint32_t*)nullptr, (uint32_t*)nullptr, (int)n, 0, bits);
+  return b;
+}
+
+cudaError_t sort_pairs_u32(void* tmp, size_t tmp_bytes, const uint32_t* kin, uint32_t* kout,
+                           const uint32_t* vin, uint32_t* vout, uint32_t n, int bits,
+                           cudaStream_t s) {
+  return cub::DeviceRadixSort::SortPairs(tmp, tmp_bytes, kin, kout, vin, vout, (int)n, 0, bits, s);
+}
+
+}  // namespace mrf

@@ -1,0 +1,988 @@
+// mrf_capi.cu -- the C ABI (include/mrfmap_gb300.h): map object, device
+// memory, the build of the incidence lists and the BP schedule.
+//
+// Layout in HBM (one map):
+//   brick table    int32 [NB0*NB1*NB2]       dense brick grid -> pool slot
+//   voxel state    fp32 L, fp32 belief        [slots*512], slot-major,
+//                                              voxel (x*8+y)*8+z in a slot
+//   rays           RayMeta [views*rows*cols]  pixel-major per view
+//   incidences     u32 pair, fp32 len, fp32 mu, fp32 p*len   [N_inc]
+//                  ray order (pixel-major, then along the ray)
+//   pairs          u32 voxel, fp32 m, fp32 cum_len, float2 (q, ln q),
+//                  fp32 dm, u32 seg   [N_cv], first-touch order per view
+//   perm           u32 [N_post] incidence ids grouped by pair (CSR)
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/mrfmap_gb300.h"
+#include "mrf_internal.h"
+
+
+using namespace mrf;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+struct Fail {
+  mrf_status st;
+};
+
+void set_err(const std::string& s) { g_last_error = s; }
+
+#define CK(expr)                                                                          \
+  do {                                                                                    \
+    cudaError_t _e = (expr);                                                              \
+    if (_e != cudaSuccess) {                                                              \
+      set_err(std::string(#expr) + ": " + cudaGetErrorString(_e));                        \
+      throw Fail{_e == cudaErrorMemoryAllocation ? MRF_ERR_OOM : MRF_ERR_CUDA};           \
+    }                                                                                     \
+  } while (0)
+
+void fail(mrf_status st, const std::string& msg) {
+  set_err(msg);
+  throw Fail{st};
+}
+
+// growable device buffer
+struct DBuf {
+  void* p = nullptr;
+  size_t cap = 0;
+  void reserve(size_t bytes, bool keep, cudaStream_t s) {
+    if (bytes <= cap) return;
+    size_t nc = std::max(bytes, cap + cap / 2);
+    void* q = nullptr;
+    CK(cudaMalloc(&q, nc));
+    if (keep && p && cap) CK(cudaMemcpyAsync(q, p, cap, cudaMemcpyDeviceToDevice, s));
+    if (p) {
+      CK(cudaStreamSynchronize(s));
+      cudaFree(p);
+    }
+    p = q;
+    cap = nc;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+  template <typename T>
+  T* as() const {
+    return reinterpret_cast<T*>(p);
+  }
+};
+
+struct View {
+  Pose pose;
+  DBuf depth;
+  uint32_t inc_base = 0, n_inc = 0;
+  uint32_t pair_base = 0, n_pairs = 0;
+  uint32_t perm_base = 0, n_perm = 0;
+};
+
+uint32_t u32_checked(int64_t v, const char* what) {
+  if (v < 0 || v > (int64_t)0xFFFFFFF0ll) fail(MRF_ERR_CAPACITY, std::string(what) + " exceeds 32-bit range");
+  return (uint32_t)v;
+}
+
+}  // namespace
+
+struct mrf_map {
+  mrf_params prm;
+  std::vector<float> sigma, bias;
+  int device = 0, num_sms = 1;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  Geom g{};
+  DBuf d_sigma, d_bias, d_slot, d_coord, d_L, d_belief;
+  int64_t nb_grid = 0, n_bricks = 0;
+  std::vector<int> h_coord;
+  int version = 0, built_version = -1;
+  bool has_messages = false;
+  std::vector<View> views;
+  // arenas
+  DBuf meta, inc_pair, inc_len, inc_mu, inc_pl, pair_vox, pair_m, pair_cum, pair_q, pair_dm,
+      pair_seg, perm;
+  int64_t n_inc = 0, n_pairs = 0, n_perm = 0;
+  // jacobi voxel CSR
+  DBuf vseg, vpairs, vvox;
+  uint32_t n_vvox = 0;
+  int jacobi_version = -1;
+  // scratch
+  DBuf s_first, s_flags, s_ind, s_scan, s_tmp, s_counts, s_offs, s_vox, s_k0, s_k1, s_v0, s_v1,
+      s_seg, s_dense, s_err, s_depth_in, s_depth, s_img, s_part, s_sum;
+  int64_t first_cap_vox = 0;
+  mrf_stats stats{};
+
+  BpArrays bp() const {
+    BpArrays a;
+    a.meta = meta.as<RayMeta>();
+    a.inc_pair = inc_pair.as<uint32_t>();
+    a.inc_len = inc_len.as<float>();
+    a.inc_mu = inc_mu.as<float>();
+    a.inc_pl = inc_pl.as<float>();
+    a.pair_vox = pair_vox.as<uint32_t>();
+    a.pair_m = pair_m.as<float>();
+    a.pair_cum = pair_cum.as<float>();
+    a.pair_q = pair_q.as<float2>();
+    a.pair_dm = pair_dm.as<float>();
+    a.pair_seg = pair_seg.as<uint32_t>();
+    a.perm = perm.as<uint32_t>();
+    a.L = d_L.as<float>();
+    a.belief = d_belief.as<float>();
+    return a;
+  }
+  int64_t hw() const { return (int64_t)prm.rows * prm.cols; }
+};
+
+namespace {
+
+void sync(mrf_map* m) { CK(cudaStreamSynchronize(m->stream)); }
+
+template <typename T>
+T read1(mrf_map* m, const T* dptr) {
+  T v;
+  CK(cudaMemcpyAsync(&v, dptr, sizeof(T), cudaMemcpyDeviceToHost, m->stream));
+  sync(m);
+  return v;
+}
+
+void check_device_err(mrf_map* m) {
+  int e = read1(m, m->s_err.as<int>());
+  if (e) {
+    CK(cudaMemsetAsync(m->s_err.p, 0, sizeof(int), m->stream));
+    fail(MRF_ERR_DEVICE, "a kernel raised its error flag (ray longer than 65535 incidences)");
+  }
+}
+
+void ensure_first(mrf_map* m) {
+  int64_t nv = m->n_bricks * kBrickVox;
+  if (nv > m->first_cap_vox) {
+    m->s_first.reserve((size_t)nv * 4, false, m->stream);
+    m->first_cap_vox = (int64_t)(m->s_first.cap / 4);
+    CK(cudaMemsetAsync(m->s_first.p, 0xFF, m->s_first.cap, m->stream));
+  }
+}
+
+// ---- activation --------------------------------------------------------
+void commit_new_bricks(mrf_map* m) {
+  int64_t n = m->nb_grid;
+  m->s_ind.reserve((size_t)n * 4, false, m->stream);
+  m->s_scan.reserve((size_t)n * 4, false, m->stream);
+  CK(launch_new_indicator(m->s_flags.as<uint8_t>(), m->d_slot.as<int>(), m->s_ind.as<int>(), n,
+                          m->stream));
+  size_t tb = scan_temp_bytes_i32(n);
+  m->s_tmp.reserve(tb, false, m->stream);
+  CK(exclusive_scan_i32(m->s_tmp.p, tb, m->s_ind.as<int>(), m->s_scan.as<int>(), n, m->stream));
+  int last_scan = read1(m, m->s_scan.as<int>() + (n - 1));
+  int last_ind = read1(m, m->s_ind.as<int>() + (n - 1));
+  int add = last_scan + last_ind;
+  if (add == 0) return;
+  int64_t nb_new = m->n_bricks + add;
+  if ((nb_new * kBrickVox) > (int64_t)0xFFFFFFF0ll) fail(MRF_ERR_CAPACITY, "brick pool exceeds 32-bit voxel ids");
+  m->d_coord.reserve((size_t)nb_new * 12, true, m->stream);
+  m->d_L.reserve((size_t)nb_new * kBrickVox * 4, true, m->stream);
+  m->d_belief.reserve((size_t)nb_new * kBrickVox * 4, true, m->stream);
+  CK(launch_assign_slots2(m->g, m->s_ind.as<int>(), m->s_scan.as<int>(), (int)m->n_bricks,
+                          m->d_slot.as<int>(), m->d_coord.as<int>(), n, m->stream));
+  float lp = logf(m->prm.prior) - logf(1.0f - m->prm.prior);
+  CK(launch_fill_new_voxels(m->d_L.as<float>(), m->d_belief.as<float>(), m->n_bricks * kBrickVox,
+                            nb_new * kBrickVox, lp, m->stream));
+  m->h_coord.resize((size_t)nb_new * 3);
+  CK(cudaMemcpyAsync(m->h_coord.data() + m->n_bricks * 3, m->d_coord.as<int>() + m->n_bricks * 3,
+                     (size_t)add * 12, cudaMemcpyDeviceToHost, m->stream));
+  sync(m);
+  m->n_bricks = nb_new;
+  m->version++;
+}
+
+void activate_view(mrf_map* m, const View& v) {
+  CK(cudaMemsetAsync(m->s_flags.p, 0, (size_t)m->nb_grid, m->stream));
+  m->g.brick_slot = m->d_slot.as<int>();
+  CK(launch_activate(m->g, v.pose, v.depth.as<float>(), m->prm.activation, m->s_flags.as<uint8_t>(),
+                     m->stream));
+  commit_new_bricks(m);
+}
+
+// ---- incidence lists ---------------------------------------------------
+void rebuild(mrf_map* m) {
+  const int V = (int)m->views.size();
+  const int64_t HW = m->hw();
+  m->g.brick_slot = m->d_slot.as<int>();
+  CK(cudaEventRecord(m->ev0, m->stream));
+  // keep old pair arrays for message remapping
+  bool remap = m->has_messages && m->n_pairs > 0;
+  DBuf old_vox, old_m;
+  std::vector<View> old_views;
+  if (remap) {
+    old_vox = m->pair_vox;
+    old_m = m->pair_m;
+    m->pair_vox = DBuf{};
+    m->pair_m = DBuf{};
+    old_views = std::vector<View>();
+    for (auto& v : m->views) {
+      View c;
+      c.pair_base = v.pair_base;
+      c.n_pairs = v.n_pairs;
+      old_views.push_back(std::move(c));
+    }
+  }
+  // 1. counts of every pixel of every view, one global scan -> offsets
+  int64_t npix = (int64_t)V * HW;
+  u32_checked(npix, "pixel count");
+  m->s_counts.reserve((size_t)npix * 4 + 4, false, m->stream);
+  m->s_offs.reserve((size_t)npix * 4 + 4, false, m->stream);
+  for (int c = 0; c < V; ++c)
+    CK(launch_trace_count(m->g, m->views[c].pose, m->views[c].depth.as<float>(),
+                          m->s_counts.as<uint32_t>() + c * HW, m->s_err.as<int>(), m->stream));
+  // sentinel 0 at the end so the scan yields the total
+  CK(cudaMemsetAsync(m->s_counts.as<uint32_t>() + npix, 0, 4, m->stream));
+  size_t tb = scan_temp_bytes((uint32_t)(npix + 1));
+  m->s_tmp.reserve(tb, false, m->stream);
+  CK(exclusive_scan_u32(m->s_tmp.p, tb, m->s_counts.as<uint32_t>(), m->s_offs.as<uint32_t>(),
+                        (uint32_t)(npix + 1), m->stream));
+  std::vector<uint32_t> bounds(V + 1);
+  for (int c = 0; c <= V; ++c)
+    CK(cudaMemcpyAsync(&bounds[c], m->s_offs.as<uint32_t>() + (int64_t)c * HW, 4,
+                       cudaMemcpyDeviceToHost, m->stream));
+  sync(m);
+  check_device_err(m);
+  int64_t n_inc = bounds[V];
+  u32_checked(n_inc, "incidence count");
+  // 2. arenas
+  m->meta.reserve((size_t)npix * sizeof(RayMeta), false, m->stream);
+  size_t ib = (size_t)std::max<int64_t>(n_inc, 1) * 4;
+  m->inc_pair.reserve(ib, false, m->stream);
+  m->inc_len.reserve(ib, false, m->stream);
+  m->inc_mu.reserve(ib, false, m->stream);
+  m->inc_pl.reserve(ib, false, m->stream);
+  m->perm.reserve(ib, false, m->stream);
+  m->s_vox.reserve(ib, false, m->stream);
+  // 3. emit
+  for (int c = 0; c < V; ++c) {
+    View& v = m->views[c];
+    v.inc_base = bounds[c];
+    v.n_inc = bounds[c + 1] - bounds[c];
+    CK(launch_trace_emit(m->g, v.pose, v.depth.as<float>(), m->s_offs.as<uint32_t>() + c * HW, 0,
+                         m->meta.as<RayMeta>() + c * HW, m->s_vox.as<uint32_t>(),
+                         m->inc_len.as<float>(), m->inc_mu.as<float>(), m->s_err.as<int>(),
+                         m->stream));
+  }
+  // 4. pairs per view (first-touch order) and the pair-grouped CSR
+  ensure_first(m);
+  int64_t pair_total = 0, perm_total = 0;
+  for (int c = 0; c < V; ++c) {
+    View& v = m->views[c];
+    uint32_t n = v.n_inc;
+    v.pair_base = (uint32_t)pair_total;
+    v.perm_base = (uint32_t)perm_total;
+    v.n_pairs = 0;
+    v.n_perm = 0;
+    if (n == 0) continue;
+    const uint32_t* vox = m->s_vox.as<uint32_t>() + v.inc_base;
+    m->s_k0.reserve((size_t)n * 4 + 4, false, m->stream);
+    m->s_k1.reserve((size_t)n * 4 + 4, false, m->stream);
+    m->s_v0.reserve((size_t)n * 4 + 4, false, m->stream);
+    m->s_v1.reserve((size_t)n * 4 + 4, false, m->stream);
+    CK(launch_first_touch(vox, n, m->s_first.as<uint32_t>(), m->stream));
+    CK(launch_flag_first(vox, n, m->s_first.as<uint32_t>(), m->s_k0.as<uint32_t>(), m->stream));
+    CK(cudaMemsetAsync(m->s_k0.as<uint32_t>() + n, 0, 4, m->stream));
+    size_t t1 = scan_temp_bytes(n + 1);
+    m->s_tmp.reserve(t1, false, m->stream);
+    CK(exclusive_scan_u32(m->s_tmp.p, t1, m->s_k0.as<uint32_t>(), m->s_k1.as<uint32_t>(), n + 1,
+                          m->stream));
+    uint32_t np = read1(m, m->s_k1.as<uint32_t>() + n);
+    u32_checked(pair_total + np + 1, "pair count");
+    size_t pb = (size_t)(pair_total + np + 1);
+    m->pair_vox.reserve(pb * 4, true, m->stream);
+    m->pair_m.reserve(pb * 4, true, m->stream);
+    m->pair_cum.reserve(pb * 4, true, m->stream);
+    m->pair_seg.reserve(pb * 4, true, m->stream);
+    CK(launch_pair_assign(vox, n, m->s_k0.as<uint32_t>(), m->s_k1.as<uint32_t>(), v.pair_base,
+                          m->pair_vox.as<uint32_t>(), m->s_first.as<uint32_t>(), m->stream));
+    CK(launch_inc_pair(vox, n, m->s_first.as<uint32_t>(), m->inc_pair.as<uint32_t>() + v.inc_base,
+                       m->stream));
+    CK(launch_reset_first(m->pair_vox.as<uint32_t>() + v.pair_base, np, m->s_first.as<uint32_t>(),
+                          m->stream));
+    CK(launch_sort_keys(m->meta.as<RayMeta>() + c * HW, (int)HW, v.inc_base,
+                        m->inc_pair.as<uint32_t>(), v.pair_base, np, m->s_k0.as<uint32_t>(),
+                        m->s_v0.as<uint32_t>(), m->stream));
+    int bits = 1;
+    while (bits < 32 && ((uint64_t)1 << bits) <= (uint64_t)np) ++bits;
+    size_t t2 = sort_temp_bytes(n, bits);
+    m->s_tmp.reserve(t2, false, m->stream);
+    CK(sort_pairs_u32(m->s_tmp.p, t2, m->s_k0.as<uint32_t>(), m->s_k1.as<uint32_t>(),
+                      m->s_v0.as<uint32_t>(), m->s_v1.as<uint32_t>(), n, bits, m->stream));
+    m->s_seg.reserve((size_t)(np + 1) * 4, false, m->stream);
+    CK(launch_seg_bounds(m->s_k1.as<uint32_t>(), n, np, m->s_seg.as<uint32_t>(), m->stream));
+    uint32_t nvalid = read1(m, m->s_seg.as<uint32_t>() + np);
+    CK(launch_perm_copy(m->s_v1.as<uint32_t>(), nvalid, v.inc_base,
+                        m->perm.as<uint32_t>() + v.perm_base, m->stream));
+    CK(launch_pair_init2(m->s_seg.as<uint32_t>(), m->s_v1.as<uint32_t>(), v.inc_base, np,
+                         m->inc_len.as<float>(), v.perm_base, v.pair_base,
+                         m->pair_seg.as<uint32_t>(), m->pair_cum.as<float>(), m->stream));
+    v.n_pairs = np;
+    v.n_perm = nvalid;
+    pair_total += np;
+    perm_total += nvalid;
+  }
+  m->n_inc = n_inc;
+  m->n_pairs = pair_total;
+  m->n_perm = perm_total;
+  size_t pb = (size_t)std::max<int64_t>(pair_total + 1, 1);
+  m->pair_vox.reserve(pb * 4, true, m->stream);
+  m->pair_m.reserve(pb * 4, true, m->stream);
+  m->pair_cum.reserve(pb * 4, true, m->stream);
+  m->pair_seg.reserve(pb * 4, true, m->stream);
+  m->pair_q.reserve(pb * 8, false, m->stream);
+  m->pair_dm.reserve(pb * 4, false, m->stream);
+  CK(launch_fill_f32(m->pair_m.as<float>(), pair_total, 0.0f, m->stream));
+  // 5. carry messages of every camera over to its new pairs
+  if (remap) {
+    int64_t nv = m->n_bricks * kBrickVox;
+    m->s_dense.reserve((size_t)nv * 4, false, m->stream);
+    CK(cudaMemsetAsync(m->s_dense.p, 0, (size_t)nv * 4, m->stream));
+    for (int c = 0; c < V && c < (int)old_views.size(); ++c) {
+      const View& o = old_views[c];
+      const View& v = m->views[c];
+      CK(launch_remap_scatter(old_vox.as<uint32_t>() + o.pair_base, old_m.as<float>() + o.pair_base,
+                              o.n_pairs, m->s_dense.as<float>(), m->stream));
+      CK(launch_remap_gather(m->pair_vox.as<uint32_t>() + v.pair_base,
+                             m->pair_m.as<float>() + v.pair_base, v.n_pairs,
+                             m->s_dense.as<float>(), m->stream));
+      CK(launch_scatter_const(old_vox.as<uint32_t>() + o.pair_base, o.n_pairs, 0.0f,
+                              m->s_dense.as<float>(), m->stream));
+    }
+    sync(m);
+    old_vox.release();
+    old_m.release();
+  }
+  CK(cudaEventRecord(m->ev1, m->stream));
+  sync(m);
+  check_device_err(m);
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, m->ev0, m->ev1);
+  m->stats.build_ms = ms;
+  m->built_version = m->version;
+  m->jacobi_version = -1;
+  // counters
+  std::vector<RayMeta> hm;
+  int64_t nrays = 0, npost = 0;
+  if (npix) {
+    hm.resize((size_t)npix);
+    CK(cudaMemcpyAsync(hm.data(), m->meta.p, (size_t)npix * sizeof(RayMeta), cudaMemcpyDeviceToHost,
+                       m->stream));
+    sync(m);
+    for (const auto& r : hm) {
+      nrays += r.n_pre > 0;
+      npost += r.n_post;
+    }
+  }
+  m->stats.n_rays = nrays;
+  m->stats.n_inc_pre = n_inc;
+  m->stats.n_inc_post = npost;
+  m->stats.n_pairs = pair_total;
+}
+
+void build_jacobi_csr(mrf_map* m) {
+  uint32_t np = (uint32_t)m->n_pairs;
+  m->vpairs.reserve((size_t)np * 4 + 4, false, m->stream);
+  m->vvox.reserve((size_t)np * 4 + 4, false, m->stream);
+  m->vseg.reserve((size_t)np * 4 + 8, false, m->stream);
+  m->s_k0.reserve((size_t)np * 4 + 4, false, m->stream);
+  m->s_v0.reserve((size_t)np * 4 + 4, false, m->stream);
+  m->s_k1.reserve((size_t)np * 4 + 4, false, m->stream);
+  m->s_v1.reserve((size_t)np * 4 + 4, false, m->stream);
+  if (np == 0) {
+    m->n_vvox = 0;
+    m->jacobi_version = m->built_version;
+    return;
+  }
+  CK(launch_iota(m->s_v0.as<uint32_t>(), np, m->stream));
+  int bits = 1;
+  while (bits < 32 && ((uint64_t)1 << bits) <= (uint64_t)(m->n_bricks * kBrickVox)) ++bits;
+  size_t t = sort_temp_bytes(np, bits);
+  m->s_tmp.reserve(t, false, m->stream);
+  CK(sort_pairs_u32(m->s_tmp.p, t, m->pair_vox.as<uint32_t>(), m->s_k1.as<uint32_t>(),
+                    m->s_v0.as<uint32_t>(), m->vpairs.as<uint32_t>(), np, bits, m->stream));
+  CK(launch_vflag(m->s_k1.as<uint32_t>(), np, m->s_k0.as<uint32_t>(), m->stream));
+  CK(cudaMemsetAsync(m->s_k0.as<uint32_t>() + np, 0, 4, m->stream));
+  size_t t2 = scan_temp_bytes(np + 1);
+  m->s_tmp.reserve(t2, false, m->stream);
+  CK(exclusive_scan_u32(m->s_tmp.p, t2, m->s_k0.as<uint32_t>(), m->s_v1.as<uint32_t>(), np + 1,
+                        m->stream));
+  uint32_t nv = read1(m, m->s_v1.as<uint32_t>() + np);
+  CK(launch_vassign(m->s_k1.as<uint32_t>(), m->s_k0.as<uint32_t>(), m->s_v1.as<uint32_t>(), np,
+                    m->vvox.as<uint32_t>(), m->vseg.as<uint32_t>(), m->stream));
+  CK(cudaMemcpyAsync(m->vseg.as<uint32_t>() + nv, &np, 4, cudaMemcpyHostToDevice, m->stream));
+  sync(m);
+  m->n_vvox = nv;
+  m->jacobi_version = m->built_version;
+}
+
+void ensure_built(mrf_map* m) {
+  if (m->built_version != m->version) rebuild(m);
+}
+
+void run_infer(mrf_map* m, const int* ids, int n_ids, int iters, int flags) {
+  ensure_built(m);
+  const bool jacobi = flags & MRF_JACOBI;
+  if (jacobi && m->jacobi_version != m->built_version) build_jacobi_csr(m);
+  const int V = (int)m->views.size();
+  const int64_t HW = m->hw();
+  if (iters <= 0) iters = m->prm.max_iters > 0 ? m->prm.max_iters : 1;
+  BpArrays a = m->bp();
+  int64_t launches = 0;
+  CK(cudaEventRecord(m->ev0, m->stream));
+  if (!(flags & MRF_INCREMENTAL)) {
+    // src/GVDBInference.cpp:128-133: the selected cameras start from zero
+    for (int k = 0; k < (ids ? n_ids : V); ++k) {
+      int c = ids ? ids[k] : k;
+      if (c < 0 || c >= V) continue;
+      const View& v = m->views[c];
+      CK(launch_fill_f32(m->pair_m.as<float>() + v.pair_base, v.n_pairs, 0.0f, m->stream));
+      ++launches;
+    }
+  }
+  const int fix = (flags & MRF_FIX_PRE_RESET) ? 1 : 0;
+  for (int it = 0; it < iters; ++it) {
+    if (!jacobi) {
+      // Gauss-Seidel over every camera (src/GVDBInference.cpp:155-167)
+      for (int c = 0; c < V; ++c) {
+        const View& v = m->views[c];
+        if (v.n_inc == 0) continue;
+        CK(launch_pair_prepare(a, v.pair_base, v.pair_base + v.n_pairs, m->stream));
+        CK(launch_ray_bp(a, (uint32_t)(c * HW), (uint32_t)((c + 1) * HW), fix, m->num_sms, m->stream));
+        CK(launch_pair_update(a, v.pair_base, v.pair_base + v.n_pairs, 0, m->stream));
+        launches += 3;
+      }
+    } else {
+      uint32_t P = (uint32_t)m->n_pairs;
+      CK(launch_pair_prepare(a, 0, P, m->stream));
+      CK(launch_ray_bp(a, 0, (uint32_t)(V * HW), fix, m->num_sms, m->stream));
+      CK(launch_pair_update(a, 0, P, 1, m->stream));
+      CK(launch_voxel_apply(m->vseg.as<uint32_t>(), m->vpairs.as<uint32_t>(), m->vvox.as<uint32_t>(),
+                            m->n_vvox, m->pair_dm.as<float>(), m->d_L.as<float>(),
+                            m->d_belief.as<float>(), m->stream));
+      launches += 4;
+    }
+  }
+  CK(cudaEventRecord(m->ev1, m->stream));
+  m->has_messages = true;
+  m->stats.iters_done = iters;
+  m->stats.kernel_launches = launches;
+  if (!(flags & MRF_ASYNC)) {
+    sync(m);
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, m->ev0, m->ev1);
+    m->stats.infer_ms = ms;
+  }
+}
+
+Geom make_geom(const mrf_params& p) {
+  Geom g{};
+  g.res = p.res;
+  g.inv_res = 1.0f / p.res;
+  g.fx = p.fx;
+  g.fy = p.fy;
+  g.cx = p.cx;
+  g.cy = p.cy;
+  g.rows = p.rows;
+  g.cols = p.cols;
+  for (int a = 0; a < 3; ++a) {
+    float gg = p.dims[a] / p.res;
+    g.hi[a] = gg;
+    int G = (int)ceilf(gg);
+    g.NB[a] = (G + 1 + kBrick - 1) / kBrick;
+    g.E[a] = kBrick * g.NB[a];
+  }
+  g.off[0] = (p.dims[0] * 0.5f) / p.res;
+  g.off[1] = (p.dims[1] * 0.5f) / p.res;
+  g.off[2] = 0.0f;
+  g.lookup_n = p.lookup_n;
+  g.n_tiles_u = (p.cols + kLookupPx - 1) / kLookupPx;
+  g.n_tiles_v = (p.rows + kLookupPx - 1) / kLookupPx;
+  return g;
+}
+
+void set_pose(Pose& P, const float* pose) {
+  for (int i = 0; i < 16; ++i) P.m[i] = pose[i];
+}
+
+mrf_status guard(mrf_map* m) {
+  if (!m) {
+    set_err("null map");
+    return MRF_ERR_INVALID;
+  }
+  cudaSetDevice(m->device);
+  return MRF_OK;
+}
+
+template <typename F>
+mrf_status wrap(F&& f) {
+  try {
+    f();
+    return MRF_OK;
+  } catch (const Fail& e) {
+    return e.st;
+  } catch (const std::exception& e) {
+    set_err(e.what());
+    return MRF_ERR_INVALID;
+  }
+}
+
+void destroy_bufs(mrf_map* m) {
+  DBuf* all[] = {&m->d_sigma, &m->d_bias, &m->d_slot, &m->d_coord, &m->d_L, &m->d_belief,
+                 &m->meta, &m->inc_pair, &m->inc_len, &m->inc_mu, &m->inc_pl, &m->pair_vox,
+                 &m->pair_m, &m->pair_cum, &m->pair_q, &m->pair_dm, &m->pair_seg, &m->perm,
+                 &m->vseg, &m->vpairs, &m->vvox, &m->s_first, &m->s_flags, &m->s_ind, &m->s_scan,
+                 &m->s_tmp, &m->s_counts, &m->s_offs, &m->s_vox, &m->s_k0, &m->s_k1, &m->s_v0,
+                 &m->s_v1, &m->s_seg, &m->s_dense, &m->s_err, &m->s_depth_in, &m->s_depth,
+                 &m->s_img, &m->s_part, &m->s_sum};
+  for (DBuf* b : all) b->release();
+  for (auto& v : m->views) v.depth.release();
+}
+
+void likelihood_dev(mrf_map* m, const Pose& P, const float* depth_clean, float* img_dev,
+                    float* sum_dev) {
+  m->g.brick_slot = m->d_slot.as<int>();
+  int nb = likelihood_blocks(m->g);
+  m->s_part.reserve((size_t)nb * 8, false, m->stream);
+  const float* bel = m->d_belief.as<float>();
+  if (m->n_bricks == 0) {
+    // an empty map still needs a valid pointer for the kernel signature
+    m->s_dense.reserve(4, false, m->stream);
+    bel = m->s_dense.as<float>();
+  }
+  CK(launch_likelihood(m->g, P, depth_clean, bel, img_dev, m->s_part.as<double>(), nb, m->stream));
+  CK(launch_reduce_partials(m->s_part.as<double>(), nb, sum_dev, m->stream));
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* mrf_last_error(void) { return g_last_error.c_str(); }
+
+mrf_status mrf_create(const mrf_params* params, mrf_map** out) {
+  if (!params || !out) {
+    set_err("null argument");
+    return MRF_ERR_INVALID;
+  }
+  *out = nullptr;
+  const mrf_params& p = *params;
+  if (!(p.res > 0.0f) || p.rows <= 0 || p.cols <= 0 || !(p.fx > 0.0f) || !(p.fy > 0.0f) ||
+      !(p.cx > 0.0f) || !(p.cy > 0.0f) || (p.lookup_n != 2 && p.lookup_n != 3) || !p.sigma_lut ||
+      !p.bias_lut || !(p.prior > 0.0f && p.prior < 1.0f) ||
+      (p.activation != MRF_ACT_ENDPOINT && p.activation != MRF_ACT_FULL_RAY)) {
+    set_err("invalid mrf_params");
+    return MRF_ERR_INVALID;
+  }
+  for (int a = 0; a < 3; ++a)
+    if (!(p.dims[a] > 0.0f)) {
+      set_err("invalid dims");
+      return MRF_ERR_INVALID;
+    }
+  mrf_map* m = new mrf_map();
+  mrf_status st = wrap([&] {
+    m->prm = p;
+    int nl = ((p.rows + kLookupPx - 1) / kLookupPx) * ((p.cols + kLookupPx - 1) / kLookupPx) *
+             p.lookup_n;
+    if (nl > 3096) fail(MRF_ERR_INVALID, "sensor lookup table larger than 3096 floats");
+    m->sigma.assign(p.sigma_lut, p.sigma_lut + nl);
+    m->bias.assign(p.bias_lut, p.bias_lut + nl);
+    m->prm.sigma_lut = m->sigma.data();
+    m->prm.bias_lut = m->bias.data();
+    CK(cudaGetDevice(&m->device));
+    CK(cudaDeviceGetAttribute(&m->num_sms, cudaDevAttrMultiProcessorCount, m->device));
+    CK(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking));
+    CK(cudaEventCreate(&m->ev0));
+    CK(cudaEventCreate(&m->ev1));
+    m->g = make_geom(p);
+    m->nb_grid = (int64_t)m->g.NB[0] * m->g.NB[1] * m->g.NB[2];
+    m->d_sigma.reserve((size_t)nl * 4, false, m->stream);
+    m->d_bias.reserve((size_t)nl * 4, false, m->stream);
+    CK(cudaMemcpyAsync(m->d_sigma.p, m->sigma.data(), (size_t)nl * 4, cudaMemcpyHostToDevice, m->stream));
+    CK(cudaMemcpyAsync(m->d_bias.p, m->bias.data(), (size_t)nl * 4, cudaMemcpyHostToDevice, m->stream));
+    m->g.sigma = m->d_sigma.as<float>();
+    m->g.bias = m->d_bias.as<float>();
+    m->d_slot.reserve((size_t)m->nb_grid * 4, false, m->stream);
+    CK(cudaMemsetAsync(m->d_slot.p, 0xFF, (size_t)m->nb_grid * 4, m->stream));
+    m->s_flags.reserve((size_t)m->nb_grid, false, m->stream);
+    m->s_err.reserve(16, false, m->stream);
+    CK(cudaMemsetAsync(m->s_err.p, 0, 16, m->stream));
+    m->s_sum.reserve(16, false, m->stream);
+    m->g.brick_slot = m->d_slot.as<int>();
+    sync(m);
+  });
+  if (st != MRF_OK) {
+    destroy_bufs(m);
+    if (m->stream) cudaStreamDestroy(m->stream);
+    delete m;
+    return st;
+  }
+  *out = m;
+  return MRF_OK;
+}
+
+void mrf_destroy(mrf_map* m) {
+  if (!m) return;
+  cudaSetDevice(m->device);
+  if (m->stream) cudaStreamSynchronize(m->stream);
+  destroy_bufs(m);
+  if (m->ev0) cudaEventDestroy(m->ev0);
+  if (m->ev1) cudaEventDestroy(m->ev1);
+  if (m->stream) cudaStreamDestroy(m->stream);
+  delete m;
+}
+
+static mrf_status add_view_impl(mrf_map* m, const float* pose, const float* depth, bool device,
+                                int* view_id) {
+  if (guard(m) != MRF_OK) return MRF_ERR_INVALID;
+  if (!pose || !depth) {
+    set_err("null pose or depth");
+    return MRF_ERR_INVALID;
+  }
+  return wrap([&] {
+    const int64_t HW = m->hw();
+    View v;
+    set_pose(v.pose, pose);
+    v.depth.reserve((size_t)HW * 4, false, m->stream);
+    const float* src = depth;
+    if (!device) {
+      m->s_depth_in.reserve((size_t)HW * 4, false, m->stream);
+      CK(cudaMemcpyAsync(m->s_depth_in.p, depth, (size_t)HW * 4, cudaMemcpyHostToDevice, m->stream));
+      src = m->s_depth_in.as<float>();
+    }
+    CK(launch_clean_depth(src, v.depth.as<float>(), m->prm.rows, m->prm.cols, m->stream));
+    activate_view(m, v);
+    m->views.push_back(std::move(v));
+    m->version++;  // the view set changed: incidence lists must be rebuilt
+    m->stats.n_views = (int64_t)m->views.size();
+    m->stats.n_bricks = m->n_bricks;
+    if (view_id) *view_id = (int)m->views.size() - 1;
+  });
+}
+
+mrf_status mrf_add_view(mrf_map* m, const float* pose, const float* depth_host, int* view_id) {
+  return add_view_impl(m, pose, depth_host, false, view_id);
+}
+
+mrf_status mrf_add_view_device(mrf_map* m, const float* pose, const float* depth_dev, int* view_id) {
+  return add_view_impl(m, pose, depth_dev, true, view_id);
+}
+
+mrf_status mrf_set_pose(mrf_map* m, int view_id, const float* pose) {
+  if (guard(m) != MRF_OK) return MRF_ERR_INVALID;
+  if (!pose || view_id < 0 || view_id >= (int)m->views.size()) {
+    set_err("invalid view id or pose");
+    return MRF_ERR_INVALID;
+  }
+  return wrap([&] {
+    set_pose(m->views[view_id].pose, pose);
+    activate_view(m, m->views[view_id]);
+    m->version++;
+    m->stats.n_bricks = m->n_bricks;
+  });
+}
+
+mrf_status mrf_infer(mrf_map* m, const int* ids, int n_ids, int iters, int flags) {
+  if (guard(m) != MRF_OK) return MRF_ERR_INVALID;
+  if (n_ids < 0 || (n_ids > 0 && !ids)) {
+    set_err("invalid ids");
+    return MRF_ERR_INVALID;
+  }
+  return wrap([&] { run_infer(m, ids, ids ? n_ids : 0, iters, flags); });
+}
+
+mrf_status mrf_reset_state(mrf_map* m) {
+  if (guard(m) != MRF_OK) return MRF_ERR_INVALID;
+  return wrap([&] {
+    float lp = logf(m->prm.prior) - logf(1.0f - m->prm.prior);
+    CK(launch_fill_new_voxels(m->d_L.as<float>(), m->d_belief.as<float>(), 0,
+                              m->n_bricks * kBrickVox, lp, m->stream));
+    if (m->n_pairs) CK(launch_fill_f32(m->pair_m.as<float>(), m->n_pairs, 0.0f, m->stream));
+  });
+}
+
+mrf_status mrf_likelihood_device(mrf_map* m, const float* pose, const float* depth_dev,
+                                 float* out_img_dev, float* out_sum_dev) {
+  if (guard(m) != MRF_OK) return MRF_ERR_INVALID;
+  if (!pose || !depth_dev || !out_sum_dev) {
+    set_err("null argument");
+    return MRF_ERR_INVALID;
+  }
+  return wrap([&] {
+    Pose P;
+    set_pose(P, pose);
+    const int64_t HW = m->hw();
+    m->s_depth.reserve((size_t)HW * 4, false, m->stream);
+    CK(launch_clean_depth(depth_dev, m->s_depth.as<float>(), m->prm.rows, m->prm.cols, m->stream));
+    likelihood_dev(m, P, m->s_depth.as<float>(), out_img_dev, out_sum_dev);
+  });
+}
+
+static mrf_status likelihood_host(mrf_map* m, const Pose& P, const float* depth_clean_dev,
+                                  float* out_img, float* out_sum) {
+  return wrap([&] {
+    const int64_t HW = m->hw();
+    float* img = nullptr;
+    if (out_img) {
+      m->s_img.reserve((size_t)HW * 4, false, m->stream);
+      img = m->s_img.as<float>();
+    }
+    likelihood_dev(m, P, depth_clean_dev, img, m->s_sum.as<float>());
+    float sum = 0.0f;
+    CK(cudaMemcpyAsync(&sum, m->s_sum.p, 4, cudaMemcpyDeviceToHost, m->stream));
+    if (out_img) CK(cudaMemcpyAsync(out_img, img, (size_t)HW * 4, cudaMemcpyDeviceToHost, m->stream));
+    sync(m);
+    if (out_sum) *out_sum = sum;
+  });
+}
+
+mrf_status mrf_likelihood(mrf_map* m, const float* pose, const float* depth_host, float* out_img,
+                          float* out_sum) {
+  if (guard(m) != MRF_OK) return MRF_ERR_INVALID;
+  if (!pose || !depth_host) {
+    set_err("null argument");
+    return MRF_ERR_INVALID;
+  }
+  mrf_status st = wrap([&] {
+    const int64_t HW = m->hw();
+    m->s_depth_in.reserve((size_t)HW * 4, false, m->stream);
+    m->s_depth.reserve((size_t)HW * 4, false, m->stream);
+    CK(cudaMemcpyAsync(m->s_depth_in.p, depth_host, (size_t)HW * 4, cudaMemcpyHostToDevice, m->stream));
+    CK(launch_clean_depth(m->s_depth_in.as<float>(), m->s_depth.as<float>(), m->prm.rows,
+                          m->prm.cols, m->stream));
+  });
+  if (st != MRF_OK) return st;
+  Pose P;
+  set_pose(P, pose);
+  return likelihood_host(m, P, m->s_depth.as<float>(), out_img, out_sum);
+}
+
+mrf_status mrf_likelihood_view(mrf_map* m, int view_id, float* out_img, float* out_sum) {
+  if (guard(m) != MRF_OK) return MRF_ERR_INVALID;
+  if (view_id < 0 || view_id >= (int)m->views.size()) {
+    set_err("invalid view id");
+    return MRF_ERR_INVALID;
+  }
+  const View& v = m->views[view_id];
+  return likelihood_host(m, v.pose, v.depth.as<float>(), out_img, out_sum);
+}
+
+mrf_status mrf_num_bricks(mrf_map* m, int64_t* n) {
+  if (guard(m) != MRF_OK || !n) return MRF_ERR_INVALID;
+  *n = m->n_bricks;
+  return MRF_OK;
+}
+
+mrf_status mrf_read_bricks(mrf_map* m, float* centres, float* beliefs, int64_t n) {
+  if (guard(m) != MRF_OK) return MRF_ERR_INVALID;
+  if (n != m->n_bricks) {
+    set_err("Dimensions for the alphas array are incorrect!");
+    return MRF_ERR_INVALID;
+  }
+  return wrap([&] {
+    if (centres)
+      for (int64_t i = 0; i < n; ++i)
+        for (int a = 0; a < 3; ++a) centres[i * 3 + a] = (float)(m->h_coord[i * 3 + a] * kBrick + kBrick / 2);
+    if (beliefs && n) {
+      CK(cudaMemcpyAsync(beliefs, m->d_belief.p, (size_t)n * kBrickVox * 4, cudaMemcpyDeviceToHost,
+                         m->stream));
+      sync(m);
+    }
+  });
+}
+
+mrf_status mrf_read_logodds(mrf_map* m, float* logodds, int64_t n) {
+  if (guard(m) != MRF_OK) return MRF_ERR_INVALID;
+  if (n != m->n_bricks || !logodds) {
+    set_err("invalid size");
+    return MRF_ERR_INVALID;
+  }
+  return wrap([&] {
+    if (n) {
+      CK(cudaMemcpyAsync(logodds, m->d_L.p, (size_t)n * kBrickVox * 4, cudaMemcpyDeviceToHost,
+                         m->stream));
+      sync(m);
+    }
+  });
+}
+
+static void node_list(mrf_map* m, int level, std::vector<int>& out) {
+  // level-l nodes span 8^(l+1) voxels per axis (gvdb_map_config 3,3,3,3,3)
+  int64_t span = 1;
+  for (int l = 0; l < level; ++l) span *= 8;
+  std::vector<int64_t> keys;
+  keys.reserve((size_t)m->n_bricks);
+  for (int64_t i = 0; i < m->n_bricks; ++i) {
+    int64_t c[3];
+    for (int a = 0; a < 3; ++a) c[a] = m->h_coord[i * 3 + a] / span;
+    keys.push_back((c[0] << 40) | (c[1] << 20) | c[2]);
+  }
+  std::vector<int64_t> seen;
+  for (int64_t k : keys)
+    if (std::find(seen.begin(), seen.end(), k) == seen.end()) seen.push_back(k);
+  out.clear();
+  for (int64_t k : seen) {
+    out.push_back((int)(k >> 40));
+    out.push_back((int)((k >> 20) & 0xFFFFF));
+    out.push_back((int)(k & 0xFFFFF));
+  }
+}
+
+mrf_status mrf_num_nodes(mrf_map* m, int level, int64_t* n) {
+  if (guard(m) != MRF_OK || !n || level < 0 || level > 4) return MRF_ERR_INVALID;
+  if (level == 0) {
+    *n = m->n_bricks;
+    return MRF_OK;
+  }
+  std::vector<int> nodes;
+  node_list(m, level, nodes);
+  *n = (int64_t)nodes.size() / 3;
+  return MRF_OK;
+}
+
+mrf_status mrf_read_nodes(mrf_map* m, int level, float* centres, int64_t n) {
+  if (guard(m) != MRF_OK || !centres || level < 0 || level > 4) return MRF_ERR_INVALID;
+  if (level == 0) return mrf_read_bricks(m, centres, nullptr, n);
+  std::vector<int> nodes;
+  node_list(m, level, nodes);
+  if ((int64_t)nodes.size() / 3 != n) {
+    set_err("invalid size");
+    return MRF_ERR_INVALID;
+  }
+  int64_t span = kBrick;
+  for (int l = 0; l < level; ++l) span *= 8;
+  for (int64_t i = 0; i < n; ++i)
+    for (int a = 0; a < 3; ++a) centres[i * 3 + a] = (float)(nodes[i * 3 + a] * span + span / 2);
+  return MRF_OK;
+}
+
+mrf_status mrf_load_map(mrf_map* m, const float* points, const float* occ, int64_t n) {
+  if (guard(m) != MRF_OK) return MRF_ERR_INVALID;
+  if (n < 0 || (n > 0 && (!points || !occ))) {
+    set_err("invalid points");
+    return MRF_ERR_INVALID;
+  }
+  return wrap([&] {
+    if (n == 0) return;
+    DBuf pts, oc;
+    pts.reserve((size_t)n * 12, false, m->stream);
+    oc.reserve((size_t)n * 4, false, m->stream);
+    CK(cudaMemcpyAsync(pts.p, points, (size_t)n * 12, cudaMemcpyHostToDevice, m->stream));
+    CK(cudaMemcpyAsync(oc.p, occ, (size_t)n * 4, cudaMemcpyHostToDevice, m->stream));
+    CK(cudaMemsetAsync(m->s_flags.p, 0, (size_t)m->nb_grid, m->stream));
+    m->g.brick_slot = m->d_slot.as<int>();
+    CK(launch_activate_points(m->g, pts.as<float>(), n, m->s_flags.as<uint8_t>(), m->stream));
+    commit_new_bricks(m);
+    m->g.brick_slot = m->d_slot.as<int>();
+    CK(launch_set_points(m->g, pts.as<float>(), oc.as<float>(), n, m->d_belief.as<float>(), m->stream));
+    sync(m);
+    pts.release();
+    oc.release();
+    m->stats.n_bricks = m->n_bricks;
+  });
+}
+
+mrf_status mrf_view_incidences(mrf_map* m, int view_id, int* meta, uint32_t* vox, float* len,
+                               float* mu, int64_t cap, int64_t* n_inc) {
+  if (guard(m) != MRF_OK) return MRF_ERR_INVALID;
+  if (view_id < 0 || view_id >= (int)m->views.size() || cap < 0) {
+    set_err("invalid view id");
+    return MRF_ERR_INVALID;
+  }
+  return wrap([&] {
+    ensure_built(m);
+    const View& v = m->views[view_id];
+    const int64_t HW = m->hw();
+    if (n_inc) *n_inc = v.n_inc;
+    if (meta) {
+      std::vector<RayMeta> hm((size_t)HW);
+      CK(cudaMemcpyAsync(hm.data(), m->meta.as<RayMeta>() + view_id * HW, (size_t)HW * sizeof(RayMeta),
+                         cudaMemcpyDeviceToHost, m->stream));
+      sync(m);
+      for (int64_t i = 0; i < HW; ++i) {
+        meta[i * 5 + 0] = hm[i].n_pre;
+        meta[i * 5 + 1] = hm[i].n_post;
+        meta[i * 5 + 2] = hm[i].r0;
+        meta[i * 5 + 3] = hm[i].rinf;
+        meta[i * 5 + 4] = (int)(hm[i].flags & 1u);
+      }
+    }
+    int64_t n = std::min<int64_t>(cap, v.n_inc);
+    if (n <= 0) return;
+    if (len) CK(cudaMemcpyAsync(len, m->inc_len.as<float>() + v.inc_base, (size_t)n * 4,
+                                cudaMemcpyDeviceToHost, m->stream));
+    if (mu) CK(cudaMemcpyAsync(mu, m->inc_mu.as<float>() + v.inc_base, (size_t)n * 4,
+                               cudaMemcpyDeviceToHost, m->stream));
+    if (vox) {
+      std::vector<uint32_t> ip((size_t)n), pv((size_t)v.n_pairs);
+      CK(cudaMemcpyAsync(ip.data(), m->inc_pair.as<uint32_t>() + v.inc_base, (size_t)n * 4,
+                         cudaMemcpyDeviceToHost, m->stream));
+      if (v.n_pairs)
+        CK(cudaMemcpyAsync(pv.data(), m->pair_vox.as<uint32_t>() + v.pair_base, (size_t)v.n_pairs * 4,
+                           cudaMemcpyDeviceToHost, m->stream));
+      sync(m);
+      for (int64_t i = 0; i < n; ++i) vox[i] = pv[ip[i] - v.pair_base];
+    }
+    sync(m);
+  });
+}
+
+mrf_status mrf_device_beliefs(mrf_map* m, const float** beliefs, int64_t* n_voxels) {
+  if (guard(m) != MRF_OK || !beliefs || !n_voxels) return MRF_ERR_INVALID;
+  *beliefs = m->d_belief.as<float>();
+  *n_voxels = m->n_bricks * kBrickVox;
+  return MRF_OK;
+}
+
+mrf_status mrf_stats_get(mrf_map* m, mrf_stats* out) {
+  if (guard(m) != MRF_OK || !out) return MRF_ERR_INVALID;
+  mrf_status st = wrap([&] {
+    ensure_built(m);
+    // active pairs and touched voxels need a device pass: cheap host pass here
+    int64_t np = m->n_pairs;
+    std::vector<float> cum((size_t)np);
+    std::vector<uint32_t> vox((size_t)np);
+    if (np) {
+      CK(cudaMemcpyAsync(cum.data(), m->pair_cum.p, (size_t)np * 4, cudaMemcpyDeviceToHost, m->stream));
+      CK(cudaMemcpyAsync(vox.data(), m->pair_vox.p, (size_t)np * 4, cudaMemcpyDeviceToHost, m->stream));
+      sync(m);
+    }
+    int64_t act = 0;
+    std::vector<uint32_t> tv;
+    for (int64_t i = 0; i < np; ++i)
+      if (cum[i] > kCumLenGate) {
+        ++act;
+        tv.push_back(vox[i]);
+      }
+    std::sort(tv.begin(), tv.end());
+    m->stats.n_pairs_active = act;
+    m->stats.n_vox_touched = (int64_t)(std::unique(tv.begin(), tv.end()) - tv.begin());
+    m->stats.n_views = (int64_t)m->views.size();
+    m->stats.n_bricks = m->n_bricks;
+  });
+  *out = m->stats;
+  return st;
+}
+
+mrf_status mrf_get_stream(mrf_map* m, void** stream) {
+  if (guard(m) != MRF_OK || !stream) return MRF_ERR_INVALID;
+  *stream = (void*)m->stream;
+  return MRF_OK;
+}
+
+mrf_status mrf_synchronize(mrf_map* m) {
+  if (guard(m) != MRF_OK) return MRF_ERR_INVALID;
+  return wrap([&] { sync(m); });
+}
+
+}  // extern "C"

@@ -1,0 +1,149 @@
+// mrf_internal.h -- structures shared between the C-ABI layer and the kernels.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace mrf {
+
+constexpr int kBrick = 8;
+constexpr int kBrickVox = 512;
+constexpr int kLookupPx = 20;          // include/mrfmap/GVDBCommon.cuh:11
+constexpr float kFEps = 1e-4f;         // GVDBCommon.cuh:5
+constexpr float kLikeEps = 1e-3f;      // GVDBCommon.cuh:8
+constexpr float kZMin = 0.1f;          // GVDBCommon.cuh:4
+constexpr float kZMax = 10.0f;         // GVDBCommon.cuh:3
+constexpr float kMuCutoff = 87.0f;     // 0.5 x^2 above which the fp32 potential is 0
+constexpr float kCumLenGate = 0.1f;    // gvdbkernels.cu:408
+constexpr int kLongRay = 512;          // rays longer than this carry FP64 sums
+
+// Geometry of one map (volume, camera intrinsics, sensor tables, brick table)
+struct Geom {
+  float res, inv_res;
+  float fx, fy, cx, cy;
+  int rows, cols;
+  float off[3];      // dims_xy/2/res, 0
+  float hi[3];       // dims/res (activation gate)
+  int NB[3];         // brick grid
+  int E[3];          // 8*NB, voxel box of the traversal
+  int lookup_n, n_tiles_u, n_tiles_v;
+  const float* sigma;   // device
+  const float* bias;    // device
+  const int* brick_slot;  // device, NB0*NB1*NB2
+};
+
+struct Pose {
+  float m[16];  // row-major camera-to-world
+};
+
+// per-ray record of the incidence lists
+struct RayMeta {
+  uint32_t off;     // global index of the ray's first incidence
+  uint16_t n_pre;   // incidences seen by the Pre pass
+  uint16_t n_post;  // incidences receiving a message
+  uint16_t r0;      // Pre-pass visibility start
+  uint16_t rinf;    // visibility start of the infinity term
+  uint32_t flags;   // bit0: infinity term applies
+};
+static_assert(sizeof(RayMeta) == 16, "RayMeta layout");
+
+constexpr int kMaxRayLen = 65535;
+
+// ---- launchers (stream-ordered; return cudaError_t of the launch) --------
+cudaError_t launch_clean_depth(const float* in, float* out, int rows, int cols, cudaStream_t s);
+cudaError_t launch_activate(const Geom& g, const Pose& P, const float* depth, int policy,
+                            uint8_t* flags, cudaStream_t s);
+cudaError_t launch_activate_points(const Geom& g, const float* pts, int64_t n, uint8_t* flags,
+                                   cudaStream_t s);
+cudaError_t launch_new_indicator(const uint8_t* flags, const int* slot, int* ind, int64_t n,
+                                 cudaStream_t s);
+cudaError_t launch_assign_slots2(const Geom& g, const int* ind, const int* scan, int nb_base,
+                                 int* brick_slot, int* brick_coord, int64_t n, cudaStream_t s);
+cudaError_t launch_fill_new_voxels(float* L, float* belief, int64_t v0, int64_t v1, float logit_prior,
+                                   cudaStream_t s);
+cudaError_t launch_set_points(const Geom& g, const float* pts, const float* occ, int64_t n,
+                              float* belief, cudaStream_t s);
+
+// traversal: count pass then emit pass
+cudaError_t launch_trace_count(const Geom& g, const Pose& P, const float* depth, uint32_t* counts,
+                               int* err, cudaStream_t s);
+cudaError_t launch_trace_emit(const Geom& g, const Pose& P, const float* depth,
+                              const uint32_t* pix_off, uint32_t inc_base, RayMeta* meta,
+                              uint32_t* inc_vox, float* inc_len, float* inc_mu, int* err,
+                              cudaStream_t s);
+// pairs (first-touch order) and the voxel-sorted CSR
+cudaError_t launch_first_touch(const uint32_t* inc_vox, uint32_t n, uint32_t* first, cudaStream_t s);
+cudaError_t launch_flag_first(const uint32_t* inc_vox, uint32_t n, const uint32_t* first,
+                              uint32_t* flag, cudaStream_t s);
+cudaError_t launch_pair_assign(const uint32_t* inc_vox, uint32_t n, const uint32_t* flag,
+                               const uint32_t* scan, uint32_t pair_base, uint32_t* pair_vox,
+                               uint32_t* first, cudaStream_t s);
+cudaError_t launch_inc_pair(const uint32_t* inc_vox, uint32_t n, const uint32_t* first,
+                            uint32_t* inc_pair, cudaStream_t s);
+cudaError_t launch_reset_first(const uint32_t* pair_vox, uint32_t npairs, uint32_t* first,
+                               cudaStream_t s);
+cudaError_t launch_sort_keys(const RayMeta* meta, int nrays, uint32_t inc_base,
+                             const uint32_t* inc_pair, uint32_t pair_base, uint32_t npairs,
+                             uint32_t* keys, uint32_t* vals, cudaStream_t s);
+cudaError_t launch_seg_bounds(const uint32_t* skeys, uint32_t n, uint32_t npairs, uint32_t* seg,
+                              cudaStream_t s);
+cudaError_t launch_pair_init2(const uint32_t* seg_local, const uint32_t* perm_local,
+                              uint32_t inc_base, uint32_t npairs, const float* inc_len,
+                              uint32_t perm_base, uint32_t pair_base, uint32_t* seg, float* cum,
+                              cudaStream_t s);
+cudaError_t launch_perm_copy(const uint32_t* perm_local, uint32_t n, uint32_t inc_base,
+                             uint32_t* perm, cudaStream_t s);
+cudaError_t launch_iota(uint32_t* out, uint32_t n, cudaStream_t s);
+// CUB helpers (scratch-managed by the caller)
+size_t scan_temp_bytes(uint32_t n);
+cudaError_t exclusive_scan_u32(void* tmp, size_t tmp_bytes, const uint32_t* in, uint32_t* out,
+                               uint32_t n, cudaStream_t s);
+size_t scan_temp_bytes_i32(int64_t n);
+cudaError_t exclusive_scan_i32(void* tmp, size_t tmp_bytes, const int* in, int* out, int64_t n,
+                               cudaStream_t s);
+size_t sort_temp_bytes(uint32_t n, int bits);
+cudaError_t sort_pairs_u32(void* tmp, size_t tmp_bytes, const uint32_t* kin, uint32_t* kout,
+                           const uint32_t* vin, uint32_t* vout, uint32_t n, int bits, cudaStream_t s);
+
+// BP
+struct BpArrays {
+  const RayMeta* meta;
+  const uint32_t* inc_pair;
+  const float* inc_len;
+  const float* inc_mu;
+  float* inc_pl;
+  const uint32_t* pair_vox;
+  float* pair_m;
+  const float* pair_cum;
+  float2* pair_q;
+  float* pair_dm;
+  const uint32_t* pair_seg;
+  const uint32_t* perm;
+  float* L;
+  float* belief;
+};
+cudaError_t launch_pair_prepare(const BpArrays& a, uint32_t p0, uint32_t p1, cudaStream_t s);
+cudaError_t launch_ray_bp(const BpArrays& a, uint32_t r0, uint32_t r1, int fix_reset, int num_sms,
+                          cudaStream_t s);
+cudaError_t launch_pair_update(const BpArrays& a, uint32_t p0, uint32_t p1, int jacobi,
+                               cudaStream_t s);
+cudaError_t launch_voxel_apply(const uint32_t* vseg, const uint32_t* vpairs, const uint32_t* vvox,
+                               uint32_t nvox, const float* pair_dm, float* L, float* belief,
+                               cudaStream_t s);
+cudaError_t launch_remap_scatter(const uint32_t* pair_vox, const float* pair_m, uint32_t n,
+                                 float* dense, cudaStream_t s);
+cudaError_t launch_remap_gather(const uint32_t* pair_vox, float* pair_m, uint32_t n,
+                                const float* dense, cudaStream_t s);
+cudaError_t launch_fill_f32(float* p, int64_t n, float v, cudaStream_t s);
+cudaError_t launch_vflag(const uint32_t* sk, uint32_t n, uint32_t* flag, cudaStream_t s);
+cudaError_t launch_vassign(const uint32_t* sk, const uint32_t* flag, const uint32_t* scan,
+                           uint32_t n, uint32_t* vvox, uint32_t* vseg, cudaStream_t s);
+cudaError_t launch_scatter_const(const uint32_t* idx, uint32_t n, float v, float* dense,
+                                 cudaStream_t s);
+
+// likelihood and readback
+cudaError_t launch_likelihood(const Geom& g, const Pose& P, const float* depth, const float* belief,
+                              float* out_img, double* partials, int nblocks, cudaStream_t s);
+int likelihood_blocks(const Geom& g);
+cudaError_t launch_reduce_partials(const double* partials, int n, float* out_sum, cudaStream_t s);
+
+}  // namespace mrf

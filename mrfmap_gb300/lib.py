@@ -1,0 +1,279 @@
+"""ctypes binding of the C ABI (``include/mrfmap_gb300.h``).
+
+This is the product path from Python: every call goes to
+``libmrfmap_gb300.so``; there is no CPU fallback.  If the library is not
+built, ``load()`` raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from .params import MapParams
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "_lib", "libmrfmap_gb300.so")
+
+MRF_OK = 0
+ACT_ENDPOINT = 0
+ACT_FULL_RAY = 1
+JACOBI = 1
+INCREMENTAL = 2
+FIX_PRE_RESET = 4
+ASYNC = 8
+
+_STATUS = {0: "MRF_OK", 1: "MRF_ERR_INVALID", 2: "MRF_ERR_CUDA", 3: "MRF_ERR_OOM",
+           4: "MRF_ERR_CAPACITY", 5: "MRF_ERR_DEVICE", 6: "MRF_ERR_STATE"}
+
+# every symbol declared in include/mrfmap_gb300.h
+EXPORTS = ["mrf_create", "mrf_destroy", "mrf_last_error", "mrf_add_view", "mrf_add_view_device",
+           "mrf_set_pose", "mrf_infer", "mrf_reset_state", "mrf_likelihood_view", "mrf_likelihood",
+           "mrf_likelihood_device", "mrf_num_bricks", "mrf_read_bricks", "mrf_read_logodds",
+           "mrf_num_nodes", "mrf_read_nodes", "mrf_load_map", "mrf_view_incidences",
+           "mrf_device_beliefs",
+           "mrf_stats_get", "mrf_get_stream", "mrf_synchronize"]
+
+
+class MrfError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{_STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+class mrf_params(C.Structure):
+    _fields_ = [("res", C.c_float), ("dims", C.c_float * 3), ("fx", C.c_float), ("fy", C.c_float),
+                ("cx", C.c_float), ("cy", C.c_float), ("rows", C.c_int), ("cols", C.c_int),
+                ("prior", C.c_float), ("max_iters", C.c_int), ("lookup_n", C.c_int),
+                ("sigma_lut", C.POINTER(C.c_float)), ("bias_lut", C.POINTER(C.c_float)),
+                ("occ_thresh", C.c_float), ("acc_thresh", C.c_float), ("activation", C.c_int),
+                ("reserved", C.c_int * 7)]
+
+
+class mrf_stats(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in ("n_views", "n_bricks", "n_rays", "n_inc_pre", "n_inc_post",
+                                         "n_pairs", "n_pairs_active", "n_vox_touched", "iters_done",
+                                         "kernel_launches")] + [("build_ms", C.c_double),
+                                                                ("infer_ms", C.c_double)]
+
+
+_lib = None
+
+
+def load(path: str | None = None):
+    """Load the native library (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or LIB_PATH
+    if not os.path.exists(path):
+        raise OSError(f"{path} not built; run __graft_entry__.build() or python -m mrfmap_gb300._build")
+    L = C.CDLL(path)
+    vp, fp, ip, i64p = C.c_void_p, C.POINTER(C.c_float), C.POINTER(C.c_int), C.POINTER(C.c_int64)
+    sig = {
+        "mrf_create": ([C.POINTER(mrf_params), C.POINTER(vp)], C.c_int),
+        "mrf_destroy": ([vp], None),
+        "mrf_last_error": ([], C.c_char_p),
+        "mrf_add_view": ([vp, fp, fp, ip], C.c_int),
+        "mrf_add_view_device": ([vp, fp, vp, ip], C.c_int),
+        "mrf_set_pose": ([vp, C.c_int, fp], C.c_int),
+        "mrf_infer": ([vp, ip, C.c_int, C.c_int, C.c_int], C.c_int),
+        "mrf_reset_state": ([vp], C.c_int),
+        "mrf_likelihood_view": ([vp, C.c_int, fp, fp], C.c_int),
+        "mrf_likelihood": ([vp, fp, fp, fp, fp], C.c_int),
+        "mrf_likelihood_device": ([vp, fp, vp, vp, vp], C.c_int),
+        "mrf_num_bricks": ([vp, i64p], C.c_int),
+        "mrf_read_bricks": ([vp, fp, fp, C.c_int64], C.c_int),
+        "mrf_read_logodds": ([vp, fp, C.c_int64], C.c_int),
+        "mrf_num_nodes": ([vp, C.c_int, i64p], C.c_int),
+        "mrf_read_nodes": ([vp, C.c_int, fp, C.c_int64], C.c_int),
+        "mrf_load_map": ([vp, fp, fp, C.c_int64], C.c_int),
+        "mrf_view_incidences": ([vp, C.c_int, ip, C.POINTER(C.c_uint32), fp, fp, C.c_int64, i64p],
+                                C.c_int),
+        "mrf_device_beliefs": ([vp, C.POINTER(vp), i64p], C.c_int),
+        "mrf_stats_get": ([vp, C.POINTER(mrf_stats)], C.c_int),
+        "mrf_get_stream": ([vp, C.POINTER(vp)], C.c_int),
+        "mrf_synchronize": ([vp], C.c_int),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = L
+    return L
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _fp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_float))
+
+
+def _check(st):
+    if st != MRF_OK:
+        raise MrfError(st, load().mrf_last_error().decode(errors="replace"))
+
+
+def make_params(p: MapParams, activation: int = ACT_ENDPOINT):
+    p.check()
+    sig = _f32(p.sigma_lut)
+    bias = _f32(p.bias_lut)
+    s = mrf_params()
+    s.res = p.res
+    s.dims = (C.c_float * 3)(*[float(v) for v in p.dims])
+    s.fx, s.fy, s.cx, s.cy = p.fx, p.fy, p.cx, p.cy
+    s.rows, s.cols = p.rows, p.cols
+    s.prior = p.prior
+    s.max_iters = p.max_iters
+    s.lookup_n = p.lookup_n
+    s.sigma_lut = _fp(sig)
+    s.bias_lut = _fp(bias)
+    s.occ_thresh = p.occ_thresh
+    s.acc_thresh = p.acc_thresh
+    s.activation = activation
+    return s, (sig, bias)
+
+
+class MRFMap:
+    """One occupancy map on the current CUDA device (C ABI handle)."""
+
+    def __init__(self, params: MapParams, activation: int = ACT_ENDPOINT):
+        self._L = load()
+        self.params = params
+        s, keep = make_params(params, activation)
+        h = C.c_void_p()
+        _check(self._L.mrf_create(C.byref(s), C.byref(h)))
+        self._h = h
+        self._keep = keep
+
+    def close(self):
+        if getattr(self, "_h", None):
+            self._L.mrf_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def add_view(self, pose, depth) -> int:
+        vid = C.c_int()
+        d = _f32(depth)
+        if d.shape != (self.params.rows, self.params.cols):
+            raise ValueError("depth image shape does not match params rows x cols")
+        _check(self._L.mrf_add_view(self._h, _fp(_f32(pose)), _fp(d), C.byref(vid)))
+        return vid.value
+
+    def add_view_device(self, pose, depth_dev_ptr: int) -> int:
+        vid = C.c_int()
+        _check(self._L.mrf_add_view_device(self._h, _fp(_f32(pose)), C.c_void_p(depth_dev_ptr),
+                                           C.byref(vid)))
+        return vid.value
+
+    def set_pose(self, view: int, pose):
+        _check(self._L.mrf_set_pose(self._h, view, _fp(_f32(pose))))
+
+    def infer(self, ids=None, iters: int = 0, flags: int = 0):
+        if ids is None:
+            _check(self._L.mrf_infer(self._h, None, 0, iters, flags))
+        else:
+            a = np.ascontiguousarray(ids, dtype=np.int32)
+            _check(self._L.mrf_infer(self._h, a.ctypes.data_as(C.POINTER(C.c_int)), len(a), iters, flags))
+
+    def reset_state(self):
+        _check(self._L.mrf_reset_state(self._h))
+
+    def synchronize(self):
+        _check(self._L.mrf_synchronize(self._h))
+
+    @property
+    def num_bricks(self) -> int:
+        n = C.c_int64()
+        _check(self._L.mrf_num_bricks(self._h, C.byref(n)))
+        return n.value
+
+    def read_bricks(self):
+        n = self.num_bricks
+        cen = np.zeros((n, 3), np.float32)
+        bel = np.zeros((n, 512), np.float32)
+        _check(self._L.mrf_read_bricks(self._h, _fp(cen), _fp(bel), n))
+        return cen, bel
+
+    def beliefs(self):
+        return self.read_bricks()[1]
+
+    def logodds(self):
+        n = self.num_bricks
+        out = np.zeros((n, 512), np.float32)
+        _check(self._L.mrf_read_logodds(self._h, _fp(out), n))
+        return out
+
+    def brick_coords(self) -> np.ndarray:
+        cen, _ = self.read_bricks()
+        return ((cen - 4) / 8).astype(np.int32)
+
+    def nodes(self, level: int):
+        n = C.c_int64()
+        _check(self._L.mrf_num_nodes(self._h, level, C.byref(n)))
+        out = np.zeros((n.value, 3), np.float32)
+        _check(self._L.mrf_read_nodes(self._h, level, _fp(out), n.value))
+        return out
+
+    def likelihood(self, pose, depth, image: bool = True):
+        img = np.zeros((self.params.rows, self.params.cols), np.float32) if image else None
+        s = C.c_float()
+        _check(self._L.mrf_likelihood(self._h, _fp(_f32(pose)), _fp(_f32(depth)),
+                                      _fp(img) if image else None, C.byref(s)))
+        return s.value, img
+
+    def likelihood_view(self, view: int, image: bool = True):
+        img = np.zeros((self.params.rows, self.params.cols), np.float32) if image else None
+        s = C.c_float()
+        _check(self._L.mrf_likelihood_view(self._h, view, _fp(img) if image else None, C.byref(s)))
+        return s.value, img
+
+    def likelihood_device(self, pose, depth_ptr: int, img_ptr: int | None, sum_ptr: int):
+        _check(self._L.mrf_likelihood_device(self._h, _fp(_f32(pose)), C.c_void_p(depth_ptr),
+                                             C.c_void_p(img_ptr) if img_ptr else None,
+                                             C.c_void_p(sum_ptr)))
+
+    def load_map(self, points, occupancies):
+        pts = _f32(points).reshape(-1, 3)
+        occ = _f32(occupancies).reshape(-1)
+        if len(pts) != len(occ):
+            raise ValueError("points and occupancies differ in length")
+        _check(self._L.mrf_load_map(self._h, _fp(pts), _fp(occ), len(pts)))
+
+    def view_incidences(self, view: int):
+        """Per-pixel meta (rows*cols, 5) and the view's incidences in ray order."""
+        n = C.c_int64()
+        hw = self.params.rows * self.params.cols
+        meta = np.zeros((hw, 5), np.int32)
+        _check(self._L.mrf_view_incidences(self._h, view, meta.ctypes.data_as(C.POINTER(C.c_int)),
+                                           None, None, None, 0, C.byref(n)))
+        k = n.value
+        vox = np.zeros(max(k, 1), np.uint32)
+        ln = np.zeros(max(k, 1), np.float32)
+        mu = np.zeros(max(k, 1), np.float32)
+        _check(self._L.mrf_view_incidences(self._h, view, None,
+                                           vox.ctypes.data_as(C.POINTER(C.c_uint32)), _fp(ln), _fp(mu),
+                                           k, C.byref(n)))
+        return meta, vox[:k], ln[:k], mu[:k]
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        _check(self._L.mrf_get_stream(self._h, C.byref(s)))
+        return s.value or 0
+
+    def stats(self) -> dict:
+        st = mrf_stats()
+        _check(self._L.mrf_stats_get(self._h, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in st._fields_}

@@ -1,0 +1,183 @@
+"""Seeded synthetic depth scenes (rooms with boxes and spheres).
+
+The reference publishes no dataset for its benchmarks; these scenes stand in
+with the shapes, sizes and noise model of the benchmark workloads:
+
+* ``small``  -- room 4x4x3 m, 6 boxes, 4 cm voxels, 5 frames 160x120
+  (fx=fy=120, cx=80, cy=60) on a 1.5 m circle at 1.2 m height aimed at the
+  room centre with +-5 deg yaw jitter, 10 BP iterations.
+* ``full``   -- room 6x6x3 m, 20 boxes + 3 spheres, 1 cm voxels, 13 frames
+  640x480 (fx=fy=525, cx=320, cy=240) on a seeded arc, max range 5 m,
+  20 BP iterations.
+
+Depth is an analytic z-depth ray cast through pixel centres plus Gaussian
+noise sigma(z) = 0.002 + 0.0012 z^2, with 2 % of pixels dropped to 0.  The
+sensor model handed to BP is the same polynomial (``const_sigmasq_poly``
+``[0.002, 0, 0.0012]``, bias 0), the prior is 0.1.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from .params import MapParams
+
+
+@dataclass
+class Scene:
+    room: np.ndarray                     # (6,) xmin ymin zmin xmax ymax zmax, seen from inside
+    boxes: np.ndarray                    # (n, 6) axis-aligned solids
+    spheres: np.ndarray = field(default_factory=lambda: np.zeros((0, 4)))
+
+
+def look_at(eye, target, yaw_jitter_rad: float = 0.0) -> np.ndarray:
+    """Camera-to-world pose (x right, y down, z forward), row-major 4x4."""
+    eye = np.asarray(eye, np.float64)
+    f = np.asarray(target, np.float64) - eye
+    if yaw_jitter_rad:
+        c, s = np.cos(yaw_jitter_rad), np.sin(yaw_jitter_rad)
+        f = np.array([c * f[0] - s * f[1], s * f[0] + c * f[1], f[2]])
+    f /= np.linalg.norm(f)
+    up = np.array([0.0, 0.0, 1.0])
+    x = np.cross(f, up)
+    x /= np.linalg.norm(x)
+    y = np.cross(f, x)
+    P = np.eye(4)
+    P[:3, 0], P[:3, 1], P[:3, 2], P[:3, 3] = x, y, f, eye
+    return P.astype(np.float32)
+
+
+def _ray_dirs(params: MapParams, pose: np.ndarray):
+    H, W = params.rows, params.cols
+    fx, fy, cx, cy = params.fx, params.fy, params.cx, params.cy
+    xs = (np.arange(W) + 0.5 - cx) / fx
+    ys = (np.arange(H) + 0.5 - cy) / fy
+    rc = np.stack(np.broadcast_arrays(xs[None, :], ys[:, None], np.ones((H, W))), -1)
+    R = pose[:3, :3].astype(np.float64)
+    return rc @ R.T  # unnormalised: z component in the camera frame is 1
+
+
+def render_depth(scene: Scene, params: MapParams, pose: np.ndarray) -> np.ndarray:
+    """Noise-free z-depth image (H, W) of the scene from ``pose``."""
+    d = _ray_dirs(params, pose).reshape(-1, 3)
+    o = pose[:3, 3].astype(np.float64)
+    with np.errstate(divide="ignore", invalid="ignore"):
+        inv = 1.0 / d
+        # room seen from inside: exit parameter of the slab intersection
+        lo = (scene.room[:3] - o) * inv
+        hi = (scene.room[3:] - o) * inv
+        t = np.min(np.maximum(lo, hi), axis=1)
+        for b in scene.boxes:
+            l = (b[:3] - o) * inv
+            h = (b[3:] - o) * inv
+            tn = np.max(np.minimum(l, h), axis=1)
+            tf = np.min(np.maximum(l, h), axis=1)
+            hit = (tn <= tf) & (tn > 0)
+            t = np.where(hit & (tn < t), tn, t)
+        for s in scene.spheres:
+            oc = o - s[:3]
+            a = np.einsum("ij,ij->i", d, d)
+            bq = 2.0 * d @ oc
+            c = oc @ oc - s[3] ** 2
+            disc = bq * bq - 4 * a * c
+            ok = disc >= 0
+            tt = (-bq - np.sqrt(np.where(ok, disc, 0))) / (2 * a)
+            hit = ok & (tt > 0)
+            t = np.where(hit & (tt < t), tt, t)
+    return t.reshape(params.rows, params.cols).astype(np.float32)
+
+
+def add_noise(depth: np.ndarray, rng: np.random.Generator, dropout: float = 0.02,
+              max_range: float | None = None) -> np.ndarray:
+    sig = 0.002 + 0.0012 * depth.astype(np.float64) ** 2
+    out = depth + rng.standard_normal(depth.shape) * sig
+    out = out.astype(np.float32)
+    out[rng.random(depth.shape) < dropout] = 0.0
+    if max_range is not None:
+        out[out > max_range] = 0.0
+    return out
+
+
+def _boxes(rng, n, half_xy, zmax, keep_out):
+    out = []
+    while len(out) < n:
+        side = rng.uniform(0.2, 1.0, 3)
+        c = np.array([rng.uniform(-half_xy + 0.6, half_xy - 0.6),
+                      rng.uniform(-half_xy + 0.6, half_xy - 0.6), side[2] / 2])
+        b = np.concatenate([c - side / 2, c + side / 2])
+        if b[5] > zmax:
+            continue
+        if any(np.all(k >= b[:3] - 0.1) and np.all(k <= b[3:] + 0.1) for k in keep_out):
+            continue
+        out.append(b)
+    return np.array(out)
+
+
+def sensor_params(params: MapParams) -> MapParams:
+    params.set_const_polys([0.002, 0.0, 0.0012], [0.0, 0.0, 0.0])
+    return params
+
+
+@dataclass
+class Workload:
+    name: str
+    params: MapParams
+    poses: list
+    depths: list
+    seed: int
+
+
+def small_room(seed: int = 0, n_frames: int = 5, rows: int = 120, cols: int = 160) -> Workload:
+    """Room 4x4x3 m, 6 boxes, 4 cm voxels, 5 frames 160x120."""
+    rng = np.random.default_rng(seed)
+    p = MapParams(res=0.04, dims=(4.0, 4.0, 3.0), rows=rows, cols=cols,
+                  fx=120.0 * cols / 160, fy=120.0 * cols / 160, cx=cols / 2, cy=rows / 2,
+                  prior=0.1, max_iters=10)
+    sensor_params(p)
+    eps = p.res / 2
+    room = np.array([-2 + eps, -2 + eps, eps, 2 - eps, 2 - eps, 3 - eps])
+    target = np.array([0.0, 0.0, 1.5])
+    phase = rng.uniform(0, 2 * np.pi)
+    eyes = [np.array([1.5 * np.cos(phase + 2 * np.pi * k / n_frames),
+                      1.5 * np.sin(phase + 2 * np.pi * k / n_frames), 1.2]) for k in range(n_frames)]
+    scene = Scene(room=room, boxes=_boxes(rng, 6, 2.0, 1.1, eyes))
+    poses, depths = [], []
+    for e in eyes:
+        P = look_at(e, target, np.deg2rad(rng.uniform(-5, 5)))
+        poses.append(P)
+        depths.append(add_noise(render_depth(scene, p, P), rng))
+    return Workload("small_room_5x160x120_4cm", p, poses, depths, seed)
+
+
+def full_room(seed: int = 1, n_frames: int = 13, rows: int = 480, cols: int = 640,
+              res: float = 0.01) -> Workload:
+    """Room 6x6x3 m, 20 boxes + 3 spheres, 1 cm voxels, 13 frames 640x480."""
+    rng = np.random.default_rng(seed)
+    f = 525.0 * cols / 640
+    p = MapParams(res=res, dims=(6.0, 6.0, 3.0), rows=rows, cols=cols,
+                  fx=f, fy=f, cx=cols / 2, cy=rows / 2, prior=0.1, max_iters=20)
+    sensor_params(p)
+    eps = res / 2
+    room = np.array([-3 + eps, -3 + eps, eps, 3 - eps, 3 - eps, 3 - eps])
+    a0 = rng.uniform(0, 2 * np.pi)
+    eyes = []
+    for k in range(n_frames):
+        a = a0 + np.pi * k / max(n_frames - 1, 1)
+        rad = 2.2 + rng.uniform(-0.2, 0.2)
+        eyes.append(np.array([rad * np.cos(a), rad * np.sin(a), 1.4 + rng.uniform(-0.2, 0.2)]))
+    boxes = _boxes(rng, 20, 3.0, 1.2, eyes)
+    sph = []
+    while len(sph) < 3:
+        r = rng.uniform(0.2, 0.5)
+        c = np.array([rng.uniform(-2.2, 2.2), rng.uniform(-2.2, 2.2), rng.uniform(0.6, 2.4)])
+        if all(np.linalg.norm(c - e) > r + 0.3 for e in eyes):
+            sph.append(np.concatenate([c, [r]]))
+    scene = Scene(room=room, boxes=boxes, spheres=np.array(sph))
+    poses, depths = [], []
+    target = np.array([0.0, 0.0, 1.2])
+    for e in eyes:
+        P = look_at(e, target, np.deg2rad(rng.uniform(-5, 5)))
+        poses.append(P)
+        depths.append(add_noise(render_depth(scene, p, P), rng, max_range=5.0))
+    return Workload(f"full_room_{n_frames}x{cols}x{rows}_{int(round(res * 100))}cm", p, poses, depths, seed)

@@ -1,0 +1,100 @@
+/*
+ * mrf_oracle.h -- CPU restatement of MRFMap's forward-ray-sensor-model BP
+ * and per-view likelihood.  TEST INFRASTRUCTURE ONLY: the parity tests, the
+ * smoke check and the CPU-baseline leg of bench.py call this; the product
+ * (libmrfmap_gb300.so) never links or calls it.
+ *
+ * PARITY UNPINNED against the reference itself: the reference depends on
+ * gvdb-voxels, Eigen, yaml-cpp and OpenCV, none of which exist in this
+ * build environment, and it ships no tests and no golden outputs.  This file
+ * restates the reference's update equations (cited per function) and
+ * replaces GVDB's brick traversal with an Amanatides-Woo voxel DDA whose
+ * float operations are specified exactly, so the GPU traversal can be
+ * checked bit-for-bit against it.
+ *
+ * Numerics: geometry (ray set-up, DDA, stop rules, potential cut-off,
+ * activation) is evaluated in fp32 with every operation rounded separately
+ * (build with -ffp-contract=off); the BP and likelihood arithmetic is FP64.
+ */
+#ifndef MRF_ORACLE_H
+#define MRF_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct {
+  float res;          /* voxel edge, metres */
+  float dims[3];      /* volume extent, metres (x, y centred; z from 0) */
+  float fx, fy, cx, cy;
+  int rows, cols;
+  float prior;        /* occupancy prior */
+  int lookup_n;       /* 3 = quadratic, 2 = linear sensor polynomials */
+  int n_tiles_u, n_tiles_v;   /* ceil(cols/20), ceil(rows/20) */
+  const float* sigma_lut;     /* n_tiles_v*n_tiles_u*lookup_n */
+  const float* bias_lut;
+} orc_params;
+
+/* activation policies */
+#define ORC_ACT_ENDPOINT 0   /* bricks around measured endpoints (reference) */
+#define ORC_ACT_FULL_RAY 1   /* + every brick the ray crosses up to d+3sigma */
+
+/* inference flags */
+#define ORC_JACOBI        1  /* all cameras from one snapshot per iteration */
+#define ORC_INCREMENTAL   2  /* keep per-camera messages across calls */
+#define ORC_FIX_PRE_RESET 4  /* carry Pre-pass visibility across all bricks */
+
+typedef struct orc_map orc_map;
+
+orc_map* orc_create(const orc_params* p);
+void orc_destroy(orc_map* m);
+void orc_set_threads(int n);
+
+/* pose: row-major 4x4 camera-to-world (metres); depth: rows*cols row-major,
+ * row 0 = top.  Returns the view id. */
+int orc_add_view(orc_map* m, const float* pose, const float* depth, int policy);
+int orc_set_pose(orc_map* m, int view, const float* pose, int policy);
+int orc_num_views(const orc_map* m);
+int orc_num_bricks(const orc_map* m);
+/* brick coordinates (n x 3 int, brick units) in slot order */
+void orc_brick_coords(const orc_map* m, int* out);
+int orc_brick_dims(const orc_map* m, int* out3);
+
+/* BP; ids selects which cameras' messages are zeroed (reference semantics);
+ * every camera is iterated. iters <= 0 -> use 1. */
+void orc_infer(orc_map* m, const int* ids, int n_ids, int iters, int flags);
+/* beliefs / log-odds, [n_bricks x 512] in slot order, element (x*8+y)*8+z */
+void orc_get_beliefs(const orc_map* m, float* out);
+void orc_get_beliefs_f64(const orc_map* m, double* out);
+void orc_get_logodds_f64(const orc_map* m, double* out);
+/* overwrite the belief field (for external-map likelihood tests) */
+void orc_set_beliefs(orc_map* m, const float* in);
+
+/* per-view incidence lists (built on demand).  Returns number of rays with
+ * at least one incidence; fills arrays when non-NULL.
+ *   ray_pix[r], ray_off[r] (int64), ray_meta[r*5+{n_pre,n_post,r0,rinf,inf_gate}]
+ *   inc_vox[i] (voxel id slot*512+local), inc_len[i], inc_s[i], inc_run[i]
+ */
+int64_t orc_view_num_incidences(orc_map* m, int view);
+int orc_view_trace(orc_map* m, int view, int* ray_pix, int64_t* ray_off,
+                   int* ray_meta, int* inc_vox, float* inc_len, float* inc_s,
+                   unsigned char* inc_run, double* inc_mu);
+
+/* trace one pixel through the current brick set (all active voxels to the
+ * volume exit; no stop rule).  Returns count, writes up to max entries. */
+int orc_trace_pixel(const orc_map* m, const float* pose, int x, int y,
+                    int* vox, float* len, float* s, int max);
+
+/* per-pixel log-likelihood image (rows*cols) of a depth image at a pose under
+ * the current belief field; returns the frame sum. */
+double orc_likelihood(const orc_map* m, const float* pose, const float* depth,
+                      float* out_img);
+
+/* counters from the last orc_infer: incidence-iterations of Post passes */
+int64_t orc_last_updates(const orc_map* m);
+
+#ifdef __cplusplus
+}
+#endif
+#endif
