@@ -1,0 +1,24 @@
+// GVDBImage.h -- a depth image handed to the map (reference:
+// include/mrfmap/GVDBImage.h).  Holds the row-major depth (metres, row 0 at
+// the top); upload and clean-up (NaN -> -1) happen when a camera is added.
+#pragma once
+#include <memory>
+#include <vector>
+
+#include "GVDBParams.h"
+
+class GVDBImage {
+ public:
+  GVDBImage(const float* depth_rowmajor, int rows, int cols);
+  GVDBImage(const float* depth_rowmajor, int rows, int cols, const gvdb_params_t& params);
+  const std::vector<float>& depth() const { return depth_; }
+  int rows() const { return rows_; }
+  int cols() const { return cols_; }
+  // back-projected valid pixels (n x 3, camera frame), GVDBImage.cpp:48-60
+  std::vector<float> get_reproj_points() const;
+
+ private:
+  std::vector<float> depth_;
+  int rows_, cols_;
+  gvdb_params_t params_;
+};

@@ -45,6 +45,7 @@ typedef enum {
 #define MRF_INCREMENTAL 2   /* keep per-camera messages across calls */
 #define MRF_FIX_PRE_RESET 4 /* carry Pre-pass visibility across all bricks */
 #define MRF_ASYNC 8         /* enqueue only; do not wait for completion */
+#define MRF_PROFILE 16      /* time every kernel with CUDA events (mrf_stats) */
 
 /* Mirrors gvdb_params_t (include/mrfmap/GVDBParams.h:11-28). */
 typedef struct mrf_params {
@@ -78,6 +79,11 @@ typedef struct mrf_stats {
   int64_t kernel_launches; /* kernels launched by the last mrf_infer */
   double build_ms;         /* last incidence-list build */
   double infer_ms;         /* last mrf_infer, device time */
+  /* MRF_PROFILE: summed device time and launch count per kernel of the last
+   * mrf_infer: [0] pair prepare, [1] ray messages, [2] pair update,
+   * [3] voxel apply (Jacobi) */
+  double kernel_ms[4];
+  int64_t kernel_count[4];
 } mrf_stats;
 
 /* Map construction: GVDBInference(...) + GVDBMRFMap::gpuAllocate

@@ -142,20 +142,17 @@ __global__ void __launch_bounds__(256) k_ray_bp(const RayMeta* __restrict__ meta
   }
 }
 
-__global__ void k_pair_update(const uint32_t* __restrict__ pair_vox, float* __restrict__ m,
-                              const float* __restrict__ cum, const uint32_t* __restrict__ seg,
-                              const uint32_t* __restrict__ perm, const float* __restrict__ pl,
-                              float* __restrict__ L, float* __restrict__ belief,
-                              float* __restrict__ dm, uint32_t p0, uint32_t p1, int jacobi) {
-  uint32_t p = p0 + blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= p1) return;
-  float c = cum[p];
-  if (!(c > kCumLenGate)) {
-    if (jacobi) dm[p] = 0.0f;
-    return;
-  }
-  float acc = 0.0f;
-  for (uint32_t k = seg[p]; k < seg[p + 1]; ++k) acc += pl[perm[k]];
+// Pair update.  The segment of a pair (its incidences in the voxel-grouped
+// permutation) is summed by a group of kGroup lanes striding through it, so
+// the permutation reads coalesce; the group's partial sums combine in a fixed
+// xor tree (deterministic).  Pairs with more than kLongSeg incidences (voxels
+// next to the camera, crossed by hundreds of rays) are skipped here and summed
+// by a whole warp in k_pair_update_long, which keeps the groups balanced.
+constexpr int kGroup = 8;
+constexpr uint32_t kLongSeg = 64;
+
+__device__ __forceinline__ void apply_pair(uint32_t p, float acc, float c, const uint32_t* pair_vox,
+                                           float* m, float* L, float* belief, float* dm, int jacobi) {
   float a = clampf(acc / c, kFEps, 1.0f - kFEps);
   float mn = logf(a) - logf(1.0f - a);
   float mo = m[p];
@@ -170,6 +167,69 @@ __global__ void k_pair_update(const uint32_t* __restrict__ pair_vox, float* __re
   belief[v] = 1.0f - clampf(1.0f / (1.0f + expf(Lv)), kFEps, 1.0f - kFEps);
 }
 
+__global__ void __launch_bounds__(256) k_pair_update(const uint32_t* __restrict__ pair_vox,
+                              float* __restrict__ m, const float* __restrict__ cum,
+                              const uint32_t* __restrict__ seg, const uint32_t* __restrict__ perm,
+                              const float* __restrict__ pl, float* __restrict__ L,
+                              float* __restrict__ belief, float* __restrict__ dm, uint32_t p0,
+                              uint32_t p1, int jacobi) {
+  const int gl = threadIdx.x & (kGroup - 1);
+  uint32_t p = p0 + (blockIdx.x * blockDim.x + threadIdx.x) / kGroup;
+  bool active = p < p1;
+  float c = 0.0f;
+  uint32_t s = 0, e = 0;
+  if (active) {
+    c = cum[p];
+    s = seg[p];
+    e = seg[p + 1];
+  }
+  bool upd = active && c > kCumLenGate && (e - s) <= kLongSeg;
+  float acc = 0.0f;
+  if (upd)
+    for (uint32_t k = s + gl; k < e; k += kGroup) acc += pl[perm[k]];
+#pragma unroll
+  for (int o = kGroup / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(kFull, acc, o);
+  if (gl != 0 || !active) return;
+  if (!(c > kCumLenGate)) {
+    if (jacobi) dm[p] = __int_as_float(0x7fc00000);  // NaN: pair not updated
+    return;
+  }
+  if (upd) apply_pair(p, acc, c, pair_vox, m, L, belief, dm, jacobi);
+}
+
+__global__ void __launch_bounds__(256) k_pair_update_long(const uint32_t* __restrict__ list,
+                                   uint32_t n, const uint32_t* __restrict__ pair_vox,
+                                   float* __restrict__ m, const float* __restrict__ cum,
+                                   const uint32_t* __restrict__ seg,
+                                   const uint32_t* __restrict__ perm, const float* __restrict__ pl,
+                                   float* __restrict__ L, float* __restrict__ belief,
+                                   float* __restrict__ dm, int jacobi) {
+  const int lane = threadIdx.x & 31;
+  for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n;
+       w += (gridDim.x * blockDim.x) >> 5) {
+    uint32_t p = list[w];
+    float c = cum[p];
+    float acc = 0.0f;
+    for (uint32_t k = seg[p] + lane; k < seg[p + 1]; k += 32) acc += pl[perm[k]];
+    acc = warp_sum(acc);
+    if (lane == 0 && c > kCumLenGate) apply_pair(p, acc, c, pair_vox, m, L, belief, dm, jacobi);
+  }
+}
+
+// list of the pairs with long segments (built once per incidence build)
+__global__ void k_long_flag(const uint32_t* __restrict__ seg, uint32_t p0, uint32_t p1,
+                            uint32_t* __restrict__ flag) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  uint32_t p = p0 + i;
+  if (p < p1) flag[i] = (seg[p + 1] - seg[p]) > kLongSeg ? 1u : 0u;
+}
+
+__global__ void k_long_scatter(const uint32_t* __restrict__ flag, const uint32_t* __restrict__ scan,
+                               uint32_t p0, uint32_t n, uint32_t* __restrict__ list) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && flag[i]) list[scan[i]] = p0 + i;
+}
+
 // Jacobi: total log-odds of each voxel moves by the sum of its cameras'
 // message changes (pairs of a voxel grouped by a voxel-sorted CSR)
 __global__ void k_voxel_apply(const uint32_t* __restrict__ vseg, const uint32_t* __restrict__ vpairs,
@@ -182,14 +242,31 @@ __global__ void k_voxel_apply(const uint32_t* __restrict__ vseg, const uint32_t*
   bool any = false;
   for (uint32_t k = vseg[i]; k < vseg[i + 1]; ++k) {
     float d = dm[vpairs[k]];
-    s += d;
-    any |= d != 0.0f;
+    if (d == d) {  // pairs below the length gate carry NaN and are skipped
+      s += d;
+      any = true;
+    }
   }
   if (!any) return;
   uint32_t v = vvox[i];
   float Lv = L[v] + s;
   L[v] = Lv;
   belief[v] = 1.0f - clampf(1.0f / (1.0f + expf(Lv)), kFEps, 1.0f - kFEps);
+}
+
+// moving a camera: take its messages out of the total log-odds
+__global__ void k_remove_messages(const uint32_t* __restrict__ pair_vox, float* __restrict__ m,
+                                  uint32_t p0, uint32_t p1, float* __restrict__ L,
+                                  float* __restrict__ belief) {
+  uint32_t p = p0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= p1) return;
+  float mo = m[p];
+  if (mo == 0.0f) return;
+  uint32_t v = pair_vox[p];
+  float Lv = L[v] - mo;
+  L[v] = Lv;
+  belief[v] = 1.0f - clampf(1.0f / (1.0f + expf(Lv)), kFEps, 1.0f - kFEps);
+  m[p] = 0.0f;
 }
 
 __global__ void k_remap_scatter(const uint32_t* __restrict__ pv, const float* __restrict__ m,
@@ -252,9 +329,33 @@ cudaError_t launch_ray_bp(const BpArrays& a, uint32_t r0, uint32_t r1, int fix_r
 cudaError_t launch_pair_update(const BpArrays& a, uint32_t p0, uint32_t p1, int jacobi,
                                cudaStream_t s) {
   if (p1 <= p0) return cudaSuccess;
-  k_pair_update<<<blocks(p1 - p0, 256), 256, 0, s>>>(a.pair_vox, a.pair_m, a.pair_cum, a.pair_seg,
-                                                     a.perm, a.inc_pl, a.L, a.belief, a.pair_dm,
-                                                     p0, p1, jacobi);
+  k_pair_update<<<blocks((int64_t)(p1 - p0) * kGroup, 256), 256, 0, s>>>(
+      a.pair_vox, a.pair_m, a.pair_cum, a.pair_seg, a.perm, a.inc_pl, a.L, a.belief, a.pair_dm, p0,
+      p1, jacobi);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pair_update_long(const BpArrays& a, const uint32_t* list, uint32_t n, int jacobi,
+                                    int num_sms, cudaStream_t s) {
+  if (!n) return cudaSuccess;
+  int64_t b = std::min<int64_t>(blocks((int64_t)n * 32, 256), (int64_t)num_sms * 8);
+  k_pair_update_long<<<(unsigned)b, 256, 0, s>>>(list, n, a.pair_vox, a.pair_m, a.pair_cum,
+                                                 a.pair_seg, a.perm, a.inc_pl, a.L, a.belief,
+                                                 a.pair_dm, jacobi);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_long_flag(const uint32_t* seg, uint32_t p0, uint32_t p1, uint32_t* flag,
+                             cudaStream_t s) {
+  if (p1 <= p0) return cudaSuccess;
+  k_long_flag<<<blocks(p1 - p0, 256), 256, 0, s>>>(seg, p0, p1, flag);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_long_scatter(const uint32_t* flag, const uint32_t* scan, uint32_t p0, uint32_t n,
+                                uint32_t* list, cudaStream_t s) {
+  if (!n) return cudaSuccess;
+  k_long_scatter<<<blocks(n, 256), 256, 0, s>>>(flag, scan, p0, n, list);
   return cudaGetLastError();
 }
 
@@ -263,6 +364,12 @@ cudaError_t launch_voxel_apply(const uint32_t* vseg, const uint32_t* vpairs, con
                                cudaStream_t s) {
   if (!nvox) return cudaSuccess;
   k_voxel_apply<<<blocks(nvox, 256), 256, 0, s>>>(vseg, vpairs, vvox, nvox, pair_dm, L, belief);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_remove_messages(const BpArrays& a, uint32_t p0, uint32_t p1, cudaStream_t s) {
+  if (p1 <= p0) return cudaSuccess;
+  k_remove_messages<<<blocks(p1 - p0, 256), 256, 0, s>>>(a.pair_vox, a.pair_m, p0, p1, a.L, a.belief);
   return cudaGetLastError();
 }
 

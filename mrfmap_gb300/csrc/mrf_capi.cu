@@ -84,6 +84,7 @@ struct View {
   uint32_t inc_base = 0, n_inc = 0;
   uint32_t pair_base = 0, n_pairs = 0;
   uint32_t perm_base = 0, n_perm = 0;
+  uint32_t long_base = 0, n_long = 0;  // pairs with long segments
 };
 
 uint32_t u32_checked(int64_t v, const char* what) {
@@ -108,7 +109,8 @@ struct mrf_map {
   std::vector<View> views;
   // arenas
   DBuf meta, inc_pair, inc_len, inc_mu, inc_pl, pair_vox, pair_m, pair_cum, pair_q, pair_dm,
-      pair_seg, perm;
+      pair_seg, perm, long_list;
+  int64_t n_long = 0;
   int64_t n_inc = 0, n_pairs = 0, n_perm = 0;
   // jacobi voxel CSR
   DBuf vseg, vpairs, vvox;
@@ -119,6 +121,9 @@ struct mrf_map {
       s_seg, s_dense, s_err, s_depth_in, s_depth, s_img, s_part, s_sum;
   int64_t first_cap_vox = 0;
   mrf_stats stats{};
+  // MRF_PROFILE event pool
+  std::vector<cudaEvent_t> prof_ev;
+  std::vector<int> prof_cat;
 
   BpArrays bp() const {
     BpArrays a;
@@ -343,7 +348,35 @@ void rebuild(mrf_map* m) {
   m->pair_q.reserve(pb * 8, false, m->stream);
   m->pair_dm.reserve(pb * 4, false, m->stream);
   CK(launch_fill_f32(m->pair_m.as<float>(), pair_total, 0.0f, m->stream));
-  // 5. carry messages of every camera over to its new pairs
+  // 5. per view, the pairs whose segments are long enough to need a warp
+  {
+    int64_t long_total = 0;
+    for (int c = 0; c < V; ++c) {
+      View& v = m->views[c];
+      v.long_base = (uint32_t)long_total;
+      v.n_long = 0;
+      if (!v.n_pairs) continue;
+      uint32_t np = v.n_pairs;
+      m->s_k0.reserve((size_t)np * 4 + 4, false, m->stream);
+      m->s_k1.reserve((size_t)np * 4 + 4, false, m->stream);
+      CK(launch_long_flag(m->pair_seg.as<uint32_t>(), v.pair_base, v.pair_base + np,
+                          m->s_k0.as<uint32_t>(), m->stream));
+      CK(cudaMemsetAsync(m->s_k0.as<uint32_t>() + np, 0, 4, m->stream));
+      size_t t = scan_temp_bytes(np + 1);
+      m->s_tmp.reserve(t, false, m->stream);
+      CK(exclusive_scan_u32(m->s_tmp.p, t, m->s_k0.as<uint32_t>(), m->s_k1.as<uint32_t>(), np + 1,
+                            m->stream));
+      uint32_t nl = read1(m, m->s_k1.as<uint32_t>() + np);
+      m->long_list.reserve((size_t)(long_total + nl + 1) * 4, true, m->stream);
+      CK(launch_long_scatter(m->s_k0.as<uint32_t>(), m->s_k1.as<uint32_t>(), v.pair_base, np,
+                             m->long_list.as<uint32_t>() + long_total, m->stream));
+      v.n_long = nl;
+      long_total += nl;
+    }
+    m->n_long = long_total;
+    m->long_list.reserve((size_t)(long_total + 1) * 4, true, m->stream);
+  }
+  // 6. carry messages of every camera over to its new pairs
   if (remap) {
     int64_t nv = m->n_bricks * kBrickVox;
     m->s_dense.reserve((size_t)nv * 4, false, m->stream);
@@ -430,6 +463,40 @@ void ensure_built(mrf_map* m) {
   if (m->built_version != m->version) rebuild(m);
 }
 
+struct Profiler {
+  mrf_map* m;
+  bool on;
+  size_t n = 0;
+  void begin(int cat) {
+    if (!on) return;
+    while (m->prof_ev.size() < 2 * (n + 1)) {
+      cudaEvent_t e;
+      CK(cudaEventCreate(&e));
+      m->prof_ev.push_back(e);
+    }
+    if (m->prof_cat.size() < n + 1) m->prof_cat.resize(n + 1);
+    m->prof_cat[n] = cat;
+    CK(cudaEventRecord(m->prof_ev[2 * n], m->stream));
+  }
+  void end() {
+    if (!on) return;
+    CK(cudaEventRecord(m->prof_ev[2 * n + 1], m->stream));
+    ++n;
+  }
+  void collect() {
+    for (int k = 0; k < 4; ++k) {
+      m->stats.kernel_ms[k] = 0.0;
+      m->stats.kernel_count[k] = 0;
+    }
+    for (size_t i = 0; i < n; ++i) {
+      float ms = 0.0f;
+      CK(cudaEventElapsedTime(&ms, m->prof_ev[2 * i], m->prof_ev[2 * i + 1]));
+      m->stats.kernel_ms[m->prof_cat[i]] += ms;
+      m->stats.kernel_count[m->prof_cat[i]] += 1;
+    }
+  }
+};
+
 void run_infer(mrf_map* m, const int* ids, int n_ids, int iters, int flags) {
   ensure_built(m);
   const bool jacobi = flags & MRF_JACOBI;
@@ -439,6 +506,7 @@ void run_infer(mrf_map* m, const int* ids, int n_ids, int iters, int flags) {
   if (iters <= 0) iters = m->prm.max_iters > 0 ? m->prm.max_iters : 1;
   BpArrays a = m->bp();
   int64_t launches = 0;
+  Profiler prof{m, (flags & MRF_PROFILE) != 0};
   CK(cudaEventRecord(m->ev0, m->stream));
   if (!(flags & MRF_INCREMENTAL)) {
     // src/GVDBInference.cpp:128-133: the selected cameras start from zero
@@ -446,6 +514,7 @@ void run_infer(mrf_map* m, const int* ids, int n_ids, int iters, int flags) {
       int c = ids ? ids[k] : k;
       if (c < 0 || c >= V) continue;
       const View& v = m->views[c];
+      if (v.n_pairs == 0) continue;
       CK(launch_fill_f32(m->pair_m.as<float>() + v.pair_base, v.n_pairs, 0.0f, m->stream));
       ++launches;
     }
@@ -457,19 +526,38 @@ void run_infer(mrf_map* m, const int* ids, int n_ids, int iters, int flags) {
       for (int c = 0; c < V; ++c) {
         const View& v = m->views[c];
         if (v.n_inc == 0) continue;
+        prof.begin(0);
         CK(launch_pair_prepare(a, v.pair_base, v.pair_base + v.n_pairs, m->stream));
+        prof.end();
+        prof.begin(1);
         CK(launch_ray_bp(a, (uint32_t)(c * HW), (uint32_t)((c + 1) * HW), fix, m->num_sms, m->stream));
+        prof.end();
+        prof.begin(2);
         CK(launch_pair_update(a, v.pair_base, v.pair_base + v.n_pairs, 0, m->stream));
-        launches += 3;
+        CK(launch_pair_update_long(a, m->long_list.as<uint32_t>() + v.long_base, v.n_long, 0,
+                                   m->num_sms, m->stream));
+        prof.end();
+        launches += v.n_long ? 4 : 3;
       }
     } else {
       uint32_t P = (uint32_t)m->n_pairs;
+      prof.begin(0);
       CK(launch_pair_prepare(a, 0, P, m->stream));
+      prof.end();
+      prof.begin(1);
       CK(launch_ray_bp(a, 0, (uint32_t)(V * HW), fix, m->num_sms, m->stream));
+      prof.end();
+      prof.begin(2);
       CK(launch_pair_update(a, 0, P, 1, m->stream));
+      CK(launch_pair_update_long(a, m->long_list.as<uint32_t>(), (uint32_t)m->n_long, 1, m->num_sms,
+                                 m->stream));
+      prof.end();
+      launches += m->n_long ? 1 : 0;
+      prof.begin(3);
       CK(launch_voxel_apply(m->vseg.as<uint32_t>(), m->vpairs.as<uint32_t>(), m->vvox.as<uint32_t>(),
                             m->n_vvox, m->pair_dm.as<float>(), m->d_L.as<float>(),
                             m->d_belief.as<float>(), m->stream));
+      prof.end();
       launches += 4;
     }
   }
@@ -477,11 +565,12 @@ void run_infer(mrf_map* m, const int* ids, int n_ids, int iters, int flags) {
   m->has_messages = true;
   m->stats.iters_done = iters;
   m->stats.kernel_launches = launches;
-  if (!(flags & MRF_ASYNC)) {
+  if (!(flags & MRF_ASYNC) || prof.on) {
     sync(m);
     float ms = 0.0f;
     cudaEventElapsedTime(&ms, m->ev0, m->ev1);
     m->stats.infer_ms = ms;
+    prof.collect();
   }
 }
 
@@ -541,6 +630,7 @@ void destroy_bufs(mrf_map* m) {
   DBuf* all[] = {&m->d_sigma, &m->d_bias, &m->d_slot, &m->d_coord, &m->d_L, &m->d_belief,
                  &m->meta, &m->inc_pair, &m->inc_len, &m->inc_mu, &m->inc_pl, &m->pair_vox,
                  &m->pair_m, &m->pair_cum, &m->pair_q, &m->pair_dm, &m->pair_seg, &m->perm,
+                 &m->long_list,
                  &m->vseg, &m->vpairs, &m->vvox, &m->s_first, &m->s_flags, &m->s_ind, &m->s_scan,
                  &m->s_tmp, &m->s_counts, &m->s_offs, &m->s_vox, &m->s_k0, &m->s_k1, &m->s_v0,
                  &m->s_v1, &m->s_seg, &m->s_dense, &m->s_err, &m->s_depth_in, &m->s_depth,
@@ -636,6 +726,7 @@ void mrf_destroy(mrf_map* m) {
   cudaSetDevice(m->device);
   if (m->stream) cudaStreamSynchronize(m->stream);
   destroy_bufs(m);
+  for (cudaEvent_t e : m->prof_ev) cudaEventDestroy(e);
   if (m->ev0) cudaEventDestroy(m->ev0);
   if (m->ev1) cudaEventDestroy(m->ev1);
   if (m->stream) cudaStreamDestroy(m->stream);
@@ -685,6 +776,11 @@ mrf_status mrf_set_pose(mrf_map* m, int view_id, const float* pose) {
     return MRF_ERR_INVALID;
   }
   return wrap([&] {
+    // take the camera's messages out of the total log-odds before it moves
+    // (src/GVDBInference.cpp:66-82 removes its ray contributions first)
+    const View& v = m->views[view_id];
+    if (m->has_messages && v.n_pairs)
+      CK(launch_remove_messages(m->bp(), v.pair_base, v.pair_base + v.n_pairs, m->stream));
     set_pose(m->views[view_id].pose, pose);
     activate_view(m, m->views[view_id]);
     m->version++;

@@ -126,9 +126,16 @@ cudaError_t launch_ray_bp(const BpArrays& a, uint32_t r0, uint32_t r1, int fix_r
                           cudaStream_t s);
 cudaError_t launch_pair_update(const BpArrays& a, uint32_t p0, uint32_t p1, int jacobi,
                                cudaStream_t s);
+cudaError_t launch_pair_update_long(const BpArrays& a, const uint32_t* list, uint32_t n, int jacobi,
+                                    int num_sms, cudaStream_t s);
+cudaError_t launch_long_flag(const uint32_t* seg, uint32_t p0, uint32_t p1, uint32_t* flag,
+                             cudaStream_t s);
+cudaError_t launch_long_scatter(const uint32_t* flag, const uint32_t* scan, uint32_t p0, uint32_t n,
+                                uint32_t* list, cudaStream_t s);
 cudaError_t launch_voxel_apply(const uint32_t* vseg, const uint32_t* vpairs, const uint32_t* vvox,
                                uint32_t nvox, const float* pair_dm, float* L, float* belief,
                                cudaStream_t s);
+cudaError_t launch_remove_messages(const BpArrays& a, uint32_t p0, uint32_t p1, cudaStream_t s);
 cudaError_t launch_remap_scatter(const uint32_t* pair_vox, const float* pair_m, uint32_t n,
                                  float* dense, cudaStream_t s);
 cudaError_t launch_remap_gather(const uint32_t* pair_vox, float* pair_m, uint32_t n,

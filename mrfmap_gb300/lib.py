@@ -23,6 +23,7 @@ JACOBI = 1
 INCREMENTAL = 2
 FIX_PRE_RESET = 4
 ASYNC = 8
+PROFILE = 16
 
 _STATUS = {0: "MRF_OK", 1: "MRF_ERR_INVALID", 2: "MRF_ERR_CUDA", 3: "MRF_ERR_OOM",
            4: "MRF_ERR_CAPACITY", 5: "MRF_ERR_DEVICE", 6: "MRF_ERR_STATE"}
@@ -55,7 +56,9 @@ class mrf_stats(C.Structure):
     _fields_ = [(n, C.c_int64) for n in ("n_views", "n_bricks", "n_rays", "n_inc_pre", "n_inc_post",
                                          "n_pairs", "n_pairs_active", "n_vox_touched", "iters_done",
                                          "kernel_launches")] + [("build_ms", C.c_double),
-                                                                ("infer_ms", C.c_double)]
+                                                                ("infer_ms", C.c_double),
+                                                                ("kernel_ms", C.c_double * 4),
+                                                                ("kernel_count", C.c_int64 * 4)]
 
 
 _lib = None
@@ -276,4 +279,7 @@ class MRFMap:
     def stats(self) -> dict:
         st = mrf_stats()
         _check(self._L.mrf_stats_get(self._h, C.byref(st)))
-        return {k: getattr(st, k) for k, _ in st._fields_}
+        out = {k: getattr(st, k) for k, _ in st._fields_}
+        out["kernel_ms"] = list(st.kernel_ms)
+        out["kernel_count"] = list(st.kernel_count)
+        return out

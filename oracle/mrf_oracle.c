@@ -441,8 +441,21 @@ int orc_add_view(orc_map* m, const float* pose, const float* depth, int policy) 
   return m->nviews - 1;
 }
 
+static double belief_of(double L);
+
+/* Moving a camera first removes its messages from the total log-odds (the
+ * reference subtracts the camera's ray contributions before re-activating,
+ * src/GVDBInference.cpp:66-82). */
 int orc_set_pose(orc_map* m, int view, const float* pose, int policy) {
   if (view < 0 || view >= m->nviews) return -1;
+  orc_view* v = &m->views[view];
+  for (int64_t i = 0; i < v->nvox_alloc; ++i) {
+    if (v->m[i] != 0.0) {
+      m->L[i] -= v->m[i];
+      m->belief[i] = belief_of(m->L[i]);
+      v->m[i] = 0.0;
+    }
+  }
   memcpy(m->views[view].pose, pose, 16 * sizeof(float));
   m->views[view].built_version = -1;
   activate_view(m, m->views[view].pose, m->views[view].depth, policy);

