@@ -125,6 +125,20 @@ MRF_API mrf_status mrf_likelihood(mrf_map* map, const float* pose, const float* 
 MRF_API mrf_status mrf_likelihood_device(mrf_map* map, const float* pose, const float* depth_dev,
                                  float* out_img_dev, float* out_sum_dev);
 
+/* Same as mrf_likelihood_device, but allocates no device memory: no
+ * counterpart in the reference.  For callers that may not allocate while
+ * scoring (real-time pose-search loops where cudaMalloc can stall the
+ * device, hosts whose allocator owns all device memory).  The depth image
+ * is cleaned on the fly; the only scratch is a fixed file-scope device array
+ * of 4096 FP64 partial sums (32 KiB), so images are limited to 524,288
+ * pixels (MRF_ERR_INVALID beyond; 640x480 and 848x480 fit).  All calls share that array: calls overlapping
+ * on the GPU race and must be serialized.  The first call on each device
+ * looks the array up with cudaGetSymbolAddress; make it before any stream
+ * capture.  The map must have active bricks (MRF_ERR_STATE otherwise). */
+MRF_API mrf_status mrf_likelihood_device_noalloc(mrf_map* map, const float* pose,
+                                                 const float* depth_dev, float* out_img_dev,
+                                                 float* out_sum_dev);
+
 /* GVDBMRFMap::get_occupied_bricks(0) (src/GVDBMRFMap.cpp:137-152). */
 MRF_API mrf_status mrf_num_bricks(mrf_map* map, int64_t* n_bricks);
 /* centres: n*3 floats, brick centres in voxel units (the reference's GVDB

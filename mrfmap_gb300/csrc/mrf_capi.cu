@@ -656,6 +656,34 @@ void likelihood_dev(mrf_map* m, const Pose& P, const float* depth_clean, float* 
 
 }  // namespace
 
+namespace mrf {
+
+mrf_status mrf_internal_like_inputs(mrf_map* m, Geom* g, const float** belief, cudaStream_t* stream,
+                                    int* device) {
+  if (!m) {
+    set_err("null map");
+    return MRF_ERR_INVALID;
+  }
+  if (cudaSetDevice(m->device) != cudaSuccess) {
+    set_err("cudaSetDevice failed");
+    return MRF_ERR_CUDA;
+  }
+  if (m->n_bricks == 0) {
+    set_err("the map has no active bricks");
+    return MRF_ERR_STATE;
+  }
+  *g = m->g;
+  g->brick_slot = m->d_slot.as<int>();
+  *belief = m->d_belief.as<float>();
+  *stream = m->stream;
+  *device = m->device;
+  return MRF_OK;
+}
+
+void mrf_internal_set_error(const std::string& msg) { set_err(msg); }
+
+}  // namespace mrf
+
 extern "C" {
 
 const char* mrf_last_error(void) { return g_last_error.c_str(); }

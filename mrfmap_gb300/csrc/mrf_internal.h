@@ -3,6 +3,10 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
+
+#include "../../include/mrfmap_gb300.h"
+
 namespace mrf {
 
 constexpr int kBrick = 8;
@@ -152,5 +156,12 @@ cudaError_t launch_likelihood(const Geom& g, const Pose& P, const float* depth, 
                               float* out_img, double* partials, int nblocks, cudaStream_t s);
 int likelihood_blocks(const Geom& g);
 cudaError_t launch_reduce_partials(const double* partials, int n, float* out_sum, cudaStream_t s);
+
+// Map state the likelihood needs, for entry points outside mrf_capi.cu: the
+// map's geometry (device brick table and sensor tables), its belief field,
+// stream and device.  Makes the map's device current.  Allocates nothing.
+mrf_status mrf_internal_like_inputs(mrf_map* map, Geom* g, const float** belief,
+                                    cudaStream_t* stream, int* device);
+void mrf_internal_set_error(const std::string& msg);
 
 }  // namespace mrf

@@ -31,7 +31,7 @@ _STATUS = {0: "MRF_OK", 1: "MRF_ERR_INVALID", 2: "MRF_ERR_CUDA", 3: "MRF_ERR_OOM
 # every symbol declared in include/mrfmap_gb300.h
 EXPORTS = ["mrf_create", "mrf_destroy", "mrf_last_error", "mrf_add_view", "mrf_add_view_device",
            "mrf_set_pose", "mrf_infer", "mrf_reset_state", "mrf_likelihood_view", "mrf_likelihood",
-           "mrf_likelihood_device", "mrf_num_bricks", "mrf_read_bricks", "mrf_read_logodds",
+           "mrf_likelihood_device", "mrf_likelihood_device_noalloc", "mrf_num_bricks", "mrf_read_bricks", "mrf_read_logodds",
            "mrf_num_nodes", "mrf_read_nodes", "mrf_load_map", "mrf_view_incidences",
            "mrf_device_beliefs",
            "mrf_stats_get", "mrf_get_stream", "mrf_synchronize"]
@@ -86,6 +86,7 @@ def load(path: str | None = None):
         "mrf_likelihood_view": ([vp, C.c_int, fp, fp], C.c_int),
         "mrf_likelihood": ([vp, fp, fp, fp, fp], C.c_int),
         "mrf_likelihood_device": ([vp, fp, vp, vp, vp], C.c_int),
+        "mrf_likelihood_device_noalloc": ([vp, fp, vp, vp, vp], C.c_int),
         "mrf_num_bricks": ([vp, i64p], C.c_int),
         "mrf_read_bricks": ([vp, fp, fp, C.c_int64], C.c_int),
         "mrf_read_logodds": ([vp, fp, C.c_int64], C.c_int),
