@@ -43,191 +43,386 @@ __device__ __forceinline__ T warp_sum(T v) {
 }
 
 __global__ void k_pair_prepare(const uint32_t* __restrict__ pair_vox, const float* __restrict__ m,
-                               const float* __restrict__ L, float2* __restrict__ q, uint32_t p0,
-                               uint32_t p1) {
+                               const float* __restrict__ L, float* __restrict__ lnq,
+                               float* __restrict__ dm, uint32_t p0, uint32_t p1) {
   uint32_t p = p0 + blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= p1) return;
   float eta = L[pair_vox[p]] - m[p];
   float qq = clampf(1.0f / (1.0f + expf(eta)), kFEps, 1.0f - kFEps);
-  q[p] = make_float2(qq, logf(qq));
+  lnq[p] = logf(qq);
+  if (dm) dm[p] = __int_as_float(0x7fc00000);  // Jacobi: NaN until the pair updates
 }
 
-// Accumulator type for the tau sums: fp32 for short rays, FP64 for rays with
-// more than kLongRay incidences (their sums run long enough for fp32
-// cancellation in R = T - F - tau to matter).
-template <typename Acc>
-__device__ __forceinline__ void ray_bp_warp(const RayMeta& me, const uint32_t* __restrict__ inc_pair,
+// ---- ray messages ----------------------------------------------------------
+// One warp per ray.  Each lane owns 4 consecutive incidences (ray offsets are
+// padded to multiples of 4, so the streams load as 16-byte vectors); a chunk
+// is 128 incidences.  Pass 1 runs over the Pre range computing the
+// visibility exponent A_i = sum_{j<=i} l_j ln q_j (thread-serial over 4, warp
+// scan across lanes), the visibility V_i = exp(A_i), q_i, and the Pre total T;
+// it stages (V_i mu_i, q_i, l_i) in shared memory.  Pass 2 reads the stage
+// back and writes p_i * l_i in ray order.  Rays longer than the stage recompute pass 1's
+// values in pass 2 and form T - F in FP64.
+//
+// Pre visibility restarts at r0 (the reference restores its carried state
+// only once the accumulated tau is non-zero, gvdbkernels.cu:708-715):
+// V^pre_i = exp(A_i - A_{r0-1}) = V_i * exp(-A_{r0-1}); Post uses V_i.
+constexpr int kRayWarps = 4;
+constexpr int kStage = 512;              // incidences staged per warp
+constexpr int kStageVec = kStage / 4;    // float4 entries per staged array
+constexpr float kUnderflowGuard = -60.0f;
+
+__device__ __forceinline__ float sel4(const float (&v)[4], int j) {
+  return j == 0 ? v[0] : (j == 1 ? v[1] : (j == 2 ? v[2] : v[3]));
+}
+
+template <typename T>
+__device__ __forceinline__ T warp_excl_scan(T v, int lane) {
+  T incl = warp_incl_scan(v, lane);
+  return incl - v;
+}
+
+// value held by lane idx/4 (element idx%4) of the current chunk
+__device__ __forceinline__ float chunk_value(const float (&A)[4], int idx_in_chunk) {
+  float mine = sel4(A, idx_in_chunk & 3);
+  return __shfl_sync(kFull, mine, idx_in_chunk >> 2);
+}
+
+struct Chunk {
+  float A[4], q[4], mu[4], len[4];
+};
+
+__device__ __forceinline__ float4 f4(const float (&v)[4]) { return make_float4(v[0], v[1], v[2], v[3]); }
+
+// loads chunk [base, base+128) of a ray (elements >= n are zero), its prefix
+// exponents and q; returns the chunk's total of l ln q
+__device__ __forceinline__ float load_chunk(Chunk& c, uint32_t off, int base, int n, float carryA,
+                                            int lane, const uint32_t* __restrict__ inc_pair,
                                             const float* __restrict__ inc_len,
                                             const float* __restrict__ inc_mu,
-                                            const float2* __restrict__ pq, float* __restrict__ inc_pl,
+                                            const float* __restrict__ lnq) {
+  int i0 = base + 4 * lane;
+  float a[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    c.q[j] = 1.0f;
+    c.mu[j] = c.len[j] = 0.0f;
+  }
+  if (i0 < n) {
+    uint4 pid = __ldg(reinterpret_cast<const uint4*>(inc_pair + off + i0));
+    float4 ln = __ldg(reinterpret_cast<const float4*>(inc_len + off + i0));
+    float4 mu = __ldg(reinterpret_cast<const float4*>(inc_mu + off + i0));
+    uint32_t pp[4] = {pid.x, pid.y, pid.z, pid.w};
+    float lv[4] = {ln.x, ln.y, ln.z, ln.w};
+    float mv[4] = {mu.x, mu.y, mu.z, mu.w};
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      if (i0 + j < n) {
+        float lq = __ldg(lnq + pp[j]);
+        c.q[j] = __expf(lq);
+        c.len[j] = lv[j];
+        c.mu[j] = mv[j];
+        a[j] = lv[j] * lq;
+      }
+    }
+  }
+  float s0 = a[0], s1 = s0 + a[1], s2 = s1 + a[2], s3 = s2 + a[3];
+  float ex = warp_excl_scan(s3, lane);
+  float b = carryA + ex;
+  c.A[0] = b + s0;
+  c.A[1] = b + s1;
+  c.A[2] = b + s2;
+  c.A[3] = b + s3;
+  return __shfl_sync(kFull, ex + s3, 31);
+}
+
+struct Stage {
+  float4 vmu[kStageVec], q[kStageVec], len[kStageVec];
+};
+
+template <bool kStaged, typename Acc>
+__device__ __forceinline__ void ray_bp_warp(const RayMeta& me, Stage& st,
+                                            const uint32_t* __restrict__ inc_pair,
+                                            const float* __restrict__ inc_len,
+                                            const float* __restrict__ inc_mu,
+                                            const float* __restrict__ lnq, float* __restrict__ inc_pl,
                                             int fix_reset, int lane) {
   const int n_pre = me.n_pre, n_post = me.n_post;
   const int r0 = fix_reset ? 0 : me.r0;
   const int rinf = fix_reset ? 0 : me.rinf;
   const uint32_t off = me.off;
-  // ---- Pre: T = sum_i V_i (1 - q_i) mu_i, visibility from r0 -------------
-  float carryA = 0.0f;
+  // ---- pass 1: prefixes, Pre total ---------------------------------------
+  float carryA = 0.0f, Ar0 = 0.0f, Arinf = 0.0f;
   Acc T = 0;
-  for (int base = r0; base < n_pre; base += 32) {
-    int i = base + lane;
-    float a = 0.0f, w = 0.0f, mu = 0.0f, q = 1.0f;
-    if (i < n_pre) {
-      float2 qq = pq[inc_pair[off + i]];
-      q = qq.x;
-      a = inc_len[off + i] * qq.y;
-      mu = inc_mu[off + i];
+  for (int base = 0; base < n_pre; base += 128) {
+    Chunk c;
+    float tot = load_chunk(c, off, base, n_pre, carryA, lane, inc_pair, inc_len, inc_mu, lnq);
+    if (r0 > 0 && r0 - 1 >= base && r0 - 1 < base + 128) Ar0 = chunk_value(c.A, r0 - 1 - base);
+    if (rinf > 0 && rinf - 1 >= base && rinf - 1 < base + 128) Arinf = chunk_value(c.A, rinf - 1 - base);
+    const int i0 = base + 4 * lane;
+    float V[4], w = 0.0f;
+    // exp(-A_{r0-1}) rescales Post visibility to Pre visibility unless the
+    // Post visibility may have underflowed (then exponentiate the difference)
+    const bool direct = Ar0 < kUnderflowGuard;
+    const float scale = direct ? 0.0f : __expf(-Ar0);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      V[j] = __expf(c.A[j]);
+      if (i0 + j >= r0 && c.mu[j] != 0.0f) {
+        float vp = direct ? __expf(c.A[j] - Ar0) : V[j] * scale;
+        w += vp * (1.0f - c.q[j]) * c.mu[j];
+      }
     }
-    float A = carryA + warp_incl_scan(a, lane);
-    if (mu != 0.0f) w = expf(A) * (1.0f - q) * mu;
+    if (kStaged && i0 < n_pre) {
+      int slot = (base >> 2) + lane;
+      float vm[4] = {V[0] * c.mu[0], V[1] * c.mu[1], V[2] * c.mu[2], V[3] * c.mu[3]};
+      st.vmu[slot] = f4(vm);
+      st.q[slot] = f4(c.q);
+      st.len[slot] = f4(c.len);
+    }
     T += (Acc)warp_sum(w);
-    carryA = __shfl_sync(kFull, A, 31);
+    carryA += tot;
   }
-  // ---- infinity term: visibility at the end of Pre ------------------------
-  if (me.flags & 1u) {
-    float Ainf;
-    if (rinf == r0) {
-      Ainf = carryA;
-    } else {
-      float s = 0.0f;
-      for (int i = rinf + lane; i < n_pre; i += 32) s += inc_len[off + i] * pq[inc_pair[off + i]].y;
-      Ainf = warp_sum(s);
-    }
-    T += (Acc)expf(Ainf);
-  }
-  // ---- Post: messages p_i for i < n_post -----------------------------------
-  carryA = 0.0f;
+  // infinity term: visibility at the end of Pre (gvdbkernels.cu:1196-1208)
+  if (me.flags & 1u) T += (Acc)__expf(carryA - Arinf);
+  if (kStaged) __syncwarp();
+  // ---- pass 2: messages ----------------------------------------------------
+  // Runs over the Pre range so that the (rare) Pre-only incidences past the
+  // Post stop get an explicit zero message.
   Acc carryF = 0;
-  for (int base = 0; base < n_post; base += 32) {
-    int i = base + lane;
-    bool valid = i < n_post;
-    float a = 0.0f, len = 0.0f, mu = 0.0f, q = 1.0f;
-    if (valid) {
-      float2 qq = pq[inc_pair[off + i]];
-      q = qq.x;
-      len = inc_len[off + i];
-      a = len * qq.y;
-      mu = inc_mu[off + i];
+  float carryA2 = 0.0f;
+  for (int base = 0; base < n_pre; base += 128) {
+    const int i0 = base + 4 * lane;
+    float vmu[4], q[4], len[4];
+    if (kStaged) {
+      int slot = (base >> 2) + lane;
+      float4 a = i0 < n_pre ? st.vmu[slot] : make_float4(0.f, 0.f, 0.f, 0.f);
+      float4 b = i0 < n_pre ? st.q[slot] : make_float4(1.f, 1.f, 1.f, 1.f);
+      float4 d = i0 < n_pre ? st.len[slot] : make_float4(0.f, 0.f, 0.f, 0.f);
+      vmu[0] = a.x; vmu[1] = a.y; vmu[2] = a.z; vmu[3] = a.w;
+      q[0] = b.x; q[1] = b.y; q[2] = b.z; q[3] = b.w;
+      len[0] = d.x; len[1] = d.y; len[2] = d.z; len[3] = d.w;
+    } else {
+      Chunk c;
+      float tot2 = load_chunk(c, off, base, n_pre, carryA2, lane, inc_pair, inc_len, inc_mu, lnq);
+      carryA2 += tot2;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        vmu[j] = __expf(c.A[j]) * c.mu[j];
+        q[j] = c.q[j];
+        len[j] = c.len[j];
+      }
     }
-    float A = carryA + warp_incl_scan(a, lane);
-    float V = expf(A);
-    float tau = valid ? V * (1.0f - q) * mu : 0.0f;
-    float tincl = warp_incl_scan(tau, lane);
-    float texcl = tincl - tau;
-    Acc F = carryF + (Acc)texcl;
-    Acc R = T - F - (Acc)tau;
-    float mu1 = (float)(F + (Acc)(V * mu));
-    float mu0 = (float)(F + R / (Acc)q);
-    float p = clampf(mu1 / (mu1 + mu0 + 1e-7f), kFEps, 1.0f - kFEps);
-    if (valid) inc_pl[off + i] = p * len;
-    carryA = __shfl_sync(kFull, A, 31);
-    carryF += (Acc)__shfl_sync(kFull, tincl, 31);
+    float tau[4];
+#pragma unroll
+    for (int j = 0; j < 4; ++j) tau[j] = (i0 + j < n_post) ? vmu[j] * (1.0f - q[j]) : 0.0f;
+    float e1 = tau[0], e2 = e1 + tau[1], e3 = e2 + tau[2], lt = e3 + tau[3];
+    float ex = warp_excl_scan(lt, lane);
+    float eloc[4] = {0.0f, e1, e2, e3};
+    // F_i = carryF + (in-chunk exclusive prefix); the long-range difference
+    // T - carryF is formed in Acc (FP64 on long rays) once per chunk
+    const float cF = (float)carryF;
+    const float D = (float)(T - carryF);
+    if (i0 < n_pre) {
+      float out[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        float fin = ex + eloc[j];
+        float F = cF + fin;
+        float R = (D - fin) - tau[j];
+        float mu1 = F + vmu[j];
+        float mu0 = F + __fdividef(R, q[j]);
+        float p = clampf(__fdividef(mu1, mu1 + mu0 + 1e-7f), kFEps, 1.0f - kFEps);
+        out[j] = (i0 + j < n_post) ? p * len[j] : 0.0f;
+      }
+      // messages in ray order (16-byte stores; the pair update gathers them)
+      *reinterpret_cast<float4*>(inc_pl + off + i0) = f4(out);
+    }
+    carryF += (Acc)__shfl_sync(kFull, ex + lt, 31);
   }
+  if (kStaged) __syncwarp();
 }
 
-__global__ void __launch_bounds__(256) k_ray_bp(const RayMeta* __restrict__ meta, uint32_t r0,
-                                                uint32_t r1, const uint32_t* __restrict__ inc_pair,
-                                                const float* __restrict__ inc_len,
-                                                const float* __restrict__ inc_mu,
-                                                const float2* __restrict__ pq,
-                                                float* __restrict__ inc_pl, int fix_reset) {
+__global__ void __launch_bounds__(kRayWarps * 32) k_ray_bp(const RayMeta* __restrict__ meta,
+                                                           uint32_t r0, uint32_t r1,
+                                                           const uint32_t* __restrict__ inc_pair,
+                                                           const float* __restrict__ inc_len,
+                                                           const float* __restrict__ inc_mu,
+                                                           const float* __restrict__ lnq,
+                                                           float* __restrict__ inc_pl,
+                                                           int fix_reset) {
+  __shared__ Stage stage_all[kRayWarps];
   const int lane = threadIdx.x & 31;
-  const uint32_t wpb = blockDim.x >> 5;
-  for (uint32_t r = r0 + blockIdx.x * wpb + (threadIdx.x >> 5); r < r1; r += gridDim.x * wpb) {
+  const int wid = threadIdx.x >> 5;
+  Stage& st = stage_all[wid];
+  for (uint32_t r = r0 + blockIdx.x * kRayWarps + wid; r < r1; r += gridDim.x * kRayWarps) {
     RayMeta me = meta[r];
     if (me.n_pre == 0) continue;
-    if (me.n_pre > kLongRay)
-      ray_bp_warp<double>(me, inc_pair, inc_len, inc_mu, pq, inc_pl, fix_reset, lane);
+    if (me.n_pre <= kStage)
+      ray_bp_warp<true, float>(me, st, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
     else
-      ray_bp_warp<float>(me, inc_pair, inc_len, inc_mu, pq, inc_pl, fix_reset, lane);
+      ray_bp_warp<false, double>(me, st, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
   }
 }
 
-// Pair update.  The segment of a pair (its incidences in the voxel-grouped
-// permutation) is summed by a group of kGroup lanes striding through it, so
-// the permutation reads coalesce; the group's partial sums combine in a fixed
-// xor tree (deterministic).  Pairs with more than kLongSeg incidences (voxels
-// next to the camera, crossed by hundreds of rays) are skipped here and summed
-// by a whole warp in k_pair_update_long, which keeps the groups balanced.
-constexpr int kGroup = 8;
-constexpr uint32_t kLongSeg = 64;
+// Pair update: a load-balanced segmented reduction over the pair-grouped
+// permutation of the messages.  Tiles of kTile consecutive positions are
+// summed by one block each (coalesced reads of the permutation and the pair
+// ids, kTile independent gathers of p*l in flight); segments that start and end inside a tile are applied there,
+// segments that cross tile edges leave partial sums that k_pair_fixup adds in
+// tile order.  Any segment length balances (voxels next to the camera are
+// crossed by thousands of rays) and the summation order is fixed.
+constexpr int kTileThreads = 256;
+constexpr int kTile = 4 * kTileThreads;
+constexpr uint32_t kOpenStart = 1u, kOpenEnd = 2u, kSingle = 4u;
 
-__device__ __forceinline__ void apply_pair(uint32_t p, float acc, float c, const uint32_t* pair_vox,
-                                           float* m, float* L, float* belief, float* dm, int jacobi) {
-  float a = clampf(acc / c, kFEps, 1.0f - kFEps);
-  float mn = logf(a) - logf(1.0f - a);
+struct SegAgg {
+  float s;
+  bool f;  // a segment head lies inside
+};
+
+__device__ __forceinline__ SegAgg seg_combine(SegAgg a, SegAgg b) {
+  return SegAgg{b.f ? b.s : a.s + b.s, a.f || b.f};
+}
+
+__global__ void __launch_bounds__(kTileThreads)
+    k_pair_reduce(const uint32_t* __restrict__ perm, const uint32_t* __restrict__ skey,
+                  const float* __restrict__ pl, uint32_t k0, uint32_t k1,
+                  TileCarry* __restrict__ carry, float* __restrict__ acc) {
+  __shared__ uint32_t sk[kTile];
+  __shared__ float sv[kTile];
+  __shared__ SegAgg wagg[kTileThreads / 32];
+  __shared__ uint32_t nb_key[2];
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  const uint32_t base = k0 + blockIdx.x * kTile;
+  const int n = (int)min((uint32_t)kTile, k1 - base);
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    int i = j * kTileThreads + t;
+    if (i < n) {
+      uint32_t kk = base + i;
+      sk[i] = skey[kk];
+      sv[i] = pl[perm[kk]];
+    }
+  }
+  if (t == 0) nb_key[0] = base > k0 ? skey[base - 1] : 0xFFFFFFFFu;
+  if (t == 1) nb_key[1] = base + n < k1 ? skey[base + n] : 0xFFFFFFFFu;
+  __syncthreads();
+  const uint32_t prev_key = nb_key[0], next_key = nb_key[1];
+  // this thread's 4 consecutive positions
+  uint32_t key[4];
+  float v[4], s[4];
+  bool h[4], valid[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    int i = 4 * t + j;
+    valid[j] = i < n;
+    key[j] = valid[j] ? sk[i] : 0xFFFFFFFEu;
+    v[j] = valid[j] ? sv[i] : 0.0f;
+    h[j] = valid[j] && (i == 0 || sk[i - 1] != key[j]);
+  }
+  s[0] = v[0];
+#pragma unroll
+  for (int j = 1; j < 4; ++j) s[j] = h[j] ? v[j] : s[j - 1] + v[j];
+  SegAgg agg{s[3], h[0] || h[1] || h[2] || h[3]};
+  // warp-level exclusive segmented scan of the thread aggregates
+  SegAgg inc = agg;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    float os = __shfl_up_sync(kFull, inc.s, o);
+    bool of = __shfl_up_sync(kFull, (int)inc.f, o) != 0;
+    if (lane >= o) inc = seg_combine(SegAgg{os, of}, inc);
+  }
+  SegAgg exw{__shfl_up_sync(kFull, inc.s, 1), __shfl_up_sync(kFull, (int)inc.f, 1) != 0};
+  if (lane == 0) exw = SegAgg{0.0f, false};
+  if (lane == 31) wagg[w] = inc;
+  __syncthreads();
+  SegAgg exb{0.0f, false};
+  for (int i = 0; i < w; ++i) exb = seg_combine(exb, wagg[i]);
+  SegAgg ex = lane == 0 ? exb : seg_combine(exb, exw);
+  // inclusive sums from each segment's first position inside the tile
+  bool head_seen = false;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    head_seen = head_seen || h[j];
+    float sj = head_seen ? s[j] : ex.s + s[j];
+    if (!valid[j]) continue;
+    int i = 4 * t + j;
+    bool last = (i == n - 1) || (sk[i + 1] != key[j]);
+    if (!last) continue;
+    // does the segment continue beyond the tile, and did it start before it?
+    // (keys are sorted, so a segment holds position 0 iff its key is sk[0])
+    bool open_end = (i == n - 1) && key[j] == next_key;
+    bool open_start = key[j] == sk[0] && sk[0] == prev_key;
+    if (!open_start && !open_end) {
+      acc[key[j]] = sj;
+    } else {
+      TileCarry& c = carry[blockIdx.x];
+      if (open_start) {
+        c.first_key = key[j];
+        c.first_sum = sj;
+      }
+      if (open_end) {
+        c.last_key = key[j];
+        c.last_sum = sj;
+      }
+    }
+  }
+  if (t == 0) {
+    uint32_t f = 0;
+    if (sk[0] == prev_key) f |= kOpenStart;
+    if (sk[n - 1] == next_key) f |= kOpenEnd;
+    if (sk[0] == sk[n - 1]) f |= kSingle;  // sorted keys: equal ends => one segment
+    carry[blockIdx.x].flags = f;
+  }
+}
+
+// segments crossing tile edges: the tile where such a segment starts walks
+// forward adding each following tile's partial, in tile order
+__global__ void k_pair_fixup(const TileCarry* __restrict__ carry, uint32_t ntiles,
+                             float* __restrict__ acc) {
+  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntiles) return;
+  TileCarry c = carry[t];
+  if (!(c.flags & kOpenEnd)) return;
+  if ((c.flags & kSingle) && (c.flags & kOpenStart)) return;  // not where the segment starts
+  float sum = c.last_sum;
+  uint32_t key = c.last_key;
+  for (uint32_t u = t + 1; u < ntiles; ++u) {
+    TileCarry d = carry[u];
+    sum += d.first_sum;
+    if ((d.flags & kSingle) && (d.flags & kOpenEnd)) continue;
+    break;
+  }
+  acc[key] = sum;
+}
+
+// factor->voxel update per pair (gvdbkernels.cu:457-479): pairs are in voxel
+// order, so every access here streams
+__global__ void __launch_bounds__(256) k_pair_apply(uint32_t p0, uint32_t p1,
+                                                    const float* __restrict__ acc,
+                                                    const uint32_t* __restrict__ pair_vox,
+                                                    float* __restrict__ m,
+                                                    const float* __restrict__ cum,
+                                                    float* __restrict__ L,
+                                                    float* __restrict__ belief,
+                                                    float* __restrict__ dm, int jacobi) {
+  uint32_t p = p0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= p1) return;
+  float c = cum[p];
+  float a0 = acc[p];
   float mo = m[p];
+  uint32_t v = pair_vox[p];
+  if (!(c > kCumLenGate)) return;  // gvdbkernels.cu:408: pair never updates
+  float a = clampf(a0 / c, kFEps, 1.0f - kFEps);
+  float mn = logf(a) - logf(1.0f - a);
   m[p] = mn;
   if (jacobi) {
     dm[p] = mn - mo;
     return;
   }
-  uint32_t v = pair_vox[p];
   float Lv = L[v] + (mn - mo);
   L[v] = Lv;
   belief[v] = 1.0f - clampf(1.0f / (1.0f + expf(Lv)), kFEps, 1.0f - kFEps);
-}
-
-__global__ void __launch_bounds__(256) k_pair_update(const uint32_t* __restrict__ pair_vox,
-                              float* __restrict__ m, const float* __restrict__ cum,
-                              const uint32_t* __restrict__ seg, const uint32_t* __restrict__ perm,
-                              const float* __restrict__ pl, float* __restrict__ L,
-                              float* __restrict__ belief, float* __restrict__ dm, uint32_t p0,
-                              uint32_t p1, int jacobi) {
-  const int gl = threadIdx.x & (kGroup - 1);
-  uint32_t p = p0 + (blockIdx.x * blockDim.x + threadIdx.x) / kGroup;
-  bool active = p < p1;
-  float c = 0.0f;
-  uint32_t s = 0, e = 0;
-  if (active) {
-    c = cum[p];
-    s = seg[p];
-    e = seg[p + 1];
-  }
-  bool upd = active && c > kCumLenGate && (e - s) <= kLongSeg;
-  float acc = 0.0f;
-  if (upd)
-    for (uint32_t k = s + gl; k < e; k += kGroup) acc += pl[perm[k]];
-#pragma unroll
-  for (int o = kGroup / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(kFull, acc, o);
-  if (gl != 0 || !active) return;
-  if (!(c > kCumLenGate)) {
-    if (jacobi) dm[p] = __int_as_float(0x7fc00000);  // NaN: pair not updated
-    return;
-  }
-  if (upd) apply_pair(p, acc, c, pair_vox, m, L, belief, dm, jacobi);
-}
-
-__global__ void __launch_bounds__(256) k_pair_update_long(const uint32_t* __restrict__ list,
-                                   uint32_t n, const uint32_t* __restrict__ pair_vox,
-                                   float* __restrict__ m, const float* __restrict__ cum,
-                                   const uint32_t* __restrict__ seg,
-                                   const uint32_t* __restrict__ perm, const float* __restrict__ pl,
-                                   float* __restrict__ L, float* __restrict__ belief,
-                                   float* __restrict__ dm, int jacobi) {
-  const int lane = threadIdx.x & 31;
-  for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n;
-       w += (gridDim.x * blockDim.x) >> 5) {
-    uint32_t p = list[w];
-    float c = cum[p];
-    float acc = 0.0f;
-    for (uint32_t k = seg[p] + lane; k < seg[p + 1]; k += 32) acc += pl[perm[k]];
-    acc = warp_sum(acc);
-    if (lane == 0 && c > kCumLenGate) apply_pair(p, acc, c, pair_vox, m, L, belief, dm, jacobi);
-  }
-}
-
-// list of the pairs with long segments (built once per incidence build)
-__global__ void k_long_flag(const uint32_t* __restrict__ seg, uint32_t p0, uint32_t p1,
-                            uint32_t* __restrict__ flag) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  uint32_t p = p0 + i;
-  if (p < p1) flag[i] = (seg[p + 1] - seg[p]) > kLongSeg ? 1u : 0u;
-}
-
-__global__ void k_long_scatter(const uint32_t* __restrict__ flag, const uint32_t* __restrict__ scan,
-                               uint32_t p0, uint32_t n, uint32_t* __restrict__ list) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n && flag[i]) list[scan[i]] = p0 + i;
 }
 
 // Jacobi: total log-odds of each voxel moves by the sum of its cameras'
@@ -281,6 +476,11 @@ __global__ void k_remap_gather(const uint32_t* __restrict__ pv, float* __restric
   if (p < n) m[p] = dense[pv[p]];
 }
 
+__global__ void k_fill_u32(uint32_t* p, int64_t n, uint32_t v) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = v;
+}
+
 __global__ void k_fill(float* p, int64_t n, float v) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) p[i] = v;
@@ -310,54 +510,43 @@ inline unsigned blocks(int64_t n, int t) { return (unsigned)std::max<int64_t>(1,
 
 }  // namespace
 
-cudaError_t launch_pair_prepare(const BpArrays& a, uint32_t p0, uint32_t p1, cudaStream_t s) {
+cudaError_t launch_pair_prepare(const BpArrays& a, uint32_t p0, uint32_t p1, int jacobi,
+                                cudaStream_t s) {
   if (p1 <= p0) return cudaSuccess;
-  k_pair_prepare<<<blocks(p1 - p0, 256), 256, 0, s>>>(a.pair_vox, a.pair_m, a.L, a.pair_q, p0, p1);
+  k_pair_prepare<<<blocks(p1 - p0, 256), 256, 0, s>>>(a.pair_vox, a.pair_m, a.L, a.pair_lnq,
+                                                      jacobi ? a.pair_dm : nullptr, p0, p1);
   return cudaGetLastError();
 }
+
 
 cudaError_t launch_ray_bp(const BpArrays& a, uint32_t r0, uint32_t r1, int fix_reset, int num_sms,
                           cudaStream_t s) {
   if (r1 <= r0) return cudaSuccess;
   int64_t warps = r1 - r0;
-  int64_t b = std::min<int64_t>(blocks(warps, 8), (int64_t)num_sms * 8);
-  k_ray_bp<<<(unsigned)b, 256, 0, s>>>(a.meta, r0, r1, a.inc_pair, a.inc_len, a.inc_mu, a.pair_q,
-                                       a.inc_pl, fix_reset);
+  int64_t b = std::min<int64_t>(blocks(warps, kRayWarps), (int64_t)num_sms * 8);
+  k_ray_bp<<<(unsigned)b, kRayWarps * 32, 0, s>>>(a.meta, r0, r1, a.inc_pair, a.inc_len, a.inc_mu,
+                                                  a.pair_lnq, a.inc_pl, fix_reset);
   return cudaGetLastError();
 }
 
-cudaError_t launch_pair_update(const BpArrays& a, uint32_t p0, uint32_t p1, int jacobi,
-                               cudaStream_t s) {
+cudaError_t launch_pair_update(const BpArrays& a, uint32_t k0, uint32_t k1, uint32_t p0, uint32_t p1,
+                               TileCarry* carry, int jacobi, cudaStream_t s) {
+  if (k1 > k0) {
+    uint32_t ntiles = (k1 - k0 + kTile - 1) / kTile;
+    k_pair_reduce<<<ntiles, kTileThreads, 0, s>>>(a.perm, a.skey, a.inc_pl, k0, k1, carry, a.pair_acc);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_pair_fixup<<<blocks(ntiles, 256), 256, 0, s>>>(carry, ntiles, a.pair_acc);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
   if (p1 <= p0) return cudaSuccess;
-  k_pair_update<<<blocks((int64_t)(p1 - p0) * kGroup, 256), 256, 0, s>>>(
-      a.pair_vox, a.pair_m, a.pair_cum, a.pair_seg, a.perm, a.inc_pl, a.L, a.belief, a.pair_dm, p0,
-      p1, jacobi);
+  k_pair_apply<<<blocks(p1 - p0, 256), 256, 0, s>>>(p0, p1, a.pair_acc, a.pair_vox, a.pair_m,
+                                                    a.pair_cum, a.L, a.belief, a.pair_dm, jacobi);
   return cudaGetLastError();
 }
 
-cudaError_t launch_pair_update_long(const BpArrays& a, const uint32_t* list, uint32_t n, int jacobi,
-                                    int num_sms, cudaStream_t s) {
-  if (!n) return cudaSuccess;
-  int64_t b = std::min<int64_t>(blocks((int64_t)n * 32, 256), (int64_t)num_sms * 8);
-  k_pair_update_long<<<(unsigned)b, 256, 0, s>>>(list, n, a.pair_vox, a.pair_m, a.pair_cum,
-                                                 a.pair_seg, a.perm, a.inc_pl, a.L, a.belief,
-                                                 a.pair_dm, jacobi);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_long_flag(const uint32_t* seg, uint32_t p0, uint32_t p1, uint32_t* flag,
-                             cudaStream_t s) {
-  if (p1 <= p0) return cudaSuccess;
-  k_long_flag<<<blocks(p1 - p0, 256), 256, 0, s>>>(seg, p0, p1, flag);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_long_scatter(const uint32_t* flag, const uint32_t* scan, uint32_t p0, uint32_t n,
-                                uint32_t* list, cudaStream_t s) {
-  if (!n) return cudaSuccess;
-  k_long_scatter<<<blocks(n, 256), 256, 0, s>>>(flag, scan, p0, n, list);
-  return cudaGetLastError();
-}
+uint32_t pair_update_tiles(uint32_t n) { return (n + kTile - 1) / kTile; }
 
 cudaError_t launch_voxel_apply(const uint32_t* vseg, const uint32_t* vpairs, const uint32_t* vvox,
                                uint32_t nvox, const float* pair_dm, float* L, float* belief,
@@ -384,6 +573,12 @@ cudaError_t launch_remap_gather(const uint32_t* pair_vox, float* pair_m, uint32_
                                 const float* dense, cudaStream_t s) {
   if (!n) return cudaSuccess;
   k_remap_gather<<<blocks(n, 256), 256, 0, s>>>(pair_vox, pair_m, n, dense);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fill_u32(uint32_t* p, int64_t n, uint32_t v, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_fill_u32<<<blocks(n, 256), 256, 0, s>>>(p, n, v);
   return cudaGetLastError();
 }
 

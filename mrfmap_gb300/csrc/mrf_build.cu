@@ -163,7 +163,7 @@ __global__ void __launch_bounds__(kThreads)
     k_trace(Geom g, Pose P, const float* __restrict__ depth, uint32_t* __restrict__ counts,
             const uint32_t* __restrict__ pix_off, uint32_t inc_base, RayMeta* __restrict__ meta,
             uint32_t* __restrict__ inc_vox, float* __restrict__ inc_len,
-            float* __restrict__ inc_mu, int* __restrict__ err) {
+            float* __restrict__ inc_mu, float* __restrict__ post_len, int* __restrict__ err) {
   int pix = blockIdx.x * blockDim.x + threadIdx.x;
   if (pix >= g.rows * g.cols) return;
   float d = depth[pix];
@@ -234,9 +234,19 @@ __global__ void __launch_bounds__(kThreads)
   }
   if (n_pre < 0) n_pre = count;
   if (n_post < 0) n_post = count;
+  // each ray's list is padded to a multiple of 4 incidences (16-byte vector
+  // loads in the BP kernels); padding carries an invalid voxel id
+  const int padded = (n_pre + 3) & ~3;
   if (!EMIT) {
-    counts[pix] = (uint32_t)n_pre;
+    counts[pix] = (uint32_t)padded;
   } else {
+    for (int k = n_pre; k < padded; ++k) {
+      inc_vox[base + k] = kNoVoxel;
+      inc_len[base + k] = 0.0f;
+      inc_mu[base + k] = 0.0f;
+    }
+    // lengths that count towards the cumulative length (Post range only)
+    for (int k = 0; k < padded; ++k) post_len[base + k] = k < n_post ? inc_len[base + k] : 0.0f;
     RayMeta m;
     m.off = inc_base + base;
     m.n_pre = (uint16_t)n_pre;
@@ -248,92 +258,46 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
-__global__ void k_first_touch(const uint32_t* __restrict__ vox, uint32_t n, uint32_t* first) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  atomicMin(&first[vox[i]], i);
+// Pairs in voxel order.  The view's incidences are sorted by voxel id
+// (stable: increasing incidence index inside a voxel); each run of one voxel
+// is a (camera, voxel) pair.  perm[k] is the incidence at pair-grouped
+// position k and skey[k] its pair.
+__global__ void k_vox_heads(const uint32_t* __restrict__ sk, uint32_t n, uint32_t* __restrict__ flag) {
+  uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) flag[k] = (k == 0 || sk[k] != sk[k - 1]) ? 1u : 0u;
 }
 
-__global__ void k_flag_first(const uint32_t* __restrict__ vox, uint32_t n,
-                             const uint32_t* __restrict__ first, uint32_t* __restrict__ flag) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  flag[i] = first[vox[i]] == i ? 1u : 0u;
-}
-
-__global__ void k_pair_assign(const uint32_t* __restrict__ vox, uint32_t n,
-                              const uint32_t* __restrict__ flag, const uint32_t* __restrict__ scan,
-                              uint32_t pair_base, uint32_t* __restrict__ pair_vox, uint32_t* first) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n || !flag[i]) return;
-  uint32_t p = pair_base + scan[i];
-  pair_vox[p] = vox[i];
-  first[vox[i]] = p;
-}
-
-__global__ void k_inc_pair(const uint32_t* __restrict__ vox, uint32_t n,
-                           const uint32_t* __restrict__ first, uint32_t* __restrict__ inc_pair) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  inc_pair[i] = first[vox[i]];
-}
-
-__global__ void k_reset_first(const uint32_t* __restrict__ pair_vox, uint32_t np, uint32_t* first) {
-  uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= np) return;
-  first[pair_vox[p]] = 0xFFFFFFFFu;
-}
-
-// sort keys: local pair id for incidences that receive a message, npairs
-// (sorted last) for Pre-only incidences
-__global__ void k_sort_keys(const RayMeta* __restrict__ meta, int nrays, uint32_t inc_base,
-                            const uint32_t* __restrict__ inc_pair, uint32_t pair_base,
-                            uint32_t npairs, uint32_t* __restrict__ keys,
-                            uint32_t* __restrict__ vals) {
-  int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= nrays) return;
-  RayMeta m = meta[r];
-  uint32_t o = m.off - inc_base;
-  for (int i = 0; i < m.n_pre; ++i) {
-    uint32_t k = o + (uint32_t)i;
-    keys[k] = i < m.n_post ? inc_pair[m.off + i] - pair_base : npairs;
-    vals[k] = k;
-  }
-}
-
-__global__ void k_seg_bounds(const uint32_t* __restrict__ skeys, uint32_t n, uint32_t npairs,
-                             uint32_t* __restrict__ seg) {
-  uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p > npairs) return;
-  uint32_t lo = 0, hi = n;
-  while (lo < hi) {
-    uint32_t mid = lo + ((hi - lo) >> 1);
-    if (skeys[mid] < p) lo = mid + 1;
-    else hi = mid;
-  }
-  seg[p] = lo;
-}
-
-// cumulative length per pair: fp32, summed in increasing incidence order
-// (the order the cumulative-length pass visits them, pixel-major)
-__global__ void k_pair_init(const uint32_t* __restrict__ seg_local,
-                            const uint32_t* __restrict__ perm_local, uint32_t inc_base,
-                            uint32_t npairs, const float* __restrict__ inc_len, uint32_t perm_base,
-                            uint32_t pair_base, uint32_t* __restrict__ seg, float* __restrict__ cum) {
-  uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p > npairs) return;
-  seg[pair_base + p] = perm_base + seg_local[p];
-  if (p == npairs) return;
-  float c = 0.0f;
-  for (uint32_t k = seg_local[p]; k < seg_local[p + 1]; ++k) c += inc_len[inc_base + perm_local[k]];
-  cum[pair_base + p] = c;
-}
-
-__global__ void k_perm_copy(const uint32_t* __restrict__ perm_local, uint32_t n, uint32_t inc_base,
-                            uint32_t* __restrict__ perm) {
+__global__ void k_pairs_from_sorted(const uint32_t* __restrict__ sk, const uint32_t* __restrict__ sidx,
+                                    const uint32_t* __restrict__ flag,
+                                    const uint32_t* __restrict__ scan, uint32_t n,
+                                    uint32_t pair_base, uint32_t perm_base, uint32_t inc_base,
+                                    uint32_t* __restrict__ pair_vox, uint32_t* __restrict__ seg,
+                                    uint32_t* __restrict__ skey, uint32_t* __restrict__ perm,
+                                    uint32_t* __restrict__ inc_pair) {
   uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
-  perm[k] = inc_base + perm_local[k];
+  uint32_t p = pair_base + scan[k] + flag[k] - 1;
+  if (flag[k]) {
+    pair_vox[p] = sk[k];
+    seg[p] = perm_base + k;
+  }
+  skey[perm_base + k] = p;
+  uint32_t i = inc_base + sidx[k];
+  perm[perm_base + k] = i;
+  inc_pair[i] = p;
+}
+
+// cumulative length of each pair: fp32, in increasing incidence order (the
+// order the reference's cumulative-length pass visits a voxel, pixel-major)
+__global__ void k_pair_cum(const uint32_t* __restrict__ seg, const uint32_t* __restrict__ sidx,
+                           uint32_t p0, uint32_t np, uint32_t perm_base, uint32_t inc_base,
+                           const float* __restrict__ post_len, float* __restrict__ cum) {
+  uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= np) return;
+  uint32_t p = p0 + q;
+  float c = 0.0f;
+  for (uint32_t k = seg[p]; k < seg[p + 1]; ++k) c += post_len[inc_base + sidx[k - perm_base]];
+  cum[p] = c;
 }
 
 __global__ void k_iota(uint32_t* out, uint32_t n) {
@@ -390,82 +354,41 @@ cudaError_t launch_set_points(const Geom& g, const float* pts, const float* occ,
 cudaError_t launch_trace_count(const Geom& g, const Pose& P, const float* depth, uint32_t* counts,
                                int* err, cudaStream_t s) {
   k_trace<false><<<grid_for((int64_t)g.rows * g.cols), kThreads, 0, s>>>(
-      g, P, depth, counts, nullptr, 0, nullptr, nullptr, nullptr, nullptr, err);
+      g, P, depth, counts, nullptr, 0, nullptr, nullptr, nullptr, nullptr, nullptr, err);
   return cudaGetLastError();
 }
 
 cudaError_t launch_trace_emit(const Geom& g, const Pose& P, const float* depth,
                               const uint32_t* pix_off, uint32_t inc_base, RayMeta* meta,
-                              uint32_t* inc_vox, float* inc_len, float* inc_mu, int* err,
-                              cudaStream_t s) {
+                              uint32_t* inc_vox, float* inc_len, float* inc_mu, float* post_len,
+                              int* err, cudaStream_t s) {
   k_trace<true><<<grid_for((int64_t)g.rows * g.cols), kThreads, 0, s>>>(
-      g, P, depth, nullptr, pix_off, inc_base, meta, inc_vox, inc_len, inc_mu, err);
+      g, P, depth, nullptr, pix_off, inc_base, meta, inc_vox, inc_len, inc_mu, post_len, err);
   return cudaGetLastError();
 }
 
-cudaError_t launch_first_touch(const uint32_t* inc_vox, uint32_t n, uint32_t* first, cudaStream_t s) {
+cudaError_t launch_vox_heads(const uint32_t* sk, uint32_t n, uint32_t* flag, cudaStream_t s) {
   if (!n) return cudaSuccess;
-  k_first_touch<<<grid_for(n), kThreads, 0, s>>>(inc_vox, n, first);
+  k_vox_heads<<<grid_for(n), kThreads, 0, s>>>(sk, n, flag);
   return cudaGetLastError();
 }
 
-cudaError_t launch_flag_first(const uint32_t* inc_vox, uint32_t n, const uint32_t* first,
-                              uint32_t* flag, cudaStream_t s) {
+cudaError_t launch_pairs_from_sorted(const uint32_t* sk, const uint32_t* sidx, const uint32_t* flag,
+                                     const uint32_t* scan, uint32_t n, uint32_t pair_base,
+                                     uint32_t perm_base, uint32_t inc_base, uint32_t* pair_vox,
+                                     uint32_t* seg, uint32_t* skey, uint32_t* perm,
+                                     uint32_t* inc_pair, cudaStream_t s) {
   if (!n) return cudaSuccess;
-  k_flag_first<<<grid_for(n), kThreads, 0, s>>>(inc_vox, n, first, flag);
+  k_pairs_from_sorted<<<grid_for(n), kThreads, 0, s>>>(sk, sidx, flag, scan, n, pair_base, perm_base,
+                                                       inc_base, pair_vox, seg, skey, perm, inc_pair);
   return cudaGetLastError();
 }
 
-cudaError_t launch_pair_assign(const uint32_t* inc_vox, uint32_t n, const uint32_t* flag,
-                               const uint32_t* scan, uint32_t pair_base, uint32_t* pair_vox,
-                               uint32_t* first, cudaStream_t s) {
-  if (!n) return cudaSuccess;
-  k_pair_assign<<<grid_for(n), kThreads, 0, s>>>(inc_vox, n, flag, scan, pair_base, pair_vox, first);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_inc_pair(const uint32_t* inc_vox, uint32_t n, const uint32_t* first,
-                            uint32_t* inc_pair, cudaStream_t s) {
-  if (!n) return cudaSuccess;
-  k_inc_pair<<<grid_for(n), kThreads, 0, s>>>(inc_vox, n, first, inc_pair);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_reset_first(const uint32_t* pair_vox, uint32_t npairs, uint32_t* first,
-                               cudaStream_t s) {
-  if (!npairs) return cudaSuccess;
-  k_reset_first<<<grid_for(npairs), kThreads, 0, s>>>(pair_vox, npairs, first);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_sort_keys(const RayMeta* meta, int nrays, uint32_t inc_base,
-                             const uint32_t* inc_pair, uint32_t pair_base, uint32_t npairs,
-                             uint32_t* keys, uint32_t* vals, cudaStream_t s) {
-  if (nrays <= 0) return cudaSuccess;
-  k_sort_keys<<<grid_for(nrays), kThreads, 0, s>>>(meta, nrays, inc_base, inc_pair, pair_base,
-                                                   npairs, keys, vals);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_seg_bounds(const uint32_t* skeys, uint32_t n, uint32_t npairs, uint32_t* seg,
-                              cudaStream_t s) {
-  k_seg_bounds<<<grid_for((int64_t)npairs + 1), kThreads, 0, s>>>(skeys, n, npairs, seg);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_pair_init2(const uint32_t* seg_local, const uint32_t* perm_local,
-                              uint32_t inc_base, uint32_t npairs, const float* inc_len,
-                              uint32_t perm_base, uint32_t pair_base, uint32_t* seg, float* cum,
-                              cudaStream_t s) {
-  k_pair_init<<<grid_for((int64_t)npairs + 1), kThreads, 0, s>>>(
-      seg_local, perm_local, inc_base, npairs, inc_len, perm_base, pair_base, seg, cum);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_perm_copy(const uint32_t* perm_local, uint32_t n, uint32_t inc_base,
-                             uint32_t* perm, cudaStream_t s) {
-  if (!n) return cudaSuccess;
-  k_perm_copy<<<grid_for(n), kThreads, 0, s>>>(perm_local, n, inc_base, perm);
+cudaError_t launch_pair_cum(const uint32_t* seg, const uint32_t* sidx, uint32_t p0, uint32_t np,
+                            uint32_t perm_base, uint32_t inc_base, const float* post_len, float* cum,
+                            cudaStream_t s) {
+  if (!np) return cudaSuccess;
+  k_pair_cum<<<grid_for(np), kThreads, 0, s>>>(seg, sidx, p0, np, perm_base, inc_base, post_len, cum);
   return cudaGetLastError();
 }
 

@@ -6,11 +6,13 @@
 //   voxel state    fp32 L, fp32 belief        [slots*512], slot-major,
 //                                              voxel (x*8+y)*8+z in a slot
 //   rays           RayMeta [views*rows*cols]  pixel-major per view
-//   incidences     u32 pair, fp32 len, fp32 mu, fp32 p*len   [N_inc]
-//                  ray order (pixel-major, then along the ray)
-//   pairs          u32 voxel, fp32 m, fp32 cum_len, float2 (q, ln q),
-//                  fp32 dm, u32 seg   [N_cv], first-touch order per view
-//   perm           u32 [N_post] incidence ids grouped by pair (CSR)
+//   incidences     u32 pair, fp32 len, fp32 mu, fp32 p*l   [N_inc]
+//                  ray order (pixel-major, then along the ray), each ray
+//                  padded to a multiple of 4
+//   pairs          u32 voxel, fp32 m, fp32 cum_len, fp32 ln q, fp32 dm,
+//                  u32 seg   [N_cv], voxel order per view
+//   grouped        u32 incidence and u32 pair id per pair-grouped position
+//                  [N_pre] (the voxel-sorted permutation, CSR by pair)
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -84,7 +86,6 @@ struct View {
   uint32_t inc_base = 0, n_inc = 0;
   uint32_t pair_base = 0, n_pairs = 0;
   uint32_t perm_base = 0, n_perm = 0;
-  uint32_t long_base = 0, n_long = 0;  // pairs with long segments
 };
 
 uint32_t u32_checked(int64_t v, const char* what) {
@@ -109,17 +110,15 @@ struct mrf_map {
   std::vector<View> views;
   // arenas
   DBuf meta, inc_pair, inc_len, inc_mu, inc_pl, pair_vox, pair_m, pair_cum, pair_q, pair_dm,
-      pair_seg, perm, long_list;
-  int64_t n_long = 0;
+      pair_seg, perm, skey, carry, pair_acc;
   int64_t n_inc = 0, n_pairs = 0, n_perm = 0;
   // jacobi voxel CSR
   DBuf vseg, vpairs, vvox;
   uint32_t n_vvox = 0;
   int jacobi_version = -1;
   // scratch
-  DBuf s_first, s_flags, s_ind, s_scan, s_tmp, s_counts, s_offs, s_vox, s_k0, s_k1, s_v0, s_v1,
+  DBuf s_postlen, s_flags, s_ind, s_scan, s_tmp, s_counts, s_offs, s_vox, s_k0, s_k1, s_v0, s_v1,
       s_seg, s_dense, s_err, s_depth_in, s_depth, s_img, s_part, s_sum;
-  int64_t first_cap_vox = 0;
   mrf_stats stats{};
   // MRF_PROFILE event pool
   std::vector<cudaEvent_t> prof_ev;
@@ -135,10 +134,12 @@ struct mrf_map {
     a.pair_vox = pair_vox.as<uint32_t>();
     a.pair_m = pair_m.as<float>();
     a.pair_cum = pair_cum.as<float>();
-    a.pair_q = pair_q.as<float2>();
+    a.pair_lnq = pair_q.as<float>();
     a.pair_dm = pair_dm.as<float>();
+    a.pair_acc = pair_acc.as<float>();
     a.pair_seg = pair_seg.as<uint32_t>();
     a.perm = perm.as<uint32_t>();
+    a.skey = skey.as<uint32_t>();
     a.L = d_L.as<float>();
     a.belief = d_belief.as<float>();
     return a;
@@ -162,16 +163,7 @@ void check_device_err(mrf_map* m) {
   int e = read1(m, m->s_err.as<int>());
   if (e) {
     CK(cudaMemsetAsync(m->s_err.p, 0, sizeof(int), m->stream));
-    fail(MRF_ERR_DEVICE, "a kernel raised its error flag (ray longer than 65535 incidences)");
-  }
-}
-
-void ensure_first(mrf_map* m) {
-  int64_t nv = m->n_bricks * kBrickVox;
-  if (nv > m->first_cap_vox) {
-    m->s_first.reserve((size_t)nv * 4, false, m->stream);
-    m->first_cap_vox = (int64_t)(m->s_first.cap / 4);
-    CK(cudaMemsetAsync(m->s_first.p, 0xFF, m->s_first.cap, m->stream));
+    fail(MRF_ERR_DEVICE, "a kernel raised its error flag (ray longer than 65532 incidences)");
   }
 }
 
@@ -266,9 +258,11 @@ void rebuild(mrf_map* m) {
   m->inc_pair.reserve(ib, false, m->stream);
   m->inc_len.reserve(ib, false, m->stream);
   m->inc_mu.reserve(ib, false, m->stream);
-  m->inc_pl.reserve(ib, false, m->stream);
   m->perm.reserve(ib, false, m->stream);
+  m->inc_pl.reserve(ib, false, m->stream);
+  m->skey.reserve(ib, false, m->stream);
   m->s_vox.reserve(ib, false, m->stream);
+  m->s_postlen.reserve(ib, false, m->stream);
   // 3. emit
   for (int c = 0; c < V; ++c) {
     View& v = m->views[c];
@@ -276,66 +270,77 @@ void rebuild(mrf_map* m) {
     v.n_inc = bounds[c + 1] - bounds[c];
     CK(launch_trace_emit(m->g, v.pose, v.depth.as<float>(), m->s_offs.as<uint32_t>() + c * HW, 0,
                          m->meta.as<RayMeta>() + c * HW, m->s_vox.as<uint32_t>(),
-                         m->inc_len.as<float>(), m->inc_mu.as<float>(), m->s_err.as<int>(),
-                         m->stream));
+                         m->inc_len.as<float>(), m->inc_mu.as<float>(), m->s_postlen.as<float>(),
+                         m->s_err.as<int>(), m->stream));
   }
-  // 4. pairs per view (first-touch order) and the pair-grouped CSR
-  ensure_first(m);
+  // per-view counters from the ray records
+  std::vector<RayMeta> hm((size_t)npix);
+  std::vector<int64_t> nreal(V, 0);
+  int64_t nrays = 0, npost = 0, npre = 0;
+  if (npix) {
+    CK(cudaMemcpyAsync(hm.data(), m->meta.p, (size_t)npix * sizeof(RayMeta), cudaMemcpyDeviceToHost,
+                       m->stream));
+    sync(m);
+    check_device_err(m);
+    for (int c = 0; c < V; ++c)
+      for (int64_t i = 0; i < HW; ++i) {
+        const RayMeta& r = hm[(size_t)(c * HW + i)];
+        nreal[c] += r.n_pre;
+        nrays += r.n_pre > 0;
+        npost += r.n_post;
+      }
+    for (int c = 0; c < V; ++c) npre += nreal[c];
+  }
+  // 4. pairs per view in voxel order: sort the view's incidences by voxel
+  //    (stable), one pair per run; pos[i] = pair-grouped position of i
+  int bits = 1;
+  while (bits < 32 && ((uint64_t)1 << bits) <= (uint64_t)(m->n_bricks * kBrickVox)) ++bits;
   int64_t pair_total = 0, perm_total = 0;
   for (int c = 0; c < V; ++c) {
     View& v = m->views[c];
     uint32_t n = v.n_inc;
+    uint32_t nr = (uint32_t)nreal[c];
     v.pair_base = (uint32_t)pair_total;
     v.perm_base = (uint32_t)perm_total;
     v.n_pairs = 0;
     v.n_perm = 0;
-    if (n == 0) continue;
-    const uint32_t* vox = m->s_vox.as<uint32_t>() + v.inc_base;
+    if (nr == 0) continue;
     m->s_k0.reserve((size_t)n * 4 + 4, false, m->stream);
     m->s_k1.reserve((size_t)n * 4 + 4, false, m->stream);
     m->s_v0.reserve((size_t)n * 4 + 4, false, m->stream);
     m->s_v1.reserve((size_t)n * 4 + 4, false, m->stream);
-    CK(launch_first_touch(vox, n, m->s_first.as<uint32_t>(), m->stream));
-    CK(launch_flag_first(vox, n, m->s_first.as<uint32_t>(), m->s_k0.as<uint32_t>(), m->stream));
-    CK(cudaMemsetAsync(m->s_k0.as<uint32_t>() + n, 0, 4, m->stream));
-    size_t t1 = scan_temp_bytes(n + 1);
+    CK(launch_iota(m->s_v0.as<uint32_t>(), n, m->stream));
+    size_t t2 = sort_temp_bytes(n, bits);
+    m->s_tmp.reserve(t2, false, m->stream);
+    // padding incidences carry kNoVoxel, whose low bits exceed every voxel id
+    CK(sort_pairs_u32(m->s_tmp.p, t2, m->s_vox.as<uint32_t>() + v.inc_base, m->s_k1.as<uint32_t>(),
+                      m->s_v0.as<uint32_t>(), m->s_v1.as<uint32_t>(), n, bits, m->stream));
+    CK(launch_vox_heads(m->s_k1.as<uint32_t>(), nr, m->s_k0.as<uint32_t>(), m->stream));
+    CK(cudaMemsetAsync(m->s_k0.as<uint32_t>() + nr, 0, 4, m->stream));
+    size_t t1 = scan_temp_bytes(nr + 1);
     m->s_tmp.reserve(t1, false, m->stream);
-    CK(exclusive_scan_u32(m->s_tmp.p, t1, m->s_k0.as<uint32_t>(), m->s_k1.as<uint32_t>(), n + 1,
+    CK(exclusive_scan_u32(m->s_tmp.p, t1, m->s_k0.as<uint32_t>(), m->s_v0.as<uint32_t>(), nr + 1,
                           m->stream));
-    uint32_t np = read1(m, m->s_k1.as<uint32_t>() + n);
+    uint32_t np = read1(m, m->s_v0.as<uint32_t>() + nr);
     u32_checked(pair_total + np + 1, "pair count");
     size_t pb = (size_t)(pair_total + np + 1);
     m->pair_vox.reserve(pb * 4, true, m->stream);
     m->pair_m.reserve(pb * 4, true, m->stream);
     m->pair_cum.reserve(pb * 4, true, m->stream);
     m->pair_seg.reserve(pb * 4, true, m->stream);
-    CK(launch_pair_assign(vox, n, m->s_k0.as<uint32_t>(), m->s_k1.as<uint32_t>(), v.pair_base,
-                          m->pair_vox.as<uint32_t>(), m->s_first.as<uint32_t>(), m->stream));
-    CK(launch_inc_pair(vox, n, m->s_first.as<uint32_t>(), m->inc_pair.as<uint32_t>() + v.inc_base,
+    CK(launch_pairs_from_sorted(m->s_k1.as<uint32_t>(), m->s_v1.as<uint32_t>(), m->s_k0.as<uint32_t>(),
+                                m->s_v0.as<uint32_t>(), nr, v.pair_base, v.perm_base, v.inc_base,
+                                m->pair_vox.as<uint32_t>(), m->pair_seg.as<uint32_t>(),
+                                m->skey.as<uint32_t>(), m->perm.as<uint32_t>(),
+                                m->inc_pair.as<uint32_t>(), m->stream));
+    CK(launch_fill_u32(m->pair_seg.as<uint32_t>() + v.pair_base + np, 1, v.perm_base + nr, m->stream));
+    CK(launch_pair_cum(m->pair_seg.as<uint32_t>(), m->s_v1.as<uint32_t>(), v.pair_base, np,
+                       v.perm_base, v.inc_base, m->s_postlen.as<float>(), m->pair_cum.as<float>(),
                        m->stream));
-    CK(launch_reset_first(m->pair_vox.as<uint32_t>() + v.pair_base, np, m->s_first.as<uint32_t>(),
-                          m->stream));
-    CK(launch_sort_keys(m->meta.as<RayMeta>() + c * HW, (int)HW, v.inc_base,
-                        m->inc_pair.as<uint32_t>(), v.pair_base, np, m->s_k0.as<uint32_t>(),
-                        m->s_v0.as<uint32_t>(), m->stream));
-    int bits = 1;
-    while (bits < 32 && ((uint64_t)1 << bits) <= (uint64_t)np) ++bits;
-    size_t t2 = sort_temp_bytes(n, bits);
-    m->s_tmp.reserve(t2, false, m->stream);
-    CK(sort_pairs_u32(m->s_tmp.p, t2, m->s_k0.as<uint32_t>(), m->s_k1.as<uint32_t>(),
-                      m->s_v0.as<uint32_t>(), m->s_v1.as<uint32_t>(), n, bits, m->stream));
-    m->s_seg.reserve((size_t)(np + 1) * 4, false, m->stream);
-    CK(launch_seg_bounds(m->s_k1.as<uint32_t>(), n, np, m->s_seg.as<uint32_t>(), m->stream));
-    uint32_t nvalid = read1(m, m->s_seg.as<uint32_t>() + np);
-    CK(launch_perm_copy(m->s_v1.as<uint32_t>(), nvalid, v.inc_base,
-                        m->perm.as<uint32_t>() + v.perm_base, m->stream));
-    CK(launch_pair_init2(m->s_seg.as<uint32_t>(), m->s_v1.as<uint32_t>(), v.inc_base, np,
-                         m->inc_len.as<float>(), v.perm_base, v.pair_base,
-                         m->pair_seg.as<uint32_t>(), m->pair_cum.as<float>(), m->stream));
     v.n_pairs = np;
-    v.n_perm = nvalid;
+    v.n_perm = nr;
     pair_total += np;
-    perm_total += nvalid;
+    perm_total += nr;
   }
   m->n_inc = n_inc;
   m->n_pairs = pair_total;
@@ -345,38 +350,16 @@ void rebuild(mrf_map* m) {
   m->pair_m.reserve(pb * 4, true, m->stream);
   m->pair_cum.reserve(pb * 4, true, m->stream);
   m->pair_seg.reserve(pb * 4, true, m->stream);
-  m->pair_q.reserve(pb * 8, false, m->stream);
+  m->pair_q.reserve(pb * 4, false, m->stream);
   m->pair_dm.reserve(pb * 4, false, m->stream);
+  m->pair_acc.reserve(pb * 4, false, m->stream);
   CK(launch_fill_f32(m->pair_m.as<float>(), pair_total, 0.0f, m->stream));
-  // 5. per view, the pairs whose segments are long enough to need a warp
   {
-    int64_t long_total = 0;
-    for (int c = 0; c < V; ++c) {
-      View& v = m->views[c];
-      v.long_base = (uint32_t)long_total;
-      v.n_long = 0;
-      if (!v.n_pairs) continue;
-      uint32_t np = v.n_pairs;
-      m->s_k0.reserve((size_t)np * 4 + 4, false, m->stream);
-      m->s_k1.reserve((size_t)np * 4 + 4, false, m->stream);
-      CK(launch_long_flag(m->pair_seg.as<uint32_t>(), v.pair_base, v.pair_base + np,
-                          m->s_k0.as<uint32_t>(), m->stream));
-      CK(cudaMemsetAsync(m->s_k0.as<uint32_t>() + np, 0, 4, m->stream));
-      size_t t = scan_temp_bytes(np + 1);
-      m->s_tmp.reserve(t, false, m->stream);
-      CK(exclusive_scan_u32(m->s_tmp.p, t, m->s_k0.as<uint32_t>(), m->s_k1.as<uint32_t>(), np + 1,
-                            m->stream));
-      uint32_t nl = read1(m, m->s_k1.as<uint32_t>() + np);
-      m->long_list.reserve((size_t)(long_total + nl + 1) * 4, true, m->stream);
-      CK(launch_long_scatter(m->s_k0.as<uint32_t>(), m->s_k1.as<uint32_t>(), v.pair_base, np,
-                             m->long_list.as<uint32_t>() + long_total, m->stream));
-      v.n_long = nl;
-      long_total += nl;
-    }
-    m->n_long = long_total;
-    m->long_list.reserve((size_t)(long_total + 1) * 4, true, m->stream);
+    // tile carries of the pair update: enough for any view or all of them
+    int64_t tiles = (int64_t)pair_update_tiles((uint32_t)std::min<int64_t>(perm_total, 0xFFFFFFF0ll)) + V + 1;
+    m->carry.reserve((size_t)tiles * sizeof(TileCarry), false, m->stream);
   }
-  // 6. carry messages of every camera over to its new pairs
+  // 5. carry messages of every camera over to its new pairs
   if (remap) {
     int64_t nv = m->n_bricks * kBrickVox;
     m->s_dense.reserve((size_t)nv * 4, false, m->stream);
@@ -404,21 +387,8 @@ void rebuild(mrf_map* m) {
   m->stats.build_ms = ms;
   m->built_version = m->version;
   m->jacobi_version = -1;
-  // counters
-  std::vector<RayMeta> hm;
-  int64_t nrays = 0, npost = 0;
-  if (npix) {
-    hm.resize((size_t)npix);
-    CK(cudaMemcpyAsync(hm.data(), m->meta.p, (size_t)npix * sizeof(RayMeta), cudaMemcpyDeviceToHost,
-                       m->stream));
-    sync(m);
-    for (const auto& r : hm) {
-      nrays += r.n_pre > 0;
-      npost += r.n_post;
-    }
-  }
   m->stats.n_rays = nrays;
-  m->stats.n_inc_pre = n_inc;
+  m->stats.n_inc_pre = npre;
   m->stats.n_inc_post = npost;
   m->stats.n_pairs = pair_total;
 }
@@ -527,32 +497,29 @@ void run_infer(mrf_map* m, const int* ids, int n_ids, int iters, int flags) {
         const View& v = m->views[c];
         if (v.n_inc == 0) continue;
         prof.begin(0);
-        CK(launch_pair_prepare(a, v.pair_base, v.pair_base + v.n_pairs, m->stream));
+        CK(launch_pair_prepare(a, v.pair_base, v.pair_base + v.n_pairs, 0, m->stream));
         prof.end();
         prof.begin(1);
         CK(launch_ray_bp(a, (uint32_t)(c * HW), (uint32_t)((c + 1) * HW), fix, m->num_sms, m->stream));
         prof.end();
         prof.begin(2);
-        CK(launch_pair_update(a, v.pair_base, v.pair_base + v.n_pairs, 0, m->stream));
-        CK(launch_pair_update_long(a, m->long_list.as<uint32_t>() + v.long_base, v.n_long, 0,
-                                   m->num_sms, m->stream));
+        CK(launch_pair_update(a, v.perm_base, v.perm_base + v.n_perm, v.pair_base,
+                              v.pair_base + v.n_pairs, m->carry.as<TileCarry>(), 0, m->stream));
         prof.end();
-        launches += v.n_long ? 4 : 3;
+        launches += 5;
       }
     } else {
       uint32_t P = (uint32_t)m->n_pairs;
       prof.begin(0);
-      CK(launch_pair_prepare(a, 0, P, m->stream));
+      CK(launch_pair_prepare(a, 0, P, 1, m->stream));
       prof.end();
       prof.begin(1);
       CK(launch_ray_bp(a, 0, (uint32_t)(V * HW), fix, m->num_sms, m->stream));
       prof.end();
       prof.begin(2);
-      CK(launch_pair_update(a, 0, P, 1, m->stream));
-      CK(launch_pair_update_long(a, m->long_list.as<uint32_t>(), (uint32_t)m->n_long, 1, m->num_sms,
-                                 m->stream));
+      CK(launch_pair_update(a, 0, (uint32_t)m->n_perm, 0, P, m->carry.as<TileCarry>(), 1, m->stream));
       prof.end();
-      launches += m->n_long ? 1 : 0;
+      launches += 2;
       prof.begin(3);
       CK(launch_voxel_apply(m->vseg.as<uint32_t>(), m->vpairs.as<uint32_t>(), m->vvox.as<uint32_t>(),
                             m->n_vvox, m->pair_dm.as<float>(), m->d_L.as<float>(),
@@ -630,8 +597,8 @@ void destroy_bufs(mrf_map* m) {
   DBuf* all[] = {&m->d_sigma, &m->d_bias, &m->d_slot, &m->d_coord, &m->d_L, &m->d_belief,
                  &m->meta, &m->inc_pair, &m->inc_len, &m->inc_mu, &m->inc_pl, &m->pair_vox,
                  &m->pair_m, &m->pair_cum, &m->pair_q, &m->pair_dm, &m->pair_seg, &m->perm,
-                 &m->long_list,
-                 &m->vseg, &m->vpairs, &m->vvox, &m->s_first, &m->s_flags, &m->s_ind, &m->s_scan,
+                 &m->skey, &m->carry, &m->pair_acc,
+                 &m->vseg, &m->vpairs, &m->vvox, &m->s_postlen, &m->s_flags, &m->s_ind, &m->s_scan,
                  &m->s_tmp, &m->s_counts, &m->s_offs, &m->s_vox, &m->s_k0, &m->s_k1, &m->s_v0,
                  &m->s_v1, &m->s_seg, &m->s_dense, &m->s_err, &m->s_depth_in, &m->s_depth,
                  &m->s_img, &m->s_part, &m->s_sum};
@@ -1027,13 +994,14 @@ mrf_status mrf_view_incidences(mrf_map* m, int view_id, int* meta, uint32_t* vox
     ensure_built(m);
     const View& v = m->views[view_id];
     const int64_t HW = m->hw();
-    if (n_inc) *n_inc = v.n_inc;
-    if (meta) {
-      std::vector<RayMeta> hm((size_t)HW);
-      CK(cudaMemcpyAsync(hm.data(), m->meta.as<RayMeta>() + view_id * HW, (size_t)HW * sizeof(RayMeta),
-                         cudaMemcpyDeviceToHost, m->stream));
-      sync(m);
-      for (int64_t i = 0; i < HW; ++i) {
+    std::vector<RayMeta> hm((size_t)HW);
+    CK(cudaMemcpyAsync(hm.data(), m->meta.as<RayMeta>() + view_id * HW, (size_t)HW * sizeof(RayMeta),
+                       cudaMemcpyDeviceToHost, m->stream));
+    sync(m);
+    int64_t total = 0;
+    for (int64_t i = 0; i < HW; ++i) {
+      total += hm[i].n_pre;
+      if (meta) {
         meta[i * 5 + 0] = hm[i].n_pre;
         meta[i * 5 + 1] = hm[i].n_post;
         meta[i * 5 + 2] = hm[i].r0;
@@ -1041,23 +1009,30 @@ mrf_status mrf_view_incidences(mrf_map* m, int view_id, int* meta, uint32_t* vox
         meta[i * 5 + 4] = (int)(hm[i].flags & 1u);
       }
     }
-    int64_t n = std::min<int64_t>(cap, v.n_inc);
-    if (n <= 0) return;
-    if (len) CK(cudaMemcpyAsync(len, m->inc_len.as<float>() + v.inc_base, (size_t)n * 4,
-                                cudaMemcpyDeviceToHost, m->stream));
-    if (mu) CK(cudaMemcpyAsync(mu, m->inc_mu.as<float>() + v.inc_base, (size_t)n * 4,
-                               cudaMemcpyDeviceToHost, m->stream));
-    if (vox) {
-      std::vector<uint32_t> ip((size_t)n), pv((size_t)v.n_pairs);
-      CK(cudaMemcpyAsync(ip.data(), m->inc_pair.as<uint32_t>() + v.inc_base, (size_t)n * 4,
+    if (n_inc) *n_inc = total;
+    if (cap <= 0 || v.n_inc == 0 || (!len && !mu && !vox)) return;
+    // device lists are padded per ray: copy the view's range, then compact
+    std::vector<float> hl(v.n_inc), hmu(v.n_inc);
+    std::vector<uint32_t> ip(v.n_inc), pv(v.n_pairs);
+    CK(cudaMemcpyAsync(hl.data(), m->inc_len.as<float>() + v.inc_base, (size_t)v.n_inc * 4,
+                       cudaMemcpyDeviceToHost, m->stream));
+    CK(cudaMemcpyAsync(hmu.data(), m->inc_mu.as<float>() + v.inc_base, (size_t)v.n_inc * 4,
+                       cudaMemcpyDeviceToHost, m->stream));
+    CK(cudaMemcpyAsync(ip.data(), m->inc_pair.as<uint32_t>() + v.inc_base, (size_t)v.n_inc * 4,
+                       cudaMemcpyDeviceToHost, m->stream));
+    if (v.n_pairs)
+      CK(cudaMemcpyAsync(pv.data(), m->pair_vox.as<uint32_t>() + v.pair_base, (size_t)v.n_pairs * 4,
                          cudaMemcpyDeviceToHost, m->stream));
-      if (v.n_pairs)
-        CK(cudaMemcpyAsync(pv.data(), m->pair_vox.as<uint32_t>() + v.pair_base, (size_t)v.n_pairs * 4,
-                           cudaMemcpyDeviceToHost, m->stream));
-      sync(m);
-      for (int64_t i = 0; i < n; ++i) vox[i] = pv[ip[i] - v.pair_base];
-    }
     sync(m);
+    int64_t k = 0;
+    for (int64_t i = 0; i < HW && k < cap; ++i) {
+      int64_t o = (int64_t)hm[i].off - v.inc_base;
+      for (int j = 0; j < hm[i].n_pre && k < cap; ++j, ++k) {
+        if (len) len[k] = hl[o + j];
+        if (mu) mu[k] = hmu[o + j];
+        if (vox) vox[k] = pv[ip[o + j] - v.pair_base];
+      }
+    }
   });
 }
 

@@ -50,7 +50,8 @@ struct RayMeta {
 };
 static_assert(sizeof(RayMeta) == 16, "RayMeta layout");
 
-constexpr int kMaxRayLen = 65535;
+constexpr int kMaxRayLen = 65532;        // n_pre fits uint16 after padding to 4
+constexpr uint32_t kNoVoxel = 0xFFFFFFFFu;  // padding incidences
 
 // ---- launchers (stream-ordered; return cudaError_t of the launch) --------
 cudaError_t launch_clean_depth(const float* in, float* out, int rows, int cols, cudaStream_t s);
@@ -72,30 +73,18 @@ cudaError_t launch_trace_count(const Geom& g, const Pose& P, const float* depth,
                                int* err, cudaStream_t s);
 cudaError_t launch_trace_emit(const Geom& g, const Pose& P, const float* depth,
                               const uint32_t* pix_off, uint32_t inc_base, RayMeta* meta,
-                              uint32_t* inc_vox, float* inc_len, float* inc_mu, int* err,
-                              cudaStream_t s);
-// pairs (first-touch order) and the voxel-sorted CSR
-cudaError_t launch_first_touch(const uint32_t* inc_vox, uint32_t n, uint32_t* first, cudaStream_t s);
-cudaError_t launch_flag_first(const uint32_t* inc_vox, uint32_t n, const uint32_t* first,
-                              uint32_t* flag, cudaStream_t s);
-cudaError_t launch_pair_assign(const uint32_t* inc_vox, uint32_t n, const uint32_t* flag,
-                               const uint32_t* scan, uint32_t pair_base, uint32_t* pair_vox,
-                               uint32_t* first, cudaStream_t s);
-cudaError_t launch_inc_pair(const uint32_t* inc_vox, uint32_t n, const uint32_t* first,
-                            uint32_t* inc_pair, cudaStream_t s);
-cudaError_t launch_reset_first(const uint32_t* pair_vox, uint32_t npairs, uint32_t* first,
-                               cudaStream_t s);
-cudaError_t launch_sort_keys(const RayMeta* meta, int nrays, uint32_t inc_base,
-                             const uint32_t* inc_pair, uint32_t pair_base, uint32_t npairs,
-                             uint32_t* keys, uint32_t* vals, cudaStream_t s);
-cudaError_t launch_seg_bounds(const uint32_t* skeys, uint32_t n, uint32_t npairs, uint32_t* seg,
-                              cudaStream_t s);
-cudaError_t launch_pair_init2(const uint32_t* seg_local, const uint32_t* perm_local,
-                              uint32_t inc_base, uint32_t npairs, const float* inc_len,
-                              uint32_t perm_base, uint32_t pair_base, uint32_t* seg, float* cum,
-                              cudaStream_t s);
-cudaError_t launch_perm_copy(const uint32_t* perm_local, uint32_t n, uint32_t inc_base,
-                             uint32_t* perm, cudaStream_t s);
+                              uint32_t* inc_vox, float* inc_len, float* inc_mu, float* post_len,
+                              int* err, cudaStream_t s);
+// pairs in voxel order and the pair-grouped positions
+cudaError_t launch_vox_heads(const uint32_t* sk, uint32_t n, uint32_t* flag, cudaStream_t s);
+cudaError_t launch_pairs_from_sorted(const uint32_t* sk, const uint32_t* sidx, const uint32_t* flag,
+                                     const uint32_t* scan, uint32_t n, uint32_t pair_base,
+                                     uint32_t perm_base, uint32_t inc_base, uint32_t* pair_vox,
+                                     uint32_t* seg, uint32_t* skey, uint32_t* perm,
+                                     uint32_t* inc_pair, cudaStream_t s);
+cudaError_t launch_pair_cum(const uint32_t* seg, const uint32_t* sidx, uint32_t p0, uint32_t np,
+                            uint32_t perm_base, uint32_t inc_base, const float* post_len, float* cum,
+                            cudaStream_t s);
 cudaError_t launch_iota(uint32_t* out, uint32_t n, cudaStream_t s);
 // CUB helpers (scratch-managed by the caller)
 size_t scan_temp_bytes(uint32_t n);
@@ -114,28 +103,33 @@ struct BpArrays {
   const uint32_t* inc_pair;
   const float* inc_len;
   const float* inc_mu;
-  float* inc_pl;
+  float* inc_pl;           // p*l per incidence, ray order
+  const uint32_t* perm;    // incidence at each pair-grouped position
   const uint32_t* pair_vox;
   float* pair_m;
   const float* pair_cum;
-  float2* pair_q;
+  float* pair_lnq;
   float* pair_dm;
+  float* pair_acc;         // sum of p*l per pair (pair update scratch)
   const uint32_t* pair_seg;
-  const uint32_t* perm;
+  const uint32_t* skey;  // pair id of each pair-grouped position
   float* L;
   float* belief;
 };
-cudaError_t launch_pair_prepare(const BpArrays& a, uint32_t p0, uint32_t p1, cudaStream_t s);
+// per-tile partial sums of the pair-update segmented reduction
+struct TileCarry {
+  uint32_t first_key, last_key;
+  float first_sum, last_sum;
+  uint32_t flags;
+};
+uint32_t pair_update_tiles(uint32_t n);
+cudaError_t launch_pair_prepare(const BpArrays& a, uint32_t p0, uint32_t p1, int jacobi,
+                                cudaStream_t s);
 cudaError_t launch_ray_bp(const BpArrays& a, uint32_t r0, uint32_t r1, int fix_reset, int num_sms,
                           cudaStream_t s);
-cudaError_t launch_pair_update(const BpArrays& a, uint32_t p0, uint32_t p1, int jacobi,
-                               cudaStream_t s);
-cudaError_t launch_pair_update_long(const BpArrays& a, const uint32_t* list, uint32_t n, int jacobi,
-                                    int num_sms, cudaStream_t s);
-cudaError_t launch_long_flag(const uint32_t* seg, uint32_t p0, uint32_t p1, uint32_t* flag,
-                             cudaStream_t s);
-cudaError_t launch_long_scatter(const uint32_t* flag, const uint32_t* scan, uint32_t p0, uint32_t n,
-                                uint32_t* list, cudaStream_t s);
+// k0..k1: range of sorted (pair-grouped) positions
+cudaError_t launch_pair_update(const BpArrays& a, uint32_t k0, uint32_t k1, uint32_t p0, uint32_t p1,
+                               TileCarry* carry, int jacobi, cudaStream_t s);
 cudaError_t launch_voxel_apply(const uint32_t* vseg, const uint32_t* vpairs, const uint32_t* vvox,
                                uint32_t nvox, const float* pair_dm, float* L, float* belief,
                                cudaStream_t s);
@@ -145,6 +139,7 @@ cudaError_t launch_remap_scatter(const uint32_t* pair_vox, const float* pair_m, 
 cudaError_t launch_remap_gather(const uint32_t* pair_vox, float* pair_m, uint32_t n,
                                 const float* dense, cudaStream_t s);
 cudaError_t launch_fill_f32(float* p, int64_t n, float v, cudaStream_t s);
+cudaError_t launch_fill_u32(uint32_t* p, int64_t n, uint32_t v, cudaStream_t s);
 cudaError_t launch_vflag(const uint32_t* sk, uint32_t n, uint32_t* flag, cudaStream_t s);
 cudaError_t launch_vassign(const uint32_t* sk, const uint32_t* flag, const uint32_t* scan,
                            uint32_t n, uint32_t* vvox, uint32_t* vseg, cudaStream_t s);
