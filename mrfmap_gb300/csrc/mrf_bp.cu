@@ -242,8 +242,14 @@ __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, Stage& st,
   if (kStaged) __syncwarp();
 }
 
+// Persistent launch: each warp takes the next ray from a work counter; rays
+// are queued longest first (sorted once per incidence build), so the long
+// rays start early and the short ones fill the tail.  Which warp handles a
+// ray does not change its result.
 __global__ void __launch_bounds__(kRayWarps * 32) k_ray_bp(const RayMeta* __restrict__ meta,
-                                                           uint32_t r0, uint32_t r1,
+                                                           const uint32_t* __restrict__ order,
+                                                           uint32_t n_rays,
+                                                           uint32_t* __restrict__ counter,
                                                            const uint32_t* __restrict__ inc_pair,
                                                            const float* __restrict__ inc_len,
                                                            const float* __restrict__ inc_mu,
@@ -254,14 +260,27 @@ __global__ void __launch_bounds__(kRayWarps * 32) k_ray_bp(const RayMeta* __rest
   const int lane = threadIdx.x & 31;
   const int wid = threadIdx.x >> 5;
   Stage& st = stage_all[wid];
-  for (uint32_t r = r0 + blockIdx.x * kRayWarps + wid; r < r1; r += gridDim.x * kRayWarps) {
-    RayMeta me = meta[r];
-    if (me.n_pre == 0) continue;
+  for (;;) {
+    uint32_t idx = 0;
+    if (lane == 0) idx = atomicAdd(counter, 1u);
+    idx = __shfl_sync(kFull, idx, 0);
+    if (idx >= n_rays) break;
+    RayMeta me = meta[order[idx]];
     if (me.n_pre <= kStage)
       ray_bp_warp<true, float>(me, st, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
     else
       ray_bp_warp<false, double>(me, st, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
   }
+}
+
+// ray queue of one build: active rays sorted by decreasing length
+__global__ void k_ray_keys(const RayMeta* __restrict__ meta, uint32_t n, uint32_t* __restrict__ keys,
+                           uint32_t* __restrict__ vals) {
+  uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  uint32_t len = meta[r].n_pre;
+  keys[r] = len ? 0xFFFFu - len : 0x10000u;  // empty rays sort last
+  vals[r] = r;
 }
 
 // Pair update: a load-balanced segmented reduction over the pair-grouped
@@ -476,6 +495,11 @@ __global__ void k_remap_gather(const uint32_t* __restrict__ pv, float* __restric
   if (p < n) m[p] = dense[pv[p]];
 }
 
+__global__ void k_add_u32(uint32_t* p, uint32_t n, uint32_t v) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] += v;
+}
+
 __global__ void k_fill_u32(uint32_t* p, int64_t n, uint32_t v) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) p[i] = v;
@@ -519,13 +543,28 @@ cudaError_t launch_pair_prepare(const BpArrays& a, uint32_t p0, uint32_t p1, int
 }
 
 
-cudaError_t launch_ray_bp(const BpArrays& a, uint32_t r0, uint32_t r1, int fix_reset, int num_sms,
-                          cudaStream_t s) {
-  if (r1 <= r0) return cudaSuccess;
-  int64_t warps = r1 - r0;
-  int64_t b = std::min<int64_t>(blocks(warps, kRayWarps), (int64_t)num_sms * 8);
-  k_ray_bp<<<(unsigned)b, kRayWarps * 32, 0, s>>>(a.meta, r0, r1, a.inc_pair, a.inc_len, a.inc_mu,
-                                                  a.pair_lnq, a.inc_pl, fix_reset);
+cudaError_t launch_ray_bp(const BpArrays& a, const uint32_t* order, uint32_t n_rays,
+                          uint32_t* counter, int fix_reset, int num_sms, cudaStream_t s) {
+  if (!n_rays) return cudaSuccess;
+  static int resident = 0;
+  if (!resident) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ray_bp, kRayWarps * 32, 0) !=
+            cudaSuccess ||
+        per_sm < 1)
+      per_sm = 1;
+    resident = per_sm;
+  }
+  int64_t b = std::min<int64_t>((int64_t)num_sms * resident, (n_rays + kRayWarps - 1) / kRayWarps);
+  k_ray_bp<<<(unsigned)std::max<int64_t>(b, 1), kRayWarps * 32, 0, s>>>(
+      a.meta, order, n_rays, counter, a.inc_pair, a.inc_len, a.inc_mu, a.pair_lnq, a.inc_pl, fix_reset);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ray_keys(const RayMeta* meta, uint32_t n, uint32_t* keys, uint32_t* vals,
+                            cudaStream_t s) {
+  if (!n) return cudaSuccess;
+  k_ray_keys<<<blocks(n, 256), 256, 0, s>>>(meta, n, keys, vals);
   return cudaGetLastError();
 }
 
@@ -573,6 +612,12 @@ cudaError_t launch_remap_gather(const uint32_t* pair_vox, float* pair_m, uint32_
                                 const float* dense, cudaStream_t s) {
   if (!n) return cudaSuccess;
   k_remap_gather<<<blocks(n, 256), 256, 0, s>>>(pair_vox, pair_m, n, dense);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_add_u32(uint32_t* p, uint32_t n, uint32_t v, cudaStream_t s) {
+  if (!n) return cudaSuccess;
+  k_add_u32<<<blocks(n, 256), 256, 0, s>>>(p, n, v);
   return cudaGetLastError();
 }
 

@@ -86,6 +86,7 @@ struct View {
   uint32_t inc_base = 0, n_inc = 0;
   uint32_t pair_base = 0, n_pairs = 0;
   uint32_t perm_base = 0, n_perm = 0;
+  uint32_t order_base = 0, n_active = 0;  // ray queue (longest first)
 };
 
 uint32_t u32_checked(int64_t v, const char* what) {
@@ -110,7 +111,7 @@ struct mrf_map {
   std::vector<View> views;
   // arenas
   DBuf meta, inc_pair, inc_len, inc_mu, inc_pl, pair_vox, pair_m, pair_cum, pair_q, pair_dm,
-      pair_seg, perm, skey, carry, pair_acc;
+      pair_seg, perm, skey, carry, pair_acc, ray_order, counters;
   int64_t n_inc = 0, n_pairs = 0, n_perm = 0;
   // jacobi voxel CSR
   DBuf vseg, vpairs, vvox;
@@ -342,6 +343,32 @@ void rebuild(mrf_map* m) {
     pair_total += np;
     perm_total += nr;
   }
+  // ray queues: per view, the active rays longest first
+  {
+    m->ray_order.reserve((size_t)std::max<int64_t>(npix, 1) * 4, false, m->stream);
+    m->s_k0.reserve((size_t)HW * 4 + 4, false, m->stream);
+    m->s_k1.reserve((size_t)HW * 4 + 4, false, m->stream);
+    m->s_v0.reserve((size_t)HW * 4 + 4, false, m->stream);
+    int64_t base = 0;
+    for (int c = 0; c < V; ++c) {
+      View& v = m->views[c];
+      int64_t act = 0;
+      for (int64_t i = 0; i < HW; ++i) act += hm[(size_t)(c * HW + i)].n_pre > 0;
+      v.order_base = (uint32_t)base;
+      v.n_active = (uint32_t)act;
+      CK(launch_ray_keys(m->meta.as<RayMeta>() + c * HW, (uint32_t)HW, m->s_k0.as<uint32_t>(),
+                         m->s_v0.as<uint32_t>(), m->stream));
+      size_t t = sort_temp_bytes((uint32_t)HW, 17);
+      m->s_tmp.reserve(t, false, m->stream);
+      CK(sort_pairs_u32(m->s_tmp.p, t, m->s_k0.as<uint32_t>(), m->s_k1.as<uint32_t>(),
+                        m->s_v0.as<uint32_t>(), m->ray_order.as<uint32_t>() + base, (uint32_t)HW, 17,
+                        m->stream));
+      // queue entries are global ray indices
+      CK(launch_add_u32(m->ray_order.as<uint32_t>() + base, (uint32_t)act, (uint32_t)(c * HW), m->stream));
+      base += act;
+    }
+    m->counters.reserve((size_t)(V + 1) * 4, false, m->stream);
+  }
   m->n_inc = n_inc;
   m->n_pairs = pair_total;
   m->n_perm = perm_total;
@@ -491,6 +518,7 @@ void run_infer(mrf_map* m, const int* ids, int n_ids, int iters, int flags) {
   }
   const int fix = (flags & MRF_FIX_PRE_RESET) ? 1 : 0;
   for (int it = 0; it < iters; ++it) {
+    CK(cudaMemsetAsync(m->counters.p, 0, (size_t)(V + 1) * 4, m->stream));
     if (!jacobi) {
       // Gauss-Seidel over every camera (src/GVDBInference.cpp:155-167)
       for (int c = 0; c < V; ++c) {
@@ -500,7 +528,8 @@ void run_infer(mrf_map* m, const int* ids, int n_ids, int iters, int flags) {
         CK(launch_pair_prepare(a, v.pair_base, v.pair_base + v.n_pairs, 0, m->stream));
         prof.end();
         prof.begin(1);
-        CK(launch_ray_bp(a, (uint32_t)(c * HW), (uint32_t)((c + 1) * HW), fix, m->num_sms, m->stream));
+        CK(launch_ray_bp(a, m->ray_order.as<uint32_t>() + v.order_base, v.n_active,
+                         m->counters.as<uint32_t>() + c, fix, m->num_sms, m->stream));
         prof.end();
         prof.begin(2);
         CK(launch_pair_update(a, v.perm_base, v.perm_base + v.n_perm, v.pair_base,
@@ -514,7 +543,11 @@ void run_infer(mrf_map* m, const int* ids, int n_ids, int iters, int flags) {
       CK(launch_pair_prepare(a, 0, P, 1, m->stream));
       prof.end();
       prof.begin(1);
-      CK(launch_ray_bp(a, 0, (uint32_t)(V * HW), fix, m->num_sms, m->stream));
+      // the queues of all views are contiguous: one launch over all rays
+      uint32_t nact = 0;
+      for (const View& v : m->views) nact += v.n_active;
+      CK(launch_ray_bp(a, m->ray_order.as<uint32_t>(), nact, m->counters.as<uint32_t>() + V, fix,
+                       m->num_sms, m->stream));
       prof.end();
       prof.begin(2);
       CK(launch_pair_update(a, 0, (uint32_t)m->n_perm, 0, P, m->carry.as<TileCarry>(), 1, m->stream));
@@ -597,7 +630,7 @@ void destroy_bufs(mrf_map* m) {
   DBuf* all[] = {&m->d_sigma, &m->d_bias, &m->d_slot, &m->d_coord, &m->d_L, &m->d_belief,
                  &m->meta, &m->inc_pair, &m->inc_len, &m->inc_mu, &m->inc_pl, &m->pair_vox,
                  &m->pair_m, &m->pair_cum, &m->pair_q, &m->pair_dm, &m->pair_seg, &m->perm,
-                 &m->skey, &m->carry, &m->pair_acc,
+                 &m->skey, &m->carry, &m->pair_acc, &m->ray_order, &m->counters,
                  &m->vseg, &m->vpairs, &m->vvox, &m->s_postlen, &m->s_flags, &m->s_ind, &m->s_scan,
                  &m->s_tmp, &m->s_counts, &m->s_offs, &m->s_vox, &m->s_k0, &m->s_k1, &m->s_v0,
                  &m->s_v1, &m->s_seg, &m->s_dense, &m->s_err, &m->s_depth_in, &m->s_depth,

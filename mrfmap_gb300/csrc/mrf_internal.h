@@ -125,8 +125,11 @@ struct TileCarry {
 uint32_t pair_update_tiles(uint32_t n);
 cudaError_t launch_pair_prepare(const BpArrays& a, uint32_t p0, uint32_t p1, int jacobi,
                                 cudaStream_t s);
-cudaError_t launch_ray_bp(const BpArrays& a, uint32_t r0, uint32_t r1, int fix_reset, int num_sms,
-                          cudaStream_t s);
+// rays order[0..n_rays) of the queue; counter: one zeroed u32 per launch
+cudaError_t launch_ray_bp(const BpArrays& a, const uint32_t* order, uint32_t n_rays,
+                          uint32_t* counter, int fix_reset, int num_sms, cudaStream_t s);
+cudaError_t launch_ray_keys(const RayMeta* meta, uint32_t n, uint32_t* keys, uint32_t* vals,
+                            cudaStream_t s);
 // k0..k1: range of sorted (pair-grouped) positions
 cudaError_t launch_pair_update(const BpArrays& a, uint32_t k0, uint32_t k1, uint32_t p0, uint32_t p1,
                                TileCarry* carry, int jacobi, cudaStream_t s);
@@ -140,6 +143,7 @@ cudaError_t launch_remap_gather(const uint32_t* pair_vox, float* pair_m, uint32_
                                 const float* dense, cudaStream_t s);
 cudaError_t launch_fill_f32(float* p, int64_t n, float v, cudaStream_t s);
 cudaError_t launch_fill_u32(uint32_t* p, int64_t n, uint32_t v, cudaStream_t s);
+cudaError_t launch_add_u32(uint32_t* p, uint32_t n, uint32_t v, cudaStream_t s);
 cudaError_t launch_vflag(const uint32_t* sk, uint32_t n, uint32_t* flag, cudaStream_t s);
 cudaError_t launch_vassign(const uint32_t* sk, const uint32_t* flag, const uint32_t* scan,
                            uint32_t n, uint32_t* vvox, uint32_t* vseg, cudaStream_t s);
