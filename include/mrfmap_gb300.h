@@ -46,6 +46,8 @@ typedef enum {
 #define MRF_FIX_PRE_RESET 4 /* carry Pre-pass visibility across all bricks */
 #define MRF_ASYNC 8         /* enqueue only; do not wait for completion */
 #define MRF_PROFILE 16      /* time every kernel with CUDA events (mrf_stats) */
+#define MRF_NO_GRAPH 32     /* launch kernels one by one instead of replaying the
+                               captured CUDA graph of one iteration */
 
 /* Mirrors gvdb_params_t (include/mrfmap/GVDBParams.h:11-28). */
 typedef struct mrf_params {

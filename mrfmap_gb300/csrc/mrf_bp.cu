@@ -56,18 +56,20 @@ __global__ void k_pair_prepare(const uint32_t* __restrict__ pair_vox, const floa
 // ---- ray messages ----------------------------------------------------------
 // One warp per ray.  Each lane owns 4 consecutive incidences (ray offsets are
 // padded to multiples of 4, so the streams load as 16-byte vectors); a chunk
-// is 128 incidences.  Pass 1 runs over the Pre range computing the
+// is 128 incidences and the next chunk's streams are prefetched while the
+// current one computes.  Pass 1 runs over the Pre range computing the
 // visibility exponent A_i = sum_{j<=i} l_j ln q_j (thread-serial over 4, warp
-// scan across lanes), the visibility V_i = exp(A_i), q_i, and the Pre total T;
-// it stages (V_i mu_i, q_i, l_i) in shared memory.  Pass 2 reads the stage
-// back and writes p_i * l_i in ray order.  Rays longer than the stage recompute pass 1's
-// values in pass 2 and form T - F in FP64.
+// scan across lanes), V_i = exp(A_i), q_i and the Pre total T; it stages
+// (V_i mu_i, q_i) in shared memory.  Pass 2 reads the stage back (lengths
+// again from global memory, an L2 hit) and writes p_i * l_i in ray order.
+// Rays longer than the stage recompute pass 1's values in pass 2.  The tau
+// sums of rays longer than kLongRay are formed in FP64.
 //
 // Pre visibility restarts at r0 (the reference restores its carried state
 // only once the accumulated tau is non-zero, gvdbkernels.cu:708-715):
 // V^pre_i = exp(A_i - A_{r0-1}) = V_i * exp(-A_{r0-1}); Post uses V_i.
 constexpr int kRayWarps = 4;
-constexpr int kStage = 512;              // incidences staged per warp
+constexpr int kStage = 1024;             // incidences staged per warp
 constexpr int kStageVec = kStage / 4;    // float4 entries per staged array
 constexpr float kUnderflowGuard = -60.0f;
 
@@ -87,43 +89,50 @@ __device__ __forceinline__ float chunk_value(const float (&A)[4], int idx_in_chu
   return __shfl_sync(kFull, mine, idx_in_chunk >> 2);
 }
 
+__device__ __forceinline__ float4 f4(const float (&v)[4]) { return make_float4(v[0], v[1], v[2], v[3]); }
+
+// raw streams of one chunk for one lane
+struct Streams {
+  uint4 pid;
+  float4 len, mu;
+};
+
+__device__ __forceinline__ void load_streams(Streams& s, uint32_t off, int i0, int n,
+                                             const uint32_t* __restrict__ inc_pair,
+                                             const float* __restrict__ inc_len,
+                                             const float* __restrict__ inc_mu) {
+  if (i0 < n) {
+    s.pid = __ldg(reinterpret_cast<const uint4*>(inc_pair + off + i0));
+    s.len = __ldg(reinterpret_cast<const float4*>(inc_len + off + i0));
+    s.mu = __ldg(reinterpret_cast<const float4*>(inc_mu + off + i0));
+  } else {
+    s.pid = make_uint4(0u, 0u, 0u, 0u);
+    s.len = make_float4(0.f, 0.f, 0.f, 0.f);
+    s.mu = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+}
+
 struct Chunk {
   float A[4], q[4], mu[4], len[4];
 };
 
-__device__ __forceinline__ float4 f4(const float (&v)[4]) { return make_float4(v[0], v[1], v[2], v[3]); }
-
-// loads chunk [base, base+128) of a ray (elements >= n are zero), its prefix
-// exponents and q; returns the chunk's total of l ln q
-__device__ __forceinline__ float load_chunk(Chunk& c, uint32_t off, int base, int n, float carryA,
-                                            int lane, const uint32_t* __restrict__ inc_pair,
-                                            const float* __restrict__ inc_len,
-                                            const float* __restrict__ inc_mu,
-                                            const float* __restrict__ lnq) {
-  int i0 = base + 4 * lane;
-  float a[4] = {0.f, 0.f, 0.f, 0.f};
+// gathers ln q for a chunk's streams and forms prefix exponents and q;
+// returns the chunk's total of l ln q
+__device__ __forceinline__ float expand_chunk(Chunk& c, const Streams& s, int i0, int n, float carryA,
+                                              int lane, const float* __restrict__ lnq) {
+  uint32_t pp[4] = {s.pid.x, s.pid.y, s.pid.z, s.pid.w};
+  float lv[4] = {s.len.x, s.len.y, s.len.z, s.len.w};
+  float mv[4] = {s.mu.x, s.mu.y, s.mu.z, s.mu.w};
+  float lq[4], a[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) lq[j] = (i0 + j < n) ? __ldg(lnq + pp[j]) : 0.0f;
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
-    c.q[j] = 1.0f;
-    c.mu[j] = c.len[j] = 0.0f;
-  }
-  if (i0 < n) {
-    uint4 pid = __ldg(reinterpret_cast<const uint4*>(inc_pair + off + i0));
-    float4 ln = __ldg(reinterpret_cast<const float4*>(inc_len + off + i0));
-    float4 mu = __ldg(reinterpret_cast<const float4*>(inc_mu + off + i0));
-    uint32_t pp[4] = {pid.x, pid.y, pid.z, pid.w};
-    float lv[4] = {ln.x, ln.y, ln.z, ln.w};
-    float mv[4] = {mu.x, mu.y, mu.z, mu.w};
-#pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      if (i0 + j < n) {
-        float lq = __ldg(lnq + pp[j]);
-        c.q[j] = __expf(lq);
-        c.len[j] = lv[j];
-        c.mu[j] = mv[j];
-        a[j] = lv[j] * lq;
-      }
-    }
+    bool ok = i0 + j < n;
+    c.q[j] = ok ? __expf(lq[j]) : 1.0f;
+    c.len[j] = ok ? lv[j] : 0.0f;
+    c.mu[j] = ok ? mv[j] : 0.0f;
+    a[j] = ok ? lv[j] * lq[j] : 0.0f;
   }
   float s0 = a[0], s1 = s0 + a[1], s2 = s1 + a[2], s3 = s2 + a[3];
   float ex = warp_excl_scan(s3, lane);
@@ -136,7 +145,7 @@ __device__ __forceinline__ float load_chunk(Chunk& c, uint32_t off, int base, in
 }
 
 struct Stage {
-  float4 vmu[kStageVec], q[kStageVec], len[kStageVec];
+  float4 vmu[kStageVec], q[kStageVec];
 };
 
 template <bool kStaged, typename Acc>
@@ -153,12 +162,15 @@ __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, Stage& st,
   // ---- pass 1: prefixes, Pre total ---------------------------------------
   float carryA = 0.0f, Ar0 = 0.0f, Arinf = 0.0f;
   Acc T = 0;
+  Streams cur;
+  load_streams(cur, off, 4 * lane, n_pre, inc_pair, inc_len, inc_mu);
   for (int base = 0; base < n_pre; base += 128) {
+    const int i0 = base + 4 * lane;
     Chunk c;
-    float tot = load_chunk(c, off, base, n_pre, carryA, lane, inc_pair, inc_len, inc_mu, lnq);
+    float tot = expand_chunk(c, cur, i0, n_pre, carryA, lane, lnq);
+    if (base + 128 < n_pre) load_streams(cur, off, i0 + 128, n_pre, inc_pair, inc_len, inc_mu);
     if (r0 > 0 && r0 - 1 >= base && r0 - 1 < base + 128) Ar0 = chunk_value(c.A, r0 - 1 - base);
     if (rinf > 0 && rinf - 1 >= base && rinf - 1 < base + 128) Arinf = chunk_value(c.A, rinf - 1 - base);
-    const int i0 = base + 4 * lane;
     float V[4], w = 0.0f;
     // exp(-A_{r0-1}) rescales Post visibility to Pre visibility unless the
     // Post visibility may have underflowed (then exponentiate the difference)
@@ -177,7 +189,6 @@ __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, Stage& st,
       float vm[4] = {V[0] * c.mu[0], V[1] * c.mu[1], V[2] * c.mu[2], V[3] * c.mu[3]};
       st.vmu[slot] = f4(vm);
       st.q[slot] = f4(c.q);
-      st.len[slot] = f4(c.len);
     }
     T += (Acc)warp_sum(w);
     carryA += tot;
@@ -190,6 +201,7 @@ __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, Stage& st,
   // Post stop get an explicit zero message.
   Acc carryF = 0;
   float carryA2 = 0.0f;
+  if (!kStaged) load_streams(cur, off, 4 * lane, n_pre, inc_pair, inc_len, inc_mu);
   for (int base = 0; base < n_pre; base += 128) {
     const int i0 = base + 4 * lane;
     float vmu[4], q[4], len[4];
@@ -197,13 +209,15 @@ __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, Stage& st,
       int slot = (base >> 2) + lane;
       float4 a = i0 < n_pre ? st.vmu[slot] : make_float4(0.f, 0.f, 0.f, 0.f);
       float4 b = i0 < n_pre ? st.q[slot] : make_float4(1.f, 1.f, 1.f, 1.f);
-      float4 d = i0 < n_pre ? st.len[slot] : make_float4(0.f, 0.f, 0.f, 0.f);
+      float4 d = i0 < n_pre ? __ldg(reinterpret_cast<const float4*>(inc_len + off + i0))
+                            : make_float4(0.f, 0.f, 0.f, 0.f);
       vmu[0] = a.x; vmu[1] = a.y; vmu[2] = a.z; vmu[3] = a.w;
       q[0] = b.x; q[1] = b.y; q[2] = b.z; q[3] = b.w;
       len[0] = d.x; len[1] = d.y; len[2] = d.z; len[3] = d.w;
     } else {
       Chunk c;
-      float tot2 = load_chunk(c, off, base, n_pre, carryA2, lane, inc_pair, inc_len, inc_mu, lnq);
+      float tot2 = expand_chunk(c, cur, i0, n_pre, carryA2, lane, lnq);
+      if (base + 128 < n_pre) load_streams(cur, off, i0 + 128, n_pre, inc_pair, inc_len, inc_mu);
       carryA2 += tot2;
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
@@ -266,8 +280,10 @@ __global__ void __launch_bounds__(kRayWarps * 32) k_ray_bp(const RayMeta* __rest
     idx = __shfl_sync(kFull, idx, 0);
     if (idx >= n_rays) break;
     RayMeta me = meta[order[idx]];
-    if (me.n_pre <= kStage)
+    if (me.n_pre <= kLongRay)
       ray_bp_warp<true, float>(me, st, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
+    else if (me.n_pre <= kStage)
+      ray_bp_warp<true, double>(me, st, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
     else
       ray_bp_warp<false, double>(me, st, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
   }
@@ -543,9 +559,7 @@ cudaError_t launch_pair_prepare(const BpArrays& a, uint32_t p0, uint32_t p1, int
 }
 
 
-cudaError_t launch_ray_bp(const BpArrays& a, const uint32_t* order, uint32_t n_rays,
-                          uint32_t* counter, int fix_reset, int num_sms, cudaStream_t s) {
-  if (!n_rays) return cudaSuccess;
+int ray_bp_resident_blocks() {
   static int resident = 0;
   if (!resident) {
     int per_sm = 0;
@@ -555,7 +569,14 @@ cudaError_t launch_ray_bp(const BpArrays& a, const uint32_t* order, uint32_t n_r
       per_sm = 1;
     resident = per_sm;
   }
-  int64_t b = std::min<int64_t>((int64_t)num_sms * resident, (n_rays + kRayWarps - 1) / kRayWarps);
+  return resident;
+}
+
+cudaError_t launch_ray_bp(const BpArrays& a, const uint32_t* order, uint32_t n_rays,
+                          uint32_t* counter, int fix_reset, int num_sms, cudaStream_t s) {
+  if (!n_rays) return cudaSuccess;
+  int64_t b = std::min<int64_t>((int64_t)num_sms * ray_bp_resident_blocks(),
+                                (n_rays + kRayWarps - 1) / kRayWarps);
   k_ray_bp<<<(unsigned)std::max<int64_t>(b, 1), kRayWarps * 32, 0, s>>>(
       a.meta, order, n_rays, counter, a.inc_pair, a.inc_len, a.inc_mu, a.pair_lnq, a.inc_pl, fix_reset);
   return cudaGetLastError();

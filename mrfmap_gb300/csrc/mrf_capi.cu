@@ -124,6 +124,12 @@ struct mrf_map {
   // MRF_PROFILE event pool
   std::vector<cudaEvent_t> prof_ev;
   std::vector<int> prof_cat;
+  // captured BP iteration per schedule (Jacobi bit, fixed-reset bit)
+  struct GraphSlot {
+    cudaGraphExec_t exec = nullptr;
+    int version = -1;
+    int64_t launches = 0;
+  } graphs[4];
 
   BpArrays bp() const {
     BpArrays a;
@@ -494,12 +500,95 @@ struct Profiler {
   }
 };
 
+// one BP iteration over every camera (src/GVDBInference.cpp:155-167):
+// Gauss-Seidel camera by camera, or Jacobi over all cameras at once
+void enqueue_iteration(mrf_map* m, const BpArrays& a, bool jacobi, int fix, Profiler& prof,
+                       int64_t& launches) {
+  const int V = (int)m->views.size();
+  CK(cudaMemsetAsync(m->counters.p, 0, (size_t)(V + 1) * 4, m->stream));
+  if (!jacobi) {
+    for (int c = 0; c < V; ++c) {
+      const View& v = m->views[c];
+      if (v.n_inc == 0) continue;
+      prof.begin(0);
+      CK(launch_pair_prepare(a, v.pair_base, v.pair_base + v.n_pairs, 0, m->stream));
+      prof.end();
+      prof.begin(1);
+      CK(launch_ray_bp(a, m->ray_order.as<uint32_t>() + v.order_base, v.n_active,
+                       m->counters.as<uint32_t>() + c, fix, m->num_sms, m->stream));
+      prof.end();
+      prof.begin(2);
+      CK(launch_pair_update(a, v.perm_base, v.perm_base + v.n_perm, v.pair_base,
+                            v.pair_base + v.n_pairs, m->carry.as<TileCarry>(), 0, m->stream));
+      prof.end();
+      launches += 5;
+    }
+  } else {
+    uint32_t P = (uint32_t)m->n_pairs;
+    prof.begin(0);
+    CK(launch_pair_prepare(a, 0, P, 1, m->stream));
+    prof.end();
+    prof.begin(1);
+    // the queues of all views are contiguous: one launch over all rays
+    uint32_t nact = 0;
+    for (const View& v : m->views) nact += v.n_active;
+    CK(launch_ray_bp(a, m->ray_order.as<uint32_t>(), nact, m->counters.as<uint32_t>() + V, fix,
+                     m->num_sms, m->stream));
+    prof.end();
+    prof.begin(2);
+    CK(launch_pair_update(a, 0, (uint32_t)m->n_perm, 0, P, m->carry.as<TileCarry>(), 1, m->stream));
+    prof.end();
+    prof.begin(3);
+    CK(launch_voxel_apply(m->vseg.as<uint32_t>(), m->vpairs.as<uint32_t>(), m->vvox.as<uint32_t>(),
+                          m->n_vvox, m->pair_dm.as<float>(), m->d_L.as<float>(),
+                          m->d_belief.as<float>(), m->stream));
+    prof.end();
+    launches += 6;
+  }
+}
+
+// The iteration is captured once per incidence build and schedule into a
+// CUDA graph and replayed iters times.
+cudaGraphExec_t iteration_graph(mrf_map* m, const BpArrays& a, bool jacobi, int fix,
+                                int64_t& launches_per_iter) {
+  int key = (jacobi ? 1 : 0) | (fix ? 2 : 0);
+  auto& slot = m->graphs[key];
+  if (slot.exec && slot.version == m->built_version) {
+    launches_per_iter = slot.launches;
+    return slot.exec;
+  }
+  if (slot.exec) {
+    cudaGraphExecDestroy(slot.exec);
+    slot.exec = nullptr;
+  }
+  Profiler off{m, false};
+  int64_t launches = 0;
+  cudaGraph_t graph = nullptr;
+  CK(cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal));
+  try {
+    enqueue_iteration(m, a, jacobi, fix, off, launches);
+  } catch (...) {
+    cudaStreamEndCapture(m->stream, &graph);
+    if (graph) cudaGraphDestroy(graph);
+    throw;
+  }
+  CK(cudaStreamEndCapture(m->stream, &graph));
+  cudaGraphExec_t exec = nullptr;
+  cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  CK(e);
+  slot.exec = exec;
+  slot.version = m->built_version;
+  slot.launches = launches;
+  launches_per_iter = launches;
+  return exec;
+}
+
 void run_infer(mrf_map* m, const int* ids, int n_ids, int iters, int flags) {
   ensure_built(m);
   const bool jacobi = flags & MRF_JACOBI;
   if (jacobi && m->jacobi_version != m->built_version) build_jacobi_csr(m);
   const int V = (int)m->views.size();
-  const int64_t HW = m->hw();
   if (iters <= 0) iters = m->prm.max_iters > 0 ? m->prm.max_iters : 1;
   BpArrays a = m->bp();
   int64_t launches = 0;
@@ -517,48 +606,14 @@ void run_infer(mrf_map* m, const int* ids, int n_ids, int iters, int flags) {
     }
   }
   const int fix = (flags & MRF_FIX_PRE_RESET) ? 1 : 0;
-  for (int it = 0; it < iters; ++it) {
-    CK(cudaMemsetAsync(m->counters.p, 0, (size_t)(V + 1) * 4, m->stream));
-    if (!jacobi) {
-      // Gauss-Seidel over every camera (src/GVDBInference.cpp:155-167)
-      for (int c = 0; c < V; ++c) {
-        const View& v = m->views[c];
-        if (v.n_inc == 0) continue;
-        prof.begin(0);
-        CK(launch_pair_prepare(a, v.pair_base, v.pair_base + v.n_pairs, 0, m->stream));
-        prof.end();
-        prof.begin(1);
-        CK(launch_ray_bp(a, m->ray_order.as<uint32_t>() + v.order_base, v.n_active,
-                         m->counters.as<uint32_t>() + c, fix, m->num_sms, m->stream));
-        prof.end();
-        prof.begin(2);
-        CK(launch_pair_update(a, v.perm_base, v.perm_base + v.n_perm, v.pair_base,
-                              v.pair_base + v.n_pairs, m->carry.as<TileCarry>(), 0, m->stream));
-        prof.end();
-        launches += 5;
-      }
+  if (m->n_inc > 0) {
+    if (prof.on || (flags & MRF_NO_GRAPH)) {
+      for (int it = 0; it < iters; ++it) enqueue_iteration(m, a, jacobi, fix, prof, launches);
     } else {
-      uint32_t P = (uint32_t)m->n_pairs;
-      prof.begin(0);
-      CK(launch_pair_prepare(a, 0, P, 1, m->stream));
-      prof.end();
-      prof.begin(1);
-      // the queues of all views are contiguous: one launch over all rays
-      uint32_t nact = 0;
-      for (const View& v : m->views) nact += v.n_active;
-      CK(launch_ray_bp(a, m->ray_order.as<uint32_t>(), nact, m->counters.as<uint32_t>() + V, fix,
-                       m->num_sms, m->stream));
-      prof.end();
-      prof.begin(2);
-      CK(launch_pair_update(a, 0, (uint32_t)m->n_perm, 0, P, m->carry.as<TileCarry>(), 1, m->stream));
-      prof.end();
-      launches += 2;
-      prof.begin(3);
-      CK(launch_voxel_apply(m->vseg.as<uint32_t>(), m->vpairs.as<uint32_t>(), m->vvox.as<uint32_t>(),
-                            m->n_vvox, m->pair_dm.as<float>(), m->d_L.as<float>(),
-                            m->d_belief.as<float>(), m->stream));
-      prof.end();
-      launches += 4;
+      int64_t per = 0;
+      cudaGraphExec_t exec = iteration_graph(m, a, jacobi, fix, per);
+      for (int it = 0; it < iters; ++it) CK(cudaGraphLaunch(exec, m->stream));
+      launches += per * iters;
     }
   }
   CK(cudaEventRecord(m->ev1, m->stream));
@@ -719,6 +774,7 @@ mrf_status mrf_create(const mrf_params* params, mrf_map** out) {
     m->prm.bias_lut = m->bias.data();
     CK(cudaGetDevice(&m->device));
     CK(cudaDeviceGetAttribute(&m->num_sms, cudaDevAttrMultiProcessorCount, m->device));
+    ray_bp_resident_blocks();
     CK(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking));
     CK(cudaEventCreate(&m->ev0));
     CK(cudaEventCreate(&m->ev1));
@@ -755,6 +811,8 @@ void mrf_destroy(mrf_map* m) {
   if (m->stream) cudaStreamSynchronize(m->stream);
   destroy_bufs(m);
   for (cudaEvent_t e : m->prof_ev) cudaEventDestroy(e);
+  for (auto& g : m->graphs)
+    if (g.exec) cudaGraphExecDestroy(g.exec);
   if (m->ev0) cudaEventDestroy(m->ev0);
   if (m->ev1) cudaEventDestroy(m->ev1);
   if (m->stream) cudaStreamDestroy(m->stream);

@@ -125,6 +125,8 @@ struct TileCarry {
 uint32_t pair_update_tiles(uint32_t n);
 cudaError_t launch_pair_prepare(const BpArrays& a, uint32_t p0, uint32_t p1, int jacobi,
                                 cudaStream_t s);
+// resident blocks per SM of the persistent ray kernel (queried once)
+int ray_bp_resident_blocks();
 // rays order[0..n_rays) of the queue; counter: one zeroed u32 per launch
 cudaError_t launch_ray_bp(const BpArrays& a, const uint32_t* order, uint32_t n_rays,
                           uint32_t* counter, int fix_reset, int num_sms, cudaStream_t s);

@@ -24,6 +24,7 @@ INCREMENTAL = 2
 FIX_PRE_RESET = 4
 ASYNC = 8
 PROFILE = 16
+NO_GRAPH = 32
 
 _STATUS = {0: "MRF_OK", 1: "MRF_ERR_INVALID", 2: "MRF_ERR_CUDA", 3: "MRF_ERR_OOM",
            4: "MRF_ERR_CAPACITY", 5: "MRF_ERR_DEVICE", 6: "MRF_ERR_STATE"}
