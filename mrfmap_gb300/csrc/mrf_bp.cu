@@ -54,28 +54,26 @@ __global__ void k_pair_prepare(const uint32_t* __restrict__ pair_vox, const floa
 }
 
 // ---- ray messages ----------------------------------------------------------
-// One warp per ray.  Each lane owns 4 consecutive incidences (ray offsets are
-// padded to multiples of 4, so the streams load as 16-byte vectors); a chunk
-// is 128 incidences and the next chunk's streams are prefetched while the
-// current one computes.  Pass 1 runs over the Pre range computing the
-// visibility exponent A_i = sum_{j<=i} l_j ln q_j (thread-serial over 4, warp
-// scan across lanes), V_i = exp(A_i), q_i and the Pre total T; it stages
-// (V_i mu_i, q_i) in shared memory.  Pass 2 reads the stage back (lengths
-// again from global memory, an L2 hit) and writes p_i * l_i in ray order.
-// Rays longer than the stage recompute pass 1's values in pass 2.  The tau
-// sums of rays longer than kLongRay are formed in FP64.
+// One warp per ray.  Each lane owns kE = 8 consecutive incidences of a
+// chunk of 256 (ray offsets are padded to multiples of 4, so the streams load
+// as 16-byte vectors): the prefix over the ray is a serial sum inside the
+// lane plus one warp scan per chunk, and a lane keeps 8 gathers in flight.
+//
+// Pass 1 forms the visibility exponent A_i = sum_{j<=i} l_j ln q_j,
+// V_i = exp(A_i), q_i and the Pre total T; pass 2 turns (V_i mu_i, q_i, l_i)
+// and T into the messages p_i * l_i, written in ray order.  A ray of one chunk
+// keeps pass 1's values in registers; rays of up to four chunks stage them in
+// shared memory; longer rays recompute them in pass 2.  The tau sums of rays longer
+// than kLongRay are formed in FP64.
 //
 // Pre visibility restarts at r0 (the reference restores its carried state
 // only once the accumulated tau is non-zero, gvdbkernels.cu:708-715):
 // V^pre_i = exp(A_i - A_{r0-1}) = V_i * exp(-A_{r0-1}); Post uses V_i.
 constexpr int kRayWarps = 4;
-constexpr int kStage = 1024;             // incidences staged per warp
-constexpr int kStageVec = kStage / 4;    // float4 entries per staged array
+constexpr int kE = 8;                    // incidences per lane per chunk
+constexpr int kChunk = 32 * kE;          // 512
+constexpr int kStage = 4 * kChunk;       // incidences staged per warp
 constexpr float kUnderflowGuard = -60.0f;
-
-__device__ __forceinline__ float sel4(const float (&v)[4], int j) {
-  return j == 0 ? v[0] : (j == 1 ? v[1] : (j == 2 ? v[2] : v[3]));
-}
 
 template <typename T>
 __device__ __forceinline__ T warp_excl_scan(T v, int lane) {
@@ -83,72 +81,110 @@ __device__ __forceinline__ T warp_excl_scan(T v, int lane) {
   return incl - v;
 }
 
-// value held by lane idx/4 (element idx%4) of the current chunk
-__device__ __forceinline__ float chunk_value(const float (&A)[4], int idx_in_chunk) {
-  float mine = sel4(A, idx_in_chunk & 3);
-  return __shfl_sync(kFull, mine, idx_in_chunk >> 2);
-}
-
-__device__ __forceinline__ float4 f4(const float (&v)[4]) { return make_float4(v[0], v[1], v[2], v[3]); }
-
-// raw streams of one chunk for one lane
-struct Streams {
-  uint4 pid;
-  float4 len, mu;
-};
-
-__device__ __forceinline__ void load_streams(Streams& s, uint32_t off, int i0, int n,
-                                             const uint32_t* __restrict__ inc_pair,
-                                             const float* __restrict__ inc_len,
-                                             const float* __restrict__ inc_mu) {
-  if (i0 < n) {
-    s.pid = __ldg(reinterpret_cast<const uint4*>(inc_pair + off + i0));
-    s.len = __ldg(reinterpret_cast<const float4*>(inc_len + off + i0));
-    s.mu = __ldg(reinterpret_cast<const float4*>(inc_mu + off + i0));
-  } else {
-    s.pid = make_uint4(0u, 0u, 0u, 0u);
-    s.len = make_float4(0.f, 0.f, 0.f, 0.f);
-    s.mu = make_float4(0.f, 0.f, 0.f, 0.f);
-  }
-}
-
-struct Chunk {
-  float A[4], q[4], mu[4], len[4];
-};
-
-// gathers ln q for a chunk's streams and forms prefix exponents and q;
-// returns the chunk's total of l ln q
-__device__ __forceinline__ float expand_chunk(Chunk& c, const Streams& s, int i0, int n, float carryA,
-                                              int lane, const float* __restrict__ lnq) {
-  uint32_t pp[4] = {s.pid.x, s.pid.y, s.pid.z, s.pid.w};
-  float lv[4] = {s.len.x, s.len.y, s.len.z, s.len.w};
-  float mv[4] = {s.mu.x, s.mu.y, s.mu.z, s.mu.w};
-  float lq[4], a[4];
-#pragma unroll
-  for (int j = 0; j < 4; ++j) lq[j] = (i0 + j < n) ? __ldg(lnq + pp[j]) : 0.0f;
-#pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    bool ok = i0 + j < n;
-    c.q[j] = ok ? __expf(lq[j]) : 1.0f;
-    c.len[j] = ok ? lv[j] : 0.0f;
-    c.mu[j] = ok ? mv[j] : 0.0f;
-    a[j] = ok ? lv[j] * lq[j] : 0.0f;
-  }
-  float s0 = a[0], s1 = s0 + a[1], s2 = s1 + a[2], s3 = s2 + a[3];
-  float ex = warp_excl_scan(s3, lane);
-  float b = carryA + ex;
-  c.A[0] = b + s0;
-  c.A[1] = b + s1;
-  c.A[2] = b + s2;
-  c.A[3] = b + s3;
-  return __shfl_sync(kFull, ex + s3, 31);
-}
-
 struct Stage {
-  float4 vmu[kStageVec], q[kStageVec];
+  float vmu[kStage], q[kStage];
 };
 
-template <bool kStaged, typename Acc>
+// one lane's slice of a chunk
+struct Slice {
+  float A[kE], q[kE], mu[kE], len[kE];
+};
+
+// loads a lane's kE incidences at i0 (those >= n read as zero), gathers
+// ln q, forms prefix exponents from carryA; returns the chunk total of l ln q
+__device__ __forceinline__ float load_slice(Slice& s, uint32_t off, int i0, int n, float carryA,
+                                            int lane, const uint32_t* __restrict__ inc_pair,
+                                            const float* __restrict__ inc_len,
+                                            const float* __restrict__ inc_mu,
+                                            const float* __restrict__ lnq) {
+  uint32_t pid[kE];
+#pragma unroll
+  for (int v = 0; v < kE / 4; ++v) {
+    const int i = i0 + 4 * v;
+    uint4 p = make_uint4(0u, 0u, 0u, 0u);
+    float4 l = make_float4(0.f, 0.f, 0.f, 0.f), m = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (i < n) {
+      p = __ldg(reinterpret_cast<const uint4*>(inc_pair + off + i));
+      l = __ldg(reinterpret_cast<const float4*>(inc_len + off + i));
+      m = __ldg(reinterpret_cast<const float4*>(inc_mu + off + i));
+    }
+    pid[4 * v + 0] = p.x; pid[4 * v + 1] = p.y; pid[4 * v + 2] = p.z; pid[4 * v + 3] = p.w;
+    s.len[4 * v + 0] = l.x; s.len[4 * v + 1] = l.y; s.len[4 * v + 2] = l.z; s.len[4 * v + 3] = l.w;
+    s.mu[4 * v + 0] = m.x; s.mu[4 * v + 1] = m.y; s.mu[4 * v + 2] = m.z; s.mu[4 * v + 3] = m.w;
+  }
+  float lq[kE];
+#pragma unroll
+  for (int j = 0; j < kE; ++j) lq[j] = (i0 + j < n) ? __ldg(lnq + pid[j]) : 0.0f;
+  float run = 0.0f;
+#pragma unroll
+  for (int j = 0; j < kE; ++j) {
+    const bool ok = i0 + j < n;
+    s.q[j] = ok ? __expf(lq[j]) : 1.0f;
+    if (!ok) {
+      s.len[j] = 0.0f;
+      s.mu[j] = 0.0f;
+    }
+    run += s.len[j] * lq[j];
+    s.A[j] = run;  // lane-local inclusive prefix, rebased below
+  }
+  float ex = warp_excl_scan(run, lane);
+  float b = carryA + ex;
+#pragma unroll
+  for (int j = 0; j < kE; ++j) s.A[j] += b;
+  return __shfl_sync(kFull, ex + run, 31);
+}
+
+// A at chunk position idx (held by lane idx / kE)
+__device__ __forceinline__ float slice_value(const Slice& s, int idx) {
+  const int jj = idx % kE;
+  float mine = 0.0f;
+#pragma unroll
+  for (int j = 0; j < kE; ++j)
+    if (j == jj) mine = s.A[j];
+  return __shfl_sync(kFull, mine, idx / kE);
+}
+
+// pass 2 on one lane's slice: messages p*l for positions i0..i0+kE-1
+template <typename Acc>
+__device__ __forceinline__ Acc emit_slice(const float (&vmu)[kE], const float (&q)[kE],
+                                          const float (&len)[kE], int i0, int n_pre, int n_post,
+                                          Acc T, Acc carryF, int lane, uint32_t off,
+                                          float* __restrict__ inc_pl) {
+  float tau[kE], eloc[kE];
+  float run = 0.0f;
+#pragma unroll
+  for (int j = 0; j < kE; ++j) {
+    tau[j] = (i0 + j < n_post) ? vmu[j] * (1.0f - q[j]) : 0.0f;
+    eloc[j] = run;
+    run += tau[j];
+  }
+  float ex = warp_excl_scan(run, lane);
+  // F_i = carryF + (in-chunk exclusive prefix); the long-range difference
+  // T - carryF is formed in Acc (FP64 on long rays) once per chunk
+  const float cF = (float)carryF;
+  const float D = (float)(T - carryF);
+  float out[kE];
+#pragma unroll
+  for (int j = 0; j < kE; ++j) {
+    float fin = ex + eloc[j];
+    float F = cF + fin;
+    float R = (D - fin) - tau[j];
+    float mu1 = F + vmu[j];
+    float mu0 = F + __fdividef(R, q[j]);
+    float p = clampf(__fdividef(mu1, mu1 + mu0 + 1e-7f), kFEps, 1.0f - kFEps);
+    out[j] = (i0 + j < n_post) ? p * len[j] : 0.0f;
+  }
+#pragma unroll
+  for (int v = 0; v < kE / 4; ++v)
+    if (i0 + 4 * v < n_pre)
+      *reinterpret_cast<float4*>(inc_pl + off + i0 + 4 * v) =
+          make_float4(out[4 * v], out[4 * v + 1], out[4 * v + 2], out[4 * v + 3]);
+  return carryF + (Acc)__shfl_sync(kFull, ex + run, 31);
+}
+
+// mode 0: one chunk (registers), 1: up to four chunks (shared-memory
+// stage), 2: longer (recompute in pass 2)
+template <int kMode, typename Acc>
 __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, Stage& st,
                                             const uint32_t* __restrict__ inc_pair,
                                             const float* __restrict__ inc_len,
@@ -162,98 +198,75 @@ __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, Stage& st,
   // ---- pass 1: prefixes, Pre total ---------------------------------------
   float carryA = 0.0f, Ar0 = 0.0f, Arinf = 0.0f;
   Acc T = 0;
-  Streams cur;
-  load_streams(cur, off, 4 * lane, n_pre, inc_pair, inc_len, inc_mu);
-  for (int base = 0; base < n_pre; base += 128) {
-    const int i0 = base + 4 * lane;
-    Chunk c;
-    float tot = expand_chunk(c, cur, i0, n_pre, carryA, lane, lnq);
-    if (base + 128 < n_pre) load_streams(cur, off, i0 + 128, n_pre, inc_pair, inc_len, inc_mu);
-    if (r0 > 0 && r0 - 1 >= base && r0 - 1 < base + 128) Ar0 = chunk_value(c.A, r0 - 1 - base);
-    if (rinf > 0 && rinf - 1 >= base && rinf - 1 < base + 128) Arinf = chunk_value(c.A, rinf - 1 - base);
-    float V[4], w = 0.0f;
+  Slice s;
+  float vmu[kE];
+  for (int base = 0; base < n_pre; base += kChunk) {
+    const int i0 = base + kE * lane;
+    float tot = load_slice(s, off, i0, n_pre, carryA, lane, inc_pair, inc_len, inc_mu, lnq);
+    if (r0 > 0 && r0 - 1 >= base && r0 - 1 < base + kChunk) Ar0 = slice_value(s, r0 - 1 - base);
+    if (rinf > 0 && rinf - 1 >= base && rinf - 1 < base + kChunk) Arinf = slice_value(s, rinf - 1 - base);
     // exp(-A_{r0-1}) rescales Post visibility to Pre visibility unless the
     // Post visibility may have underflowed (then exponentiate the difference)
     const bool direct = Ar0 < kUnderflowGuard;
     const float scale = direct ? 0.0f : __expf(-Ar0);
+    float w = 0.0f;
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      V[j] = __expf(c.A[j]);
-      if (i0 + j >= r0 && c.mu[j] != 0.0f) {
-        float vp = direct ? __expf(c.A[j] - Ar0) : V[j] * scale;
-        w += vp * (1.0f - c.q[j]) * c.mu[j];
+    for (int j = 0; j < kE; ++j) {
+      float V = __expf(s.A[j]);
+      vmu[j] = V * s.mu[j];
+      if (i0 + j >= r0 && s.mu[j] != 0.0f) {
+        float vp = direct ? __expf(s.A[j] - Ar0) : V * scale;
+        w += vp * (1.0f - s.q[j]) * s.mu[j];
       }
     }
-    if (kStaged && i0 < n_pre) {
-      int slot = (base >> 2) + lane;
-      float vm[4] = {V[0] * c.mu[0], V[1] * c.mu[1], V[2] * c.mu[2], V[3] * c.mu[3]};
-      st.vmu[slot] = f4(vm);
-      st.q[slot] = f4(c.q);
+    if (kMode == 1) {
+#pragma unroll
+      for (int j = 0; j < kE; j += 4) {
+        *reinterpret_cast<float4*>(&st.vmu[base + kE * lane + j]) =
+            make_float4(vmu[j], vmu[j + 1], vmu[j + 2], vmu[j + 3]);
+        *reinterpret_cast<float4*>(&st.q[base + kE * lane + j]) =
+            make_float4(s.q[j], s.q[j + 1], s.q[j + 2], s.q[j + 3]);
+      }
     }
     T += (Acc)warp_sum(w);
     carryA += tot;
   }
   // infinity term: visibility at the end of Pre (gvdbkernels.cu:1196-1208)
   if (me.flags & 1u) T += (Acc)__expf(carryA - Arinf);
-  if (kStaged) __syncwarp();
   // ---- pass 2: messages ----------------------------------------------------
   // Runs over the Pre range so that the (rare) Pre-only incidences past the
   // Post stop get an explicit zero message.
   Acc carryF = 0;
+  if (kMode == 0) {
+    emit_slice<Acc>(vmu, s.q, s.len, kE * lane, n_pre, n_post, T, carryF, lane, off, inc_pl);
+    return;
+  }
+  if (kMode == 1) __syncwarp();
   float carryA2 = 0.0f;
-  if (!kStaged) load_streams(cur, off, 4 * lane, n_pre, inc_pair, inc_len, inc_mu);
-  for (int base = 0; base < n_pre; base += 128) {
-    const int i0 = base + 4 * lane;
-    float vmu[4], q[4], len[4];
-    if (kStaged) {
-      int slot = (base >> 2) + lane;
-      float4 a = i0 < n_pre ? st.vmu[slot] : make_float4(0.f, 0.f, 0.f, 0.f);
-      float4 b = i0 < n_pre ? st.q[slot] : make_float4(1.f, 1.f, 1.f, 1.f);
-      float4 d = i0 < n_pre ? __ldg(reinterpret_cast<const float4*>(inc_len + off + i0))
-                            : make_float4(0.f, 0.f, 0.f, 0.f);
-      vmu[0] = a.x; vmu[1] = a.y; vmu[2] = a.z; vmu[3] = a.w;
-      q[0] = b.x; q[1] = b.y; q[2] = b.z; q[3] = b.w;
-      len[0] = d.x; len[1] = d.y; len[2] = d.z; len[3] = d.w;
+  for (int base = 0; base < n_pre; base += kChunk) {
+    const int i0 = base + kE * lane;
+    if (kMode == 1) {
+      float q[kE], len[kE];
+#pragma unroll
+      for (int j = 0; j < kE; j += 4) {
+        float4 a = *reinterpret_cast<const float4*>(&st.vmu[base + kE * lane + j]);
+        float4 b = *reinterpret_cast<const float4*>(&st.q[base + kE * lane + j]);
+        float4 d = (i0 + j < n_pre) ? __ldg(reinterpret_cast<const float4*>(inc_len + off + i0 + j))
+                                    : make_float4(0.f, 0.f, 0.f, 0.f);
+        vmu[j] = a.x; vmu[j + 1] = a.y; vmu[j + 2] = a.z; vmu[j + 3] = a.w;
+        q[j] = b.x; q[j + 1] = b.y; q[j + 2] = b.z; q[j + 3] = b.w;
+        len[j] = d.x; len[j + 1] = d.y; len[j + 2] = d.z; len[j + 3] = d.w;
+      }
+      carryF = emit_slice<Acc>(vmu, q, len, i0, n_pre, n_post, T, carryF, lane, off, inc_pl);
     } else {
-      Chunk c;
-      float tot2 = expand_chunk(c, cur, i0, n_pre, carryA2, lane, lnq);
-      if (base + 128 < n_pre) load_streams(cur, off, i0 + 128, n_pre, inc_pair, inc_len, inc_mu);
+      float tot2 = load_slice(s, off, i0, n_pre, carryA2, lane, inc_pair, inc_len, inc_mu, lnq);
       carryA2 += tot2;
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        vmu[j] = __expf(c.A[j]) * c.mu[j];
-        q[j] = c.q[j];
-        len[j] = c.len[j];
-      }
+      for (int j = 0; j < kE; ++j) vmu[j] = __expf(s.A[j]) * s.mu[j];
+      carryF = emit_slice<Acc>(vmu, s.q, s.len, i0, n_pre, n_post, T, carryF, lane, off, inc_pl);
     }
-    float tau[4];
-#pragma unroll
-    for (int j = 0; j < 4; ++j) tau[j] = (i0 + j < n_post) ? vmu[j] * (1.0f - q[j]) : 0.0f;
-    float e1 = tau[0], e2 = e1 + tau[1], e3 = e2 + tau[2], lt = e3 + tau[3];
-    float ex = warp_excl_scan(lt, lane);
-    float eloc[4] = {0.0f, e1, e2, e3};
-    // F_i = carryF + (in-chunk exclusive prefix); the long-range difference
-    // T - carryF is formed in Acc (FP64 on long rays) once per chunk
-    const float cF = (float)carryF;
-    const float D = (float)(T - carryF);
-    if (i0 < n_pre) {
-      float out[4];
-#pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        float fin = ex + eloc[j];
-        float F = cF + fin;
-        float R = (D - fin) - tau[j];
-        float mu1 = F + vmu[j];
-        float mu0 = F + __fdividef(R, q[j]);
-        float p = clampf(__fdividef(mu1, mu1 + mu0 + 1e-7f), kFEps, 1.0f - kFEps);
-        out[j] = (i0 + j < n_post) ? p * len[j] : 0.0f;
-      }
-      // messages in ray order (16-byte stores; the pair update gathers them)
-      *reinterpret_cast<float4*>(inc_pl + off + i0) = f4(out);
-    }
-    carryF += (Acc)__shfl_sync(kFull, ex + lt, 31);
   }
-  if (kStaged) __syncwarp();
+  if (kMode == 1) __syncwarp();
 }
 
 // Persistent launch: each warp takes the next ray from a work counter; rays
@@ -280,12 +293,14 @@ __global__ void __launch_bounds__(kRayWarps * 32) k_ray_bp(const RayMeta* __rest
     idx = __shfl_sync(kFull, idx, 0);
     if (idx >= n_rays) break;
     RayMeta me = meta[order[idx]];
-    if (me.n_pre <= kLongRay)
-      ray_bp_warp<true, float>(me, st, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
+    if (me.n_pre <= kChunk)
+      ray_bp_warp<0, float>(me, st, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
+    else if (me.n_pre <= kLongRay)
+      ray_bp_warp<1, float>(me, st, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
     else if (me.n_pre <= kStage)
-      ray_bp_warp<true, double>(me, st, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
+      ray_bp_warp<1, double>(me, st, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
     else
-      ray_bp_warp<false, double>(me, st, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
+      ray_bp_warp<2, double>(me, st, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
   }
 }
 
