@@ -315,12 +315,14 @@ __global__ void k_ray_keys(const RayMeta* __restrict__ meta, uint32_t n, uint32_
 }
 
 // Pair update: a load-balanced segmented reduction over the pair-grouped
-// permutation of the messages.  Tiles of kTile consecutive positions are
-// summed by one block each (coalesced reads of the permutation and the pair
-// ids, kTile independent gathers of p*l in flight); segments that start and end inside a tile are applied there,
-// segments that cross tile edges leave partial sums that k_pair_fixup adds in
-// tile order.  Any segment length balances (voxels next to the camera are
-// crossed by thousands of rays) and the summation order is fixed.
+// permutation of the messages, fused with the per-pair update.  Tiles of
+// kTile consecutive positions are summed by one block each (coalesced reads
+// of the permutation and the pair ids, kTile independent gathers of p*l in
+// flight); pairs whose segment lies inside the tile are then updated by the
+// block's threads in parallel; segments that cross tile edges leave partial
+// sums that k_pair_fixup adds in tile order.  Any segment length balances
+// (voxels next to the camera are crossed by thousands of rays) and the
+// summation order is fixed.
 constexpr int kTileThreads = 256;
 constexpr int kTile = 4 * kTileThreads;
 constexpr uint32_t kOpenStart = 1u, kOpenEnd = 2u, kSingle = 4u;
@@ -334,12 +336,35 @@ __device__ __forceinline__ SegAgg seg_combine(SegAgg a, SegAgg b) {
   return SegAgg{b.f ? b.s : a.s + b.s, a.f || b.f};
 }
 
-__global__ void __launch_bounds__(kTileThreads)
+// factor->voxel update of one pair (gvdbkernels.cu:457-479)
+__device__ __forceinline__ void apply_pair(uint32_t p, float acc, const uint32_t* __restrict__ pair_vox,
+                                           float* __restrict__ m, const float* __restrict__ cum,
+                                           float* __restrict__ L, float* __restrict__ belief,
+                                           float* __restrict__ dm, int jacobi) {
+  const float c = cum[p];
+  const float mo = m[p];
+  const uint32_t v = pair_vox[p];
+  if (!(c > kCumLenGate)) return;  // gvdbkernels.cu:408: the pair never updates
+  float a = clampf(acc / c, kFEps, 1.0f - kFEps);
+  float mn = logf(a) - logf(1.0f - a);
+  m[p] = mn;
+  if (jacobi) {
+    dm[p] = mn - mo;
+    return;
+  }
+  float Lv = L[v] + (mn - mo);
+  L[v] = Lv;
+  belief[v] = 1.0f - clampf(1.0f / (1.0f + expf(Lv)), kFEps, 1.0f - kFEps);
+}
+
+__global__ void __launch_bounds__(kTileThreads, 8)
     k_pair_reduce(const uint32_t* __restrict__ perm, const uint32_t* __restrict__ skey,
                   const float* __restrict__ pl, uint32_t k0, uint32_t k1,
-                  TileCarry* __restrict__ carry, float* __restrict__ acc) {
+                  TileCarry* __restrict__ carry, const uint32_t* __restrict__ pair_vox,
+                  float* __restrict__ m, const float* __restrict__ cum, float* __restrict__ L,
+                  float* __restrict__ belief, float* __restrict__ dm, int jacobi) {
   __shared__ uint32_t sk[kTile];
-  __shared__ float sv[kTile];
+  __shared__ float sv[kTile];  // messages, then (after a barrier) segment sums
   __shared__ SegAgg wagg[kTileThreads / 32];
   __shared__ uint32_t nb_key[2];
   const int t = threadIdx.x, lane = t & 31, w = t >> 5;
@@ -358,6 +383,8 @@ __global__ void __launch_bounds__(kTileThreads)
   if (t == 1) nb_key[1] = base + n < k1 ? skey[base + n] : 0xFFFFFFFFu;
   __syncthreads();
   const uint32_t prev_key = nb_key[0], next_key = nb_key[1];
+  const uint32_t key0 = sk[0], keyn = sk[n - 1];
+  const bool open_start = key0 == prev_key, open_end = keyn == next_key;
   // this thread's 4 consecutive positions
   uint32_t key[4];
   float v[4], s[4];
@@ -374,7 +401,8 @@ __global__ void __launch_bounds__(kTileThreads)
 #pragma unroll
   for (int j = 1; j < 4; ++j) s[j] = h[j] ? v[j] : s[j - 1] + v[j];
   SegAgg agg{s[3], h[0] || h[1] || h[2] || h[3]};
-  // warp-level exclusive segmented scan of the thread aggregates
+  float* ssum = sv;  // sv is dead once every thread holds its 4 values
+  // warp-level inclusive segmented scan of the thread aggregates
   SegAgg inc = agg;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
@@ -389,7 +417,8 @@ __global__ void __launch_bounds__(kTileThreads)
   SegAgg exb{0.0f, false};
   for (int i = 0; i < w; ++i) exb = seg_combine(exb, wagg[i]);
   SegAgg ex = lane == 0 ? exb : seg_combine(exb, exw);
-  // inclusive sums from each segment's first position inside the tile
+  // inclusive sums from each segment's first position inside the tile; the
+  // last position of a segment records the segment's sum
   bool head_seen = false;
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
@@ -397,21 +426,20 @@ __global__ void __launch_bounds__(kTileThreads)
     float sj = head_seen ? s[j] : ex.s + s[j];
     if (!valid[j]) continue;
     int i = 4 * t + j;
-    bool last = (i == n - 1) || (sk[i + 1] != key[j]);
-    if (!last) continue;
-    // does the segment continue beyond the tile, and did it start before it?
-    // (keys are sorted, so a segment holds position 0 iff its key is sk[0])
-    bool open_end = (i == n - 1) && key[j] == next_key;
-    bool open_start = key[j] == sk[0] && sk[0] == prev_key;
-    if (!open_start && !open_end) {
-      acc[key[j]] = sj;
+    if (!((i == n - 1) || (sk[i + 1] != key[j]))) continue;
+    // keys are sorted and contiguous, so key - key0 indexes the tile's pairs;
+    // only the first segment can be open at the start, the last at the end
+    const bool seg_open_start = open_start && key[j] == key0;
+    const bool seg_open_end = open_end && i == n - 1;
+    if (!seg_open_start && !seg_open_end) {
+      ssum[key[j] - key0] = sj;
     } else {
       TileCarry& c = carry[blockIdx.x];
-      if (open_start) {
+      if (seg_open_start) {
         c.first_key = key[j];
         c.first_sum = sj;
       }
-      if (open_end) {
+      if (seg_open_end) {
         c.last_key = key[j];
         c.last_sum = sj;
       }
@@ -419,17 +447,27 @@ __global__ void __launch_bounds__(kTileThreads)
   }
   if (t == 0) {
     uint32_t f = 0;
-    if (sk[0] == prev_key) f |= kOpenStart;
-    if (sk[n - 1] == next_key) f |= kOpenEnd;
-    if (sk[0] == sk[n - 1]) f |= kSingle;  // sorted keys: equal ends => one segment
+    if (open_start) f |= kOpenStart;
+    if (open_end) f |= kOpenEnd;
+    if (key0 == keyn) f |= kSingle;  // sorted keys: equal ends => one segment
     carry[blockIdx.x].flags = f;
+  }
+  __syncthreads();
+  // update the pairs whose segments lie inside the tile
+  const uint32_t np = keyn - key0 + 1;
+  for (uint32_t q = t; q < np; q += kTileThreads) {
+    const uint32_t p = key0 + q;
+    if ((open_start && p == key0) || (open_end && p == keyn)) continue;
+    apply_pair(p, ssum[q], pair_vox, m, cum, L, belief, dm, jacobi);
   }
 }
 
 // segments crossing tile edges: the tile where such a segment starts walks
 // forward adding each following tile's partial, in tile order
 __global__ void k_pair_fixup(const TileCarry* __restrict__ carry, uint32_t ntiles,
-                             float* __restrict__ acc) {
+                             const uint32_t* __restrict__ pair_vox, float* __restrict__ m,
+                             const float* __restrict__ cum, float* __restrict__ L,
+                             float* __restrict__ belief, float* __restrict__ dm, int jacobi) {
   uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ntiles) return;
   TileCarry c = carry[t];
@@ -443,36 +481,7 @@ __global__ void k_pair_fixup(const TileCarry* __restrict__ carry, uint32_t ntile
     if ((d.flags & kSingle) && (d.flags & kOpenEnd)) continue;
     break;
   }
-  acc[key] = sum;
-}
-
-// factor->voxel update per pair (gvdbkernels.cu:457-479): pairs are in voxel
-// order, so every access here streams
-__global__ void __launch_bounds__(256) k_pair_apply(uint32_t p0, uint32_t p1,
-                                                    const float* __restrict__ acc,
-                                                    const uint32_t* __restrict__ pair_vox,
-                                                    float* __restrict__ m,
-                                                    const float* __restrict__ cum,
-                                                    float* __restrict__ L,
-                                                    float* __restrict__ belief,
-                                                    float* __restrict__ dm, int jacobi) {
-  uint32_t p = p0 + blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= p1) return;
-  float c = cum[p];
-  float a0 = acc[p];
-  float mo = m[p];
-  uint32_t v = pair_vox[p];
-  if (!(c > kCumLenGate)) return;  // gvdbkernels.cu:408: pair never updates
-  float a = clampf(a0 / c, kFEps, 1.0f - kFEps);
-  float mn = logf(a) - logf(1.0f - a);
-  m[p] = mn;
-  if (jacobi) {
-    dm[p] = mn - mo;
-    return;
-  }
-  float Lv = L[v] + (mn - mo);
-  L[v] = Lv;
-  belief[v] = 1.0f - clampf(1.0f / (1.0f + expf(Lv)), kFEps, 1.0f - kFEps);
+  apply_pair(key, sum, pair_vox, m, cum, L, belief, dm, jacobi);
 }
 
 // Jacobi: total log-odds of each voxel moves by the sum of its cameras'
@@ -606,18 +615,16 @@ cudaError_t launch_ray_keys(const RayMeta* meta, uint32_t n, uint32_t* keys, uin
 
 cudaError_t launch_pair_update(const BpArrays& a, uint32_t k0, uint32_t k1, uint32_t p0, uint32_t p1,
                                TileCarry* carry, int jacobi, cudaStream_t s) {
-  if (k1 > k0) {
-    uint32_t ntiles = (k1 - k0 + kTile - 1) / kTile;
-    k_pair_reduce<<<ntiles, kTileThreads, 0, s>>>(a.perm, a.skey, a.inc_pl, k0, k1, carry, a.pair_acc);
-    cudaError_t e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    k_pair_fixup<<<blocks(ntiles, 256), 256, 0, s>>>(carry, ntiles, a.pair_acc);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-  }
-  if (p1 <= p0) return cudaSuccess;
-  k_pair_apply<<<blocks(p1 - p0, 256), 256, 0, s>>>(p0, p1, a.pair_acc, a.pair_vox, a.pair_m,
-                                                    a.pair_cum, a.L, a.belief, a.pair_dm, jacobi);
+  (void)p0;
+  (void)p1;
+  if (k1 <= k0) return cudaSuccess;
+  uint32_t ntiles = (k1 - k0 + kTile - 1) / kTile;
+  k_pair_reduce<<<ntiles, kTileThreads, 0, s>>>(a.perm, a.skey, a.inc_pl, k0, k1, carry, a.pair_vox,
+                                                a.pair_m, a.pair_cum, a.L, a.belief, a.pair_dm, jacobi);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_pair_fixup<<<blocks(ntiles, 256), 256, 0, s>>>(carry, ntiles, a.pair_vox, a.pair_m, a.pair_cum,
+                                                   a.L, a.belief, a.pair_dm, jacobi);
   return cudaGetLastError();
 }
 

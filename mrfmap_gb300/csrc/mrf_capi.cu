@@ -111,7 +111,7 @@ struct mrf_map {
   std::vector<View> views;
   // arenas
   DBuf meta, inc_pair, inc_len, inc_mu, inc_pl, pair_vox, pair_m, pair_cum, pair_q, pair_dm,
-      pair_seg, perm, skey, carry, pair_acc, ray_order, counters;
+      pair_seg, perm, skey, carry, ray_order, counters;
   int64_t n_inc = 0, n_pairs = 0, n_perm = 0;
   // jacobi voxel CSR
   DBuf vseg, vpairs, vvox;
@@ -143,7 +143,6 @@ struct mrf_map {
     a.pair_cum = pair_cum.as<float>();
     a.pair_lnq = pair_q.as<float>();
     a.pair_dm = pair_dm.as<float>();
-    a.pair_acc = pair_acc.as<float>();
     a.pair_seg = pair_seg.as<uint32_t>();
     a.perm = perm.as<uint32_t>();
     a.skey = skey.as<uint32_t>();
@@ -385,7 +384,6 @@ void rebuild(mrf_map* m) {
   m->pair_seg.reserve(pb * 4, true, m->stream);
   m->pair_q.reserve(pb * 4, false, m->stream);
   m->pair_dm.reserve(pb * 4, false, m->stream);
-  m->pair_acc.reserve(pb * 4, false, m->stream);
   CK(launch_fill_f32(m->pair_m.as<float>(), pair_total, 0.0f, m->stream));
   {
     // tile carries of the pair update: enough for any view or all of them
@@ -521,7 +519,7 @@ void enqueue_iteration(mrf_map* m, const BpArrays& a, bool jacobi, int fix, Prof
       CK(launch_pair_update(a, v.perm_base, v.perm_base + v.n_perm, v.pair_base,
                             v.pair_base + v.n_pairs, m->carry.as<TileCarry>(), 0, m->stream));
       prof.end();
-      launches += 5;
+      launches += 4;
     }
   } else {
     uint32_t P = (uint32_t)m->n_pairs;
@@ -543,7 +541,7 @@ void enqueue_iteration(mrf_map* m, const BpArrays& a, bool jacobi, int fix, Prof
                           m->n_vvox, m->pair_dm.as<float>(), m->d_L.as<float>(),
                           m->d_belief.as<float>(), m->stream));
     prof.end();
-    launches += 6;
+    launches += 5;
   }
 }
 
@@ -685,7 +683,7 @@ void destroy_bufs(mrf_map* m) {
   DBuf* all[] = {&m->d_sigma, &m->d_bias, &m->d_slot, &m->d_coord, &m->d_L, &m->d_belief,
                  &m->meta, &m->inc_pair, &m->inc_len, &m->inc_mu, &m->inc_pl, &m->pair_vox,
                  &m->pair_m, &m->pair_cum, &m->pair_q, &m->pair_dm, &m->pair_seg, &m->perm,
-                 &m->skey, &m->carry, &m->pair_acc, &m->ray_order, &m->counters,
+                 &m->skey, &m->carry, &m->ray_order, &m->counters,
                  &m->vseg, &m->vpairs, &m->vvox, &m->s_postlen, &m->s_flags, &m->s_ind, &m->s_scan,
                  &m->s_tmp, &m->s_counts, &m->s_offs, &m->s_vox, &m->s_k0, &m->s_k1, &m->s_v0,
                  &m->s_v1, &m->s_seg, &m->s_dense, &m->s_err, &m->s_depth_in, &m->s_depth,

@@ -110,7 +110,6 @@ struct BpArrays {
   const float* pair_cum;
   float* pair_lnq;
   float* pair_dm;
-  float* pair_acc;         // sum of p*l per pair (pair update scratch)
   const uint32_t* pair_seg;
   const uint32_t* skey;  // pair id of each pair-grouped position
   float* L;
