@@ -302,6 +302,54 @@ def run_ours(args):
     else:
         e2e_t, e2e_val = None, None
 
+    # per-view likelihood of every keyframe under the final map (device buffers)
+    like = None
+    try:
+        m.reset_state()
+        m.infer(iters=iters)
+        img = torch.empty(w.params.rows * w.params.cols, device="cuda")
+        sums = torch.empty(len(w.poses), device="cuda")
+        for k in range(2):  # warm-up
+            m.likelihood_device(w.poses[k], dev_depths[k].data_ptr(), img.data_ptr(), sums[k:].data_ptr())
+        m.synchronize()
+        l0 = torch.cuda.Event(enable_timing=True)
+        l1 = torch.cuda.Event(enable_timing=True)
+        l0.record(stream)
+        for k in range(len(w.poses)):
+            m.likelihood_device(w.poses[k], dev_depths[k].data_ptr(), img.data_ptr(), sums[k:].data_ptr())
+        l1.record(stream)
+        m.synchronize()
+        lms = l0.elapsed_time(l1)
+        like = {"frames_per_s": len(w.poses) / (lms / 1e3), "ms_per_frame": lms / len(w.poses),
+                "rays_per_frame": w.params.rows * w.params.cols}
+    except Exception as e:  # reported, not fatal
+        like = {"error": str(e)}
+
+    # belief error against the FP64 oracle on the small-room workload
+    parity = None
+    if rank == 0 and not args.no_cpu_baseline:
+        try:
+            from mrfmap_gb300 import synthetic
+            from oracle import oracle as O
+            ws = synthetic.small_room(0)
+            gm = L.MRFMap(ws.params, activation=act)
+            om = O.OracleMap(ws.params, threads=os.cpu_count() or 1)
+            for P, D in zip(ws.poses, ws.depths):
+                gm.add_view(P, D)
+                om.add_view(P, D, O.ACT_FULL_RAY if act == L.ACT_FULL_RAY else O.ACT_ENDPOINT)
+            gm.infer()
+            om.infer()
+            gb, ob = gm.beliefs().astype(np.float64), om.beliefs()
+            touched = (gb > 0) | (ob > 0)
+            parity = {"workload": ws.name, "iters": ws.params.max_iters,
+                      "max_abs_belief_err": float(np.abs(gb - ob).max()),
+                      "class_agreement_at_0.5": float(((gb > 0.5) == (ob > 0.5))[touched].mean()),
+                      "reference": "FP64 CPU oracle"}
+            gm.close()
+            om.close()
+        except Exception as e:
+            parity = {"error": str(e)}
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         threads = os.cpu_count() or 1
@@ -333,6 +381,8 @@ def run_ours(args):
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h, "s_per_step": e2e_t},
             "cpu_baseline": cpu,
+            "likelihood": like,
+            "parity_vs_fp64": parity,
         }
         print(json.dumps(line))
     m.close()

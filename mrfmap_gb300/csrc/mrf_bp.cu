@@ -315,26 +315,18 @@ __global__ void k_ray_keys(const RayMeta* __restrict__ meta, uint32_t n, uint32_
 }
 
 // Pair update: a load-balanced segmented reduction over the pair-grouped
-// permutation of the messages, fused with the per-pair update.  Tiles of
-// kTile consecutive positions are summed by one block each (coalesced reads
-// of the permutation and the pair ids, kTile independent gathers of p*l in
-// flight); pairs whose segment lies inside the tile are then updated by the
-// block's threads in parallel; segments that cross tile edges leave partial
-// sums that k_pair_fixup adds in tile order.  Any segment length balances
-// (voxels next to the camera are crossed by thousands of rays) and the
-// summation order is fixed.
+// permutation of the messages, fused with the per-pair update.  One block
+// takes a tile of kTile consecutive positions: it gathers the tile's messages
+// into shared memory (coalesced permutation reads, kTile independent gathers
+// in flight) together with the segment bounds of the pairs the tile
+// touches; each thread then sums whole pairs sequentially from shared memory
+// (a fixed order) and updates the pairs that lie inside the tile.  Segments
+// that cross tile edges leave partial sums that k_pair_fixup adds in tile
+// order.  Any segment length balances: voxels next to the camera are crossed
+// by thousands of rays.
 constexpr int kTileThreads = 256;
 constexpr int kTile = 4 * kTileThreads;
 constexpr uint32_t kOpenStart = 1u, kOpenEnd = 2u, kSingle = 4u;
-
-struct SegAgg {
-  float s;
-  bool f;  // a segment head lies inside
-};
-
-__device__ __forceinline__ SegAgg seg_combine(SegAgg a, SegAgg b) {
-  return SegAgg{b.f ? b.s : a.s + b.s, a.f || b.f};
-}
 
 // factor->voxel update of one pair (gvdbkernels.cu:457-479)
 __device__ __forceinline__ void apply_pair(uint32_t p, float acc, const uint32_t* __restrict__ pair_vox,
@@ -358,108 +350,81 @@ __device__ __forceinline__ void apply_pair(uint32_t p, float acc, const uint32_t
 }
 
 __global__ void __launch_bounds__(kTileThreads, 8)
-    k_pair_reduce(const uint32_t* __restrict__ perm, const uint32_t* __restrict__ skey,
-                  const float* __restrict__ pl, uint32_t k0, uint32_t k1,
-                  TileCarry* __restrict__ carry, const uint32_t* __restrict__ pair_vox,
-                  float* __restrict__ m, const float* __restrict__ cum, float* __restrict__ L,
-                  float* __restrict__ belief, float* __restrict__ dm, int jacobi) {
-  __shared__ uint32_t sk[kTile];
-  __shared__ float sv[kTile];  // messages, then (after a barrier) segment sums
-  __shared__ SegAgg wagg[kTileThreads / 32];
-  __shared__ uint32_t nb_key[2];
-  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    k_pair_reduce(const uint32_t* __restrict__ perm, const float* __restrict__ pl,
+                  const uint32_t* __restrict__ seg, const uint32_t* __restrict__ tile_first,
+                  uint32_t k0, uint32_t k1, uint32_t p_end, TileCarry* __restrict__ carry,
+                  const uint32_t* __restrict__ pair_vox, float* __restrict__ m,
+                  const float* __restrict__ cum, float* __restrict__ L, float* __restrict__ belief,
+                  float* __restrict__ dm, int jacobi) {
+  __shared__ float sv[kTile];
+  __shared__ uint32_t sseg[kTile + 2];
+  const int t = threadIdx.x;
   const uint32_t base = k0 + blockIdx.x * kTile;
-  const int n = (int)min((uint32_t)kTile, k1 - base);
+  const uint32_t n = min((uint32_t)kTile, k1 - base);
+  const uint32_t end = base + n;
+  const uint32_t pf = tile_first[blockIdx.x];
+  // a tile touches at most n pairs: their starts and the next pair's start
+  const uint32_t nseg = min(n + 1, p_end - pf) + 1;
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
-    int i = j * kTileThreads + t;
-    if (i < n) {
-      uint32_t kk = base + i;
-      sk[i] = skey[kk];
-      sv[i] = pl[perm[kk]];
+    uint32_t i = j * kTileThreads + t;
+    if (i < n) sv[i] = pl[perm[base + i]];
+  }
+  for (uint32_t q = t; q < nseg; q += kTileThreads) sseg[q] = seg[pf + q];
+  __syncthreads();
+  for (uint32_t q = t; q < n && pf + q < p_end && sseg[q] < end; q += kTileThreads) {
+    const uint32_t s0 = sseg[q], s1 = sseg[q + 1];
+    const uint32_t a = max(s0, base) - base, b = min(s1, end) - base;
+    float acc = 0.0f;
+    for (uint32_t i = a; i < b; ++i) acc += sv[i];
+    const bool open_start = s0 < base, open_end = s1 > end;
+    if (!open_start && !open_end) {
+      apply_pair(pf + q, acc, pair_vox, m, cum, L, belief, dm, jacobi);
+      continue;
     }
-  }
-  if (t == 0) nb_key[0] = base > k0 ? skey[base - 1] : 0xFFFFFFFFu;
-  if (t == 1) nb_key[1] = base + n < k1 ? skey[base + n] : 0xFFFFFFFFu;
-  __syncthreads();
-  const uint32_t prev_key = nb_key[0], next_key = nb_key[1];
-  const uint32_t key0 = sk[0], keyn = sk[n - 1];
-  const bool open_start = key0 == prev_key, open_end = keyn == next_key;
-  // this thread's 4 consecutive positions
-  uint32_t key[4];
-  float v[4], s[4];
-  bool h[4], valid[4];
-#pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    int i = 4 * t + j;
-    valid[j] = i < n;
-    key[j] = valid[j] ? sk[i] : 0xFFFFFFFEu;
-    v[j] = valid[j] ? sv[i] : 0.0f;
-    h[j] = valid[j] && (i == 0 || sk[i - 1] != key[j]);
-  }
-  s[0] = v[0];
-#pragma unroll
-  for (int j = 1; j < 4; ++j) s[j] = h[j] ? v[j] : s[j - 1] + v[j];
-  SegAgg agg{s[3], h[0] || h[1] || h[2] || h[3]};
-  float* ssum = sv;  // sv is dead once every thread holds its 4 values
-  // warp-level inclusive segmented scan of the thread aggregates
-  SegAgg inc = agg;
-#pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    float os = __shfl_up_sync(kFull, inc.s, o);
-    bool of = __shfl_up_sync(kFull, (int)inc.f, o) != 0;
-    if (lane >= o) inc = seg_combine(SegAgg{os, of}, inc);
-  }
-  SegAgg exw{__shfl_up_sync(kFull, inc.s, 1), __shfl_up_sync(kFull, (int)inc.f, 1) != 0};
-  if (lane == 0) exw = SegAgg{0.0f, false};
-  if (lane == 31) wagg[w] = inc;
-  __syncthreads();
-  SegAgg exb{0.0f, false};
-  for (int i = 0; i < w; ++i) exb = seg_combine(exb, wagg[i]);
-  SegAgg ex = lane == 0 ? exb : seg_combine(exb, exw);
-  // inclusive sums from each segment's first position inside the tile; the
-  // last position of a segment records the segment's sum
-  bool head_seen = false;
-#pragma unroll
-  for (int j = 0; j < 4; ++j) {
-    head_seen = head_seen || h[j];
-    float sj = head_seen ? s[j] : ex.s + s[j];
-    if (!valid[j]) continue;
-    int i = 4 * t + j;
-    if (!((i == n - 1) || (sk[i + 1] != key[j]))) continue;
-    // keys are sorted and contiguous, so key - key0 indexes the tile's pairs;
-    // only the first segment can be open at the start, the last at the end
-    const bool seg_open_start = open_start && key[j] == key0;
-    const bool seg_open_end = open_end && i == n - 1;
-    if (!seg_open_start && !seg_open_end) {
-      ssum[key[j] - key0] = sj;
-    } else {
-      TileCarry& c = carry[blockIdx.x];
-      if (seg_open_start) {
-        c.first_key = key[j];
-        c.first_sum = sj;
-      }
-      if (seg_open_end) {
-        c.last_key = key[j];
-        c.last_sum = sj;
-      }
+    TileCarry& c = carry[blockIdx.x];
+    if (open_start) {
+      c.first_key = pf + q;
+      c.first_sum = acc;
+    }
+    if (open_end) {
+      c.last_key = pf + q;
+      c.last_sum = acc;
     }
   }
   if (t == 0) {
+    // the first pair is open at the start iff it began before the tile; the
+    // last pair (the one holding position end-1) is open iff it goes on
+    // ql = last q with sseg[q] < end (binary search over the loaded starts)
+    uint32_t lo = 0, hi = min(n, p_end - pf);
+    while (hi - lo > 1) {
+      uint32_t mid = (lo + hi) >> 1;
+      if (sseg[mid] < end) lo = mid;
+      else hi = mid;
+    }
+    const uint32_t ql = lo;
     uint32_t f = 0;
-    if (open_start) f |= kOpenStart;
-    if (open_end) f |= kOpenEnd;
-    if (key0 == keyn) f |= kSingle;  // sorted keys: equal ends => one segment
+    if (sseg[0] < base) f |= kOpenStart;
+    if (sseg[ql + 1] > end) f |= kOpenEnd;
+    if (ql == 0) f |= kSingle;
     carry[blockIdx.x].flags = f;
   }
-  __syncthreads();
-  // update the pairs whose segments lie inside the tile
-  const uint32_t np = keyn - key0 + 1;
-  for (uint32_t q = t; q < np; q += kTileThreads) {
-    const uint32_t p = key0 + q;
-    if ((open_start && p == key0) || (open_end && p == keyn)) continue;
-    apply_pair(p, ssum[q], pair_vox, m, cum, L, belief, dm, jacobi);
+}
+
+// first pair of every tile of a position range (pairs are sorted, so it is
+// the pair whose segment holds the tile's first position)
+__global__ void k_tile_first(const uint32_t* __restrict__ seg, uint32_t p0, uint32_t p1, uint32_t k0,
+                             uint32_t ntiles, uint32_t* __restrict__ out) {
+  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ntiles) return;
+  uint32_t pos = k0 + t * kTile;
+  uint32_t lo = p0, hi = p1;  // last p with seg[p] <= pos
+  while (hi - lo > 1) {
+    uint32_t mid = lo + ((hi - lo) >> 1);
+    if (seg[mid] <= pos) lo = mid;
+    else hi = mid;
   }
+  out[t] = lo;
 }
 
 // segments crossing tile edges: the tile where such a segment starts walks
@@ -614,17 +579,26 @@ cudaError_t launch_ray_keys(const RayMeta* meta, uint32_t n, uint32_t* keys, uin
 }
 
 cudaError_t launch_pair_update(const BpArrays& a, uint32_t k0, uint32_t k1, uint32_t p0, uint32_t p1,
-                               TileCarry* carry, int jacobi, cudaStream_t s) {
+                               const uint32_t* tile_first, TileCarry* carry, int jacobi,
+                               cudaStream_t s) {
   (void)p0;
-  (void)p1;
   if (k1 <= k0) return cudaSuccess;
   uint32_t ntiles = (k1 - k0 + kTile - 1) / kTile;
-  k_pair_reduce<<<ntiles, kTileThreads, 0, s>>>(a.perm, a.skey, a.inc_pl, k0, k1, carry, a.pair_vox,
-                                                a.pair_m, a.pair_cum, a.L, a.belief, a.pair_dm, jacobi);
+  k_pair_reduce<<<ntiles, kTileThreads, 0, s>>>(a.perm, a.inc_pl, a.pair_seg, tile_first, k0, k1, p1,
+                                                carry, a.pair_vox, a.pair_m, a.pair_cum, a.L,
+                                                a.belief, a.pair_dm, jacobi);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   k_pair_fixup<<<blocks(ntiles, 256), 256, 0, s>>>(carry, ntiles, a.pair_vox, a.pair_m, a.pair_cum,
                                                    a.L, a.belief, a.pair_dm, jacobi);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tile_first(const uint32_t* seg, uint32_t p0, uint32_t p1, uint32_t k0, uint32_t k1,
+                              uint32_t* out, cudaStream_t s) {
+  if (k1 <= k0) return cudaSuccess;
+  uint32_t ntiles = (k1 - k0 + kTile - 1) / kTile;
+  k_tile_first<<<blocks(ntiles, 256), 256, 0, s>>>(seg, p0, p1, k0, ntiles, out);
   return cudaGetLastError();
 }
 

@@ -261,7 +261,7 @@ __global__ void __launch_bounds__(kThreads)
 // Pairs in voxel order.  The view's incidences are sorted by voxel id
 // (stable: increasing incidence index inside a voxel); each run of one voxel
 // is a (camera, voxel) pair.  perm[k] is the incidence at pair-grouped
-// position k and skey[k] its pair.
+// position k; seg[p] the first position of pair p.
 __global__ void k_vox_heads(const uint32_t* __restrict__ sk, uint32_t n, uint32_t* __restrict__ flag) {
   uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k < n) flag[k] = (k == 0 || sk[k] != sk[k - 1]) ? 1u : 0u;
@@ -272,8 +272,7 @@ __global__ void k_pairs_from_sorted(const uint32_t* __restrict__ sk, const uint3
                                     const uint32_t* __restrict__ scan, uint32_t n,
                                     uint32_t pair_base, uint32_t perm_base, uint32_t inc_base,
                                     uint32_t* __restrict__ pair_vox, uint32_t* __restrict__ seg,
-                                    uint32_t* __restrict__ skey, uint32_t* __restrict__ perm,
-                                    uint32_t* __restrict__ inc_pair) {
+                                    uint32_t* __restrict__ perm, uint32_t* __restrict__ inc_pair) {
   uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
   uint32_t p = pair_base + scan[k] + flag[k] - 1;
@@ -281,7 +280,6 @@ __global__ void k_pairs_from_sorted(const uint32_t* __restrict__ sk, const uint3
     pair_vox[p] = sk[k];
     seg[p] = perm_base + k;
   }
-  skey[perm_base + k] = p;
   uint32_t i = inc_base + sidx[k];
   perm[perm_base + k] = i;
   inc_pair[i] = p;
@@ -376,11 +374,11 @@ cudaError_t launch_vox_heads(const uint32_t* sk, uint32_t n, uint32_t* flag, cud
 cudaError_t launch_pairs_from_sorted(const uint32_t* sk, const uint32_t* sidx, const uint32_t* flag,
                                      const uint32_t* scan, uint32_t n, uint32_t pair_base,
                                      uint32_t perm_base, uint32_t inc_base, uint32_t* pair_vox,
-                                     uint32_t* seg, uint32_t* skey, uint32_t* perm,
-                                     uint32_t* inc_pair, cudaStream_t s) {
+                                     uint32_t* seg, uint32_t* perm, uint32_t* inc_pair,
+                                     cudaStream_t s) {
   if (!n) return cudaSuccess;
   k_pairs_from_sorted<<<grid_for(n), kThreads, 0, s>>>(sk, sidx, flag, scan, n, pair_base, perm_base,
-                                                       inc_base, pair_vox, seg, skey, perm, inc_pair);
+                                                       inc_base, pair_vox, seg, perm, inc_pair);
   return cudaGetLastError();
 }
 

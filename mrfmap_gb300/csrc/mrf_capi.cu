@@ -87,6 +87,7 @@ struct View {
   uint32_t pair_base = 0, n_pairs = 0;
   uint32_t perm_base = 0, n_perm = 0;
   uint32_t order_base = 0, n_active = 0;  // ray queue (longest first)
+  uint32_t tile_base = 0;                 // first pair of each pair-update tile
 };
 
 uint32_t u32_checked(int64_t v, const char* what) {
@@ -111,7 +112,8 @@ struct mrf_map {
   std::vector<View> views;
   // arenas
   DBuf meta, inc_pair, inc_len, inc_mu, inc_pl, pair_vox, pair_m, pair_cum, pair_q, pair_dm,
-      pair_seg, perm, skey, carry, ray_order, counters;
+      pair_seg, perm, carry, ray_order, counters, tile_first;
+  uint32_t jac_tile_base = 0;
   int64_t n_inc = 0, n_pairs = 0, n_perm = 0;
   // jacobi voxel CSR
   DBuf vseg, vpairs, vvox;
@@ -145,7 +147,6 @@ struct mrf_map {
     a.pair_dm = pair_dm.as<float>();
     a.pair_seg = pair_seg.as<uint32_t>();
     a.perm = perm.as<uint32_t>();
-    a.skey = skey.as<uint32_t>();
     a.L = d_L.as<float>();
     a.belief = d_belief.as<float>();
     return a;
@@ -266,7 +267,6 @@ void rebuild(mrf_map* m) {
   m->inc_mu.reserve(ib, false, m->stream);
   m->perm.reserve(ib, false, m->stream);
   m->inc_pl.reserve(ib, false, m->stream);
-  m->skey.reserve(ib, false, m->stream);
   m->s_vox.reserve(ib, false, m->stream);
   m->s_postlen.reserve(ib, false, m->stream);
   // 3. emit
@@ -337,8 +337,7 @@ void rebuild(mrf_map* m) {
     CK(launch_pairs_from_sorted(m->s_k1.as<uint32_t>(), m->s_v1.as<uint32_t>(), m->s_k0.as<uint32_t>(),
                                 m->s_v0.as<uint32_t>(), nr, v.pair_base, v.perm_base, v.inc_base,
                                 m->pair_vox.as<uint32_t>(), m->pair_seg.as<uint32_t>(),
-                                m->skey.as<uint32_t>(), m->perm.as<uint32_t>(),
-                                m->inc_pair.as<uint32_t>(), m->stream));
+                                m->perm.as<uint32_t>(), m->inc_pair.as<uint32_t>(), m->stream));
     CK(launch_fill_u32(m->pair_seg.as<uint32_t>() + v.pair_base + np, 1, v.perm_base + nr, m->stream));
     CK(launch_pair_cum(m->pair_seg.as<uint32_t>(), m->s_v1.as<uint32_t>(), v.pair_base, np,
                        v.perm_base, v.inc_base, m->s_postlen.as<float>(), m->pair_cum.as<float>(),
@@ -386,9 +385,24 @@ void rebuild(mrf_map* m) {
   m->pair_dm.reserve(pb * 4, false, m->stream);
   CK(launch_fill_f32(m->pair_m.as<float>(), pair_total, 0.0f, m->stream));
   {
-    // tile carries of the pair update: enough for any view or all of them
+    // tile carries of the pair update: enough for any view or all of them;
+    // first pair of every tile, per view (Gauss-Seidel) and over all views
+    // (Jacobi)
     int64_t tiles = (int64_t)pair_update_tiles((uint32_t)std::min<int64_t>(perm_total, 0xFFFFFFF0ll)) + V + 1;
     m->carry.reserve((size_t)tiles * sizeof(TileCarry), false, m->stream);
+    m->tile_first.reserve((size_t)(2 * tiles + 2) * 4, false, m->stream);
+    uint32_t tb = 0;
+    for (int c = 0; c < V; ++c) {
+      View& v = m->views[c];
+      v.tile_base = tb;
+      CK(launch_tile_first(m->pair_seg.as<uint32_t>(), v.pair_base, v.pair_base + v.n_pairs,
+                           v.perm_base, v.perm_base + v.n_perm, m->tile_first.as<uint32_t>() + tb,
+                           m->stream));
+      tb += pair_update_tiles(v.n_perm);
+    }
+    m->jac_tile_base = tb;
+    CK(launch_tile_first(m->pair_seg.as<uint32_t>(), 0, (uint32_t)pair_total, 0, (uint32_t)perm_total,
+                         m->tile_first.as<uint32_t>() + tb, m->stream));
   }
   // 5. carry messages of every camera over to its new pairs
   if (remap) {
@@ -517,7 +531,8 @@ void enqueue_iteration(mrf_map* m, const BpArrays& a, bool jacobi, int fix, Prof
       prof.end();
       prof.begin(2);
       CK(launch_pair_update(a, v.perm_base, v.perm_base + v.n_perm, v.pair_base,
-                            v.pair_base + v.n_pairs, m->carry.as<TileCarry>(), 0, m->stream));
+                            v.pair_base + v.n_pairs, m->tile_first.as<uint32_t>() + v.tile_base,
+                            m->carry.as<TileCarry>(), 0, m->stream));
       prof.end();
       launches += 4;
     }
@@ -534,7 +549,9 @@ void enqueue_iteration(mrf_map* m, const BpArrays& a, bool jacobi, int fix, Prof
                      m->num_sms, m->stream));
     prof.end();
     prof.begin(2);
-    CK(launch_pair_update(a, 0, (uint32_t)m->n_perm, 0, P, m->carry.as<TileCarry>(), 1, m->stream));
+    CK(launch_pair_update(a, 0, (uint32_t)m->n_perm, 0, P,
+                          m->tile_first.as<uint32_t>() + m->jac_tile_base, m->carry.as<TileCarry>(),
+                          1, m->stream));
     prof.end();
     prof.begin(3);
     CK(launch_voxel_apply(m->vseg.as<uint32_t>(), m->vpairs.as<uint32_t>(), m->vvox.as<uint32_t>(),
@@ -683,7 +700,7 @@ void destroy_bufs(mrf_map* m) {
   DBuf* all[] = {&m->d_sigma, &m->d_bias, &m->d_slot, &m->d_coord, &m->d_L, &m->d_belief,
                  &m->meta, &m->inc_pair, &m->inc_len, &m->inc_mu, &m->inc_pl, &m->pair_vox,
                  &m->pair_m, &m->pair_cum, &m->pair_q, &m->pair_dm, &m->pair_seg, &m->perm,
-                 &m->skey, &m->carry, &m->ray_order, &m->counters,
+                 &m->carry, &m->ray_order, &m->counters, &m->tile_first,
                  &m->vseg, &m->vpairs, &m->vvox, &m->s_postlen, &m->s_flags, &m->s_ind, &m->s_scan,
                  &m->s_tmp, &m->s_counts, &m->s_offs, &m->s_vox, &m->s_k0, &m->s_k1, &m->s_v0,
                  &m->s_v1, &m->s_seg, &m->s_dense, &m->s_err, &m->s_depth_in, &m->s_depth,

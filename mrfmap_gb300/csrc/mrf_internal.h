@@ -80,8 +80,8 @@ cudaError_t launch_vox_heads(const uint32_t* sk, uint32_t n, uint32_t* flag, cud
 cudaError_t launch_pairs_from_sorted(const uint32_t* sk, const uint32_t* sidx, const uint32_t* flag,
                                      const uint32_t* scan, uint32_t n, uint32_t pair_base,
                                      uint32_t perm_base, uint32_t inc_base, uint32_t* pair_vox,
-                                     uint32_t* seg, uint32_t* skey, uint32_t* perm,
-                                     uint32_t* inc_pair, cudaStream_t s);
+                                     uint32_t* seg, uint32_t* perm, uint32_t* inc_pair,
+                                     cudaStream_t s);
 cudaError_t launch_pair_cum(const uint32_t* seg, const uint32_t* sidx, uint32_t p0, uint32_t np,
                             uint32_t perm_base, uint32_t inc_base, const float* post_len, float* cum,
                             cudaStream_t s);
@@ -111,7 +111,6 @@ struct BpArrays {
   float* pair_lnq;
   float* pair_dm;
   const uint32_t* pair_seg;
-  const uint32_t* skey;  // pair id of each pair-grouped position
   float* L;
   float* belief;
 };
@@ -132,8 +131,12 @@ cudaError_t launch_ray_bp(const BpArrays& a, const uint32_t* order, uint32_t n_r
 cudaError_t launch_ray_keys(const RayMeta* meta, uint32_t n, uint32_t* keys, uint32_t* vals,
                             cudaStream_t s);
 // k0..k1: range of sorted (pair-grouped) positions
+// positions k0..k1 hold the pairs p0..p1; tile_first from launch_tile_first
 cudaError_t launch_pair_update(const BpArrays& a, uint32_t k0, uint32_t k1, uint32_t p0, uint32_t p1,
-                               TileCarry* carry, int jacobi, cudaStream_t s);
+                               const uint32_t* tile_first, TileCarry* carry, int jacobi,
+                               cudaStream_t s);
+cudaError_t launch_tile_first(const uint32_t* seg, uint32_t p0, uint32_t p1, uint32_t k0, uint32_t k1,
+                              uint32_t* out, cudaStream_t s);
 cudaError_t launch_voxel_apply(const uint32_t* vseg, const uint32_t* vpairs, const uint32_t* vvox,
                                uint32_t nvox, const float* pair_dm, float* L, float* belief,
                                cudaStream_t s);
