@@ -198,11 +198,16 @@ def run_reference(args):
     print(json.dumps(line))
 
 
+# bumped whenever k_ray_bp's memory traffic changes (profiles/ray_bp_traffic.json)
+RAY_KERNEL_VERSION = 2
+
+
 def ray_kernel_bytes(st, iters):
-    """Algorithmic bytes of the ray-message kernel for one launch-sum:
-    per Pre incidence 20 B (pair id 4, length 4, potential 4, (q, ln q) 8),
-    per Post incidence +4 B (message write), per ray 16 B of metadata."""
-    return (20 * st["n_inc_pre"] + 4 * st["n_inc_post"] + 16 * st["n_rays"]) * iters
+    """Algorithmic bytes of the ray-message kernel for one launch-sum: per
+    Pre incidence 12 B (pair id 4, length 4, ln q gather 4); per dynamic
+    incidence (from the ray's first non-zero potential on) +8 B (potential
+    4, message write 4); per ray 16 B of metadata."""
+    return (12 * st["n_inc_pre"] + 8 * st["n_inc_dyn"] + 16 * st["n_rays"]) * iters
 
 
 def run_ours(args):
@@ -270,8 +275,10 @@ def run_ours(args):
     if os.path.exists(tfile):
         try:
             t = json.load(open(tfile))
-            if t.get("workload") == w.name and t.get("activation") == args.policy:
-                traffic = t["bytes_per_launch"]
+            if t.get("kernel_version") == RAY_KERNEL_VERSION and t.get("activation") == args.policy:
+                # DRAM bytes per Pre incidence from a capture of the same
+                # kernel on a smaller case, scaled by this launch's incidences
+                traffic = t["dram_bytes_per_pre_incidence"] * prof["n_inc_pre"] * iters / k_n
         except Exception:
             pass
     kernel_share = {n: round(v / max(sum(prof["kernel_ms"]), 1e-9), 4)
@@ -331,17 +338,17 @@ def run_ours(args):
         try:
             from mrfmap_gb300 import synthetic
             from oracle import oracle as O
-            ws = synthetic.small_room(0)
-            gm = L.MRFMap(ws.params, activation=act)
-            om = O.OracleMap(ws.params, threads=os.cpu_count() or 1)
-            for P, D in zip(ws.poses, ws.depths):
+            wsm = synthetic.small_room(0)
+            gm = L.MRFMap(wsm.params, activation=act)
+            om = O.OracleMap(wsm.params, threads=os.cpu_count() or 1)
+            for P, D in zip(wsm.poses, wsm.depths):
                 gm.add_view(P, D)
                 om.add_view(P, D, O.ACT_FULL_RAY if act == L.ACT_FULL_RAY else O.ACT_ENDPOINT)
             gm.infer()
             om.infer()
             gb, ob = gm.beliefs().astype(np.float64), om.beliefs()
             touched = (gb > 0) | (ob > 0)
-            parity = {"workload": ws.name, "iters": ws.params.max_iters,
+            parity = {"workload": wsm.name, "iters": wsm.params.max_iters,
                       "max_abs_belief_err": float(np.abs(gb - ob).max()),
                       "class_agreement_at_0.5": float(((gb > 0.5) == (ob > 0.5))[touched].mean()),
                       "reference": "FP64 CPU oracle"}
@@ -367,7 +374,8 @@ def run_ours(args):
             "data": "synthetic (seeded room scenes; no public dataset)",
             "config": {"workload": w.name, "activation": args.policy, "iters": iters,
                        "views": len(w.poses), "seed": w.seed, "n_inc_per_iter": st["n_inc_post"],
-                       "n_inc_pre_per_iter": st["n_inc_pre"], "n_pairs": st["n_pairs"],
+                       "n_inc_pre_per_iter": st["n_inc_pre"], "n_inc_dyn_per_iter": st["n_inc_dyn"],
+                       "n_pairs": st["n_pairs"], "n_pairs_dyn": st["n_pairs_dyn"],
                        "n_rays": st["n_rays"], "n_bricks": st["n_bricks"],
                        "l2": "inputs larger than L2 (no flush)",
                        "parallelism": f"replicas{ws}" if ws > 1 else "single"},

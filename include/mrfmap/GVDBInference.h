@@ -27,6 +27,10 @@ class GVDBInference {
   float get_likelihood_image(unsigned id, float* out_rowmajor);
   float get_likelihood_image_at_pose(const float* pose, const std::shared_ptr<GVDBImage>& img,
                                      float* out_rowmajor);
+  // evaluation renders (src/GVDBInference.cpp:242-247, 385-429)
+  void get_expected_depth_image(unsigned id, float* out_rowmajor);
+  float get_accuracy_image_at_pose(const float* pose, const std::shared_ptr<GVDBImage>& img,
+                                   float* out_rowmajor);
   std::vector<float> get_occupied_bricks(int lev) { return map_->get_occupied_bricks(lev); }
   void get_alphas(float* out, int64_t rows, int64_t cols) { map_->get_alphas(out, rows, cols); }
   // debug selectors of the reference (printf probes); recorded, no effect

@@ -26,6 +26,17 @@ class GVDBMapLikelihoodEstimator {
                                      float* out_rowmajor);
   float get_likelihood_image_at_pose_with_depth(const float* pose, const float* depth,
                                                 float* out_rowmajor);
+  // evaluation renders (src/GVDBMapLikelihoodEstimator.cpp:328-434)
+  void get_accuracy_image(unsigned id, float* out_rowmajor);
+  float get_accuracy_image_at_pose(const float* pose, const std::shared_ptr<GVDBImage>& img,
+                                   float* out_rowmajor);
+  float get_accuracy_image_at_pose_with_depth(const float* pose, const float* depth,
+                                              float* out_rowmajor);
+  float get_simple_accuracy_at_pose(const float* pose, const std::shared_ptr<GVDBImage>& img);
+  float get_simple_accuracy_image_at_pose_with_depth(const float* pose, const float* depth,
+                                                     float* out_rowmajor);
+  void get_occ_thresh_image_at_pose(const float* pose, const std::shared_ptr<GVDBImage>& img,
+                                    float* out_rowmajor, float occ_thresh);
   std::vector<float> get_occupied_bricks(int lev) { return map_->get_occupied_bricks(lev); }
   void get_alphas(float* out, int64_t rows, int64_t cols) { map_->get_alphas(out, rows, cols); }
   void set_selected_x_y(unsigned, unsigned) {}

@@ -86,6 +86,9 @@ typedef struct mrf_stats {
    * [3] voxel apply (Jacobi) */
   double kernel_ms[4];
   int64_t kernel_count[4];
+  int64_t n_inc_dyn;       /* Post incidences from the first non-zero potential
+                              on: the messages recomputed every iteration */
+  int64_t n_pairs_dyn;     /* pairs holding at least one of them */
 } mrf_stats;
 
 /* Map construction: GVDBInference(...) + GVDBMRFMap::gpuAllocate
@@ -111,6 +114,15 @@ MRF_API mrf_status mrf_set_pose(mrf_map* map, int view_id, const float* pose);
  * zeroes the messages of the cameras in ids (unless MRF_INCREMENTAL) and
  * runs iters BP iterations over every camera. ids == NULL -> all cameras. */
 MRF_API mrf_status mrf_infer(mrf_map* map, const int* ids, int n_ids, int iters, int flags);
+/* mrf_infer run to convergence: iterations stop after the first one whose
+ * largest belief change (over every voxel) is below tol, checked every
+ * check_every iterations, with max_iters as the cap (<= 0: params.max_iters).
+ * The reference runs a fixed count (src/GVDBInference.cpp:155); this is
+ * what "time to converged map" is measured with.  iters_done and last_delta
+ * (the last measured change) may be NULL. */
+MRF_API mrf_status mrf_infer_converge(mrf_map* map, const int* ids, int n_ids, int max_iters,
+                                      float tol, int check_every, int flags, int* iters_done,
+                                      float* last_delta);
 /* Extension: log-odds back to the prior, beliefs to 0, messages to 0. */
 MRF_API mrf_status mrf_reset_state(mrf_map* map);
 
@@ -140,6 +152,30 @@ MRF_API mrf_status mrf_likelihood_device(mrf_map* map, const float* pose, const 
 MRF_API mrf_status mrf_likelihood_device_noalloc(mrf_map* map, const float* pose,
                                                  const float* depth_dev, float* out_img_dev,
                                                  float* out_sum_dev);
+
+/* Evaluation renders over the belief field (depth image on the host, image
+ * out on the host, rows*cols floats, may be NULL):
+ *  MRF_RENDER_EXPECTED_DEPTH  GVDBInference::get_expected_depth_image
+ *                             (src/GVDBInference.cpp:242-247)
+ *  MRF_RENDER_ACCURACY        get_accuracy_image_at_pose; score = fraction of
+ *                             labelled pixels with the density peak within
+ *                             1 sigma (src/GVDBInference.cpp:385-429)
+ *  MRF_RENDER_SIMPLE_ACCURACY get_simple_accuracy_at_pose with threshold
+ *                             (acc_thresh when < 0); score = (TP+TN)/pixels
+ *                             (src/GVDBMapLikelihoodEstimator.cpp:365-408)
+ *  MRF_RENDER_OCC_THRESH      get_occ_thresh_image_at_pose with threshold
+ *                             (occ_thresh when < 0)
+ *                             (src/GVDBMapLikelihoodEstimator.cpp:410-434)
+ * counts (may be NULL) receives the label histogram of -1, 0, 1, 2. */
+#define MRF_RENDER_EXPECTED_DEPTH 0
+#define MRF_RENDER_ACCURACY 1
+#define MRF_RENDER_SIMPLE_ACCURACY 2
+#define MRF_RENDER_OCC_THRESH 3
+MRF_API mrf_status mrf_render(mrf_map* map, int mode, const float* pose, const float* depth_host,
+                              float threshold, float* out_img, float* out_score, int64_t* counts);
+/* Same at a stored view's pose and depth image. */
+MRF_API mrf_status mrf_render_view(mrf_map* map, int mode, int view_id, float threshold,
+                                   float* out_img, float* out_score, int64_t* counts);
 
 /* GVDBMRFMap::get_occupied_bricks(0) (src/GVDBMRFMap.cpp:137-152). */
 MRF_API mrf_status mrf_num_bricks(mrf_map* map, int64_t* n_bricks);

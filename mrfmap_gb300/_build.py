@@ -27,7 +27,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
               "-Xcompiler", "-ffp-contract=off", "-Xcompiler", "-fvisibility=hidden"]
 
-CU_SOURCES = ["mrf_build.cu", "mrf_bp.cu", "mrf_like.cu", "mrf_capi.cu", "mrf_noalloc.cu"]
+CU_SOURCES = ["mrf_build.cu", "mrf_bp.cu", "mrf_like.cu", "mrf_capi.cu", "mrf_noalloc.cu",
+              "mrf_render.cu"]
 HEADERS = ["mrf_internal.h", "mrf_geometry.cuh", "mrf_like_pixel.cuh"]
 
 

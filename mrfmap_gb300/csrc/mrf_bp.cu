@@ -60,19 +60,22 @@ __global__ void k_pair_prepare(const uint32_t* __restrict__ pair_vox, const floa
 // lane plus one warp scan per chunk, and a lane keeps 8 gathers in flight.
 //
 // Pass 1 forms the visibility exponent A_i = sum_{j<=i} l_j ln q_j,
-// V_i = exp(A_i), q_i and the Pre total T; pass 2 turns (V_i mu_i, q_i, l_i)
-// and T into the messages p_i * l_i, written in ray order.  A ray of one chunk
-// keeps pass 1's values in registers; rays of up to four chunks stage them in
-// shared memory; longer rays recompute them in pass 2.  The tau sums of rays longer
-// than kLongRay are formed in FP64.
+// V_i = exp(A_i), q_i and the Pre total T over the whole ray.  Pass 2 turns
+// (V_i mu_i, q_i, l_i) and T into the messages p_i * l_i of the dynamic
+// range [k_dyn, n_post) only: before k_dyn every potential is zero, so
+// tau_i = 0, F_i = 0, mu1_i = 0 and p_i is exactly the clamp floor F_EPS
+// (static messages, summed once per build into the pairs).  Potentials are
+// loaded from k_dyn (rounded down to a vector) on.  A ray of one chunk keeps
+// pass 1's values in registers; longer rays recompute the dynamic range in
+// pass 2 from A_{k_dyn - 1}.  The tau sums of rays longer than kLongRay are
+// formed in FP64.
 //
 // Pre visibility restarts at r0 (the reference restores its carried state
 // only once the accumulated tau is non-zero, gvdbkernels.cu:708-715):
 // V^pre_i = exp(A_i - A_{r0-1}) = V_i * exp(-A_{r0-1}); Post uses V_i.
 constexpr int kRayWarps = 4;
 constexpr int kE = 8;                    // incidences per lane per chunk
-constexpr int kChunk = 32 * kE;          // 512
-constexpr int kStage = 4 * kChunk;       // incidences staged per warp
+constexpr int kChunk = 32 * kE;          // 256
 constexpr float kUnderflowGuard = -60.0f;
 
 template <typename T>
@@ -81,19 +84,17 @@ __device__ __forceinline__ T warp_excl_scan(T v, int lane) {
   return incl - v;
 }
 
-struct Stage {
-  float vmu[kStage], q[kStage];
-};
-
 // one lane's slice of a chunk
 struct Slice {
   float A[kE], q[kE], mu[kE], len[kE];
 };
 
-// loads a lane's kE incidences at i0 (those >= n read as zero), gathers
-// ln q, forms prefix exponents from carryA; returns the chunk total of l ln q
-__device__ __forceinline__ float load_slice(Slice& s, uint32_t off, int i0, int n, float carryA,
-                                            int lane, const uint32_t* __restrict__ inc_pair,
+// loads a lane's kE incidences at i0 (those >= n read as zero; potentials
+// below kmu, a multiple of 4, are known zeros and not loaded), gathers ln q,
+// forms prefix exponents from carryA; returns the chunk total of l ln q
+__device__ __forceinline__ float load_slice(Slice& s, uint32_t off, int i0, int n, int kmu,
+                                            float carryA, int lane,
+                                            const uint32_t* __restrict__ inc_pair,
                                             const float* __restrict__ inc_len,
                                             const float* __restrict__ inc_mu,
                                             const float* __restrict__ lnq) {
@@ -106,7 +107,7 @@ __device__ __forceinline__ float load_slice(Slice& s, uint32_t off, int i0, int 
     if (i < n) {
       p = __ldg(reinterpret_cast<const uint4*>(inc_pair + off + i));
       l = __ldg(reinterpret_cast<const float4*>(inc_len + off + i));
-      m = __ldg(reinterpret_cast<const float4*>(inc_mu + off + i));
+      if (i >= kmu) m = __ldg(reinterpret_cast<const float4*>(inc_mu + off + i));
     }
     pid[4 * v + 0] = p.x; pid[4 * v + 1] = p.y; pid[4 * v + 2] = p.z; pid[4 * v + 3] = p.w;
     s.len[4 * v + 0] = l.x; s.len[4 * v + 1] = l.y; s.len[4 * v + 2] = l.z; s.len[4 * v + 3] = l.w;
@@ -134,7 +135,7 @@ __device__ __forceinline__ float load_slice(Slice& s, uint32_t off, int i0, int 
   return __shfl_sync(kFull, ex + run, 31);
 }
 
-// A at chunk position idx (held by lane idx / kE)
+// A at chunk-relative index idx (0 <= idx < kChunk), broadcast to the warp
 __device__ __forceinline__ float slice_value(const Slice& s, int idx) {
   const int jj = idx % kE;
   float mine = 0.0f;
@@ -144,10 +145,11 @@ __device__ __forceinline__ float slice_value(const Slice& s, int idx) {
   return __shfl_sync(kFull, mine, idx / kE);
 }
 
-// pass 2 on one lane's slice: messages p*l for positions i0..i0+kE-1
+// pass 2 on one lane's slice: messages p*l for positions i0..i0+kE-1; the
+// 4-vectors inside [k4, n_post) are written (k4 a multiple of 4)
 template <typename Acc>
 __device__ __forceinline__ Acc emit_slice(const float (&vmu)[kE], const float (&q)[kE],
-                                          const float (&len)[kE], int i0, int n_pre, int n_post,
+                                          const float (&len)[kE], int i0, int k4, int n_post,
                                           Acc T, Acc carryF, int lane, uint32_t off,
                                           float* __restrict__ inc_pl) {
   float tau[kE], eloc[kE];
@@ -175,18 +177,19 @@ __device__ __forceinline__ Acc emit_slice(const float (&vmu)[kE], const float (&
     out[j] = (i0 + j < n_post) ? p * len[j] : 0.0f;
   }
 #pragma unroll
-  for (int v = 0; v < kE / 4; ++v)
-    if (i0 + 4 * v < n_pre)
-      *reinterpret_cast<float4*>(inc_pl + off + i0 + 4 * v) =
+  for (int v = 0; v < kE / 4; ++v) {
+    const int i = i0 + 4 * v;
+    if (i >= k4 && i < n_post)
+      *reinterpret_cast<float4*>(inc_pl + off + i) =
           make_float4(out[4 * v], out[4 * v + 1], out[4 * v + 2], out[4 * v + 3]);
+  }
   return carryF + (Acc)__shfl_sync(kFull, ex + run, 31);
 }
 
-// mode 0: one chunk (registers), 1: up to four chunks (shared-memory
-// stage), 2: longer (recompute in pass 2)
-template <int kMode, typename Acc>
-__device__ __forceinline__ void ray_bp_warp(const RayMeta& me, Stage& st,
-                                            const uint32_t* __restrict__ inc_pair,
+// kOne: the ray fits one chunk (pass 2 from registers); otherwise pass 2
+// recomputes the dynamic range
+template <bool kOne, typename Acc>
+__device__ __forceinline__ void ray_bp_warp(const RayMeta& me, const uint32_t* __restrict__ inc_pair,
                                             const float* __restrict__ inc_len,
                                             const float* __restrict__ inc_mu,
                                             const float* __restrict__ lnq, float* __restrict__ inc_pl,
@@ -194,17 +197,20 @@ __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, Stage& st,
   const int n_pre = me.n_pre, n_post = me.n_post;
   const int r0 = fix_reset ? 0 : me.r0;
   const int rinf = fix_reset ? 0 : me.rinf;
+  const int kdyn = ray_kdyn(me);
+  const int k4 = kdyn & ~3;
   const uint32_t off = me.off;
   // ---- pass 1: prefixes, Pre total ---------------------------------------
-  float carryA = 0.0f, Ar0 = 0.0f, Arinf = 0.0f;
+  float carryA = 0.0f, Ar0 = 0.0f, Arinf = 0.0f, Ak = 0.0f;
   Acc T = 0;
   Slice s;
   float vmu[kE];
   for (int base = 0; base < n_pre; base += kChunk) {
     const int i0 = base + kE * lane;
-    float tot = load_slice(s, off, i0, n_pre, carryA, lane, inc_pair, inc_len, inc_mu, lnq);
+    float tot = load_slice(s, off, i0, n_pre, k4, carryA, lane, inc_pair, inc_len, inc_mu, lnq);
     if (r0 > 0 && r0 - 1 >= base && r0 - 1 < base + kChunk) Ar0 = slice_value(s, r0 - 1 - base);
     if (rinf > 0 && rinf - 1 >= base && rinf - 1 < base + kChunk) Arinf = slice_value(s, rinf - 1 - base);
+    if (!kOne && k4 > 0 && k4 - 1 >= base && k4 - 1 < base + kChunk) Ak = slice_value(s, k4 - 1 - base);
     // exp(-A_{r0-1}) rescales Post visibility to Pre visibility unless the
     // Post visibility may have underflowed (then exponentiate the difference)
     const bool direct = Ar0 < kUnderflowGuard;
@@ -219,54 +225,28 @@ __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, Stage& st,
         w += vp * (1.0f - s.q[j]) * s.mu[j];
       }
     }
-    if (kMode == 1) {
-#pragma unroll
-      for (int j = 0; j < kE; j += 4) {
-        *reinterpret_cast<float4*>(&st.vmu[base + kE * lane + j]) =
-            make_float4(vmu[j], vmu[j + 1], vmu[j + 2], vmu[j + 3]);
-        *reinterpret_cast<float4*>(&st.q[base + kE * lane + j]) =
-            make_float4(s.q[j], s.q[j + 1], s.q[j + 2], s.q[j + 3]);
-      }
-    }
     T += (Acc)warp_sum(w);
     carryA += tot;
   }
   // infinity term: visibility at the end of Pre (gvdbkernels.cu:1196-1208)
   if (me.flags & 1u) T += (Acc)__expf(carryA - Arinf);
-  // ---- pass 2: messages ----------------------------------------------------
-  // Runs over the Pre range so that the (rare) Pre-only incidences past the
-  // Post stop get an explicit zero message.
-  Acc carryF = 0;
-  if (kMode == 0) {
-    emit_slice<Acc>(vmu, s.q, s.len, kE * lane, n_pre, n_post, T, carryF, lane, off, inc_pl);
+  if (kdyn >= n_post) return;  // every message of the ray is static
+  // ---- pass 2: dynamic messages ------------------------------------------
+  // F is zero before k_dyn, so the running F starts at zero at k4
+  if (kOne) {
+    emit_slice<Acc>(vmu, s.q, s.len, kE * lane, k4, n_post, T, (Acc)0, lane, off, inc_pl);
     return;
   }
-  if (kMode == 1) __syncwarp();
-  float carryA2 = 0.0f;
-  for (int base = 0; base < n_pre; base += kChunk) {
+  Acc carryF = 0;
+  float carryA2 = Ak;
+  for (int base = k4; base < n_post; base += kChunk) {
     const int i0 = base + kE * lane;
-    if (kMode == 1) {
-      float q[kE], len[kE];
+    float tot2 = load_slice(s, off, i0, n_post, k4, carryA2, lane, inc_pair, inc_len, inc_mu, lnq);
+    carryA2 += tot2;
 #pragma unroll
-      for (int j = 0; j < kE; j += 4) {
-        float4 a = *reinterpret_cast<const float4*>(&st.vmu[base + kE * lane + j]);
-        float4 b = *reinterpret_cast<const float4*>(&st.q[base + kE * lane + j]);
-        float4 d = (i0 + j < n_pre) ? __ldg(reinterpret_cast<const float4*>(inc_len + off + i0 + j))
-                                    : make_float4(0.f, 0.f, 0.f, 0.f);
-        vmu[j] = a.x; vmu[j + 1] = a.y; vmu[j + 2] = a.z; vmu[j + 3] = a.w;
-        q[j] = b.x; q[j + 1] = b.y; q[j + 2] = b.z; q[j + 3] = b.w;
-        len[j] = d.x; len[j + 1] = d.y; len[j + 2] = d.z; len[j + 3] = d.w;
-      }
-      carryF = emit_slice<Acc>(vmu, q, len, i0, n_pre, n_post, T, carryF, lane, off, inc_pl);
-    } else {
-      float tot2 = load_slice(s, off, i0, n_pre, carryA2, lane, inc_pair, inc_len, inc_mu, lnq);
-      carryA2 += tot2;
-#pragma unroll
-      for (int j = 0; j < kE; ++j) vmu[j] = __expf(s.A[j]) * s.mu[j];
-      carryF = emit_slice<Acc>(vmu, s.q, s.len, i0, n_pre, n_post, T, carryF, lane, off, inc_pl);
-    }
+    for (int j = 0; j < kE; ++j) vmu[j] = __expf(s.A[j]) * s.mu[j];
+    carryF = emit_slice<Acc>(vmu, s.q, s.len, i0, k4, n_post, T, carryF, lane, off, inc_pl);
   }
-  if (kMode == 1) __syncwarp();
 }
 
 // Persistent launch: each warp takes the next ray from a work counter; rays
@@ -283,10 +263,7 @@ __global__ void __launch_bounds__(kRayWarps * 32) k_ray_bp(const RayMeta* __rest
                                                            const float* __restrict__ lnq,
                                                            float* __restrict__ inc_pl,
                                                            int fix_reset) {
-  __shared__ Stage stage_all[kRayWarps];
   const int lane = threadIdx.x & 31;
-  const int wid = threadIdx.x >> 5;
-  Stage& st = stage_all[wid];
   for (;;) {
     uint32_t idx = 0;
     if (lane == 0) idx = atomicAdd(counter, 1u);
@@ -294,13 +271,11 @@ __global__ void __launch_bounds__(kRayWarps * 32) k_ray_bp(const RayMeta* __rest
     if (idx >= n_rays) break;
     RayMeta me = meta[order[idx]];
     if (me.n_pre <= kChunk)
-      ray_bp_warp<0, float>(me, st, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
+      ray_bp_warp<true, float>(me, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
     else if (me.n_pre <= kLongRay)
-      ray_bp_warp<1, float>(me, st, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
-    else if (me.n_pre <= kStage)
-      ray_bp_warp<1, double>(me, st, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
+      ray_bp_warp<false, float>(me, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
     else
-      ray_bp_warp<2, double>(me, st, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
+      ray_bp_warp<false, double>(me, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
   }
 }
 
@@ -353,6 +328,7 @@ __global__ void __launch_bounds__(kTileThreads, 8)
     k_pair_reduce(const uint32_t* __restrict__ perm, const float* __restrict__ pl,
                   const uint32_t* __restrict__ seg, const uint32_t* __restrict__ tile_first,
                   uint32_t k0, uint32_t k1, uint32_t p_end, TileCarry* __restrict__ carry,
+                  const uint32_t* __restrict__ dpair, const float* __restrict__ stat,
                   const uint32_t* __restrict__ pair_vox, float* __restrict__ m,
                   const float* __restrict__ cum, float* __restrict__ L, float* __restrict__ belief,
                   float* __restrict__ dm, int jacobi) {
@@ -379,7 +355,8 @@ __global__ void __launch_bounds__(kTileThreads, 8)
     for (uint32_t i = a; i < b; ++i) acc += sv[i];
     const bool open_start = s0 < base, open_end = s1 > end;
     if (!open_start && !open_end) {
-      apply_pair(pf + q, acc, pair_vox, m, cum, L, belief, dm, jacobi);
+      const uint32_t pid = dpair[pf + q];
+      apply_pair(pid, stat[pid] + acc, pair_vox, m, cum, L, belief, dm, jacobi);
       continue;
     }
     TileCarry& c = carry[blockIdx.x];
@@ -430,6 +407,7 @@ __global__ void k_tile_first(const uint32_t* __restrict__ seg, uint32_t p0, uint
 // segments crossing tile edges: the tile where such a segment starts walks
 // forward adding each following tile's partial, in tile order
 __global__ void k_pair_fixup(const TileCarry* __restrict__ carry, uint32_t ntiles,
+                             const uint32_t* __restrict__ dpair, const float* __restrict__ stat,
                              const uint32_t* __restrict__ pair_vox, float* __restrict__ m,
                              const float* __restrict__ cum, float* __restrict__ L,
                              float* __restrict__ belief, float* __restrict__ dm, int jacobi) {
@@ -446,7 +424,21 @@ __global__ void k_pair_fixup(const TileCarry* __restrict__ carry, uint32_t ntile
     if ((d.flags & kSingle) && (d.flags & kOpenEnd)) continue;
     break;
   }
-  apply_pair(key, sum, pair_vox, m, cum, L, belief, dm, jacobi);
+  const uint32_t pid = dpair[key];
+  apply_pair(pid, stat[pid] + sum, pair_vox, m, cum, L, belief, dm, jacobi);
+}
+
+// pairs whose incidences are all static: a = (sum of F_EPS * l) / cum is a
+// build constant, so their update changes the state only right after their
+// messages were zeroed or remapped
+__global__ void k_static_pairs(uint32_t p0, uint32_t p1, const uint32_t* __restrict__ ndyn,
+                               const float* __restrict__ stat, const uint32_t* __restrict__ pair_vox,
+                               float* __restrict__ m, const float* __restrict__ cum,
+                               float* __restrict__ L, float* __restrict__ belief,
+                               float* __restrict__ dm, int jacobi) {
+  uint32_t p = p0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= p1 || ndyn[p]) return;
+  apply_pair(p, stat[p], pair_vox, m, cum, L, belief, dm, jacobi);
 }
 
 // Jacobi: total log-odds of each voxel moves by the sum of its cameras'
@@ -471,6 +463,17 @@ __global__ void k_voxel_apply(const uint32_t* __restrict__ vseg, const uint32_t*
   float Lv = L[v] + s;
   L[v] = Lv;
   belief[v] = 1.0f - clampf(1.0f / (1.0f + expf(Lv)), kFEps, 1.0f - kFEps);
+}
+
+__global__ void k_max_abs_diff(const float* __restrict__ a, const float* __restrict__ b, int64_t n,
+                               uint32_t* __restrict__ out) {
+  float mx = 0.0f;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    mx = fmaxf(mx, fabsf(a[i] - b[i]));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(kFull, mx, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(mx));
 }
 
 // moving a camera: take its messages out of the total log-odds
@@ -578,19 +581,29 @@ cudaError_t launch_ray_keys(const RayMeta* meta, uint32_t n, uint32_t* keys, uin
   return cudaGetLastError();
 }
 
-cudaError_t launch_pair_update(const BpArrays& a, uint32_t k0, uint32_t k1, uint32_t p0, uint32_t p1,
+cudaError_t launch_pair_update(const BpArrays& a, uint32_t k0, uint32_t k1, uint32_t j0, uint32_t j1,
                                const uint32_t* tile_first, TileCarry* carry, int jacobi,
                                cudaStream_t s) {
-  (void)p0;
+  (void)j0;
   if (k1 <= k0) return cudaSuccess;
   uint32_t ntiles = (k1 - k0 + kTile - 1) / kTile;
-  k_pair_reduce<<<ntiles, kTileThreads, 0, s>>>(a.perm, a.inc_pl, a.pair_seg, tile_first, k0, k1, p1,
-                                                carry, a.pair_vox, a.pair_m, a.pair_cum, a.L,
-                                                a.belief, a.pair_dm, jacobi);
+  k_pair_reduce<<<ntiles, kTileThreads, 0, s>>>(a.dperm, a.inc_pl, a.dseg, tile_first, k0, k1, j1,
+                                                carry, a.dpair, a.pair_stat, a.pair_vox, a.pair_m,
+                                                a.pair_cum, a.L, a.belief, a.pair_dm, jacobi);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  k_pair_fixup<<<blocks(ntiles, 256), 256, 0, s>>>(carry, ntiles, a.pair_vox, a.pair_m, a.pair_cum,
-                                                   a.L, a.belief, a.pair_dm, jacobi);
+  k_pair_fixup<<<blocks(ntiles, 256), 256, 0, s>>>(carry, ntiles, a.dpair, a.pair_stat, a.pair_vox,
+                                                   a.pair_m, a.pair_cum, a.L, a.belief, a.pair_dm,
+                                                   jacobi);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_static_pairs(const BpArrays& a, uint32_t p0, uint32_t p1, int jacobi,
+                                cudaStream_t s) {
+  if (p1 <= p0) return cudaSuccess;
+  k_static_pairs<<<blocks(p1 - p0, 256), 256, 0, s>>>(p0, p1, a.pair_ndyn, a.pair_stat, a.pair_vox,
+                                                      a.pair_m, a.pair_cum, a.L, a.belief, a.pair_dm,
+                                                      jacobi);
   return cudaGetLastError();
 }
 
@@ -609,6 +622,15 @@ cudaError_t launch_voxel_apply(const uint32_t* vseg, const uint32_t* vpairs, con
                                cudaStream_t s) {
   if (!nvox) return cudaSuccess;
   k_voxel_apply<<<blocks(nvox, 256), 256, 0, s>>>(vseg, vpairs, vvox, nvox, pair_dm, L, belief);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_max_abs_diff(const float* a, const float* b, int64_t n, uint32_t* out,
+                                cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(out, 0, 4, s);
+  if (e != cudaSuccess || n <= 0) return e;
+  int64_t nb = std::min<int64_t>((n + 255) / 256, 4096);
+  k_max_abs_diff<<<(unsigned)nb, 256, 0, s>>>(a, b, n, out);
   return cudaGetLastError();
 }
 

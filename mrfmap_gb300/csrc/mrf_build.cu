@@ -163,11 +163,12 @@ __global__ void __launch_bounds__(kThreads)
     k_trace(Geom g, Pose P, const float* __restrict__ depth, uint32_t* __restrict__ counts,
             const uint32_t* __restrict__ pix_off, uint32_t inc_base, RayMeta* __restrict__ meta,
             uint32_t* __restrict__ inc_vox, float* __restrict__ inc_len,
-            float* __restrict__ inc_mu, float* __restrict__ post_len, int* __restrict__ err) {
+            float* __restrict__ inc_mu, float* __restrict__ post_len, uint8_t* __restrict__ inc_cls,
+            int* __restrict__ err) {
   int pix = blockIdx.x * blockDim.x + threadIdx.x;
   if (pix >= g.rows * g.cols) return;
   float d = depth[pix];
-  int count = 0, n_pre = -1, n_post = -1, r0 = -1, run_start = 0;
+  int count = 0, n_pre = -1, n_post = -1, r0 = -1, run_start = 0, kmu = -1;
   bool gate = false;
   uint32_t base = EMIT ? pix_off[pix] : 0;
   if (d > 0.0f) {
@@ -215,6 +216,7 @@ __global__ void __launch_bounds__(kThreads)
           bool z = potential_is_zero(sg, bs, n, s, d);
           inc_mu[k] = z ? 0.0f : potential(sg, bs, n, s, d);
           if (r0 < 0 && !z) r0 = run_start;
+          if (kmu < 0 && !z) kmu = count;
         }
         run_open = true;
         s_last = s;
@@ -245,15 +247,20 @@ __global__ void __launch_bounds__(kThreads)
       inc_len[base + k] = 0.0f;
       inc_mu[base + k] = 0.0f;
     }
-    // lengths that count towards the cumulative length (Post range only)
-    for (int k = 0; k < padded; ++k) post_len[base + k] = k < n_post ? inc_len[base + k] : 0.0f;
+    // lengths that count towards the cumulative length (Post range only) and
+    // the class of each incidence's message
+    const int kdyn = (kmu >= 0 && kmu < n_post) ? kmu : n_post;
+    for (int k = 0; k < padded; ++k) {
+      post_len[base + k] = k < n_post ? inc_len[base + k] : 0.0f;
+      inc_cls[base + k] = k < kdyn ? kIncStatic : (k < n_post ? kIncDyn : kIncNone);
+    }
     RayMeta m;
     m.off = inc_base + base;
     m.n_pre = (uint16_t)n_pre;
     m.n_post = (uint16_t)n_post;
     m.r0 = (uint16_t)(r0 >= 0 ? r0 : n_pre);
     m.rinf = (uint16_t)(r0 >= 0 ? r0 : run_start);
-    m.flags = gate ? 1u : 0u;
+    m.flags = (gate ? 1u : 0u) | ((uint32_t)kdyn << 16);
     meta[pix] = m;
   }
 }
@@ -272,7 +279,7 @@ __global__ void k_pairs_from_sorted(const uint32_t* __restrict__ sk, const uint3
                                     const uint32_t* __restrict__ scan, uint32_t n,
                                     uint32_t pair_base, uint32_t perm_base, uint32_t inc_base,
                                     uint32_t* __restrict__ pair_vox, uint32_t* __restrict__ seg,
-                                    uint32_t* __restrict__ perm, uint32_t* __restrict__ inc_pair) {
+                                    uint32_t* __restrict__ inc_pair) {
   uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
   uint32_t p = pair_base + scan[k] + flag[k] - 1;
@@ -280,22 +287,67 @@ __global__ void k_pairs_from_sorted(const uint32_t* __restrict__ sk, const uint3
     pair_vox[p] = sk[k];
     seg[p] = perm_base + k;
   }
-  uint32_t i = inc_base + sidx[k];
-  perm[perm_base + k] = i;
-  inc_pair[i] = p;
+  inc_pair[inc_base + sidx[k]] = p;
 }
 
-// cumulative length of each pair: fp32, in increasing incidence order (the
-// order the reference's cumulative-length pass visits a voxel, pixel-major)
-__global__ void k_pair_cum(const uint32_t* __restrict__ seg, const uint32_t* __restrict__ sidx,
-                           uint32_t p0, uint32_t np, uint32_t perm_base, uint32_t inc_base,
-                           const float* __restrict__ post_len, float* __restrict__ cum) {
+// Per pair, over its incidences in increasing incidence order (the order
+// the reference's cumulative-length pass visits a voxel, pixel-major):
+// cumulative length (fp32), the sum of its static messages F_EPS * l (fp32,
+// each product rounded as the ray kernel would round it) and the number of
+// dynamic incidences.
+__global__ void k_pair_stats(const uint32_t* __restrict__ seg, const uint32_t* __restrict__ sidx,
+                             uint32_t p0, uint32_t np, uint32_t perm_base, uint32_t inc_base,
+                             const float* __restrict__ post_len, const uint8_t* __restrict__ cls,
+                             float* __restrict__ cum, float* __restrict__ stat,
+                             uint32_t* __restrict__ ndyn) {
   uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= np) return;
   uint32_t p = p0 + q;
-  float c = 0.0f;
-  for (uint32_t k = seg[p]; k < seg[p + 1]; ++k) c += post_len[inc_base + sidx[k - perm_base]];
+  float c = 0.0f, st = 0.0f;
+  uint32_t nd = 0;
+  for (uint32_t k = seg[p]; k < seg[p + 1]; ++k) {
+    uint32_t i = inc_base + sidx[k - perm_base];
+    float l = post_len[i];
+    c += l;
+    uint8_t t = cls[i];
+    if (t == kIncStatic) st += __fmul_rn(kFEps, l);
+    nd += t == kIncDyn;
+  }
   cum[p] = c;
+  stat[p] = st;
+  ndyn[p] = nd;
+}
+
+__global__ void k_dyn_flags(const uint32_t* __restrict__ sidx, uint32_t n, uint32_t inc_base,
+                            const uint8_t* __restrict__ cls, uint32_t* __restrict__ flag) {
+  uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) flag[k] = cls[inc_base + sidx[k]] == kIncDyn ? 1u : 0u;
+}
+
+__global__ void k_dyn_scatter(const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ flag,
+                              const uint32_t* __restrict__ scan, uint32_t n, uint32_t inc_base,
+                              uint32_t dperm_base, uint32_t* __restrict__ dperm) {
+  uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n && flag[k]) dperm[dperm_base + scan[k]] = inc_base + sidx[k];
+}
+
+__global__ void k_dpair_flags(const uint32_t* __restrict__ ndyn, uint32_t p0, uint32_t np,
+                              uint32_t* __restrict__ flag) {
+  uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q < np) flag[q] = ndyn[p0 + q] ? 1u : 0u;
+}
+
+__global__ void k_dpairs(const uint32_t* __restrict__ pflag, const uint32_t* __restrict__ pscan,
+                         uint32_t p0, uint32_t np, const uint32_t* __restrict__ seg, uint32_t perm_base,
+                         const uint32_t* __restrict__ dscan, uint32_t dperm_base, uint32_t dpair_base,
+                         uint32_t* __restrict__ dpair, uint32_t* __restrict__ dseg) {
+  uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= np || !pflag[q]) return;
+  uint32_t j = dpair_base + pscan[q];
+  dpair[j] = p0 + q;
+  // the run keeps the pair grouping: it starts at the dynamic rank of the
+  // pair's first position
+  dseg[j] = dperm_base + dscan[seg[p0 + q] - perm_base];
 }
 
 __global__ void k_iota(uint32_t* out, uint32_t n) {
@@ -352,16 +404,16 @@ cudaError_t launch_set_points(const Geom& g, const float* pts, const float* occ,
 cudaError_t launch_trace_count(const Geom& g, const Pose& P, const float* depth, uint32_t* counts,
                                int* err, cudaStream_t s) {
   k_trace<false><<<grid_for((int64_t)g.rows * g.cols), kThreads, 0, s>>>(
-      g, P, depth, counts, nullptr, 0, nullptr, nullptr, nullptr, nullptr, nullptr, err);
+      g, P, depth, counts, nullptr, 0, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, err);
   return cudaGetLastError();
 }
 
 cudaError_t launch_trace_emit(const Geom& g, const Pose& P, const float* depth,
                               const uint32_t* pix_off, uint32_t inc_base, RayMeta* meta,
                               uint32_t* inc_vox, float* inc_len, float* inc_mu, float* post_len,
-                              int* err, cudaStream_t s) {
+                              uint8_t* inc_cls, int* err, cudaStream_t s) {
   k_trace<true><<<grid_for((int64_t)g.rows * g.cols), kThreads, 0, s>>>(
-      g, P, depth, nullptr, pix_off, inc_base, meta, inc_vox, inc_len, inc_mu, post_len, err);
+      g, P, depth, nullptr, pix_off, inc_base, meta, inc_vox, inc_len, inc_mu, post_len, inc_cls, err);
   return cudaGetLastError();
 }
 
@@ -374,19 +426,52 @@ cudaError_t launch_vox_heads(const uint32_t* sk, uint32_t n, uint32_t* flag, cud
 cudaError_t launch_pairs_from_sorted(const uint32_t* sk, const uint32_t* sidx, const uint32_t* flag,
                                      const uint32_t* scan, uint32_t n, uint32_t pair_base,
                                      uint32_t perm_base, uint32_t inc_base, uint32_t* pair_vox,
-                                     uint32_t* seg, uint32_t* perm, uint32_t* inc_pair,
-                                     cudaStream_t s) {
+                                     uint32_t* seg, uint32_t* inc_pair, cudaStream_t s) {
   if (!n) return cudaSuccess;
   k_pairs_from_sorted<<<grid_for(n), kThreads, 0, s>>>(sk, sidx, flag, scan, n, pair_base, perm_base,
-                                                       inc_base, pair_vox, seg, perm, inc_pair);
+                                                       inc_base, pair_vox, seg, inc_pair);
   return cudaGetLastError();
 }
 
-cudaError_t launch_pair_cum(const uint32_t* seg, const uint32_t* sidx, uint32_t p0, uint32_t np,
-                            uint32_t perm_base, uint32_t inc_base, const float* post_len, float* cum,
-                            cudaStream_t s) {
+cudaError_t launch_pair_stats(const uint32_t* seg, const uint32_t* sidx, uint32_t p0, uint32_t np,
+                              uint32_t perm_base, uint32_t inc_base, const float* post_len,
+                              const uint8_t* cls, float* cum, float* stat, uint32_t* ndyn,
+                              cudaStream_t s) {
   if (!np) return cudaSuccess;
-  k_pair_cum<<<grid_for(np), kThreads, 0, s>>>(seg, sidx, p0, np, perm_base, inc_base, post_len, cum);
+  k_pair_stats<<<grid_for(np), kThreads, 0, s>>>(seg, sidx, p0, np, perm_base, inc_base, post_len, cls,
+                                                 cum, stat, ndyn);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dyn_flags(const uint32_t* sidx, uint32_t n, uint32_t inc_base, const uint8_t* cls,
+                             uint32_t* flag, cudaStream_t s) {
+  if (!n) return cudaSuccess;
+  k_dyn_flags<<<grid_for(n), kThreads, 0, s>>>(sidx, n, inc_base, cls, flag);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dyn_scatter(const uint32_t* sidx, const uint32_t* flag, const uint32_t* scan,
+                               uint32_t n, uint32_t inc_base, uint32_t dperm_base, uint32_t* dperm,
+                               cudaStream_t s) {
+  if (!n) return cudaSuccess;
+  k_dyn_scatter<<<grid_for(n), kThreads, 0, s>>>(sidx, flag, scan, n, inc_base, dperm_base, dperm);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dpair_flags(const uint32_t* ndyn, uint32_t p0, uint32_t np, uint32_t* flag,
+                               cudaStream_t s) {
+  if (!np) return cudaSuccess;
+  k_dpair_flags<<<grid_for(np), kThreads, 0, s>>>(ndyn, p0, np, flag);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dpairs(const uint32_t* pflag, const uint32_t* pscan, uint32_t p0, uint32_t np,
+                          const uint32_t* seg, uint32_t perm_base, const uint32_t* dscan,
+                          uint32_t dperm_base, uint32_t dpair_base, uint32_t* dpair, uint32_t* dseg,
+                          cudaStream_t s) {
+  if (!np) return cudaSuccess;
+  k_dpairs<<<grid_for(np), kThreads, 0, s>>>(pflag, pscan, p0, np, seg, perm_base, dscan, dperm_base,
+                                            dpair_base, dpair, dseg);
   return cudaGetLastError();
 }
 

@@ -85,7 +85,9 @@ struct View {
   DBuf depth;
   uint32_t inc_base = 0, n_inc = 0;
   uint32_t pair_base = 0, n_pairs = 0;
-  uint32_t perm_base = 0, n_perm = 0;
+  uint32_t perm_base = 0, n_perm = 0;     // pair-grouped positions of all incidences
+  uint32_t dperm_base = 0, n_dperm = 0;   // ... of the dynamic ones
+  uint32_t dpair_base = 0, n_dpairs = 0;  // runs of dynamic incidences (one per pair)
   uint32_t order_base = 0, n_active = 0;  // ray queue (longest first)
   uint32_t tile_base = 0;                 // first pair of each pair-update tile
 };
@@ -111,27 +113,28 @@ struct mrf_map {
   bool has_messages = false;
   std::vector<View> views;
   // arenas
-  DBuf meta, inc_pair, inc_len, inc_mu, inc_pl, pair_vox, pair_m, pair_cum, pair_q, pair_dm,
-      pair_seg, perm, carry, ray_order, counters, tile_first;
+  DBuf meta, inc_pair, inc_len, inc_mu, inc_pl, pair_vox, pair_m, pair_cum, pair_stat, pair_ndyn,
+      pair_q, pair_dm, pair_seg, dperm, dpair, dseg, carry, ray_order, counters, tile_first;
   uint32_t jac_tile_base = 0;
-  int64_t n_inc = 0, n_pairs = 0, n_perm = 0;
+  int64_t n_inc = 0, n_pairs = 0, n_dperm = 0, n_dpairs = 0;
   // jacobi voxel CSR
   DBuf vseg, vpairs, vvox;
   uint32_t n_vvox = 0;
   int jacobi_version = -1;
   // scratch
-  DBuf s_postlen, s_flags, s_ind, s_scan, s_tmp, s_counts, s_offs, s_vox, s_k0, s_k1, s_v0, s_v1,
-      s_seg, s_dense, s_err, s_depth_in, s_depth, s_img, s_part, s_sum;
+  DBuf s_postlen, s_cls, s_pf, s_ps, s_flags, s_ind, s_scan, s_tmp, s_counts, s_offs, s_vox, s_k0, s_k1, s_v0, s_v1,
+      s_seg, s_dense, s_err, s_depth_in, s_depth, s_img, s_part, s_sum, s_prev, s_delta;
   mrf_stats stats{};
   // MRF_PROFILE event pool
   std::vector<cudaEvent_t> prof_ev;
   std::vector<int> prof_cat;
-  // captured BP iteration per schedule (Jacobi bit, fixed-reset bit)
+  // captured BP iteration per schedule (Jacobi bit, fixed-reset bit, first
+  // iteration of an mrf_infer call bit)
   struct GraphSlot {
     cudaGraphExec_t exec = nullptr;
     int version = -1;
     int64_t launches = 0;
-  } graphs[4];
+  } graphs[8];
 
   BpArrays bp() const {
     BpArrays a;
@@ -140,13 +143,16 @@ struct mrf_map {
     a.inc_len = inc_len.as<float>();
     a.inc_mu = inc_mu.as<float>();
     a.inc_pl = inc_pl.as<float>();
+    a.dperm = dperm.as<uint32_t>();
+    a.dpair = dpair.as<uint32_t>();
+    a.dseg = dseg.as<uint32_t>();
     a.pair_vox = pair_vox.as<uint32_t>();
     a.pair_m = pair_m.as<float>();
     a.pair_cum = pair_cum.as<float>();
+    a.pair_stat = pair_stat.as<float>();
+    a.pair_ndyn = pair_ndyn.as<uint32_t>();
     a.pair_lnq = pair_q.as<float>();
     a.pair_dm = pair_dm.as<float>();
-    a.pair_seg = pair_seg.as<uint32_t>();
-    a.perm = perm.as<uint32_t>();
     a.L = d_L.as<float>();
     a.belief = d_belief.as<float>();
     return a;
@@ -265,10 +271,11 @@ void rebuild(mrf_map* m) {
   m->inc_pair.reserve(ib, false, m->stream);
   m->inc_len.reserve(ib, false, m->stream);
   m->inc_mu.reserve(ib, false, m->stream);
-  m->perm.reserve(ib, false, m->stream);
+  m->dperm.reserve(ib, false, m->stream);
   m->inc_pl.reserve(ib, false, m->stream);
   m->s_vox.reserve(ib, false, m->stream);
   m->s_postlen.reserve(ib, false, m->stream);
+  m->s_cls.reserve(ib / 4, false, m->stream);
   // 3. emit
   for (int c = 0; c < V; ++c) {
     View& v = m->views[c];
@@ -277,12 +284,12 @@ void rebuild(mrf_map* m) {
     CK(launch_trace_emit(m->g, v.pose, v.depth.as<float>(), m->s_offs.as<uint32_t>() + c * HW, 0,
                          m->meta.as<RayMeta>() + c * HW, m->s_vox.as<uint32_t>(),
                          m->inc_len.as<float>(), m->inc_mu.as<float>(), m->s_postlen.as<float>(),
-                         m->s_err.as<int>(), m->stream));
+                         m->s_cls.as<uint8_t>(), m->s_err.as<int>(), m->stream));
   }
   // per-view counters from the ray records
   std::vector<RayMeta> hm((size_t)npix);
   std::vector<int64_t> nreal(V, 0);
-  int64_t nrays = 0, npost = 0, npre = 0;
+  int64_t nrays = 0, npost = 0, npre = 0, ndyn = 0;
   if (npix) {
     CK(cudaMemcpyAsync(hm.data(), m->meta.p, (size_t)npix * sizeof(RayMeta), cudaMemcpyDeviceToHost,
                        m->stream));
@@ -294,6 +301,7 @@ void rebuild(mrf_map* m) {
         nreal[c] += r.n_pre;
         nrays += r.n_pre > 0;
         npost += r.n_post;
+        ndyn += r.n_post - std::min<int>(ray_kdyn(r), r.n_post);
       }
     for (int c = 0; c < V; ++c) npre += nreal[c];
   }
@@ -301,15 +309,19 @@ void rebuild(mrf_map* m) {
   //    (stable), one pair per run; pos[i] = pair-grouped position of i
   int bits = 1;
   while (bits < 32 && ((uint64_t)1 << bits) <= (uint64_t)(m->n_bricks * kBrickVox)) ++bits;
-  int64_t pair_total = 0, perm_total = 0;
+  int64_t pair_total = 0, perm_total = 0, dperm_total = 0, dpair_total = 0;
   for (int c = 0; c < V; ++c) {
     View& v = m->views[c];
     uint32_t n = v.n_inc;
     uint32_t nr = (uint32_t)nreal[c];
     v.pair_base = (uint32_t)pair_total;
     v.perm_base = (uint32_t)perm_total;
+    v.dperm_base = (uint32_t)dperm_total;
+    v.dpair_base = (uint32_t)dpair_total;
     v.n_pairs = 0;
     v.n_perm = 0;
+    v.n_dperm = 0;
+    v.n_dpairs = 0;
     if (nr == 0) continue;
     m->s_k0.reserve((size_t)n * 4 + 4, false, m->stream);
     m->s_k1.reserve((size_t)n * 4 + 4, false, m->stream);
@@ -333,19 +345,53 @@ void rebuild(mrf_map* m) {
     m->pair_vox.reserve(pb * 4, true, m->stream);
     m->pair_m.reserve(pb * 4, true, m->stream);
     m->pair_cum.reserve(pb * 4, true, m->stream);
+    m->pair_stat.reserve(pb * 4, true, m->stream);
+    m->pair_ndyn.reserve(pb * 4, true, m->stream);
     m->pair_seg.reserve(pb * 4, true, m->stream);
     CK(launch_pairs_from_sorted(m->s_k1.as<uint32_t>(), m->s_v1.as<uint32_t>(), m->s_k0.as<uint32_t>(),
                                 m->s_v0.as<uint32_t>(), nr, v.pair_base, v.perm_base, v.inc_base,
                                 m->pair_vox.as<uint32_t>(), m->pair_seg.as<uint32_t>(),
-                                m->perm.as<uint32_t>(), m->inc_pair.as<uint32_t>(), m->stream));
+                                m->inc_pair.as<uint32_t>(), m->stream));
     CK(launch_fill_u32(m->pair_seg.as<uint32_t>() + v.pair_base + np, 1, v.perm_base + nr, m->stream));
-    CK(launch_pair_cum(m->pair_seg.as<uint32_t>(), m->s_v1.as<uint32_t>(), v.pair_base, np,
-                       v.perm_base, v.inc_base, m->s_postlen.as<float>(), m->pair_cum.as<float>(),
-                       m->stream));
+    CK(launch_pair_stats(m->pair_seg.as<uint32_t>(), m->s_v1.as<uint32_t>(), v.pair_base, np,
+                         v.perm_base, v.inc_base, m->s_postlen.as<float>(), m->s_cls.as<uint8_t>(),
+                         m->pair_cum.as<float>(), m->pair_stat.as<float>(),
+                         m->pair_ndyn.as<uint32_t>(), m->stream));
+    // dynamic incidences in pair-grouped order (a stable compaction of the
+    // sorted positions) and the run of each pair that has any
+    CK(launch_dyn_flags(m->s_v1.as<uint32_t>(), nr, v.inc_base, m->s_cls.as<uint8_t>(),
+                        m->s_k0.as<uint32_t>(), m->stream));
+    CK(cudaMemsetAsync(m->s_k0.as<uint32_t>() + nr, 0, 4, m->stream));
+    CK(exclusive_scan_u32(m->s_tmp.p, t1, m->s_k0.as<uint32_t>(), m->s_v0.as<uint32_t>(), nr + 1,
+                          m->stream));
+    uint32_t nd = read1(m, m->s_v0.as<uint32_t>() + nr);
+    CK(launch_dyn_scatter(m->s_v1.as<uint32_t>(), m->s_k0.as<uint32_t>(), m->s_v0.as<uint32_t>(), nr,
+                          v.inc_base, v.dperm_base, m->dperm.as<uint32_t>(), m->stream));
+    m->s_pf.reserve((size_t)np * 4 + 4, false, m->stream);
+    m->s_ps.reserve((size_t)np * 4 + 4, false, m->stream);
+    CK(launch_dpair_flags(m->pair_ndyn.as<uint32_t>(), v.pair_base, np, m->s_pf.as<uint32_t>(),
+                          m->stream));
+    CK(cudaMemsetAsync(m->s_pf.as<uint32_t>() + np, 0, 4, m->stream));
+    size_t t3 = scan_temp_bytes(np + 1);
+    m->s_tmp.reserve(t3, false, m->stream);
+    CK(exclusive_scan_u32(m->s_tmp.p, t3, m->s_pf.as<uint32_t>(), m->s_ps.as<uint32_t>(), np + 1,
+                          m->stream));
+    uint32_t ndp = read1(m, m->s_ps.as<uint32_t>() + np);
+    size_t db = (size_t)(dpair_total + ndp + 1);
+    m->dpair.reserve(db * 4, true, m->stream);
+    m->dseg.reserve(db * 4, true, m->stream);
+    CK(launch_dpairs(m->s_pf.as<uint32_t>(), m->s_ps.as<uint32_t>(), v.pair_base, np,
+                     m->pair_seg.as<uint32_t>(), v.perm_base, m->s_v0.as<uint32_t>(), v.dperm_base,
+                     v.dpair_base, m->dpair.as<uint32_t>(), m->dseg.as<uint32_t>(), m->stream));
+    CK(launch_fill_u32(m->dseg.as<uint32_t>() + v.dpair_base + ndp, 1, v.dperm_base + nd, m->stream));
     v.n_pairs = np;
     v.n_perm = nr;
+    v.n_dperm = nd;
+    v.n_dpairs = ndp;
     pair_total += np;
     perm_total += nr;
+    dperm_total += nd;
+    dpair_total += ndp;
   }
   // ray queues: per view, the active rays longest first
   {
@@ -375,12 +421,18 @@ void rebuild(mrf_map* m) {
   }
   m->n_inc = n_inc;
   m->n_pairs = pair_total;
-  m->n_perm = perm_total;
+  m->n_dperm = dperm_total;
+  m->n_dpairs = dpair_total;
   size_t pb = (size_t)std::max<int64_t>(pair_total + 1, 1);
   m->pair_vox.reserve(pb * 4, true, m->stream);
   m->pair_m.reserve(pb * 4, true, m->stream);
   m->pair_cum.reserve(pb * 4, true, m->stream);
+  m->pair_stat.reserve(pb * 4, true, m->stream);
+  m->pair_ndyn.reserve(pb * 4, true, m->stream);
   m->pair_seg.reserve(pb * 4, true, m->stream);
+  m->dpair.reserve((size_t)(dpair_total + 1) * 4, true, m->stream);
+  m->dseg.reserve((size_t)(dpair_total + 1) * 4, true, m->stream);
+  if (dpair_total == 0) CK(launch_fill_u32(m->dseg.as<uint32_t>(), 1, 0u, m->stream));
   m->pair_q.reserve(pb * 4, false, m->stream);
   m->pair_dm.reserve(pb * 4, false, m->stream);
   CK(launch_fill_f32(m->pair_m.as<float>(), pair_total, 0.0f, m->stream));
@@ -388,20 +440,20 @@ void rebuild(mrf_map* m) {
     // tile carries of the pair update: enough for any view or all of them;
     // first pair of every tile, per view (Gauss-Seidel) and over all views
     // (Jacobi)
-    int64_t tiles = (int64_t)pair_update_tiles((uint32_t)std::min<int64_t>(perm_total, 0xFFFFFFF0ll)) + V + 1;
+    int64_t tiles = (int64_t)pair_update_tiles((uint32_t)std::min<int64_t>(dperm_total, 0xFFFFFFF0ll)) + V + 1;
     m->carry.reserve((size_t)tiles * sizeof(TileCarry), false, m->stream);
     m->tile_first.reserve((size_t)(2 * tiles + 2) * 4, false, m->stream);
     uint32_t tb = 0;
     for (int c = 0; c < V; ++c) {
       View& v = m->views[c];
       v.tile_base = tb;
-      CK(launch_tile_first(m->pair_seg.as<uint32_t>(), v.pair_base, v.pair_base + v.n_pairs,
-                           v.perm_base, v.perm_base + v.n_perm, m->tile_first.as<uint32_t>() + tb,
+      CK(launch_tile_first(m->dseg.as<uint32_t>(), v.dpair_base, v.dpair_base + v.n_dpairs,
+                           v.dperm_base, v.dperm_base + v.n_dperm, m->tile_first.as<uint32_t>() + tb,
                            m->stream));
-      tb += pair_update_tiles(v.n_perm);
+      tb += pair_update_tiles(v.n_dperm);
     }
     m->jac_tile_base = tb;
-    CK(launch_tile_first(m->pair_seg.as<uint32_t>(), 0, (uint32_t)pair_total, 0, (uint32_t)perm_total,
+    CK(launch_tile_first(m->dseg.as<uint32_t>(), 0, (uint32_t)dpair_total, 0, (uint32_t)dperm_total,
                          m->tile_first.as<uint32_t>() + tb, m->stream));
   }
   // 5. carry messages of every camera over to its new pairs
@@ -436,6 +488,8 @@ void rebuild(mrf_map* m) {
   m->stats.n_inc_pre = npre;
   m->stats.n_inc_post = npost;
   m->stats.n_pairs = pair_total;
+  m->stats.n_inc_dyn = ndyn;
+  m->stats.n_pairs_dyn = dpair_total;
 }
 
 void build_jacobi_csr(mrf_map* m) {
@@ -513,9 +567,12 @@ struct Profiler {
 };
 
 // one BP iteration over every camera (src/GVDBInference.cpp:155-167):
-// Gauss-Seidel camera by camera, or Jacobi over all cameras at once
-void enqueue_iteration(mrf_map* m, const BpArrays& a, bool jacobi, int fix, Profiler& prof,
-                       int64_t& launches) {
+// Gauss-Seidel camera by camera, or Jacobi over all cameras at once.  The
+// pairs without dynamic incidences get their (constant) update in the first
+// iteration of each mrf_infer call only: afterwards it would leave every
+// value unchanged (L + (m_new - m_new) = L).
+void enqueue_iteration(mrf_map* m, const BpArrays& a, bool jacobi, int fix, bool first,
+                       Profiler& prof, int64_t& launches) {
   const int V = (int)m->views.size();
   CK(cudaMemsetAsync(m->counters.p, 0, (size_t)(V + 1) * 4, m->stream));
   if (!jacobi) {
@@ -530,11 +587,18 @@ void enqueue_iteration(mrf_map* m, const BpArrays& a, bool jacobi, int fix, Prof
                        m->counters.as<uint32_t>() + c, fix, m->num_sms, m->stream));
       prof.end();
       prof.begin(2);
-      CK(launch_pair_update(a, v.perm_base, v.perm_base + v.n_perm, v.pair_base,
-                            v.pair_base + v.n_pairs, m->tile_first.as<uint32_t>() + v.tile_base,
-                            m->carry.as<TileCarry>(), 0, m->stream));
+      if (v.n_dperm) {
+        CK(launch_pair_update(a, v.dperm_base, v.dperm_base + v.n_dperm, v.dpair_base,
+                              v.dpair_base + v.n_dpairs, m->tile_first.as<uint32_t>() + v.tile_base,
+                              m->carry.as<TileCarry>(), 0, m->stream));
+        launches += 2;
+      }
+      if (first) {
+        CK(launch_static_pairs(a, v.pair_base, v.pair_base + v.n_pairs, 0, m->stream));
+        ++launches;
+      }
       prof.end();
-      launches += 4;
+      launches += 2;
     }
   } else {
     uint32_t P = (uint32_t)m->n_pairs;
@@ -549,24 +613,25 @@ void enqueue_iteration(mrf_map* m, const BpArrays& a, bool jacobi, int fix, Prof
                      m->num_sms, m->stream));
     prof.end();
     prof.begin(2);
-    CK(launch_pair_update(a, 0, (uint32_t)m->n_perm, 0, P,
+    CK(launch_pair_update(a, 0, (uint32_t)m->n_dperm, 0, (uint32_t)m->n_dpairs,
                           m->tile_first.as<uint32_t>() + m->jac_tile_base, m->carry.as<TileCarry>(),
                           1, m->stream));
+    if (first) CK(launch_static_pairs(a, 0, P, 1, m->stream));
     prof.end();
     prof.begin(3);
     CK(launch_voxel_apply(m->vseg.as<uint32_t>(), m->vpairs.as<uint32_t>(), m->vvox.as<uint32_t>(),
                           m->n_vvox, m->pair_dm.as<float>(), m->d_L.as<float>(),
                           m->d_belief.as<float>(), m->stream));
     prof.end();
-    launches += 5;
+    launches += 5 + (first ? 1 : 0);
   }
 }
 
 // The iteration is captured once per incidence build and schedule into a
 // CUDA graph and replayed iters times.
-cudaGraphExec_t iteration_graph(mrf_map* m, const BpArrays& a, bool jacobi, int fix,
+cudaGraphExec_t iteration_graph(mrf_map* m, const BpArrays& a, bool jacobi, int fix, bool first,
                                 int64_t& launches_per_iter) {
-  int key = (jacobi ? 1 : 0) | (fix ? 2 : 0);
+  int key = (jacobi ? 1 : 0) | (fix ? 2 : 0) | (first ? 4 : 0);
   auto& slot = m->graphs[key];
   if (slot.exec && slot.version == m->built_version) {
     launches_per_iter = slot.launches;
@@ -581,7 +646,7 @@ cudaGraphExec_t iteration_graph(mrf_map* m, const BpArrays& a, bool jacobi, int 
   cudaGraph_t graph = nullptr;
   CK(cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal));
   try {
-    enqueue_iteration(m, a, jacobi, fix, off, launches);
+    enqueue_iteration(m, a, jacobi, fix, first, off, launches);
   } catch (...) {
     cudaStreamEndCapture(m->stream, &graph);
     if (graph) cudaGraphDestroy(graph);
@@ -599,12 +664,16 @@ cudaGraphExec_t iteration_graph(mrf_map* m, const BpArrays& a, bool jacobi, int 
   return exec;
 }
 
-void run_infer(mrf_map* m, const int* ids, int n_ids, int iters, int flags) {
+// tol > 0: stop after the first iteration whose largest belief change is
+// below tol (checked every check_every iterations; iters is the cap)
+void run_infer(mrf_map* m, const int* ids, int n_ids, int iters, int flags, float tol = -1.0f,
+               int check_every = 1, float* last_delta = nullptr) {
   ensure_built(m);
   const bool jacobi = flags & MRF_JACOBI;
   if (jacobi && m->jacobi_version != m->built_version) build_jacobi_csr(m);
   const int V = (int)m->views.size();
   if (iters <= 0) iters = m->prm.max_iters > 0 ? m->prm.max_iters : 1;
+  if (check_every < 1) check_every = 1;
   BpArrays a = m->bp();
   int64_t launches = 0;
   Profiler prof{m, (flags & MRF_PROFILE) != 0};
@@ -621,21 +690,52 @@ void run_infer(mrf_map* m, const int* ids, int n_ids, int iters, int flags) {
     }
   }
   const int fix = (flags & MRF_FIX_PRE_RESET) ? 1 : 0;
+  const bool conv = tol > 0.0f;
+  const int64_t nvox = m->n_bricks * kBrickVox;
+  if (conv) {
+    m->s_prev.reserve((size_t)std::max<int64_t>(nvox, 1) * 4, false, m->stream);
+    m->s_delta.reserve(64, false, m->stream);
+  }
+  float delta = -1.0f;
+  int done = 0;
   if (m->n_inc > 0) {
-    if (prof.on || (flags & MRF_NO_GRAPH)) {
-      for (int it = 0; it < iters; ++it) enqueue_iteration(m, a, jacobi, fix, prof, launches);
-    } else {
-      int64_t per = 0;
-      cudaGraphExec_t exec = iteration_graph(m, a, jacobi, fix, per);
-      for (int it = 0; it < iters; ++it) CK(cudaGraphLaunch(exec, m->stream));
-      launches += per * iters;
+    const bool direct = prof.on || (flags & MRF_NO_GRAPH);
+    int64_t per0 = 0, per = 0;
+    cudaGraphExec_t exec0 = nullptr, exec = nullptr;
+    if (!direct) {
+      exec0 = iteration_graph(m, a, jacobi, fix, true, per0);
+      if (iters > 1) exec = iteration_graph(m, a, jacobi, fix, false, per);
+    }
+    for (int it = 0; it < iters; ++it) {
+      const bool check = conv && ((it + 1) % check_every == 0 || it + 1 == iters);
+      if (check)
+        CK(cudaMemcpyAsync(m->s_prev.p, m->d_belief.p, (size_t)nvox * 4, cudaMemcpyDeviceToDevice,
+                           m->stream));
+      if (direct) {
+        enqueue_iteration(m, a, jacobi, fix, it == 0, prof, launches);
+      } else {
+        CK(cudaGraphLaunch(it == 0 ? exec0 : exec, m->stream));
+        launches += it == 0 ? per0 : per;
+      }
+      done = it + 1;
+      if (check) {
+        CK(launch_max_abs_diff(m->d_belief.as<float>(), m->s_prev.as<float>(), nvox,
+                               m->s_delta.as<uint32_t>(), m->stream));
+        ++launches;
+        uint32_t bits = 0;
+        CK(cudaMemcpyAsync(&bits, m->s_delta.p, 4, cudaMemcpyDeviceToHost, m->stream));
+        sync(m);
+        std::memcpy(&delta, &bits, 4);
+        if (delta < tol) break;
+      }
     }
   }
   CK(cudaEventRecord(m->ev1, m->stream));
   m->has_messages = true;
-  m->stats.iters_done = iters;
+  m->stats.iters_done = done;
   m->stats.kernel_launches = launches;
-  if (!(flags & MRF_ASYNC) || prof.on) {
+  if (last_delta) *last_delta = delta;
+  if (!(flags & MRF_ASYNC) || prof.on || conv) {
     sync(m);
     float ms = 0.0f;
     cudaEventElapsedTime(&ms, m->ev0, m->ev1);
@@ -699,12 +799,14 @@ mrf_status wrap(F&& f) {
 void destroy_bufs(mrf_map* m) {
   DBuf* all[] = {&m->d_sigma, &m->d_bias, &m->d_slot, &m->d_coord, &m->d_L, &m->d_belief,
                  &m->meta, &m->inc_pair, &m->inc_len, &m->inc_mu, &m->inc_pl, &m->pair_vox,
-                 &m->pair_m, &m->pair_cum, &m->pair_q, &m->pair_dm, &m->pair_seg, &m->perm,
+                 &m->pair_m, &m->pair_cum, &m->pair_stat, &m->pair_ndyn, &m->pair_q, &m->pair_dm,
+                 &m->pair_seg, &m->dperm, &m->dpair, &m->dseg,
                  &m->carry, &m->ray_order, &m->counters, &m->tile_first,
-                 &m->vseg, &m->vpairs, &m->vvox, &m->s_postlen, &m->s_flags, &m->s_ind, &m->s_scan,
+                 &m->vseg, &m->vpairs, &m->vvox, &m->s_postlen, &m->s_cls, &m->s_pf, &m->s_ps,
+                 &m->s_flags, &m->s_ind, &m->s_scan,
                  &m->s_tmp, &m->s_counts, &m->s_offs, &m->s_vox, &m->s_k0, &m->s_k1, &m->s_v0,
                  &m->s_v1, &m->s_seg, &m->s_dense, &m->s_err, &m->s_depth_in, &m->s_depth,
-                 &m->s_img, &m->s_part, &m->s_sum};
+                 &m->s_img, &m->s_part, &m->s_sum, &m->s_prev, &m->s_delta};
   for (DBuf* b : all) b->release();
   for (auto& v : m->views) v.depth.release();
 }
@@ -898,6 +1000,19 @@ mrf_status mrf_infer(mrf_map* m, const int* ids, int n_ids, int iters, int flags
   return wrap([&] { run_infer(m, ids, ids ? n_ids : 0, iters, flags); });
 }
 
+mrf_status mrf_infer_converge(mrf_map* m, const int* ids, int n_ids, int max_iters, float tol,
+                              int check_every, int flags, int* iters_done, float* last_delta) {
+  if (guard(m) != MRF_OK) return MRF_ERR_INVALID;
+  if (n_ids < 0 || (n_ids > 0 && !ids) || !(tol > 0.0f)) {
+    set_err("invalid ids or tolerance");
+    return MRF_ERR_INVALID;
+  }
+  return wrap([&] {
+    run_infer(m, ids, ids ? n_ids : 0, max_iters, flags, tol, check_every, last_delta);
+    if (iters_done) *iters_done = (int)m->stats.iters_done;
+  });
+}
+
 mrf_status mrf_reset_state(mrf_map* m) {
   if (guard(m) != MRF_OK) return MRF_ERR_INVALID;
   return wrap([&] {
@@ -972,6 +1087,80 @@ mrf_status mrf_likelihood_view(mrf_map* m, int view_id, float* out_img, float* o
   }
   const View& v = m->views[view_id];
   return likelihood_host(m, v.pose, v.depth.as<float>(), out_img, out_sum);
+}
+
+static mrf_status render_impl(mrf_map* m, int mode, const Pose& P, const float* depth_clean_dev,
+                              float threshold, float* out_img, float* out_score, int64_t* counts) {
+  if (mode < 0 || mode > 3) {
+    set_err("invalid render mode");
+    return MRF_ERR_INVALID;
+  }
+  return wrap([&] {
+    const int64_t HW = m->hw();
+    if (threshold < 0.0f)
+      threshold = mode == MRF_RENDER_SIMPLE_ACCURACY ? m->prm.acc_thresh : m->prm.occ_thresh;
+    m->s_img.reserve((size_t)HW * 4, false, m->stream);
+    m->s_part.reserve(64, false, m->stream);
+    CK(cudaMemsetAsync(m->s_part.p, 0, 32, m->stream));
+    m->g.brick_slot = m->d_slot.as<int>();
+    const float* bel = m->d_belief.as<float>();
+    if (m->n_bricks == 0) {
+      m->s_dense.reserve(4, false, m->stream);
+      bel = m->s_dense.as<float>();
+    }
+    CK(launch_render(mode, m->g, P, depth_clean_dev, bel, threshold, m->s_img.as<float>(),
+                     reinterpret_cast<unsigned long long*>(m->s_part.p), m->stream));
+    unsigned long long h[4] = {0, 0, 0, 0};
+    CK(cudaMemcpyAsync(h, m->s_part.p, 32, cudaMemcpyDeviceToHost, m->stream));
+    if (out_img)
+      CK(cudaMemcpyAsync(out_img, m->s_img.p, (size_t)HW * 4, cudaMemcpyDeviceToHost, m->stream));
+    sync(m);
+    if (counts)
+      for (int k = 0; k < 4; ++k) counts[k] = (int64_t)h[k];
+    if (out_score) {
+      double n = (double)HW;
+      // src/cuda/gvdbhelper.cu:16-62: accuracy = #1 / (pixels - #(-1));
+      // simple accuracy = (TP + TN) / pixels with TP = #1, TN = #(-1)
+      if (mode == MRF_RENDER_ACCURACY)
+        *out_score = (n - h[0]) > 0 ? (float)(h[2] / (n - (double)h[0])) : 0.0f;
+      else if (mode == MRF_RENDER_SIMPLE_ACCURACY)
+        *out_score = (float)(((double)h[2] + (double)h[0]) / n);
+      else
+        *out_score = 0.0f;
+    }
+  });
+}
+
+mrf_status mrf_render(mrf_map* m, int mode, const float* pose, const float* depth_host,
+                      float threshold, float* out_img, float* out_score, int64_t* counts) {
+  if (guard(m) != MRF_OK) return MRF_ERR_INVALID;
+  if (!pose || !depth_host) {
+    set_err("null argument");
+    return MRF_ERR_INVALID;
+  }
+  mrf_status st = wrap([&] {
+    const int64_t HW = m->hw();
+    m->s_depth_in.reserve((size_t)HW * 4, false, m->stream);
+    m->s_depth.reserve((size_t)HW * 4, false, m->stream);
+    CK(cudaMemcpyAsync(m->s_depth_in.p, depth_host, (size_t)HW * 4, cudaMemcpyHostToDevice, m->stream));
+    CK(launch_clean_depth(m->s_depth_in.as<float>(), m->s_depth.as<float>(), m->prm.rows,
+                          m->prm.cols, m->stream));
+  });
+  if (st != MRF_OK) return st;
+  Pose P;
+  set_pose(P, pose);
+  return render_impl(m, mode, P, m->s_depth.as<float>(), threshold, out_img, out_score, counts);
+}
+
+mrf_status mrf_render_view(mrf_map* m, int mode, int view_id, float threshold, float* out_img,
+                           float* out_score, int64_t* counts) {
+  if (guard(m) != MRF_OK) return MRF_ERR_INVALID;
+  if (view_id < 0 || view_id >= (int)m->views.size()) {
+    set_err("invalid view id");
+    return MRF_ERR_INVALID;
+  }
+  const View& v = m->views[view_id];
+  return render_impl(m, mode, v.pose, v.depth.as<float>(), threshold, out_img, out_score, counts);
 }
 
 mrf_status mrf_num_bricks(mrf_map* m, int64_t* n) {

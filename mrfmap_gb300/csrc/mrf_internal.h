@@ -46,9 +46,20 @@ struct RayMeta {
   uint16_t n_post;  // incidences receiving a message
   uint16_t r0;      // Pre-pass visibility start
   uint16_t rinf;    // visibility start of the infinity term
-  uint32_t flags;   // bit0: infinity term applies
+  uint32_t flags;   // bit0: infinity term applies; bits 16-31: k_dyn
 };
 static_assert(sizeof(RayMeta) == 16, "RayMeta layout");
+
+// k_dyn: first Post incidence with a non-zero potential (n_post if none).
+// Before it every Post quantity of the ray is exactly zero (tau = 0, F = 0,
+// mu1 = 0), so the outgoing probability is exactly the clamp floor F_EPS and
+// the message is F_EPS * l: static for the life of the incidence lists.
+__host__ __device__ __forceinline__ int ray_kdyn(const RayMeta& m) { return (int)(m.flags >> 16); }
+
+// incidence classes written by the trace (build scratch)
+constexpr uint8_t kIncNone = 0;    // padding, or Pre-only (no message)
+constexpr uint8_t kIncStatic = 1;  // message F_EPS * l
+constexpr uint8_t kIncDyn = 2;     // message recomputed every iteration
 
 constexpr int kMaxRayLen = 65532;        // n_pre fits uint16 after padding to 4
 constexpr uint32_t kNoVoxel = 0xFFFFFFFFu;  // padding incidences
@@ -74,17 +85,31 @@ cudaError_t launch_trace_count(const Geom& g, const Pose& P, const float* depth,
 cudaError_t launch_trace_emit(const Geom& g, const Pose& P, const float* depth,
                               const uint32_t* pix_off, uint32_t inc_base, RayMeta* meta,
                               uint32_t* inc_vox, float* inc_len, float* inc_mu, float* post_len,
-                              int* err, cudaStream_t s);
+                              uint8_t* inc_cls, int* err, cudaStream_t s);
 // pairs in voxel order and the pair-grouped positions
 cudaError_t launch_vox_heads(const uint32_t* sk, uint32_t n, uint32_t* flag, cudaStream_t s);
 cudaError_t launch_pairs_from_sorted(const uint32_t* sk, const uint32_t* sidx, const uint32_t* flag,
                                      const uint32_t* scan, uint32_t n, uint32_t pair_base,
                                      uint32_t perm_base, uint32_t inc_base, uint32_t* pair_vox,
-                                     uint32_t* seg, uint32_t* perm, uint32_t* inc_pair,
-                                     cudaStream_t s);
-cudaError_t launch_pair_cum(const uint32_t* seg, const uint32_t* sidx, uint32_t p0, uint32_t np,
-                            uint32_t perm_base, uint32_t inc_base, const float* post_len, float* cum,
-                            cudaStream_t s);
+                                     uint32_t* seg, uint32_t* inc_pair, cudaStream_t s);
+// per pair: cumulative length, summed static messages, dynamic incidences
+cudaError_t launch_pair_stats(const uint32_t* seg, const uint32_t* sidx, uint32_t p0, uint32_t np,
+                              uint32_t perm_base, uint32_t inc_base, const float* post_len,
+                              const uint8_t* cls, float* cum, float* stat, uint32_t* ndyn,
+                              cudaStream_t s);
+// dynamic incidences of a view in pair-grouped order (dperm) and the pairs
+// that own them (dpair, with their first position dseg)
+cudaError_t launch_dyn_flags(const uint32_t* sidx, uint32_t n, uint32_t inc_base, const uint8_t* cls,
+                             uint32_t* flag, cudaStream_t s);
+cudaError_t launch_dyn_scatter(const uint32_t* sidx, const uint32_t* flag, const uint32_t* scan,
+                               uint32_t n, uint32_t inc_base, uint32_t dperm_base, uint32_t* dperm,
+                               cudaStream_t s);
+cudaError_t launch_dpair_flags(const uint32_t* ndyn, uint32_t p0, uint32_t np, uint32_t* flag,
+                               cudaStream_t s);
+cudaError_t launch_dpairs(const uint32_t* pflag, const uint32_t* pscan, uint32_t p0, uint32_t np,
+                          const uint32_t* seg, uint32_t perm_base, const uint32_t* dscan,
+                          uint32_t dperm_base, uint32_t dpair_base, uint32_t* dpair, uint32_t* dseg,
+                          cudaStream_t s);
 cudaError_t launch_iota(uint32_t* out, uint32_t n, cudaStream_t s);
 // CUB helpers (scratch-managed by the caller)
 size_t scan_temp_bytes(uint32_t n);
@@ -103,14 +128,17 @@ struct BpArrays {
   const uint32_t* inc_pair;
   const float* inc_len;
   const float* inc_mu;
-  float* inc_pl;           // p*l per incidence, ray order
-  const uint32_t* perm;    // incidence at each pair-grouped position
+  float* inc_pl;           // p*l per incidence, ray order (dynamic ones only)
+  const uint32_t* dperm;   // dynamic incidence at each pair-grouped position
+  const uint32_t* dpair;   // pair owning each dynamic run
+  const uint32_t* dseg;    // first dynamic position of each run
   const uint32_t* pair_vox;
   float* pair_m;
   const float* pair_cum;
+  const float* pair_stat;  // sum of the pair's static messages
+  const uint32_t* pair_ndyn;
   float* pair_lnq;
   float* pair_dm;
-  const uint32_t* pair_seg;
   float* L;
   float* belief;
 };
@@ -130,11 +158,15 @@ cudaError_t launch_ray_bp(const BpArrays& a, const uint32_t* order, uint32_t n_r
                           uint32_t* counter, int fix_reset, int num_sms, cudaStream_t s);
 cudaError_t launch_ray_keys(const RayMeta* meta, uint32_t n, uint32_t* keys, uint32_t* vals,
                             cudaStream_t s);
-// k0..k1: range of sorted (pair-grouped) positions
-// positions k0..k1 hold the pairs p0..p1; tile_first from launch_tile_first
-cudaError_t launch_pair_update(const BpArrays& a, uint32_t k0, uint32_t k1, uint32_t p0, uint32_t p1,
+// dynamic positions k0..k1 hold the runs j0..j1 (dpair/dseg indices);
+// tile_first from launch_tile_first over dseg
+cudaError_t launch_pair_update(const BpArrays& a, uint32_t k0, uint32_t k1, uint32_t j0, uint32_t j1,
                                const uint32_t* tile_first, TileCarry* carry, int jacobi,
                                cudaStream_t s);
+// pairs p0..p1 without dynamic incidences: their constant update, needed
+// once after their messages were reset or remapped
+cudaError_t launch_static_pairs(const BpArrays& a, uint32_t p0, uint32_t p1, int jacobi,
+                                cudaStream_t s);
 cudaError_t launch_tile_first(const uint32_t* seg, uint32_t p0, uint32_t p1, uint32_t k0, uint32_t k1,
                               uint32_t* out, cudaStream_t s);
 cudaError_t launch_voxel_apply(const uint32_t* vseg, const uint32_t* vpairs, const uint32_t* vvox,
@@ -146,6 +178,10 @@ cudaError_t launch_remap_scatter(const uint32_t* pair_vox, const float* pair_m, 
 cudaError_t launch_remap_gather(const uint32_t* pair_vox, float* pair_m, uint32_t n,
                                 const float* dense, cudaStream_t s);
 cudaError_t launch_fill_f32(float* p, int64_t n, float v, cudaStream_t s);
+// out[0] = bits of max |a - b| over n floats (non-negative: the bit order is
+// the value order, so an integer max is exact and order-independent)
+cudaError_t launch_max_abs_diff(const float* a, const float* b, int64_t n, uint32_t* out,
+                                cudaStream_t s);
 cudaError_t launch_fill_u32(uint32_t* p, int64_t n, uint32_t v, cudaStream_t s);
 cudaError_t launch_add_u32(uint32_t* p, uint32_t n, uint32_t v, cudaStream_t s);
 cudaError_t launch_vflag(const uint32_t* sk, uint32_t n, uint32_t* flag, cudaStream_t s);
@@ -159,6 +195,11 @@ cudaError_t launch_likelihood(const Geom& g, const Pose& P, const float* depth, 
                               float* out_img, double* partials, int nblocks, cudaStream_t s);
 int likelihood_blocks(const Geom& g);
 cudaError_t launch_reduce_partials(const double* partials, int n, float* out_sum, cudaStream_t s);
+
+// evaluation renders (mode 0-3, see mrf_render.cu); counts: 4 zeroed u64
+cudaError_t launch_render(int mode, const Geom& g, const Pose& P, const float* depth,
+                          const float* belief, float thresh, float* out, unsigned long long* counts,
+                          cudaStream_t s);
 
 // Map state the likelihood needs, for entry points outside mrf_capi.cu: the
 // map's geometry (device brick table and sensor tables), its belief field,

@@ -34,6 +34,11 @@ float* out_buffer(py::array& out, int64_t rows, int64_t cols, const char* what) 
   return static_cast<float*>(out.mutable_data());
 }
 
+void check_depth(const farr& depth, const gvdb_params_t& p) {
+  if (depth.ndim() != 2 || depth.shape(0) != p.rows || depth.shape(1) != p.cols)
+    throw std::invalid_argument("depth image size does not match params");
+}
+
 std::shared_ptr<GVDBImage> make_image(const farr& d, const gvdb_params_t& p) {
   if (d.ndim() != 2) throw std::invalid_argument("depth image must be 2-D");
   return std::make_shared<GVDBImage>(d.data(), (int)d.shape(0), (int)d.shape(1), p);
@@ -119,6 +124,14 @@ PYBIND11_MODULE(GVDBPyModules, m) {
              return s.get_likelihood_image_at_pose(pose16(pose).data(), img,
                                                    out_buffer(out, gvdb_params_.rows, gvdb_params_.cols, "image"));
            })
+      .def("get_expected_depth_image", [](GVDBInference& s, unsigned id, py::array out) {
+        s.get_expected_depth_image(id, out_buffer(out, gvdb_params_.rows, gvdb_params_.cols, "image"));
+      })
+      .def("get_accuracy_image_at_pose",
+           [](GVDBInference& s, farr pose, std::shared_ptr<GVDBImage> img, py::array out) {
+             return s.get_accuracy_image_at_pose(pose16(pose).data(), img,
+                                                 out_buffer(out, gvdb_params_.rows, gvdb_params_.cols, "image"));
+           })
       .def("get_occupied_voxels_mask", [](GVDBInference& s, py::array out, float thr) {
         if (!py::isinstance<py::array_t<int>>(out) || out.ndim() != 2)
           throw py::type_error("mask must be a 2-D int32 array");
@@ -163,10 +176,39 @@ PYBIND11_MODULE(GVDBPyModules, m) {
            })
       .def("get_likelihood_image_at_pose_with_depth",
            [](GVDBMapLikelihoodEstimator& s, farr pose, farr depth, py::array out) {
-             if (depth.ndim() != 2 || depth.shape(0) != s.params_.rows || depth.shape(1) != s.params_.cols)
-               throw std::invalid_argument("depth image size does not match params");
+             check_depth(depth, s.params_);
              return s.get_likelihood_image_at_pose_with_depth(
                  pose16(pose).data(), depth.data(), out_buffer(out, s.params_.rows, s.params_.cols, "image"));
+           })
+      .def("get_accuracy_image", [](GVDBMapLikelihoodEstimator& s, unsigned id, py::array out) {
+        s.get_accuracy_image(id, out_buffer(out, s.params_.rows, s.params_.cols, "image"));
+      })
+      .def("get_accuracy_image_at_pose",
+           [](GVDBMapLikelihoodEstimator& s, farr pose, std::shared_ptr<GVDBImage> img, py::array out) {
+             return s.get_accuracy_image_at_pose(pose16(pose).data(), img,
+                                                 out_buffer(out, s.params_.rows, s.params_.cols, "image"));
+           })
+      .def("get_accuracy_image_at_pose_with_depth",
+           [](GVDBMapLikelihoodEstimator& s, farr pose, farr depth, py::array out) {
+             check_depth(depth, s.params_);
+             return s.get_accuracy_image_at_pose_with_depth(
+                 pose16(pose).data(), depth.data(), out_buffer(out, s.params_.rows, s.params_.cols, "image"));
+           })
+      .def("get_simple_accuracy_at_pose",
+           [](GVDBMapLikelihoodEstimator& s, farr pose, std::shared_ptr<GVDBImage> img) {
+             return s.get_simple_accuracy_at_pose(pose16(pose).data(), img);
+           })
+      .def("get_simple_accuracy_image_at_pose_with_depth",
+           [](GVDBMapLikelihoodEstimator& s, farr pose, farr depth, py::array out) {
+             check_depth(depth, s.params_);
+             return s.get_simple_accuracy_image_at_pose_with_depth(
+                 pose16(pose).data(), depth.data(), out_buffer(out, s.params_.rows, s.params_.cols, "image"));
+           })
+      .def("get_occ_thresh_image_at_pose",
+           [](GVDBMapLikelihoodEstimator& s, farr pose, std::shared_ptr<GVDBImage> img, py::array out,
+              float occ_thresh) {
+             s.get_occ_thresh_image_at_pose(pose16(pose).data(), img,
+                                            out_buffer(out, s.params_.rows, s.params_.cols, "image"), occ_thresh);
            })
       .def("set_selected_x_y", &GVDBMapLikelihoodEstimator::set_selected_x_y)
       .def("set_acc_thresh", &GVDBMapLikelihoodEstimator::set_acc_thresh)

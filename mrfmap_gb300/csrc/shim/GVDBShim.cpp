@@ -275,6 +275,19 @@ float GVDBInference::get_likelihood_image_at_pose(const float* pose,
   return s;
 }
 
+void GVDBInference::get_expected_depth_image(unsigned id, float* out) {
+  mrf_check(mrf_render_view(map_->handle(), MRF_RENDER_EXPECTED_DEPTH, (int)id, -1.0f, out, nullptr,
+                            nullptr));
+}
+
+float GVDBInference::get_accuracy_image_at_pose(const float* pose, const std::shared_ptr<GVDBImage>& img,
+                                                float* out) {
+  float s = 0.0f;
+  mrf_check(mrf_render(map_->handle(), MRF_RENDER_ACCURACY, pose, img->depth().data(), -1.0f, out, &s,
+                       nullptr));
+  return s;
+}
+
 mrf_stats GVDBInference::stats() const {
   mrf_stats s{};
   mrf_check(mrf_stats_get(map_->handle(), &s));
@@ -321,4 +334,42 @@ float GVDBMapLikelihoodEstimator::get_likelihood_image_at_pose_with_depth(const 
   float s = 0.0f;
   mrf_check(mrf_likelihood(map_->handle(), pose, depth, out, &s));
   return s;
+}
+
+void GVDBMapLikelihoodEstimator::get_accuracy_image(unsigned id, float* out) {
+  get_accuracy_image_at_pose(poses_.at(id).data(), images_.at(id), out);
+}
+
+float GVDBMapLikelihoodEstimator::get_accuracy_image_at_pose(const float* pose,
+                                                             const std::shared_ptr<GVDBImage>& img,
+                                                             float* out) {
+  return get_accuracy_image_at_pose_with_depth(pose, img->depth().data(), out);
+}
+
+float GVDBMapLikelihoodEstimator::get_accuracy_image_at_pose_with_depth(const float* pose,
+                                                                        const float* depth, float* out) {
+  float s = 0.0f;
+  mrf_check(mrf_render(map_->handle(), MRF_RENDER_ACCURACY, pose, depth, -1.0f, out, &s, nullptr));
+  return s;
+}
+
+float GVDBMapLikelihoodEstimator::get_simple_accuracy_at_pose(const float* pose,
+                                                              const std::shared_ptr<GVDBImage>& img) {
+  return get_simple_accuracy_image_at_pose_with_depth(pose, img->depth().data(), nullptr);
+}
+
+float GVDBMapLikelihoodEstimator::get_simple_accuracy_image_at_pose_with_depth(const float* pose,
+                                                                               const float* depth,
+                                                                               float* out) {
+  float s = 0.0f;
+  mrf_check(mrf_render(map_->handle(), MRF_RENDER_SIMPLE_ACCURACY, pose, depth, params_.acc_thresh, out,
+                       &s, nullptr));
+  return s;
+}
+
+void GVDBMapLikelihoodEstimator::get_occ_thresh_image_at_pose(const float* pose,
+                                                              const std::shared_ptr<GVDBImage>& img,
+                                                              float* out, float occ_thresh) {
+  mrf_check(mrf_render(map_->handle(), MRF_RENDER_OCC_THRESH, pose, img->depth().data(), occ_thresh, out,
+                       nullptr, nullptr));
 }

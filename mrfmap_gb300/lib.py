@@ -31,11 +31,16 @@ _STATUS = {0: "MRF_OK", 1: "MRF_ERR_INVALID", 2: "MRF_ERR_CUDA", 3: "MRF_ERR_OOM
 
 # every symbol declared in include/mrfmap_gb300.h
 EXPORTS = ["mrf_create", "mrf_destroy", "mrf_last_error", "mrf_add_view", "mrf_add_view_device",
-           "mrf_set_pose", "mrf_infer", "mrf_reset_state", "mrf_likelihood_view", "mrf_likelihood",
+           "mrf_set_pose", "mrf_infer", "mrf_infer_converge", "mrf_reset_state", "mrf_likelihood_view", "mrf_likelihood",
            "mrf_likelihood_device", "mrf_likelihood_device_noalloc", "mrf_num_bricks", "mrf_read_bricks", "mrf_read_logodds",
            "mrf_num_nodes", "mrf_read_nodes", "mrf_load_map", "mrf_view_incidences",
            "mrf_device_beliefs",
-           "mrf_stats_get", "mrf_get_stream", "mrf_synchronize"]
+           "mrf_stats_get", "mrf_get_stream", "mrf_synchronize", "mrf_render", "mrf_render_view"]
+
+RENDER_EXPECTED_DEPTH = 0
+RENDER_ACCURACY = 1
+RENDER_SIMPLE_ACCURACY = 2
+RENDER_OCC_THRESH = 3
 
 
 class MrfError(RuntimeError):
@@ -59,7 +64,9 @@ class mrf_stats(C.Structure):
                                          "kernel_launches")] + [("build_ms", C.c_double),
                                                                 ("infer_ms", C.c_double),
                                                                 ("kernel_ms", C.c_double * 4),
-                                                                ("kernel_count", C.c_int64 * 4)]
+                                                                ("kernel_count", C.c_int64 * 4),
+                                                                ("n_inc_dyn", C.c_int64),
+                                                                ("n_pairs_dyn", C.c_int64)]
 
 
 _lib = None
@@ -83,6 +90,7 @@ def load(path: str | None = None):
         "mrf_add_view_device": ([vp, fp, vp, ip], C.c_int),
         "mrf_set_pose": ([vp, C.c_int, fp], C.c_int),
         "mrf_infer": ([vp, ip, C.c_int, C.c_int, C.c_int], C.c_int),
+        "mrf_infer_converge": ([vp, ip, C.c_int, C.c_int, C.c_float, C.c_int, C.c_int, ip, fp], C.c_int),
         "mrf_reset_state": ([vp], C.c_int),
         "mrf_likelihood_view": ([vp, C.c_int, fp, fp], C.c_int),
         "mrf_likelihood": ([vp, fp, fp, fp, fp], C.c_int),
@@ -100,6 +108,8 @@ def load(path: str | None = None):
         "mrf_stats_get": ([vp, C.POINTER(mrf_stats)], C.c_int),
         "mrf_get_stream": ([vp, C.POINTER(vp)], C.c_int),
         "mrf_synchronize": ([vp], C.c_int),
+        "mrf_render": ([vp, C.c_int, fp, fp, C.c_float, fp, fp, i64p], C.c_int),
+        "mrf_render_view": ([vp, C.c_int, C.c_int, C.c_float, fp, fp, i64p], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -193,6 +203,21 @@ class MRFMap:
             a = np.ascontiguousarray(ids, dtype=np.int32)
             _check(self._L.mrf_infer(self._h, a.ctypes.data_as(C.POINTER(C.c_int)), len(a), iters, flags))
 
+    def infer_converge(self, tol: float, max_iters: int = 0, ids=None, flags: int = 0,
+                       check_every: int = 1):
+        """Iterate until the largest belief change is below tol; returns
+        (iterations run, last measured change)."""
+        n = C.c_int()
+        d = C.c_float()
+        if ids is None:
+            _check(self._L.mrf_infer_converge(self._h, None, 0, max_iters, tol, check_every, flags,
+                                              C.byref(n), C.byref(d)))
+        else:
+            a = np.ascontiguousarray(ids, dtype=np.int32)
+            _check(self._L.mrf_infer_converge(self._h, a.ctypes.data_as(C.POINTER(C.c_int)), len(a),
+                                              max_iters, tol, check_every, flags, C.byref(n), C.byref(d)))
+        return n.value, d.value
+
     def reset_state(self):
         _check(self._L.mrf_reset_state(self._h))
 
@@ -249,6 +274,23 @@ class MRFMap:
         _check(self._L.mrf_likelihood_device(self._h, _fp(_f32(pose)), C.c_void_p(depth_ptr),
                                              C.c_void_p(img_ptr) if img_ptr else None,
                                              C.c_void_p(sum_ptr)))
+
+    def render(self, mode: int, pose, depth, threshold: float = -1.0):
+        """Evaluation render at a pose: (image, score, label counts -1/0/1/2)."""
+        img = np.zeros((self.params.rows, self.params.cols), np.float32)
+        s = C.c_float()
+        cnt = np.zeros(4, np.int64)
+        _check(self._L.mrf_render(self._h, mode, _fp(_f32(pose)), _fp(_f32(depth)), threshold, _fp(img),
+                                  C.byref(s), cnt.ctypes.data_as(C.POINTER(C.c_int64))))
+        return img, s.value, cnt
+
+    def render_view(self, mode: int, view: int, threshold: float = -1.0):
+        img = np.zeros((self.params.rows, self.params.cols), np.float32)
+        s = C.c_float()
+        cnt = np.zeros(4, np.int64)
+        _check(self._L.mrf_render_view(self._h, mode, view, threshold, _fp(img), C.byref(s),
+                                       cnt.ctypes.data_as(C.POINTER(C.c_int64))))
+        return img, s.value, cnt
 
     def load_map(self, points, occupancies):
         pts = _f32(points).reshape(-1, 3)

@@ -912,3 +912,100 @@ double orc_likelihood(const orc_map* m, const float* pose, const float* depth, f
   free(dep);
   return total;
 }
+
+/* ---- evaluation renders --------------------------------------------------- */
+/* The likelihood traversal (every active brick to the volume exit) with the
+ * extra state the reference's evaluation kernels keep in hit/norm/clr. */
+static float render_pixel(const orc_map* m, int mode, const float* pose, int x, int y, float d,
+                          float thresh) {
+  const float* sg = lut_at(m, m->sigma_lut, x, y);
+  const float* bs = lut_at(m, m->bias_lut, x, y);
+  int n = m->p.lookup_n;
+  float o[3], dr[3], mult;
+  ray_setup(m, pose, x, y, o, dr, &mult);
+  double A = 0.0, Vprev = 1.0, sum = 0.0;
+  double peak = 0.0;   /* hit.x: peak of (V_prev - V) / l */
+  int peak_ok = 0;     /* hit.y */
+  int occ = -1;        /* norm.y (occupancy-threshold kernel) */
+  int any = 0;
+  float s_last = 0.0f;
+  int64_t cur_lin = -1;
+  int run_open = 0;
+  dda_t r;
+  if (dda_init(&r, m, o, dr)) {
+    int vv[3];
+    float l, tin, te;
+    while (dda_next(&r, vv, &l, &tin, &te)) {
+      int64_t lin;
+      int id = vox_id(m, vv, &lin);
+      if (lin != cur_lin) {
+        if (run_open && mode == 2 && s_last >= d) return 0.0f; /* passed the return: miss */
+        run_open = 0;
+        cur_lin = lin;
+      }
+      if (id < 0) continue;
+      run_open = 1;
+      any = 1;
+      double p = m->belief[id];
+      float sf = te * mult;
+      s_last = sf;
+      if (mode == 2) {
+        if ((float)p >= thresh) return fabsf(sf - d) <= m->p.res ? 1.0f : 2.0f;
+        continue;
+      }
+      double dA = -(-log(1.0 - p)) * (double)l;
+      A += dA;
+      double V = exp(A);
+      if (mode == 0) {
+        /* z-depth of the voxel's corner (GVDB atlas-to-world position) */
+        double zc = fabs((double)pose[2] * ((double)vv[0] - o[0]) + (double)pose[6] * ((double)vv[1] - o[1]) +
+                         (double)pose[10] * ((double)vv[2] - o[2])) * (double)m->p.res;
+        sum += (Vprev - V) * zc;
+      } else {
+        float pd = (sf + poly_f(bs, n, sf)) - d;
+        double w = (Vprev - V) / (double)l;
+        if (mode == 1 && w > peak) {
+          peak = w;
+          peak_ok = fabsf(pd) <= poly_f(sg, n, sf);
+        }
+        if (mode == 3 && pd > 0.0f && occ == -1) occ = (float)p >= thresh;
+      }
+      Vprev = V;
+    }
+  }
+  if (mode == 0) return (float)(sum / (1.0 - Vprev + (double)F_EPS_F));
+  if (mode == 1) {
+    if (!(d > 0.0f)) return -1.0f;
+    if (any && peak > 0.0 && Vprev >= 0.9) return (s_last + poly_f(bs, n, s_last)) <= d ? -1.0f : 0.0f;
+    if (any && peak > 0.0) return (float)peak_ok;
+    return -1.0f;
+  }
+  if (mode == 2) {
+    if (run_open && s_last >= d) return 0.0f;
+    return -1.0f;
+  }
+  return (float)occ;
+}
+
+void orc_render(const orc_map* m, int mode, const float* pose, const float* depth, float thresh,
+                float* out_img, int64_t* counts) {
+  int H = m->p.rows, W = m->p.cols;
+  float* dep = (float*)malloc((size_t)H * W * sizeof(float));
+  clean_depth(m, depth, dep);
+  int64_t cnt[4] = {0, 0, 0, 0};
+  for (int y = 0; y < H; ++y) {
+    for (int x = 0; x < W; ++x) {
+      float d = dep[y * W + x];
+      float v;
+      if (mode != 0 && !(d > 0.0f)) v = -1.0f;
+      else v = render_pixel(m, mode, pose, x, y, d, thresh);
+      out_img[y * W + x] = v;
+      if (mode != 0) {
+        int k = (int)v + 1;
+        if (k >= 0 && k < 4) cnt[k]++;
+      }
+    }
+  }
+  if (counts) memcpy(counts, cnt, sizeof(cnt));
+  free(dep);
+}

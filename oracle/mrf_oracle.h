@@ -91,6 +91,14 @@ int orc_trace_pixel(const orc_map* m, const float* pose, int x, int y,
 double orc_likelihood(const orc_map* m, const float* pose, const float* depth,
                       float* out_img);
 
+/* evaluation renders (src/cuda/gvdbkernels.cu:135-181, 183-293, 295-354,
+ * 1066-1162, 1332-1363): mode 0 expected depth, 1 accuracy (peak of the
+ * first-return density within 1 sigma), 2 simple accuracy (first voxel above
+ * thresh), 3 occupancy at the first voxel past the measurement.  counts[4]
+ * receives the label histogram of labels -1, 0, 1, 2 (modes 1-3). */
+void orc_render(const orc_map* m, int mode, const float* pose, const float* depth, float thresh,
+                float* out_img, int64_t* counts);
+
 /* counters from the last orc_infer: incidence-iterations of Post passes */
 int64_t orc_last_updates(const orc_map* m);
 

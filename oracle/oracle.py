@@ -70,6 +70,7 @@ def lib():
         L.orc_trace_pixel.argtypes = [vp, fp, C.c_int, C.c_int, ip, fp, fp, C.c_int]
         L.orc_likelihood.argtypes = [vp, fp, fp, fp]
         L.orc_likelihood.restype = C.c_double
+        L.orc_render.argtypes = [vp, C.c_int, fp, fp, C.c_float, fp, C.POINTER(C.c_int64)]
         L.orc_last_updates.argtypes = [vp]
         L.orc_last_updates.restype = C.c_int64
         _lib = L
@@ -176,6 +177,13 @@ class OracleMap:
                                     _ptr(s), max_n)
         n = min(n, max_n)
         return vox[:n], ln[:n], s[:n]
+
+    def render(self, mode, pose, depth, thresh):
+        img = np.zeros((self.params.rows, self.params.cols), np.float32)
+        cnt = np.zeros(4, np.int64)
+        self._L.orc_render(self._h, mode, _ptr(_f(pose)), _ptr(_f(depth)), thresh, _ptr(img),
+                           cnt.ctypes.data_as(C.POINTER(C.c_int64)))
+        return img, cnt
 
     def likelihood(self, pose, depth):
         img = np.zeros((self.params.rows, self.params.cols), np.float32)

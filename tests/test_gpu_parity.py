@@ -104,3 +104,22 @@ def test_updates_count(pair):
     st = gm.stats()
     om.infer(iters=1)
     assert st["n_inc_post"] == om.last_updates
+
+
+def test_dynamic_split_matches_oracle_potentials(pair):
+    """Messages before a ray's first non-zero potential are the static F_EPS
+    floor; the GPU recomputes only the rest.  Its count of recomputed
+    incidences equals the oracle's (first non-zero potential per ray)."""
+    w, gm, om, _ = pair
+    gm.infer(iters=1)
+    st = gm.stats()
+    n_dyn = 0
+    for v in range(len(w.poses)):
+        t = om.view_trace(v)
+        for r in range(len(t["meta"])):
+            n_post = t["meta"][r, 1]
+            mu = t["mu"][t["off"][r]:t["off"][r] + n_post]
+            nz = np.flatnonzero(mu)
+            n_dyn += n_post - (nz[0] if len(nz) else n_post)
+    assert st["n_inc_dyn"] == n_dyn
+    assert 0 < st["n_pairs_dyn"] <= st["n_pairs"]

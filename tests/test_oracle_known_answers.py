@@ -299,3 +299,41 @@ def test_second_infer_double_counts_unless_incremental(oracle_lib):
     lp = math.log(float(np.float32(0.1))) - math.log(1 - float(np.float32(0.1)))
     moved = np.abs(L1 - lp) > 1.0
     assert np.mean(np.abs(L2[moved] - lp) > 1.5 * np.abs(L1[moved] - lp)) > 0.5
+
+
+def test_render_single_ray_known_answers(oracle_lib):
+    """Evaluation renders on one ray through one active brick with a single
+    occupied voxel (x = 10, belief 0.9): the ray starts at x = 0.5 so that
+    voxel is left at s = 10.5."""
+    p = _params(sigma=0.5)
+    m = O.OracleMap(p)
+    P = _pose_x((0.5, 16.5, 16.5), p)
+    m.add_view(P, np.array([[10.0]], np.float32))
+    b = np.zeros((m.num_bricks, 512), np.float32)
+    slot = [tuple(c) for c in m.brick_coords()].index((1, 2, 2))
+    b[slot, (2 * 8 + 0) * 8 + 0] = 0.9
+    m.set_beliefs(b)
+
+    def r(mode, d, thresh=0.5):
+        img, cnt = m.render(mode, P, np.array([[d]], np.float32), thresh)
+        return float(img[0, 0]), cnt
+
+    # expected depth: (1 - 0.1) * z(corner 10 - 0.5) / (1 - 0.1 + F_EPS)
+    v, _ = r(0, 10.0)
+    assert v == pytest.approx(0.9 * 9.5 / (0.9 + F_EPS), rel=1e-5)
+    # accuracy: density peak at s = 10.5, within one sigma (0.5) of d
+    assert r(1, 10.2)[0] == 1.0
+    assert r(1, 11.5)[0] == 0.0
+    v, cnt = r(1, float("nan"))
+    assert v == -1.0 and list(cnt) == [1, 0, 0, 0]
+    # simple accuracy: first voxel >= thresh, true positive within one voxel
+    assert r(2, 10.0)[0] == 1.0
+    assert r(2, 12.0)[0] == 2.0
+    assert r(2, 10.0, thresh=0.95)[0] == 0.0   # brick ends (s = 15.5) past d
+    assert r(2, 20.0, thresh=0.95)[0] == -1.0  # never reaches d inside the map
+    # occupancy at the first voxel past the measurement
+    assert r(3, 10.0)[0] == 1.0
+    assert r(3, 11.0)[0] == 0.0
+    assert r(3, 20.0)[0] == -1.0
+    v, cnt = r(3, 10.0)
+    assert list(cnt) == [0, 0, 1, 0]
