@@ -123,6 +123,70 @@ MRF_API mrf_status mrf_infer(mrf_map* map, const int* ids, int n_ids, int iters,
 MRF_API mrf_status mrf_infer_converge(mrf_map* map, const int* ids, int n_ids, int max_iters,
                                       float tol, int check_every, int flags, int* iters_done,
                                       float* last_delta);
+/* Warm start (no reference counterpart).  From a predicted total log-odds
+ * field logodds[n_bricks x 512] (slot order, as mrf_read_logodds): pairs
+ * whose messages are build constants get them exactly, the other pairs of
+ * a voxel share the rest of logodds - logit(prior) in proportion to their
+ * cumulative lengths; `sweeps` (>= 0) clamped iterations m <- F(logodds -
+ * m) then refine the messages (one Jacobi evaluation of every ray factor
+ * each), and the total log-odds is rebuilt from them (logit(prior) + sum of
+ * messages).  The BP equations and their fixed point are unchanged;
+ * continue with MRF_INCREMENTAL so the messages are kept.  The _device form
+ * takes a device pointer. */
+MRF_API mrf_status mrf_warm_start(mrf_map* map, const float* logodds, int sweeps);
+MRF_API mrf_status mrf_warm_start_device(mrf_map* map, const float* logodds_dev, int sweeps);
+
+/* BP state I/O (no reference counterpart; checkpoint / resume of the
+ * message state).  mrf_read_messages writes camera view_id's messages as a
+ * dense field [n_bricks x 512] (slot order; 0 where the camera has no
+ * pair); mrf_write_messages sets them from one; mrf_rebuild_logodds sets
+ * the total log-odds to logit(prior) + the sum of every camera's messages
+ * (pairs past the length gate) and the beliefs from it. */
+MRF_API mrf_status mrf_read_messages(mrf_map* map, int view_id, float* out_dense);
+MRF_API mrf_status mrf_write_messages(mrf_map* map, int view_id, const float* dense);
+MRF_API mrf_status mrf_rebuild_logodds(mrf_map* map);
+
+/* Warm-start features (no reference counterpart): feat_dev receives
+ * [n_bricks x 512 x 4] floats (slot order): the current belief, then
+ * log(1 + x) of the voxel's pass-through length, of its potential mass
+ * (sum of mu * l) and of its length inside the cameras' potential windows,
+ * each summed over the cameras that see it (lengths in voxels). */
+MRF_API mrf_status mrf_warm_features(mrf_map* map, float* feat_dev);
+
+/* The warm-start network (no reference counterpart): three 3x3x3
+ * convolutions over 8^3 bricks, 4 -> 16 -> 16 -> 1 channels, ReLU between,
+ * zeros beyond the brick faces; BF16 tensor-core operands with FP32
+ * accumulation; FP32 master parameters (mrf_net_num_params floats:
+ * W1[27][4][16] b1[16] W2[27][16][16] b2[16] W3[27][16][1] b3[1], tap =
+ * (dx*3 + dy)*3 + dz).  Every pointer is a device pointer; stream is a
+ * cudaStream_t (NULL: the default stream); workspace holds
+ * mrf_net_workspace_bytes(n_bricks) bytes.
+ *   mrf_net_forward: out[n_bricks x 512] predicted log-odds from
+ *     feat[n_bricks x 512 x 4].
+ *   mrf_net_gradients: loss = sum w (y - target)^2 / norm over the voxels
+ *     and its gradient grads[mrf_net_num_params] (deterministic).
+ *   mrf_net_adam: one Adam step (bias-corrected, step >= 1). */
+MRF_API int64_t mrf_net_num_params(void);
+MRF_API int64_t mrf_net_workspace_bytes(int64_t n_bricks);
+MRF_API mrf_status mrf_net_forward(const float* params, const float* feat, int64_t n_bricks,
+                                   float* out, void* workspace, void* stream);
+MRF_API mrf_status mrf_net_gradients(const float* params, const float* feat, const float* target,
+                                     const float* weight, int64_t n_bricks, float norm, float* grads,
+                                     float* loss, void* workspace, void* stream);
+MRF_API mrf_status mrf_net_adam(float* params, const float* grads, float* m1, float* m2, int64_t n,
+                                float lr, float beta1, float beta2, float eps, int step, void* stream);
+
+/* Autotuner (no reference counterpart).  The ray-message kernel comes in
+ * variants that differ in register budget (resident blocks per SM) and in
+ * the cache policy of its streamed loads; their arithmetic is identical, so
+ * the choice never changes a result.  mrf_autotune times every variant on
+ * this map's own incidence lists (reps timed passes over every view after
+ * one warm-up), keeps the fastest and returns per-variant milliseconds per
+ * pass in ms_out[0..min(cap, mrf_ray_variants())). */
+MRF_API int mrf_ray_variants(void);
+MRF_API mrf_status mrf_set_ray_variant(mrf_map* map, int variant);
+MRF_API mrf_status mrf_autotune(mrf_map* map, int reps, double* ms_out, int cap, int* chosen);
+
 /* Extension: log-odds back to the prior, beliefs to 0, messages to 0. */
 MRF_API mrf_status mrf_reset_state(mrf_map* map);
 

@@ -28,7 +28,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "--expt-relaxed-constexpr", "-Xc
               "-Xcompiler", "-ffp-contract=off", "-Xcompiler", "-fvisibility=hidden"]
 
 CU_SOURCES = ["mrf_build.cu", "mrf_bp.cu", "mrf_like.cu", "mrf_capi.cu", "mrf_noalloc.cu",
-              "mrf_render.cu"]
+              "mrf_render.cu", "mrf_warmnet.cu"]
 HEADERS = ["mrf_internal.h", "mrf_geometry.cuh", "mrf_like_pixel.cuh"]
 
 

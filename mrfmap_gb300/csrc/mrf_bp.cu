@@ -42,15 +42,30 @@ __device__ __forceinline__ T warp_sum(T v) {
   return v;
 }
 
-__global__ void k_pair_prepare(const uint32_t* __restrict__ pair_vox, const float* __restrict__ m,
-                               const float* __restrict__ L, float* __restrict__ lnq,
-                               float* __restrict__ dm, uint32_t p0, uint32_t p1) {
-  uint32_t p = p0 + blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= p1) return;
-  float eta = L[pair_vox[p]] - m[p];
-  float qq = clampf(1.0f / (1.0f + expf(eta)), kFEps, 1.0f - kFEps);
-  lnq[p] = logf(qq);
-  if (dm) dm[p] = __int_as_float(0x7fc00000);  // Jacobi: NaN until the pair updates
+// kPrepPer pairs per thread, strided by the block so that every load stays
+// coalesced and a thread keeps kPrepPer independent L gathers in flight
+constexpr int kPrepThreads = 256;
+constexpr int kPrepPer = 4;
+
+__global__ void __launch_bounds__(kPrepThreads)
+    k_pair_prepare(const uint32_t* __restrict__ pair_vox, const float* __restrict__ m,
+                   const float* __restrict__ L, float* __restrict__ lnq, float* __restrict__ dm,
+                   uint32_t p0, uint32_t p1) {
+  const uint32_t base = p0 + blockIdx.x * (kPrepThreads * kPrepPer) + threadIdx.x;
+  float eta[kPrepPer];
+#pragma unroll
+  for (int k = 0; k < kPrepPer; ++k) {
+    const uint32_t p = base + k * kPrepThreads;
+    eta[k] = p < p1 ? L[pair_vox[p]] - m[p] : 0.0f;
+  }
+#pragma unroll
+  for (int k = 0; k < kPrepPer; ++k) {
+    const uint32_t p = base + k * kPrepThreads;
+    if (p >= p1) break;
+    float qq = clampf(1.0f / (1.0f + expf(eta[k])), kFEps, 1.0f - kFEps);
+    lnq[p] = logf(qq);
+    if (dm) dm[p] = __int_as_float(0x7fc00000);  // Jacobi: NaN until the pair updates
+  }
 }
 
 // ---- ray messages ----------------------------------------------------------
@@ -65,10 +80,11 @@ __global__ void k_pair_prepare(const uint32_t* __restrict__ pair_vox, const floa
 // range [k_dyn, n_post) only: before k_dyn every potential is zero, so
 // tau_i = 0, F_i = 0, mu1_i = 0 and p_i is exactly the clamp floor F_EPS
 // (static messages, summed once per build into the pairs).  Potentials are
-// loaded from k_dyn (rounded down to a vector) on.  A ray of one chunk keeps
-// pass 1's values in registers; longer rays recompute the dynamic range in
-// pass 2 from A_{k_dyn - 1}.  The tau sums of rays longer than kLongRay are
-// formed in FP64.
+// loaded from k_dyn (rounded down to a vector) on.  Pass 2 re-reads the
+// dynamic range (a sixth of the incidences, mostly still in L1/L2) from
+// A_{k_dyn - 1} instead of keeping pass 1's slice in registers: the kernel
+// then fits 64 registers, eight resident blocks per SM.  The tau sums of
+// rays longer than kLongRay are formed in FP64.
 //
 // Pre visibility restarts at r0 (the reference restores its carried state
 // only once the accumulated tau is non-zero, gvdbkernels.cu:708-715):
@@ -89,9 +105,18 @@ struct Slice {
   float A[kE], q[kE], mu[kE], len[kE];
 };
 
+// streamed incidence arrays: read-only path (kPol 0) or evict-first
+// streaming loads (kPol 1) that leave L2 to the ln q gathers
+template <int kPol, typename T>
+__device__ __forceinline__ T ld_stream(const T* p) {
+  if (kPol) return __ldcs(p);
+  return __ldg(p);
+}
+
 // loads a lane's kE incidences at i0 (those >= n read as zero; potentials
 // below kmu, a multiple of 4, are known zeros and not loaded), gathers ln q,
 // forms prefix exponents from carryA; returns the chunk total of l ln q
+template <int kPol>
 __device__ __forceinline__ float load_slice(Slice& s, uint32_t off, int i0, int n, int kmu,
                                             float carryA, int lane,
                                             const uint32_t* __restrict__ inc_pair,
@@ -105,9 +130,9 @@ __device__ __forceinline__ float load_slice(Slice& s, uint32_t off, int i0, int 
     uint4 p = make_uint4(0u, 0u, 0u, 0u);
     float4 l = make_float4(0.f, 0.f, 0.f, 0.f), m = make_float4(0.f, 0.f, 0.f, 0.f);
     if (i < n) {
-      p = __ldg(reinterpret_cast<const uint4*>(inc_pair + off + i));
-      l = __ldg(reinterpret_cast<const float4*>(inc_len + off + i));
-      if (i >= kmu) m = __ldg(reinterpret_cast<const float4*>(inc_mu + off + i));
+      p = ld_stream<kPol>(reinterpret_cast<const uint4*>(inc_pair + off + i));
+      l = ld_stream<kPol>(reinterpret_cast<const float4*>(inc_len + off + i));
+      if (i >= kmu) m = ld_stream<kPol>(reinterpret_cast<const float4*>(inc_mu + off + i));
     }
     pid[4 * v + 0] = p.x; pid[4 * v + 1] = p.y; pid[4 * v + 2] = p.z; pid[4 * v + 3] = p.w;
     s.len[4 * v + 0] = l.x; s.len[4 * v + 1] = l.y; s.len[4 * v + 2] = l.z; s.len[4 * v + 3] = l.w;
@@ -186,9 +211,7 @@ __device__ __forceinline__ Acc emit_slice(const float (&vmu)[kE], const float (&
   return carryF + (Acc)__shfl_sync(kFull, ex + run, 31);
 }
 
-// kOne: the ray fits one chunk (pass 2 from registers); otherwise pass 2
-// recomputes the dynamic range
-template <bool kOne, typename Acc>
+template <typename Acc, int kPol>
 __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, const uint32_t* __restrict__ inc_pair,
                                             const float* __restrict__ inc_len,
                                             const float* __restrict__ inc_mu,
@@ -204,13 +227,12 @@ __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, const uint32_t* _
   float carryA = 0.0f, Ar0 = 0.0f, Arinf = 0.0f, Ak = 0.0f;
   Acc T = 0;
   Slice s;
-  float vmu[kE];
   for (int base = 0; base < n_pre; base += kChunk) {
     const int i0 = base + kE * lane;
-    float tot = load_slice(s, off, i0, n_pre, k4, carryA, lane, inc_pair, inc_len, inc_mu, lnq);
+    float tot = load_slice<kPol>(s, off, i0, n_pre, k4, carryA, lane, inc_pair, inc_len, inc_mu, lnq);
     if (r0 > 0 && r0 - 1 >= base && r0 - 1 < base + kChunk) Ar0 = slice_value(s, r0 - 1 - base);
     if (rinf > 0 && rinf - 1 >= base && rinf - 1 < base + kChunk) Arinf = slice_value(s, rinf - 1 - base);
-    if (!kOne && k4 > 0 && k4 - 1 >= base && k4 - 1 < base + kChunk) Ak = slice_value(s, k4 - 1 - base);
+    if (k4 > 0 && k4 - 1 >= base && k4 - 1 < base + kChunk) Ak = slice_value(s, k4 - 1 - base);
     // exp(-A_{r0-1}) rescales Post visibility to Pre visibility unless the
     // Post visibility may have underflowed (then exponentiate the difference)
     const bool direct = Ar0 < kUnderflowGuard;
@@ -219,7 +241,6 @@ __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, const uint32_t* _
 #pragma unroll
     for (int j = 0; j < kE; ++j) {
       float V = __expf(s.A[j]);
-      vmu[j] = V * s.mu[j];
       if (i0 + j >= r0 && s.mu[j] != 0.0f) {
         float vp = direct ? __expf(s.A[j] - Ar0) : V * scale;
         w += vp * (1.0f - s.q[j]) * s.mu[j];
@@ -233,15 +254,13 @@ __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, const uint32_t* _
   if (kdyn >= n_post) return;  // every message of the ray is static
   // ---- pass 2: dynamic messages ------------------------------------------
   // F is zero before k_dyn, so the running F starts at zero at k4
-  if (kOne) {
-    emit_slice<Acc>(vmu, s.q, s.len, kE * lane, k4, n_post, T, (Acc)0, lane, off, inc_pl);
-    return;
-  }
   Acc carryF = 0;
+  float vmu[kE];
   float carryA2 = Ak;
   for (int base = k4; base < n_post; base += kChunk) {
     const int i0 = base + kE * lane;
-    float tot2 = load_slice(s, off, i0, n_post, k4, carryA2, lane, inc_pair, inc_len, inc_mu, lnq);
+    float tot2 = load_slice<kPol>(s, off, i0, n_post, k4, carryA2, lane, inc_pair, inc_len, inc_mu,
+                                  lnq);
     carryA2 += tot2;
 #pragma unroll
     for (int j = 0; j < kE; ++j) vmu[j] = __expf(s.A[j]) * s.mu[j];
@@ -252,8 +271,11 @@ __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, const uint32_t* _
 // Persistent launch: each warp takes the next ray from a work counter; rays
 // are queued longest first (sorted once per incidence build), so the long
 // rays start early and the short ones fill the tail.  Which warp handles a
-// ray does not change its result.
-__global__ void __launch_bounds__(kRayWarps * 32) k_ray_bp(const RayMeta* __restrict__ meta,
+// ray does not change its result.  Variants differ only in register budget
+// (kMinBlocks resident blocks per SM) and load policy: their arithmetic is
+// identical, so the autotuner's choice never changes a result.
+template <int kMinBlocks, int kPol>
+__global__ void __launch_bounds__(kRayWarps * 32, kMinBlocks) k_ray_bp(const RayMeta* __restrict__ meta,
                                                            const uint32_t* __restrict__ order,
                                                            uint32_t n_rays,
                                                            uint32_t* __restrict__ counter,
@@ -270,12 +292,10 @@ __global__ void __launch_bounds__(kRayWarps * 32) k_ray_bp(const RayMeta* __rest
     idx = __shfl_sync(kFull, idx, 0);
     if (idx >= n_rays) break;
     RayMeta me = meta[order[idx]];
-    if (me.n_pre <= kChunk)
-      ray_bp_warp<true, float>(me, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
-    else if (me.n_pre <= kLongRay)
-      ray_bp_warp<false, float>(me, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
+    if (me.n_pre <= kLongRay)
+      ray_bp_warp<float, kPol>(me, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
     else
-      ray_bp_warp<false, double>(me, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
+      ray_bp_warp<double, kPol>(me, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
   }
 }
 
@@ -476,6 +496,101 @@ __global__ void k_max_abs_diff(const float* __restrict__ a, const float* __restr
   if ((threadIdx.x & 31) == 0) atomicMax(out, __float_as_uint(mx));
 }
 
+// total log-odds of each voxel rebuilt from its messages (voxel CSR):
+// L = L (already the prior) + sum m over the pairs that pass the length gate
+__global__ void k_voxel_rebuild(const uint32_t* __restrict__ vseg, const uint32_t* __restrict__ vpairs,
+                                const uint32_t* __restrict__ vvox, uint32_t nvox,
+                                const float* __restrict__ m, const float* __restrict__ cum,
+                                float* __restrict__ L, float* __restrict__ belief) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nvox) return;
+  float s = 0.0f;
+  bool any = false;
+  for (uint32_t k = vseg[i]; k < vseg[i + 1]; ++k) {
+    const uint32_t p = vpairs[k];
+    if (cum[p] > kCumLenGate) {
+      s += m[p];
+      any = true;
+    }
+  }
+  if (!any) return;
+  uint32_t v = vvox[i];
+  float Lv = L[v] + s;
+  L[v] = Lv;
+  belief[v] = 1.0f - clampf(1.0f / (1.0f + expf(Lv)), kFEps, 1.0f - kFEps);
+}
+
+// Warm-start initial messages of every voxel's pairs from a predicted total
+// log-odds: pairs without dynamic incidences get their exact constant
+// message; the rest of (L_pred - logit(prior)) is shared among the dynamic
+// pairs in proportion to their cumulative length.  Pairs below the length
+// gate keep 0 (they never update).
+__global__ void k_warm_split(const uint32_t* __restrict__ vseg, const uint32_t* __restrict__ vpairs,
+                             const uint32_t* __restrict__ vvox, uint32_t nvox,
+                             const float* __restrict__ L_pred, float lp, const float* __restrict__ cum,
+                             const float* __restrict__ stat, const uint32_t* __restrict__ ndyn,
+                             float* __restrict__ m) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nvox) return;
+  float fixed = 0.0f, dyn_len = 0.0f;
+  for (uint32_t k = vseg[i]; k < vseg[i + 1]; ++k) {
+    const uint32_t p = vpairs[k];
+    const float c = cum[p];
+    if (!(c > kCumLenGate)) continue;
+    if (ndyn[p]) {
+      dyn_len += c;
+    } else {
+      float a = clampf(stat[p] / c, kFEps, 1.0f - kFEps);
+      fixed += logf(a) - logf(1.0f - a);
+    }
+  }
+  const float rest = L_pred[vvox[i]] - lp - fixed;
+  for (uint32_t k = vseg[i]; k < vseg[i + 1]; ++k) {
+    const uint32_t p = vpairs[k];
+    const float c = cum[p];
+    float mv = 0.0f;
+    if (c > kCumLenGate) {
+      if (ndyn[p]) {
+        mv = rest * (c / dyn_len);
+      } else {
+        float a = clampf(stat[p] / c, kFEps, 1.0f - kFEps);
+        mv = logf(a) - logf(1.0f - a);
+      }
+    }
+    m[p] = mv;
+  }
+}
+
+// Warm-start features of every voxel slot, [slot*512 + local][4]:
+// 0 current belief, 1 log(1 + pass-through length), 2 log(1 + potential
+// mass sum mu*l), 3 log(1 + length inside the potential windows); lengths
+// in voxels, summed over the voxel's cameras in pair order.
+__global__ void k_feat_belief(const float* __restrict__ belief, int64_t n, float* __restrict__ feat) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  *reinterpret_cast<float4*>(feat + 4 * i) = make_float4(belief[i], 0.0f, 0.0f, 0.0f);
+}
+
+__global__ void k_voxel_features(const uint32_t* __restrict__ vseg, const uint32_t* __restrict__ vpairs,
+                                 const uint32_t* __restrict__ vvox, uint32_t nvox,
+                                 const float* __restrict__ cum, const float* __restrict__ stat,
+                                 const float* __restrict__ hit, float* __restrict__ feat) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nvox) return;
+  float pass = 0.0f, mass = 0.0f, win = 0.0f;
+  for (uint32_t k = vseg[i]; k < vseg[i + 1]; ++k) {
+    const uint32_t p = vpairs[k];
+    const float sl = stat[p] * (1.0f / kFEps);
+    pass += sl;
+    mass += hit[p];
+    win += fmaxf(cum[p] - sl, 0.0f);
+  }
+  float* f = feat + 4 * (int64_t)vvox[i];
+  f[1] = log1pf(pass);
+  f[2] = log1pf(mass);
+  f[3] = log1pf(win);
+}
+
 // moving a camera: take its messages out of the total log-odds
 __global__ void k_remove_messages(const uint32_t* __restrict__ pair_vox, float* __restrict__ m,
                                   uint32_t p0, uint32_t p1, float* __restrict__ L,
@@ -545,32 +660,63 @@ inline unsigned blocks(int64_t n, int t) { return (unsigned)std::max<int64_t>(1,
 cudaError_t launch_pair_prepare(const BpArrays& a, uint32_t p0, uint32_t p1, int jacobi,
                                 cudaStream_t s) {
   if (p1 <= p0) return cudaSuccess;
-  k_pair_prepare<<<blocks(p1 - p0, 256), 256, 0, s>>>(a.pair_vox, a.pair_m, a.L, a.pair_lnq,
-                                                      jacobi ? a.pair_dm : nullptr, p0, p1);
+  k_pair_prepare<<<blocks(p1 - p0, kPrepThreads * kPrepPer), kPrepThreads, 0, s>>>(
+      a.pair_vox, a.pair_m, a.L, a.pair_lnq, jacobi ? a.pair_dm : nullptr, p0, p1);
   return cudaGetLastError();
 }
 
 
-int ray_bp_resident_blocks() {
-  static int resident = 0;
-  if (!resident) {
-    int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ray_bp, kRayWarps * 32, 0) !=
-            cudaSuccess ||
-        per_sm < 1)
-      per_sm = 1;
-    resident = per_sm;
+// ray-kernel variants: (resident-block target, load policy)
+#define MRF_RAY_VARIANTS(X) X(0, 0, 0) X(1, 0, 1) X(2, 10, 0) X(3, 10, 1) X(4, 12, 1)
+constexpr int kRayVariants = 5;
+
+int ray_bp_variants() { return kRayVariants; }
+
+namespace {
+template <int kMinBlocks, int kPol>
+int resident_of() {
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ray_bp<kMinBlocks, kPol>, kRayWarps * 32,
+                                                    0) != cudaSuccess ||
+      per_sm < 1)
+    per_sm = 1;
+  return per_sm;
+}
+}  // namespace
+
+int ray_bp_resident_blocks(int variant) {
+  static int resident[kRayVariants] = {0};
+  if (variant < 0 || variant >= kRayVariants) return 1;
+  if (!resident[variant]) {
+    switch (variant) {
+#define X(id, mb, pol) \
+  case id:             \
+    resident[variant] = resident_of<mb, pol>(); \
+    break;
+      MRF_RAY_VARIANTS(X)
+#undef X
+    }
   }
-  return resident;
+  return resident[variant];
 }
 
 cudaError_t launch_ray_bp(const BpArrays& a, const uint32_t* order, uint32_t n_rays,
-                          uint32_t* counter, int fix_reset, int num_sms, cudaStream_t s) {
+                          uint32_t* counter, int fix_reset, int num_sms, int variant, cudaStream_t s) {
   if (!n_rays) return cudaSuccess;
-  int64_t b = std::min<int64_t>((int64_t)num_sms * ray_bp_resident_blocks(),
+  if (variant < 0 || variant >= kRayVariants) return cudaErrorInvalidValue;
+  int64_t b = std::min<int64_t>((int64_t)num_sms * ray_bp_resident_blocks(variant),
                                 (n_rays + kRayWarps - 1) / kRayWarps);
-  k_ray_bp<<<(unsigned)std::max<int64_t>(b, 1), kRayWarps * 32, 0, s>>>(
-      a.meta, order, n_rays, counter, a.inc_pair, a.inc_len, a.inc_mu, a.pair_lnq, a.inc_pl, fix_reset);
+  const unsigned grid = (unsigned)std::max<int64_t>(b, 1);
+  switch (variant) {
+#define X(id, mb, pol)                                                                           \
+  case id:                                                                                       \
+    k_ray_bp<mb, pol><<<grid, kRayWarps * 32, 0, s>>>(a.meta, order, n_rays, counter, a.inc_pair, \
+                                                      a.inc_len, a.inc_mu, a.pair_lnq, a.inc_pl,  \
+                                                      fix_reset);                                 \
+    break;
+    MRF_RAY_VARIANTS(X)
+#undef X
+  }
   return cudaGetLastError();
 }
 
@@ -631,6 +777,31 @@ cudaError_t launch_max_abs_diff(const float* a, const float* b, int64_t n, uint3
   if (e != cudaSuccess || n <= 0) return e;
   int64_t nb = std::min<int64_t>((n + 255) / 256, 4096);
   k_max_abs_diff<<<(unsigned)nb, 256, 0, s>>>(a, b, n, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_warm_split(const uint32_t* vseg, const uint32_t* vpairs, const uint32_t* vvox,
+                              uint32_t nvox, const float* L_pred, float lp, const float* cum,
+                              const float* stat, const uint32_t* ndyn, float* m, cudaStream_t s) {
+  if (!nvox) return cudaSuccess;
+  k_warm_split<<<blocks(nvox, 256), 256, 0, s>>>(vseg, vpairs, vvox, nvox, L_pred, lp, cum, stat, ndyn, m);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_voxel_features(const uint32_t* vseg, const uint32_t* vpairs, const uint32_t* vvox,
+                                  uint32_t nvox, const float* cum, const float* stat, const float* hit,
+                                  const float* belief, int64_t n_slots_vox, float* feat, cudaStream_t s) {
+  if (n_slots_vox <= 0) return cudaSuccess;
+  k_feat_belief<<<blocks(n_slots_vox, 256), 256, 0, s>>>(belief, n_slots_vox, feat);
+  if (nvox) k_voxel_features<<<blocks(nvox, 256), 256, 0, s>>>(vseg, vpairs, vvox, nvox, cum, stat, hit, feat);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_voxel_rebuild(const uint32_t* vseg, const uint32_t* vpairs, const uint32_t* vvox,
+                                 uint32_t nvox, const float* m, const float* cum, float* L, float* belief,
+                                 cudaStream_t s) {
+  if (!nvox) return cudaSuccess;
+  k_voxel_rebuild<<<blocks(nvox, 256), 256, 0, s>>>(vseg, vpairs, vvox, nvox, m, cum, L, belief);
   return cudaGetLastError();
 }
 

@@ -293,17 +293,19 @@ __global__ void k_pairs_from_sorted(const uint32_t* __restrict__ sk, const uint3
 // Per pair, over its incidences in increasing incidence order (the order
 // the reference's cumulative-length pass visits a voxel, pixel-major):
 // cumulative length (fp32), the sum of its static messages F_EPS * l (fp32,
-// each product rounded as the ray kernel would round it) and the number of
-// dynamic incidences.
+// each product rounded as the ray kernel would round it), the number of
+// dynamic incidences and the potential mass sum mu * l (a warm-start
+// feature).
 __global__ void k_pair_stats(const uint32_t* __restrict__ seg, const uint32_t* __restrict__ sidx,
                              uint32_t p0, uint32_t np, uint32_t perm_base, uint32_t inc_base,
                              const float* __restrict__ post_len, const uint8_t* __restrict__ cls,
-                             float* __restrict__ cum, float* __restrict__ stat,
-                             uint32_t* __restrict__ ndyn) {
+                             const float* __restrict__ mu, float* __restrict__ cum,
+                             float* __restrict__ stat, uint32_t* __restrict__ ndyn,
+                             float* __restrict__ hit) {
   uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= np) return;
   uint32_t p = p0 + q;
-  float c = 0.0f, st = 0.0f;
+  float c = 0.0f, st = 0.0f, h = 0.0f;
   uint32_t nd = 0;
   for (uint32_t k = seg[p]; k < seg[p + 1]; ++k) {
     uint32_t i = inc_base + sidx[k - perm_base];
@@ -311,11 +313,13 @@ __global__ void k_pair_stats(const uint32_t* __restrict__ seg, const uint32_t* _
     c += l;
     uint8_t t = cls[i];
     if (t == kIncStatic) st += __fmul_rn(kFEps, l);
+    if (t == kIncDyn) h += mu[i] * l;
     nd += t == kIncDyn;
   }
   cum[p] = c;
   stat[p] = st;
   ndyn[p] = nd;
+  hit[p] = h;
 }
 
 __global__ void k_dyn_flags(const uint32_t* __restrict__ sidx, uint32_t n, uint32_t inc_base,
@@ -435,11 +439,11 @@ cudaError_t launch_pairs_from_sorted(const uint32_t* sk, const uint32_t* sidx, c
 
 cudaError_t launch_pair_stats(const uint32_t* seg, const uint32_t* sidx, uint32_t p0, uint32_t np,
                               uint32_t perm_base, uint32_t inc_base, const float* post_len,
-                              const uint8_t* cls, float* cum, float* stat, uint32_t* ndyn,
-                              cudaStream_t s) {
+                              const uint8_t* cls, const float* mu, float* cum, float* stat,
+                              uint32_t* ndyn, float* hit, cudaStream_t s) {
   if (!np) return cudaSuccess;
   k_pair_stats<<<grid_for(np), kThreads, 0, s>>>(seg, sidx, p0, np, perm_base, inc_base, post_len, cls,
-                                                 cum, stat, ndyn);
+                                                 mu, cum, stat, ndyn, hit);
   return cudaGetLastError();
 }
 

@@ -110,10 +110,11 @@ struct mrf_map {
   int64_t nb_grid = 0, n_bricks = 0;
   std::vector<int> h_coord;
   int version = 0, built_version = -1;
+  int ray_variant = 0;  // ray-kernel variant (mrf_autotune / mrf_set_ray_variant)
   bool has_messages = false;
   std::vector<View> views;
   // arenas
-  DBuf meta, inc_pair, inc_len, inc_mu, inc_pl, pair_vox, pair_m, pair_cum, pair_stat, pair_ndyn,
+  DBuf meta, inc_pair, inc_len, inc_mu, inc_pl, pair_vox, pair_m, pair_cum, pair_stat, pair_ndyn, pair_hit,
       pair_q, pair_dm, pair_seg, dperm, dpair, dseg, carry, ray_order, counters, tile_first;
   uint32_t jac_tile_base = 0;
   int64_t n_inc = 0, n_pairs = 0, n_dperm = 0, n_dpairs = 0;
@@ -347,6 +348,7 @@ void rebuild(mrf_map* m) {
     m->pair_cum.reserve(pb * 4, true, m->stream);
     m->pair_stat.reserve(pb * 4, true, m->stream);
     m->pair_ndyn.reserve(pb * 4, true, m->stream);
+    m->pair_hit.reserve(pb * 4, true, m->stream);
     m->pair_seg.reserve(pb * 4, true, m->stream);
     CK(launch_pairs_from_sorted(m->s_k1.as<uint32_t>(), m->s_v1.as<uint32_t>(), m->s_k0.as<uint32_t>(),
                                 m->s_v0.as<uint32_t>(), nr, v.pair_base, v.perm_base, v.inc_base,
@@ -355,8 +357,8 @@ void rebuild(mrf_map* m) {
     CK(launch_fill_u32(m->pair_seg.as<uint32_t>() + v.pair_base + np, 1, v.perm_base + nr, m->stream));
     CK(launch_pair_stats(m->pair_seg.as<uint32_t>(), m->s_v1.as<uint32_t>(), v.pair_base, np,
                          v.perm_base, v.inc_base, m->s_postlen.as<float>(), m->s_cls.as<uint8_t>(),
-                         m->pair_cum.as<float>(), m->pair_stat.as<float>(),
-                         m->pair_ndyn.as<uint32_t>(), m->stream));
+                         m->inc_mu.as<float>(), m->pair_cum.as<float>(), m->pair_stat.as<float>(),
+                         m->pair_ndyn.as<uint32_t>(), m->pair_hit.as<float>(), m->stream));
     // dynamic incidences in pair-grouped order (a stable compaction of the
     // sorted positions) and the run of each pair that has any
     CK(launch_dyn_flags(m->s_v1.as<uint32_t>(), nr, v.inc_base, m->s_cls.as<uint8_t>(),
@@ -429,6 +431,7 @@ void rebuild(mrf_map* m) {
   m->pair_cum.reserve(pb * 4, true, m->stream);
   m->pair_stat.reserve(pb * 4, true, m->stream);
   m->pair_ndyn.reserve(pb * 4, true, m->stream);
+  m->pair_hit.reserve(pb * 4, true, m->stream);
   m->pair_seg.reserve(pb * 4, true, m->stream);
   m->dpair.reserve((size_t)(dpair_total + 1) * 4, true, m->stream);
   m->dseg.reserve((size_t)(dpair_total + 1) * 4, true, m->stream);
@@ -584,7 +587,7 @@ void enqueue_iteration(mrf_map* m, const BpArrays& a, bool jacobi, int fix, bool
       prof.end();
       prof.begin(1);
       CK(launch_ray_bp(a, m->ray_order.as<uint32_t>() + v.order_base, v.n_active,
-                       m->counters.as<uint32_t>() + c, fix, m->num_sms, m->stream));
+                       m->counters.as<uint32_t>() + c, fix, m->num_sms, m->ray_variant, m->stream));
       prof.end();
       prof.begin(2);
       if (v.n_dperm) {
@@ -610,7 +613,7 @@ void enqueue_iteration(mrf_map* m, const BpArrays& a, bool jacobi, int fix, bool
     uint32_t nact = 0;
     for (const View& v : m->views) nact += v.n_active;
     CK(launch_ray_bp(a, m->ray_order.as<uint32_t>(), nact, m->counters.as<uint32_t>() + V, fix,
-                     m->num_sms, m->stream));
+                     m->num_sms, m->ray_variant, m->stream));
     prof.end();
     prof.begin(2);
     CK(launch_pair_update(a, 0, (uint32_t)m->n_dperm, 0, (uint32_t)m->n_dpairs,
@@ -799,7 +802,8 @@ mrf_status wrap(F&& f) {
 void destroy_bufs(mrf_map* m) {
   DBuf* all[] = {&m->d_sigma, &m->d_bias, &m->d_slot, &m->d_coord, &m->d_L, &m->d_belief,
                  &m->meta, &m->inc_pair, &m->inc_len, &m->inc_mu, &m->inc_pl, &m->pair_vox,
-                 &m->pair_m, &m->pair_cum, &m->pair_stat, &m->pair_ndyn, &m->pair_q, &m->pair_dm,
+                 &m->pair_m, &m->pair_cum, &m->pair_stat, &m->pair_ndyn, &m->pair_hit, &m->pair_q,
+                 &m->pair_dm,
                  &m->pair_seg, &m->dperm, &m->dpair, &m->dseg,
                  &m->carry, &m->ray_order, &m->counters, &m->tile_first,
                  &m->vseg, &m->vpairs, &m->vvox, &m->s_postlen, &m->s_cls, &m->s_pf, &m->s_ps,
@@ -891,7 +895,7 @@ mrf_status mrf_create(const mrf_params* params, mrf_map** out) {
     m->prm.bias_lut = m->bias.data();
     CK(cudaGetDevice(&m->device));
     CK(cudaDeviceGetAttribute(&m->num_sms, cudaDevAttrMultiProcessorCount, m->device));
-    ray_bp_resident_blocks();
+    for (int k = 0; k < ray_bp_variants(); ++k) ray_bp_resident_blocks(k);
     CK(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking));
     CK(cudaEventCreate(&m->ev0));
     CK(cudaEventCreate(&m->ev1));
@@ -1010,6 +1014,204 @@ mrf_status mrf_infer_converge(mrf_map* m, const int* ids, int n_ids, int max_ite
   return wrap([&] {
     run_infer(m, ids, ids ? n_ids : 0, max_iters, flags, tol, check_every, last_delta);
     if (iters_done) *iters_done = (int)m->stats.iters_done;
+  });
+}
+
+// Warm start.  The messages start from a split of the predicted field
+// L_pred: pairs without dynamic incidences get their exact (constant)
+// message, the dynamic pairs of a voxel share the rest of
+// L_pred - logit(prior) in proportion to their cumulative lengths.  Then,
+// with the total log-odds held at L_pred, `sweeps` clamped iterations
+// m <- F(L_pred - m) refine them (each one Jacobi evaluation of every ray
+// factor).  Finally the total log-odds is rebuilt from the messages,
+// L = logit(prior) + sum m, so the state is a consistent BP state: the
+// equations and their fixed point are those of the plain start.
+static void warm_start_impl(mrf_map* m, const float* L_pred, bool device_ptr, int sweeps) {
+  ensure_built(m);
+  if (m->jacobi_version != m->built_version) build_jacobi_csr(m);
+  const int64_t nvox = m->n_bricks * kBrickVox;
+  if (nvox == 0 || m->n_inc == 0) return;
+  if (sweeps < 0) sweeps = 0;
+  const float lp = logf(m->prm.prior) - logf(1.0f - m->prm.prior);
+  CK(cudaMemcpyAsync(m->d_L.p, L_pred, (size_t)nvox * 4,
+                     device_ptr ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, m->stream));
+  CK(launch_warm_split(m->vseg.as<uint32_t>(), m->vpairs.as<uint32_t>(), m->vvox.as<uint32_t>(), m->n_vvox,
+                       m->d_L.as<float>(), lp, m->pair_cum.as<float>(), m->pair_stat.as<float>(),
+                       m->pair_ndyn.as<uint32_t>(), m->pair_m.as<float>(), m->stream));
+  BpArrays a = m->bp();
+  const int V = (int)m->views.size();
+  const uint32_t P = (uint32_t)m->n_pairs;
+  uint32_t nact = 0;
+  for (const View& v : m->views) nact += v.n_active;
+  for (int k = 0; k < sweeps; ++k) {
+    CK(cudaMemsetAsync(m->counters.p, 0, (size_t)(V + 1) * 4, m->stream));
+    CK(launch_pair_prepare(a, 0, P, 1, m->stream));
+    CK(launch_ray_bp(a, m->ray_order.as<uint32_t>(), nact, m->counters.as<uint32_t>() + V, 0,
+                     m->num_sms, m->ray_variant, m->stream));
+    CK(launch_pair_update(a, 0, (uint32_t)m->n_dperm, 0, (uint32_t)m->n_dpairs,
+                          m->tile_first.as<uint32_t>() + m->jac_tile_base, m->carry.as<TileCarry>(),
+                          1, m->stream));
+  }
+  CK(launch_fill_new_voxels(m->d_L.as<float>(), m->d_belief.as<float>(), 0, nvox, lp, m->stream));
+  CK(launch_voxel_rebuild(m->vseg.as<uint32_t>(), m->vpairs.as<uint32_t>(), m->vvox.as<uint32_t>(),
+                          m->n_vvox, m->pair_m.as<float>(), m->pair_cum.as<float>(),
+                          m->d_L.as<float>(), m->d_belief.as<float>(), m->stream));
+  m->has_messages = true;
+  sync(m);
+  check_device_err(m);
+}
+
+// BP state I/O: one camera's messages as a dense field over the voxel slots
+// (0 where the camera has no pair), and the reverse.
+mrf_status mrf_read_messages(mrf_map* m, int view_id, float* out_dense) {
+  if (guard(m) != MRF_OK) return MRF_ERR_INVALID;
+  if (view_id < 0 || view_id >= (int)m->views.size() || !out_dense) {
+    set_err("invalid view id or null argument");
+    return MRF_ERR_INVALID;
+  }
+  return wrap([&] {
+    ensure_built(m);
+    const int64_t nvox = m->n_bricks * kBrickVox;
+    if (nvox == 0) return;
+    const View& v = m->views[view_id];
+    m->s_dense.reserve((size_t)nvox * 4, false, m->stream);
+    CK(cudaMemsetAsync(m->s_dense.p, 0, (size_t)nvox * 4, m->stream));
+    CK(launch_remap_scatter(m->pair_vox.as<uint32_t>() + v.pair_base, m->pair_m.as<float>() + v.pair_base,
+                            v.n_pairs, m->s_dense.as<float>(), m->stream));
+    CK(cudaMemcpyAsync(out_dense, m->s_dense.p, (size_t)nvox * 4, cudaMemcpyDeviceToHost, m->stream));
+    sync(m);
+  });
+}
+
+mrf_status mrf_write_messages(mrf_map* m, int view_id, const float* dense) {
+  if (guard(m) != MRF_OK) return MRF_ERR_INVALID;
+  if (view_id < 0 || view_id >= (int)m->views.size() || !dense) {
+    set_err("invalid view id or null argument");
+    return MRF_ERR_INVALID;
+  }
+  return wrap([&] {
+    ensure_built(m);
+    const int64_t nvox = m->n_bricks * kBrickVox;
+    if (nvox == 0) return;
+    const View& v = m->views[view_id];
+    m->s_dense.reserve((size_t)nvox * 4, false, m->stream);
+    CK(cudaMemcpyAsync(m->s_dense.p, dense, (size_t)nvox * 4, cudaMemcpyHostToDevice, m->stream));
+    CK(launch_remap_gather(m->pair_vox.as<uint32_t>() + v.pair_base, m->pair_m.as<float>() + v.pair_base,
+                           v.n_pairs, m->s_dense.as<float>(), m->stream));
+    m->has_messages = true;
+    sync(m);
+  });
+}
+
+mrf_status mrf_rebuild_logodds(mrf_map* m) {
+  if (guard(m) != MRF_OK) return MRF_ERR_INVALID;
+  return wrap([&] {
+    ensure_built(m);
+    if (m->jacobi_version != m->built_version) build_jacobi_csr(m);
+    const int64_t nvox = m->n_bricks * kBrickVox;
+    if (nvox == 0) return;
+    const float lp = logf(m->prm.prior) - logf(1.0f - m->prm.prior);
+    CK(launch_fill_new_voxels(m->d_L.as<float>(), m->d_belief.as<float>(), 0, nvox, lp, m->stream));
+    CK(launch_voxel_rebuild(m->vseg.as<uint32_t>(), m->vpairs.as<uint32_t>(), m->vvox.as<uint32_t>(),
+                            m->n_vvox, m->pair_m.as<float>(), m->pair_cum.as<float>(),
+                            m->d_L.as<float>(), m->d_belief.as<float>(), m->stream));
+    sync(m);
+  });
+}
+
+mrf_status mrf_warm_features(mrf_map* m, float* feat_dev) {
+  if (guard(m) != MRF_OK) return MRF_ERR_INVALID;
+  if (!feat_dev) {
+    set_err("null argument");
+    return MRF_ERR_INVALID;
+  }
+  return wrap([&] {
+    ensure_built(m);
+    if (m->jacobi_version != m->built_version) build_jacobi_csr(m);
+    const int64_t nvox = m->n_bricks * kBrickVox;
+    CK(launch_voxel_features(m->vseg.as<uint32_t>(), m->vpairs.as<uint32_t>(), m->vvox.as<uint32_t>(),
+                             m->n_vvox, m->pair_cum.as<float>(), m->pair_stat.as<float>(),
+                             m->pair_hit.as<float>(), m->d_belief.as<float>(), nvox, feat_dev,
+                             m->stream));
+    sync(m);
+  });
+}
+
+mrf_status mrf_warm_start(mrf_map* m, const float* logodds, int sweeps) {
+  if (guard(m) != MRF_OK) return MRF_ERR_INVALID;
+  if (!logodds) {
+    set_err("null argument");
+    return MRF_ERR_INVALID;
+  }
+  return wrap([&] { warm_start_impl(m, logodds, false, sweeps); });
+}
+
+mrf_status mrf_warm_start_device(mrf_map* m, const float* logodds_dev, int sweeps) {
+  if (guard(m) != MRF_OK) return MRF_ERR_INVALID;
+  if (!logodds_dev) {
+    set_err("null argument");
+    return MRF_ERR_INVALID;
+  }
+  return wrap([&] { warm_start_impl(m, logodds_dev, true, sweeps); });
+}
+
+int mrf_ray_variants(void) { return ray_bp_variants(); }
+
+static void drop_graphs(mrf_map* m) {
+  for (auto& g : m->graphs) g.version = -1;
+}
+
+mrf_status mrf_set_ray_variant(mrf_map* m, int variant) {
+  if (guard(m) != MRF_OK) return MRF_ERR_INVALID;
+  if (variant < 0 || variant >= ray_bp_variants()) {
+    set_err("invalid ray-kernel variant");
+    return MRF_ERR_INVALID;
+  }
+  m->ray_variant = variant;
+  drop_graphs(m);
+  return MRF_OK;
+}
+
+mrf_status mrf_autotune(mrf_map* m, int reps, double* ms_out, int cap, int* chosen) {
+  if (guard(m) != MRF_OK) return MRF_ERR_INVALID;
+  if (reps < 1 || cap < 0 || (cap > 0 && !ms_out)) {
+    set_err("invalid autotune arguments");
+    return MRF_ERR_INVALID;
+  }
+  return wrap([&] {
+    ensure_built(m);
+    const int V = (int)m->views.size();
+    const int NV = ray_bp_variants();
+    BpArrays a = m->bp();
+    std::vector<double> ms(NV, 0.0);
+    if (m->n_inc > 0) {
+      // ln q of the current state for every pair; the ray pass only writes
+      // the per-iteration message scratch, so the map state is untouched
+      CK(launch_pair_prepare(a, 0, (uint32_t)m->n_pairs, 0, m->stream));
+      for (int k = 0; k < NV; ++k) {
+        for (int r = 0; r <= reps; ++r) {
+          CK(cudaMemsetAsync(m->counters.p, 0, (size_t)(V + 1) * 4, m->stream));
+          if (r == 1) CK(cudaEventRecord(m->ev0, m->stream));
+          for (int c = 0; c < V; ++c) {
+            const View& v = m->views[c];
+            CK(launch_ray_bp(a, m->ray_order.as<uint32_t>() + v.order_base, v.n_active,
+                             m->counters.as<uint32_t>() + c, 0, m->num_sms, k, m->stream));
+          }
+        }
+        CK(cudaEventRecord(m->ev1, m->stream));
+        sync(m);
+        float t = 0.0f;
+        CK(cudaEventElapsedTime(&t, m->ev0, m->ev1));
+        ms[k] = t / reps;
+      }
+    }
+    int best = 0;
+    for (int k = 1; k < NV; ++k)
+      if (ms[k] < ms[best]) best = k;
+    for (int k = 0; k < NV && k < cap; ++k) ms_out[k] = ms[k];
+    m->ray_variant = best;
+    drop_graphs(m);
+    if (chosen) *chosen = best;
   });
 }
 

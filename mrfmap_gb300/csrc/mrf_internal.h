@@ -92,11 +92,20 @@ cudaError_t launch_pairs_from_sorted(const uint32_t* sk, const uint32_t* sidx, c
                                      const uint32_t* scan, uint32_t n, uint32_t pair_base,
                                      uint32_t perm_base, uint32_t inc_base, uint32_t* pair_vox,
                                      uint32_t* seg, uint32_t* inc_pair, cudaStream_t s);
-// per pair: cumulative length, summed static messages, dynamic incidences
+// per pair: cumulative length, summed static messages, dynamic incidences,
+// potential mass
 cudaError_t launch_pair_stats(const uint32_t* seg, const uint32_t* sidx, uint32_t p0, uint32_t np,
                               uint32_t perm_base, uint32_t inc_base, const float* post_len,
-                              const uint8_t* cls, float* cum, float* stat, uint32_t* ndyn,
-                              cudaStream_t s);
+                              const uint8_t* cls, const float* mu, float* cum, float* stat,
+                              uint32_t* ndyn, float* hit, cudaStream_t s);
+// warm-start initial messages from a predicted log-odds field (voxel CSR)
+cudaError_t launch_warm_split(const uint32_t* vseg, const uint32_t* vpairs, const uint32_t* vvox,
+                              uint32_t nvox, const float* L_pred, float lp, const float* cum,
+                              const float* stat, const uint32_t* ndyn, float* m, cudaStream_t s);
+// warm-start features per voxel [nvox_slots][4] from the voxel CSR
+cudaError_t launch_voxel_features(const uint32_t* vseg, const uint32_t* vpairs, const uint32_t* vvox,
+                                  uint32_t nvox, const float* cum, const float* stat, const float* hit,
+                                  const float* belief, int64_t n_slots_vox, float* feat, cudaStream_t s);
 // dynamic incidences of a view in pair-grouped order (dperm) and the pairs
 // that own them (dpair, with their first position dseg)
 cudaError_t launch_dyn_flags(const uint32_t* sidx, uint32_t n, uint32_t inc_base, const uint8_t* cls,
@@ -151,11 +160,13 @@ struct TileCarry {
 uint32_t pair_update_tiles(uint32_t n);
 cudaError_t launch_pair_prepare(const BpArrays& a, uint32_t p0, uint32_t p1, int jacobi,
                                 cudaStream_t s);
-// resident blocks per SM of the persistent ray kernel (queried once)
-int ray_bp_resident_blocks();
+// ray-kernel variants (register budget x load policy; identical arithmetic)
+int ray_bp_variants();
+// resident blocks per SM of a variant of the persistent ray kernel (queried once)
+int ray_bp_resident_blocks(int variant);
 // rays order[0..n_rays) of the queue; counter: one zeroed u32 per launch
 cudaError_t launch_ray_bp(const BpArrays& a, const uint32_t* order, uint32_t n_rays,
-                          uint32_t* counter, int fix_reset, int num_sms, cudaStream_t s);
+                          uint32_t* counter, int fix_reset, int num_sms, int variant, cudaStream_t s);
 cudaError_t launch_ray_keys(const RayMeta* meta, uint32_t n, uint32_t* keys, uint32_t* vals,
                             cudaStream_t s);
 // dynamic positions k0..k1 hold the runs j0..j1 (dpair/dseg indices);
@@ -172,6 +183,9 @@ cudaError_t launch_tile_first(const uint32_t* seg, uint32_t p0, uint32_t p1, uin
 cudaError_t launch_voxel_apply(const uint32_t* vseg, const uint32_t* vpairs, const uint32_t* vvox,
                                uint32_t nvox, const float* pair_dm, float* L, float* belief,
                                cudaStream_t s);
+cudaError_t launch_voxel_rebuild(const uint32_t* vseg, const uint32_t* vpairs, const uint32_t* vvox,
+                                 uint32_t nvox, const float* m, const float* cum, float* L, float* belief,
+                                 cudaStream_t s);
 cudaError_t launch_remove_messages(const BpArrays& a, uint32_t p0, uint32_t p1, cudaStream_t s);
 cudaError_t launch_remap_scatter(const uint32_t* pair_vox, const float* pair_m, uint32_t n,
                                  float* dense, cudaStream_t s);

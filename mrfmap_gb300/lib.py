@@ -31,7 +31,11 @@ _STATUS = {0: "MRF_OK", 1: "MRF_ERR_INVALID", 2: "MRF_ERR_CUDA", 3: "MRF_ERR_OOM
 
 # every symbol declared in include/mrfmap_gb300.h
 EXPORTS = ["mrf_create", "mrf_destroy", "mrf_last_error", "mrf_add_view", "mrf_add_view_device",
-           "mrf_set_pose", "mrf_infer", "mrf_infer_converge", "mrf_reset_state", "mrf_likelihood_view", "mrf_likelihood",
+           "mrf_set_pose", "mrf_infer", "mrf_infer_converge", "mrf_warm_start", "mrf_warm_start_device",
+           "mrf_warm_features", "mrf_read_messages", "mrf_write_messages", "mrf_rebuild_logodds", "mrf_net_num_params", "mrf_net_workspace_bytes", "mrf_net_forward",
+           "mrf_net_gradients", "mrf_net_adam",
+           "mrf_ray_variants", "mrf_set_ray_variant",
+           "mrf_autotune", "mrf_reset_state", "mrf_likelihood_view", "mrf_likelihood",
            "mrf_likelihood_device", "mrf_likelihood_device_noalloc", "mrf_num_bricks", "mrf_read_bricks", "mrf_read_logodds",
            "mrf_num_nodes", "mrf_read_nodes", "mrf_load_map", "mrf_view_incidences",
            "mrf_device_beliefs",
@@ -91,6 +95,22 @@ def load(path: str | None = None):
         "mrf_set_pose": ([vp, C.c_int, fp], C.c_int),
         "mrf_infer": ([vp, ip, C.c_int, C.c_int, C.c_int], C.c_int),
         "mrf_infer_converge": ([vp, ip, C.c_int, C.c_int, C.c_float, C.c_int, C.c_int, ip, fp], C.c_int),
+        "mrf_warm_start": ([vp, fp, C.c_int], C.c_int),
+        "mrf_warm_start_device": ([vp, C.c_void_p, C.c_int], C.c_int),
+        "mrf_warm_features": ([vp, C.c_void_p], C.c_int),
+        "mrf_read_messages": ([vp, C.c_int, fp], C.c_int),
+        "mrf_write_messages": ([vp, C.c_int, fp], C.c_int),
+        "mrf_rebuild_logodds": ([vp], C.c_int),
+        "mrf_net_num_params": ([], C.c_int64),
+        "mrf_net_workspace_bytes": ([C.c_int64], C.c_int64),
+        "mrf_net_forward": ([C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+        "mrf_net_gradients": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_float,
+                               C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+        "mrf_net_adam": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_float, C.c_float,
+                          C.c_float, C.c_float, C.c_int, C.c_void_p], C.c_int),
+        "mrf_ray_variants": ([], C.c_int),
+        "mrf_set_ray_variant": ([vp, C.c_int], C.c_int),
+        "mrf_autotune": ([vp, C.c_int, C.POINTER(C.c_double), C.c_int, ip], C.c_int),
         "mrf_reset_state": ([vp], C.c_int),
         "mrf_likelihood_view": ([vp, C.c_int, fp, fp], C.c_int),
         "mrf_likelihood": ([vp, fp, fp, fp, fp], C.c_int),
@@ -217,6 +237,48 @@ class MRFMap:
             _check(self._L.mrf_infer_converge(self._h, a.ctypes.data_as(C.POINTER(C.c_int)), len(a),
                                               max_iters, tol, check_every, flags, C.byref(n), C.byref(d)))
         return n.value, d.value
+
+    def warm_start(self, logodds, sweeps: int = 3):
+        """Messages iterated at a predicted log-odds field [n_bricks, 512]
+        held fixed; continue with flags=INCREMENTAL."""
+        lo = np.ascontiguousarray(logodds, dtype=np.float32)
+        if lo.size != self.num_bricks * 512:
+            raise ValueError("logodds must hold n_bricks x 512 values")
+        _check(self._L.mrf_warm_start(self._h, _fp(lo), sweeps))
+
+    def warm_start_device(self, logodds_dev_ptr: int, sweeps: int = 3):
+        _check(self._L.mrf_warm_start_device(self._h, C.c_void_p(logodds_dev_ptr), sweeps))
+
+    def read_messages(self, view: int) -> np.ndarray:
+        out = np.zeros((self.num_bricks, 512), np.float32)
+        _check(self._L.mrf_read_messages(self._h, view, _fp(out)))
+        return out
+
+    def write_messages(self, view: int, dense):
+        d = np.ascontiguousarray(dense, dtype=np.float32)
+        if d.size != self.num_bricks * 512:
+            raise ValueError("messages must hold n_bricks x 512 values")
+        _check(self._L.mrf_write_messages(self._h, view, _fp(d)))
+
+    def rebuild_logodds(self):
+        _check(self._L.mrf_rebuild_logodds(self._h))
+
+    def warm_features(self, feat_dev_ptr: int):
+        """Writes [n_bricks, 512, 4] float features to a device buffer."""
+        _check(self._L.mrf_warm_features(self._h, C.c_void_p(feat_dev_ptr)))
+
+    def set_ray_variant(self, variant: int):
+        _check(self._L.mrf_set_ray_variant(self._h, variant))
+
+    def autotune(self, reps: int = 3):
+        """Times every ray-kernel variant on this map; keeps the fastest.
+        Returns (chosen variant, ms per pass of each variant)."""
+        nv = self._L.mrf_ray_variants()
+        ms = np.zeros(nv, np.float64)
+        ch = C.c_int()
+        _check(self._L.mrf_autotune(self._h, reps, ms.ctypes.data_as(C.POINTER(C.c_double)), nv,
+                                    C.byref(ch)))
+        return ch.value, ms
 
     def reset_state(self):
         _check(self._L.mrf_reset_state(self._h))

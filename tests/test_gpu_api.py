@@ -214,3 +214,49 @@ def test_runs_are_reproducible(native_lib, w):
         m.close()
     np.testing.assert_array_equal(res[0][0], res[1][0])
     np.testing.assert_array_equal(res[0][1], res[1][1])
+
+
+def test_infer_converge(native_lib, w):
+    """Convergence-checked inference stops once the largest belief change is
+    below the tolerance, and its state equals a fixed-count run of the same
+    number of iterations (the check reads, never writes, the state)."""
+    m = L.MRFMap(w.params, activation=L.ACT_FULL_RAY)
+    for P, D in zip(w.poses, w.depths):
+        m.add_view(P, D)
+    n, d = m.infer_converge(1e-4, max_iters=60)
+    assert 1 < n < 60 and 0.0 <= d < 1e-4
+    b1 = m.beliefs()
+    m.reset_state()
+    m.infer(iters=n)
+    np.testing.assert_array_equal(m.beliefs(), b1)
+    # a coarse check interval: stops at a multiple of it
+    m.reset_state()
+    n2, d2 = m.infer_converge(1e-4, max_iters=60, check_every=4)
+    assert n2 % 4 == 0 and d2 < 1e-4
+    with pytest.raises(L.MrfError):
+        m.infer_converge(0.0)
+
+
+def test_ray_variants_identical_and_autotune(native_lib, w):
+    """Every ray-kernel variant computes the same bits; the autotuner picks
+    one of them and leaves the map state untouched."""
+    out = []
+    for k in range(L.load().mrf_ray_variants()):
+        m = L.MRFMap(w.params, activation=L.ACT_FULL_RAY)
+        for P, D in zip(w.poses, w.depths):
+            m.add_view(P, D)
+        m.set_ray_variant(k)
+        m.infer(iters=3)
+        out.append(m.beliefs())
+        if k == 0:
+            before = (m.beliefs(), m.logodds())
+            best, ms = m.autotune(reps=2)
+            assert 0 <= best < len(ms) and (ms > 0).all()
+            np.testing.assert_array_equal(m.beliefs(), before[0])
+            np.testing.assert_array_equal(m.logodds(), before[1])
+        m.close()
+    for b in out[1:]:
+        np.testing.assert_array_equal(b, out[0])
+    m = L.MRFMap(w.params)
+    with pytest.raises(L.MrfError):
+        m.set_ray_variant(99)
