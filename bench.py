@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-sample-views", type=int, default=2)
+    ap.add_argument("--warm-scenes", type=int, default=4,
+                    help="held-out 10x320x240 2 cm scenes for the warm-start comparison (0: skip)")
     return ap.parse_args()
 
 
@@ -335,6 +337,34 @@ def run_ours(args):
     except Exception as e:  # reported, not fatal
         like = {"error": str(e)}
 
+    # time to a converged map: learned warm start vs plain BP (held-out
+    # seeded scenes of the training distribution, weights trained by
+    # python -m mrfmap_gb300.warmstart)
+    warm = None
+    if rank == 0 and args.warm_scenes > 0:
+        try:
+            from mrfmap_gb300 import warmstart as WS
+            if not os.path.exists(WS.DEFAULT_WEIGHTS):
+                raise FileNotFoundError("no trained warm-start weights")
+            net = WS.WarmNet.load_file(WS.DEFAULT_WEIGHTS)
+            rows = WS.evaluate(net, WS.scenes(range(9000, 9000 + args.warm_scenes)))
+            both = [r for r in rows if r["plain_converged"] and r["learned_converged"]]
+            mean = lambda k, rs: float(np.mean([r[k] for r in rs])) if rs else None
+            warm = {"workload": "held-out full_room 10x320x240 2 cm, seeds 9000+",
+                    "scenes": len(rows), "tol": 1e-3, "max_iters": 300,
+                    "scenes_converged_plain": sum(r["plain_converged"] for r in rows),
+                    "scenes_converged_learned": sum(r["learned_converged"] for r in rows),
+                    "plain_ms": mean("plain_ms", both), "plain_iters": mean("plain_iters", both),
+                    "learned_ms": mean("learned_ms", both), "learned_iters": mean("learned_iters", both),
+                    "prior_init_ms": mean("prior_ms", both), "prior_init_iters": mean("prior_iters", both),
+                    "speedup_learned_vs_plain": (mean("plain_ms", both) / mean("learned_ms", both)) if both else None,
+                    "learned_max_belief_err_vs_plain": max(r["learned_max_err"] for r in both) if both else None,
+                    "learned_min_class_agreement": min(r["learned_agree"] for r in both) if both else None,
+                    "per_scene": [{k: (round(v, 4) if isinstance(v, float) else v) for k, v in r.items()}
+                                  for r in rows]}
+        except Exception as e:  # reported, not fatal
+            warm = {"error": str(e)}
+
     # belief error against the FP64 oracle on the small-room workload
     parity = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -396,7 +426,7 @@ def run_ours(args):
                     "d2h_bytes_per_step": d2h, "s_per_step": e2e_t},
             "cpu_baseline": cpu,
             "likelihood": like,
-            "parity_vs_fp64": parity,
+            "parity_vs_fp64": parity, "warm_start": warm,
         }
         print(json.dumps(line))
     m.close()

@@ -113,28 +113,36 @@ __device__ __forceinline__ T ld_stream(const T* p) {
   return __ldg(p);
 }
 
-// loads a lane's kE incidences at i0 (those >= n read as zero; potentials
-// below kmu, a multiple of 4, are known zeros and not loaded), gathers ln q,
-// forms prefix exponents from carryA; returns the chunk total of l ln q
+// a lane's kE pair ids at i0 (those >= n read as zero)
 template <int kPol>
-__device__ __forceinline__ float load_slice(Slice& s, uint32_t off, int i0, int n, int kmu,
-                                            float carryA, int lane,
-                                            const uint32_t* __restrict__ inc_pair,
-                                            const float* __restrict__ inc_len,
-                                            const float* __restrict__ inc_mu,
-                                            const float* __restrict__ lnq) {
-  uint32_t pid[kE];
+__device__ __forceinline__ void load_pids(uint32_t (&pid)[kE], uint32_t off, int i0, int n,
+                                          const uint32_t* __restrict__ inc_pair) {
 #pragma unroll
   for (int v = 0; v < kE / 4; ++v) {
     const int i = i0 + 4 * v;
     uint4 p = make_uint4(0u, 0u, 0u, 0u);
+    if (i < n) p = ld_stream<kPol>(reinterpret_cast<const uint4*>(inc_pair + off + i));
+    pid[4 * v + 0] = p.x; pid[4 * v + 1] = p.y; pid[4 * v + 2] = p.z; pid[4 * v + 3] = p.w;
+  }
+}
+
+// with the lane's pair ids loaded: loads lengths (and potentials at and
+// after kmu, a multiple of 4; below it they are known zeros), gathers ln q,
+// forms prefix exponents from carryA; returns the chunk total of l ln q
+template <int kPol>
+__device__ __forceinline__ float slice_from_pids(Slice& s, const uint32_t (&pid)[kE], uint32_t off, int i0,
+                                                 int n, int kmu, float carryA, int lane,
+                                                 const float* __restrict__ inc_len,
+                                                 const float* __restrict__ inc_mu,
+                                                 const float* __restrict__ lnq) {
+#pragma unroll
+  for (int v = 0; v < kE / 4; ++v) {
+    const int i = i0 + 4 * v;
     float4 l = make_float4(0.f, 0.f, 0.f, 0.f), m = make_float4(0.f, 0.f, 0.f, 0.f);
     if (i < n) {
-      p = ld_stream<kPol>(reinterpret_cast<const uint4*>(inc_pair + off + i));
       l = ld_stream<kPol>(reinterpret_cast<const float4*>(inc_len + off + i));
       if (i >= kmu) m = ld_stream<kPol>(reinterpret_cast<const float4*>(inc_mu + off + i));
     }
-    pid[4 * v + 0] = p.x; pid[4 * v + 1] = p.y; pid[4 * v + 2] = p.z; pid[4 * v + 3] = p.w;
     s.len[4 * v + 0] = l.x; s.len[4 * v + 1] = l.y; s.len[4 * v + 2] = l.z; s.len[4 * v + 3] = l.w;
     s.mu[4 * v + 0] = m.x; s.mu[4 * v + 1] = m.y; s.mu[4 * v + 2] = m.z; s.mu[4 * v + 3] = m.w;
   }
@@ -158,6 +166,18 @@ __device__ __forceinline__ float load_slice(Slice& s, uint32_t off, int i0, int 
 #pragma unroll
   for (int j = 0; j < kE; ++j) s.A[j] += b;
   return __shfl_sync(kFull, ex + run, 31);
+}
+
+template <int kPol>
+__device__ __forceinline__ float load_slice(Slice& s, uint32_t off, int i0, int n, int kmu,
+                                            float carryA, int lane,
+                                            const uint32_t* __restrict__ inc_pair,
+                                            const float* __restrict__ inc_len,
+                                            const float* __restrict__ inc_mu,
+                                            const float* __restrict__ lnq) {
+  uint32_t pid[kE];
+  load_pids<kPol>(pid, off, i0, n, inc_pair);
+  return slice_from_pids<kPol>(s, pid, off, i0, n, kmu, carryA, lane, inc_len, inc_mu, lnq);
 }
 
 // A at chunk-relative index idx (0 <= idx < kChunk), broadcast to the warp
@@ -211,7 +231,7 @@ __device__ __forceinline__ Acc emit_slice(const float (&vmu)[kE], const float (&
   return carryF + (Acc)__shfl_sync(kFull, ex + run, 31);
 }
 
-template <typename Acc, int kPol>
+template <typename Acc, int kPol, bool kPf>
 __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, const uint32_t* __restrict__ inc_pair,
                                             const float* __restrict__ inc_len,
                                             const float* __restrict__ inc_mu,
@@ -227,9 +247,21 @@ __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, const uint32_t* _
   float carryA = 0.0f, Ar0 = 0.0f, Arinf = 0.0f, Ak = 0.0f;
   Acc T = 0;
   Slice s;
+  // kPf: the next chunk's pair ids are requested before this chunk's ln q
+  // gathers, so a chunk waits on one memory round trip instead of two
+  uint32_t pid_next[kE];
+  if (kPf) load_pids<kPol>(pid_next, off, kE * lane, n_pre, inc_pair);
   for (int base = 0; base < n_pre; base += kChunk) {
     const int i0 = base + kE * lane;
-    float tot = load_slice<kPol>(s, off, i0, n_pre, k4, carryA, lane, inc_pair, inc_len, inc_mu, lnq);
+    uint32_t pid[kE];
+    if (kPf) {
+#pragma unroll
+      for (int j = 0; j < kE; ++j) pid[j] = pid_next[j];
+      if (base + kChunk < n_pre) load_pids<kPol>(pid_next, off, i0 + kChunk, n_pre, inc_pair);
+    } else {
+      load_pids<kPol>(pid, off, i0, n_pre, inc_pair);
+    }
+    float tot = slice_from_pids<kPol>(s, pid, off, i0, n_pre, k4, carryA, lane, inc_len, inc_mu, lnq);
     if (r0 > 0 && r0 - 1 >= base && r0 - 1 < base + kChunk) Ar0 = slice_value(s, r0 - 1 - base);
     if (rinf > 0 && rinf - 1 >= base && rinf - 1 < base + kChunk) Arinf = slice_value(s, rinf - 1 - base);
     if (k4 > 0 && k4 - 1 >= base && k4 - 1 < base + kChunk) Ak = slice_value(s, k4 - 1 - base);
@@ -274,7 +306,7 @@ __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, const uint32_t* _
 // ray does not change its result.  Variants differ only in register budget
 // (kMinBlocks resident blocks per SM) and load policy: their arithmetic is
 // identical, so the autotuner's choice never changes a result.
-template <int kMinBlocks, int kPol>
+template <int kMinBlocks, int kPol, bool kPf>
 __global__ void __launch_bounds__(kRayWarps * 32, kMinBlocks) k_ray_bp(const RayMeta* __restrict__ meta,
                                                            const uint32_t* __restrict__ order,
                                                            uint32_t n_rays,
@@ -293,9 +325,9 @@ __global__ void __launch_bounds__(kRayWarps * 32, kMinBlocks) k_ray_bp(const Ray
     if (idx >= n_rays) break;
     RayMeta me = meta[order[idx]];
     if (me.n_pre <= kLongRay)
-      ray_bp_warp<float, kPol>(me, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
+      ray_bp_warp<float, kPol, kPf>(me, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
     else
-      ray_bp_warp<double, kPol>(me, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
+      ray_bp_warp<double, kPol, kPf>(me, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
   }
 }
 
@@ -666,18 +698,18 @@ cudaError_t launch_pair_prepare(const BpArrays& a, uint32_t p0, uint32_t p1, int
 }
 
 
-// ray-kernel variants: (resident-block target, load policy)
-#define MRF_RAY_VARIANTS(X) X(0, 0, 0) X(1, 0, 1) X(2, 10, 0) X(3, 10, 1) X(4, 12, 1)
-constexpr int kRayVariants = 5;
+// ray-kernel variants: (id, resident-block target, load policy, pair-id prefetch)
+#define MRF_RAY_VARIANTS(X) X(0, 0, 0, false) X(1, 0, 1, false) X(2, 0, 0, true) X(3, 0, 1, true)
+constexpr int kRayVariants = 4;
 
 int ray_bp_variants() { return kRayVariants; }
 
 namespace {
-template <int kMinBlocks, int kPol>
+template <int kMinBlocks, int kPol, bool kPf>
 int resident_of() {
   int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ray_bp<kMinBlocks, kPol>, kRayWarps * 32,
-                                                    0) != cudaSuccess ||
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ray_bp<kMinBlocks, kPol, kPf>,
+                                                    kRayWarps * 32, 0) != cudaSuccess ||
       per_sm < 1)
     per_sm = 1;
   return per_sm;
@@ -689,9 +721,9 @@ int ray_bp_resident_blocks(int variant) {
   if (variant < 0 || variant >= kRayVariants) return 1;
   if (!resident[variant]) {
     switch (variant) {
-#define X(id, mb, pol) \
-  case id:             \
-    resident[variant] = resident_of<mb, pol>(); \
+#define X(id, mb, pol, pf) \
+  case id:                 \
+    resident[variant] = resident_of<mb, pol, pf>(); \
     break;
       MRF_RAY_VARIANTS(X)
 #undef X
@@ -708,11 +740,11 @@ cudaError_t launch_ray_bp(const BpArrays& a, const uint32_t* order, uint32_t n_r
                                 (n_rays + kRayWarps - 1) / kRayWarps);
   const unsigned grid = (unsigned)std::max<int64_t>(b, 1);
   switch (variant) {
-#define X(id, mb, pol)                                                                           \
-  case id:                                                                                       \
-    k_ray_bp<mb, pol><<<grid, kRayWarps * 32, 0, s>>>(a.meta, order, n_rays, counter, a.inc_pair, \
-                                                      a.inc_len, a.inc_mu, a.pair_lnq, a.inc_pl,  \
-                                                      fix_reset);                                 \
+#define X(id, mb, pol, pf)                                                                        \
+  case id:                                                                                        \
+    k_ray_bp<mb, pol, pf><<<grid, kRayWarps * 32, 0, s>>>(a.meta, order, n_rays, counter, a.inc_pair, \
+                                                          a.inc_len, a.inc_mu, a.pair_lnq,          \
+                                                          a.inc_pl, fix_reset);                    \
     break;
     MRF_RAY_VARIANTS(X)
 #undef X

@@ -931,6 +931,7 @@ void mrf_destroy(mrf_map* m) {
   cudaSetDevice(m->device);
   if (m->stream) cudaStreamSynchronize(m->stream);
   destroy_bufs(m);
+  if (m->stream) cudaStreamSynchronize(m->stream);
   for (cudaEvent_t e : m->prof_ev) cudaEventDestroy(e);
   for (auto& g : m->graphs)
     if (g.exec) cudaGraphExecDestroy(g.exec);

@@ -151,7 +151,7 @@ def training_pairs(m: L.MRFMap, tol: float = 1e-4, max_iters: int = 200):
     return feat, lo, touched
 
 
-def warm_start(m: L.MRFMap, net: WarmNet, sweeps: int = 1):
+def warm_start(m: L.MRFMap, net: WarmNet, sweeps: int = 0):
     """Predict the map's log-odds and start BP from messages at that field."""
     feat = map_features(m)
     pred = net.predict(feat)
@@ -162,3 +162,135 @@ def warm_start(m: L.MRFMap, net: WarmNet, sweeps: int = 1):
 
 
 DEFAULT_WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "warmnet_params.bin")
+
+
+def _scene(seed: int, frames: int, rows: int, cols: int, res: float):
+    from . import synthetic
+    return synthetic.full_room(seed, n_frames=frames, rows=rows, cols=cols, res=res)
+
+
+def scenes(seeds, frames=10, rows=240, cols=320, res=0.02, workers: int = 0):
+    """Seeded training / held-out scenes (the C4 shape: 10 frames 320x240,
+    2 cm); generated on host cores in spawned processes."""
+    import multiprocessing as mp
+    args = [(s, frames, rows, cols, res) for s in seeds]
+    workers = workers or min(len(args), os.cpu_count() or 1)
+    if workers <= 1:
+        return [_scene(*a) for a in args]
+    with mp.get_context("spawn").Pool(workers) as pool:
+        return pool.starmap(_scene, args)
+
+
+def build_dataset(workloads, activation=L.ACT_FULL_RAY, bricks_per_scene: int = 2048, seed: int = 0,
+                  tol: float = 1e-4, max_iters: int = 200):
+    """Training tensors from plain BP run to convergence on each workload:
+    every brick holding a dynamic (near-surface) voxel plus a random share
+    of the others, up to bricks_per_scene per scene."""
+    torch = _torch()
+    rng = np.random.default_rng(seed)
+    F, T, Wt = [], [], []
+    for w in workloads:
+        m = L.MRFMap(w.params, activation=activation)
+        for P, D in zip(w.poses, w.depths):
+            m.add_view(P, D)
+        feat, lo, wt = training_pairs(m, tol=tol, max_iters=max_iters)
+        near = (feat[:, :, 2] > 0).any(dim=1).cpu().numpy()
+        seen = (wt > 0).any(dim=1).cpu().numpy()
+        idx = np.flatnonzero(near & seen)
+        rest = np.flatnonzero(~near & seen)
+        if len(idx) > bricks_per_scene:
+            idx = rng.choice(idx, bricks_per_scene, replace=False)
+        extra = min(len(rest), max(bricks_per_scene - len(idx), 0), bricks_per_scene // 4)
+        if extra:
+            idx = np.concatenate([idx, rng.choice(rest, extra, replace=False)])
+        sel = torch.from_numpy(np.sort(idx)).cuda()
+        F.append(feat[sel])
+        T.append(lo[sel])
+        Wt.append(wt[sel])
+        m.close()
+    return torch.cat(F), torch.cat(T), torch.cat(Wt)
+
+
+def evaluate(net, workloads, tol: float = 1e-3, max_iters: int = 300, sweeps: int = 0,
+             activation=L.ACT_FULL_RAY):
+    """Time to a converged map (largest belief change below tol): plain BP
+    from the prior against BP warm-started by the network and, as the
+    method without the network, by a prediction of the prior everywhere.
+    Times are device times of the whole procedure (features, network,
+    initial messages and BP iterations) with the incidence lists built
+    beforehand; each warm-started map is checked against the plain one."""
+    torch = _torch()
+    rows = []
+    for w in workloads:
+        m = L.MRFMap(w.params, activation=activation)
+        for P, D in zip(w.poses, w.depths):
+            m.add_view(P, D)
+        m.infer(iters=1)  # incidence lists
+        m.reset_state()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        torch.cuda.synchronize()
+        ev[0].record()
+        n_plain, _ = m.infer_converge(tol, max_iters=max_iters)
+        ev[1].record()
+        torch.cuda.synchronize()
+        t_plain = ev[0].elapsed_time(ev[1])
+        Bp = m.beliefs()
+        rec = {"workload": w.name, "seed": w.seed, "plain_iters": n_plain, "plain_ms": t_plain,
+               "plain_converged": n_plain < max_iters}
+        lp = float(np.log(w.params.prior / (1 - w.params.prior)))
+        for label in ("learned", "prior"):
+            m.reset_state()
+            torch.cuda.synchronize()
+            ev[0].record()
+            if label == "learned":
+                warm_start(m, net, sweeps)
+            else:
+                m.warm_start(np.full((m.num_bricks, 512), lp, np.float32), sweeps)
+            n, _ = m.infer_converge(tol, max_iters=max_iters, flags=L.INCREMENTAL)
+            ev[1].record()
+            torch.cuda.synchronize()
+            Bw = m.beliefs()
+            touched = (Bp > 0) | (Bw > 0)
+            rec[label + "_iters"] = n
+            rec[label + "_converged"] = n < max_iters
+            rec[label + "_ms"] = ev[0].elapsed_time(ev[1])
+            rec[label + "_max_err"] = float(np.abs(Bw - Bp).max())
+            rec[label + "_agree"] = float(((Bw > 0.5) == (Bp > 0.5))[touched].mean()) if touched.any() else 1.0
+        rows.append(rec)
+        m.close()
+    return rows
+
+
+def main(argv=None):
+    """Train the warm-start network on plain-BP solutions of seeded scenes
+    and write its parameters (fp32, mrf_net_num_params values)."""
+    import argparse
+    import json
+    import time
+    ap = argparse.ArgumentParser(description=main.__doc__)
+    ap.add_argument("--scenes", type=int, default=200)
+    ap.add_argument("--first-seed", type=int, default=1000)
+    ap.add_argument("--epochs", type=int, default=12)
+    ap.add_argument("--batch", type=int, default=512)
+    ap.add_argument("--lr", type=float, default=1e-3)
+    ap.add_argument("--out", default=DEFAULT_WEIGHTS)
+    a = ap.parse_args(argv)
+    t0 = time.time()
+    ws = scenes(range(a.first_seed, a.first_seed + a.scenes))
+    t1 = time.time()
+    print(f"{len(ws)} scenes in {t1 - t0:.1f} s", flush=True)
+    feats, targets, weights = build_dataset(ws)
+    t2 = time.time()
+    print(f"{feats.shape[0]} training bricks in {t2 - t1:.1f} s", flush=True)
+    net = WarmNet(seed=0)
+    hist = net.train(feats, targets, weights, epochs=a.epochs, batch=a.batch, lr=a.lr)
+    _torch().cuda.synchronize()
+    t3 = time.time()
+    net.save(a.out)
+    print(json.dumps({"scenes": a.scenes, "bricks": int(feats.shape[0]), "epochs": a.epochs,
+                      "loss_per_epoch": [round(h, 5) for h in hist], "scene_s": round(t1 - t0, 1),
+                      "dataset_s": round(t2 - t1, 1), "train_s": round(t3 - t2, 1), "out": a.out}))
+
+
+if __name__ == "__main__":
+    main()

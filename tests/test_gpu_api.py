@@ -260,3 +260,32 @@ def test_ray_variants_identical_and_autotune(native_lib, w):
     m = L.MRFMap(w.params)
     with pytest.raises(L.MrfError):
         m.set_ray_variant(99)
+
+
+def test_message_checkpoint_resume(native_lib, w):
+    """The BP state is the per-camera messages: written back into a fresh map
+    (and the total log-odds rebuilt from them) the run resumes where it
+    stopped.  The rebuilt log-odds are one sum instead of a running sum, so
+    the resumed run agrees to rounding."""
+    ref = L.MRFMap(w.params, activation=L.ACT_FULL_RAY)
+    for P, D in zip(w.poses, w.depths):
+        ref.add_view(P, D)
+    ref.infer(iters=4)
+    msgs = [ref.read_messages(v) for v in range(len(w.poses))]
+    L4 = ref.logodds()
+    ref.infer(iters=4, flags=L.INCREMENTAL)
+    b8 = ref.beliefs()
+    m = L.MRFMap(w.params, activation=L.ACT_FULL_RAY)
+    for P, D in zip(w.poses, w.depths):
+        m.add_view(P, D)
+    m.infer(iters=1)
+    for v, d in enumerate(msgs):
+        m.write_messages(v, d)
+    m.rebuild_logodds()
+    np.testing.assert_allclose(m.logodds(), L4, atol=1e-4)
+    for v, d in enumerate(msgs):
+        np.testing.assert_array_equal(m.read_messages(v), d)
+    m.infer(iters=4, flags=L.INCREMENTAL)
+    assert np.abs(m.beliefs() - b8).max() <= 1e-4
+    with pytest.raises(L.MrfError):
+        m.read_messages(len(w.poses))
