@@ -163,7 +163,7 @@ __global__ void __launch_bounds__(kThreads)
     k_trace(Geom g, Pose P, const float* __restrict__ depth, uint32_t* __restrict__ counts,
             const uint32_t* __restrict__ pix_off, uint32_t inc_base, RayMeta* __restrict__ meta,
             uint32_t* __restrict__ inc_vox, float* __restrict__ inc_len,
-            float* __restrict__ inc_mu, float* __restrict__ post_len, uint8_t* __restrict__ inc_cls,
+            float* __restrict__ inc_mu, float2* __restrict__ inc_rec,
             int* __restrict__ err) {
   int pix = blockIdx.x * blockDim.x + threadIdx.x;
   if (pix >= g.rows * g.cols) return;
@@ -247,12 +247,14 @@ __global__ void __launch_bounds__(kThreads)
       inc_len[base + k] = 0.0f;
       inc_mu[base + k] = 0.0f;
     }
-    // lengths that count towards the cumulative length (Post range only) and
-    // the class of each incidence's message
+    // per-incidence build record: the length that counts towards the
+    // cumulative length (Post range only) and, for a dynamic incidence,
+    // -(mu * l) (the sign bit marks the class; -0 when mu is 0)
     const int kdyn = (kmu >= 0 && kmu < n_post) ? kmu : n_post;
     for (int k = 0; k < padded; ++k) {
-      post_len[base + k] = k < n_post ? inc_len[base + k] : 0.0f;
-      inc_cls[base + k] = k < kdyn ? kIncStatic : (k < n_post ? kIncDyn : kIncNone);
+      const float pl = k < n_post ? inc_len[base + k] : 0.0f;
+      const bool dyn = k >= kdyn && k < n_post;
+      inc_rec[base + k] = make_float2(pl, dyn ? copysignf(inc_mu[base + k] * pl, -1.0f) : 0.0f);
     }
     RayMeta m;
     m.off = inc_base + base;
@@ -290,16 +292,21 @@ __global__ void k_pairs_from_sorted(const uint32_t* __restrict__ sk, const uint3
   inc_pair[inc_base + sidx[k]] = p;
 }
 
+// build records in pair-grouped (sorted) order: one gather per position
+__global__ void k_gather_rec(const uint32_t* __restrict__ sidx, uint32_t n, uint32_t inc_base,
+                             const float2* __restrict__ rec, float2* __restrict__ out) {
+  uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) out[k] = rec[inc_base + sidx[k]];
+}
+
 // Per pair, over its incidences in increasing incidence order (the order
 // the reference's cumulative-length pass visits a voxel, pixel-major):
 // cumulative length (fp32), the sum of its static messages F_EPS * l (fp32,
 // each product rounded as the ray kernel would round it), the number of
 // dynamic incidences and the potential mass sum mu * l (a warm-start
-// feature).
-__global__ void k_pair_stats(const uint32_t* __restrict__ seg, const uint32_t* __restrict__ sidx,
-                             uint32_t p0, uint32_t np, uint32_t perm_base, uint32_t inc_base,
-                             const float* __restrict__ post_len, const uint8_t* __restrict__ cls,
-                             const float* __restrict__ mu, float* __restrict__ cum,
+// feature).  Reads the pair's contiguous run of sorted records.
+__global__ void k_pair_stats(const uint32_t* __restrict__ seg, uint32_t p0, uint32_t np, uint32_t perm_base,
+                             const float2* __restrict__ srec, float* __restrict__ cum,
                              float* __restrict__ stat, uint32_t* __restrict__ ndyn,
                              float* __restrict__ hit) {
   uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
@@ -308,13 +315,14 @@ __global__ void k_pair_stats(const uint32_t* __restrict__ seg, const uint32_t* _
   float c = 0.0f, st = 0.0f, h = 0.0f;
   uint32_t nd = 0;
   for (uint32_t k = seg[p]; k < seg[p + 1]; ++k) {
-    uint32_t i = inc_base + sidx[k - perm_base];
-    float l = post_len[i];
-    c += l;
-    uint8_t t = cls[i];
-    if (t == kIncStatic) st += __fmul_rn(kFEps, l);
-    if (t == kIncDyn) h += mu[i] * l;
-    nd += t == kIncDyn;
+    const float2 r = srec[k - perm_base];
+    c += r.x;
+    if (signbit(r.y)) {
+      h -= r.y;
+      ++nd;
+    } else {
+      st += __fmul_rn(kFEps, r.x);
+    }
   }
   cum[p] = c;
   stat[p] = st;
@@ -322,10 +330,9 @@ __global__ void k_pair_stats(const uint32_t* __restrict__ seg, const uint32_t* _
   hit[p] = h;
 }
 
-__global__ void k_dyn_flags(const uint32_t* __restrict__ sidx, uint32_t n, uint32_t inc_base,
-                            const uint8_t* __restrict__ cls, uint32_t* __restrict__ flag) {
+__global__ void k_dyn_flags(const float2* __restrict__ srec, uint32_t n, uint32_t* __restrict__ flag) {
   uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k < n) flag[k] = cls[inc_base + sidx[k]] == kIncDyn ? 1u : 0u;
+  if (k < n) flag[k] = signbit(srec[k].y) ? 1u : 0u;
 }
 
 __global__ void k_dyn_scatter(const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ flag,
@@ -408,16 +415,16 @@ cudaError_t launch_set_points(const Geom& g, const float* pts, const float* occ,
 cudaError_t launch_trace_count(const Geom& g, const Pose& P, const float* depth, uint32_t* counts,
                                int* err, cudaStream_t s) {
   k_trace<false><<<grid_for((int64_t)g.rows * g.cols), kThreads, 0, s>>>(
-      g, P, depth, counts, nullptr, 0, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, err);
+      g, P, depth, counts, nullptr, 0, nullptr, nullptr, nullptr, nullptr, nullptr, err);
   return cudaGetLastError();
 }
 
 cudaError_t launch_trace_emit(const Geom& g, const Pose& P, const float* depth,
                               const uint32_t* pix_off, uint32_t inc_base, RayMeta* meta,
-                              uint32_t* inc_vox, float* inc_len, float* inc_mu, float* post_len,
-                              uint8_t* inc_cls, int* err, cudaStream_t s) {
+                              uint32_t* inc_vox, float* inc_len, float* inc_mu, float2* inc_rec,
+                              int* err, cudaStream_t s) {
   k_trace<true><<<grid_for((int64_t)g.rows * g.cols), kThreads, 0, s>>>(
-      g, P, depth, nullptr, pix_off, inc_base, meta, inc_vox, inc_len, inc_mu, post_len, inc_cls, err);
+      g, P, depth, nullptr, pix_off, inc_base, meta, inc_vox, inc_len, inc_mu, inc_rec, err);
   return cudaGetLastError();
 }
 
@@ -437,20 +444,24 @@ cudaError_t launch_pairs_from_sorted(const uint32_t* sk, const uint32_t* sidx, c
   return cudaGetLastError();
 }
 
-cudaError_t launch_pair_stats(const uint32_t* seg, const uint32_t* sidx, uint32_t p0, uint32_t np,
-                              uint32_t perm_base, uint32_t inc_base, const float* post_len,
-                              const uint8_t* cls, const float* mu, float* cum, float* stat,
-                              uint32_t* ndyn, float* hit, cudaStream_t s) {
-  if (!np) return cudaSuccess;
-  k_pair_stats<<<grid_for(np), kThreads, 0, s>>>(seg, sidx, p0, np, perm_base, inc_base, post_len, cls,
-                                                 mu, cum, stat, ndyn, hit);
+cudaError_t launch_gather_rec(const uint32_t* sidx, uint32_t n, uint32_t inc_base, const float2* rec,
+                              float2* out, cudaStream_t s) {
+  if (!n) return cudaSuccess;
+  k_gather_rec<<<grid_for(n), kThreads, 0, s>>>(sidx, n, inc_base, rec, out);
   return cudaGetLastError();
 }
 
-cudaError_t launch_dyn_flags(const uint32_t* sidx, uint32_t n, uint32_t inc_base, const uint8_t* cls,
-                             uint32_t* flag, cudaStream_t s) {
+cudaError_t launch_pair_stats(const uint32_t* seg, uint32_t p0, uint32_t np, uint32_t perm_base,
+                              const float2* srec, float* cum, float* stat, uint32_t* ndyn, float* hit,
+                              cudaStream_t s) {
+  if (!np) return cudaSuccess;
+  k_pair_stats<<<grid_for(np), kThreads, 0, s>>>(seg, p0, np, perm_base, srec, cum, stat, ndyn, hit);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_dyn_flags(const float2* srec, uint32_t n, uint32_t* flag, cudaStream_t s) {
   if (!n) return cudaSuccess;
-  k_dyn_flags<<<grid_for(n), kThreads, 0, s>>>(sidx, n, inc_base, cls, flag);
+  k_dyn_flags<<<grid_for(n), kThreads, 0, s>>>(srec, n, flag);
   return cudaGetLastError();
 }
 

@@ -123,7 +123,7 @@ struct mrf_map {
   uint32_t n_vvox = 0;
   int jacobi_version = -1;
   // scratch
-  DBuf s_postlen, s_cls, s_pf, s_ps, s_flags, s_ind, s_scan, s_tmp, s_counts, s_offs, s_vox, s_k0, s_k1, s_v0, s_v1,
+  DBuf s_rec, s_recs, s_pf, s_ps, s_flags, s_ind, s_scan, s_tmp, s_counts, s_offs, s_vox, s_k0, s_k1, s_v0, s_v1,
       s_seg, s_dense, s_err, s_depth_in, s_depth, s_img, s_part, s_sum, s_prev, s_delta;
   mrf_stats stats{};
   // MRF_PROFILE event pool
@@ -275,8 +275,7 @@ void rebuild(mrf_map* m) {
   m->dperm.reserve(ib, false, m->stream);
   m->inc_pl.reserve(ib, false, m->stream);
   m->s_vox.reserve(ib, false, m->stream);
-  m->s_postlen.reserve(ib, false, m->stream);
-  m->s_cls.reserve(ib / 4, false, m->stream);
+  m->s_rec.reserve(ib * 2, false, m->stream);
   // 3. emit
   for (int c = 0; c < V; ++c) {
     View& v = m->views[c];
@@ -284,8 +283,8 @@ void rebuild(mrf_map* m) {
     v.n_inc = bounds[c + 1] - bounds[c];
     CK(launch_trace_emit(m->g, v.pose, v.depth.as<float>(), m->s_offs.as<uint32_t>() + c * HW, 0,
                          m->meta.as<RayMeta>() + c * HW, m->s_vox.as<uint32_t>(),
-                         m->inc_len.as<float>(), m->inc_mu.as<float>(), m->s_postlen.as<float>(),
-                         m->s_cls.as<uint8_t>(), m->s_err.as<int>(), m->stream));
+                         m->inc_len.as<float>(), m->inc_mu.as<float>(), m->s_rec.as<float2>(),
+                         m->s_err.as<int>(), m->stream));
   }
   // per-view counters from the ray records
   std::vector<RayMeta> hm((size_t)npix);
@@ -355,14 +354,15 @@ void rebuild(mrf_map* m) {
                                 m->pair_vox.as<uint32_t>(), m->pair_seg.as<uint32_t>(),
                                 m->inc_pair.as<uint32_t>(), m->stream));
     CK(launch_fill_u32(m->pair_seg.as<uint32_t>() + v.pair_base + np, 1, v.perm_base + nr, m->stream));
-    CK(launch_pair_stats(m->pair_seg.as<uint32_t>(), m->s_v1.as<uint32_t>(), v.pair_base, np,
-                         v.perm_base, v.inc_base, m->s_postlen.as<float>(), m->s_cls.as<uint8_t>(),
-                         m->inc_mu.as<float>(), m->pair_cum.as<float>(), m->pair_stat.as<float>(),
-                         m->pair_ndyn.as<uint32_t>(), m->pair_hit.as<float>(), m->stream));
+    m->s_recs.reserve((size_t)nr * 8, false, m->stream);
+    CK(launch_gather_rec(m->s_v1.as<uint32_t>(), nr, v.inc_base, m->s_rec.as<float2>(),
+                         m->s_recs.as<float2>(), m->stream));
+    CK(launch_pair_stats(m->pair_seg.as<uint32_t>(), v.pair_base, np, v.perm_base, m->s_recs.as<float2>(),
+                         m->pair_cum.as<float>(), m->pair_stat.as<float>(), m->pair_ndyn.as<uint32_t>(),
+                         m->pair_hit.as<float>(), m->stream));
     // dynamic incidences in pair-grouped order (a stable compaction of the
     // sorted positions) and the run of each pair that has any
-    CK(launch_dyn_flags(m->s_v1.as<uint32_t>(), nr, v.inc_base, m->s_cls.as<uint8_t>(),
-                        m->s_k0.as<uint32_t>(), m->stream));
+    CK(launch_dyn_flags(m->s_recs.as<float2>(), nr, m->s_k0.as<uint32_t>(), m->stream));
     CK(cudaMemsetAsync(m->s_k0.as<uint32_t>() + nr, 0, 4, m->stream));
     CK(exclusive_scan_u32(m->s_tmp.p, t1, m->s_k0.as<uint32_t>(), m->s_v0.as<uint32_t>(), nr + 1,
                           m->stream));
@@ -806,7 +806,7 @@ void destroy_bufs(mrf_map* m) {
                  &m->pair_dm,
                  &m->pair_seg, &m->dperm, &m->dpair, &m->dseg,
                  &m->carry, &m->ray_order, &m->counters, &m->tile_first,
-                 &m->vseg, &m->vpairs, &m->vvox, &m->s_postlen, &m->s_cls, &m->s_pf, &m->s_ps,
+                 &m->vseg, &m->vpairs, &m->vvox, &m->s_rec, &m->s_recs, &m->s_pf, &m->s_ps,
                  &m->s_flags, &m->s_ind, &m->s_scan,
                  &m->s_tmp, &m->s_counts, &m->s_offs, &m->s_vox, &m->s_k0, &m->s_k1, &m->s_v0,
                  &m->s_v1, &m->s_seg, &m->s_dense, &m->s_err, &m->s_depth_in, &m->s_depth,

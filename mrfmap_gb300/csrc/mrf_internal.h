@@ -56,10 +56,6 @@ static_assert(sizeof(RayMeta) == 16, "RayMeta layout");
 // the message is F_EPS * l: static for the life of the incidence lists.
 __host__ __device__ __forceinline__ int ray_kdyn(const RayMeta& m) { return (int)(m.flags >> 16); }
 
-// incidence classes written by the trace (build scratch)
-constexpr uint8_t kIncNone = 0;    // padding, or Pre-only (no message)
-constexpr uint8_t kIncStatic = 1;  // message F_EPS * l
-constexpr uint8_t kIncDyn = 2;     // message recomputed every iteration
 
 constexpr int kMaxRayLen = 65532;        // n_pre fits uint16 after padding to 4
 constexpr uint32_t kNoVoxel = 0xFFFFFFFFu;  // padding incidences
@@ -84,20 +80,22 @@ cudaError_t launch_trace_count(const Geom& g, const Pose& P, const float* depth,
                                int* err, cudaStream_t s);
 cudaError_t launch_trace_emit(const Geom& g, const Pose& P, const float* depth,
                               const uint32_t* pix_off, uint32_t inc_base, RayMeta* meta,
-                              uint32_t* inc_vox, float* inc_len, float* inc_mu, float* post_len,
-                              uint8_t* inc_cls, int* err, cudaStream_t s);
+                              uint32_t* inc_vox, float* inc_len, float* inc_mu, float2* inc_rec,
+                              int* err, cudaStream_t s);
 // pairs in voxel order and the pair-grouped positions
 cudaError_t launch_vox_heads(const uint32_t* sk, uint32_t n, uint32_t* flag, cudaStream_t s);
 cudaError_t launch_pairs_from_sorted(const uint32_t* sk, const uint32_t* sidx, const uint32_t* flag,
                                      const uint32_t* scan, uint32_t n, uint32_t pair_base,
                                      uint32_t perm_base, uint32_t inc_base, uint32_t* pair_vox,
                                      uint32_t* seg, uint32_t* inc_pair, cudaStream_t s);
+// build records (post length, -(mu l) on dynamic incidences) in sorted order
+cudaError_t launch_gather_rec(const uint32_t* sidx, uint32_t n, uint32_t inc_base, const float2* rec,
+                              float2* out, cudaStream_t s);
 // per pair: cumulative length, summed static messages, dynamic incidences,
-// potential mass
-cudaError_t launch_pair_stats(const uint32_t* seg, const uint32_t* sidx, uint32_t p0, uint32_t np,
-                              uint32_t perm_base, uint32_t inc_base, const float* post_len,
-                              const uint8_t* cls, const float* mu, float* cum, float* stat,
-                              uint32_t* ndyn, float* hit, cudaStream_t s);
+// potential mass (from the sorted records)
+cudaError_t launch_pair_stats(const uint32_t* seg, uint32_t p0, uint32_t np, uint32_t perm_base,
+                              const float2* srec, float* cum, float* stat, uint32_t* ndyn, float* hit,
+                              cudaStream_t s);
 // warm-start initial messages from a predicted log-odds field (voxel CSR)
 cudaError_t launch_warm_split(const uint32_t* vseg, const uint32_t* vpairs, const uint32_t* vvox,
                               uint32_t nvox, const float* L_pred, float lp, const float* cum,
@@ -108,8 +106,7 @@ cudaError_t launch_voxel_features(const uint32_t* vseg, const uint32_t* vpairs, 
                                   const float* belief, int64_t n_slots_vox, float* feat, cudaStream_t s);
 // dynamic incidences of a view in pair-grouped order (dperm) and the pairs
 // that own them (dpair, with their first position dseg)
-cudaError_t launch_dyn_flags(const uint32_t* sidx, uint32_t n, uint32_t inc_base, const uint8_t* cls,
-                             uint32_t* flag, cudaStream_t s);
+cudaError_t launch_dyn_flags(const float2* srec, uint32_t n, uint32_t* flag, cudaStream_t s);
 cudaError_t launch_dyn_scatter(const uint32_t* sidx, const uint32_t* flag, const uint32_t* scan,
                                uint32_t n, uint32_t inc_base, uint32_t dperm_base, uint32_t* dperm,
                                cudaStream_t s);
