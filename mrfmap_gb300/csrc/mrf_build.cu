@@ -299,35 +299,88 @@ __global__ void k_gather_rec(const uint32_t* __restrict__ sidx, uint32_t n, uint
   if (k < n) out[k] = rec[inc_base + sidx[k]];
 }
 
-// Per pair, over its incidences in increasing incidence order (the order
-// the reference's cumulative-length pass visits a voxel, pixel-major):
-// cumulative length (fp32), the sum of its static messages F_EPS * l (fp32,
-// each product rounded as the ray kernel would round it), the number of
-// dynamic incidences and the potential mass sum mu * l (a warm-start
-// feature).  Reads the pair's contiguous run of sorted records.
+// Per pair: cumulative length, the sum of its static messages F_EPS * l
+// (each product rounded as the ray kernel rounds it), the number of dynamic
+// incidences and the potential mass sum mu * l (a warm-start feature).  The
+// sums are FP64 and rounded once, so their value does not depend on the
+// summation order (the reference adds with float atomics in no fixed order).
+// A thread sums a pair's contiguous run of sorted records; runs longer than
+// kLongRun (voxels next to a camera, crossed by up to ~10^5 rays) are
+// appended to a list and summed by a whole block each.
+constexpr uint32_t kLongRun = 512;
+constexpr int kStatThreads = 256;
+
+struct PairSums {
+  double c, st, h;
+  uint32_t nd;
+};
+
+__device__ __forceinline__ void add_rec(PairSums& a, const float2 r) {
+  a.c += (double)r.x;
+  if (signbit(r.y)) {
+    a.h -= (double)r.y;
+    ++a.nd;
+  } else {
+    a.st += (double)__fmul_rn(kFEps, r.x);
+  }
+}
+
+__device__ __forceinline__ void store_sums(uint32_t p, const PairSums& a, float* __restrict__ cum,
+                                           float* __restrict__ stat, uint32_t* __restrict__ ndyn,
+                                           float* __restrict__ hit) {
+  cum[p] = (float)a.c;
+  stat[p] = (float)a.st;
+  ndyn[p] = a.nd;
+  hit[p] = (float)a.h;
+}
+
 __global__ void k_pair_stats(const uint32_t* __restrict__ seg, uint32_t p0, uint32_t np, uint32_t perm_base,
                              const float2* __restrict__ srec, float* __restrict__ cum,
                              float* __restrict__ stat, uint32_t* __restrict__ ndyn,
-                             float* __restrict__ hit) {
+                             float* __restrict__ hit, uint32_t* __restrict__ long_list) {
   uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= np) return;
   uint32_t p = p0 + q;
-  float c = 0.0f, st = 0.0f, h = 0.0f;
-  uint32_t nd = 0;
-  for (uint32_t k = seg[p]; k < seg[p + 1]; ++k) {
-    const float2 r = srec[k - perm_base];
-    c += r.x;
-    if (signbit(r.y)) {
-      h -= r.y;
-      ++nd;
-    } else {
-      st += __fmul_rn(kFEps, r.x);
-    }
+  const uint32_t k0 = seg[p] - perm_base, k1 = seg[p + 1] - perm_base;
+  if (k1 - k0 > kLongRun) {
+    long_list[1 + atomicAdd(long_list, 1u)] = p;
+    return;
   }
-  cum[p] = c;
-  stat[p] = st;
-  ndyn[p] = nd;
-  hit[p] = h;
+  PairSums a{0.0, 0.0, 0.0, 0u};
+  for (uint32_t k = k0; k < k1; ++k) add_rec(a, srec[k]);
+  store_sums(p, a, cum, stat, ndyn, hit);
+}
+
+// one block per listed long run; block sums in a fixed tree order
+__global__ void __launch_bounds__(kStatThreads)
+    k_pair_stats_long(const uint32_t* __restrict__ seg, uint32_t perm_base, const float2* __restrict__ srec,
+                      const uint32_t* __restrict__ long_list, float* __restrict__ cum,
+                      float* __restrict__ stat, uint32_t* __restrict__ ndyn, float* __restrict__ hit) {
+  __shared__ double sc[kStatThreads], sst[kStatThreads], sh[kStatThreads];
+  __shared__ uint32_t snd[kStatThreads];
+  const uint32_t n = long_list[0];
+  for (uint32_t j = blockIdx.x; j < n; j += gridDim.x) {
+    const uint32_t p = long_list[1 + j];
+    const uint32_t k0 = seg[p] - perm_base, k1 = seg[p + 1] - perm_base;
+    PairSums a{0.0, 0.0, 0.0, 0u};
+    for (uint32_t k = k0 + threadIdx.x; k < k1; k += kStatThreads) add_rec(a, srec[k]);
+    sc[threadIdx.x] = a.c;
+    sst[threadIdx.x] = a.st;
+    sh[threadIdx.x] = a.h;
+    snd[threadIdx.x] = a.nd;
+    __syncthreads();
+    for (int o = kStatThreads / 2; o > 0; o >>= 1) {
+      if (threadIdx.x < o) {
+        sc[threadIdx.x] += sc[threadIdx.x + o];
+        sst[threadIdx.x] += sst[threadIdx.x + o];
+        sh[threadIdx.x] += sh[threadIdx.x + o];
+        snd[threadIdx.x] += snd[threadIdx.x + o];
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) store_sums(p, PairSums{sc[0], sst[0], sh[0], snd[0]}, cum, stat, ndyn, hit);
+    __syncthreads();
+  }
 }
 
 __global__ void k_dyn_flags(const float2* __restrict__ srec, uint32_t n, uint32_t* __restrict__ flag) {
@@ -453,9 +506,15 @@ cudaError_t launch_gather_rec(const uint32_t* sidx, uint32_t n, uint32_t inc_bas
 
 cudaError_t launch_pair_stats(const uint32_t* seg, uint32_t p0, uint32_t np, uint32_t perm_base,
                               const float2* srec, float* cum, float* stat, uint32_t* ndyn, float* hit,
-                              cudaStream_t s) {
+                              uint32_t* long_list, cudaStream_t s) {
   if (!np) return cudaSuccess;
-  k_pair_stats<<<grid_for(np), kThreads, 0, s>>>(seg, p0, np, perm_base, srec, cum, stat, ndyn, hit);
+  cudaError_t e = cudaMemsetAsync(long_list, 0, 4, s);
+  if (e != cudaSuccess) return e;
+  k_pair_stats<<<grid_for(np), kThreads, 0, s>>>(seg, p0, np, perm_base, srec, cum, stat, ndyn, hit,
+                                                 long_list);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_pair_stats_long<<<1024, kStatThreads, 0, s>>>(seg, perm_base, srec, long_list, cum, stat, ndyn, hit);
   return cudaGetLastError();
 }
 

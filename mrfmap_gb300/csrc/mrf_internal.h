@@ -93,9 +93,10 @@ cudaError_t launch_gather_rec(const uint32_t* sidx, uint32_t n, uint32_t inc_bas
                               float2* out, cudaStream_t s);
 // per pair: cumulative length, summed static messages, dynamic incidences,
 // potential mass (from the sorted records)
+// long_list: scratch of 1 + np u32 (count, then the pairs with long runs)
 cudaError_t launch_pair_stats(const uint32_t* seg, uint32_t p0, uint32_t np, uint32_t perm_base,
                               const float2* srec, float* cum, float* stat, uint32_t* ndyn, float* hit,
-                              cudaStream_t s);
+                              uint32_t* long_list, cudaStream_t s);
 // warm-start initial messages from a predicted log-odds field (voxel CSR)
 cudaError_t launch_warm_split(const uint32_t* vseg, const uint32_t* vpairs, const uint32_t* vvox,
                               uint32_t nvox, const float* L_pred, float lp, const float* cum,

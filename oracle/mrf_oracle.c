@@ -576,10 +576,12 @@ static void build_view(orc_map* m, int c) {
       v->nrays++;
     }
   }
-  /* potentials (FP64) and cumulative lengths (fp32, incidence order) */
+  /* potentials (FP64) and cumulative lengths (summed in FP64, rounded once
+   * to fp32: the value then does not depend on the order of the additions,
+   * which the reference leaves to float atomics) */
   v->mu = (double*)malloc((size_t)(v->ninc ? v->ninc : 1) * sizeof(double));
   int64_t nv = (int64_t)m->nbricks * BVOX;
-  for (int64_t i = 0; i < nv; ++i) v->cum_len[i] = 0.0f;
+  double* cum_d = (double*)calloc((size_t)(nv ? nv : 1), sizeof(double));
   unsigned char* seen = (unsigned char*)calloc((size_t)(nv ? nv : 1), 1);
   v->touch = (int*)malloc((size_t)(nv ? nv : 1) * sizeof(int));
   v->ntouch = 0;
@@ -596,7 +598,7 @@ static void build_view(orc_map* m, int c) {
       v->mu[k] = potential_is_zero_f(sg, bs, m->p.lookup_n, s, d)
                      ? 0.0
                      : potential_d(sg, bs, m->p.lookup_n, (double)s, (double)d);
-      if (i < me[1]) v->cum_len[v->vox[k]] += v->len[k];
+      if (i < me[1]) cum_d[v->vox[k]] += (double)v->len[k];
       if (!seen[v->vox[k]]) {
         seen[v->vox[k]] = 1;
         v->touch[v->ntouch++] = v->vox[k];
@@ -604,6 +606,8 @@ static void build_view(orc_map* m, int c) {
     }
   }
   free(seen);
+  for (int64_t i = 0; i < nv; ++i) v->cum_len[i] = (float)cum_d[i];
+  free(cum_d);
   v->built_version = m->version;
 }
 
