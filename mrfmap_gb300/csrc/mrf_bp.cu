@@ -101,8 +101,10 @@ __device__ __forceinline__ T warp_excl_scan(T v, int lane) {
 }
 
 // one lane's slice of a chunk
+// (ln q is kept; q itself is formed only where a potential is non-zero or
+// a message is computed)
 struct Slice {
-  float A[kE], q[kE], mu[kE], len[kE];
+  float A[kE], lq[kE], mu[kE], len[kE];
 };
 
 // streamed incidence arrays: read-only path (kPol 0) or evict-first
@@ -153,7 +155,7 @@ __device__ __forceinline__ float slice_from_pids(Slice& s, const uint32_t (&pid)
 #pragma unroll
   for (int j = 0; j < kE; ++j) {
     const bool ok = i0 + j < n;
-    s.q[j] = ok ? __expf(lq[j]) : 1.0f;
+    s.lq[j] = ok ? lq[j] : 0.0f;
     if (!ok) {
       s.len[j] = 0.0f;
       s.mu[j] = 0.0f;
@@ -245,7 +247,7 @@ __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, const uint32_t* _
   const uint32_t off = me.off;
   // ---- pass 1: prefixes, Pre total ---------------------------------------
   float carryA = 0.0f, Ar0 = 0.0f, Arinf = 0.0f, Ak = 0.0f;
-  Acc T = 0;
+  Acc T = 0, Tl = 0;
   Slice s;
   // kPf: the next chunk's pair ids are requested before this chunk's ln q
   // gathers, so a chunk waits on one memory round trip instead of two
@@ -272,15 +274,15 @@ __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, const uint32_t* _
     float w = 0.0f;
 #pragma unroll
     for (int j = 0; j < kE; ++j) {
-      float V = __expf(s.A[j]);
       if (i0 + j >= r0 && s.mu[j] != 0.0f) {
-        float vp = direct ? __expf(s.A[j] - Ar0) : V * scale;
-        w += vp * (1.0f - s.q[j]) * s.mu[j];
+        float vp = direct ? __expf(s.A[j] - Ar0) : __expf(s.A[j]) * scale;
+        w += vp * (1.0f - __expf(s.lq[j])) * s.mu[j];
       }
     }
-    T += (Acc)warp_sum(w);
+    Tl += (Acc)w;
     carryA += tot;
   }
+  T = warp_sum(Tl);  // each lane's share of the Pre total, summed once per ray
   // infinity term: visibility at the end of Pre (gvdbkernels.cu:1196-1208)
   if (me.flags & 1u) T += (Acc)__expf(carryA - Arinf);
   if (kdyn >= n_post) return;  // every message of the ray is static
@@ -294,9 +296,13 @@ __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, const uint32_t* _
     float tot2 = load_slice<kPol>(s, off, i0, n_post, k4, carryA2, lane, inc_pair, inc_len, inc_mu,
                                   lnq);
     carryA2 += tot2;
+    float q[kE];
 #pragma unroll
-    for (int j = 0; j < kE; ++j) vmu[j] = __expf(s.A[j]) * s.mu[j];
-    carryF = emit_slice<Acc>(vmu, s.q, s.len, i0, k4, n_post, T, carryF, lane, off, inc_pl);
+    for (int j = 0; j < kE; ++j) {
+      vmu[j] = __expf(s.A[j]) * s.mu[j];
+      q[j] = __expf(s.lq[j]);
+    }
+    carryF = emit_slice<Acc>(vmu, q, s.len, i0, k4, n_post, T, carryF, lane, off, inc_pl);
   }
 }
 
