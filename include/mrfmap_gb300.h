@@ -177,12 +177,14 @@ MRF_API mrf_status mrf_net_adam(float* params, const float* grads, float* m1, fl
                                 float lr, float beta1, float beta2, float eps, int step, void* stream);
 
 /* Autotuner (no reference counterpart).  The ray-message kernel comes in
- * variants that differ in register budget (resident blocks per SM) and in
- * the cache policy of its streamed loads; their arithmetic is identical, so
- * the choice never changes a result.  mrf_autotune times every variant on
- * this map's own incidence lists (reps timed passes over every view after
- * one warm-up), keeps the fastest and returns per-variant milliseconds per
- * pass in ms_out[0..min(cap, mrf_ray_variants())). */
+ * variants that differ in the cache policy of its streamed loads and in
+ * whether a chunk's pair ids are requested one chunk ahead; their
+ * arithmetic is identical, so the choice never changes a result.
+ * mrf_autotune times every variant on this map's own incidence lists (reps
+ * timed Gauss-Seidel iterations after one warm-up, the map state saved
+ * before and restored after each variant), keeps the fastest and returns
+ * per-variant milliseconds per iteration in
+ * ms_out[0..min(cap, mrf_ray_variants())). */
 MRF_API int mrf_ray_variants(void);
 MRF_API mrf_status mrf_set_ray_variant(mrf_map* map, int variant);
 MRF_API mrf_status mrf_autotune(mrf_map* map, int reps, double* ms_out, int cap, int* chosen);

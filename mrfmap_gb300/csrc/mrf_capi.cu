@@ -124,7 +124,7 @@ struct mrf_map {
   int jacobi_version = -1;
   // scratch
   DBuf s_rec, s_recs, s_pf, s_ps, s_flags, s_ind, s_scan, s_tmp, s_counts, s_offs, s_vox, s_k0, s_k1, s_v0, s_v1,
-      s_seg, s_dense, s_err, s_depth_in, s_depth, s_img, s_part, s_sum, s_prev, s_delta;
+      s_seg, s_dense, s_err, s_depth_in, s_depth, s_img, s_part, s_sum, s_prev, s_delta, s_snap;
   mrf_stats stats{};
   // MRF_PROFILE event pool
   std::vector<cudaEvent_t> prof_ev;
@@ -811,7 +811,7 @@ void destroy_bufs(mrf_map* m) {
                  &m->s_flags, &m->s_ind, &m->s_scan,
                  &m->s_tmp, &m->s_counts, &m->s_offs, &m->s_vox, &m->s_k0, &m->s_k1, &m->s_v0,
                  &m->s_v1, &m->s_seg, &m->s_dense, &m->s_err, &m->s_depth_in, &m->s_depth,
-                 &m->s_img, &m->s_part, &m->s_sum, &m->s_prev, &m->s_delta};
+                 &m->s_img, &m->s_part, &m->s_sum, &m->s_prev, &m->s_delta, &m->s_snap};
   for (DBuf* b : all) b->release();
   for (auto& v : m->views) v.depth.release();
 }
@@ -1187,25 +1187,35 @@ mrf_status mrf_autotune(mrf_map* m, int reps, double* ms_out, int cap, int* chos
     BpArrays a = m->bp();
     std::vector<double> ms(NV, 0.0);
     if (m->n_inc > 0) {
-      // ln q of the current state for every pair; the ray pass only writes
-      // the per-iteration message scratch, so the map state is untouched
-      CK(launch_pair_prepare(a, 0, (uint32_t)m->n_pairs, 0, m->stream));
+      // Each variant runs whole Gauss-Seidel iterations (the ray kernel's
+      // cache policy also changes what the pair kernels after it find in
+      // L2); the map state is saved first and restored after every variant.
+      const size_t nv = (size_t)m->n_bricks * kBrickVox * 4, npb = (size_t)m->n_pairs * 4;
+      m->s_snap.reserve(2 * nv + npb, false, m->stream);
+      char* snap = static_cast<char*>(m->s_snap.p);
+      CK(cudaMemcpyAsync(snap, m->d_L.p, nv, cudaMemcpyDeviceToDevice, m->stream));
+      CK(cudaMemcpyAsync(snap + nv, m->d_belief.p, nv, cudaMemcpyDeviceToDevice, m->stream));
+      CK(cudaMemcpyAsync(snap + 2 * nv, m->pair_m.p, npb, cudaMemcpyDeviceToDevice, m->stream));
+      const int keep = m->ray_variant;
+      Profiler off{m, false};
+      int64_t launches = 0;
       for (int k = 0; k < NV; ++k) {
+        m->ray_variant = k;
         for (int r = 0; r <= reps; ++r) {
-          CK(cudaMemsetAsync(m->counters.p, 0, (size_t)(V + 1) * 4, m->stream));
           if (r == 1) CK(cudaEventRecord(m->ev0, m->stream));
-          for (int c = 0; c < V; ++c) {
-            const View& v = m->views[c];
-            CK(launch_ray_bp(a, m->ray_order.as<uint32_t>() + v.order_base, v.n_active,
-                             m->counters.as<uint32_t>() + c, 0, m->num_sms, k, m->stream));
-          }
+          enqueue_iteration(m, a, false, 0, false, off, launches);
         }
         CK(cudaEventRecord(m->ev1, m->stream));
         sync(m);
         float t = 0.0f;
         CK(cudaEventElapsedTime(&t, m->ev0, m->ev1));
         ms[k] = t / reps;
+        CK(cudaMemcpyAsync(m->d_L.p, snap, nv, cudaMemcpyDeviceToDevice, m->stream));
+        CK(cudaMemcpyAsync(m->d_belief.p, snap + nv, nv, cudaMemcpyDeviceToDevice, m->stream));
+        CK(cudaMemcpyAsync(m->pair_m.p, snap + 2 * nv, npb, cudaMemcpyDeviceToDevice, m->stream));
       }
+      m->ray_variant = keep;
+      sync(m);
     }
     int best = 0;
     for (int k = 1; k < NV; ++k)
