@@ -128,15 +128,21 @@ __device__ __forceinline__ void load_pids(uint32_t (&pid)[kE], uint32_t off, int
   }
 }
 
-// with the lane's pair ids loaded: loads lengths (and potentials at and
-// after kmu, a multiple of 4; below it they are known zeros), gathers ln q,
-// forms prefix exponents from carryA; returns the chunk total of l ln q
+// ln q of a lane's kE incidences (those >= n read as zero)
+__device__ __forceinline__ void gather_lq(float (&lq)[kE], const uint32_t (&pid)[kE], int i0, int n,
+                                          const float* __restrict__ lnq) {
+#pragma unroll
+  for (int j = 0; j < kE; ++j) lq[j] = (i0 + j < n) ? __ldg(lnq + pid[j]) : 0.0f;
+}
+
+// with the lane's ln q gathered: loads lengths (and potentials at and after
+// kmu, a multiple of 4; below it they are known zeros), forms prefix
+// exponents from carryA; returns the chunk total of l ln q
 template <int kPol>
-__device__ __forceinline__ float slice_from_pids(Slice& s, const uint32_t (&pid)[kE], uint32_t off, int i0,
-                                                 int n, int kmu, float carryA, int lane,
-                                                 const float* __restrict__ inc_len,
-                                                 const float* __restrict__ inc_mu,
-                                                 const float* __restrict__ lnq) {
+__device__ __forceinline__ float slice_from_lq(Slice& s, const float (&lq)[kE], uint32_t off, int i0, int n,
+                                               int kmu, float carryA, int lane,
+                                               const float* __restrict__ inc_len,
+                                               const float* __restrict__ inc_mu) {
 #pragma unroll
   for (int v = 0; v < kE / 4; ++v) {
     const int i = i0 + 4 * v;
@@ -148,9 +154,6 @@ __device__ __forceinline__ float slice_from_pids(Slice& s, const uint32_t (&pid)
     s.len[4 * v + 0] = l.x; s.len[4 * v + 1] = l.y; s.len[4 * v + 2] = l.z; s.len[4 * v + 3] = l.w;
     s.mu[4 * v + 0] = m.x; s.mu[4 * v + 1] = m.y; s.mu[4 * v + 2] = m.z; s.mu[4 * v + 3] = m.w;
   }
-  float lq[kE];
-#pragma unroll
-  for (int j = 0; j < kE; ++j) lq[j] = (i0 + j < n) ? __ldg(lnq + pid[j]) : 0.0f;
   float run = 0.0f;
 #pragma unroll
   for (int j = 0; j < kE; ++j) {
@@ -168,6 +171,17 @@ __device__ __forceinline__ float slice_from_pids(Slice& s, const uint32_t (&pid)
 #pragma unroll
   for (int j = 0; j < kE; ++j) s.A[j] += b;
   return __shfl_sync(kFull, ex + run, 31);
+}
+
+template <int kPol>
+__device__ __forceinline__ float slice_from_pids(Slice& s, const uint32_t (&pid)[kE], uint32_t off, int i0,
+                                                 int n, int kmu, float carryA, int lane,
+                                                 const float* __restrict__ inc_len,
+                                                 const float* __restrict__ inc_mu,
+                                                 const float* __restrict__ lnq) {
+  float lq[kE];
+  gather_lq(lq, pid, i0, n, lnq);
+  return slice_from_lq<kPol>(s, lq, off, i0, n, kmu, carryA, lane, inc_len, inc_mu);
 }
 
 template <int kPol>
@@ -233,7 +247,7 @@ __device__ __forceinline__ Acc emit_slice(const float (&vmu)[kE], const float (&
   return carryF + (Acc)__shfl_sync(kFull, ex + run, 31);
 }
 
-template <typename Acc, int kPol, bool kPf>
+template <typename Acc, int kPol, int kPf>
 __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, const uint32_t* __restrict__ inc_pair,
                                             const float* __restrict__ inc_len,
                                             const float* __restrict__ inc_mu,
@@ -250,7 +264,9 @@ __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, const uint32_t* _
   Acc T = 0, Tl = 0;
   Slice s;
   // kPf: the next chunk's pair ids are requested before this chunk's ln q
-  // gathers, so a chunk waits on one memory round trip instead of two
+  // gathers, so a chunk waits on one memory round trip instead of two.
+  // (Issuing the next chunk's gathers early as well needs ~95 registers;
+  // the lost occupancy made it slower.)
   uint32_t pid_next[kE];
   if (kPf) load_pids<kPol>(pid_next, off, kE * lane, n_pre, inc_pair);
   for (int base = 0; base < n_pre; base += kChunk) {
@@ -312,7 +328,7 @@ __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, const uint32_t* _
 // ray does not change its result.  Variants differ only in register budget
 // (kMinBlocks resident blocks per SM) and load policy: their arithmetic is
 // identical, so the autotuner's choice never changes a result.
-template <int kMinBlocks, int kPol, bool kPf>
+template <int kMinBlocks, int kPol, int kPf>
 __global__ void __launch_bounds__(kRayWarps * 32, kMinBlocks) k_ray_bp(const RayMeta* __restrict__ meta,
                                                            const uint32_t* __restrict__ order,
                                                            uint32_t n_rays,
@@ -382,14 +398,35 @@ __device__ __forceinline__ void apply_pair(uint32_t p, float acc, const uint32_t
   belief[v] = 1.0f - clampf(1.0f / (1.0f + expf(Lv)), kFEps, 1.0f - kFEps);
 }
 
+// the same for a dynamic run, whose pair id, voxel, cumulative length and
+// static-message sum are stored together (one 16-byte load; the voxel's L
+// gather does not wait on a pair-id lookup)
+__device__ __forceinline__ void apply_run(const uint4 r, float acc_dyn, float* __restrict__ m,
+                                          float* __restrict__ L, float* __restrict__ belief,
+                                          float* __restrict__ dm, int jacobi) {
+  const uint32_t p = r.x, v = r.y;
+  const float c = __uint_as_float(r.z);
+  if (!(c > kCumLenGate)) return;  // gvdbkernels.cu:408: the pair never updates
+  const float mo = m[p];
+  const float Lo = jacobi ? 0.0f : L[v];
+  float a = clampf((__uint_as_float(r.w) + acc_dyn) / c, kFEps, 1.0f - kFEps);
+  float mn = logf(a) - logf(1.0f - a);
+  m[p] = mn;
+  if (jacobi) {
+    dm[p] = mn - mo;
+    return;
+  }
+  float Lv = Lo + (mn - mo);
+  L[v] = Lv;
+  belief[v] = 1.0f - clampf(1.0f / (1.0f + expf(Lv)), kFEps, 1.0f - kFEps);
+}
+
 __global__ void __launch_bounds__(kTileThreads, 8)
     k_pair_reduce(const uint32_t* __restrict__ perm, const float* __restrict__ pl,
                   const uint32_t* __restrict__ seg, const uint32_t* __restrict__ tile_first,
                   uint32_t k0, uint32_t k1, uint32_t p_end, TileCarry* __restrict__ carry,
-                  const uint32_t* __restrict__ dpair, const float* __restrict__ stat,
-                  const uint32_t* __restrict__ pair_vox, float* __restrict__ m,
-                  const float* __restrict__ cum, float* __restrict__ L, float* __restrict__ belief,
-                  float* __restrict__ dm, int jacobi) {
+                  const uint4* __restrict__ drun, float* __restrict__ m, float* __restrict__ L,
+                  float* __restrict__ belief, float* __restrict__ dm, int jacobi) {
   __shared__ float sv[kTile];
   __shared__ uint32_t sseg[kTile + 2];
   const int t = threadIdx.x;
@@ -413,8 +450,7 @@ __global__ void __launch_bounds__(kTileThreads, 8)
     for (uint32_t i = a; i < b; ++i) acc += sv[i];
     const bool open_start = s0 < base, open_end = s1 > end;
     if (!open_start && !open_end) {
-      const uint32_t pid = dpair[pf + q];
-      apply_pair(pid, stat[pid] + acc, pair_vox, m, cum, L, belief, dm, jacobi);
+      apply_run(drun[pf + q], acc, m, L, belief, dm, jacobi);
       continue;
     }
     TileCarry& c = carry[blockIdx.x];
@@ -465,10 +501,9 @@ __global__ void k_tile_first(const uint32_t* __restrict__ seg, uint32_t p0, uint
 // segments crossing tile edges: the tile where such a segment starts walks
 // forward adding each following tile's partial, in tile order
 __global__ void k_pair_fixup(const TileCarry* __restrict__ carry, uint32_t ntiles,
-                             const uint32_t* __restrict__ dpair, const float* __restrict__ stat,
-                             const uint32_t* __restrict__ pair_vox, float* __restrict__ m,
-                             const float* __restrict__ cum, float* __restrict__ L,
-                             float* __restrict__ belief, float* __restrict__ dm, int jacobi) {
+                             const uint4* __restrict__ drun, float* __restrict__ m,
+                             float* __restrict__ L, float* __restrict__ belief, float* __restrict__ dm,
+                             int jacobi) {
   uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ntiles) return;
   TileCarry c = carry[t];
@@ -482,8 +517,17 @@ __global__ void k_pair_fixup(const TileCarry* __restrict__ carry, uint32_t ntile
     if ((d.flags & kSingle) && (d.flags & kOpenEnd)) continue;
     break;
   }
-  const uint32_t pid = dpair[key];
-  apply_pair(pid, stat[pid] + sum, pair_vox, m, cum, L, belief, dm, jacobi);
+  apply_run(drun[key], sum, m, L, belief, dm, jacobi);
+}
+
+// per dynamic run: {pair id, voxel, cumulative length, static-message sum}
+__global__ void k_drun(const uint32_t* __restrict__ dpair, uint32_t n, const uint32_t* __restrict__ pair_vox,
+                       const float* __restrict__ cum, const float* __restrict__ stat,
+                       uint4* __restrict__ drun) {
+  uint32_t j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= n) return;
+  const uint32_t p = dpair[j];
+  drun[j] = make_uint4(p, pair_vox[p], __float_as_uint(cum[p]), __float_as_uint(stat[p]));
 }
 
 // pairs whose incidences are all static: a = (sum of F_EPS * l) / cum is a
@@ -705,13 +749,13 @@ cudaError_t launch_pair_prepare(const BpArrays& a, uint32_t p0, uint32_t p1, int
 
 
 // ray-kernel variants: (id, resident-block target, load policy, pair-id prefetch)
-#define MRF_RAY_VARIANTS(X) X(0, 0, 0, false) X(1, 0, 1, false) X(2, 0, 0, true) X(3, 0, 1, true)
+#define MRF_RAY_VARIANTS(X) X(0, 0, 0, 0) X(1, 0, 1, 0) X(2, 0, 0, 1) X(3, 0, 1, 1)
 constexpr int kRayVariants = 4;
 
 int ray_bp_variants() { return kRayVariants; }
 
 namespace {
-template <int kMinBlocks, int kPol, bool kPf>
+template <int kMinBlocks, int kPol, int kPf>
 int resident_of() {
   int per_sm = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ray_bp<kMinBlocks, kPol, kPf>,
@@ -772,13 +816,19 @@ cudaError_t launch_pair_update(const BpArrays& a, uint32_t k0, uint32_t k1, uint
   if (k1 <= k0) return cudaSuccess;
   uint32_t ntiles = (k1 - k0 + kTile - 1) / kTile;
   k_pair_reduce<<<ntiles, kTileThreads, 0, s>>>(a.dperm, a.inc_pl, a.dseg, tile_first, k0, k1, j1,
-                                                carry, a.dpair, a.pair_stat, a.pair_vox, a.pair_m,
-                                                a.pair_cum, a.L, a.belief, a.pair_dm, jacobi);
+                                                carry, a.drun, a.pair_m, a.L, a.belief, a.pair_dm,
+                                                jacobi);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  k_pair_fixup<<<blocks(ntiles, 256), 256, 0, s>>>(carry, ntiles, a.dpair, a.pair_stat, a.pair_vox,
-                                                   a.pair_m, a.pair_cum, a.L, a.belief, a.pair_dm,
-                                                   jacobi);
+  k_pair_fixup<<<blocks(ntiles, 256), 256, 0, s>>>(carry, ntiles, a.drun, a.pair_m, a.L, a.belief,
+                                                   a.pair_dm, jacobi);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_drun(const uint32_t* dpair, uint32_t n, const uint32_t* pair_vox, const float* cum,
+                        const float* stat, uint4* drun, cudaStream_t s) {
+  if (!n) return cudaSuccess;
+  k_drun<<<blocks(n, 256), 256, 0, s>>>(dpair, n, pair_vox, cum, stat, drun);
   return cudaGetLastError();
 }
 

@@ -115,7 +115,7 @@ struct mrf_map {
   std::vector<View> views;
   // arenas
   DBuf meta, inc_pair, inc_len, inc_mu, inc_pl, pair_vox, pair_m, pair_cum, pair_stat, pair_ndyn, pair_hit,
-      pair_q, pair_dm, pair_seg, dperm, dpair, dseg, carry, ray_order, counters, tile_first;
+      pair_q, pair_dm, pair_seg, dperm, dpair, dseg, drun, carry, ray_order, counters, tile_first;
   uint32_t jac_tile_base = 0;
   int64_t n_inc = 0, n_pairs = 0, n_dperm = 0, n_dpairs = 0;
   // jacobi voxel CSR
@@ -147,6 +147,7 @@ struct mrf_map {
     a.dperm = dperm.as<uint32_t>();
     a.dpair = dpair.as<uint32_t>();
     a.dseg = dseg.as<uint32_t>();
+    a.drun = drun.as<uint4>();
     a.pair_vox = pair_vox.as<uint32_t>();
     a.pair_m = pair_m.as<float>();
     a.pair_cum = pair_cum.as<float>();
@@ -437,6 +438,9 @@ void rebuild(mrf_map* m) {
   m->dpair.reserve((size_t)(dpair_total + 1) * 4, true, m->stream);
   m->dseg.reserve((size_t)(dpair_total + 1) * 4, true, m->stream);
   if (dpair_total == 0) CK(launch_fill_u32(m->dseg.as<uint32_t>(), 1, 0u, m->stream));
+  m->drun.reserve((size_t)(dpair_total + 1) * 16, false, m->stream);
+  CK(launch_drun(m->dpair.as<uint32_t>(), (uint32_t)dpair_total, m->pair_vox.as<uint32_t>(),
+                 m->pair_cum.as<float>(), m->pair_stat.as<float>(), m->drun.as<uint4>(), m->stream));
   m->pair_q.reserve(pb * 4, false, m->stream);
   m->pair_dm.reserve(pb * 4, false, m->stream);
   CK(launch_fill_f32(m->pair_m.as<float>(), pair_total, 0.0f, m->stream));
@@ -805,7 +809,7 @@ void destroy_bufs(mrf_map* m) {
                  &m->meta, &m->inc_pair, &m->inc_len, &m->inc_mu, &m->inc_pl, &m->pair_vox,
                  &m->pair_m, &m->pair_cum, &m->pair_stat, &m->pair_ndyn, &m->pair_hit, &m->pair_q,
                  &m->pair_dm,
-                 &m->pair_seg, &m->dperm, &m->dpair, &m->dseg,
+                 &m->pair_seg, &m->dperm, &m->dpair, &m->dseg, &m->drun,
                  &m->carry, &m->ray_order, &m->counters, &m->tile_first,
                  &m->vseg, &m->vpairs, &m->vvox, &m->s_rec, &m->s_recs, &m->s_pf, &m->s_ps,
                  &m->s_flags, &m->s_ind, &m->s_scan,

@@ -139,6 +139,7 @@ struct BpArrays {
   const uint32_t* dperm;   // dynamic incidence at each pair-grouped position
   const uint32_t* dpair;   // pair owning each dynamic run
   const uint32_t* dseg;    // first dynamic position of each run
+  const uint4* drun;       // per run: pair id, voxel, cumulative length, static sum
   const uint32_t* pair_vox;
   float* pair_m;
   const float* pair_cum;
@@ -172,6 +173,9 @@ cudaError_t launch_ray_keys(const RayMeta* meta, uint32_t n, uint32_t* keys, uin
 cudaError_t launch_pair_update(const BpArrays& a, uint32_t k0, uint32_t k1, uint32_t j0, uint32_t j1,
                                const uint32_t* tile_first, TileCarry* carry, int jacobi,
                                cudaStream_t s);
+// per-run records of the pair update (from dpair and the pair arrays)
+cudaError_t launch_drun(const uint32_t* dpair, uint32_t n, const uint32_t* pair_vox, const float* cum,
+                        const float* stat, uint4* drun, cudaStream_t s);
 // pairs p0..p1 without dynamic incidences: their constant update, needed
 // once after their messages were reset or remapped
 cudaError_t launch_static_pairs(const BpArrays& a, uint32_t p0, uint32_t p1, int jacobi,
