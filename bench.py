@@ -48,7 +48,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="full", choices=["full", "mid", "small"])
+    ap.add_argument("--workload", default="full", choices=["full", "mid", "small", "mixed"])
     ap.add_argument("--policy", default="fullray", choices=["fullray", "endpoint"])
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -64,6 +64,8 @@ def workload(name):
         return synthetic.full_room(1)
     if name == "mid":  # profiling-sized cut of the full scene: 3 views at 320x240, same voxels
         return synthetic.full_room(1, n_frames=3, rows=240, cols=320)
+    if name == "mixed":  # uneven batch: 24 views of 160x120 / 320x240 / 640x480, 2 cm
+        return synthetic.mixed_room(2, n_frames=24)
     return synthetic.small_room(0)
 
 
@@ -156,8 +158,12 @@ def cpu_port_rate(w, policy, n_views, iters, threads):
     iters Gauss-Seidel iterations over the first n_views keyframes."""
     from oracle import oracle as O
     m = O.OracleMap(w.params, threads=threads)
-    for P, D in list(zip(w.poses, w.depths))[:n_views]:
-        m.add_view(P, D, O.ACT_FULL_RAY if policy == "fullray" else O.ACT_ENDPOINT)
+    pol = O.ACT_FULL_RAY if policy == "fullray" else O.ACT_ENDPOINT
+    for k, (P, D) in enumerate(list(zip(w.poses, w.depths))[:n_views]):
+        if w.cams:
+            m.add_view_camera(P, D, D.shape[0], D.shape[1], *w.cams[k], pol)
+        else:
+            m.add_view(P, D, pol)
     for c in range(n_views):
         m.view_trace(c)  # incidence build outside the timed region
     t0 = time.perf_counter()
@@ -227,8 +233,11 @@ def run_ours(args):
     # inputs resident in HBM before the timed region
     dev_depths = [torch.from_numpy(np.ascontiguousarray(d)).cuda() for d in w.depths]
     torch.cuda.synchronize()
-    for P, D in zip(w.poses, dev_depths):
-        m.add_view_device(P, D.data_ptr())
+    for k, (P, D) in enumerate(zip(w.poses, dev_depths)):
+        if w.cams:  # views with their own cameras (host depth images)
+            m.add_view_camera(P, w.depths[k], *w.cams[k])
+        else:
+            m.add_view_device(P, D.data_ptr())
     m.infer(iters=1)  # builds the incidence lists
     # ray-kernel variant chosen by the autotuner on this workload (before the
     # timed region; variants are numerically identical)
@@ -299,8 +308,11 @@ def run_ours(args):
         barrier(ws)
         t0 = time.perf_counter()
         mm = L.MRFMap(w.params, activation=act)
-        for P, D in zip(w.poses, pinned):
-            mm.add_view(P, D.numpy())
+        for k, (P, D) in enumerate(zip(w.poses, pinned)):
+            if w.cams:
+                mm.add_view_camera(P, D.numpy(), *w.cams[k])
+            else:
+                mm.add_view(P, D.numpy())
         mm.infer(iters=iters)
         cen, bel = mm.read_bricks()
         mm.close()
@@ -317,6 +329,8 @@ def run_ours(args):
     # per-view likelihood of every keyframe under the final map (device buffers)
     like = None
     try:
+        if w.cams:
+            raise RuntimeError("per-view cameras: the device likelihood at a pose uses the params' camera")
         m.reset_state()
         m.infer(iters=iters)
         img = torch.empty(w.params.rows * w.params.cols, device="cuda")

@@ -33,7 +33,14 @@ class GVDBInference {
                                    float* out_rowmajor);
   std::vector<float> get_occupied_bricks(int lev) { return map_->get_occupied_bricks(lev); }
   void get_alphas(float* out, int64_t rows, int64_t cols) { map_->get_alphas(out, rows, cols); }
-  // debug selectors of the reference (printf probes); recorded, no effect
+  // debugging probes (src/GVDBInference.cpp:269-378): the selected pixel's
+  // per-voxel ray records (mode 0; mode 1 records nothing under the
+  // FULL_INFERENCE build), brick extents by slot (voxel units, n x 6)
+  void get_diagnostic_image(unsigned id, float* out_rowmajor, unsigned mode = 0);
+  void get_diagnostic_image_at_pose(const float* pose, const std::shared_ptr<GVDBImage>& img,
+                                    float* out_rowmajor);
+  std::vector<float> get_voxel_coords(const std::vector<uint64_t>& indices) const;
+  // selected pixel of the diagnostics; the selected voxel is recorded only
   void set_selected_x_y(unsigned x, unsigned y) { sel_x_ = x; sel_y_ = y; }
   void set_selected_voxel(uint64_t id) { sel_vox_ = id; }
   size_t num_cameras() const { return n_cams_; }

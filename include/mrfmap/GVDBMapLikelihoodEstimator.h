@@ -39,10 +39,16 @@ class GVDBMapLikelihoodEstimator {
                                     float* out_rowmajor, float occ_thresh);
   std::vector<float> get_occupied_bricks(int lev) { return map_->get_occupied_bricks(lev); }
   void get_alphas(float* out, int64_t rows, int64_t cols) { map_->get_alphas(out, rows, cols); }
-  void set_selected_x_y(unsigned, unsigned) {}
+  void set_selected_x_y(unsigned x, unsigned y) { sel_x_ = x; sel_y_ = y; }
+  // the selected pixel's per-voxel ray records
+  // (src/GVDBMapLikelihoodEstimator.cpp:436-500)
+  void get_diagnostic_image(unsigned id, float* out_rowmajor);
+  void get_diagnostic_image_at_pose(const float* pose, const std::shared_ptr<GVDBImage>& img,
+                                    float* out_rowmajor);
   void set_acc_thresh(float t) { params_.acc_thresh = t; }
 
  private:
   std::vector<std::vector<float>> poses_;
   std::vector<std::shared_ptr<GVDBImage>> images_;
+  unsigned sel_x_ = 0, sel_y_ = 0;
 };

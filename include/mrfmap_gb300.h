@@ -106,6 +106,17 @@ MRF_API mrf_status mrf_add_view(mrf_map* map, const float* pose, const float* de
 /* Same, with the depth image already in device memory. */
 MRF_API mrf_status mrf_add_view_device(mrf_map* map, const float* pose, const float* depth_dev,
                                int* view_id);
+/* A view with its own pinhole camera (no counterpart in the reference, whose
+ * cameras all share gvdb_params_t's rows, cols and K): depth_host holds
+ * rows*cols floats.  The sensor tables (params' sigma/bias, tiled over the
+ * params' image) are looked up at the pixel's position scaled into the
+ * params' image, so one table serves every resolution of the same sensor.
+ * Views of any sizes can share a map; mrf_likelihood_view, mrf_render_view
+ * and mrf_view_incidences use the view's camera. */
+MRF_API mrf_status mrf_add_view_camera(mrf_map* map, const float* pose, const float* depth_host, int rows,
+                                       int cols, float fx, float fy, float cx, float cy, int* view_id);
+/* A view's camera: rows, cols, and fx, fy, cx, cy in k4 (any may be NULL). */
+MRF_API mrf_status mrf_view_camera(mrf_map* map, int view_id, int* rows, int* cols, float* k4);
 /* GVDBInference::set_pose (src/GVDBInference.cpp:66-82): moves a view and
  * activates bricks for its new pose. */
 MRF_API mrf_status mrf_set_pose(mrf_map* map, int view_id, const float* pose);
@@ -242,6 +253,19 @@ MRF_API mrf_status mrf_render(mrf_map* map, int mode, const float* pose, const f
 /* Same at a stored view's pose and depth image. */
 MRF_API mrf_status mrf_render_view(mrf_map* map, int mode, int view_id, float threshold,
                                    float* out_img, float* out_score, int64_t* counts);
+
+/* GVDBInference::get_diagnostic_image(id, img, 0) and
+ * get_diagnostic_image_at_pose (src/GVDBInference.cpp:287-378, kernel
+ * src/cuda/gvdbkernels.cu:573-672, 1365-1384): the ray of pixel (x, y) at a
+ * pose, traversed through every active brick to the volume exit, one record
+ * of ten floats per voxel in out[n_floats] (host): [0] exit distance (m),
+ * [1] belief, [2..3] voxel id as uint64 (slot*512 + (x*8+y)*8+z), [4] first
+ * return density w = (V_prev - V)/l, [5] visibility V, [6..7] brick slot as
+ * uint64, [8] brick-local x, y, z as bytes; out[n_floats-1] holds the number
+ * of records; the rest is zero.  n_floats >= 11 (the reference uses the
+ * rows*cols image). */
+MRF_API mrf_status mrf_pixel_diagnostics(mrf_map* map, const float* pose, int x, int y, float* out,
+                                         int64_t n_floats);
 
 /* GVDBMRFMap::get_occupied_bricks(0) (src/GVDBMRFMap.cpp:137-152). */
 MRF_API mrf_status mrf_num_bricks(mrf_map* map, int64_t* n_bricks);

@@ -99,7 +99,7 @@ def build_pymodule(force: bool = False) -> str:
     inc = _torch_pybind_include()
     if inc is None:
         raise RuntimeError("pybind11 headers not found")
-    srcs = [os.path.join(CSRC, "shim", f) for f in ("GVDBShim.cpp", "GVDBPyModules.cpp")]
+    srcs = [os.path.join(CSRC, "shim", f) for f in ("GVDBShim.cpp", "GVDBPyModules.cpp", "KeyframeSelector.cpp")]
     hdrs = [os.path.join(ROOT, "include", "mrfmap", h) for h in
             ("GVDBParams.h", "GVDBImage.h", "GVDBInference.h", "GVDBMapLikelihoodEstimator.h",
              "GVDBMRFMap.h")]

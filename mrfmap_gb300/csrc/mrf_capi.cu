@@ -82,6 +82,8 @@ struct DBuf {
 
 struct View {
   Pose pose;
+  Geom cam;                  // the map geometry with this view's camera
+  int64_t pix_base = 0;      // first pixel of the view in the per-pixel arrays
   DBuf depth;
   uint32_t inc_base = 0, n_inc = 0;
   uint32_t pair_base = 0, n_pairs = 0;
@@ -217,7 +219,9 @@ void commit_new_bricks(mrf_map* m) {
 void activate_view(mrf_map* m, const View& v) {
   CK(cudaMemsetAsync(m->s_flags.p, 0, (size_t)m->nb_grid, m->stream));
   m->g.brick_slot = m->d_slot.as<int>();
-  CK(launch_activate(m->g, v.pose, v.depth.as<float>(), m->prm.activation, m->s_flags.as<uint8_t>(),
+  Geom g = v.cam;
+  g.brick_slot = m->d_slot.as<int>();
+  CK(launch_activate(g, v.pose, v.depth.as<float>(), m->prm.activation, m->s_flags.as<uint8_t>(),
                      m->stream));
   commit_new_bricks(m);
 }
@@ -225,8 +229,14 @@ void activate_view(mrf_map* m, const View& v) {
 // ---- incidence lists ---------------------------------------------------
 void rebuild(mrf_map* m) {
   const int V = (int)m->views.size();
-  const int64_t HW = m->hw();
   m->g.brick_slot = m->d_slot.as<int>();
+  // per-pixel arrays of all views back to back (views may differ in size)
+  int64_t npix = 0;
+  for (View& v : m->views) {
+    v.pix_base = npix;
+    v.cam.brick_slot = m->g.brick_slot;
+    npix += (int64_t)v.cam.rows * v.cam.cols;
+  }
   CK(cudaEventRecord(m->ev0, m->stream));
   // keep old pair arrays for message remapping
   bool remap = m->has_messages && m->n_pairs > 0;
@@ -246,13 +256,12 @@ void rebuild(mrf_map* m) {
     }
   }
   // 1. counts of every pixel of every view, one global scan -> offsets
-  int64_t npix = (int64_t)V * HW;
   u32_checked(npix, "pixel count");
   m->s_counts.reserve((size_t)npix * 4 + 4, false, m->stream);
   m->s_offs.reserve((size_t)npix * 4 + 4, false, m->stream);
   for (int c = 0; c < V; ++c)
-    CK(launch_trace_count(m->g, m->views[c].pose, m->views[c].depth.as<float>(),
-                          m->s_counts.as<uint32_t>() + c * HW, m->s_err.as<int>(), m->stream));
+    CK(launch_trace_count(m->views[c].cam, m->views[c].pose, m->views[c].depth.as<float>(),
+                          m->s_counts.as<uint32_t>() + m->views[c].pix_base, m->s_err.as<int>(), m->stream));
   // sentinel 0 at the end so the scan yields the total
   CK(cudaMemsetAsync(m->s_counts.as<uint32_t>() + npix, 0, 4, m->stream));
   size_t tb = scan_temp_bytes((uint32_t)(npix + 1));
@@ -261,7 +270,7 @@ void rebuild(mrf_map* m) {
                         (uint32_t)(npix + 1), m->stream));
   std::vector<uint32_t> bounds(V + 1);
   for (int c = 0; c <= V; ++c)
-    CK(cudaMemcpyAsync(&bounds[c], m->s_offs.as<uint32_t>() + (int64_t)c * HW, 4,
+    CK(cudaMemcpyAsync(&bounds[c], m->s_offs.as<uint32_t>() + (c < V ? m->views[c].pix_base : npix), 4,
                        cudaMemcpyDeviceToHost, m->stream));
   sync(m);
   check_device_err(m);
@@ -282,8 +291,8 @@ void rebuild(mrf_map* m) {
     View& v = m->views[c];
     v.inc_base = bounds[c];
     v.n_inc = bounds[c + 1] - bounds[c];
-    CK(launch_trace_emit(m->g, v.pose, v.depth.as<float>(), m->s_offs.as<uint32_t>() + c * HW, 0,
-                         m->meta.as<RayMeta>() + c * HW, m->s_vox.as<uint32_t>(),
+    CK(launch_trace_emit(v.cam, v.pose, v.depth.as<float>(), m->s_offs.as<uint32_t>() + v.pix_base, 0,
+                         m->meta.as<RayMeta>() + v.pix_base, m->s_vox.as<uint32_t>(),
                          m->inc_len.as<float>(), m->inc_mu.as<float>(), m->s_rec.as<float2>(),
                          m->s_err.as<int>(), m->stream));
   }
@@ -296,14 +305,16 @@ void rebuild(mrf_map* m) {
                        m->stream));
     sync(m);
     check_device_err(m);
-    for (int c = 0; c < V; ++c)
-      for (int64_t i = 0; i < HW; ++i) {
-        const RayMeta& r = hm[(size_t)(c * HW + i)];
+    for (int c = 0; c < V; ++c) {
+      const View& vc = m->views[c];
+      for (int64_t i = 0; i < (int64_t)vc.cam.rows * vc.cam.cols; ++i) {
+        const RayMeta& r = hm[(size_t)(vc.pix_base + i)];
         nreal[c] += r.n_pre;
         nrays += r.n_pre > 0;
         npost += r.n_post;
         ndyn += r.n_post - std::min<int>(ray_kdyn(r), r.n_post);
       }
+    }
     for (int c = 0; c < V; ++c) npre += nreal[c];
   }
   // 4. pairs per view in voxel order: sort the view's incidences by voxel
@@ -399,26 +410,29 @@ void rebuild(mrf_map* m) {
   }
   // ray queues: per view, the active rays longest first
   {
+    int64_t hw_max = 0;
+    for (const View& v : m->views) hw_max = std::max<int64_t>(hw_max, (int64_t)v.cam.rows * v.cam.cols);
     m->ray_order.reserve((size_t)std::max<int64_t>(npix, 1) * 4, false, m->stream);
-    m->s_k0.reserve((size_t)HW * 4 + 4, false, m->stream);
-    m->s_k1.reserve((size_t)HW * 4 + 4, false, m->stream);
-    m->s_v0.reserve((size_t)HW * 4 + 4, false, m->stream);
+    m->s_k0.reserve((size_t)hw_max * 4 + 4, false, m->stream);
+    m->s_k1.reserve((size_t)hw_max * 4 + 4, false, m->stream);
+    m->s_v0.reserve((size_t)hw_max * 4 + 4, false, m->stream);
     int64_t base = 0;
     for (int c = 0; c < V; ++c) {
       View& v = m->views[c];
+      const int64_t hw = (int64_t)v.cam.rows * v.cam.cols;
       int64_t act = 0;
-      for (int64_t i = 0; i < HW; ++i) act += hm[(size_t)(c * HW + i)].n_pre > 0;
+      for (int64_t i = 0; i < hw; ++i) act += hm[(size_t)(v.pix_base + i)].n_pre > 0;
       v.order_base = (uint32_t)base;
       v.n_active = (uint32_t)act;
-      CK(launch_ray_keys(m->meta.as<RayMeta>() + c * HW, (uint32_t)HW, m->s_k0.as<uint32_t>(),
+      CK(launch_ray_keys(m->meta.as<RayMeta>() + v.pix_base, (uint32_t)hw, m->s_k0.as<uint32_t>(),
                          m->s_v0.as<uint32_t>(), m->stream));
-      size_t t = sort_temp_bytes((uint32_t)HW, 17);
+      size_t t = sort_temp_bytes((uint32_t)hw, 17);
       m->s_tmp.reserve(t, false, m->stream);
       CK(sort_pairs_u32(m->s_tmp.p, t, m->s_k0.as<uint32_t>(), m->s_k1.as<uint32_t>(),
-                        m->s_v0.as<uint32_t>(), m->ray_order.as<uint32_t>() + base, (uint32_t)HW, 17,
+                        m->s_v0.as<uint32_t>(), m->ray_order.as<uint32_t>() + base, (uint32_t)hw, 17,
                         m->stream));
       // queue entries are global ray indices
-      CK(launch_add_u32(m->ray_order.as<uint32_t>() + base, (uint32_t)act, (uint32_t)(c * HW), m->stream));
+      CK(launch_add_u32(m->ray_order.as<uint32_t>() + base, (uint32_t)act, (uint32_t)v.pix_base, m->stream));
       base += act;
     }
     m->counters.reserve((size_t)(V + 1) * 4, false, m->stream);
@@ -775,6 +789,8 @@ Geom make_geom(const mrf_params& p) {
   g.lookup_n = p.lookup_n;
   g.n_tiles_u = (p.cols + kLookupPx - 1) / kLookupPx;
   g.n_tiles_v = (p.rows + kLookupPx - 1) / kLookupPx;
+  g.lut_rows = p.rows;
+  g.lut_cols = p.cols;
   return g;
 }
 
@@ -820,10 +836,12 @@ void destroy_bufs(mrf_map* m) {
   for (auto& v : m->views) v.depth.release();
 }
 
+// cam: the camera geometry (a view's, or the map's for an arbitrary pose)
 void likelihood_dev(mrf_map* m, const Pose& P, const float* depth_clean, float* img_dev,
-                    float* sum_dev) {
-  m->g.brick_slot = m->d_slot.as<int>();
-  int nb = likelihood_blocks(m->g);
+                    float* sum_dev, const Geom* cam = nullptr) {
+  Geom g = cam ? *cam : m->g;
+  g.brick_slot = m->d_slot.as<int>();
+  int nb = likelihood_blocks(g);
   m->s_part.reserve((size_t)nb * 8, false, m->stream);
   const float* bel = m->d_belief.as<float>();
   if (m->n_bricks == 0) {
@@ -831,7 +849,7 @@ void likelihood_dev(mrf_map* m, const Pose& P, const float* depth_clean, float* 
     m->s_dense.reserve(4, false, m->stream);
     bel = m->s_dense.as<float>();
   }
-  CK(launch_likelihood(m->g, P, depth_clean, bel, img_dev, m->s_part.as<double>(), nb, m->stream));
+  CK(launch_likelihood(g, P, depth_clean, bel, img_dev, m->s_part.as<double>(), nb, m->stream));
   CK(launch_reduce_partials(m->s_part.as<double>(), nb, sum_dev, m->stream));
 }
 
@@ -947,16 +965,30 @@ void mrf_destroy(mrf_map* m) {
 }
 
 static mrf_status add_view_impl(mrf_map* m, const float* pose, const float* depth, bool device,
-                                int* view_id) {
+                                int* view_id, const int* cam_size = nullptr, const float* cam_k = nullptr) {
   if (guard(m) != MRF_OK) return MRF_ERR_INVALID;
   if (!pose || !depth) {
     set_err("null pose or depth");
     return MRF_ERR_INVALID;
   }
+  if (cam_size && (cam_size[0] < 1 || cam_size[1] < 1 || (int64_t)cam_size[0] * cam_size[1] > (1 << 26) ||
+                   !(cam_k[0] > 0.0f) || !(cam_k[1] > 0.0f))) {
+    set_err("invalid camera");
+    return MRF_ERR_INVALID;
+  }
   return wrap([&] {
-    const int64_t HW = m->hw();
     View v;
     set_pose(v.pose, pose);
+    v.cam = m->g;
+    if (cam_size) {
+      v.cam.rows = cam_size[0];
+      v.cam.cols = cam_size[1];
+      v.cam.fx = cam_k[0];
+      v.cam.fy = cam_k[1];
+      v.cam.cx = cam_k[2];
+      v.cam.cy = cam_k[3];
+    }
+    const int64_t HW = (int64_t)v.cam.rows * v.cam.cols;
     v.depth.reserve((size_t)HW * 4, false, m->stream);
     const float* src = depth;
     if (!device) {
@@ -964,7 +996,7 @@ static mrf_status add_view_impl(mrf_map* m, const float* pose, const float* dept
       CK(cudaMemcpyAsync(m->s_depth_in.p, depth, (size_t)HW * 4, cudaMemcpyHostToDevice, m->stream));
       src = m->s_depth_in.as<float>();
     }
-    CK(launch_clean_depth(src, v.depth.as<float>(), m->prm.rows, m->prm.cols, m->stream));
+    CK(launch_clean_depth(src, v.depth.as<float>(), v.cam.rows, v.cam.cols, m->stream));
     activate_view(m, v);
     m->views.push_back(std::move(v));
     m->version++;  // the view set changed: incidence lists must be rebuilt
@@ -980,6 +1012,31 @@ mrf_status mrf_add_view(mrf_map* m, const float* pose, const float* depth_host, 
 
 mrf_status mrf_add_view_device(mrf_map* m, const float* pose, const float* depth_dev, int* view_id) {
   return add_view_impl(m, pose, depth_dev, true, view_id);
+}
+
+mrf_status mrf_add_view_camera(mrf_map* m, const float* pose, const float* depth_host, int rows, int cols,
+                               float fx, float fy, float cx, float cy, int* view_id) {
+  const int size[2] = {rows, cols};
+  const float k[4] = {fx, fy, cx, cy};
+  return add_view_impl(m, pose, depth_host, false, view_id, size, k);
+}
+
+mrf_status mrf_view_camera(mrf_map* m, int view_id, int* rows, int* cols, float* k4) {
+  if (guard(m) != MRF_OK) return MRF_ERR_INVALID;
+  if (view_id < 0 || view_id >= (int)m->views.size()) {
+    set_err("invalid view id");
+    return MRF_ERR_INVALID;
+  }
+  const Geom& c = m->views[view_id].cam;
+  if (rows) *rows = c.rows;
+  if (cols) *cols = c.cols;
+  if (k4) {
+    k4[0] = c.fx;
+    k4[1] = c.fy;
+    k4[2] = c.cx;
+    k4[3] = c.cy;
+  }
+  return MRF_OK;
 }
 
 mrf_status mrf_set_pose(mrf_map* m, int view_id, const float* pose) {
@@ -1259,15 +1316,15 @@ mrf_status mrf_likelihood_device(mrf_map* m, const float* pose, const float* dep
 }
 
 static mrf_status likelihood_host(mrf_map* m, const Pose& P, const float* depth_clean_dev,
-                                  float* out_img, float* out_sum) {
+                                  float* out_img, float* out_sum, const Geom* cam = nullptr) {
   return wrap([&] {
-    const int64_t HW = m->hw();
+    const int64_t HW = cam ? (int64_t)cam->rows * cam->cols : m->hw();
     float* img = nullptr;
     if (out_img) {
       m->s_img.reserve((size_t)HW * 4, false, m->stream);
       img = m->s_img.as<float>();
     }
-    likelihood_dev(m, P, depth_clean_dev, img, m->s_sum.as<float>());
+    likelihood_dev(m, P, depth_clean_dev, img, m->s_sum.as<float>(), cam);
     float sum = 0.0f;
     CK(cudaMemcpyAsync(&sum, m->s_sum.p, 4, cudaMemcpyDeviceToHost, m->stream));
     if (out_img) CK(cudaMemcpyAsync(out_img, img, (size_t)HW * 4, cudaMemcpyDeviceToHost, m->stream));
@@ -1304,29 +1361,31 @@ mrf_status mrf_likelihood_view(mrf_map* m, int view_id, float* out_img, float* o
     return MRF_ERR_INVALID;
   }
   const View& v = m->views[view_id];
-  return likelihood_host(m, v.pose, v.depth.as<float>(), out_img, out_sum);
+  return likelihood_host(m, v.pose, v.depth.as<float>(), out_img, out_sum, &v.cam);
 }
 
 static mrf_status render_impl(mrf_map* m, int mode, const Pose& P, const float* depth_clean_dev,
-                              float threshold, float* out_img, float* out_score, int64_t* counts) {
+                              float threshold, float* out_img, float* out_score, int64_t* counts,
+                              const Geom* cam = nullptr) {
   if (mode < 0 || mode > 3) {
     set_err("invalid render mode");
     return MRF_ERR_INVALID;
   }
   return wrap([&] {
-    const int64_t HW = m->hw();
+    Geom g = cam ? *cam : m->g;
+    const int64_t HW = (int64_t)g.rows * g.cols;
     if (threshold < 0.0f)
       threshold = mode == MRF_RENDER_SIMPLE_ACCURACY ? m->prm.acc_thresh : m->prm.occ_thresh;
     m->s_img.reserve((size_t)HW * 4, false, m->stream);
     m->s_part.reserve(64, false, m->stream);
     CK(cudaMemsetAsync(m->s_part.p, 0, 32, m->stream));
-    m->g.brick_slot = m->d_slot.as<int>();
+    g.brick_slot = m->d_slot.as<int>();
     const float* bel = m->d_belief.as<float>();
     if (m->n_bricks == 0) {
       m->s_dense.reserve(4, false, m->stream);
       bel = m->s_dense.as<float>();
     }
-    CK(launch_render(mode, m->g, P, depth_clean_dev, bel, threshold, m->s_img.as<float>(),
+    CK(launch_render(mode, g, P, depth_clean_dev, bel, threshold, m->s_img.as<float>(),
                      reinterpret_cast<unsigned long long*>(m->s_part.p), m->stream));
     unsigned long long h[4] = {0, 0, 0, 0};
     CK(cudaMemcpyAsync(h, m->s_part.p, 32, cudaMemcpyDeviceToHost, m->stream));
@@ -1378,7 +1437,30 @@ mrf_status mrf_render_view(mrf_map* m, int mode, int view_id, float threshold, f
     return MRF_ERR_INVALID;
   }
   const View& v = m->views[view_id];
-  return render_impl(m, mode, v.pose, v.depth.as<float>(), threshold, out_img, out_score, counts);
+  return render_impl(m, mode, v.pose, v.depth.as<float>(), threshold, out_img, out_score, counts, &v.cam);
+}
+
+mrf_status mrf_pixel_diagnostics(mrf_map* m, const float* pose, int x, int y, float* out, int64_t n_floats) {
+  if (guard(m) != MRF_OK) return MRF_ERR_INVALID;
+  if (!pose || !out || n_floats < 11 || x < 0 || y < 0 || x >= m->prm.cols || y >= m->prm.rows) {
+    set_err("invalid pixel diagnostics arguments");
+    return MRF_ERR_INVALID;
+  }
+  return wrap([&] {
+    Pose P;
+    set_pose(P, pose);
+    m->s_img.reserve((size_t)n_floats * 4, false, m->stream);
+    CK(cudaMemsetAsync(m->s_img.p, 0, (size_t)n_floats * 4, m->stream));
+    m->g.brick_slot = m->d_slot.as<int>();
+    const float* bel = m->d_belief.as<float>();
+    if (m->n_bricks == 0) {
+      m->s_dense.reserve(4, false, m->stream);
+      bel = m->s_dense.as<float>();
+    }
+    CK(launch_pixel_diag(m->g, P, bel, x, y, m->s_img.as<float>(), n_floats, m->stream));
+    CK(cudaMemcpyAsync(out, m->s_img.p, (size_t)n_floats * 4, cudaMemcpyDeviceToHost, m->stream));
+    sync(m);
+  });
 }
 
 mrf_status mrf_num_bricks(mrf_map* m, int64_t* n) {
@@ -1506,9 +1588,9 @@ mrf_status mrf_view_incidences(mrf_map* m, int view_id, int* meta, uint32_t* vox
   return wrap([&] {
     ensure_built(m);
     const View& v = m->views[view_id];
-    const int64_t HW = m->hw();
+    const int64_t HW = (int64_t)v.cam.rows * v.cam.cols;
     std::vector<RayMeta> hm((size_t)HW);
-    CK(cudaMemcpyAsync(hm.data(), m->meta.as<RayMeta>() + view_id * HW, (size_t)HW * sizeof(RayMeta),
+    CK(cudaMemcpyAsync(hm.data(), m->meta.as<RayMeta>() + v.pix_base, (size_t)HW * sizeof(RayMeta),
                        cudaMemcpyDeviceToHost, m->stream));
     sync(m);
     int64_t total = 0;

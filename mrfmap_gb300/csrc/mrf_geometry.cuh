@@ -27,9 +27,13 @@ __device__ __forceinline__ float poly_f(const float* c, int n, float z) {
 
 // per-20x20-tile coefficient rows; tiles indexed by the upward (GL) row as in
 // gvdbkernels.cu:47 (the reference flips the image on upload)
+// a camera of another resolution than the tables' maps its pixel into the
+// tables' image (identity for the map's own camera)
 __device__ __forceinline__ const float* lut_at(const Geom& g, const float* lut, int x, int y) {
   int ygl = g.rows - 1 - y;
-  return lut + ((ygl / kLookupPx) * g.n_tiles_u + (x / kLookupPx)) * g.lookup_n;
+  int xs = (int)(((int64_t)x * g.lut_cols) / g.cols);
+  int ys = (int)(((int64_t)ygl * g.lut_rows) / g.rows);
+  return lut + ((ys / kLookupPx) * g.n_tiles_u + (xs / kLookupPx)) * g.lookup_n;
 }
 
 // exact-zero test of the fp32 depth potential (gvdbkernels.cu:57-72; the

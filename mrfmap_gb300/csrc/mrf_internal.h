@@ -30,6 +30,7 @@ struct Geom {
   int NB[3];         // brick grid
   int E[3];          // 8*NB, voxel box of the traversal
   int lookup_n, n_tiles_u, n_tiles_v;
+  int lut_rows, lut_cols;  // image size the sensor tables are tiled for
   const float* sigma;   // device
   const float* bias;    // device
   const int* brick_slot;  // device, NB0*NB1*NB2
@@ -212,6 +213,10 @@ cudaError_t launch_likelihood(const Geom& g, const Pose& P, const float* depth, 
 int likelihood_blocks(const Geom& g);
 cudaError_t launch_reduce_partials(const double* partials, int n, float* out_sum, cudaStream_t s);
 
+// per-voxel records of one pixel's ray (debug probe; out zeroed by the caller,
+// 8-byte aligned, n_floats >= 11)
+cudaError_t launch_pixel_diag(const Geom& g, const Pose& P, const float* belief, int x, int y, float* out,
+                              int64_t n_floats, cudaStream_t s);
 // evaluation renders (mode 0-3, see mrf_render.cu); counts: 4 zeroed u64
 cudaError_t launch_render(int mode, const Geom& g, const Pose& P, const float* depth,
                           const float* belief, float thresh, float* out, unsigned long long* counts,

@@ -111,7 +111,65 @@ __global__ void __launch_bounds__(kRenderThreads)
     atomicAdd(&counts[threadIdx.x], (unsigned long long)hist[threadIdx.x]);
 }
 
+// Per-voxel record of one pixel's ray (src/cuda/gvdbkernels.cu:573-672,
+// 1365-1384): ten floats per active voxel along the ray to the volume exit
+// -- [0] exit distance s, [1] belief, [2..3] voxel id (u64: slot*512 +
+// local), [4] w = (V_prev - V) / l, [5] visibility V, [6..7] brick slot
+// (u64), [8] brick-local x, y, z as bytes -- and the record count in the
+// last float.  One thread: this is a debugging probe.
+__global__ void k_pixel_diag(Geom g, Pose P, const float* __restrict__ belief, int x, int y,
+                             float* __restrict__ out, int64_t n_floats) {
+  if (blockIdx.x || threadIdx.x) return;
+  constexpr int kStride = 10;
+  const int64_t cap = (n_floats - 1) / kStride;
+  Ray ray;
+  ray_setup(g, P, x, y, ray);
+  int64_t count = 0;
+  float A = 0.0f, Vprev = 1.0f;
+  Dda r;
+  if (dda_init(r, g, ray)) {
+    int64_t cur = -1;
+    int slot = -1;
+    int vx, vy, vz;
+    float l, tin, te;
+    while (dda_next(r, g, vx, vy, vz, l, tin, te)) {
+      int64_t lin = brick_lin(g, vx, vy, vz);
+      if (lin != cur) {
+        cur = lin;
+        slot = g.brick_slot[lin];
+      }
+      if (slot < 0) continue;
+      if (count >= cap) break;
+      const int loc = voxel_local(vx, vy, vz);
+      const float p = belief[(int64_t)slot * kBrickVox + loc];
+      A += log1pf(-p) * l;
+      const float V = expf(A);
+      float* rec = out + count * kStride;
+      rec[0] = fm(te, ray.mult);
+      rec[1] = p;
+      reinterpret_cast<unsigned long long*>(out)[count * (kStride / 2) + 1] =
+          (unsigned long long)slot * kBrickVox + loc;
+      rec[4] = (Vprev - V) / l;
+      rec[5] = V;
+      reinterpret_cast<unsigned long long*>(out)[count * (kStride / 2) + 3] = (unsigned long long)slot;
+      unsigned char* b = reinterpret_cast<unsigned char*>(rec + 8);
+      b[0] = (unsigned char)(vx & 7);
+      b[1] = (unsigned char)(vy & 7);
+      b[2] = (unsigned char)(vz & 7);
+      Vprev = V;
+      ++count;
+    }
+  }
+  out[n_floats - 1] = (float)count;
+}
+
 }  // namespace
+
+cudaError_t launch_pixel_diag(const Geom& g, const Pose& P, const float* belief, int x, int y, float* out,
+                              int64_t n_floats, cudaStream_t s) {
+  k_pixel_diag<<<1, 1, 0, s>>>(g, P, belief, x, y, out, n_floats);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_render(int mode, const Geom& g, const Pose& P, const float* depth,
                           const float* belief, float thresh, float* out, unsigned long long* counts,

@@ -14,6 +14,7 @@
 #include "mrfmap/GVDBImage.h"
 #include "mrfmap/GVDBInference.h"
 #include "mrfmap/GVDBMapLikelihoodEstimator.h"
+#include "mrfmap/KeyframeSelector.h"
 #include "mrfmap/GVDBParams.h"
 
 namespace py = pybind11;
@@ -112,6 +113,23 @@ PYBIND11_MODULE(GVDBPyModules, m) {
         return s.get_likelihood_image(id, out_buffer(out, gvdb_params_.rows, gvdb_params_.cols, "image"));
       })
       .def("compute_likelihood", &GVDBInference::compute_likelihood)
+      .def("get_diagnostic_image",
+           [](GVDBInference& s, unsigned id, py::array out, unsigned mode) {
+             s.get_diagnostic_image(id, out_buffer(out, gvdb_params_.rows, gvdb_params_.cols, "image"), mode);
+           },
+           py::arg("id"), py::arg("img"), py::arg("mode") = 0)
+      .def("get_diagnostic_image_at_pose",
+           [](GVDBInference& s, farr pose, std::shared_ptr<GVDBImage> img, py::array out) {
+             s.get_diagnostic_image_at_pose(pose16(pose).data(), img,
+                                            out_buffer(out, gvdb_params_.rows, gvdb_params_.cols, "image"));
+           })
+      .def("get_voxel_coords",
+           [](GVDBInference& s, std::vector<uint64_t> idx) {
+             std::vector<float> c = s.get_voxel_coords(idx);
+             py::array_t<float> a({(py::ssize_t)idx.size(), (py::ssize_t)6});
+             std::copy(c.begin(), c.end(), a.mutable_data());
+             return a;
+           })
       .def("set_selected_x_y", &GVDBInference::set_selected_x_y)
       .def("set_selected_voxel", &GVDBInference::set_selected_voxel)
       .def("set_owned_context", [](GVDBInference&) {})
@@ -210,6 +228,14 @@ PYBIND11_MODULE(GVDBPyModules, m) {
              s.get_occ_thresh_image_at_pose(pose16(pose).data(), img,
                                             out_buffer(out, s.params_.rows, s.params_.cols, "image"), occ_thresh);
            })
+      .def("get_diagnostic_image", [](GVDBMapLikelihoodEstimator& s, unsigned id, py::array out) {
+        s.get_diagnostic_image(id, out_buffer(out, s.params_.rows, s.params_.cols, "image"));
+      })
+      .def("get_diagnostic_image_at_pose",
+           [](GVDBMapLikelihoodEstimator& s, farr pose, std::shared_ptr<GVDBImage> img, py::array out) {
+             s.get_diagnostic_image_at_pose(pose16(pose).data(), img,
+                                            out_buffer(out, s.params_.rows, s.params_.cols, "image"));
+           })
       .def("set_selected_x_y", &GVDBMapLikelihoodEstimator::set_selected_x_y)
       .def("set_acc_thresh", &GVDBMapLikelihoodEstimator::set_acc_thresh)
       .def("get_occupied_bricks",
@@ -217,4 +243,25 @@ PYBIND11_MODULE(GVDBPyModules, m) {
       .def("get_indices_and_alphas", [](GVDBMapLikelihoodEstimator& s, py::array out) {
         s.get_alphas(out_buffer(out, out.ndim() == 2 ? out.shape(0) : -1, 512, "alphas"), out.shape(0), 512);
       });
+
+  // src/GVDBPyModules.cpp:130-133.  compute_distance takes (rot, trans,
+  // first, second) like the reference; Python cannot see the two outputs
+  // through float references, so it returns rot + trans, as the reference
+  // binding does.
+  py::class_<KeyframeSelector>(m, "KeyframeSelector")
+      .def(py::init<float, float>(), py::arg("rotation_thresh") = 0.1f, py::arg("translation_thresh") = 0.1f)
+      .def("set_thresh", &KeyframeSelector::set_thresh)
+      .def("is_keyframe", [](KeyframeSelector& s, farr pose) { return s.is_keyframe(pose16(pose).data()); })
+      .def("compute_distance",
+           [](const KeyframeSelector& s, float, float, farr a, farr b) {
+             float r = 0.0f, t = 0.0f;
+             return s.compute_distance(r, t, pose16(a).data(), pose16(b).data());
+           })
+      .def("compute_rot_trans",
+           [](const KeyframeSelector& s, farr a, farr b) {
+             float r = 0.0f, t = 0.0f;
+             s.compute_distance(r, t, pose16(a).data(), pose16(b).data());
+             return py::make_tuple(r, t);
+           })
+      .def("num_keyframes", &KeyframeSelector::num_keyframes);
 }

@@ -288,6 +288,38 @@ float GVDBInference::get_accuracy_image_at_pose(const float* pose, const std::sh
   return s;
 }
 
+void GVDBInference::get_diagnostic_image(unsigned id, float* out, unsigned mode) {
+  const int64_t n = (int64_t)gvdb_params_.rows * gvdb_params_.cols;
+  if (mode != 0) {  // the factor-debug mode records nothing under FULL_INFERENCE
+    std::fill(out, out + n, 0.0f);
+    return;
+  }
+  mrf_check(mrf_pixel_diagnostics(map_->handle(), poses_.at(id).data(), (int)sel_x_, (int)sel_y_, out, n));
+}
+
+void GVDBInference::get_diagnostic_image_at_pose(const float* pose, const std::shared_ptr<GVDBImage>&,
+                                                 float* out) {
+  const int64_t n = (int64_t)gvdb_params_.rows * gvdb_params_.cols;
+  mrf_check(mrf_pixel_diagnostics(map_->handle(), pose, (int)sel_x_, (int)sel_y_, out, n));
+}
+
+std::vector<float> GVDBInference::get_voxel_coords(const std::vector<uint64_t>& indices) const {
+  // brick slots -> world-frame (voxel units) min and max corners; unknown
+  // slots give zeros, as the reference leaves rows of missing nodes at 0
+  const int64_t n = map_->num_bricks();
+  std::vector<float> c((size_t)n * 3);
+  if (n) mrf_check(mrf_read_bricks(map_->handle(), c.data(), nullptr, n));
+  std::vector<float> out(indices.size() * 6, 0.0f);
+  for (size_t k = 0; k < indices.size(); ++k) {
+    if (indices[k] >= (uint64_t)n) continue;
+    for (int a = 0; a < 3; ++a) {
+      out[k * 6 + a] = c[indices[k] * 3 + a] - 4.0f;
+      out[k * 6 + 3 + a] = c[indices[k] * 3 + a] + 4.0f;
+    }
+  }
+  return out;
+}
+
 mrf_stats GVDBInference::stats() const {
   mrf_stats s{};
   mrf_check(mrf_stats_get(map_->handle(), &s));
@@ -372,4 +404,14 @@ void GVDBMapLikelihoodEstimator::get_occ_thresh_image_at_pose(const float* pose,
                                                               float* out, float occ_thresh) {
   mrf_check(mrf_render(map_->handle(), MRF_RENDER_OCC_THRESH, pose, img->depth().data(), occ_thresh, out,
                        nullptr, nullptr));
+}
+
+void GVDBMapLikelihoodEstimator::get_diagnostic_image(unsigned id, float* out) {
+  get_diagnostic_image_at_pose(poses_.at(id).data(), images_.at(id), out);
+}
+
+void GVDBMapLikelihoodEstimator::get_diagnostic_image_at_pose(const float* pose,
+                                                              const std::shared_ptr<GVDBImage>&, float* out) {
+  const int64_t n = (int64_t)params_.rows * params_.cols;
+  mrf_check(mrf_pixel_diagnostics(map_->handle(), pose, (int)sel_x_, (int)sel_y_, out, n));
 }

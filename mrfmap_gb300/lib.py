@@ -39,7 +39,8 @@ EXPORTS = ["mrf_create", "mrf_destroy", "mrf_last_error", "mrf_add_view", "mrf_a
            "mrf_likelihood_device", "mrf_likelihood_device_noalloc", "mrf_num_bricks", "mrf_read_bricks", "mrf_read_logodds",
            "mrf_num_nodes", "mrf_read_nodes", "mrf_load_map", "mrf_view_incidences",
            "mrf_device_beliefs",
-           "mrf_stats_get", "mrf_get_stream", "mrf_synchronize", "mrf_render", "mrf_render_view"]
+           "mrf_stats_get", "mrf_get_stream", "mrf_synchronize", "mrf_render", "mrf_render_view", "mrf_pixel_diagnostics", "mrf_add_view_camera",
+           "mrf_view_camera"]
 
 RENDER_EXPECTED_DEPTH = 0
 RENDER_ACCURACY = 1
@@ -130,6 +131,10 @@ def load(path: str | None = None):
         "mrf_synchronize": ([vp], C.c_int),
         "mrf_render": ([vp, C.c_int, fp, fp, C.c_float, fp, fp, i64p], C.c_int),
         "mrf_render_view": ([vp, C.c_int, C.c_int, C.c_float, fp, fp, i64p], C.c_int),
+        "mrf_pixel_diagnostics": ([vp, fp, C.c_int, C.c_int, fp, C.c_int64], C.c_int),
+        "mrf_add_view_camera": ([vp, fp, fp, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float,
+                                 ip], C.c_int),
+        "mrf_view_camera": ([vp, C.c_int, ip, ip, fp], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -206,6 +211,23 @@ class MRFMap:
             raise ValueError("depth image shape does not match params rows x cols")
         _check(self._L.mrf_add_view(self._h, _fp(_f32(pose)), _fp(d), C.byref(vid)))
         return vid.value
+
+    def add_view_camera(self, pose, depth, fx: float, fy: float, cx: float, cy: float) -> int:
+        """A view with its own camera; the depth image's shape is its size."""
+        vid = C.c_int()
+        d = _f32(depth)
+        if d.ndim != 2:
+            raise ValueError("depth image must be 2-D")
+        _check(self._L.mrf_add_view_camera(self._h, _fp(_f32(pose)), _fp(d), d.shape[0], d.shape[1], fx, fy,
+                                           cx, cy, C.byref(vid)))
+        return vid.value
+
+    def view_camera(self, view: int):
+        """(rows, cols, (fx, fy, cx, cy)) of a view."""
+        r, c = C.c_int(), C.c_int()
+        k = np.zeros(4, np.float32)
+        _check(self._L.mrf_view_camera(self._h, view, C.byref(r), C.byref(c), _fp(k)))
+        return r.value, c.value, tuple(float(x) for x in k)
 
     def add_view_device(self, pose, depth_dev_ptr: int) -> int:
         vid = C.c_int()
@@ -327,7 +349,8 @@ class MRFMap:
         return s.value, img
 
     def likelihood_view(self, view: int, image: bool = True):
-        img = np.zeros((self.params.rows, self.params.cols), np.float32) if image else None
+        rows, cols, _ = self.view_camera(view)
+        img = np.zeros((rows, cols), np.float32) if image else None
         s = C.c_float()
         _check(self._L.mrf_likelihood_view(self._h, view, _fp(img) if image else None, C.byref(s)))
         return s.value, img
@@ -347,12 +370,27 @@ class MRFMap:
         return img, s.value, cnt
 
     def render_view(self, mode: int, view: int, threshold: float = -1.0):
-        img = np.zeros((self.params.rows, self.params.cols), np.float32)
+        rows, cols, _ = self.view_camera(view)
+        img = np.zeros((rows, cols), np.float32)
         s = C.c_float()
         cnt = np.zeros(4, np.int64)
         _check(self._L.mrf_render_view(self._h, mode, view, threshold, _fp(img), C.byref(s),
                                        cnt.ctypes.data_as(C.POINTER(C.c_int64))))
         return img, s.value, cnt
+
+    def pixel_diagnostics(self, pose, x: int, y: int, n_floats: int | None = None):
+        """Per-voxel records of pixel (x, y)'s ray at a pose (the layout of
+        mrf_pixel_diagnostics), parsed: dict of arrays s, belief, vox, w, vis,
+        slot, local (n x 3)."""
+        n_floats = n_floats or self.params.rows * self.params.cols
+        buf = np.zeros(n_floats + (n_floats & 1), np.float32)  # 8-byte records need an even count
+        _check(self._L.mrf_pixel_diagnostics(self._h, _fp(_f32(pose)), x, y, _fp(buf), n_floats))
+        cnt = int(buf[n_floats - 1])
+        rec = buf[:cnt * 10].reshape(cnt, 10)
+        u64 = buf[:cnt * 10].view(np.uint64).reshape(cnt, 5)
+        loc = rec[:, 8].copy().view(np.uint8).reshape(cnt, 4)[:, :3]
+        return dict(s=rec[:, 0].copy(), belief=rec[:, 1].copy(), vox=u64[:, 1].copy(), w=rec[:, 4].copy(),
+                    vis=rec[:, 5].copy(), slot=u64[:, 3].copy(), local=loc.astype(np.int32))
 
     def load_map(self, points, occupancies):
         pts = _f32(points).reshape(-1, 3)
@@ -364,8 +402,8 @@ class MRFMap:
     def view_incidences(self, view: int):
         """Per-pixel meta (rows*cols, 5) and the view's incidences in ray order."""
         n = C.c_int64()
-        hw = self.params.rows * self.params.cols
-        meta = np.zeros((hw, 5), np.int32)
+        rows, cols, _ = self.view_camera(view)
+        meta = np.zeros((rows * cols, 5), np.int32)
         _check(self._L.mrf_view_incidences(self._h, view, meta.ctypes.data_as(C.POINTER(C.c_int)),
                                            None, None, None, 0, C.byref(n)))
         k = n.value

@@ -126,6 +126,8 @@ class Workload:
     poses: list
     depths: list
     seed: int
+    cams: list | None = None  # per view (fx, fy, cx, cy) when views differ in camera
+    scene: Scene | None = None
 
 
 def small_room(seed: int = 0, n_frames: int = 5, rows: int = 120, cols: int = 160) -> Workload:
@@ -180,4 +182,31 @@ def full_room(seed: int = 1, n_frames: int = 13, rows: int = 480, cols: int = 64
         P = look_at(e, target, np.deg2rad(rng.uniform(-5, 5)))
         poses.append(P)
         depths.append(add_noise(render_depth(scene, p, P), rng, max_range=5.0))
-    return Workload(f"full_room_{n_frames}x{cols}x{rows}_{int(round(res * 100))}cm", p, poses, depths, seed)
+    return Workload(f"full_room_{n_frames}x{cols}x{rows}_{int(round(res * 100))}cm", p, poses, depths, seed,
+                    scene=scene)
+
+
+def mixed_room(seed: int = 2, n_frames: int = 12,
+               sizes=((120, 160), (240, 320), (480, 640)), res: float = 0.02) -> Workload:
+    """The full room's scene seen by views of mixed resolution (the sizes
+    cycle over the frames; f = 525 cols / 640, principal point at the
+    centre), 2 cm voxels: uneven image sizes and ray lengths in one map.
+    ``params`` is the largest camera (the sensor tables' image)."""
+    base = full_room(seed, n_frames=n_frames, rows=24, cols=32, res=res)  # scene and poses
+    rows0, cols0 = sizes[-1]
+    f0 = 525.0 * cols0 / 640
+    base.params = sensor_params(MapParams(res=res, dims=base.params.dims, rows=rows0, cols=cols0, fx=f0, fy=f0,
+                                          cx=cols0 / 2, cy=rows0 / 2, prior=0.1, max_iters=20))
+    rng = np.random.default_rng(seed + 1000)
+    scene = base.scene
+    poses, depths, cams = [], [], []
+    for k, P in enumerate(base.poses):
+        rows, cols = sizes[k % len(sizes)]
+        f = 525.0 * cols / 640
+        cp = MapParams(res=res, dims=base.params.dims, rows=rows, cols=cols, fx=f, fy=f, cx=cols / 2,
+                       cy=rows / 2, prior=0.1, max_iters=20)
+        poses.append(P)
+        depths.append(add_noise(render_depth(scene, cp, P), rng, max_range=5.0))
+        cams.append((f, f, cols / 2, rows / 2))
+    return Workload(f"mixed_room_{n_frames}x{len(sizes)}res_{int(round(res * 100))}cm", base.params, poses,
+                    depths, seed, cams)

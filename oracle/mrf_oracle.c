@@ -47,6 +47,12 @@
 #define MU_CUTOFF_F 87.0f
 #define CUMLEN_GATE_F 0.1f
 
+/* a pinhole camera of one view (the map's own camera comes from params) */
+typedef struct {
+  int rows, cols;
+  float fx, fy, cx, cy;
+} orc_cam;
+
 typedef struct {
   float pose[16];
   float* depth;
@@ -63,6 +69,7 @@ typedef struct {
   float* s;
   unsigned char* run;
   double* mu;
+  orc_cam cam; /* the view's camera */
   /* per-voxel state over the pool */
   double* m;
   float* cum_len;
@@ -73,6 +80,7 @@ typedef struct {
 
 struct orc_map {
   orc_params p;
+  orc_cam cam; /* the map's camera (params) */
   float* sigma_lut;
   float* bias_lut;
   int G[3], NB[3];
@@ -103,11 +111,14 @@ static void* xrealloc(void* p, size_t n) {
 }
 
 /* ---- sensor model (src/cuda/gvdbkernels.cu:46-55) ---------------------- */
-static const float* lut_at(const orc_map* m, const float* lut, int x, int y) {
+static const float* lut_at(const orc_map* m, const orc_cam* cam, const float* lut, int x, int y) {
   /* tile row indexed by the GL row (image flipped on upload,
-   * src/GVDBImage.cpp:33 and gvdbkernels.cu:47) */
-  int ygl = m->p.rows - 1 - y;
-  int tu = x / LOOKUP_PX, tv = ygl / LOOKUP_PX;
+   * src/GVDBImage.cpp:33 and gvdbkernels.cu:47); a camera of another
+   * resolution than the tables' maps its pixel into the tables' grid */
+  int ygl = cam->rows - 1 - y;
+  int xs = (int)(((int64_t)x * m->p.cols) / cam->cols);
+  int ys = (int)(((int64_t)ygl * m->p.rows) / cam->rows);
+  int tu = xs / LOOKUP_PX, tv = ys / LOOKUP_PX;
   return lut + ((size_t)tv * m->p.n_tiles_u + tu) * m->p.lookup_n;
 }
 static float poly_f(const float* c, int n, float z) {
@@ -149,6 +160,12 @@ orc_map* orc_create(const orc_params* p) {
   memcpy(m->bias_lut, p->bias_lut, nl * sizeof(float));
   m->p.sigma_lut = m->sigma_lut;
   m->p.bias_lut = m->bias_lut;
+  m->cam.rows = p->rows;
+  m->cam.cols = p->cols;
+  m->cam.fx = p->fx;
+  m->cam.fy = p->fy;
+  m->cam.cx = p->cx;
+  m->cam.cy = p->cy;
   m->inv_res = 1.0f / p->res;
   for (int a = 0; a < 3; ++a) {
     float g = p->dims[a] / p->res;
@@ -218,13 +235,13 @@ static void grow_pool(orc_map* m, int new_nbricks) {
 }
 
 /* ---- ray set-up (src/GVDBCamera.cpp:7-32; gvdbkernels.cu:1178-1179) ------ */
-static void ray_setup(const orc_map* m, const float* pose, int x, int y, float o[3],
+static void ray_setup(const orc_map* m, const orc_cam* cam, const float* pose, int x, int y, float o[3],
                       float d[3], float* mult) {
-  float W = (float)m->p.cols, H = (float)m->p.rows;
+  float W = (float)cam->cols, H = (float)cam->rows;
   float ndcx = 2.0f * (((float)x + 0.5f) / W) - 1.0f;
   float ndcy = 2.0f * (((float)y + 0.5f) / H) - 1.0f;
-  float rx = ndcx * (m->p.cx / m->p.fx);
-  float ry = ndcy * (m->p.cy / m->p.fy);
+  float rx = ndcx * (cam->cx / cam->fx);
+  float ry = ndcy * (cam->cy / cam->fy);
   float dw[3];
   for (int a = 0; a < 3; ++a) {
     float u = pose[a * 4 + 0] * rx;
@@ -327,8 +344,8 @@ static int vox_id(const orc_map* m, const int v[3], int64_t* lin_out) {
 }
 
 /* ---- image clean-up (src/GVDBImage.cpp:32-40) ---------------------------- */
-static void clean_depth(const orc_map* m, const float* in, float* out) {
-  int H = m->p.rows, W = m->p.cols;
+static void clean_depth(const orc_cam* cam, const float* in, float* out) {
+  int H = cam->rows, W = cam->cols;
   for (int i = 0; i < H * W; ++i) out[i] = isfinite(in[i]) ? in[i] : -1.0f;
   if (H == 480 && W == 848) {
     for (int y = 0; y < H; ++y)
@@ -354,8 +371,9 @@ static void mark_point_bricks(const orc_map* m, const float pv[3], unsigned char
       for (int bz = lo[2]; bz <= hi[2]; ++bz) flag[blin(m, bx, by, bz)] = 1;
 }
 
-static void activate_view(orc_map* m, const float* pose, const float* depth, int policy) {
-  int H = m->p.rows, W = m->p.cols;
+static void activate_view(orc_map* m, const orc_cam* cam, const float* pose, const float* depth,
+                          int policy) {
+  int H = cam->rows, W = cam->cols;
   size_t nb = (size_t)m->NB[0] * m->NB[1] * m->NB[2];
   unsigned char* flag = (unsigned char*)calloc(nb, 1);
   for (int y = 0; y < H; ++y) {
@@ -364,9 +382,9 @@ static void activate_view(orc_map* m, const float* pose, const float* depth, int
       if (!(d > 0.0f)) continue;
       /* back-projection uses fx for both axes and integer pixel coords
        * (src/GVDBImage.cpp:48-56) */
-      float f = d / m->p.fx;
-      float X = f * ((float)x - m->p.cx);
-      float Y = f * ((float)y - m->p.cy);
+      float f = d / cam->fx;
+      float X = f * ((float)x - cam->cx);
+      float Y = f * ((float)y - cam->cy);
       float Z = d;
       float pv[3];
       int inside = 1;
@@ -381,8 +399,8 @@ static void activate_view(orc_map* m, const float* pose, const float* depth, int
       if (inside) mark_point_bricks(m, pv, flag);
       if (policy == ORC_ACT_FULL_RAY) {
         float o[3], dr[3], mult;
-        ray_setup(m, pose, x, y, o, dr, &mult);
-        float lim = d + 3.0f * poly_f(lut_at(m, m->sigma_lut, x, y), m->p.lookup_n, d);
+        ray_setup(m, cam, pose, x, y, o, dr, &mult);
+        float lim = d + 3.0f * poly_f(lut_at(m, cam, m->sigma_lut, x, y), m->p.lookup_n, d);
         dda_t r;
         if (dda_init(&r, m, o, dr)) {
           int v[3];
@@ -420,7 +438,8 @@ static void activate_view(orc_map* m, const float* pose, const float* depth, int
   free(flag);
 }
 
-int orc_add_view(orc_map* m, const float* pose, const float* depth, int policy) {
+int orc_add_view_camera(orc_map* m, const float* pose, const float* depth, int policy, int rows, int cols,
+                        float fx, float fy, float cx, float cy) {
   if (m->nviews == m->cap_views) {
     m->cap_views = m->cap_views ? 2 * m->cap_views : 8;
     m->views = (orc_view*)xrealloc(m->views, (size_t)m->cap_views * sizeof(orc_view));
@@ -428,8 +447,14 @@ int orc_add_view(orc_map* m, const float* pose, const float* depth, int policy) 
   orc_view* v = &m->views[m->nviews];
   memset(v, 0, sizeof(*v));
   memcpy(v->pose, pose, sizeof(v->pose));
-  v->depth = (float*)malloc((size_t)m->p.rows * m->p.cols * sizeof(float));
-  clean_depth(m, depth, v->depth);
+  v->cam.rows = rows;
+  v->cam.cols = cols;
+  v->cam.fx = fx;
+  v->cam.fy = fy;
+  v->cam.cx = cx;
+  v->cam.cy = cy;
+  v->depth = (float*)malloc((size_t)rows * cols * sizeof(float));
+  clean_depth(&v->cam, depth, v->depth);
   v->policy = policy;
   v->built_version = -1;
   int64_t nv = (int64_t)m->nbricks * BVOX;
@@ -437,8 +462,18 @@ int orc_add_view(orc_map* m, const float* pose, const float* depth, int policy) 
   v->cum_len = (float*)calloc((size_t)(nv ? nv : 1), sizeof(float));
   v->nvox_alloc = nv;
   m->nviews++;
-  activate_view(m, v->pose, v->depth, policy);
+  activate_view(m, &v->cam, v->pose, v->depth, policy);
   return m->nviews - 1;
+}
+
+int orc_add_view(orc_map* m, const float* pose, const float* depth, int policy) {
+  return orc_add_view_camera(m, pose, depth, policy, m->cam.rows, m->cam.cols, m->cam.fx, m->cam.fy,
+                             m->cam.cx, m->cam.cy);
+}
+
+int orc_view_pixels(const orc_map* m, int view) {
+  if (view < 0 || view >= m->nviews) return 0;
+  return m->views[view].cam.rows * m->views[view].cam.cols;
 }
 
 static double belief_of(double L);
@@ -458,7 +493,7 @@ int orc_set_pose(orc_map* m, int view, const float* pose, int policy) {
   }
   memcpy(m->views[view].pose, pose, 16 * sizeof(float));
   m->views[view].built_version = -1;
-  activate_view(m, m->views[view].pose, m->views[view].depth, policy);
+  activate_view(m, &m->views[view].cam, m->views[view].pose, m->views[view].depth, policy);
   return 0;
 }
 
@@ -483,11 +518,11 @@ static void push_inc(orc_view* v, int vox, float len, float s, unsigned char run
  * :1035 / :568 (Post and cumulative length, '>=') are evaluated at the exit
  * depth of the run's last voxel. */
 static void build_ray(orc_map* m, orc_view* v, int x, int y, float d, int* meta) {
-  const float* sg = lut_at(m, m->sigma_lut, x, y);
-  const float* bs = lut_at(m, m->bias_lut, x, y);
+  const float* sg = lut_at(m, &v->cam, m->sigma_lut, x, y);
+  const float* bs = lut_at(m, &v->cam, m->bias_lut, x, y);
   int n = m->p.lookup_n;
   float o[3], dr[3], mult;
-  ray_setup(m, v->pose, x, y, o, dr, &mult);
+  ray_setup(m, &v->cam, v->pose, x, y, o, dr, &mult);
   int64_t start = v->ninc;
   int count = 0, n_post = -1, n_pre = -1;
   int run_open = 0;
@@ -555,7 +590,7 @@ static void build_ray(orc_map* m, orc_view* v, int x, int y, float d, int* meta)
 
 static void build_view(orc_map* m, int c) {
   orc_view* v = &m->views[c];
-  int H = m->p.rows, W = m->p.cols;
+  int H = v->cam.rows, W = v->cam.cols;
   free(v->ray_pix); free(v->ray_off); free(v->meta); free(v->mu); free(v->touch);
   v->ray_pix = (int*)malloc((size_t)H * W * sizeof(int));
   v->ray_off = (int64_t*)malloc((size_t)H * W * sizeof(int64_t));
@@ -588,8 +623,8 @@ static void build_view(orc_map* m, int c) {
   for (int r = 0; r < v->nrays; ++r) {
     int pix = v->ray_pix[r];
     int x = pix % W, y = pix / W;
-    const float* sg = lut_at(m, m->sigma_lut, x, y);
-    const float* bs = lut_at(m, m->bias_lut, x, y);
+    const float* sg = lut_at(m, &v->cam, m->sigma_lut, x, y);
+    const float* bs = lut_at(m, &v->cam, m->bias_lut, x, y);
     float d = v->depth[pix];
     const int* me = &v->meta[r * 5];
     for (int i = 0; i < me[0]; ++i) {
@@ -815,7 +850,7 @@ void orc_set_beliefs(orc_map* m, const float* in) {
 int orc_trace_pixel(const orc_map* m, const float* pose, int x, int y, int* vox, float* len,
                     float* s, int max) {
   float o[3], dr[3], mult;
-  ray_setup(m, pose, x, y, o, dr, &mult);
+  ray_setup(m, &m->cam, pose, x, y, o, dr, &mult);
   dda_t r;
   int n = 0;
   if (!dda_init(&r, m, o, dr)) return 0;
@@ -837,12 +872,12 @@ int orc_trace_pixel(const orc_map* m, const float* pose, int x, int y, int* vox,
 
 /* ---- likelihood (gvdbkernels.cu:183-293, 1246-1274) ---------------------- */
 static double like_pixel(const orc_map* m, const float* pose, int x, int y, float d) {
-  const float* sg = lut_at(m, m->sigma_lut, x, y);
-  const float* bs = lut_at(m, m->bias_lut, x, y);
+  const float* sg = lut_at(m, &m->cam, m->sigma_lut, x, y);
+  const float* bs = lut_at(m, &m->cam, m->bias_lut, x, y);
   int n = m->p.lookup_n;
   const double LE = (double)LIKE_EPS_F;
   float o[3], dr[3], mult;
-  ray_setup(m, pose, x, y, o, dr, &mult);
+  ray_setup(m, &m->cam, pose, x, y, o, dr, &mult);
   double A = 0.0, Vprev = 1.0, sum = 0.0, prev_s = 0.0;
   int first_run = 1, run_open = 0;
   int64_t cur_lin = -1;
@@ -901,7 +936,7 @@ static double like_pixel(const orc_map* m, const float* pose, int x, int y, floa
 double orc_likelihood(const orc_map* m, const float* pose, const float* depth, float* out_img) {
   int H = m->p.rows, W = m->p.cols;
   float* dep = (float*)malloc((size_t)H * W * sizeof(float));
-  clean_depth(m, depth, dep);
+  clean_depth(&m->cam, depth, dep);
   double total = 0.0;
 #pragma omp parallel for schedule(dynamic, 16) reduction(+ : total) num_threads(g_threads)
   for (int y = 0; y < H; ++y) {
@@ -922,11 +957,11 @@ double orc_likelihood(const orc_map* m, const float* pose, const float* depth, f
  * extra state the reference's evaluation kernels keep in hit/norm/clr. */
 static float render_pixel(const orc_map* m, int mode, const float* pose, int x, int y, float d,
                           float thresh) {
-  const float* sg = lut_at(m, m->sigma_lut, x, y);
-  const float* bs = lut_at(m, m->bias_lut, x, y);
+  const float* sg = lut_at(m, &m->cam, m->sigma_lut, x, y);
+  const float* bs = lut_at(m, &m->cam, m->bias_lut, x, y);
   int n = m->p.lookup_n;
   float o[3], dr[3], mult;
-  ray_setup(m, pose, x, y, o, dr, &mult);
+  ray_setup(m, &m->cam, pose, x, y, o, dr, &mult);
   double A = 0.0, Vprev = 1.0, sum = 0.0;
   double peak = 0.0;   /* hit.x: peak of (V_prev - V) / l */
   int peak_ok = 0;     /* hit.y */
@@ -995,7 +1030,7 @@ void orc_render(const orc_map* m, int mode, const float* pose, const float* dept
                 float* out_img, int64_t* counts) {
   int H = m->p.rows, W = m->p.cols;
   float* dep = (float*)malloc((size_t)H * W * sizeof(float));
-  clean_depth(m, depth, dep);
+  clean_depth(&m->cam, depth, dep);
   int64_t cnt[4] = {0, 0, 0, 0};
   for (int y = 0; y < H; ++y) {
     for (int x = 0; x < W; ++x) {

@@ -54,6 +54,11 @@ void orc_set_threads(int n);
 /* pose: row-major 4x4 camera-to-world (metres); depth: rows*cols row-major,
  * row 0 = top.  Returns the view id. */
 int orc_add_view(orc_map* m, const float* pose, const float* depth, int policy);
+/* a view with its own camera (rows x cols, intrinsics); the sensor tables
+ * are looked up at the pixel's position scaled into the params' image */
+int orc_add_view_camera(orc_map* m, const float* pose, const float* depth, int policy, int rows, int cols,
+                        float fx, float fy, float cx, float cy);
+int orc_view_pixels(const orc_map* m, int view);
 int orc_set_pose(orc_map* m, int view, const float* pose, int policy);
 int orc_num_views(const orc_map* m);
 int orc_num_bricks(const orc_map* m);

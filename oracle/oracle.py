@@ -53,6 +53,11 @@ def lib():
         L.orc_set_threads.argtypes = [C.c_int]
         L.orc_add_view.argtypes = [vp, fp, fp, C.c_int]
         L.orc_add_view.restype = C.c_int
+        L.orc_add_view_camera.argtypes = [vp, fp, fp, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float,
+                                          C.c_float, C.c_float]
+        L.orc_add_view_camera.restype = C.c_int
+        L.orc_view_pixels.argtypes = [vp, C.c_int]
+        L.orc_view_pixels.restype = C.c_int
         L.orc_set_pose.argtypes = [vp, C.c_int, fp, C.c_int]
         L.orc_num_views.argtypes = [vp]
         L.orc_num_bricks.argtypes = [vp]
@@ -117,6 +122,11 @@ class OracleMap:
     def add_view(self, pose, depth, policy=ACT_ENDPOINT) -> int:
         return self._L.orc_add_view(self._h, _ptr(_f(pose)), _ptr(_f(depth)), policy)
 
+    def add_view_camera(self, pose, depth, rows, cols, fx, fy, cx, cy, policy=ACT_ENDPOINT) -> int:
+        d = _f(depth)
+        assert d.size == rows * cols
+        return self._L.orc_add_view_camera(self._h, _ptr(_f(pose)), _ptr(d), policy, rows, cols, fx, fy, cx, cy)
+
     def set_pose(self, view, pose, policy=ACT_ENDPOINT):
         return self._L.orc_set_pose(self._h, view, _ptr(_f(pose)), policy)
 
@@ -154,7 +164,7 @@ class OracleMap:
 
     def view_trace(self, view):
         ninc = self._L.orc_view_num_incidences(self._h, view)
-        npx = self.params.rows * self.params.cols
+        npx = self._L.orc_view_pixels(self._h, view)
         pix = np.zeros(npx, np.int32)
         off = np.zeros(npx, np.int64)
         meta = np.zeros((npx, 5), np.int32)

@@ -143,3 +143,75 @@ def test_python_module_render_names(inferred):
     a3 = est.get_accuracy_image_at_pose_with_depth(w.poses[0], w.depths[0], out)
     np.testing.assert_array_equal(out, out2)
     assert 0.0 <= a3 <= 1.0
+
+
+def test_pixel_diagnostics_match_oracle_trace(inferred):
+    """The per-voxel records of one pixel's ray (the reference's diagnostic
+    probe) follow the oracle's traversal bit for bit; visibility and first
+    return density follow from the beliefs along it."""
+    w, m, om = inferred
+    bel = m.beliefs().reshape(-1)
+    for (x, y), P in (((40, 30), w.poses[0]), ((5, 52), w.poses[1]), ((77, 3), w.poses[2])):
+        d = m.pixel_diagnostics(P, x, y)
+        vox, ln, s = om.trace_pixel(P, x, y)
+        assert len(d["s"]) == len(vox) > 0
+        np.testing.assert_array_equal(d["vox"].astype(np.int64), vox.astype(np.int64))
+        np.testing.assert_array_equal(d["s"].view(np.uint32), s.view(np.uint32))
+        np.testing.assert_array_equal(d["belief"], bel[vox])
+        np.testing.assert_array_equal(d["slot"], vox // 512)
+        loc = vox % 512
+        np.testing.assert_array_equal(d["local"], np.stack([loc // 64, (loc // 8) % 8, loc % 8], 1))
+        A = np.cumsum(np.log1p(-bel[vox].astype(np.float64)) * ln)
+        V = np.exp(A)
+        np.testing.assert_allclose(d["vis"], V, rtol=1e-4, atol=1e-7)
+        Vp = np.concatenate([[1.0], V[:-1]])
+        # w = (V_prev - V) / l in fp32: the difference of two visibilities near
+        # 1 keeps a few ulps of 1 in absolute terms
+        np.testing.assert_allclose(d["w"] * ln, Vp - V, rtol=1e-3, atol=5e-7)
+    # a short buffer keeps the first records and says how many it kept
+    d = m.pixel_diagnostics(w.poses[0], 40, 30, n_floats=41)
+    assert len(d["s"]) == 4
+    with pytest.raises(L.MrfError):
+        m.pixel_diagnostics(w.poses[0], w.params.cols, 0)
+
+
+def test_python_module_diagnostics(inferred):
+    w, m, _ = inferred
+    path = _build.build_pymodule()
+    sys.path.insert(0, os.path.dirname(path))
+    import GVDBPyModules as G
+    p = w.params
+    gp = G.gvdb_params()
+    gp.res, gp.prior, gp.rows, gp.cols = p.res, p.prior, p.rows, p.cols
+    gp.dims = list(p.dims)
+    gp.K = p.K
+    gp.max_iters = p.max_iters
+    gp.lookup_n = 3
+    gp.const_sigmasq_poly = list(p.const_sigmasq_poly)
+    gp.populate_lookup_tables()
+    gp.set_from_python()
+    inf = G.GVDBInference(True, False)
+    for P, D in zip(w.poses, w.depths):
+        inf.add_camera_with_depth(P, D)
+    inf.perform_inference()
+    mm = L.MRFMap(w.params)
+    for P, D in zip(w.poses, w.depths):
+        mm.add_view(P, D)
+    mm.infer()
+    inf.set_selected_x_y(40, 30)
+    out = np.zeros((p.rows, p.cols), np.float32)
+    inf.get_diagnostic_image(1, out)
+    n = int(out.reshape(-1)[-1])
+    d = mm.pixel_diagnostics(w.poses[1], 40, 30)
+    assert n == len(d["s"]) > 0
+    np.testing.assert_array_equal(out.reshape(-1)[:n * 10].reshape(n, 10)[:, 0], d["s"])
+    out2 = np.zeros_like(out)
+    inf.get_diagnostic_image_at_pose(w.poses[1], G.GVDBImage(w.depths[1]), out2)
+    np.testing.assert_array_equal(out, out2)
+    inf.get_diagnostic_image(1, out, 1)
+    assert not out.any()
+    cen = inf.get_occupied_bricks(0)
+    vc = inf.get_voxel_coords([0, 1, 10 ** 9])
+    np.testing.assert_array_equal(vc[:2, :3], cen[:2] - 4)
+    np.testing.assert_array_equal(vc[:2, 3:], cen[:2] + 4)
+    assert not vc[2].any()
