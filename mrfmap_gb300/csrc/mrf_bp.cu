@@ -90,8 +90,10 @@ __global__ void __launch_bounds__(kPrepThreads)
 // only once the accumulated tau is non-zero, gvdbkernels.cu:708-715):
 // V^pre_i = exp(A_i - A_{r0-1}) = V_i * exp(-A_{r0-1}); Post uses V_i.
 constexpr int kRayWarps = 4;
-constexpr int kE = 8;                    // incidences per lane per chunk
+constexpr int kE = 8;                    // incidences per lane of a full chunk
 constexpr int kChunk = 32 * kE;          // 256
+constexpr int kES = 2;                   // incidences per lane of a short chunk
+constexpr int kChunkS = 32 * kES;        // 64: ray tails and the dynamic range
 constexpr float kUnderflowGuard = -60.0f;
 
 template <typename T>
@@ -100,11 +102,11 @@ __device__ __forceinline__ T warp_excl_scan(T v, int lane) {
   return incl - v;
 }
 
-// one lane's slice of a chunk
-// (ln q is kept; q itself is formed only where a potential is non-zero or
-// a message is computed)
+// one lane's slice of a chunk (KE incidences).  ln q is kept; q itself is
+// formed only where a potential is non-zero or a message is computed.
+template <int KE>
 struct Slice {
-  float A[kE], lq[kE], mu[kE], len[kE];
+  float A[KE], lq[KE], mu[KE], len[KE];
 };
 
 // streamed incidence arrays: read-only path (kPol 0) or evict-first
@@ -115,48 +117,86 @@ __device__ __forceinline__ T ld_stream(const T* p) {
   return __ldg(p);
 }
 
-// a lane's kE pair ids at i0 (those >= n read as zero)
-template <int kPol>
-__device__ __forceinline__ void load_pids(uint32_t (&pid)[kE], uint32_t off, int i0, int n,
-                                          const uint32_t* __restrict__ inc_pair) {
+template <typename T>
+__device__ __forceinline__ T from_bits(uint32_t u);
+template <>
+__device__ __forceinline__ uint32_t from_bits<uint32_t>(uint32_t u) { return u; }
+template <>
+__device__ __forceinline__ float from_bits<float>(uint32_t u) { return __uint_as_float(u); }
+
+// KE consecutive values at element i (i a multiple of KE; KE = 2 or a
+// multiple of 4): 8-byte or 16-byte vector loads, zeros when !ok
+template <int KE, int kPol, typename T>
+__device__ __forceinline__ void ld_vec(T (&out)[KE], const T* __restrict__ base, int i, bool ok) {
+  static_assert(sizeof(T) == 4, "4-byte elements");
+  if constexpr (KE % 4 == 0) {
 #pragma unroll
-  for (int v = 0; v < kE / 4; ++v) {
-    const int i = i0 + 4 * v;
-    uint4 p = make_uint4(0u, 0u, 0u, 0u);
-    if (i < n) p = ld_stream<kPol>(reinterpret_cast<const uint4*>(inc_pair + off + i));
-    pid[4 * v + 0] = p.x; pid[4 * v + 1] = p.y; pid[4 * v + 2] = p.z; pid[4 * v + 3] = p.w;
+    for (int v = 0; v < KE / 4; ++v) {
+      uint4 u = make_uint4(0u, 0u, 0u, 0u);
+      if (ok) u = ld_stream<kPol>(reinterpret_cast<const uint4*>(base + i + 4 * v));
+      out[4 * v + 0] = from_bits<T>(u.x);
+      out[4 * v + 1] = from_bits<T>(u.y);
+      out[4 * v + 2] = from_bits<T>(u.z);
+      out[4 * v + 3] = from_bits<T>(u.w);
+    }
+  } else {
+    static_assert(KE == 2, "short chunks hold two incidences per lane");
+    uint2 u = make_uint2(0u, 0u);
+    if (ok) u = ld_stream<kPol>(reinterpret_cast<const uint2*>(base + i));
+    out[0] = from_bits<T>(u.x);
+    out[1] = from_bits<T>(u.y);
   }
 }
 
-// ln q of a lane's kE incidences (those >= n read as zero)
-__device__ __forceinline__ void gather_lq(float (&lq)[kE], const uint32_t (&pid)[kE], int i0, int n,
+// a lane's KE pair ids at i0 (those >= n read as zero)
+template <int KE, int kPol>
+__device__ __forceinline__ void load_pids(uint32_t (&pid)[KE], uint32_t off, int i0, int n,
+                                          const uint32_t* __restrict__ inc_pair) {
+  if constexpr (KE % 4 == 0) {
+#pragma unroll
+    for (int v = 0; v < KE / 4; ++v) {
+      uint32_t t[4];
+      ld_vec<4, kPol>(t, inc_pair + off, i0 + 4 * v, i0 + 4 * v < n);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) pid[4 * v + j] = t[j];
+    }
+  } else {
+    ld_vec<KE, kPol>(pid, inc_pair + off, i0, i0 < n);
+  }
+}
+
+// ln q of a lane's KE incidences (those >= n read as zero)
+template <int KE>
+__device__ __forceinline__ void gather_lq(float (&lq)[KE], const uint32_t (&pid)[KE], int i0, int n,
                                           const float* __restrict__ lnq) {
 #pragma unroll
-  for (int j = 0; j < kE; ++j) lq[j] = (i0 + j < n) ? __ldg(lnq + pid[j]) : 0.0f;
+  for (int j = 0; j < KE; ++j) lq[j] = (i0 + j < n) ? __ldg(lnq + pid[j]) : 0.0f;
 }
 
 // with the lane's ln q gathered: loads lengths (and potentials at and after
 // kmu, a multiple of 4; below it they are known zeros), forms prefix
 // exponents from carryA; returns the chunk total of l ln q
-template <int kPol>
-__device__ __forceinline__ float slice_from_lq(Slice& s, const float (&lq)[kE], uint32_t off, int i0, int n,
-                                               int kmu, float carryA, int lane,
+template <int KE, int kPol>
+__device__ __forceinline__ float slice_from_lq(Slice<KE>& s, const float (&lq)[KE], uint32_t off, int i0,
+                                               int n, int kmu, float carryA, int lane,
                                                const float* __restrict__ inc_len,
                                                const float* __restrict__ inc_mu) {
+  constexpr int VW = KE % 4 == 0 ? 4 : KE;  // vector width
 #pragma unroll
-  for (int v = 0; v < kE / 4; ++v) {
-    const int i = i0 + 4 * v;
-    float4 l = make_float4(0.f, 0.f, 0.f, 0.f), m = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (i < n) {
-      l = ld_stream<kPol>(reinterpret_cast<const float4*>(inc_len + off + i));
-      if (i >= kmu) m = ld_stream<kPol>(reinterpret_cast<const float4*>(inc_mu + off + i));
+  for (int v = 0; v < KE / VW; ++v) {
+    const int i = i0 + VW * v;
+    float l[VW], m[VW];
+    ld_vec<VW, kPol>(l, inc_len + off, i, i < n);
+    ld_vec<VW, kPol>(m, inc_mu + off, i, i < n && i >= kmu);
+#pragma unroll
+    for (int j = 0; j < VW; ++j) {
+      s.len[VW * v + j] = l[j];
+      s.mu[VW * v + j] = m[j];
     }
-    s.len[4 * v + 0] = l.x; s.len[4 * v + 1] = l.y; s.len[4 * v + 2] = l.z; s.len[4 * v + 3] = l.w;
-    s.mu[4 * v + 0] = m.x; s.mu[4 * v + 1] = m.y; s.mu[4 * v + 2] = m.z; s.mu[4 * v + 3] = m.w;
   }
   float run = 0.0f;
 #pragma unroll
-  for (int j = 0; j < kE; ++j) {
+  for (int j = 0; j < KE; ++j) {
     const bool ok = i0 + j < n;
     s.lq[j] = ok ? lq[j] : 0.0f;
     if (!ok) {
@@ -169,54 +209,55 @@ __device__ __forceinline__ float slice_from_lq(Slice& s, const float (&lq)[kE], 
   float ex = warp_excl_scan(run, lane);
   float b = carryA + ex;
 #pragma unroll
-  for (int j = 0; j < kE; ++j) s.A[j] += b;
+  for (int j = 0; j < KE; ++j) s.A[j] += b;
   return __shfl_sync(kFull, ex + run, 31);
 }
 
-template <int kPol>
-__device__ __forceinline__ float slice_from_pids(Slice& s, const uint32_t (&pid)[kE], uint32_t off, int i0,
-                                                 int n, int kmu, float carryA, int lane,
+template <int KE, int kPol>
+__device__ __forceinline__ float slice_from_pids(Slice<KE>& s, const uint32_t (&pid)[KE], uint32_t off,
+                                                 int i0, int n, int kmu, float carryA, int lane,
                                                  const float* __restrict__ inc_len,
                                                  const float* __restrict__ inc_mu,
                                                  const float* __restrict__ lnq) {
-  float lq[kE];
-  gather_lq(lq, pid, i0, n, lnq);
-  return slice_from_lq<kPol>(s, lq, off, i0, n, kmu, carryA, lane, inc_len, inc_mu);
+  float lq[KE];
+  gather_lq<KE>(lq, pid, i0, n, lnq);
+  return slice_from_lq<KE, kPol>(s, lq, off, i0, n, kmu, carryA, lane, inc_len, inc_mu);
 }
 
-template <int kPol>
-__device__ __forceinline__ float load_slice(Slice& s, uint32_t off, int i0, int n, int kmu,
+template <int KE, int kPol>
+__device__ __forceinline__ float load_slice(Slice<KE>& s, uint32_t off, int i0, int n, int kmu,
                                             float carryA, int lane,
                                             const uint32_t* __restrict__ inc_pair,
                                             const float* __restrict__ inc_len,
                                             const float* __restrict__ inc_mu,
                                             const float* __restrict__ lnq) {
-  uint32_t pid[kE];
-  load_pids<kPol>(pid, off, i0, n, inc_pair);
-  return slice_from_pids<kPol>(s, pid, off, i0, n, kmu, carryA, lane, inc_len, inc_mu, lnq);
+  uint32_t pid[KE];
+  load_pids<KE, kPol>(pid, off, i0, n, inc_pair);
+  return slice_from_pids<KE, kPol>(s, pid, off, i0, n, kmu, carryA, lane, inc_len, inc_mu, lnq);
 }
 
-// A at chunk-relative index idx (0 <= idx < kChunk), broadcast to the warp
-__device__ __forceinline__ float slice_value(const Slice& s, int idx) {
-  const int jj = idx % kE;
+// A at chunk-relative index idx (0 <= idx < 32 * KE), broadcast to the warp
+template <int KE>
+__device__ __forceinline__ float slice_value(const Slice<KE>& s, int idx) {
+  const int jj = idx % KE;
   float mine = 0.0f;
 #pragma unroll
-  for (int j = 0; j < kE; ++j)
+  for (int j = 0; j < KE; ++j)
     if (j == jj) mine = s.A[j];
-  return __shfl_sync(kFull, mine, idx / kE);
+  return __shfl_sync(kFull, mine, idx / KE);
 }
 
-// pass 2 on one lane's slice: messages p*l for positions i0..i0+kE-1; the
-// 4-vectors inside [k4, n_post) are written (k4 a multiple of 4)
-template <typename Acc>
-__device__ __forceinline__ Acc emit_slice(const float (&vmu)[kE], const float (&q)[kE],
-                                          const float (&len)[kE], int i0, int k4, int n_post,
+// pass 2 on one lane's slice: messages p*l for positions i0..i0+KE-1; the
+// vectors starting inside [k4, n_post) are written (k4 a multiple of 4)
+template <int KE, typename Acc>
+__device__ __forceinline__ Acc emit_slice(const float (&vmu)[KE], const float (&q)[KE],
+                                          const float (&len)[KE], int i0, int k4, int n_post,
                                           Acc T, Acc carryF, int lane, uint32_t off,
                                           float* __restrict__ inc_pl) {
-  float tau[kE], eloc[kE];
+  float tau[KE], eloc[KE];
   float run = 0.0f;
 #pragma unroll
-  for (int j = 0; j < kE; ++j) {
+  for (int j = 0; j < KE; ++j) {
     tau[j] = (i0 + j < n_post) ? vmu[j] * (1.0f - q[j]) : 0.0f;
     eloc[j] = run;
     run += tau[j];
@@ -226,9 +267,9 @@ __device__ __forceinline__ Acc emit_slice(const float (&vmu)[kE], const float (&
   // T - carryF is formed in Acc (FP64 on long rays) once per chunk
   const float cF = (float)carryF;
   const float D = (float)(T - carryF);
-  float out[kE];
+  float out[KE];
 #pragma unroll
-  for (int j = 0; j < kE; ++j) {
+  for (int j = 0; j < KE; ++j) {
     float fin = ex + eloc[j];
     float F = cF + fin;
     float R = (D - fin) - tau[j];
@@ -237,14 +278,43 @@ __device__ __forceinline__ Acc emit_slice(const float (&vmu)[kE], const float (&
     float p = clampf(__fdividef(mu1, mu1 + mu0 + 1e-7f), kFEps, 1.0f - kFEps);
     out[j] = (i0 + j < n_post) ? p * len[j] : 0.0f;
   }
+  constexpr int VW = KE % 4 == 0 ? 4 : KE;
 #pragma unroll
-  for (int v = 0; v < kE / 4; ++v) {
-    const int i = i0 + 4 * v;
-    if (i >= k4 && i < n_post)
-      *reinterpret_cast<float4*>(inc_pl + off + i) =
-          make_float4(out[4 * v], out[4 * v + 1], out[4 * v + 2], out[4 * v + 3]);
+  for (int v = 0; v < KE / VW; ++v) {
+    const int i = i0 + VW * v;
+    if (i >= k4 && i < n_post) {
+      if constexpr (VW == 4)
+        *reinterpret_cast<float4*>(inc_pl + off + i) =
+            make_float4(out[4 * v], out[4 * v + 1], out[4 * v + 2], out[4 * v + 3]);
+      else
+        *reinterpret_cast<float2*>(inc_pl + off + i) = make_float2(out[2 * v], out[2 * v + 1]);
+    }
   }
   return carryF + (Acc)__shfl_sync(kFull, ex + run, 31);
+}
+
+// Pass-1 work of one slice: record the prefix values the ray needs and add
+// the lane's share of the Pre total
+template <int KE, typename Acc>
+__device__ __forceinline__ void pre_slice(const Slice<KE>& s, int base, int i0, int r0, int rinf, int k4,
+                                          float& Ar0, float& Arinf, float& Ak, Acc& Tl) {
+  constexpr int CH = 32 * KE;
+  if (r0 > 0 && r0 - 1 >= base && r0 - 1 < base + CH) Ar0 = slice_value<KE>(s, r0 - 1 - base);
+  if (rinf > 0 && rinf - 1 >= base && rinf - 1 < base + CH) Arinf = slice_value<KE>(s, rinf - 1 - base);
+  if (k4 > 0 && k4 - 1 >= base && k4 - 1 < base + CH) Ak = slice_value<KE>(s, k4 - 1 - base);
+  // exp(-A_{r0-1}) rescales Post visibility to Pre visibility unless the
+  // Post visibility may have underflowed (then exponentiate the difference)
+  const bool direct = Ar0 < kUnderflowGuard;
+  const float scale = direct ? 0.0f : __expf(-Ar0);
+  float w = 0.0f;
+#pragma unroll
+  for (int j = 0; j < KE; ++j) {
+    if (i0 + j >= r0 && s.mu[j] != 0.0f) {
+      float vp = direct ? __expf(s.A[j] - Ar0) : __expf(s.A[j]) * scale;
+      w += vp * (1.0f - __expf(s.lq[j])) * s.mu[j];
+    }
+  }
+  Tl += (Acc)w;
 }
 
 template <typename Acc, int kPol, int kPf>
@@ -260,65 +330,64 @@ __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, const uint32_t* _
   const int k4 = kdyn & ~3;
   const uint32_t off = me.off;
   // ---- pass 1: prefixes, Pre total ---------------------------------------
+  // Full chunks of 256, then the ray's tail in chunks of 64 (a chunk costs
+  // the same instructions however many of its lanes hold incidences).
   float carryA = 0.0f, Ar0 = 0.0f, Arinf = 0.0f, Ak = 0.0f;
   Acc T = 0, Tl = 0;
-  Slice s;
-  // kPf: the next chunk's pair ids are requested before this chunk's ln q
-  // gathers, so a chunk waits on one memory round trip instead of two.
-  // (Issuing the next chunk's gathers early as well needs ~95 registers;
-  // the lost occupancy made it slower.)
-  uint32_t pid_next[kE];
-  if (kPf) load_pids<kPol>(pid_next, off, kE * lane, n_pre, inc_pair);
-  for (int base = 0; base < n_pre; base += kChunk) {
-    const int i0 = base + kE * lane;
-    uint32_t pid[kE];
-    if (kPf) {
+  const int full = n_pre & ~(kChunk - 1);
+  {
+    Slice<kE> s;
+    // kPf: the next chunk's pair ids are requested before this chunk's ln q
+    // gathers, so a chunk waits on one memory round trip instead of two.
+    // (Issuing the next chunk's gathers early as well needs ~95 registers;
+    // the lost occupancy made it slower.)
+    uint32_t pid_next[kE];
+    if (kPf && full) load_pids<kE, kPol>(pid_next, off, kE * lane, n_pre, inc_pair);
+    for (int base = 0; base < full; base += kChunk) {
+      const int i0 = base + kE * lane;
+      uint32_t pid[kE];
+      if (kPf) {
 #pragma unroll
-      for (int j = 0; j < kE; ++j) pid[j] = pid_next[j];
-      if (base + kChunk < n_pre) load_pids<kPol>(pid_next, off, i0 + kChunk, n_pre, inc_pair);
-    } else {
-      load_pids<kPol>(pid, off, i0, n_pre, inc_pair);
-    }
-    float tot = slice_from_pids<kPol>(s, pid, off, i0, n_pre, k4, carryA, lane, inc_len, inc_mu, lnq);
-    if (r0 > 0 && r0 - 1 >= base && r0 - 1 < base + kChunk) Ar0 = slice_value(s, r0 - 1 - base);
-    if (rinf > 0 && rinf - 1 >= base && rinf - 1 < base + kChunk) Arinf = slice_value(s, rinf - 1 - base);
-    if (k4 > 0 && k4 - 1 >= base && k4 - 1 < base + kChunk) Ak = slice_value(s, k4 - 1 - base);
-    // exp(-A_{r0-1}) rescales Post visibility to Pre visibility unless the
-    // Post visibility may have underflowed (then exponentiate the difference)
-    const bool direct = Ar0 < kUnderflowGuard;
-    const float scale = direct ? 0.0f : __expf(-Ar0);
-    float w = 0.0f;
-#pragma unroll
-    for (int j = 0; j < kE; ++j) {
-      if (i0 + j >= r0 && s.mu[j] != 0.0f) {
-        float vp = direct ? __expf(s.A[j] - Ar0) : __expf(s.A[j]) * scale;
-        w += vp * (1.0f - __expf(s.lq[j])) * s.mu[j];
+        for (int j = 0; j < kE; ++j) pid[j] = pid_next[j];
+        if (base + kChunk < full) load_pids<kE, kPol>(pid_next, off, i0 + kChunk, n_pre, inc_pair);
+      } else {
+        load_pids<kE, kPol>(pid, off, i0, n_pre, inc_pair);
       }
+      float tot = slice_from_pids<kE, kPol>(s, pid, off, i0, n_pre, k4, carryA, lane, inc_len, inc_mu, lnq);
+      pre_slice<kE, Acc>(s, base, i0, r0, rinf, k4, Ar0, Arinf, Ak, Tl);
+      carryA += tot;
     }
-    Tl += (Acc)w;
-    carryA += tot;
+  }
+  {
+    Slice<kES> s;
+    for (int base = full; base < n_pre; base += kChunkS) {
+      const int i0 = base + kES * lane;
+      float tot = load_slice<kES, kPol>(s, off, i0, n_pre, k4, carryA, lane, inc_pair, inc_len, inc_mu, lnq);
+      pre_slice<kES, Acc>(s, base, i0, r0, rinf, k4, Ar0, Arinf, Ak, Tl);
+      carryA += tot;
+    }
   }
   T = warp_sum(Tl);  // each lane's share of the Pre total, summed once per ray
   // infinity term: visibility at the end of Pre (gvdbkernels.cu:1196-1208)
   if (me.flags & 1u) T += (Acc)__expf(carryA - Arinf);
   if (kdyn >= n_post) return;  // every message of the ray is static
-  // ---- pass 2: dynamic messages ------------------------------------------
+  // ---- pass 2: dynamic messages, chunks of 64 ------------------------------
   // F is zero before k_dyn, so the running F starts at zero at k4
   Acc carryF = 0;
-  float vmu[kE];
   float carryA2 = Ak;
-  for (int base = k4; base < n_post; base += kChunk) {
-    const int i0 = base + kE * lane;
-    float tot2 = load_slice<kPol>(s, off, i0, n_post, k4, carryA2, lane, inc_pair, inc_len, inc_mu,
-                                  lnq);
+  Slice<kES> s;
+  for (int base = k4; base < n_post; base += kChunkS) {
+    const int i0 = base + kES * lane;
+    float tot2 = load_slice<kES, kPol>(s, off, i0, n_post, k4, carryA2, lane, inc_pair, inc_len, inc_mu,
+                                       lnq);
     carryA2 += tot2;
-    float q[kE];
+    float vmu[kES], q[kES];
 #pragma unroll
-    for (int j = 0; j < kE; ++j) {
+    for (int j = 0; j < kES; ++j) {
       vmu[j] = __expf(s.A[j]) * s.mu[j];
       q[j] = __expf(s.lq[j]);
     }
-    carryF = emit_slice<Acc>(vmu, q, s.len, i0, k4, n_post, T, carryF, lane, off, inc_pl);
+    carryF = emit_slice<kES, Acc>(vmu, q, s.len, i0, k4, n_post, T, carryF, lane, off, inc_pl);
   }
 }
 
