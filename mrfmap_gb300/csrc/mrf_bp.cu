@@ -69,10 +69,10 @@ __global__ void __launch_bounds__(kPrepThreads)
 }
 
 // ---- ray messages ----------------------------------------------------------
-// One warp per ray.  Each lane owns kE = 8 consecutive incidences of a
-// chunk of 256 (ray offsets are padded to multiples of 4, so the streams load
+// One warp per ray.  Each lane owns kE = 4 consecutive incidences of a
+// chunk of 128 (ray offsets are padded to multiples of 4, so the streams load
 // as 16-byte vectors): the prefix over the ray is a serial sum inside the
-// lane plus one warp scan per chunk, and a lane keeps 8 gathers in flight.
+// lane plus one warp scan per chunk, and a lane keeps 4 gathers in flight.
 //
 // Pass 1 forms the visibility exponent A_i = sum_{j<=i} l_j ln q_j,
 // V_i = exp(A_i), q_i and the Pre total T over the whole ray.  Pass 2 turns
@@ -83,17 +83,15 @@ __global__ void __launch_bounds__(kPrepThreads)
 // loaded from k_dyn (rounded down to a vector) on.  Pass 2 re-reads the
 // dynamic range (a sixth of the incidences, mostly still in L1/L2) from
 // A_{k_dyn - 1} instead of keeping pass 1's slice in registers: the kernel
-// then fits 64 registers, eight resident blocks per SM.  The tau sums of
+// then fits 40 registers, twelve resident blocks per SM.  The tau sums of
 // rays longer than kLongRay are formed in FP64.
 //
 // Pre visibility restarts at r0 (the reference restores its carried state
 // only once the accumulated tau is non-zero, gvdbkernels.cu:708-715):
 // V^pre_i = exp(A_i - A_{r0-1}) = V_i * exp(-A_{r0-1}); Post uses V_i.
 constexpr int kRayWarps = 4;
-constexpr int kE = 8;                    // incidences per lane of a full chunk
-constexpr int kChunk = 32 * kE;          // 256
-constexpr int kES = 2;                   // incidences per lane of a short chunk
-constexpr int kChunkS = 32 * kES;        // 64: ray tails and the dynamic range
+constexpr int kE = 4;                    // incidences per lane of a chunk
+constexpr int kChunk = 32 * kE;          // 128
 constexpr float kUnderflowGuard = -60.0f;
 
 template <typename T>
@@ -330,64 +328,50 @@ __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, const uint32_t* _
   const int k4 = kdyn & ~3;
   const uint32_t off = me.off;
   // ---- pass 1: prefixes, Pre total ---------------------------------------
-  // Full chunks of 256, then the ray's tail in chunks of 64 (a chunk costs
-  // the same instructions however many of its lanes hold incidences).
+  // Chunks of 128 (a chunk costs the same instructions however many of its
+  // lanes hold incidences: measured against 256-incidence chunks and against
+  // 256-incidence chunks with 64- or 128-incidence tails, this was fastest).
   float carryA = 0.0f, Ar0 = 0.0f, Arinf = 0.0f, Ak = 0.0f;
   Acc T = 0, Tl = 0;
-  const int full = n_pre & ~(kChunk - 1);
-  {
-    Slice<kE> s;
-    // kPf: the next chunk's pair ids are requested before this chunk's ln q
-    // gathers, so a chunk waits on one memory round trip instead of two.
-    // (Issuing the next chunk's gathers early as well needs ~95 registers;
-    // the lost occupancy made it slower.)
-    uint32_t pid_next[kE];
-    if (kPf && full) load_pids<kE, kPol>(pid_next, off, kE * lane, n_pre, inc_pair);
-    for (int base = 0; base < full; base += kChunk) {
-      const int i0 = base + kE * lane;
-      uint32_t pid[kE];
-      if (kPf) {
+  Slice<kE> s;
+  // kPf: the next chunk's pair ids are requested before this chunk's ln q
+  // gathers, so a chunk waits on one memory round trip instead of two.
+  uint32_t pid_next[kE];
+  if (kPf) load_pids<kE, kPol>(pid_next, off, kE * lane, n_pre, inc_pair);
+  for (int base = 0; base < n_pre; base += kChunk) {
+    const int i0 = base + kE * lane;
+    uint32_t pid[kE];
+    if (kPf) {
 #pragma unroll
-        for (int j = 0; j < kE; ++j) pid[j] = pid_next[j];
-        if (base + kChunk < full) load_pids<kE, kPol>(pid_next, off, i0 + kChunk, n_pre, inc_pair);
-      } else {
-        load_pids<kE, kPol>(pid, off, i0, n_pre, inc_pair);
-      }
-      float tot = slice_from_pids<kE, kPol>(s, pid, off, i0, n_pre, k4, carryA, lane, inc_len, inc_mu, lnq);
-      pre_slice<kE, Acc>(s, base, i0, r0, rinf, k4, Ar0, Arinf, Ak, Tl);
-      carryA += tot;
+      for (int j = 0; j < kE; ++j) pid[j] = pid_next[j];
+      if (base + kChunk < n_pre) load_pids<kE, kPol>(pid_next, off, i0 + kChunk, n_pre, inc_pair);
+    } else {
+      load_pids<kE, kPol>(pid, off, i0, n_pre, inc_pair);
     }
-  }
-  {
-    Slice<kES> s;
-    for (int base = full; base < n_pre; base += kChunkS) {
-      const int i0 = base + kES * lane;
-      float tot = load_slice<kES, kPol>(s, off, i0, n_pre, k4, carryA, lane, inc_pair, inc_len, inc_mu, lnq);
-      pre_slice<kES, Acc>(s, base, i0, r0, rinf, k4, Ar0, Arinf, Ak, Tl);
-      carryA += tot;
-    }
+    float tot = slice_from_pids<kE, kPol>(s, pid, off, i0, n_pre, k4, carryA, lane, inc_len, inc_mu, lnq);
+    pre_slice<kE, Acc>(s, base, i0, r0, rinf, k4, Ar0, Arinf, Ak, Tl);
+    carryA += tot;
   }
   T = warp_sum(Tl);  // each lane's share of the Pre total, summed once per ray
   // infinity term: visibility at the end of Pre (gvdbkernels.cu:1196-1208)
   if (me.flags & 1u) T += (Acc)__expf(carryA - Arinf);
   if (kdyn >= n_post) return;  // every message of the ray is static
-  // ---- pass 2: dynamic messages, chunks of 64 ------------------------------
+  // ---- pass 2: dynamic messages ------------------------------------------
   // F is zero before k_dyn, so the running F starts at zero at k4
   Acc carryF = 0;
   float carryA2 = Ak;
-  Slice<kES> s;
-  for (int base = k4; base < n_post; base += kChunkS) {
-    const int i0 = base + kES * lane;
-    float tot2 = load_slice<kES, kPol>(s, off, i0, n_post, k4, carryA2, lane, inc_pair, inc_len, inc_mu,
-                                       lnq);
+  for (int base = k4; base < n_post; base += kChunk) {
+    const int i0 = base + kE * lane;
+    float tot2 = load_slice<kE, kPol>(s, off, i0, n_post, k4, carryA2, lane, inc_pair, inc_len, inc_mu,
+                                      lnq);
     carryA2 += tot2;
-    float vmu[kES], q[kES];
+    float vmu[kE], q[kE];
 #pragma unroll
-    for (int j = 0; j < kES; ++j) {
+    for (int j = 0; j < kE; ++j) {
       vmu[j] = __expf(s.A[j]) * s.mu[j];
       q[j] = __expf(s.lq[j]);
     }
-    carryF = emit_slice<kES, Acc>(vmu, q, s.len, i0, k4, n_post, T, carryF, lane, off, inc_pl);
+    carryF = emit_slice<kE, Acc>(vmu, q, s.len, i0, k4, n_post, T, carryF, lane, off, inc_pl);
   }
 }
 
