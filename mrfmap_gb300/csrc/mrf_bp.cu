@@ -49,8 +49,8 @@ constexpr int kPrepPer = 4;
 
 __global__ void __launch_bounds__(kPrepThreads)
     k_pair_prepare(const uint32_t* __restrict__ pair_vox, const float* __restrict__ m,
-                   const float* __restrict__ L, float* __restrict__ lnq, float* __restrict__ dm,
-                   uint32_t p0, uint32_t p1) {
+                   const float* __restrict__ L, float* __restrict__ lnq, float* __restrict__ dm, uint32_t p0,
+                   uint32_t p1) {
   const uint32_t base = p0 + blockIdx.x * (kPrepThreads * kPrepPer) + threadIdx.x;
   float eta[kPrepPer];
 #pragma unroll
@@ -65,6 +65,27 @@ __global__ void __launch_bounds__(kPrepThreads)
     float qq = clampf(1.0f / (1.0f + expf(eta[k])), kFEps, 1.0f - kFEps);
     lnq[p] = logf(qq);
     if (dm) dm[p] = __int_as_float(0x7fc00000);  // Jacobi: NaN until the pair updates
+  }
+}
+
+// ln q into slot order (first visit along the rays, the order the ray
+// kernel gathers in): lnq[q] = lnv[pair_of_slot[q]].  The voxel-order values
+// were just written by k_pair_prepare and the slots of a view are a
+// permutation of its pairs, so the gathers read L2; four slots per thread.
+__global__ void __launch_bounds__(256)
+    k_lnq_slots(const uint32_t* __restrict__ pair_of_slot, const float* __restrict__ lnv,
+                float* __restrict__ lnq, uint32_t q0, uint32_t q1) {
+  const uint32_t base = q0 + blockIdx.x * (256 * 4) + threadIdx.x;
+  float v[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const uint32_t q = base + k * 256;
+    v[k] = q < q1 ? lnv[pair_of_slot[q]] : 0.0f;
+  }
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const uint32_t q = base + k * 256;
+    if (q < q1) lnq[q] = v[k];
   }
 }
 
@@ -163,29 +184,37 @@ __device__ __forceinline__ void load_pids(uint32_t (&pid)[KE], uint32_t off, int
   }
 }
 
-// ln q of a lane's KE incidences (those >= n read as zero)
-template <int KE>
+// ln q of a lane's KE incidences (those >= n read as zero; kWhole: the
+// whole chunk lies inside the ray and nothing is checked)
+template <int KE, bool kWhole>
 __device__ __forceinline__ void gather_lq(float (&lq)[KE], const uint32_t (&pid)[KE], int i0, int n,
                                           const float* __restrict__ lnq) {
 #pragma unroll
-  for (int j = 0; j < KE; ++j) lq[j] = (i0 + j < n) ? __ldg(lnq + pid[j]) : 0.0f;
+  for (int j = 0; j < KE; ++j) lq[j] = (kWhole || i0 + j < n) ? __ldg(lnq + pid[j]) : 0.0f;
 }
 
 // with the lane's ln q gathered: loads lengths (and potentials at and after
 // kmu, a multiple of 4; below it they are known zeros), forms prefix
 // exponents from carryA; returns the chunk total of l ln q
-template <int KE, int kPol>
+// (kLenIn: the lengths were loaded ahead into len_in)
+template <int KE, int kPol, bool kWhole, bool kLenIn = false>
 __device__ __forceinline__ float slice_from_lq(Slice<KE>& s, const float (&lq)[KE], uint32_t off, int i0,
                                                int n, int kmu, float carryA, int lane,
                                                const float* __restrict__ inc_len,
-                                               const float* __restrict__ inc_mu) {
+                                               const float* __restrict__ inc_mu,
+                                               const float* len_in = nullptr) {
   constexpr int VW = KE % 4 == 0 ? 4 : KE;  // vector width
 #pragma unroll
   for (int v = 0; v < KE / VW; ++v) {
     const int i = i0 + VW * v;
     float l[VW], m[VW];
-    ld_vec<VW, kPol>(l, inc_len + off, i, i < n);
-    ld_vec<VW, kPol>(m, inc_mu + off, i, i < n && i >= kmu);
+    if constexpr (kLenIn) {
+#pragma unroll
+      for (int j = 0; j < VW; ++j) l[j] = len_in[VW * v + j];
+    } else {
+      ld_vec<VW, kPol>(l, inc_len + off, i, kWhole || i < n);
+    }
+    ld_vec<VW, kPol>(m, inc_mu + off, i, (kWhole || i < n) && i >= kmu);
 #pragma unroll
     for (int j = 0; j < VW; ++j) {
       s.len[VW * v + j] = l[j];
@@ -195,7 +224,7 @@ __device__ __forceinline__ float slice_from_lq(Slice<KE>& s, const float (&lq)[K
   float run = 0.0f;
 #pragma unroll
   for (int j = 0; j < KE; ++j) {
-    const bool ok = i0 + j < n;
+    const bool ok = kWhole || i0 + j < n;
     s.lq[j] = ok ? lq[j] : 0.0f;
     if (!ok) {
       s.len[j] = 0.0f;
@@ -211,18 +240,20 @@ __device__ __forceinline__ float slice_from_lq(Slice<KE>& s, const float (&lq)[K
   return __shfl_sync(kFull, ex + run, 31);
 }
 
-template <int KE, int kPol>
+template <int KE, int kPol, bool kWhole, bool kLenIn = false>
 __device__ __forceinline__ float slice_from_pids(Slice<KE>& s, const uint32_t (&pid)[KE], uint32_t off,
                                                  int i0, int n, int kmu, float carryA, int lane,
                                                  const float* __restrict__ inc_len,
                                                  const float* __restrict__ inc_mu,
-                                                 const float* __restrict__ lnq) {
+                                                 const float* __restrict__ lnq,
+                                                 const float* len_in = nullptr) {
   float lq[KE];
-  gather_lq<KE>(lq, pid, i0, n, lnq);
-  return slice_from_lq<KE, kPol>(s, lq, off, i0, n, kmu, carryA, lane, inc_len, inc_mu);
+  gather_lq<KE, kWhole>(lq, pid, i0, n, lnq);
+  return slice_from_lq<KE, kPol, kWhole, kLenIn>(s, lq, off, i0, n, kmu, carryA, lane, inc_len, inc_mu,
+                                                len_in);
 }
 
-template <int KE, int kPol>
+template <int KE, int kPol, bool kWhole>
 __device__ __forceinline__ float load_slice(Slice<KE>& s, uint32_t off, int i0, int n, int kmu,
                                             float carryA, int lane,
                                             const uint32_t* __restrict__ inc_pair,
@@ -230,8 +261,8 @@ __device__ __forceinline__ float load_slice(Slice<KE>& s, uint32_t off, int i0, 
                                             const float* __restrict__ inc_mu,
                                             const float* __restrict__ lnq) {
   uint32_t pid[KE];
-  load_pids<KE, kPol>(pid, off, i0, n, inc_pair);
-  return slice_from_pids<KE, kPol>(s, pid, off, i0, n, kmu, carryA, lane, inc_len, inc_mu, lnq);
+  load_pids<KE, kPol>(pid, off, i0, kWhole ? i0 + KE : n, inc_pair);
+  return slice_from_pids<KE, kPol, kWhole>(s, pid, off, i0, n, kmu, carryA, lane, inc_len, inc_mu, lnq);
 }
 
 // A at chunk-relative index idx (0 <= idx < 32 * KE), broadcast to the warp
@@ -246,25 +277,23 @@ __device__ __forceinline__ float slice_value(const Slice<KE>& s, int idx) {
 }
 
 // pass 2 on one lane's slice: messages p*l for positions i0..i0+KE-1; the
-// vectors starting inside [k4, n_post) are written (k4 a multiple of 4)
-template <int KE, typename Acc>
-__device__ __forceinline__ Acc emit_slice(const float (&vmu)[KE], const float (&q)[KE],
-                                          const float (&len)[KE], int i0, int k4, int n_post,
-                                          Acc T, Acc carryF, int lane, uint32_t off,
-                                          float* __restrict__ inc_pl) {
+// vectors starting inside [k4, n_post) are written (k4 a multiple of 4).
+// cF is F at the chunk start and D = T - cF, formed in the ray's
+// accumulation type by the caller; returns the chunk's total of tau.
+template <int KE, bool kWhole>
+__device__ __forceinline__ float emit_slice(const float (&vmu)[KE], const float (&q)[KE],
+                                            const float (&len)[KE], int i0, int k4, int n_post,
+                                            float cF, float D, int lane, uint32_t off,
+                                            float* __restrict__ inc_pl) {
   float tau[KE], eloc[KE];
   float run = 0.0f;
 #pragma unroll
   for (int j = 0; j < KE; ++j) {
-    tau[j] = (i0 + j < n_post) ? vmu[j] * (1.0f - q[j]) : 0.0f;
+    tau[j] = (kWhole || i0 + j < n_post) ? vmu[j] * (1.0f - q[j]) : 0.0f;
     eloc[j] = run;
     run += tau[j];
   }
   float ex = warp_excl_scan(run, lane);
-  // F_i = carryF + (in-chunk exclusive prefix); the long-range difference
-  // T - carryF is formed in Acc (FP64 on long rays) once per chunk
-  const float cF = (float)carryF;
-  const float D = (float)(T - carryF);
   float out[KE];
 #pragma unroll
   for (int j = 0; j < KE; ++j) {
@@ -274,13 +303,13 @@ __device__ __forceinline__ Acc emit_slice(const float (&vmu)[KE], const float (&
     float mu1 = F + vmu[j];
     float mu0 = F + __fdividef(R, q[j]);
     float p = clampf(__fdividef(mu1, mu1 + mu0 + 1e-7f), kFEps, 1.0f - kFEps);
-    out[j] = (i0 + j < n_post) ? p * len[j] : 0.0f;
+    out[j] = (kWhole || i0 + j < n_post) ? p * len[j] : 0.0f;
   }
   constexpr int VW = KE % 4 == 0 ? 4 : KE;
 #pragma unroll
   for (int v = 0; v < KE / VW; ++v) {
     const int i = i0 + VW * v;
-    if (i >= k4 && i < n_post) {
+    if (i >= k4 && (kWhole || i < n_post)) {
       if constexpr (VW == 4)
         *reinterpret_cast<float4*>(inc_pl + off + i) =
             make_float4(out[4 * v], out[4 * v + 1], out[4 * v + 2], out[4 * v + 3]);
@@ -288,18 +317,25 @@ __device__ __forceinline__ Acc emit_slice(const float (&vmu)[KE], const float (&
         *reinterpret_cast<float2*>(inc_pl + off + i) = make_float2(out[2 * v], out[2 * v + 1]);
     }
   }
-  return carryF + (Acc)__shfl_sync(kFull, ex + run, 31);
+  return __shfl_sync(kFull, ex + run, 31);
 }
 
-// Pass-1 work of one slice: record the prefix values the ray needs and add
-// the lane's share of the Pre total
-template <int KE, typename Acc>
-__device__ __forceinline__ void pre_slice(const Slice<KE>& s, int base, int i0, int r0, int rinf, int k4,
-                                          float& Ar0, float& Arinf, float& Ak, Acc& Tl) {
+// Pass-1b bookkeeping of one slice (base >= 1): A_{r0-1} and A_{rinf-1}
+// where those positions fall inside it
+template <int KE>
+__device__ __forceinline__ void pre_marks(const Slice<KE>& s, int base, int r0, int rinf, float& Ar0,
+                                          float& Arinf) {
   constexpr int CH = 32 * KE;
-  if (r0 > 0 && r0 - 1 >= base && r0 - 1 < base + CH) Ar0 = slice_value<KE>(s, r0 - 1 - base);
-  if (rinf > 0 && rinf - 1 >= base && rinf - 1 < base + CH) Arinf = slice_value<KE>(s, rinf - 1 - base);
-  if (k4 > 0 && k4 - 1 >= base && k4 - 1 < base + CH) Ak = slice_value<KE>(s, k4 - 1 - base);
+  if (r0 - 1 >= base && r0 - 1 < base + CH) Ar0 = slice_value<KE>(s, r0 - 1 - base);
+  if (rinf - 1 >= base && rinf - 1 < base + CH) Arinf = slice_value<KE>(s, rinf - 1 - base);
+}
+
+// the lane's share of the Pre total from one slice that may hold non-zero
+// potentials, added to a compensated FP32 sum (ts, tc): the error of the
+// lane's sum stays at a few ulps however long the ray is
+template <int KE>
+__device__ __forceinline__ void pre_total(const Slice<KE>& s, int i0, int r0, float Ar0, float& ts,
+                                          float& tc) {
   // exp(-A_{r0-1}) rescales Post visibility to Pre visibility unless the
   // Post visibility may have underflowed (then exponentiate the difference)
   const bool direct = Ar0 < kUnderflowGuard;
@@ -312,7 +348,32 @@ __device__ __forceinline__ void pre_slice(const Slice<KE>& s, int base, int i0, 
       w += vp * (1.0f - __expf(s.lq[j])) * s.mu[j];
     }
   }
-  Tl += (Acc)w;
+  const float y = w - tc;
+  const float t = ts + y;
+  tc = (t - ts) - y;
+  ts = t;
+}
+
+// static-prefix sums of one lane's vector x (positions i0..i0+3, all inside
+// [0, k4)): the total and the parts before r0 and before rinf
+__device__ __forceinline__ void static_accum(const float (&x)[4], int i0, int r0, int rinf, float& sa,
+                                             float& sr0, float& srf) {
+  const float xs = ((x[0] + x[1]) + x[2]) + x[3];
+  sa += xs;
+  if (i0 + 4 <= r0) {
+    sr0 += xs;
+  } else if (i0 < r0) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if (i0 + j < r0) sr0 += x[j];
+  }
+  if (i0 + 4 <= rinf) {
+    srf += xs;
+  } else if (i0 < rinf) {
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if (i0 + j < rinf) srf += x[j];
+  }
 }
 
 template <typename Acc, int kPol, int kPf>
@@ -327,43 +388,108 @@ __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, const uint32_t* _
   const int kdyn = ray_kdyn(me);
   const int k4 = kdyn & ~3;
   const uint32_t off = me.off;
-  // ---- pass 1: prefixes, Pre total ---------------------------------------
-  // Chunks of 128 (a chunk costs the same instructions however many of its
-  // lanes hold incidences: measured against 256-incidence chunks and against
-  // 256-incidence chunks with 64- or 128-incidence tails, this was fastest).
-  float carryA = 0.0f, Ar0 = 0.0f, Arinf = 0.0f, Ak = 0.0f;
-  Acc T = 0, Tl = 0;
-  Slice<kE> s;
-  // kPf: the next chunk's pair ids are requested before this chunk's ln q
-  // gathers, so a chunk waits on one memory round trip instead of two.
-  uint32_t pid_next[kE];
-  if (kPf) load_pids<kE, kPol>(pid_next, off, kE * lane, n_pre, inc_pair);
-  for (int base = 0; base < n_pre; base += kChunk) {
-    const int i0 = base + kE * lane;
-    uint32_t pid[kE];
-    if (kPf) {
-#pragma unroll
-      for (int j = 0; j < kE; ++j) pid[j] = pid_next[j];
-      if (base + kChunk < n_pre) load_pids<kE, kPol>(pid_next, off, i0 + kChunk, n_pre, inc_pair);
-    } else {
-      load_pids<kE, kPol>(pid, off, i0, n_pre, inc_pair);
+  // ---- pass 1a: the static prefix [0, k4) --------------------------------
+  // No potential is non-zero before k_dyn, so pass 1 needs only sums of
+  // l ln q over [0, k4) -- to k4, and to r0 and rinf where those lie
+  // inside: per-lane sums with the next chunk's pair ids and lengths in
+  // flight, and one warp reduction per ray instead of a scan per chunk.
+  float carryA = 0.0f, Ar0 = 0.0f, Arinf = 0.0f;
+  {
+    float sa = 0.0f, sr0 = 0.0f, srf = 0.0f;
+    uint32_t pidn[kE];
+    float lenn[kE];
+    if (k4 > 0) {
+      ld_vec<kE, kPol>(pidn, inc_pair + off, kE * lane, kE * lane < k4);
+      ld_vec<kE, kPol>(lenn, inc_len + off, kE * lane, kE * lane < k4);
     }
-    float tot = slice_from_pids<kE, kPol>(s, pid, off, i0, n_pre, k4, carryA, lane, inc_len, inc_mu, lnq);
-    pre_slice<kE, Acc>(s, base, i0, r0, rinf, k4, Ar0, Arinf, Ak, Tl);
-    carryA += tot;
+    for (int base = 0; base < k4; base += kChunk) {
+      const int i0 = base + kE * lane;  // k4 is a multiple of 4: a lane's vector is all in or all out
+      uint32_t pid[kE];
+      float len[kE];
+#pragma unroll
+      for (int j = 0; j < kE; ++j) {
+        pid[j] = pidn[j];
+        len[j] = lenn[j];
+      }
+      if (base + kChunk < k4) {
+        ld_vec<kE, kPol>(pidn, inc_pair + off, i0 + kChunk, i0 + kChunk < k4);
+        ld_vec<kE, kPol>(lenn, inc_len + off, i0 + kChunk, i0 + kChunk < k4);
+      }
+      if (i0 < k4) {
+        float x[kE];
+#pragma unroll
+        for (int j = 0; j < kE; ++j) x[j] = len[j] * __ldg(lnq + pid[j]);
+        static_accum(x, i0, r0, rinf, sa, sr0, srf);
+      }
+    }
+    if (k4 > 0) {
+      carryA = warp_sum(sa);
+      if (r0 > 0 && r0 <= k4) Ar0 = warp_sum(sr0);
+      if (rinf > 0 && rinf <= k4) Arinf = warp_sum(srf);
+    }
   }
-  T = warp_sum(Tl);  // each lane's share of the Pre total, summed once per ray
+  const float Ak = carryA;  // A_{k4 - 1}
+  // ---- pass 1b: the dynamic range [k4, n_pre): prefixes, Pre total -------
+  // Chunks of 128 (a chunk costs the same instructions however many of its
+  // lanes hold incidences).  Chunks wholly inside the ray skip the bounds
+  // checks.  kPf 1: the next chunk's pair ids are requested before this
+  // chunk's ln q gathers; kPf 2: its lengths as well.
+  float ts = 0.0f, tc = 0.0f;
+  Slice<kE> s;
+  {
+    uint32_t pid_next[kE];
+    float len_next[kE], len[kE];
+    if (kPf && k4 < n_pre) load_pids<kE, kPol>(pid_next, off, k4 + kE * lane, n_pre, inc_pair);
+    if (kPf == 2 && k4 < n_pre)
+      ld_vec<kE, kPol>(len_next, inc_len + off, k4 + kE * lane, k4 + kE * lane < n_pre);
+    for (int base = k4; base < n_pre; base += kChunk) {
+      const int i0 = base + kE * lane;
+      uint32_t pid[kE];
+      if (kPf) {
+#pragma unroll
+        for (int j = 0; j < kE; ++j) pid[j] = pid_next[j];
+        if (kPf == 2) {
+#pragma unroll
+          for (int j = 0; j < kE; ++j) len[j] = len_next[j];
+        }
+        if (base + kChunk < n_pre) {
+          load_pids<kE, kPol>(pid_next, off, i0 + kChunk, n_pre, inc_pair);
+          if (kPf == 2) ld_vec<kE, kPol>(len_next, inc_len + off, i0 + kChunk, i0 + kChunk < n_pre);
+        }
+      } else {
+        load_pids<kE, kPol>(pid, off, i0, n_pre, inc_pair);
+      }
+      const float tot =
+          base + kChunk <= n_pre
+              ? slice_from_pids<kE, kPol, true, kPf == 2>(s, pid, off, i0, n_pre, k4, carryA, lane, inc_len,
+                                                          inc_mu, lnq, len)
+              : slice_from_pids<kE, kPol, false, kPf == 2>(s, pid, off, i0, n_pre, k4, carryA, lane,
+                                                           inc_len, inc_mu, lnq, len);
+      pre_marks<kE>(s, base, r0, rinf, Ar0, Arinf);
+      pre_total<kE>(s, i0, r0, Ar0, ts, tc);
+      carryA += tot;
+    }
+  }
+  // the lanes' compensated shares, summed in Acc once per ray (FP64 on
+  // rays longer than kLongRay)
+  Acc T = warp_sum((Acc)ts - (Acc)tc);
   // infinity term: visibility at the end of Pre (gvdbkernels.cu:1196-1208)
   if (me.flags & 1u) T += (Acc)__expf(carryA - Arinf);
   if (kdyn >= n_post) return;  // every message of the ray is static
   // ---- pass 2: dynamic messages ------------------------------------------
-  // F is zero before k_dyn, so the running F starts at zero at k4
-  Acc carryF = 0;
+  // F is zero before k_dyn, so the running F starts at zero at k4; the
+  // long-range difference T - F is carried in Acc, one subtraction per chunk
+  Acc Dd = T;
+  float cF = 0.0f;
   float carryA2 = Ak;
   for (int base = k4; base < n_post; base += kChunk) {
     const int i0 = base + kE * lane;
-    float tot2 = load_slice<kE, kPol>(s, off, i0, n_post, k4, carryA2, lane, inc_pair, inc_len, inc_mu,
-                                      lnq);
+    const bool full = base + kChunk <= n_post;
+    const float tot2 =
+        full ? load_slice<kE, kPol, true>(s, off, i0, n_post, k4, carryA2, lane, inc_pair, inc_len, inc_mu,
+                                          lnq)
+             : load_slice<kE, kPol, false>(s, off, i0, n_post, k4, carryA2, lane, inc_pair, inc_len,
+                                           inc_mu, lnq);
     carryA2 += tot2;
     float vmu[kE], q[kE];
 #pragma unroll
@@ -371,20 +497,31 @@ __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, const uint32_t* _
       vmu[j] = __expf(s.A[j]) * s.mu[j];
       q[j] = __expf(s.lq[j]);
     }
-    carryF = emit_slice<kE, Acc>(vmu, q, s.len, i0, k4, n_post, T, carryF, lane, off, inc_pl);
+    const float D = (float)Dd;
+    const float ct = full ? emit_slice<kE, true>(vmu, q, s.len, i0, k4, n_post, cF, D, lane, off, inc_pl)
+                          : emit_slice<kE, false>(vmu, q, s.len, i0, k4, n_post, cF, D, lane, off, inc_pl);
+    Dd -= (Acc)ct;
+    cF += ct;
   }
 }
 
-// Persistent launch: each warp takes the next ray from a work counter; rays
-// are queued longest first (sorted once per incidence build), so the long
-// rays start early and the short ones fill the tail.  Which warp handles a
-// ray does not change its result.  Variants differ only in register budget
-// (kMinBlocks resident blocks per SM) and load policy: their arithmetic is
-// identical, so the autotuner's choice never changes a result.
-template <int kMinBlocks, int kPol, int kPf>
-__global__ void __launch_bounds__(kRayWarps * 32, kMinBlocks) k_ray_bp(const RayMeta* __restrict__ meta,
-                                                           const uint32_t* __restrict__ order,
+// Persistent launch.  Longest-first queue (kTiles false): each warp takes
+// the next ray from a work counter; rays are queued longest first (sorted
+// once per incidence build, their RayMeta records copied into queue order),
+// so the long rays start early and the short ones fill the tail.  Tile
+// queue (kTiles true): a block takes the next 8x8 pixel tile (tiles queued
+// by total length, longest first) and its warps take the tile's rays in
+// pixel order, so the block's warps trace neighbouring rays at the same
+// time -- rays that cross the same voxels, whose ln q gathers then share L1
+// lines.  Which warp handles a ray does not change its result.  Variants
+// differ only in register budget (kMinBlocks resident blocks per SM), load
+// policy and scheduling: their arithmetic is identical, so the autotuner's
+// choice never changes a result.
+template <int kMinBlocks, int kPol, int kPf, bool kTiles>
+__global__ void __launch_bounds__(kRayWarps * 32, kMinBlocks) k_ray_bp(const RayMeta* __restrict__ queue,
                                                            uint32_t n_rays,
+                                                           const uint2* __restrict__ tiles,
+                                                           uint32_t n_tiles,
                                                            uint32_t* __restrict__ counter,
                                                            const uint32_t* __restrict__ inc_pair,
                                                            const float* __restrict__ inc_len,
@@ -393,17 +530,43 @@ __global__ void __launch_bounds__(kRayWarps * 32, kMinBlocks) k_ray_bp(const Ray
                                                            float* __restrict__ inc_pl,
                                                            int fix_reset) {
   const int lane = threadIdx.x & 31;
-  for (;;) {
-    uint32_t idx = 0;
-    if (lane == 0) idx = atomicAdd(counter, 1u);
-    idx = __shfl_sync(kFull, idx, 0);
-    if (idx >= n_rays) break;
-    RayMeta me = meta[order[idx]];
+  auto ray = [&](const RayMeta& me) {
     if (me.n_pre <= kLongRay)
       ray_bp_warp<float, kPol, kPf>(me, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
     else
       ray_bp_warp<double, kPol, kPf>(me, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
+  };
+  if constexpr (kTiles) {
+    __shared__ uint2 s_tile;
+    const uint32_t warp = threadIdx.x >> 5;
+    for (;;) {
+      if (threadIdx.x == 0) {
+        const uint32_t t = atomicAdd(counter, 1u);
+        s_tile = t < n_tiles ? tiles[t] : make_uint2(0u, 0u);  // (first ray, rays); 0 rays: done
+      }
+      __syncthreads();
+      const uint2 tl = s_tile;
+      __syncthreads();  // read by every warp before thread 0 takes the next tile
+      if (tl.y == 0) break;
+      for (uint32_t r = warp; r < tl.y; r += kRayWarps) ray(queue[tl.x + r]);
+    }
+  } else {
+    for (;;) {
+      uint32_t idx = 0;
+      if (lane == 0) idx = atomicAdd(counter, 1u);
+      idx = __shfl_sync(kFull, idx, 0);
+      if (idx >= n_rays) break;
+      ray(queue[idx]);
+    }
   }
+}
+
+// queue records: queue[i] = meta[base + order[i]] (order: view-local ray
+// indices, longest first)
+__global__ void k_ray_queue(const RayMeta* __restrict__ meta, const uint32_t* __restrict__ order,
+                            uint32_t n, RayMeta* __restrict__ queue) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) queue[i] = meta[order[i]];
 }
 
 // ray queue of one build: active rays sorted by decreasing length
@@ -753,11 +916,6 @@ __global__ void k_remap_gather(const uint32_t* __restrict__ pv, float* __restric
   if (p < n) m[p] = dense[pv[p]];
 }
 
-__global__ void k_add_u32(uint32_t* p, uint32_t n, uint32_t v) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) p[i] += v;
-}
-
 __global__ void k_fill_u32(uint32_t* p, int64_t n, uint32_t v) {
   int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) p[i] = v;
@@ -796,22 +954,29 @@ cudaError_t launch_pair_prepare(const BpArrays& a, uint32_t p0, uint32_t p1, int
                                 cudaStream_t s) {
   if (p1 <= p0) return cudaSuccess;
   k_pair_prepare<<<blocks(p1 - p0, kPrepThreads * kPrepPer), kPrepThreads, 0, s>>>(
-      a.pair_vox, a.pair_m, a.L, a.pair_lnq, jacobi ? a.pair_dm : nullptr, p0, p1);
+      a.pair_vox, a.pair_m, a.L, a.pair_lnv, jacobi ? a.pair_dm : nullptr, p0, p1);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  k_lnq_slots<<<blocks(p1 - p0, 256 * 4), 256, 0, s>>>(a.pair_of_slot, a.pair_lnv, a.pair_lnq, p0, p1);
   return cudaGetLastError();
 }
 
 
-// ray-kernel variants: (id, resident-block target, load policy, pair-id prefetch)
-#define MRF_RAY_VARIANTS(X) X(0, 0, 0, 0) X(1, 0, 1, 0) X(2, 0, 0, 1) X(3, 0, 1, 1)
-constexpr int kRayVariants = 4;
+// ray-kernel variants: (id, resident-block target, load policy, chunk
+// prefetch, tile queue)
+#define MRF_RAY_VARIANTS(X) \
+  X(0, 0, 0, 0, false) X(1, 0, 0, 1, false) X(2, 0, 0, 2, false) X(3, 0, 0, 0, true) X(4, 0, 0, 1, true) \
+  X(5, 0, 0, 2, true)
+constexpr int kRayVariants = 6;
+constexpr bool kRayTiles[kRayVariants] = {false, false, false, true, true, true};
 
 int ray_bp_variants() { return kRayVariants; }
 
 namespace {
-template <int kMinBlocks, int kPol, int kPf>
-int resident_of() {
+template <typename K>
+int resident_of(K kernel) {
   int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_ray_bp<kMinBlocks, kPol, kPf>,
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel,
                                                     kRayWarps * 32, 0) != cudaSuccess ||
       per_sm < 1)
     per_sm = 1;
@@ -824,9 +989,9 @@ int ray_bp_resident_blocks(int variant) {
   if (variant < 0 || variant >= kRayVariants) return 1;
   if (!resident[variant]) {
     switch (variant) {
-#define X(id, mb, pol, pf) \
-  case id:                 \
-    resident[variant] = resident_of<mb, pol, pf>(); \
+#define X(id, mb, pol, pf, tl) \
+  case id:                     \
+    resident[variant] = resident_of(k_ray_bp<mb, pol, pf, tl>); \
     break;
       MRF_RAY_VARIANTS(X)
 #undef X
@@ -835,19 +1000,21 @@ int ray_bp_resident_blocks(int variant) {
   return resident[variant];
 }
 
-cudaError_t launch_ray_bp(const BpArrays& a, const uint32_t* order, uint32_t n_rays,
-                          uint32_t* counter, int fix_reset, int num_sms, int variant, cudaStream_t s) {
-  if (!n_rays) return cudaSuccess;
+cudaError_t launch_ray_bp(const BpArrays& a, const RayWork& w, uint32_t* counter, int fix_reset,
+                          int num_sms, int variant, cudaStream_t s) {
   if (variant < 0 || variant >= kRayVariants) return cudaErrorInvalidValue;
-  int64_t b = std::min<int64_t>((int64_t)num_sms * ray_bp_resident_blocks(variant),
-                                (n_rays + kRayWarps - 1) / kRayWarps);
+  const bool tiled = kRayTiles[variant];
+  const int64_t need = tiled ? w.n_tiles : (w.n_rays + kRayWarps - 1) / kRayWarps;
+  if (need == 0) return cudaSuccess;
+  int64_t b = std::min<int64_t>((int64_t)num_sms * ray_bp_resident_blocks(variant), need);
   const unsigned grid = (unsigned)std::max<int64_t>(b, 1);
+  const RayMeta* q = tiled ? w.tile_queue : w.queue;
   switch (variant) {
-#define X(id, mb, pol, pf)                                                                        \
+#define X(id, mb, pol, pf, tl)                                                                     \
   case id:                                                                                        \
-    k_ray_bp<mb, pol, pf><<<grid, kRayWarps * 32, 0, s>>>(a.meta, order, n_rays, counter, a.inc_pair, \
-                                                          a.inc_len, a.inc_mu, a.pair_lnq,          \
-                                                          a.inc_pl, fix_reset);                    \
+    k_ray_bp<mb, pol, pf, tl><<<grid, kRayWarps * 32, 0, s>>>(q, w.n_rays, w.tiles, w.n_tiles, counter, \
+                                                              a.inc_pair, a.inc_len, a.inc_mu,      \
+                                                              a.pair_lnq, a.inc_pl, fix_reset);     \
     break;
     MRF_RAY_VARIANTS(X)
 #undef X
@@ -859,6 +1026,13 @@ cudaError_t launch_ray_keys(const RayMeta* meta, uint32_t n, uint32_t* keys, uin
                             cudaStream_t s) {
   if (!n) return cudaSuccess;
   k_ray_keys<<<blocks(n, 256), 256, 0, s>>>(meta, n, keys, vals);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ray_queue(const RayMeta* meta, const uint32_t* order, uint32_t n, RayMeta* queue,
+                             cudaStream_t s) {
+  if (!n) return cudaSuccess;
+  k_ray_queue<<<blocks(n, 256), 256, 0, s>>>(meta, order, n, queue);
   return cudaGetLastError();
 }
 
@@ -963,12 +1137,6 @@ cudaError_t launch_remap_gather(const uint32_t* pair_vox, float* pair_m, uint32_
                                 const float* dense, cudaStream_t s) {
   if (!n) return cudaSuccess;
   k_remap_gather<<<blocks(n, 256), 256, 0, s>>>(pair_vox, pair_m, n, dense);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_add_u32(uint32_t* p, uint32_t n, uint32_t v, cudaStream_t s) {
-  if (!n) return cudaSuccess;
-  k_add_u32<<<blocks(n, 256), 256, 0, s>>>(p, n, v);
   return cudaGetLastError();
 }
 

@@ -281,15 +281,33 @@ __global__ void k_pairs_from_sorted(const uint32_t* __restrict__ sk, const uint3
                                     const uint32_t* __restrict__ scan, uint32_t n,
                                     uint32_t pair_base, uint32_t perm_base, uint32_t inc_base,
                                     uint32_t* __restrict__ pair_vox, uint32_t* __restrict__ seg,
-                                    uint32_t* __restrict__ inc_pair) {
+                                    const uint32_t* __restrict__ slot, uint32_t* __restrict__ inc_pair) {
   uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
   uint32_t p = pair_base + scan[k] + flag[k] - 1;
-  if (flag[k]) {
+  if (pair_vox && flag[k]) {
     pair_vox[p] = sk[k];
     seg[p] = perm_base + k;
   }
-  inc_pair[inc_base + sidx[k]] = p;
+  if (inc_pair) inc_pair[inc_base + sidx[k]] = slot[p];
+}
+
+// ln q slots by first visit: key[p] = the first incidence of pair p (its
+// first sorted position, the voxel sort being stable); after the pairs are
+// sorted by key, slot[pair_base + order[q]] = pair_base + q (and the
+// inverse), and every incidence carries its pair's slot
+__global__ void k_pair_first(const uint32_t* __restrict__ seg, uint32_t np, uint32_t perm_base,
+                             const uint32_t* __restrict__ sidx, uint32_t* __restrict__ key) {
+  uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < np) key[p] = sidx[seg[p] - perm_base];
+}
+
+__global__ void k_pair_slots(const uint32_t* __restrict__ order, uint32_t np, uint32_t pair_base,
+                             uint32_t* __restrict__ slot, uint32_t* __restrict__ pair_of_slot) {
+  uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= np) return;
+  slot[pair_base + order[q]] = pair_base + q;
+  pair_of_slot[pair_base + q] = pair_base + order[q];
 }
 
 // build records in pair-grouped (sorted) order: one gather per position
@@ -490,10 +508,25 @@ cudaError_t launch_vox_heads(const uint32_t* sk, uint32_t n, uint32_t* flag, cud
 cudaError_t launch_pairs_from_sorted(const uint32_t* sk, const uint32_t* sidx, const uint32_t* flag,
                                      const uint32_t* scan, uint32_t n, uint32_t pair_base,
                                      uint32_t perm_base, uint32_t inc_base, uint32_t* pair_vox,
-                                     uint32_t* seg, uint32_t* inc_pair, cudaStream_t s) {
+                                     uint32_t* seg, const uint32_t* slot, uint32_t* inc_pair,
+                                     cudaStream_t s) {
   if (!n) return cudaSuccess;
   k_pairs_from_sorted<<<grid_for(n), kThreads, 0, s>>>(sk, sidx, flag, scan, n, pair_base, perm_base,
-                                                       inc_base, pair_vox, seg, inc_pair);
+                                                       inc_base, pair_vox, seg, slot, inc_pair);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pair_first(const uint32_t* seg, uint32_t np, uint32_t perm_base, const uint32_t* sidx,
+                              uint32_t* key, cudaStream_t s) {
+  if (!np) return cudaSuccess;
+  k_pair_first<<<grid_for(np), kThreads, 0, s>>>(seg, np, perm_base, sidx, key);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pair_slots(const uint32_t* order, uint32_t np, uint32_t pair_base, uint32_t* slot,
+                              uint32_t* pair_of_slot, cudaStream_t s) {
+  if (!np) return cudaSuccess;
+  k_pair_slots<<<grid_for(np), kThreads, 0, s>>>(order, np, pair_base, slot, pair_of_slot);
   return cudaGetLastError();
 }
 

@@ -91,6 +91,7 @@ struct View {
   uint32_t dperm_base = 0, n_dperm = 0;   // ... of the dynamic ones
   uint32_t dpair_base = 0, n_dpairs = 0;  // runs of dynamic incidences (one per pair)
   uint32_t order_base = 0, n_active = 0;  // ray queue (longest first)
+  uint32_t tiles_base = 0, n_tiles = 0;   // tile-queue descriptors (8x8 pixel tiles)
   uint32_t tile_base = 0;                 // first pair of each pair-update tile
 };
 
@@ -113,11 +114,13 @@ struct mrf_map {
   std::vector<int> h_coord;
   int version = 0, built_version = -1;
   int ray_variant = 0;  // ray-kernel variant (mrf_autotune / mrf_set_ray_variant)
+  uint32_t n_tiles_all = 0;  // tile-queue descriptors of all views
   bool has_messages = false;
   std::vector<View> views;
   // arenas
   DBuf meta, inc_pair, inc_len, inc_mu, inc_pl, pair_vox, pair_m, pair_cum, pair_stat, pair_ndyn, pair_hit,
-      pair_q, pair_dm, pair_seg, dperm, dpair, dseg, drun, carry, ray_order, counters, tile_first;
+      pair_q, pair_dm, pair_seg, pair_lq, pair_of_slot, pair_lnv, dperm, dpair, dseg, drun, carry, ray_order, ray_queue, tile_queue, tiles, counters,
+      tile_first;
   uint32_t jac_tile_base = 0;
   int64_t n_inc = 0, n_pairs = 0, n_dperm = 0, n_dpairs = 0;
   // jacobi voxel CSR
@@ -156,6 +159,8 @@ struct mrf_map {
     a.pair_stat = pair_stat.as<float>();
     a.pair_ndyn = pair_ndyn.as<uint32_t>();
     a.pair_lnq = pair_q.as<float>();
+    a.pair_lnv = pair_lnv.as<float>();
+    a.pair_of_slot = pair_of_slot.as<uint32_t>();
     a.pair_dm = pair_dm.as<float>();
     a.L = d_L.as<float>();
     a.belief = d_belief.as<float>();
@@ -318,7 +323,8 @@ void rebuild(mrf_map* m) {
     for (int c = 0; c < V; ++c) npre += nreal[c];
   }
   // 4. pairs per view in voxel order: sort the view's incidences by voxel
-  //    (stable), one pair per run; pos[i] = pair-grouped position of i
+  //    (stable), one pair per run; pos[i] = pair-grouped position of i.
+  //    The pairs' ln q slots are numbered by first visit (see below).
   int bits = 1;
   while (bits < 32 && ((uint64_t)1 << bits) <= (uint64_t)(m->n_bricks * kBrickVox)) ++bits;
   int64_t pair_total = 0, perm_total = 0, dperm_total = 0, dpair_total = 0;
@@ -345,10 +351,10 @@ void rebuild(mrf_map* m) {
     // padding incidences carry kNoVoxel, whose low bits exceed every voxel id
     CK(sort_pairs_u32(m->s_tmp.p, t2, m->s_vox.as<uint32_t>() + v.inc_base, m->s_k1.as<uint32_t>(),
                       m->s_v0.as<uint32_t>(), m->s_v1.as<uint32_t>(), n, bits, m->stream));
-    CK(launch_vox_heads(m->s_k1.as<uint32_t>(), nr, m->s_k0.as<uint32_t>(), m->stream));
-    CK(cudaMemsetAsync(m->s_k0.as<uint32_t>() + nr, 0, 4, m->stream));
     size_t t1 = scan_temp_bytes(nr + 1);
     m->s_tmp.reserve(t1, false, m->stream);
+    CK(launch_vox_heads(m->s_k1.as<uint32_t>(), nr, m->s_k0.as<uint32_t>(), m->stream));
+    CK(cudaMemsetAsync(m->s_k0.as<uint32_t>() + nr, 0, 4, m->stream));
     CK(exclusive_scan_u32(m->s_tmp.p, t1, m->s_k0.as<uint32_t>(), m->s_v0.as<uint32_t>(), nr + 1,
                           m->stream));
     uint32_t np = read1(m, m->s_v0.as<uint32_t>() + nr);
@@ -361,11 +367,38 @@ void rebuild(mrf_map* m) {
     m->pair_ndyn.reserve(pb * 4, true, m->stream);
     m->pair_hit.reserve(pb * 4, true, m->stream);
     m->pair_seg.reserve(pb * 4, true, m->stream);
+    m->pair_lq.reserve(pb * 4, true, m->stream);
+    m->pair_of_slot.reserve(pb * 4, true, m->stream);
     CK(launch_pairs_from_sorted(m->s_k1.as<uint32_t>(), m->s_v1.as<uint32_t>(), m->s_k0.as<uint32_t>(),
                                 m->s_v0.as<uint32_t>(), nr, v.pair_base, v.perm_base, v.inc_base,
-                                m->pair_vox.as<uint32_t>(), m->pair_seg.as<uint32_t>(),
-                                m->inc_pair.as<uint32_t>(), m->stream));
+                                m->pair_vox.as<uint32_t>(), m->pair_seg.as<uint32_t>(), nullptr, nullptr,
+                                m->stream));
     CK(launch_fill_u32(m->pair_seg.as<uint32_t>() + v.pair_base + np, 1, v.perm_base + nr, m->stream));
+    // ln q slots by first visit: the pairs ordered by their first incidence
+    // (pixel order, then along the ray; a pair's first sorted position holds
+    // it, the voxel sort being stable).  Rays of neighbouring pixels cross
+    // the same voxels in the same order, so the slots met along a ray come
+    // in runs of consecutive indices and the ray kernel's ln q gathers share
+    // sectors.  The pairs stay in voxel order; the incidences carry slots.
+    {
+      m->s_pf.reserve((size_t)np * 4 + 4, false, m->stream);
+      m->s_ps.reserve((size_t)np * 4 + 4, false, m->stream);
+      m->s_recs.reserve((size_t)nr * 8, false, m->stream);
+      CK(launch_pair_first(m->pair_seg.as<uint32_t>() + v.pair_base, np, v.perm_base, m->s_v1.as<uint32_t>(),
+                           m->s_k1.as<uint32_t>(), m->stream));
+      CK(launch_iota(m->s_ps.as<uint32_t>(), np, m->stream));
+      int ibits = 1;
+      while (ibits < 32 && ((uint64_t)1 << ibits) < (uint64_t)n) ++ibits;
+      size_t t4 = sort_temp_bytes(np, ibits);
+      m->s_tmp.reserve(t4, false, m->stream);
+      CK(sort_pairs_u32(m->s_tmp.p, t4, m->s_k1.as<uint32_t>(), m->s_recs.as<uint32_t>(),
+                        m->s_ps.as<uint32_t>(), m->s_pf.as<uint32_t>(), np, ibits, m->stream));
+      CK(launch_pair_slots(m->s_pf.as<uint32_t>(), np, v.pair_base, m->pair_lq.as<uint32_t>(),
+                           m->pair_of_slot.as<uint32_t>(), m->stream));
+      CK(launch_pairs_from_sorted(nullptr, m->s_v1.as<uint32_t>(), m->s_k0.as<uint32_t>(),
+                                  m->s_v0.as<uint32_t>(), nr, v.pair_base, v.perm_base, v.inc_base, nullptr,
+                                  nullptr, m->pair_lq.as<uint32_t>(), m->inc_pair.as<uint32_t>(), m->stream));
+    }
     m->s_recs.reserve((size_t)nr * 8, false, m->stream);
     CK(launch_gather_rec(m->s_v1.as<uint32_t>(), nr, v.inc_base, m->s_rec.as<float2>(),
                          m->s_recs.as<float2>(), m->stream));
@@ -413,6 +446,7 @@ void rebuild(mrf_map* m) {
     int64_t hw_max = 0;
     for (const View& v : m->views) hw_max = std::max<int64_t>(hw_max, (int64_t)v.cam.rows * v.cam.cols);
     m->ray_order.reserve((size_t)std::max<int64_t>(npix, 1) * 4, false, m->stream);
+    m->ray_queue.reserve((size_t)std::max<int64_t>(npix, 1) * sizeof(RayMeta), false, m->stream);
     m->s_k0.reserve((size_t)hw_max * 4 + 4, false, m->stream);
     m->s_k1.reserve((size_t)hw_max * 4 + 4, false, m->stream);
     m->s_v0.reserve((size_t)hw_max * 4 + 4, false, m->stream);
@@ -431,11 +465,60 @@ void rebuild(mrf_map* m) {
       CK(sort_pairs_u32(m->s_tmp.p, t, m->s_k0.as<uint32_t>(), m->s_k1.as<uint32_t>(),
                         m->s_v0.as<uint32_t>(), m->ray_order.as<uint32_t>() + base, (uint32_t)hw, 17,
                         m->stream));
-      // queue entries are global ray indices
-      CK(launch_add_u32(m->ray_order.as<uint32_t>() + base, (uint32_t)act, (uint32_t)v.pix_base, m->stream));
+      // queue records in queue order
+      CK(launch_ray_queue(m->meta.as<RayMeta>() + v.pix_base, m->ray_order.as<uint32_t>() + base,
+                          (uint32_t)act, m->ray_queue.as<RayMeta>() + base, m->stream));
       base += act;
     }
     m->counters.reserve((size_t)(V + 1) * 4, false, m->stream);
+    // tile queue: per view the 8x8 pixel tiles that hold active rays, by
+    // total Pre length (longest first, ties by tile index), each with its
+    // active rays in pixel order
+    std::vector<uint32_t> torder;
+    std::vector<uint2> tdesc;
+    torder.reserve((size_t)base);
+    for (int c = 0; c < V; ++c) {
+      View& v = m->views[c];
+      const int rows = v.cam.rows, cols = v.cam.cols;
+      const int tx = (cols + kRayTile - 1) / kRayTile, ty = (rows + kRayTile - 1) / kRayTile;
+      std::vector<std::pair<int64_t, int>> order;  // (-length, tile)
+      for (int t = 0; t < tx * ty; ++t) {
+        const int x0 = (t % tx) * kRayTile, y0 = (t / tx) * kRayTile;
+        int64_t len = 0;
+        for (int y = y0; y < std::min(y0 + kRayTile, rows); ++y)
+          for (int x = x0; x < std::min(x0 + kRayTile, cols); ++x)
+            len += hm[(size_t)(v.pix_base + (int64_t)y * cols + x)].n_pre;
+        if (len) order.emplace_back(-len, t);
+      }
+      std::sort(order.begin(), order.end());
+      v.tiles_base = (uint32_t)tdesc.size();
+      for (const auto& o : order) {
+        const int t = o.second;
+        const int x0 = (t % tx) * kRayTile, y0 = (t / tx) * kRayTile;
+        const uint32_t first = (uint32_t)torder.size();
+        for (int y = y0; y < std::min(y0 + kRayTile, rows); ++y)
+          for (int x = x0; x < std::min(x0 + kRayTile, cols); ++x) {
+            const int64_t pix = v.pix_base + (int64_t)y * cols + x;
+            if (hm[(size_t)pix].n_pre > 0) torder.push_back((uint32_t)pix);
+          }
+        tdesc.push_back(make_uint2(first, (uint32_t)torder.size() - first));
+      }
+      v.n_tiles = (uint32_t)tdesc.size() - v.tiles_base;
+    }
+    const size_t nq = std::max<size_t>(torder.size(), 1);
+    m->tile_queue.reserve(nq * sizeof(RayMeta), false, m->stream);
+    m->tiles.reserve(std::max<size_t>(tdesc.size(), 1) * sizeof(uint2), false, m->stream);
+    if (!torder.empty()) {
+      // ray_order is free again once the longest-first queues are gathered
+      CK(cudaMemcpyAsync(m->ray_order.p, torder.data(), torder.size() * 4, cudaMemcpyHostToDevice,
+                         m->stream));
+      CK(launch_ray_queue(m->meta.as<RayMeta>(), m->ray_order.as<uint32_t>(), (uint32_t)torder.size(),
+                          m->tile_queue.as<RayMeta>(), m->stream));
+      CK(cudaMemcpyAsync(m->tiles.p, tdesc.data(), tdesc.size() * sizeof(uint2), cudaMemcpyHostToDevice,
+                         m->stream));
+      sync(m);  // the host vectors go out of scope
+    }
+    m->n_tiles_all = (uint32_t)tdesc.size();
   }
   m->n_inc = n_inc;
   m->n_pairs = pair_total;
@@ -456,6 +539,7 @@ void rebuild(mrf_map* m) {
   CK(launch_drun(m->dpair.as<uint32_t>(), (uint32_t)dpair_total, m->pair_vox.as<uint32_t>(),
                  m->pair_cum.as<float>(), m->pair_stat.as<float>(), m->drun.as<uint4>(), m->stream));
   m->pair_q.reserve(pb * 4, false, m->stream);
+  m->pair_lnv.reserve(pb * 4, false, m->stream);
   m->pair_dm.reserve(pb * 4, false, m->stream);
   CK(launch_fill_f32(m->pair_m.as<float>(), pair_total, 0.0f, m->stream));
   {
@@ -593,6 +677,18 @@ struct Profiler {
 // pairs without dynamic incidences get their (constant) update in the first
 // iteration of each mrf_infer call only: afterwards it would leave every
 // value unchanged (L + (m_new - m_new) = L).
+// the rays of one view, and of all views (their queues are contiguous)
+RayWork view_work(mrf_map* m, const View& v) {
+  return RayWork{m->ray_queue.as<RayMeta>() + v.order_base, v.n_active, m->tile_queue.as<RayMeta>(),
+                 m->tiles.as<uint2>() + v.tiles_base, v.n_tiles};
+}
+RayWork all_work(mrf_map* m) {
+  uint32_t nact = 0;
+  for (const View& v : m->views) nact += v.n_active;
+  return RayWork{m->ray_queue.as<RayMeta>(), nact, m->tile_queue.as<RayMeta>(), m->tiles.as<uint2>(),
+                 m->n_tiles_all};
+}
+
 void enqueue_iteration(mrf_map* m, const BpArrays& a, bool jacobi, int fix, bool first,
                        Profiler& prof, int64_t& launches) {
   const int V = (int)m->views.size();
@@ -605,8 +701,8 @@ void enqueue_iteration(mrf_map* m, const BpArrays& a, bool jacobi, int fix, bool
       CK(launch_pair_prepare(a, v.pair_base, v.pair_base + v.n_pairs, 0, m->stream));
       prof.end();
       prof.begin(1);
-      CK(launch_ray_bp(a, m->ray_order.as<uint32_t>() + v.order_base, v.n_active,
-                       m->counters.as<uint32_t>() + c, fix, m->num_sms, m->ray_variant, m->stream));
+      CK(launch_ray_bp(a, view_work(m, v), m->counters.as<uint32_t>() + c, fix, m->num_sms, m->ray_variant,
+                       m->stream));
       prof.end();
       prof.begin(2);
       if (v.n_dperm) {
@@ -620,7 +716,7 @@ void enqueue_iteration(mrf_map* m, const BpArrays& a, bool jacobi, int fix, bool
         ++launches;
       }
       prof.end();
-      launches += 2;
+      launches += 3;  // prepare (two kernels) and the ray kernel
     }
   } else {
     uint32_t P = (uint32_t)m->n_pairs;
@@ -629,10 +725,8 @@ void enqueue_iteration(mrf_map* m, const BpArrays& a, bool jacobi, int fix, bool
     prof.end();
     prof.begin(1);
     // the queues of all views are contiguous: one launch over all rays
-    uint32_t nact = 0;
-    for (const View& v : m->views) nact += v.n_active;
-    CK(launch_ray_bp(a, m->ray_order.as<uint32_t>(), nact, m->counters.as<uint32_t>() + V, fix,
-                     m->num_sms, m->ray_variant, m->stream));
+    CK(launch_ray_bp(a, all_work(m), m->counters.as<uint32_t>() + V, fix, m->num_sms, m->ray_variant,
+                     m->stream));
     prof.end();
     prof.begin(2);
     CK(launch_pair_update(a, 0, (uint32_t)m->n_dperm, 0, (uint32_t)m->n_dpairs,
@@ -645,7 +739,7 @@ void enqueue_iteration(mrf_map* m, const BpArrays& a, bool jacobi, int fix, bool
                           m->n_vvox, m->pair_dm.as<float>(), m->d_L.as<float>(),
                           m->d_belief.as<float>(), m->stream));
     prof.end();
-    launches += 5 + (first ? 1 : 0);
+    launches += 6 + (first ? 1 : 0);
   }
 }
 
@@ -825,8 +919,8 @@ void destroy_bufs(mrf_map* m) {
                  &m->meta, &m->inc_pair, &m->inc_len, &m->inc_mu, &m->inc_pl, &m->pair_vox,
                  &m->pair_m, &m->pair_cum, &m->pair_stat, &m->pair_ndyn, &m->pair_hit, &m->pair_q,
                  &m->pair_dm,
-                 &m->pair_seg, &m->dperm, &m->dpair, &m->dseg, &m->drun,
-                 &m->carry, &m->ray_order, &m->counters, &m->tile_first,
+                 &m->pair_seg, &m->pair_lq, &m->pair_of_slot, &m->pair_lnv, &m->dperm, &m->dpair, &m->dseg, &m->drun,
+                 &m->carry, &m->ray_order, &m->ray_queue, &m->tile_queue, &m->tiles, &m->counters, &m->tile_first,
                  &m->vseg, &m->vpairs, &m->vvox, &m->s_rec, &m->s_recs, &m->s_pf, &m->s_ps,
                  &m->s_flags, &m->s_ind, &m->s_scan,
                  &m->s_tmp, &m->s_counts, &m->s_offs, &m->s_vox, &m->s_k0, &m->s_k1, &m->s_v0,
@@ -1104,13 +1198,11 @@ static void warm_start_impl(mrf_map* m, const float* L_pred, bool device_ptr, in
   BpArrays a = m->bp();
   const int V = (int)m->views.size();
   const uint32_t P = (uint32_t)m->n_pairs;
-  uint32_t nact = 0;
-  for (const View& v : m->views) nact += v.n_active;
   for (int k = 0; k < sweeps; ++k) {
     CK(cudaMemsetAsync(m->counters.p, 0, (size_t)(V + 1) * 4, m->stream));
     CK(launch_pair_prepare(a, 0, P, 1, m->stream));
-    CK(launch_ray_bp(a, m->ray_order.as<uint32_t>(), nact, m->counters.as<uint32_t>() + V, 0,
-                     m->num_sms, m->ray_variant, m->stream));
+    CK(launch_ray_bp(a, all_work(m), m->counters.as<uint32_t>() + V, 0, m->num_sms, m->ray_variant,
+                     m->stream));
     CK(launch_pair_update(a, 0, (uint32_t)m->n_dperm, 0, (uint32_t)m->n_dpairs,
                           m->tile_first.as<uint32_t>() + m->jac_tile_base, m->carry.as<TileCarry>(),
                           1, m->stream));
@@ -1608,24 +1700,29 @@ mrf_status mrf_view_incidences(mrf_map* m, int view_id, int* meta, uint32_t* vox
     if (cap <= 0 || v.n_inc == 0 || (!len && !mu && !vox)) return;
     // device lists are padded per ray: copy the view's range, then compact
     std::vector<float> hl(v.n_inc), hmu(v.n_inc);
-    std::vector<uint32_t> ip(v.n_inc), pv(v.n_pairs);
+    std::vector<uint32_t> ip(v.n_inc), pv(v.n_pairs), slot(v.n_pairs), slot_pair(v.n_pairs);
     CK(cudaMemcpyAsync(hl.data(), m->inc_len.as<float>() + v.inc_base, (size_t)v.n_inc * 4,
                        cudaMemcpyDeviceToHost, m->stream));
     CK(cudaMemcpyAsync(hmu.data(), m->inc_mu.as<float>() + v.inc_base, (size_t)v.n_inc * 4,
                        cudaMemcpyDeviceToHost, m->stream));
     CK(cudaMemcpyAsync(ip.data(), m->inc_pair.as<uint32_t>() + v.inc_base, (size_t)v.n_inc * 4,
                        cudaMemcpyDeviceToHost, m->stream));
-    if (v.n_pairs)
+    if (v.n_pairs) {
       CK(cudaMemcpyAsync(pv.data(), m->pair_vox.as<uint32_t>() + v.pair_base, (size_t)v.n_pairs * 4,
                          cudaMemcpyDeviceToHost, m->stream));
+      CK(cudaMemcpyAsync(slot.data(), m->pair_lq.as<uint32_t>() + v.pair_base, (size_t)v.n_pairs * 4,
+                         cudaMemcpyDeviceToHost, m->stream));
+    }
     sync(m);
+    // incidences carry ln q slots: back to pairs
+    for (uint32_t p = 0; p < v.n_pairs; ++p) slot_pair[slot[p] - v.pair_base] = p;
     int64_t k = 0;
     for (int64_t i = 0; i < HW && k < cap; ++i) {
       int64_t o = (int64_t)hm[i].off - v.inc_base;
       for (int j = 0; j < hm[i].n_pre && k < cap; ++j, ++k) {
         if (len) len[k] = hl[o + j];
         if (mu) mu[k] = hmu[o + j];
-        if (vox) vox[k] = pv[ip[o + j] - v.pair_base];
+        if (vox) vox[k] = pv[slot_pair[ip[o + j] - v.pair_base]];
       }
     }
   });

@@ -85,10 +85,21 @@ cudaError_t launch_trace_emit(const Geom& g, const Pose& P, const float* depth,
                               int* err, cudaStream_t s);
 // pairs in voxel order and the pair-grouped positions
 cudaError_t launch_vox_heads(const uint32_t* sk, uint32_t n, uint32_t* flag, cudaStream_t s);
+// ln q slots by first visit: key[p] = first incidence of pair p (local);
+// after sorting the pairs by key (order[q] = local pair), slot[pair_base +
+// order[q]] = pair_base + q and pair_of_slot[pair_base + q] = pair_base +
+// order[q]
+cudaError_t launch_pair_first(const uint32_t* seg, uint32_t np, uint32_t perm_base, const uint32_t* sidx,
+                              uint32_t* key, cudaStream_t s);
+cudaError_t launch_pair_slots(const uint32_t* order, uint32_t np, uint32_t pair_base, uint32_t* slot,
+                              uint32_t* pair_of_slot, cudaStream_t s);
+// pairs from the voxel-sorted incidences: pair_vox and seg when pair_vox is
+// given; inc_pair[i] = slot[pair of i] when inc_pair is given
 cudaError_t launch_pairs_from_sorted(const uint32_t* sk, const uint32_t* sidx, const uint32_t* flag,
                                      const uint32_t* scan, uint32_t n, uint32_t pair_base,
                                      uint32_t perm_base, uint32_t inc_base, uint32_t* pair_vox,
-                                     uint32_t* seg, uint32_t* inc_pair, cudaStream_t s);
+                                     uint32_t* seg, const uint32_t* slot, uint32_t* inc_pair,
+                                     cudaStream_t s);
 // build records (post length, -(mu l) on dynamic incidences) in sorted order
 cudaError_t launch_gather_rec(const uint32_t* sidx, uint32_t n, uint32_t inc_base, const float2* rec,
                               float2* out, cudaStream_t s);
@@ -146,7 +157,9 @@ struct BpArrays {
   const float* pair_cum;
   const float* pair_stat;  // sum of the pair's static messages
   const uint32_t* pair_ndyn;
-  float* pair_lnq;
+  float* pair_lnq;               // ln q in slot order (first visit along the rays)
+  float* pair_lnv;               // ln q in pair (voxel) order, k_pair_prepare's output
+  const uint32_t* pair_of_slot;  // pair of each ln q slot
   float* pair_dm;
   float* L;
   float* belief;
@@ -158,17 +171,34 @@ struct TileCarry {
   uint32_t flags;
 };
 uint32_t pair_update_tiles(uint32_t n);
+// ln q of pairs [p0, p1) in voxel order, then into slot order (slots of
+// a view span the same range as its pairs): two kernels
 cudaError_t launch_pair_prepare(const BpArrays& a, uint32_t p0, uint32_t p1, int jacobi,
                                 cudaStream_t s);
 // ray-kernel variants (register budget x load policy; identical arithmetic)
 int ray_bp_variants();
 // resident blocks per SM of a variant of the persistent ray kernel (queried once)
 int ray_bp_resident_blocks(int variant);
-// rays order[0..n_rays) of the queue; counter: one zeroed u32 per launch
-cudaError_t launch_ray_bp(const BpArrays& a, const uint32_t* order, uint32_t n_rays,
-                          uint32_t* counter, int fix_reset, int num_sms, int variant, cudaStream_t s);
+// the rays of one ray-kernel launch, in two schedules: queue[0..n_rays)
+// longest first, and the tile queue (rays of 8x8 pixel tiles in pixel
+// order, tiles longest first) with its descriptors tiles[0..n_tiles) =
+// (first tile-queue index, rays)
+constexpr int kRayTile = 8;  // tile-queue tiles are kRayTile x kRayTile pixels
+struct RayWork {
+  const RayMeta* queue;
+  uint32_t n_rays;
+  const RayMeta* tile_queue;
+  const uint2* tiles;
+  uint32_t n_tiles;
+};
+// counter: one zeroed u32 per launch
+cudaError_t launch_ray_bp(const BpArrays& a, const RayWork& w, uint32_t* counter, int fix_reset,
+                          int num_sms, int variant, cudaStream_t s);
 cudaError_t launch_ray_keys(const RayMeta* meta, uint32_t n, uint32_t* keys, uint32_t* vals,
                             cudaStream_t s);
+// queue[i] = meta[order[i]], i < n
+cudaError_t launch_ray_queue(const RayMeta* meta, const uint32_t* order, uint32_t n, RayMeta* queue,
+                             cudaStream_t s);
 // dynamic positions k0..k1 hold the runs j0..j1 (dpair/dseg indices);
 // tile_first from launch_tile_first over dseg
 cudaError_t launch_pair_update(const BpArrays& a, uint32_t k0, uint32_t k1, uint32_t j0, uint32_t j1,
@@ -200,7 +230,6 @@ cudaError_t launch_fill_f32(float* p, int64_t n, float v, cudaStream_t s);
 cudaError_t launch_max_abs_diff(const float* a, const float* b, int64_t n, uint32_t* out,
                                 cudaStream_t s);
 cudaError_t launch_fill_u32(uint32_t* p, int64_t n, uint32_t v, cudaStream_t s);
-cudaError_t launch_add_u32(uint32_t* p, uint32_t n, uint32_t v, cudaStream_t s);
 cudaError_t launch_vflag(const uint32_t* sk, uint32_t n, uint32_t* flag, cudaStream_t s);
 cudaError_t launch_vassign(const uint32_t* sk, const uint32_t* flag, const uint32_t* scan,
                            uint32_t n, uint32_t* vvox, uint32_t* vseg, cudaStream_t s);
