@@ -303,7 +303,7 @@ def run_ours(args):
     pinned = [torch.from_numpy(np.ascontiguousarray(d)).pin_memory() for d in w.depths]
     h2d = sum(p.numel() * 4 for p in pinned) + 16 * 4 * len(w.poses)
     e2e_times, d2h = [], 0
-    for k in range(args.e2e_steps + 1 if args.e2e_steps > 0 else 0):
+    for step in range(args.e2e_steps + 1 if args.e2e_steps > 0 else 0):
         torch.cuda.synchronize()
         barrier(ws)
         t0 = time.perf_counter()
@@ -318,7 +318,7 @@ def run_ours(args):
         mm.close()
         dt = time.perf_counter() - t0
         d2h = cen.nbytes + bel.nbytes
-        if k > 0:  # first pass warms allocator and host paths
+        if step > 0:  # first pass warms allocator and host paths
             e2e_times.append(dt)
     if e2e_times:
         e2e_t = max_over_ranks(float(np.mean(e2e_times)), ws)

@@ -95,6 +95,10 @@ typedef struct mrf_stats {
  * (src/GVDBInference.cpp:20-37, src/GVDBMRFMap.cpp:23-93). */
 MRF_API mrf_status mrf_create(const mrf_params* params, mrf_map** out);
 MRF_API void mrf_destroy(mrf_map* map);
+/* Device memory of destroyed maps stays pooled (per device) for the next
+ * map; this returns the pooled blocks to the driver.  No reference
+ * counterpart. */
+MRF_API mrf_status mrf_release_cached_memory(void);
 /* Text of the last error raised on this thread. */
 MRF_API const char* mrf_last_error(void);
 

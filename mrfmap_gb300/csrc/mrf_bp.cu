@@ -68,27 +68,6 @@ __global__ void __launch_bounds__(kPrepThreads)
   }
 }
 
-// ln q into slot order (first visit along the rays, the order the ray
-// kernel gathers in): lnq[q] = lnv[pair_of_slot[q]].  The voxel-order values
-// were just written by k_pair_prepare and the slots of a view are a
-// permutation of its pairs, so the gathers read L2; four slots per thread.
-__global__ void __launch_bounds__(256)
-    k_lnq_slots(const uint32_t* __restrict__ pair_of_slot, const float* __restrict__ lnv,
-                float* __restrict__ lnq, uint32_t q0, uint32_t q1) {
-  const uint32_t base = q0 + blockIdx.x * (256 * 4) + threadIdx.x;
-  float v[4];
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const uint32_t q = base + k * 256;
-    v[k] = q < q1 ? lnv[pair_of_slot[q]] : 0.0f;
-  }
-#pragma unroll
-  for (int k = 0; k < 4; ++k) {
-    const uint32_t q = base + k * 256;
-    if (q < q1) lnq[q] = v[k];
-  }
-}
-
 // ---- ray messages ----------------------------------------------------------
 // One warp per ray.  Each lane owns kE = 4 consecutive incidences of a
 // chunk of 128 (ray offsets are padded to multiples of 4, so the streams load
@@ -954,10 +933,7 @@ cudaError_t launch_pair_prepare(const BpArrays& a, uint32_t p0, uint32_t p1, int
                                 cudaStream_t s) {
   if (p1 <= p0) return cudaSuccess;
   k_pair_prepare<<<blocks(p1 - p0, kPrepThreads * kPrepPer), kPrepThreads, 0, s>>>(
-      a.pair_vox, a.pair_m, a.L, a.pair_lnv, jacobi ? a.pair_dm : nullptr, p0, p1);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
-  k_lnq_slots<<<blocks(p1 - p0, 256 * 4), 256, 0, s>>>(a.pair_of_slot, a.pair_lnv, a.pair_lnq, p0, p1);
+      a.pair_vox, a.pair_m, a.L, a.pair_lnq, jacobi ? a.pair_dm : nullptr, p0, p1);
   return cudaGetLastError();
 }
 

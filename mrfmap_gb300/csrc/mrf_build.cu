@@ -281,33 +281,80 @@ __global__ void k_pairs_from_sorted(const uint32_t* __restrict__ sk, const uint3
                                     const uint32_t* __restrict__ scan, uint32_t n,
                                     uint32_t pair_base, uint32_t perm_base, uint32_t inc_base,
                                     uint32_t* __restrict__ pair_vox, uint32_t* __restrict__ seg,
-                                    const uint32_t* __restrict__ slot, uint32_t* __restrict__ inc_pair) {
+                                    uint32_t* __restrict__ inc_pair) {
   uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
   uint32_t p = pair_base + scan[k] + flag[k] - 1;
-  if (pair_vox && flag[k]) {
+  if (flag[k]) {
     pair_vox[p] = sk[k];
     seg[p] = perm_base + k;
   }
-  if (inc_pair) inc_pair[inc_base + sidx[k]] = slot[p];
+  if (inc_pair) inc_pair[inc_base + sidx[k]] = p;
 }
 
-// ln q slots by first visit: key[p] = the first incidence of pair p (its
-// first sorted position, the voxel sort being stable); after the pairs are
-// sorted by key, slot[pair_base + order[q]] = pair_base + q (and the
-// inverse), and every incidence carries its pair's slot
+// Pair numbering, brick-major by first visit.  The pairs of a view are
+// first found in voxel order (a stable sort of the incidences by voxel);
+// they are then renumbered by the first visit of their brick (the lowest
+// incidence index -- pixel order, then along the ray -- over the brick's
+// pairs) and, within a brick, by their own first visit, and the
+// pair-grouped incidence order is rebuilt in the new pair order.  Rays of
+// neighbouring pixels cross the same bricks and voxels in the same order,
+// so the pair ids met along a ray come in runs of nearby ids (the ray
+// kernel's ln q gathers share sectors), while a brick's pairs stay together
+// (the per-pair kernels' L accesses stay within the brick).
+//   key[p]         = first incidence of pair p (its first sorted position
+//                    holds it, the sort being stable)
+//   bfirst[brick]  = min key over the brick's pairs
+//   order[q]       = old pair of new pair q; slot_of[old] = q
 __global__ void k_pair_first(const uint32_t* __restrict__ seg, uint32_t np, uint32_t perm_base,
                              const uint32_t* __restrict__ sidx, uint32_t* __restrict__ key) {
   uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
   if (p < np) key[p] = sidx[seg[p] - perm_base];
 }
 
-__global__ void k_pair_slots(const uint32_t* __restrict__ order, uint32_t np, uint32_t pair_base,
-                             uint32_t* __restrict__ slot, uint32_t* __restrict__ pair_of_slot) {
+// pairs come in voxel order, so a warp's lanes mostly share a brick: the
+// lanes of one brick reduce among themselves and one of them does the atomic
+__global__ void k_brick_first(const uint32_t* __restrict__ pair_vox, const uint32_t* __restrict__ key,
+                              uint32_t np, uint32_t* __restrict__ bfirst) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool ok = p < np;
+  const uint32_t b = ok ? pair_vox[p] / kBrickVox : 0xFFFFFFFFu;
+  const uint32_t k = ok ? key[p] : 0xFFFFFFFFu;
+  const unsigned same = __match_any_sync(0xFFFFFFFFu, b);
+  const uint32_t m = __reduce_min_sync(same, k);
+  if (ok && (threadIdx.x & 31) == (unsigned)(__ffs(same) - 1)) atomicMin(bfirst + b, m);
+}
+
+__global__ void k_brick_keys(const uint32_t* __restrict__ order, uint32_t np,
+                             const uint32_t* __restrict__ pair_vox, const uint32_t* __restrict__ bfirst,
+                             uint32_t* __restrict__ key) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < np) key[i] = bfirst[pair_vox[order[i]] / kBrickVox];
+}
+
+// run lengths in the new order and the old -> new map
+__global__ void k_new_lengths(const uint32_t* __restrict__ order, uint32_t np, const uint32_t* __restrict__ seg,
+                              uint32_t* __restrict__ len, uint32_t* __restrict__ slot_of) {
   uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
   if (q >= np) return;
-  slot[pair_base + order[q]] = pair_base + q;
-  pair_of_slot[pair_base + q] = pair_base + order[q];
+  const uint32_t p = order[q];
+  len[q] = seg[p + 1] - seg[p];
+  slot_of[p] = q;
+}
+
+// every sorted position k moves to its pair's new run: out_idx / out_key
+// (incidence index, voxel) in the new pair-grouped order
+__global__ void k_move_positions(const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ flag,
+                                 const uint32_t* __restrict__ scan, const uint32_t* __restrict__ seg,
+                                 const uint32_t* __restrict__ pair_vox, const uint32_t* __restrict__ slot_of,
+                                 const uint32_t* __restrict__ start, uint32_t n, uint32_t perm_base,
+                                 uint32_t* __restrict__ out_idx, uint32_t* __restrict__ out_key) {
+  uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= n) return;
+  const uint32_t p = scan[k] + flag[k] - 1;
+  const uint32_t dst = start[slot_of[p]] + (k - (seg[p] - perm_base));
+  out_idx[dst] = sidx[k];
+  out_key[dst] = pair_vox[p];
 }
 
 // build records in pair-grouped (sorted) order: one gather per position
@@ -508,11 +555,10 @@ cudaError_t launch_vox_heads(const uint32_t* sk, uint32_t n, uint32_t* flag, cud
 cudaError_t launch_pairs_from_sorted(const uint32_t* sk, const uint32_t* sidx, const uint32_t* flag,
                                      const uint32_t* scan, uint32_t n, uint32_t pair_base,
                                      uint32_t perm_base, uint32_t inc_base, uint32_t* pair_vox,
-                                     uint32_t* seg, const uint32_t* slot, uint32_t* inc_pair,
-                                     cudaStream_t s) {
+                                     uint32_t* seg, uint32_t* inc_pair, cudaStream_t s) {
   if (!n) return cudaSuccess;
   k_pairs_from_sorted<<<grid_for(n), kThreads, 0, s>>>(sk, sidx, flag, scan, n, pair_base, perm_base,
-                                                       inc_base, pair_vox, seg, slot, inc_pair);
+                                                       inc_base, pair_vox, seg, inc_pair);
   return cudaGetLastError();
 }
 
@@ -523,10 +569,34 @@ cudaError_t launch_pair_first(const uint32_t* seg, uint32_t np, uint32_t perm_ba
   return cudaGetLastError();
 }
 
-cudaError_t launch_pair_slots(const uint32_t* order, uint32_t np, uint32_t pair_base, uint32_t* slot,
-                              uint32_t* pair_of_slot, cudaStream_t s) {
+cudaError_t launch_brick_first(const uint32_t* pair_vox, const uint32_t* key, uint32_t np, uint32_t* bfirst,
+                               cudaStream_t s) {
   if (!np) return cudaSuccess;
-  k_pair_slots<<<grid_for(np), kThreads, 0, s>>>(order, np, pair_base, slot, pair_of_slot);
+  k_brick_first<<<grid_for(np), kThreads, 0, s>>>(pair_vox, key, np, bfirst);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_brick_keys(const uint32_t* order, uint32_t np, const uint32_t* pair_vox,
+                              const uint32_t* bfirst, uint32_t* key, cudaStream_t s) {
+  if (!np) return cudaSuccess;
+  k_brick_keys<<<grid_for(np), kThreads, 0, s>>>(order, np, pair_vox, bfirst, key);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_new_lengths(const uint32_t* order, uint32_t np, const uint32_t* seg, uint32_t* len,
+                               uint32_t* slot_of, cudaStream_t s) {
+  if (!np) return cudaSuccess;
+  k_new_lengths<<<grid_for(np), kThreads, 0, s>>>(order, np, seg, len, slot_of);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_move_positions(const uint32_t* sidx, const uint32_t* flag, const uint32_t* scan,
+                                  const uint32_t* seg, const uint32_t* pair_vox, const uint32_t* slot_of,
+                                  const uint32_t* start, uint32_t n, uint32_t perm_base, uint32_t* out_idx,
+                                  uint32_t* out_key, cudaStream_t s) {
+  if (!n) return cudaSuccess;
+  k_move_positions<<<grid_for(n), kThreads, 0, s>>>(sidx, flag, scan, seg, pair_vox, slot_of, start, n,
+                                                    perm_base, out_idx, out_key);
   return cudaGetLastError();
 }
 

@@ -16,6 +16,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <mutex>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -52,25 +53,52 @@ void fail(mrf_status st, const std::string& msg) {
   throw Fail{st};
 }
 
-// growable device buffer
+// Device memory of every map comes from one stream-ordered pool per
+// device that keeps freed blocks for reuse (release threshold: never), so a
+// map built after another one allocates nothing from the driver and
+// destroying a map does not wait on cudaFree.  mrf_release_cached_memory
+// hands the pooled blocks back.
+constexpr int kMaxDevices = 64;
+std::mutex g_pool_mu;
+cudaMemPool_t g_pools[kMaxDevices] = {};
+
+cudaMemPool_t map_pool() {
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) fail(MRF_ERR_INVALID, "device index out of range");
+  std::lock_guard<std::mutex> lk(g_pool_mu);
+  if (!g_pools[dev]) {
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t pool = nullptr;
+    CK(cudaMemPoolCreate(&pool, &props));
+    uint64_t keep_all = ~0ull;
+    CK(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep_all));
+    g_pools[dev] = pool;
+  }
+  return g_pools[dev];
+}
+
+// growable device buffer (stream-ordered on the stream that last sized it)
 struct DBuf {
   void* p = nullptr;
   size_t cap = 0;
+  cudaStream_t owner = nullptr;
   void reserve(size_t bytes, bool keep, cudaStream_t s) {
     if (bytes <= cap) return;
     size_t nc = std::max(bytes, cap + cap / 2);
     void* q = nullptr;
-    CK(cudaMalloc(&q, nc));
+    CK(cudaMallocFromPoolAsync(&q, nc, map_pool(), s));
     if (keep && p && cap) CK(cudaMemcpyAsync(q, p, cap, cudaMemcpyDeviceToDevice, s));
-    if (p) {
-      CK(cudaStreamSynchronize(s));
-      cudaFree(p);
-    }
+    if (p) CK(cudaFreeAsync(p, s));
     p = q;
     cap = nc;
+    owner = s;
   }
   void release() {
-    if (p) cudaFree(p);
+    if (p) cudaFreeAsync(p, owner);
     p = nullptr;
     cap = 0;
   }
@@ -119,7 +147,7 @@ struct mrf_map {
   std::vector<View> views;
   // arenas
   DBuf meta, inc_pair, inc_len, inc_mu, inc_pl, pair_vox, pair_m, pair_cum, pair_stat, pair_ndyn, pair_hit,
-      pair_q, pair_dm, pair_seg, pair_lq, pair_of_slot, pair_lnv, dperm, dpair, dseg, drun, carry, ray_order, ray_queue, tile_queue, tiles, counters,
+      pair_q, pair_dm, pair_seg, dperm, s_q0, s_q1, s_q2, s_q3, s_bf, dpair, dseg, drun, carry, ray_order, ray_queue, tile_queue, tiles, counters,
       tile_first;
   uint32_t jac_tile_base = 0;
   int64_t n_inc = 0, n_pairs = 0, n_dperm = 0, n_dpairs = 0;
@@ -159,8 +187,6 @@ struct mrf_map {
     a.pair_stat = pair_stat.as<float>();
     a.pair_ndyn = pair_ndyn.as<uint32_t>();
     a.pair_lnq = pair_q.as<float>();
-    a.pair_lnv = pair_lnv.as<float>();
-    a.pair_of_slot = pair_of_slot.as<uint32_t>();
     a.pair_dm = pair_dm.as<float>();
     a.L = d_L.as<float>();
     a.belief = d_belief.as<float>();
@@ -322,9 +348,10 @@ void rebuild(mrf_map* m) {
     }
     for (int c = 0; c < V; ++c) npre += nreal[c];
   }
-  // 4. pairs per view in voxel order: sort the view's incidences by voxel
-  //    (stable), one pair per run; pos[i] = pair-grouped position of i.
-  //    The pairs' ln q slots are numbered by first visit (see below).
+  // 4. pairs per view: sort the view's incidences by voxel (stable), one
+  //    pair per run, then renumber the pairs brick-major by first visit
+  //    (mrf_build.cu, k_pair_first) and regroup the incidences in the new
+  //    pair order; pos[i] = pair-grouped position of i
   int bits = 1;
   while (bits < 32 && ((uint64_t)1 << bits) <= (uint64_t)(m->n_bricks * kBrickVox)) ++bits;
   int64_t pair_total = 0, perm_total = 0, dperm_total = 0, dpair_total = 0;
@@ -353,6 +380,59 @@ void rebuild(mrf_map* m) {
                       m->s_v0.as<uint32_t>(), m->s_v1.as<uint32_t>(), n, bits, m->stream));
     size_t t1 = scan_temp_bytes(nr + 1);
     m->s_tmp.reserve(t1, false, m->stream);
+    {
+      // voxel-order pairs: runs of the sorted voxel keys (pair_vox and
+      // pair_seg hold them until the renumbered pairs overwrite them)
+      CK(launch_vox_heads(m->s_k1.as<uint32_t>(), nr, m->s_k0.as<uint32_t>(), m->stream));
+      CK(cudaMemsetAsync(m->s_k0.as<uint32_t>() + nr, 0, 4, m->stream));
+      CK(exclusive_scan_u32(m->s_tmp.p, t1, m->s_k0.as<uint32_t>(), m->s_v0.as<uint32_t>(), nr + 1,
+                            m->stream));
+      const uint32_t np0 = read1(m, m->s_v0.as<uint32_t>() + nr);
+      const size_t pb0 = (size_t)(pair_total + np0 + 1);
+      m->pair_vox.reserve(pb0 * 4, true, m->stream);
+      m->pair_seg.reserve(pb0 * 4, true, m->stream);
+      uint32_t* pv = m->pair_vox.as<uint32_t>() + v.pair_base;
+      uint32_t* sg = m->pair_seg.as<uint32_t>() + v.pair_base;
+      CK(launch_pairs_from_sorted(m->s_k1.as<uint32_t>(), m->s_v1.as<uint32_t>(), m->s_k0.as<uint32_t>(),
+                                  m->s_v0.as<uint32_t>(), nr, 0, 0, v.inc_base, pv, sg, nullptr, m->stream));
+      CK(launch_fill_u32(sg + np0, 1, nr, m->stream));
+      // first visits: of each pair, and of each brick (min over its pairs)
+      const size_t q4 = (size_t)np0 * 4 + 4;
+      m->s_q0.reserve(q4, false, m->stream);
+      m->s_q1.reserve(q4, false, m->stream);
+      m->s_q2.reserve(q4, false, m->stream);
+      m->s_q3.reserve(q4, false, m->stream);
+      m->s_bf.reserve((size_t)m->n_bricks * 4 + 4, false, m->stream);
+      uint32_t* q0 = m->s_q0.as<uint32_t>();
+      uint32_t* q1 = m->s_q1.as<uint32_t>();
+      uint32_t* q2 = m->s_q2.as<uint32_t>();
+      uint32_t* q3 = m->s_q3.as<uint32_t>();
+      CK(launch_pair_first(sg, np0, 0, m->s_v1.as<uint32_t>(), q0, m->stream));
+      CK(launch_fill_u32(m->s_bf.as<uint32_t>(), m->n_bricks, 0xFFFFFFFFu, m->stream));
+      CK(launch_brick_first(pv, q0, np0, m->s_bf.as<uint32_t>(), m->stream));
+      // order: by own first visit, then (stable) by the brick's first visit
+      int ibits = 1;
+      while (ibits < 32 && ((uint64_t)1 << ibits) < (uint64_t)n) ++ibits;
+      size_t t4 = sort_temp_bytes(np0, ibits);
+      m->s_tmp.reserve(std::max(t4, t1), false, m->stream);
+      CK(launch_iota(q2, np0, m->stream));
+      CK(sort_pairs_u32(m->s_tmp.p, t4, q0, q1, q2, q3, np0, ibits, m->stream));  // q3: by own visit
+      CK(launch_brick_keys(q3, np0, pv, m->s_bf.as<uint32_t>(), q0, m->stream));
+      CK(sort_pairs_u32(m->s_tmp.p, t4, q0, q1, q3, q2, np0, ibits, m->stream));  // q2: new order
+      // new runs: lengths in the new order, their starts, the old -> new map
+      CK(launch_new_lengths(q2, np0, sg, q0, q3, m->stream));
+      CK(cudaMemsetAsync(q0 + np0, 0, 4, m->stream));
+      size_t t5 = scan_temp_bytes(np0 + 1);
+      m->s_tmp.reserve(t5, false, m->stream);
+      CK(exclusive_scan_u32(m->s_tmp.p, t5, q0, q1, np0 + 1, m->stream));
+      // the sorted positions in the new pair order: incidence index and voxel
+      m->s_recs.reserve((size_t)nr * 8, false, m->stream);
+      uint32_t* nidx = m->s_recs.as<uint32_t>();
+      CK(launch_move_positions(m->s_v1.as<uint32_t>(), m->s_k0.as<uint32_t>(), m->s_v0.as<uint32_t>(), sg, pv,
+                               q3, q1, nr, 0, nidx, m->s_k1.as<uint32_t>(), m->stream));
+      std::swap(m->s_v1, m->s_recs);  // the moved positions become the sorted order
+      m->s_v1.reserve((size_t)n * 4 + 4, true, m->stream);
+    }
     CK(launch_vox_heads(m->s_k1.as<uint32_t>(), nr, m->s_k0.as<uint32_t>(), m->stream));
     CK(cudaMemsetAsync(m->s_k0.as<uint32_t>() + nr, 0, 4, m->stream));
     CK(exclusive_scan_u32(m->s_tmp.p, t1, m->s_k0.as<uint32_t>(), m->s_v0.as<uint32_t>(), nr + 1,
@@ -367,38 +447,11 @@ void rebuild(mrf_map* m) {
     m->pair_ndyn.reserve(pb * 4, true, m->stream);
     m->pair_hit.reserve(pb * 4, true, m->stream);
     m->pair_seg.reserve(pb * 4, true, m->stream);
-    m->pair_lq.reserve(pb * 4, true, m->stream);
-    m->pair_of_slot.reserve(pb * 4, true, m->stream);
     CK(launch_pairs_from_sorted(m->s_k1.as<uint32_t>(), m->s_v1.as<uint32_t>(), m->s_k0.as<uint32_t>(),
                                 m->s_v0.as<uint32_t>(), nr, v.pair_base, v.perm_base, v.inc_base,
-                                m->pair_vox.as<uint32_t>(), m->pair_seg.as<uint32_t>(), nullptr, nullptr,
-                                m->stream));
+                                m->pair_vox.as<uint32_t>(), m->pair_seg.as<uint32_t>(),
+                                m->inc_pair.as<uint32_t>(), m->stream));
     CK(launch_fill_u32(m->pair_seg.as<uint32_t>() + v.pair_base + np, 1, v.perm_base + nr, m->stream));
-    // ln q slots by first visit: the pairs ordered by their first incidence
-    // (pixel order, then along the ray; a pair's first sorted position holds
-    // it, the voxel sort being stable).  Rays of neighbouring pixels cross
-    // the same voxels in the same order, so the slots met along a ray come
-    // in runs of consecutive indices and the ray kernel's ln q gathers share
-    // sectors.  The pairs stay in voxel order; the incidences carry slots.
-    {
-      m->s_pf.reserve((size_t)np * 4 + 4, false, m->stream);
-      m->s_ps.reserve((size_t)np * 4 + 4, false, m->stream);
-      m->s_recs.reserve((size_t)nr * 8, false, m->stream);
-      CK(launch_pair_first(m->pair_seg.as<uint32_t>() + v.pair_base, np, v.perm_base, m->s_v1.as<uint32_t>(),
-                           m->s_k1.as<uint32_t>(), m->stream));
-      CK(launch_iota(m->s_ps.as<uint32_t>(), np, m->stream));
-      int ibits = 1;
-      while (ibits < 32 && ((uint64_t)1 << ibits) < (uint64_t)n) ++ibits;
-      size_t t4 = sort_temp_bytes(np, ibits);
-      m->s_tmp.reserve(t4, false, m->stream);
-      CK(sort_pairs_u32(m->s_tmp.p, t4, m->s_k1.as<uint32_t>(), m->s_recs.as<uint32_t>(),
-                        m->s_ps.as<uint32_t>(), m->s_pf.as<uint32_t>(), np, ibits, m->stream));
-      CK(launch_pair_slots(m->s_pf.as<uint32_t>(), np, v.pair_base, m->pair_lq.as<uint32_t>(),
-                           m->pair_of_slot.as<uint32_t>(), m->stream));
-      CK(launch_pairs_from_sorted(nullptr, m->s_v1.as<uint32_t>(), m->s_k0.as<uint32_t>(),
-                                  m->s_v0.as<uint32_t>(), nr, v.pair_base, v.perm_base, v.inc_base, nullptr,
-                                  nullptr, m->pair_lq.as<uint32_t>(), m->inc_pair.as<uint32_t>(), m->stream));
-    }
     m->s_recs.reserve((size_t)nr * 8, false, m->stream);
     CK(launch_gather_rec(m->s_v1.as<uint32_t>(), nr, v.inc_base, m->s_rec.as<float2>(),
                          m->s_recs.as<float2>(), m->stream));
@@ -539,7 +592,6 @@ void rebuild(mrf_map* m) {
   CK(launch_drun(m->dpair.as<uint32_t>(), (uint32_t)dpair_total, m->pair_vox.as<uint32_t>(),
                  m->pair_cum.as<float>(), m->pair_stat.as<float>(), m->drun.as<uint4>(), m->stream));
   m->pair_q.reserve(pb * 4, false, m->stream);
-  m->pair_lnv.reserve(pb * 4, false, m->stream);
   m->pair_dm.reserve(pb * 4, false, m->stream);
   CK(launch_fill_f32(m->pair_m.as<float>(), pair_total, 0.0f, m->stream));
   {
@@ -716,7 +768,7 @@ void enqueue_iteration(mrf_map* m, const BpArrays& a, bool jacobi, int fix, bool
         ++launches;
       }
       prof.end();
-      launches += 3;  // prepare (two kernels) and the ray kernel
+      launches += 2;
     }
   } else {
     uint32_t P = (uint32_t)m->n_pairs;
@@ -739,7 +791,7 @@ void enqueue_iteration(mrf_map* m, const BpArrays& a, bool jacobi, int fix, bool
                           m->n_vvox, m->pair_dm.as<float>(), m->d_L.as<float>(),
                           m->d_belief.as<float>(), m->stream));
     prof.end();
-    launches += 6 + (first ? 1 : 0);
+    launches += 5 + (first ? 1 : 0);
   }
 }
 
@@ -919,10 +971,11 @@ void destroy_bufs(mrf_map* m) {
                  &m->meta, &m->inc_pair, &m->inc_len, &m->inc_mu, &m->inc_pl, &m->pair_vox,
                  &m->pair_m, &m->pair_cum, &m->pair_stat, &m->pair_ndyn, &m->pair_hit, &m->pair_q,
                  &m->pair_dm,
-                 &m->pair_seg, &m->pair_lq, &m->pair_of_slot, &m->pair_lnv, &m->dperm, &m->dpair, &m->dseg, &m->drun,
+                 &m->pair_seg, &m->dperm, &m->dpair, &m->dseg, &m->drun,
                  &m->carry, &m->ray_order, &m->ray_queue, &m->tile_queue, &m->tiles, &m->counters, &m->tile_first,
                  &m->vseg, &m->vpairs, &m->vvox, &m->s_rec, &m->s_recs, &m->s_pf, &m->s_ps,
                  &m->s_flags, &m->s_ind, &m->s_scan,
+                 &m->s_q0, &m->s_q1, &m->s_q2, &m->s_q3, &m->s_bf,
                  &m->s_tmp, &m->s_counts, &m->s_offs, &m->s_vox, &m->s_k0, &m->s_k1, &m->s_v0,
                  &m->s_v1, &m->s_seg, &m->s_dense, &m->s_err, &m->s_depth_in, &m->s_depth,
                  &m->s_img, &m->s_part, &m->s_sum, &m->s_prev, &m->s_delta, &m->s_snap};
@@ -1056,6 +1109,19 @@ void mrf_destroy(mrf_map* m) {
   if (m->ev1) cudaEventDestroy(m->ev1);
   if (m->stream) cudaStreamDestroy(m->stream);
   delete m;
+}
+
+mrf_status mrf_release_cached_memory(void) {
+  std::lock_guard<std::mutex> lk(g_pool_mu);
+  for (int d = 0; d < kMaxDevices; ++d) {
+    if (!g_pools[d]) continue;
+    cudaError_t e = cudaMemPoolTrimTo(g_pools[d], 0);
+    if (e != cudaSuccess) {
+      set_err(std::string("cudaMemPoolTrimTo: ") + cudaGetErrorString(e));
+      return MRF_ERR_CUDA;
+    }
+  }
+  return MRF_OK;
 }
 
 static mrf_status add_view_impl(mrf_map* m, const float* pose, const float* depth, bool device,
@@ -1700,29 +1766,24 @@ mrf_status mrf_view_incidences(mrf_map* m, int view_id, int* meta, uint32_t* vox
     if (cap <= 0 || v.n_inc == 0 || (!len && !mu && !vox)) return;
     // device lists are padded per ray: copy the view's range, then compact
     std::vector<float> hl(v.n_inc), hmu(v.n_inc);
-    std::vector<uint32_t> ip(v.n_inc), pv(v.n_pairs), slot(v.n_pairs), slot_pair(v.n_pairs);
+    std::vector<uint32_t> ip(v.n_inc), pv(v.n_pairs);
     CK(cudaMemcpyAsync(hl.data(), m->inc_len.as<float>() + v.inc_base, (size_t)v.n_inc * 4,
                        cudaMemcpyDeviceToHost, m->stream));
     CK(cudaMemcpyAsync(hmu.data(), m->inc_mu.as<float>() + v.inc_base, (size_t)v.n_inc * 4,
                        cudaMemcpyDeviceToHost, m->stream));
     CK(cudaMemcpyAsync(ip.data(), m->inc_pair.as<uint32_t>() + v.inc_base, (size_t)v.n_inc * 4,
                        cudaMemcpyDeviceToHost, m->stream));
-    if (v.n_pairs) {
+    if (v.n_pairs)
       CK(cudaMemcpyAsync(pv.data(), m->pair_vox.as<uint32_t>() + v.pair_base, (size_t)v.n_pairs * 4,
                          cudaMemcpyDeviceToHost, m->stream));
-      CK(cudaMemcpyAsync(slot.data(), m->pair_lq.as<uint32_t>() + v.pair_base, (size_t)v.n_pairs * 4,
-                         cudaMemcpyDeviceToHost, m->stream));
-    }
     sync(m);
-    // incidences carry ln q slots: back to pairs
-    for (uint32_t p = 0; p < v.n_pairs; ++p) slot_pair[slot[p] - v.pair_base] = p;
     int64_t k = 0;
     for (int64_t i = 0; i < HW && k < cap; ++i) {
       int64_t o = (int64_t)hm[i].off - v.inc_base;
       for (int j = 0; j < hm[i].n_pre && k < cap; ++j, ++k) {
         if (len) len[k] = hl[o + j];
         if (mu) mu[k] = hmu[o + j];
-        if (vox) vox[k] = pv[slot_pair[ip[o + j] - v.pair_base]];
+        if (vox) vox[k] = pv[ip[o + j] - v.pair_base];
       }
     }
   });

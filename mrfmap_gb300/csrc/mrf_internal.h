@@ -85,21 +85,25 @@ cudaError_t launch_trace_emit(const Geom& g, const Pose& P, const float* depth,
                               int* err, cudaStream_t s);
 // pairs in voxel order and the pair-grouped positions
 cudaError_t launch_vox_heads(const uint32_t* sk, uint32_t n, uint32_t* flag, cudaStream_t s);
-// ln q slots by first visit: key[p] = first incidence of pair p (local);
-// after sorting the pairs by key (order[q] = local pair), slot[pair_base +
-// order[q]] = pair_base + q and pair_of_slot[pair_base + q] = pair_base +
-// order[q]
+// brick-major first-visit pair numbering (mrf_build.cu)
 cudaError_t launch_pair_first(const uint32_t* seg, uint32_t np, uint32_t perm_base, const uint32_t* sidx,
                               uint32_t* key, cudaStream_t s);
-cudaError_t launch_pair_slots(const uint32_t* order, uint32_t np, uint32_t pair_base, uint32_t* slot,
-                              uint32_t* pair_of_slot, cudaStream_t s);
-// pairs from the voxel-sorted incidences: pair_vox and seg when pair_vox is
-// given; inc_pair[i] = slot[pair of i] when inc_pair is given
+cudaError_t launch_brick_first(const uint32_t* pair_vox, const uint32_t* key, uint32_t np, uint32_t* bfirst,
+                               cudaStream_t s);
+cudaError_t launch_brick_keys(const uint32_t* order, uint32_t np, const uint32_t* pair_vox,
+                              const uint32_t* bfirst, uint32_t* key, cudaStream_t s);
+cudaError_t launch_new_lengths(const uint32_t* order, uint32_t np, const uint32_t* seg, uint32_t* len,
+                               uint32_t* slot_of, cudaStream_t s);
+cudaError_t launch_move_positions(const uint32_t* sidx, const uint32_t* flag, const uint32_t* scan,
+                                  const uint32_t* seg, const uint32_t* pair_vox, const uint32_t* slot_of,
+                                  const uint32_t* start, uint32_t n, uint32_t perm_base, uint32_t* out_idx,
+                                  uint32_t* out_key, cudaStream_t s);
+// pairs from the pair-grouped incidences: pair_vox, seg and (when given)
+// inc_pair
 cudaError_t launch_pairs_from_sorted(const uint32_t* sk, const uint32_t* sidx, const uint32_t* flag,
                                      const uint32_t* scan, uint32_t n, uint32_t pair_base,
                                      uint32_t perm_base, uint32_t inc_base, uint32_t* pair_vox,
-                                     uint32_t* seg, const uint32_t* slot, uint32_t* inc_pair,
-                                     cudaStream_t s);
+                                     uint32_t* seg, uint32_t* inc_pair, cudaStream_t s);
 // build records (post length, -(mu l) on dynamic incidences) in sorted order
 cudaError_t launch_gather_rec(const uint32_t* sidx, uint32_t n, uint32_t inc_base, const float2* rec,
                               float2* out, cudaStream_t s);
@@ -157,9 +161,7 @@ struct BpArrays {
   const float* pair_cum;
   const float* pair_stat;  // sum of the pair's static messages
   const uint32_t* pair_ndyn;
-  float* pair_lnq;               // ln q in slot order (first visit along the rays)
-  float* pair_lnv;               // ln q in pair (voxel) order, k_pair_prepare's output
-  const uint32_t* pair_of_slot;  // pair of each ln q slot
+  float* pair_lnq;
   float* pair_dm;
   float* L;
   float* belief;
@@ -171,8 +173,6 @@ struct TileCarry {
   uint32_t flags;
 };
 uint32_t pair_update_tiles(uint32_t n);
-// ln q of pairs [p0, p1) in voxel order, then into slot order (slots of
-// a view span the same range as its pairs): two kernels
 cudaError_t launch_pair_prepare(const BpArrays& a, uint32_t p0, uint32_t p1, int jacobi,
                                 cudaStream_t s);
 // ray-kernel variants (register budget x load policy; identical arithmetic)

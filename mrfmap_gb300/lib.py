@@ -30,7 +30,7 @@ _STATUS = {0: "MRF_OK", 1: "MRF_ERR_INVALID", 2: "MRF_ERR_CUDA", 3: "MRF_ERR_OOM
            4: "MRF_ERR_CAPACITY", 5: "MRF_ERR_DEVICE", 6: "MRF_ERR_STATE"}
 
 # every symbol declared in include/mrfmap_gb300.h
-EXPORTS = ["mrf_create", "mrf_destroy", "mrf_last_error", "mrf_add_view", "mrf_add_view_device",
+EXPORTS = ["mrf_create", "mrf_destroy", "mrf_release_cached_memory", "mrf_last_error", "mrf_add_view", "mrf_add_view_device",
            "mrf_set_pose", "mrf_infer", "mrf_infer_converge", "mrf_warm_start", "mrf_warm_start_device",
            "mrf_warm_features", "mrf_read_messages", "mrf_write_messages", "mrf_rebuild_logodds", "mrf_net_num_params", "mrf_net_workspace_bytes", "mrf_net_forward",
            "mrf_net_gradients", "mrf_net_adam",
@@ -90,6 +90,7 @@ def load(path: str | None = None):
     sig = {
         "mrf_create": ([C.POINTER(mrf_params), C.POINTER(vp)], C.c_int),
         "mrf_destroy": ([vp], None),
+        "mrf_release_cached_memory": ([], C.c_int),
         "mrf_last_error": ([], C.c_char_p),
         "mrf_add_view": ([vp, fp, fp, ip], C.c_int),
         "mrf_add_view_device": ([vp, fp, vp, ip], C.c_int),
