@@ -83,8 +83,15 @@ __global__ void __launch_bounds__(kPrepThreads)
 // loaded from k_dyn (rounded down to a vector) on.  Pass 2 re-reads the
 // dynamic range (a sixth of the incidences, mostly still in L1/L2) from
 // A_{k_dyn - 1} instead of keeping pass 1's slice in registers: the kernel
-// then fits 40 registers, twelve resident blocks per SM.  The tau sums of
-// rays longer than kLongRay are formed in FP64.
+// then fits 40 registers, twelve resident blocks per SM.  On rays longer
+// than kLongRay the Pre total T is summed across lanes in FP64 and the
+// running difference T - F of pass 2 is carried in FP64; each lane's share
+// of T is a compensated FP32 sum.  (GB300 issues FP64 at 1/64 of the FP32
+// rate, so FP64 stays out of the per-incidence arithmetic.)
+//
+// The ln q gathers are the kernel's cost.  Pairs are numbered brick-major
+// by first visit (mrf_build.cu), so consecutive incidences of a ray gather
+// from nearby addresses and neighbouring rays from the same ones.
 //
 // Pre visibility restarts at r0 (the reference restores its carried state
 // only once the accumulated tau is non-zero, gvdbkernels.cu:708-715):
@@ -299,14 +306,15 @@ __device__ __forceinline__ float emit_slice(const float (&vmu)[KE], const float 
   return __shfl_sync(kFull, ex + run, 31);
 }
 
-// Pass-1b bookkeeping of one slice (base >= 1): A_{r0-1} and A_{rinf-1}
-// where those positions fall inside it
+// Pass-1 bookkeeping of one slice: A_{r0-1}, A_{rinf-1} and A_{k4-1} where
+// those positions fall inside it
 template <int KE>
-__device__ __forceinline__ void pre_marks(const Slice<KE>& s, int base, int r0, int rinf, float& Ar0,
-                                          float& Arinf) {
+__device__ __forceinline__ void pre_marks(const Slice<KE>& s, int base, int r0, int rinf, int k4,
+                                          float& Ar0, float& Arinf, float& Ak) {
   constexpr int CH = 32 * KE;
   if (r0 - 1 >= base && r0 - 1 < base + CH) Ar0 = slice_value<KE>(s, r0 - 1 - base);
   if (rinf - 1 >= base && rinf - 1 < base + CH) Arinf = slice_value<KE>(s, rinf - 1 - base);
+  if (k4 - 1 >= base && k4 - 1 < base + CH) Ak = slice_value<KE>(s, k4 - 1 - base);
 }
 
 // the lane's share of the Pre total from one slice that may hold non-zero
@@ -333,28 +341,6 @@ __device__ __forceinline__ void pre_total(const Slice<KE>& s, int i0, int r0, fl
   ts = t;
 }
 
-// static-prefix sums of one lane's vector x (positions i0..i0+3, all inside
-// [0, k4)): the total and the parts before r0 and before rinf
-__device__ __forceinline__ void static_accum(const float (&x)[4], int i0, int r0, int rinf, float& sa,
-                                             float& sr0, float& srf) {
-  const float xs = ((x[0] + x[1]) + x[2]) + x[3];
-  sa += xs;
-  if (i0 + 4 <= r0) {
-    sr0 += xs;
-  } else if (i0 < r0) {
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-      if (i0 + j < r0) sr0 += x[j];
-  }
-  if (i0 + 4 <= rinf) {
-    srf += xs;
-  } else if (i0 < rinf) {
-#pragma unroll
-    for (int j = 0; j < 4; ++j)
-      if (i0 + j < rinf) srf += x[j];
-  }
-}
-
 template <typename Acc, int kPol, int kPf>
 __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, const uint32_t* __restrict__ inc_pair,
                                             const float* __restrict__ inc_len,
@@ -367,61 +353,23 @@ __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, const uint32_t* _
   const int kdyn = ray_kdyn(me);
   const int k4 = kdyn & ~3;
   const uint32_t off = me.off;
-  // ---- pass 1a: the static prefix [0, k4) --------------------------------
-  // No potential is non-zero before k_dyn, so pass 1 needs only sums of
-  // l ln q over [0, k4) -- to k4, and to r0 and rinf where those lie
-  // inside: per-lane sums with the next chunk's pair ids and lengths in
-  // flight, and one warp reduction per ray instead of a scan per chunk.
-  float carryA = 0.0f, Ar0 = 0.0f, Arinf = 0.0f;
-  {
-    float sa = 0.0f, sr0 = 0.0f, srf = 0.0f;
-    uint32_t pidn[kE];
-    float lenn[kE];
-    if (k4 > 0) {
-      ld_vec<kE, kPol>(pidn, inc_pair + off, kE * lane, kE * lane < k4);
-      ld_vec<kE, kPol>(lenn, inc_len + off, kE * lane, kE * lane < k4);
-    }
-    for (int base = 0; base < k4; base += kChunk) {
-      const int i0 = base + kE * lane;  // k4 is a multiple of 4: a lane's vector is all in or all out
-      uint32_t pid[kE];
-      float len[kE];
-#pragma unroll
-      for (int j = 0; j < kE; ++j) {
-        pid[j] = pidn[j];
-        len[j] = lenn[j];
-      }
-      if (base + kChunk < k4) {
-        ld_vec<kE, kPol>(pidn, inc_pair + off, i0 + kChunk, i0 + kChunk < k4);
-        ld_vec<kE, kPol>(lenn, inc_len + off, i0 + kChunk, i0 + kChunk < k4);
-      }
-      if (i0 < k4) {
-        float x[kE];
-#pragma unroll
-        for (int j = 0; j < kE; ++j) x[j] = len[j] * __ldg(lnq + pid[j]);
-        static_accum(x, i0, r0, rinf, sa, sr0, srf);
-      }
-    }
-    if (k4 > 0) {
-      carryA = warp_sum(sa);
-      if (r0 > 0 && r0 <= k4) Ar0 = warp_sum(sr0);
-      if (rinf > 0 && rinf <= k4) Arinf = warp_sum(srf);
-    }
-  }
-  const float Ak = carryA;  // A_{k4 - 1}
-  // ---- pass 1b: the dynamic range [k4, n_pre): prefixes, Pre total -------
+  float carryA = 0.0f, Ar0 = 0.0f, Arinf = 0.0f, Ak = 0.0f;
+  // ---- pass 1: prefixes, Pre total ---------------------------------------
   // Chunks of 128 (a chunk costs the same instructions however many of its
-  // lanes hold incidences).  Chunks wholly inside the ray skip the bounds
-  // checks.  kPf 1: the next chunk's pair ids are requested before this
-  // chunk's ln q gathers; kPf 2: its lengths as well.
+  // lanes hold incidences: measured against 256-incidence chunks and against
+  // 256-incidence chunks with 64- or 128-incidence tails, this was fastest).
+  // Chunks wholly inside the ray skip the bounds checks; chunks wholly
+  // before k4 hold no potential and skip the Pre-total work.  kPf 1: the
+  // next chunk's pair ids are requested before this chunk's ln q gathers;
+  // kPf 2: its lengths as well.
   float ts = 0.0f, tc = 0.0f;
   Slice<kE> s;
   {
     uint32_t pid_next[kE];
     float len_next[kE], len[kE];
-    if (kPf && k4 < n_pre) load_pids<kE, kPol>(pid_next, off, k4 + kE * lane, n_pre, inc_pair);
-    if (kPf == 2 && k4 < n_pre)
-      ld_vec<kE, kPol>(len_next, inc_len + off, k4 + kE * lane, k4 + kE * lane < n_pre);
-    for (int base = k4; base < n_pre; base += kChunk) {
+    if (kPf) load_pids<kE, kPol>(pid_next, off, kE * lane, n_pre, inc_pair);
+    if (kPf == 2) ld_vec<kE, kPol>(len_next, inc_len + off, kE * lane, kE * lane < n_pre);
+    for (int base = 0; base < n_pre; base += kChunk) {
       const int i0 = base + kE * lane;
       uint32_t pid[kE];
       if (kPf) {
@@ -444,8 +392,8 @@ __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, const uint32_t* _
                                                           inc_mu, lnq, len)
               : slice_from_pids<kE, kPol, false, kPf == 2>(s, pid, off, i0, n_pre, k4, carryA, lane,
                                                            inc_len, inc_mu, lnq, len);
-      pre_marks<kE>(s, base, r0, rinf, Ar0, Arinf);
-      pre_total<kE>(s, i0, r0, Ar0, ts, tc);
+      pre_marks<kE>(s, base, r0, rinf, k4, Ar0, Arinf, Ak);
+      if (base + kChunk > k4) pre_total<kE>(s, i0, r0, Ar0, ts, tc);
       carryA += tot;
     }
   }
@@ -484,23 +432,16 @@ __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, const uint32_t* _
   }
 }
 
-// Persistent launch.  Longest-first queue (kTiles false): each warp takes
-// the next ray from a work counter; rays are queued longest first (sorted
-// once per incidence build, their RayMeta records copied into queue order),
-// so the long rays start early and the short ones fill the tail.  Tile
-// queue (kTiles true): a block takes the next 8x8 pixel tile (tiles queued
-// by total length, longest first) and its warps take the tile's rays in
-// pixel order, so the block's warps trace neighbouring rays at the same
-// time -- rays that cross the same voxels, whose ln q gathers then share L1
-// lines.  Which warp handles a ray does not change its result.  Variants
-// differ only in register budget (kMinBlocks resident blocks per SM), load
-// policy and scheduling: their arithmetic is identical, so the autotuner's
-// choice never changes a result.
-template <int kMinBlocks, int kPol, int kPf, bool kTiles>
+// Persistent launch: each warp takes the next ray from a work counter; rays
+// are queued longest first (sorted once per incidence build, their RayMeta
+// records copied into queue order), so the long rays start early and the
+// short ones fill the tail.  Which warp handles a ray does not change its
+// result.  Variants differ only in register budget (kMinBlocks resident
+// blocks per SM) and load policy: their arithmetic is identical, so the
+// autotuner's choice never changes a result.
+template <int kMinBlocks, int kPol, int kPf>
 __global__ void __launch_bounds__(kRayWarps * 32, kMinBlocks) k_ray_bp(const RayMeta* __restrict__ queue,
                                                            uint32_t n_rays,
-                                                           const uint2* __restrict__ tiles,
-                                                           uint32_t n_tiles,
                                                            uint32_t* __restrict__ counter,
                                                            const uint32_t* __restrict__ inc_pair,
                                                            const float* __restrict__ inc_len,
@@ -509,34 +450,16 @@ __global__ void __launch_bounds__(kRayWarps * 32, kMinBlocks) k_ray_bp(const Ray
                                                            float* __restrict__ inc_pl,
                                                            int fix_reset) {
   const int lane = threadIdx.x & 31;
-  auto ray = [&](const RayMeta& me) {
+  for (;;) {
+    uint32_t idx = 0;
+    if (lane == 0) idx = atomicAdd(counter, 1u);
+    idx = __shfl_sync(kFull, idx, 0);
+    if (idx >= n_rays) break;
+    const RayMeta me = queue[idx];
     if (me.n_pre <= kLongRay)
       ray_bp_warp<float, kPol, kPf>(me, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
     else
       ray_bp_warp<double, kPol, kPf>(me, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
-  };
-  if constexpr (kTiles) {
-    __shared__ uint2 s_tile;
-    const uint32_t warp = threadIdx.x >> 5;
-    for (;;) {
-      if (threadIdx.x == 0) {
-        const uint32_t t = atomicAdd(counter, 1u);
-        s_tile = t < n_tiles ? tiles[t] : make_uint2(0u, 0u);  // (first ray, rays); 0 rays: done
-      }
-      __syncthreads();
-      const uint2 tl = s_tile;
-      __syncthreads();  // read by every warp before thread 0 takes the next tile
-      if (tl.y == 0) break;
-      for (uint32_t r = warp; r < tl.y; r += kRayWarps) ray(queue[tl.x + r]);
-    }
-  } else {
-    for (;;) {
-      uint32_t idx = 0;
-      if (lane == 0) idx = atomicAdd(counter, 1u);
-      idx = __shfl_sync(kFull, idx, 0);
-      if (idx >= n_rays) break;
-      ray(queue[idx]);
-    }
   }
 }
 
@@ -939,12 +862,9 @@ cudaError_t launch_pair_prepare(const BpArrays& a, uint32_t p0, uint32_t p1, int
 
 
 // ray-kernel variants: (id, resident-block target, load policy, chunk
-// prefetch, tile queue)
-#define MRF_RAY_VARIANTS(X) \
-  X(0, 0, 0, 0, false) X(1, 0, 0, 1, false) X(2, 0, 0, 2, false) X(3, 0, 0, 0, true) X(4, 0, 0, 1, true) \
-  X(5, 0, 0, 2, true)
-constexpr int kRayVariants = 6;
-constexpr bool kRayTiles[kRayVariants] = {false, false, false, true, true, true};
+// prefetch)
+#define MRF_RAY_VARIANTS(X) X(0, 0, 0, 0) X(1, 0, 0, 1) X(2, 0, 0, 2) X(3, 0, 1, 1)
+constexpr int kRayVariants = 4;
 
 int ray_bp_variants() { return kRayVariants; }
 
@@ -965,9 +885,9 @@ int ray_bp_resident_blocks(int variant) {
   if (variant < 0 || variant >= kRayVariants) return 1;
   if (!resident[variant]) {
     switch (variant) {
-#define X(id, mb, pol, pf, tl) \
-  case id:                     \
-    resident[variant] = resident_of(k_ray_bp<mb, pol, pf, tl>); \
+#define X(id, mb, pol, pf) \
+  case id:                 \
+    resident[variant] = resident_of(k_ray_bp<mb, pol, pf>); \
     break;
       MRF_RAY_VARIANTS(X)
 #undef X
@@ -976,21 +896,19 @@ int ray_bp_resident_blocks(int variant) {
   return resident[variant];
 }
 
-cudaError_t launch_ray_bp(const BpArrays& a, const RayWork& w, uint32_t* counter, int fix_reset,
-                          int num_sms, int variant, cudaStream_t s) {
+cudaError_t launch_ray_bp(const BpArrays& a, const RayMeta* queue, uint32_t n_rays, uint32_t* counter,
+                          int fix_reset, int num_sms, int variant, cudaStream_t s) {
+  if (!n_rays) return cudaSuccess;
   if (variant < 0 || variant >= kRayVariants) return cudaErrorInvalidValue;
-  const bool tiled = kRayTiles[variant];
-  const int64_t need = tiled ? w.n_tiles : (w.n_rays + kRayWarps - 1) / kRayWarps;
-  if (need == 0) return cudaSuccess;
-  int64_t b = std::min<int64_t>((int64_t)num_sms * ray_bp_resident_blocks(variant), need);
+  int64_t b = std::min<int64_t>((int64_t)num_sms * ray_bp_resident_blocks(variant),
+                                (n_rays + kRayWarps - 1) / kRayWarps);
   const unsigned grid = (unsigned)std::max<int64_t>(b, 1);
-  const RayMeta* q = tiled ? w.tile_queue : w.queue;
   switch (variant) {
-#define X(id, mb, pol, pf, tl)                                                                     \
+#define X(id, mb, pol, pf)                                                                        \
   case id:                                                                                        \
-    k_ray_bp<mb, pol, pf, tl><<<grid, kRayWarps * 32, 0, s>>>(q, w.n_rays, w.tiles, w.n_tiles, counter, \
-                                                              a.inc_pair, a.inc_len, a.inc_mu,      \
-                                                              a.pair_lnq, a.inc_pl, fix_reset);     \
+    k_ray_bp<mb, pol, pf><<<grid, kRayWarps * 32, 0, s>>>(queue, n_rays, counter, a.inc_pair,         \
+                                                          a.inc_len, a.inc_mu, a.pair_lnq,          \
+                                                          a.inc_pl, fix_reset);                    \
     break;
     MRF_RAY_VARIANTS(X)
 #undef X

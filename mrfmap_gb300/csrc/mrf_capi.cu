@@ -119,7 +119,6 @@ struct View {
   uint32_t dperm_base = 0, n_dperm = 0;   // ... of the dynamic ones
   uint32_t dpair_base = 0, n_dpairs = 0;  // runs of dynamic incidences (one per pair)
   uint32_t order_base = 0, n_active = 0;  // ray queue (longest first)
-  uint32_t tiles_base = 0, n_tiles = 0;   // tile-queue descriptors (8x8 pixel tiles)
   uint32_t tile_base = 0;                 // first pair of each pair-update tile
 };
 
@@ -142,12 +141,11 @@ struct mrf_map {
   std::vector<int> h_coord;
   int version = 0, built_version = -1;
   int ray_variant = 0;  // ray-kernel variant (mrf_autotune / mrf_set_ray_variant)
-  uint32_t n_tiles_all = 0;  // tile-queue descriptors of all views
   bool has_messages = false;
   std::vector<View> views;
   // arenas
   DBuf meta, inc_pair, inc_len, inc_mu, inc_pl, pair_vox, pair_m, pair_cum, pair_stat, pair_ndyn, pair_hit,
-      pair_q, pair_dm, pair_seg, dperm, s_q0, s_q1, s_q2, s_q3, s_bf, dpair, dseg, drun, carry, ray_order, ray_queue, tile_queue, tiles, counters,
+      pair_q, pair_dm, pair_seg, dperm, s_q0, s_q1, s_q2, s_q3, s_bf, dpair, dseg, drun, carry, ray_order, ray_queue, counters,
       tile_first;
   uint32_t jac_tile_base = 0;
   int64_t n_inc = 0, n_pairs = 0, n_dperm = 0, n_dpairs = 0;
@@ -524,54 +522,6 @@ void rebuild(mrf_map* m) {
       base += act;
     }
     m->counters.reserve((size_t)(V + 1) * 4, false, m->stream);
-    // tile queue: per view the 8x8 pixel tiles that hold active rays, by
-    // total Pre length (longest first, ties by tile index), each with its
-    // active rays in pixel order
-    std::vector<uint32_t> torder;
-    std::vector<uint2> tdesc;
-    torder.reserve((size_t)base);
-    for (int c = 0; c < V; ++c) {
-      View& v = m->views[c];
-      const int rows = v.cam.rows, cols = v.cam.cols;
-      const int tx = (cols + kRayTile - 1) / kRayTile, ty = (rows + kRayTile - 1) / kRayTile;
-      std::vector<std::pair<int64_t, int>> order;  // (-length, tile)
-      for (int t = 0; t < tx * ty; ++t) {
-        const int x0 = (t % tx) * kRayTile, y0 = (t / tx) * kRayTile;
-        int64_t len = 0;
-        for (int y = y0; y < std::min(y0 + kRayTile, rows); ++y)
-          for (int x = x0; x < std::min(x0 + kRayTile, cols); ++x)
-            len += hm[(size_t)(v.pix_base + (int64_t)y * cols + x)].n_pre;
-        if (len) order.emplace_back(-len, t);
-      }
-      std::sort(order.begin(), order.end());
-      v.tiles_base = (uint32_t)tdesc.size();
-      for (const auto& o : order) {
-        const int t = o.second;
-        const int x0 = (t % tx) * kRayTile, y0 = (t / tx) * kRayTile;
-        const uint32_t first = (uint32_t)torder.size();
-        for (int y = y0; y < std::min(y0 + kRayTile, rows); ++y)
-          for (int x = x0; x < std::min(x0 + kRayTile, cols); ++x) {
-            const int64_t pix = v.pix_base + (int64_t)y * cols + x;
-            if (hm[(size_t)pix].n_pre > 0) torder.push_back((uint32_t)pix);
-          }
-        tdesc.push_back(make_uint2(first, (uint32_t)torder.size() - first));
-      }
-      v.n_tiles = (uint32_t)tdesc.size() - v.tiles_base;
-    }
-    const size_t nq = std::max<size_t>(torder.size(), 1);
-    m->tile_queue.reserve(nq * sizeof(RayMeta), false, m->stream);
-    m->tiles.reserve(std::max<size_t>(tdesc.size(), 1) * sizeof(uint2), false, m->stream);
-    if (!torder.empty()) {
-      // ray_order is free again once the longest-first queues are gathered
-      CK(cudaMemcpyAsync(m->ray_order.p, torder.data(), torder.size() * 4, cudaMemcpyHostToDevice,
-                         m->stream));
-      CK(launch_ray_queue(m->meta.as<RayMeta>(), m->ray_order.as<uint32_t>(), (uint32_t)torder.size(),
-                          m->tile_queue.as<RayMeta>(), m->stream));
-      CK(cudaMemcpyAsync(m->tiles.p, tdesc.data(), tdesc.size() * sizeof(uint2), cudaMemcpyHostToDevice,
-                         m->stream));
-      sync(m);  // the host vectors go out of scope
-    }
-    m->n_tiles_all = (uint32_t)tdesc.size();
   }
   m->n_inc = n_inc;
   m->n_pairs = pair_total;
@@ -729,16 +679,11 @@ struct Profiler {
 // pairs without dynamic incidences get their (constant) update in the first
 // iteration of each mrf_infer call only: afterwards it would leave every
 // value unchanged (L + (m_new - m_new) = L).
-// the rays of one view, and of all views (their queues are contiguous)
-RayWork view_work(mrf_map* m, const View& v) {
-  return RayWork{m->ray_queue.as<RayMeta>() + v.order_base, v.n_active, m->tile_queue.as<RayMeta>(),
-                 m->tiles.as<uint2>() + v.tiles_base, v.n_tiles};
-}
-RayWork all_work(mrf_map* m) {
+// rays of all views (the views' queues are contiguous)
+uint32_t all_rays(const mrf_map* m) {
   uint32_t nact = 0;
   for (const View& v : m->views) nact += v.n_active;
-  return RayWork{m->ray_queue.as<RayMeta>(), nact, m->tile_queue.as<RayMeta>(), m->tiles.as<uint2>(),
-                 m->n_tiles_all};
+  return nact;
 }
 
 void enqueue_iteration(mrf_map* m, const BpArrays& a, bool jacobi, int fix, bool first,
@@ -753,8 +698,8 @@ void enqueue_iteration(mrf_map* m, const BpArrays& a, bool jacobi, int fix, bool
       CK(launch_pair_prepare(a, v.pair_base, v.pair_base + v.n_pairs, 0, m->stream));
       prof.end();
       prof.begin(1);
-      CK(launch_ray_bp(a, view_work(m, v), m->counters.as<uint32_t>() + c, fix, m->num_sms, m->ray_variant,
-                       m->stream));
+      CK(launch_ray_bp(a, m->ray_queue.as<RayMeta>() + v.order_base, v.n_active,
+                       m->counters.as<uint32_t>() + c, fix, m->num_sms, m->ray_variant, m->stream));
       prof.end();
       prof.begin(2);
       if (v.n_dperm) {
@@ -777,8 +722,8 @@ void enqueue_iteration(mrf_map* m, const BpArrays& a, bool jacobi, int fix, bool
     prof.end();
     prof.begin(1);
     // the queues of all views are contiguous: one launch over all rays
-    CK(launch_ray_bp(a, all_work(m), m->counters.as<uint32_t>() + V, fix, m->num_sms, m->ray_variant,
-                     m->stream));
+    CK(launch_ray_bp(a, m->ray_queue.as<RayMeta>(), all_rays(m), m->counters.as<uint32_t>() + V, fix,
+                     m->num_sms, m->ray_variant, m->stream));
     prof.end();
     prof.begin(2);
     CK(launch_pair_update(a, 0, (uint32_t)m->n_dperm, 0, (uint32_t)m->n_dpairs,
@@ -972,7 +917,7 @@ void destroy_bufs(mrf_map* m) {
                  &m->pair_m, &m->pair_cum, &m->pair_stat, &m->pair_ndyn, &m->pair_hit, &m->pair_q,
                  &m->pair_dm,
                  &m->pair_seg, &m->dperm, &m->dpair, &m->dseg, &m->drun,
-                 &m->carry, &m->ray_order, &m->ray_queue, &m->tile_queue, &m->tiles, &m->counters, &m->tile_first,
+                 &m->carry, &m->ray_order, &m->ray_queue, &m->counters, &m->tile_first,
                  &m->vseg, &m->vpairs, &m->vvox, &m->s_rec, &m->s_recs, &m->s_pf, &m->s_ps,
                  &m->s_flags, &m->s_ind, &m->s_scan,
                  &m->s_q0, &m->s_q1, &m->s_q2, &m->s_q3, &m->s_bf,
@@ -1267,8 +1212,8 @@ static void warm_start_impl(mrf_map* m, const float* L_pred, bool device_ptr, in
   for (int k = 0; k < sweeps; ++k) {
     CK(cudaMemsetAsync(m->counters.p, 0, (size_t)(V + 1) * 4, m->stream));
     CK(launch_pair_prepare(a, 0, P, 1, m->stream));
-    CK(launch_ray_bp(a, all_work(m), m->counters.as<uint32_t>() + V, 0, m->num_sms, m->ray_variant,
-                     m->stream));
+    CK(launch_ray_bp(a, m->ray_queue.as<RayMeta>(), all_rays(m), m->counters.as<uint32_t>() + V, 0,
+                     m->num_sms, m->ray_variant, m->stream));
     CK(launch_pair_update(a, 0, (uint32_t)m->n_dperm, 0, (uint32_t)m->n_dpairs,
                           m->tile_first.as<uint32_t>() + m->jac_tile_base, m->carry.as<TileCarry>(),
                           1, m->stream));

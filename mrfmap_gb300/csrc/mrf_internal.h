@@ -179,21 +179,10 @@ cudaError_t launch_pair_prepare(const BpArrays& a, uint32_t p0, uint32_t p1, int
 int ray_bp_variants();
 // resident blocks per SM of a variant of the persistent ray kernel (queried once)
 int ray_bp_resident_blocks(int variant);
-// the rays of one ray-kernel launch, in two schedules: queue[0..n_rays)
-// longest first, and the tile queue (rays of 8x8 pixel tiles in pixel
-// order, tiles longest first) with its descriptors tiles[0..n_tiles) =
-// (first tile-queue index, rays)
-constexpr int kRayTile = 8;  // tile-queue tiles are kRayTile x kRayTile pixels
-struct RayWork {
-  const RayMeta* queue;
-  uint32_t n_rays;
-  const RayMeta* tile_queue;
-  const uint2* tiles;
-  uint32_t n_tiles;
-};
-// counter: one zeroed u32 per launch
-cudaError_t launch_ray_bp(const BpArrays& a, const RayWork& w, uint32_t* counter, int fix_reset,
-                          int num_sms, int variant, cudaStream_t s);
+// rays queue[0..n_rays) (RayMeta records, longest first); counter: one
+// zeroed u32 per launch
+cudaError_t launch_ray_bp(const BpArrays& a, const RayMeta* queue, uint32_t n_rays, uint32_t* counter,
+                          int fix_reset, int num_sms, int variant, cudaStream_t s);
 cudaError_t launch_ray_keys(const RayMeta* meta, uint32_t n, uint32_t* keys, uint32_t* vals,
                             cudaStream_t s);
 // queue[i] = meta[order[i]], i < n
