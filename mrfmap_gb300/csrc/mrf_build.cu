@@ -157,9 +157,16 @@ __global__ void k_set_points(Geom g, const float* __restrict__ pts, const float*
 
 // One thread per pixel walks the DDA through the active bricks.  Runs of
 // voxels in one brick end with the reference's per-brick stop tests; the
-// count pass and the emit pass execute the identical loop.
+// count pass and the emit pass execute the identical loop.  The emit pass
+// keeps the last four incidences in registers (a shift register) and
+// stores each aligned group of four as 16-byte vectors: ray offsets are
+// multiples of four, so a ray's lists start on a group boundary, and the
+// last group is completed with padding.  Every field of an incidence,
+// including its build record, is known when it is emitted: the Post range
+// ends at a brick-run boundary after which nothing more counts, and an
+// incidence is dynamic once a non-zero potential has been seen inside it.
 template <bool EMIT>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 4)
     k_trace(Geom g, Pose P, const float* __restrict__ depth, uint32_t* __restrict__ counts,
             const uint32_t* __restrict__ pix_off, uint32_t inc_base, RayMeta* __restrict__ meta,
             uint32_t* __restrict__ inc_vox, float* __restrict__ inc_len,
@@ -171,6 +178,43 @@ __global__ void __launch_bounds__(kThreads)
   int count = 0, n_pre = -1, n_post = -1, r0 = -1, run_start = 0, kmu = -1;
   bool gate = false;
   uint32_t base = EMIT ? pix_off[pix] : 0;
+  uint32_t bv[4] = {kNoVoxel, kNoVoxel, kNoVoxel, kNoVoxel};
+  float bl[4] = {0.0f, 0.0f, 0.0f, 0.0f}, bm[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+  uint32_t bf = 0;  // per slot: bit 0 in the Post range, bit 1 dynamic
+  // shift one incidence into the group; store the group when it is whole
+  auto push = [&](uint32_t v, float len, float mu, uint32_t f) {
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      bv[j] = bv[j + 1];
+      bl[j] = bl[j + 1];
+      bm[j] = bm[j + 1];
+    }
+    bv[3] = v;
+    bl[3] = len;
+    bm[3] = mu;
+    bf = (bf >> 2) | (f << 6);
+  };
+  // build record: the length counting towards the cumulative length (Post
+  // range only) and, for a dynamic incidence, -(mu * l) (the sign bit marks
+  // the class; -0 when mu is 0)
+  auto rec = [&](int j, float& pl, float& dl) {
+    const uint32_t f = (bf >> (2 * j)) & 3u;
+    pl = (f & 1u) ? bl[j] : 0.0f;
+    dl = (f & 2u) ? -(bm[j] * pl) : 0.0f;
+  };
+  auto store = [&](uint32_t k0) {
+    *reinterpret_cast<uint4*>(inc_vox + k0) = make_uint4(bv[0], bv[1], bv[2], bv[3]);
+    *reinterpret_cast<float4*>(inc_len + k0) = make_float4(bl[0], bl[1], bl[2], bl[3]);
+    *reinterpret_cast<float4*>(inc_mu + k0) = make_float4(bm[0], bm[1], bm[2], bm[3]);
+    float p0, d0, p1, d1, p2, d2, p3, d3;
+    rec(0, p0, d0);
+    rec(1, p1, d1);
+    rec(2, p2, d2);
+    rec(3, p3, d3);
+    float4* r = reinterpret_cast<float4*>(inc_rec + k0);
+    r[0] = make_float4(p0, d0, p1, d1);
+    r[1] = make_float4(p2, d2, p3, d3);
+  };
   if (d > 0.0f) {
     int x = pix % g.cols, y = pix / g.cols;
     const float* sg = lut_at(g, g.sigma, x, y);
@@ -210,13 +254,16 @@ __global__ void __launch_bounds__(kThreads)
         float s = fm(te, ray.mult);
         if (!run_open) run_start = count;
         if (EMIT) {
-          uint32_t k = base + (uint32_t)count;
-          inc_vox[k] = (uint32_t)slot * kBrickVox + voxel_local(vx, vy, vz);
-          inc_len[k] = l;
-          bool z = potential_is_zero(sg, bs, n, s, d);
-          inc_mu[k] = z ? 0.0f : potential(sg, bs, n, s, d);
+          const bool z = potential_is_zero(sg, bs, n, s, d);
+          const float mu = z ? 0.0f : potential(sg, bs, n, s, d);
           if (r0 < 0 && !z) r0 = run_start;
           if (kmu < 0 && !z) kmu = count;
+          // in the Post range until n_post is set; dynamic from the first
+          // non-zero potential on
+          const uint32_t in_post = n_post < 0 ? 1u : 0u;
+          const uint32_t f = in_post | ((in_post && kmu >= 0) ? 2u : 0u);
+          push((uint32_t)slot * kBrickVox + voxel_local(vx, vy, vz), l, mu, f);
+          if ((count & 3) == 3) store(base + (uint32_t)(count - 3));
         }
         run_open = true;
         s_last = s;
@@ -242,20 +289,13 @@ __global__ void __launch_bounds__(kThreads)
   if (!EMIT) {
     counts[pix] = (uint32_t)padded;
   } else {
-    for (int k = n_pre; k < padded; ++k) {
-      inc_vox[base + k] = kNoVoxel;
-      inc_len[base + k] = 0.0f;
-      inc_mu[base + k] = 0.0f;
+    // the last group, completed with padding (invalid voxel, zeros)
+    if (count & 3) {
+      const int k0 = count & ~3;
+      for (int k = count; k < padded; ++k) push(kNoVoxel, 0.0f, 0.0f, 0u);
+      store(base + (uint32_t)k0);
     }
-    // per-incidence build record: the length that counts towards the
-    // cumulative length (Post range only) and, for a dynamic incidence,
-    // -(mu * l) (the sign bit marks the class; -0 when mu is 0)
     const int kdyn = (kmu >= 0 && kmu < n_post) ? kmu : n_post;
-    for (int k = 0; k < padded; ++k) {
-      const float pl = k < n_post ? inc_len[base + k] : 0.0f;
-      const bool dyn = k >= kdyn && k < n_post;
-      inc_rec[base + k] = make_float2(pl, dyn ? copysignf(inc_mu[base + k] * pl, -1.0f) : 0.0f);
-    }
     RayMeta m;
     m.off = inc_base + base;
     m.n_pre = (uint16_t)n_pre;
