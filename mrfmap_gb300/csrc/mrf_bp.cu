@@ -495,6 +495,26 @@ constexpr int kTileThreads = 256;
 constexpr int kTile = 4 * kTileThreads;
 constexpr uint32_t kOpenStart = 1u, kOpenEnd = 2u, kSingle = 4u;
 
+// a dynamic run's update with its old message mo and the voxel's old total
+// Lo already loaded (the gate c > kCumLenGate already checked)
+__device__ __forceinline__ void apply_run_loaded(const uint4 r, float mo, float Lo, float acc_dyn,
+                                                 float* __restrict__ m, float* __restrict__ L,
+                                                 float* __restrict__ belief, float* __restrict__ dm,
+                                                 int jacobi) {
+  const uint32_t p = r.x, v = r.y;
+  const float c = __uint_as_float(r.z);
+  float a = clampf((__uint_as_float(r.w) + acc_dyn) / c, kFEps, 1.0f - kFEps);
+  float mn = logf(a) - logf(1.0f - a);
+  m[p] = mn;
+  if (jacobi) {
+    dm[p] = mn - mo;
+    return;
+  }
+  float Lv = Lo + (mn - mo);
+  L[v] = Lv;
+  belief[v] = 1.0f - clampf(1.0f / (1.0f + expf(Lv)), kFEps, 1.0f - kFEps);
+}
+
 // factor->voxel update of one pair (gvdbkernels.cu:457-479)
 __device__ __forceinline__ void apply_pair(uint32_t p, float acc, const uint32_t* __restrict__ pair_vox,
                                            float* __restrict__ m, const float* __restrict__ cum,
@@ -525,18 +545,7 @@ __device__ __forceinline__ void apply_run(const uint4 r, float acc_dyn, float* _
   const uint32_t p = r.x, v = r.y;
   const float c = __uint_as_float(r.z);
   if (!(c > kCumLenGate)) return;  // gvdbkernels.cu:408: the pair never updates
-  const float mo = m[p];
-  const float Lo = jacobi ? 0.0f : L[v];
-  float a = clampf((__uint_as_float(r.w) + acc_dyn) / c, kFEps, 1.0f - kFEps);
-  float mn = logf(a) - logf(1.0f - a);
-  m[p] = mn;
-  if (jacobi) {
-    dm[p] = mn - mo;
-    return;
-  }
-  float Lv = Lo + (mn - mo);
-  L[v] = Lv;
-  belief[v] = 1.0f - clampf(1.0f / (1.0f + expf(Lv)), kFEps, 1.0f - kFEps);
+  apply_run_loaded(r, m[p], jacobi ? 0.0f : L[v], acc_dyn, m, L, belief, dm, jacobi);
 }
 
 __global__ void __launch_bounds__(kTileThreads, 8)
@@ -554,12 +563,24 @@ __global__ void __launch_bounds__(kTileThreads, 8)
   const uint32_t pf = tile_first[blockIdx.x];
   // a tile touches at most n pairs: their starts and the next pair's start
   const uint32_t nseg = min(n + 1, p_end - pf) + 1;
+  // the run record of this thread's first pair, and that pair's message and
+  // voxel total, are requested before the message gathers so that neither
+  // dependent load waits after the barrier
+  uint4 r0 = make_uint4(0u, 0u, 0u, 0u);
+  float mo0 = 0.0f, Lo0 = 0.0f;
+  const bool pre = t < n && pf + t < p_end;
+  if (pre) r0 = drun[pf + t];
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
     uint32_t i = j * kTileThreads + t;
     if (i < n) sv[i] = pl[perm[base + i]];
   }
   for (uint32_t q = t; q < nseg; q += kTileThreads) sseg[q] = seg[pf + q];
+  const bool gate0 = pre && __uint_as_float(r0.z) > kCumLenGate;
+  if (gate0) {
+    mo0 = m[r0.x];
+    if (!jacobi) Lo0 = L[r0.y];
+  }
   __syncthreads();
   for (uint32_t q = t; q < n && pf + q < p_end && sseg[q] < end; q += kTileThreads) {
     const uint32_t s0 = sseg[q], s1 = sseg[q + 1];
@@ -568,7 +589,11 @@ __global__ void __launch_bounds__(kTileThreads, 8)
     for (uint32_t i = a; i < b; ++i) acc += sv[i];
     const bool open_start = s0 < base, open_end = s1 > end;
     if (!open_start && !open_end) {
-      apply_run(drun[pf + q], acc, m, L, belief, dm, jacobi);
+      if (q == t) {
+        if (gate0) apply_run_loaded(r0, mo0, Lo0, acc, m, L, belief, dm, jacobi);
+      } else {
+        apply_run(drun[pf + q], acc, m, L, belief, dm, jacobi);
+      }
       continue;
     }
     TileCarry& c = carry[blockIdx.x];
