@@ -432,16 +432,29 @@ __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, const uint32_t* _
   }
 }
 
-// Persistent launch: each warp takes the next ray from a work counter; rays
-// are queued longest first (sorted once per incidence build, their RayMeta
-// records copied into queue order), so the long rays start early and the
-// short ones fill the tail.  Which warp handles a ray does not change its
-// result.  Variants differ only in register budget (kMinBlocks resident
-// blocks per SM) and load policy: their arithmetic is identical, so the
-// autotuner's choice never changes a result.
-template <int kMinBlocks, int kPol, int kPf>
+// Persistent launch: each warp takes the next ray from a work counter.
+// kReg false: one queue, rays longest first (sorted once per incidence
+// build, their RayMeta records copied into queue order), so the long rays
+// start early and the short ones fill the tail.  kReg true (SM-affine):
+// the view's pixels are cut into regions of consecutive pixels holding
+// equal shares of its incidences, one region per SM-resident group of
+// blocks (block b serves regions b mod G, + G, ..., G = min(grid, regions);
+// the persistent grid is dispatched round-robin over the SMs, so the
+// blocks of one region share an SM); a warp takes the home rays of its
+// regions, then drains the view's leftover queue of short rays.  The warps
+// of one SM trace neighbouring rays at the same time -- rays that cross the
+// same voxels, so their ln q gathers hit the SM's L1.  Which warp handles a ray does not
+// change its result.  Variants differ only in register budget (kMinBlocks
+// resident blocks per SM), load policy and schedule: their arithmetic is
+// identical, so the autotuner's choice never changes a result.
+template <int kMinBlocks, int kPol, int kPf, bool kReg>
 __global__ void __launch_bounds__(kRayWarps * 32, kMinBlocks) k_ray_bp(const RayMeta* __restrict__ queue,
                                                            uint32_t n_rays,
+                                                           const uint32_t* __restrict__ rstart,
+                                                           uint32_t nreg,
+                                                           const RayMeta* __restrict__ left,
+                                                           uint32_t n_left,
+                                                           uint32_t* __restrict__ lcounter,
                                                            uint32_t* __restrict__ counter,
                                                            const uint32_t* __restrict__ inc_pair,
                                                            const float* __restrict__ inc_len,
@@ -450,16 +463,42 @@ __global__ void __launch_bounds__(kRayWarps * 32, kMinBlocks) k_ray_bp(const Ray
                                                            float* __restrict__ inc_pl,
                                                            int fix_reset) {
   const int lane = threadIdx.x & 31;
-  for (;;) {
-    uint32_t idx = 0;
-    if (lane == 0) idx = atomicAdd(counter, 1u);
-    idx = __shfl_sync(kFull, idx, 0);
-    if (idx >= n_rays) break;
-    const RayMeta me = queue[idx];
+  auto ray = [&](const RayMeta& me) {
     if (me.n_pre <= kLongRay)
       ray_bp_warp<float, kPol, kPf>(me, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
     else
       ray_bp_warp<double, kPol, kPf>(me, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
+  };
+  if constexpr (kReg) {
+    // counter[r]: tickets of region r; rstart[r] .. rstart[r + 1] its home
+    // rays.  Block b serves regions b mod G, + G, ... (G = min(grid,
+    // regions): every region has a home block).
+    const uint32_t G = min(gridDim.x, nreg);
+    for (uint32_t r = blockIdx.x % G; r < nreg; r += G) {
+      const uint32_t a = rstart[r], nr = rstart[r + 1] - a;
+      for (;;) {
+        uint32_t idx = 0;
+        if (lane == 0) idx = atomicAdd(counter + r, 1u);
+        idx = __shfl_sync(kFull, idx, 0);
+        if (idx >= nr) break;
+        ray(queue[a + idx]);
+      }
+    }
+    for (;;) {
+      uint32_t idx = 0;
+      if (lane == 0) idx = atomicAdd(lcounter, 1u);
+      idx = __shfl_sync(kFull, idx, 0);
+      if (idx >= n_left) break;
+      ray(left[idx]);
+    }
+  } else {
+    for (;;) {
+      uint32_t idx = 0;
+      if (lane == 0) idx = atomicAdd(counter, 1u);
+      idx = __shfl_sync(kFull, idx, 0);
+      if (idx >= n_rays) break;
+      ray(queue[idx]);
+    }
   }
 }
 
@@ -887,9 +926,10 @@ cudaError_t launch_pair_prepare(const BpArrays& a, uint32_t p0, uint32_t p1, int
 
 
 // ray-kernel variants: (id, resident-block target, load policy, chunk
-// prefetch)
-#define MRF_RAY_VARIANTS(X) X(0, 0, 0, 0) X(1, 0, 0, 1) X(2, 0, 0, 2) X(3, 0, 1, 1)
-constexpr int kRayVariants = 4;
+// prefetch, schedule: 0 longest first, 1 SM regions)
+#define MRF_RAY_VARIANTS(X) \
+  X(0, 0, 0, 0, 0) X(1, 0, 0, 1, 0) X(2, 0, 0, 2, 0) X(3, 0, 0, 0, 1) X(4, 0, 0, 1, 1) X(5, 0, 0, 2, 1)
+constexpr int kRayVariants = 6;
 
 int ray_bp_variants() { return kRayVariants; }
 
@@ -910,9 +950,9 @@ int ray_bp_resident_blocks(int variant) {
   if (variant < 0 || variant >= kRayVariants) return 1;
   if (!resident[variant]) {
     switch (variant) {
-#define X(id, mb, pol, pf) \
-  case id:                 \
-    resident[variant] = resident_of(k_ray_bp<mb, pol, pf>); \
+#define X(id, mb, pol, pf, sc) \
+  case id:                     \
+    resident[variant] = resident_of(k_ray_bp<mb, pol, pf, (sc > 0)>); \
     break;
       MRF_RAY_VARIANTS(X)
 #undef X
@@ -921,19 +961,20 @@ int ray_bp_resident_blocks(int variant) {
   return resident[variant];
 }
 
-cudaError_t launch_ray_bp(const BpArrays& a, const RayMeta* queue, uint32_t n_rays, uint32_t* counter,
-                          int fix_reset, int num_sms, int variant, cudaStream_t s) {
-  if (!n_rays) return cudaSuccess;
+cudaError_t launch_ray_bp(const BpArrays& a, const RayWork& w, int fix_reset, int num_sms, int variant,
+                          cudaStream_t s) {
+  if (!w.n_rays) return cudaSuccess;
   if (variant < 0 || variant >= kRayVariants) return cudaErrorInvalidValue;
   int64_t b = std::min<int64_t>((int64_t)num_sms * ray_bp_resident_blocks(variant),
-                                (n_rays + kRayWarps - 1) / kRayWarps);
+                                (w.n_rays + kRayWarps - 1) / kRayWarps);
   const unsigned grid = (unsigned)std::max<int64_t>(b, 1);
   switch (variant) {
-#define X(id, mb, pol, pf)                                                                        \
+#define X(id, mb, pol, pf, sc)                                                                    \
   case id:                                                                                        \
-    k_ray_bp<mb, pol, pf><<<grid, kRayWarps * 32, 0, s>>>(queue, n_rays, counter, a.inc_pair,         \
-                                                          a.inc_len, a.inc_mu, a.pair_lnq,          \
-                                                          a.inc_pl, fix_reset);                    \
+    k_ray_bp<mb, pol, pf, (sc > 0)><<<grid, kRayWarps * 32, 0, s>>>(                              \
+        sc == 0 ? w.queue : w.region, w.n_rays, w.rstart, w.nreg,                                 \
+        w.left, w.n_left, w.lcounter, sc == 0 ? w.counter : w.rcounter, a.inc_pair, a.inc_len,       \
+        a.inc_mu, a.pair_lnq, a.inc_pl, fix_reset);                                               \
     break;
     MRF_RAY_VARIANTS(X)
 #undef X

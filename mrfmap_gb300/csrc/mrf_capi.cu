@@ -17,6 +17,7 @@
 
 #include <algorithm>
 #include <mutex>
+#include <thread>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -119,6 +120,7 @@ struct View {
   uint32_t dperm_base = 0, n_dperm = 0;   // ... of the dynamic ones
   uint32_t dpair_base = 0, n_dpairs = 0;  // runs of dynamic incidences (one per pair)
   uint32_t order_base = 0, n_active = 0;  // ray queue (longest first)
+  uint32_t left_base = 0, n_left = 0;     // leftover queue of the SM-affine schedule
   uint32_t tile_base = 0;                 // first pair of each pair-update tile
 };
 
@@ -140,12 +142,16 @@ struct mrf_map {
   int64_t nb_grid = 0, n_bricks = 0;
   std::vector<int> h_coord;
   int version = 0, built_version = -1;
-  int ray_variant = 0;  // ray-kernel variant (mrf_autotune / mrf_set_ray_variant)
+  int ray_variant = 4;  // ray-kernel variant (mrf_autotune / mrf_set_ray_variant); 4: SM regions,
+                        // pair-id prefetch, the fastest on the bench workloads
+  uint32_t nreg = 1;    // SM regions per view of the region queues
+  uint32_t n_left_all = 0;
+  uint32_t region_home_n = 0;  // region_q: home rays of all regions, then the leftovers
   bool has_messages = false;
   std::vector<View> views;
   // arenas
   DBuf meta, inc_pair, inc_len, inc_mu, inc_pl, pair_vox, pair_m, pair_cum, pair_stat, pair_ndyn, pair_hit,
-      pair_q, pair_dm, pair_seg, dperm, s_q0, s_q1, s_q2, s_q3, s_bf, dpair, dseg, drun, carry, ray_order, ray_queue, counters,
+      pair_q, pair_dm, pair_seg, dperm, s_q0, s_q1, s_q2, s_q3, s_bf, dpair, dseg, drun, carry, ray_order, ray_queue, region_q, rstart, rcounters, counters,
       tile_first;
   uint32_t jac_tile_base = 0;
   int64_t n_inc = 0, n_pairs = 0, n_dperm = 0, n_dpairs = 0;
@@ -522,6 +528,120 @@ void rebuild(mrf_map* m) {
       base += act;
     }
     m->counters.reserve((size_t)(V + 1) * 4, false, m->stream);
+    // SM-affine region queues: per view, R = SM count regions of
+    // consecutive pixels holding equal shares of the view's Pre incidences.
+    // A region's home rays (its longest rays up to kHomeShare of its
+    // incidences, longest first) are taken by the blocks homed on it; every region's remaining short rays go to one leftover
+    // queue of the view (longest first) that the blocks drain afterwards,
+    // which evens out the regions' finishing times (home shares of 60, 75
+    // and 85 % measured: 75 % best on the bench workloads).  rstart (flat over the views,
+    // V * R + 1 entries) holds each region's first home position.
+    const int R = std::max(1, m->num_sms);
+    constexpr int64_t kHomeShare = 75;  // per cent of a region's incidences taken by its home blocks
+    // per view, in parallel host threads, in linear time: a counting sort
+    // by length (longest first) feeds the regions' buckets in order, so each
+    // bucket is longest first
+    struct RegionLists {
+      std::vector<uint32_t> home, left, starts;  // starts: view-local home positions
+    };
+    std::vector<RegionLists> lists((size_t)V);
+    auto build_view = [&](int c) {
+      const View& v = m->views[c];
+      RegionLists& out = lists[(size_t)c];
+      const int64_t hw = (int64_t)v.cam.rows * v.cam.cols;
+      const RayMeta* vm = hm.data() + v.pix_base;
+      std::vector<uint32_t> lcount(65536, 0u), reg((size_t)hw, 0u), bucket_off((size_t)R + 1, 0u);
+      int64_t work = 0;
+      for (int64_t i = 0; i < hw; ++i) {
+        work += vm[i].n_pre;
+        if (vm[i].n_pre) ++lcount[65535 - vm[i].n_pre];
+      }
+      // region of each active pixel: equal shares of the view's work
+      int64_t acc = 0;
+      for (int64_t i = 0; i < hw; ++i) {
+        if (!vm[i].n_pre) continue;
+        const uint32_t r = (uint32_t)std::min<int64_t>(R - 1, acc * R / std::max<int64_t>(work, 1));
+        reg[(size_t)i] = r;
+        ++bucket_off[r + 1];
+        acc += vm[i].n_pre;
+      }
+      for (int r = 0; r < R; ++r) bucket_off[r + 1] += bucket_off[r];
+      // the view's active rays longest first (pixel order within a length)
+      uint32_t pos = 0;
+      for (int k = 0; k < 65536; ++k) {
+        const uint32_t c0 = lcount[k];
+        lcount[k] = pos;
+        pos += c0;
+      }
+      std::vector<uint32_t> lsorted(pos), buckets(pos), fill(bucket_off.begin(), bucket_off.end() - 1);
+      for (int64_t i = 0; i < hw; ++i)
+        if (vm[i].n_pre) lsorted[lcount[65535 - vm[i].n_pre]++] = (uint32_t)i;
+      for (uint32_t i : lsorted) buckets[fill[reg[i]]++] = i;
+      // home = each region's longest rays up to kHomeShare of its work
+      std::vector<uint8_t> is_home((size_t)hw, 0);
+      out.home.reserve(pos);
+      for (int r = 0; r < R; ++r) {
+        int64_t rw = 0, hwk = 0;
+        for (uint32_t k = bucket_off[r]; k < bucket_off[r + 1]; ++k) rw += vm[buckets[k]].n_pre;
+        out.starts.push_back((uint32_t)out.home.size());
+        for (uint32_t k = bucket_off[r]; k < bucket_off[r + 1] && hwk * 100 < rw * kHomeShare; ++k) {
+          const uint32_t i = buckets[k];
+          is_home[i] = 1;
+          hwk += vm[i].n_pre;
+          out.home.push_back((uint32_t)(v.pix_base + i));
+        }
+      }
+      // leftovers longest first
+      for (uint32_t i : lsorted)
+        if (!is_home[i]) out.left.push_back((uint32_t)(v.pix_base + i));
+    };
+    {
+      std::vector<std::thread> pool;
+      std::vector<char> failed((size_t)V, 0);
+      for (int c = 0; c < V; ++c)
+        pool.emplace_back([&, c] {
+          try {
+            build_view(c);
+          } catch (...) {
+            failed[(size_t)c] = 1;
+          }
+        });
+      for (auto& t : pool) t.join();
+      for (char f : failed)
+        if (f) fail(MRF_ERR_OOM, "host memory for the region queues");
+    }
+    std::vector<uint32_t> rq_long, rq_left, rst;
+    rq_long.reserve((size_t)base);
+    rq_left.reserve((size_t)base);
+    rst.reserve((size_t)V * R + 1);
+    for (int c = 0; c < V; ++c) {
+      View& v = m->views[c];
+      const RegionLists& l = lists[(size_t)c];
+      for (uint32_t st : l.starts) rst.push_back((uint32_t)rq_long.size() + st);
+      rq_long.insert(rq_long.end(), l.home.begin(), l.home.end());
+      v.left_base = (uint32_t)rq_left.size();
+      v.n_left = (uint32_t)l.left.size();
+      rq_left.insert(rq_left.end(), l.left.begin(), l.left.end());
+    }
+    rst.push_back((uint32_t)rq_long.size());
+    m->rstart.reserve(rst.size() * 4, false, m->stream);
+    m->rcounters.reserve(((size_t)2 * V * R + 2 * (size_t)V + 2) * 4, false, m->stream);
+    m->nreg = (uint32_t)R;
+    m->n_left_all = (uint32_t)rq_left.size();
+    CK(cudaMemcpyAsync(m->rstart.p, rst.data(), rst.size() * 4, cudaMemcpyHostToDevice, m->stream));
+    // home rays and leftovers in one array: one upload of the pixel
+    // indices (into ray_order, free again once the longest-first queues are
+    // gathered) and one gather of their records
+    m->region_home_n = (uint32_t)rq_long.size();
+    rq_long.insert(rq_long.end(), rq_left.begin(), rq_left.end());
+    m->region_q.reserve(std::max<size_t>(rq_long.size(), 1) * sizeof(RayMeta), false, m->stream);
+    if (!rq_long.empty()) {
+      CK(cudaMemcpyAsync(m->ray_order.p, rq_long.data(), rq_long.size() * 4, cudaMemcpyHostToDevice,
+                         m->stream));
+      CK(launch_ray_queue(m->meta.as<RayMeta>(), m->ray_order.as<uint32_t>(), (uint32_t)rq_long.size(),
+                          m->region_q.as<RayMeta>(), m->stream));
+      sync(m);  // the host vector goes out of scope
+    }
   }
   m->n_inc = n_inc;
   m->n_pairs = pair_total;
@@ -679,17 +799,49 @@ struct Profiler {
 // pairs without dynamic incidences get their (constant) update in the first
 // iteration of each mrf_infer call only: afterwards it would leave every
 // value unchanged (L + (m_new - m_new) = L).
-// rays of all views (the views' queues are contiguous)
-uint32_t all_rays(const mrf_map* m) {
-  uint32_t nact = 0;
-  for (const View& v : m->views) nact += v.n_active;
-  return nact;
+// the rays of view c, and of all views (c = -1; the views' queues and
+// regions are contiguous), with their counters
+RayWork ray_work(mrf_map* m, int c) {
+  const int V = (int)m->views.size();
+  const uint32_t R = m->nreg;
+  RayWork w{};
+  w.region = m->region_q.as<RayMeta>();
+  uint32_t* lc = m->rcounters.as<uint32_t>() + (size_t)2 * V * R;  // leftover counters
+  if (c >= 0) {
+    const View& v = m->views[c];
+    w.queue = m->ray_queue.as<RayMeta>() + v.order_base;
+    w.n_rays = v.n_active;
+    w.counter = m->counters.as<uint32_t>() + c;
+    w.rstart = m->rstart.as<uint32_t>() + (size_t)c * R;
+    w.nreg = R;
+    w.rcounter = m->rcounters.as<uint32_t>() + (size_t)c * R;
+    w.left = m->region_q.as<RayMeta>() + m->region_home_n + v.left_base;
+    w.n_left = v.n_left;
+    w.lcounter = lc + c;
+  } else {
+    w.queue = m->ray_queue.as<RayMeta>();
+    for (const View& v : m->views) w.n_rays += v.n_active;
+    w.counter = m->counters.as<uint32_t>() + V;
+    w.rstart = m->rstart.as<uint32_t>();
+    w.nreg = (uint32_t)V * R;
+    w.rcounter = m->rcounters.as<uint32_t>() + (size_t)V * R;
+    w.left = m->region_q.as<RayMeta>() + m->region_home_n;
+    w.n_left = m->n_left_all;
+    w.lcounter = lc + V;
+  }
+  return w;
+}
+
+void zero_counters(mrf_map* m) {
+  const size_t V = m->views.size();
+  CK(cudaMemsetAsync(m->counters.p, 0, (V + 1) * 4, m->stream));
+  CK(cudaMemsetAsync(m->rcounters.p, 0, (2 * V * m->nreg + V + 1) * 4, m->stream));
 }
 
 void enqueue_iteration(mrf_map* m, const BpArrays& a, bool jacobi, int fix, bool first,
                        Profiler& prof, int64_t& launches) {
   const int V = (int)m->views.size();
-  CK(cudaMemsetAsync(m->counters.p, 0, (size_t)(V + 1) * 4, m->stream));
+  zero_counters(m);
   if (!jacobi) {
     for (int c = 0; c < V; ++c) {
       const View& v = m->views[c];
@@ -698,8 +850,7 @@ void enqueue_iteration(mrf_map* m, const BpArrays& a, bool jacobi, int fix, bool
       CK(launch_pair_prepare(a, v.pair_base, v.pair_base + v.n_pairs, 0, m->stream));
       prof.end();
       prof.begin(1);
-      CK(launch_ray_bp(a, m->ray_queue.as<RayMeta>() + v.order_base, v.n_active,
-                       m->counters.as<uint32_t>() + c, fix, m->num_sms, m->ray_variant, m->stream));
+      CK(launch_ray_bp(a, ray_work(m, c), fix, m->num_sms, m->ray_variant, m->stream));
       prof.end();
       prof.begin(2);
       if (v.n_dperm) {
@@ -722,8 +873,7 @@ void enqueue_iteration(mrf_map* m, const BpArrays& a, bool jacobi, int fix, bool
     prof.end();
     prof.begin(1);
     // the queues of all views are contiguous: one launch over all rays
-    CK(launch_ray_bp(a, m->ray_queue.as<RayMeta>(), all_rays(m), m->counters.as<uint32_t>() + V, fix,
-                     m->num_sms, m->ray_variant, m->stream));
+    CK(launch_ray_bp(a, ray_work(m, -1), fix, m->num_sms, m->ray_variant, m->stream));
     prof.end();
     prof.begin(2);
     CK(launch_pair_update(a, 0, (uint32_t)m->n_dperm, 0, (uint32_t)m->n_dpairs,
@@ -917,7 +1067,7 @@ void destroy_bufs(mrf_map* m) {
                  &m->pair_m, &m->pair_cum, &m->pair_stat, &m->pair_ndyn, &m->pair_hit, &m->pair_q,
                  &m->pair_dm,
                  &m->pair_seg, &m->dperm, &m->dpair, &m->dseg, &m->drun,
-                 &m->carry, &m->ray_order, &m->ray_queue, &m->counters, &m->tile_first,
+                 &m->carry, &m->ray_order, &m->ray_queue, &m->region_q, &m->rstart, &m->rcounters, &m->counters, &m->tile_first,
                  &m->vseg, &m->vpairs, &m->vvox, &m->s_rec, &m->s_recs, &m->s_pf, &m->s_ps,
                  &m->s_flags, &m->s_ind, &m->s_scan,
                  &m->s_q0, &m->s_q1, &m->s_q2, &m->s_q3, &m->s_bf,
@@ -1210,10 +1360,9 @@ static void warm_start_impl(mrf_map* m, const float* L_pred, bool device_ptr, in
   const int V = (int)m->views.size();
   const uint32_t P = (uint32_t)m->n_pairs;
   for (int k = 0; k < sweeps; ++k) {
-    CK(cudaMemsetAsync(m->counters.p, 0, (size_t)(V + 1) * 4, m->stream));
+    zero_counters(m);
     CK(launch_pair_prepare(a, 0, P, 1, m->stream));
-    CK(launch_ray_bp(a, m->ray_queue.as<RayMeta>(), all_rays(m), m->counters.as<uint32_t>() + V, 0,
-                     m->num_sms, m->ray_variant, m->stream));
+    CK(launch_ray_bp(a, ray_work(m, -1), 0, m->num_sms, m->ray_variant, m->stream));
     CK(launch_pair_update(a, 0, (uint32_t)m->n_dperm, 0, (uint32_t)m->n_dpairs,
                           m->tile_first.as<uint32_t>() + m->jac_tile_base, m->carry.as<TileCarry>(),
                           1, m->stream));

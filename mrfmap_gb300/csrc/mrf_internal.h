@@ -179,10 +179,26 @@ cudaError_t launch_pair_prepare(const BpArrays& a, uint32_t p0, uint32_t p1, int
 int ray_bp_variants();
 // resident blocks per SM of a variant of the persistent ray kernel (queried once)
 int ray_bp_resident_blocks(int variant);
-// rays queue[0..n_rays) (RayMeta records, longest first); counter: one
-// zeroed u32 per launch
-cudaError_t launch_ray_bp(const BpArrays& a, const RayMeta* queue, uint32_t n_rays, uint32_t* counter,
-                          int fix_reset, int num_sms, int variant, cudaStream_t s);
+// the rays of one ray-kernel launch in its schedules: queue[0..n_rays)
+// longest first with one zeroed counter; the same rays as nreg regions of
+// consecutive pixels, region r's home rays (longest first) at positions
+// rstart[r] .. rstart[r + 1] of region (nreg zeroed counters) and the
+// regions' remaining short rays in left[0..n_left) (longest first; one
+// zeroed counter)
+struct RayWork {
+  const RayMeta* queue;
+  uint32_t n_rays;
+  uint32_t* counter;
+  const RayMeta* region;
+  const uint32_t* rstart;
+  uint32_t nreg;
+  uint32_t* rcounter;
+  const RayMeta* left;
+  uint32_t n_left;
+  uint32_t* lcounter;
+};
+cudaError_t launch_ray_bp(const BpArrays& a, const RayWork& w, int fix_reset, int num_sms, int variant,
+                          cudaStream_t s);
 cudaError_t launch_ray_keys(const RayMeta* meta, uint32_t n, uint32_t* keys, uint32_t* vals,
                             cudaStream_t s);
 // queue[i] = meta[order[i]], i < n
