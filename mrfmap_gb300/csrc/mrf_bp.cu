@@ -437,14 +437,13 @@ __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, const uint32_t* _
 // build, their RayMeta records copied into queue order), so the long rays
 // start early and the short ones fill the tail.  kReg true (SM-affine):
 // the view's pixels are cut into regions of consecutive pixels holding
-// equal shares of its incidences, one region per SM-resident group of
-// blocks (block b serves regions b mod G, + G, ..., G = min(grid, regions);
-// the persistent grid is dispatched round-robin over the SMs, so the
-// blocks of one region share an SM); a warp takes the home rays of its
-// regions, then drains the view's leftover queue of short rays.  The warps
-// of one SM trace neighbouring rays at the same time -- rays that cross the
-// same voxels, so their ln q gathers hit the SM's L1.  Which warp handles a ray does not
-// change its result.  Variants differ only in register budget (kMinBlocks
+// equal shares of its incidences, one region per SM (block b serves
+// regions b mod G, + G, ..., G = min(grid, regions); a persistent grid is
+// placed on the SMs in block order, so a region's blocks share an SM); a
+// warp takes the home rays of its regions, then drains the view's leftover
+// queue of short rays.  The warps of one SM trace neighbouring rays at the
+// same time -- rays that cross the same voxels, so their ln q gathers hit
+// the SM's L1.  Which warp handles a ray does not change its result.  Variants differ only in register budget (kMinBlocks
 // resident blocks per SM), load policy and schedule: their arithmetic is
 // identical, so the autotuner's choice never changes a result.
 template <int kMinBlocks, int kPol, int kPf, bool kReg>
