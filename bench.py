@@ -207,7 +207,7 @@ def run_reference(args):
 
 
 # bumped whenever k_ray_bp's memory traffic changes (profiles/ray_bp_traffic.json)
-RAY_KERNEL_VERSION = 3
+RAY_KERNEL_VERSION = 4
 
 
 def ray_kernel_bytes(st, iters):
