@@ -407,36 +407,52 @@ __global__ void k_gather_rec(const uint32_t* __restrict__ sidx, uint32_t n, uint
 // Per pair: cumulative length, the sum of its static messages F_EPS * l
 // (each product rounded as the ray kernel rounds it), the number of dynamic
 // incidences and the potential mass sum mu * l (a warm-start feature).  The
-// sums are FP64 and rounded once, so their value does not depend on the
-// summation order (the reference adds with float atomics in no fixed order).
-// A thread sums a pair's contiguous run of sorted records; runs longer than
-// kLongRun (voxels next to a camera, crossed by up to ~10^5 rays) are
-// appended to a list and summed by a whole block each.
+// sums are carried as unevaluated FP32 pairs (s, e) updated by an
+// error-free two-sum (Knuth's TwoSum: e collects every rounding error of
+// s), i.e. to about twice FP32's precision, and rounded once through FP64
+// at the end, so their value does not depend on the summation order (the
+// reference adds with float atomics in no fixed order).  GB300 issues FP64
+// at 1/64 of the FP32 rate: plain FP64 accumulation made this kernel
+// FP64-bound.  A thread sums a pair's contiguous run of sorted records;
+// runs longer than kLongRun (voxels next to a camera, crossed by up to
+// ~10^5 rays) are appended to a list and summed by a whole block each.
 constexpr uint32_t kLongRun = 512;
 constexpr int kStatThreads = 256;
 
+struct F2 {
+  float s, e;
+  __device__ __forceinline__ void add(float x) {
+    const float t = __fadd_rn(s, x);
+    const float bp = __fsub_rn(t, s);
+    const float err = __fadd_rn(__fsub_rn(s, __fsub_rn(t, bp)), __fsub_rn(x, bp));
+    e = __fadd_rn(e, err);
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return (double)s + (double)e; }
+};
+
 struct PairSums {
-  double c, st, h;
+  F2 c, st, h;
   uint32_t nd;
 };
 
 __device__ __forceinline__ void add_rec(PairSums& a, const float2 r) {
-  a.c += (double)r.x;
+  a.c.add(r.x);
   if (signbit(r.y)) {
-    a.h -= (double)r.y;
+    a.h.add(-r.y);
     ++a.nd;
   } else {
-    a.st += (double)__fmul_rn(kFEps, r.x);
+    a.st.add(__fmul_rn(kFEps, r.x));
   }
 }
 
-__device__ __forceinline__ void store_sums(uint32_t p, const PairSums& a, float* __restrict__ cum,
-                                           float* __restrict__ stat, uint32_t* __restrict__ ndyn,
-                                           float* __restrict__ hit) {
-  cum[p] = (float)a.c;
-  stat[p] = (float)a.st;
-  ndyn[p] = a.nd;
-  hit[p] = (float)a.h;
+__device__ __forceinline__ void store_sums(uint32_t p, double c, double st, double h, uint32_t nd,
+                                           float* __restrict__ cum, float* __restrict__ stat,
+                                           uint32_t* __restrict__ ndyn, float* __restrict__ hit) {
+  cum[p] = (float)c;
+  stat[p] = (float)st;
+  ndyn[p] = nd;
+  hit[p] = (float)h;
 }
 
 __global__ void k_pair_stats(const uint32_t* __restrict__ seg, uint32_t p0, uint32_t np, uint32_t perm_base,
@@ -451,9 +467,9 @@ __global__ void k_pair_stats(const uint32_t* __restrict__ seg, uint32_t p0, uint
     long_list[1 + atomicAdd(long_list, 1u)] = p;
     return;
   }
-  PairSums a{0.0, 0.0, 0.0, 0u};
+  PairSums a{{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, 0u};
   for (uint32_t k = k0; k < k1; ++k) add_rec(a, srec[k]);
-  store_sums(p, a, cum, stat, ndyn, hit);
+  store_sums(p, a.c.value(), a.st.value(), a.h.value(), a.nd, cum, stat, ndyn, hit);
 }
 
 // one block per listed long run; block sums in a fixed tree order
@@ -467,11 +483,11 @@ __global__ void __launch_bounds__(kStatThreads)
   for (uint32_t j = blockIdx.x; j < n; j += gridDim.x) {
     const uint32_t p = long_list[1 + j];
     const uint32_t k0 = seg[p] - perm_base, k1 = seg[p + 1] - perm_base;
-    PairSums a{0.0, 0.0, 0.0, 0u};
+    PairSums a{{0.0f, 0.0f}, {0.0f, 0.0f}, {0.0f, 0.0f}, 0u};
     for (uint32_t k = k0 + threadIdx.x; k < k1; k += kStatThreads) add_rec(a, srec[k]);
-    sc[threadIdx.x] = a.c;
-    sst[threadIdx.x] = a.st;
-    sh[threadIdx.x] = a.h;
+    sc[threadIdx.x] = a.c.value();
+    sst[threadIdx.x] = a.st.value();
+    sh[threadIdx.x] = a.h.value();
     snd[threadIdx.x] = a.nd;
     __syncthreads();
     for (int o = kStatThreads / 2; o > 0; o >>= 1) {
@@ -483,7 +499,7 @@ __global__ void __launch_bounds__(kStatThreads)
       }
       __syncthreads();
     }
-    if (threadIdx.x == 0) store_sums(p, PairSums{sc[0], sst[0], sh[0], snd[0]}, cum, stat, ndyn, hit);
+    if (threadIdx.x == 0) store_sums(p, sc[0], sst[0], sh[0], snd[0], cum, stat, ndyn, hit);
     __syncthreads();
   }
 }
