@@ -262,6 +262,41 @@ def test_ray_variants_identical_and_autotune(native_lib, w):
         m.set_ray_variant(99)
 
 
+def test_ray_variants_identical_jacobi(native_lib, w):
+    """The Jacobi schedule runs one ray launch over all views' queues (the
+    SM-region schedule then has regions of every view and one leftover
+    queue for all): every variant still computes the same bits."""
+    out = []
+    for k in range(L.load().mrf_ray_variants()):
+        m = L.MRFMap(w.params, activation=L.ACT_FULL_RAY)
+        for P, D in zip(w.poses, w.depths):
+            m.add_view(P, D)
+        m.set_ray_variant(k)
+        m.infer(iters=3, flags=L.JACOBI)
+        out.append(m.beliefs())
+        m.close()
+    for b in out[1:]:
+        np.testing.assert_array_equal(b, out[0])
+
+
+def test_release_cached_memory(native_lib, w):
+    """Device memory of destroyed maps stays pooled for the next map;
+    mrf_release_cached_memory hands it back, and later maps still work."""
+    m = L.MRFMap(w.params)
+    for P, D in zip(w.poses, w.depths):
+        m.add_view(P, D)
+    m.infer(iters=2)
+    b = m.beliefs()
+    m.close()
+    assert L.load().mrf_release_cached_memory() == 0
+    m = L.MRFMap(w.params)
+    for P, D in zip(w.poses, w.depths):
+        m.add_view(P, D)
+    m.infer(iters=2)
+    np.testing.assert_array_equal(m.beliefs(), b)
+    m.close()
+
+
 def test_message_checkpoint_resume(native_lib, w):
     """The BP state is the per-camera messages: written back into a fresh map
     (and the total log-odds rebuilt from them) the run resumes where it
