@@ -365,11 +365,34 @@ __global__ void k_brick_first(const uint32_t* __restrict__ pair_vox, const uint3
   if (ok && (threadIdx.x & 31) == (unsigned)(__ffs(same) - 1)) atomicMin(bfirst + b, m);
 }
 
+// second sort key: pairs on quiet voxels last (bit `bits` set), then the
+// brick's first visit
 __global__ void k_brick_keys(const uint32_t* __restrict__ order, uint32_t np,
                              const uint32_t* __restrict__ pair_vox, const uint32_t* __restrict__ bfirst,
-                             uint32_t* __restrict__ key) {
+                             const uint8_t* __restrict__ loud, int bits, uint32_t* __restrict__ key) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < np) key[i] = bfirst[pair_vox[order[i]] / kBrickVox];
+  if (i >= np) return;
+  const uint32_t v = pair_vox[order[i]];
+  key[i] = bfirst[v / kBrickVox] | (loud[v] ? 0u : (1u << bits));
+}
+
+// loud[v] = 1 for every voxel with a dynamic incidence (any view): one
+// thread per ray walks its dynamic range [k_dyn, n_post)
+__global__ void k_loud_voxels(const RayMeta* __restrict__ meta, int64_t npix, const uint32_t* __restrict__ vox,
+                              uint8_t* __restrict__ loud) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= npix) return;
+  const RayMeta me = meta[r];
+  for (int i = ray_kdyn(me); i < me.n_post; ++i) loud[vox[me.off + i]] = 1;
+}
+
+// *count += number of pairs on loud voxels
+__global__ void k_count_loud(const uint32_t* __restrict__ pair_vox, uint32_t np,
+                             const uint8_t* __restrict__ loud, uint32_t* __restrict__ count) {
+  uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool l = p < np && loud[pair_vox[p]];
+  const unsigned b = __ballot_sync(0xFFFFFFFFu, l);
+  if ((threadIdx.x & 31) == 0 && b) atomicAdd(count, (uint32_t)__popc(b));
 }
 
 // run lengths in the new order and the old -> new map
@@ -633,9 +656,24 @@ cudaError_t launch_brick_first(const uint32_t* pair_vox, const uint32_t* key, ui
 }
 
 cudaError_t launch_brick_keys(const uint32_t* order, uint32_t np, const uint32_t* pair_vox,
-                              const uint32_t* bfirst, uint32_t* key, cudaStream_t s) {
+                              const uint32_t* bfirst, const uint8_t* loud, int bits, uint32_t* key,
+                              cudaStream_t s) {
   if (!np) return cudaSuccess;
-  k_brick_keys<<<grid_for(np), kThreads, 0, s>>>(order, np, pair_vox, bfirst, key);
+  k_brick_keys<<<grid_for(np), kThreads, 0, s>>>(order, np, pair_vox, bfirst, loud, bits, key);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_loud_voxels(const RayMeta* meta, int64_t npix, const uint32_t* vox, uint8_t* loud,
+                               cudaStream_t s) {
+  if (npix <= 0) return cudaSuccess;
+  k_loud_voxels<<<grid_for(npix), kThreads, 0, s>>>(meta, npix, vox, loud);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_count_loud(const uint32_t* pair_vox, uint32_t np, const uint8_t* loud, uint32_t* count,
+                              cudaStream_t s) {
+  if (!np) return cudaSuccess;
+  k_count_loud<<<grid_for(np), kThreads, 0, s>>>(pair_vox, np, loud, count);
   return cudaGetLastError();
 }
 

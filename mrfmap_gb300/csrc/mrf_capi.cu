@@ -121,6 +121,7 @@ struct View {
   uint32_t dpair_base = 0, n_dpairs = 0;  // runs of dynamic incidences (one per pair)
   uint32_t order_base = 0, n_active = 0;  // ray queue (longest first)
   uint32_t left_base = 0, n_left = 0;     // leftover queue of the SM-affine schedule
+  uint32_t n_loud = 0;                    // pairs on voxels with a dynamic incidence (numbered first)
   uint32_t tile_base = 0;                 // first pair of each pair-update tile
 };
 
@@ -151,7 +152,7 @@ struct mrf_map {
   std::vector<View> views;
   // arenas
   DBuf meta, inc_pair, inc_len, inc_mu, inc_pl, pair_vox, pair_m, pair_cum, pair_stat, pair_ndyn, pair_hit,
-      pair_q, pair_dm, pair_seg, dperm, s_q0, s_q1, s_q2, s_q3, s_bf, dpair, dseg, drun, carry, ray_order, ray_queue, region_q, rstart, rcounters, counters,
+      pair_q, pair_dm, pair_seg, dperm, s_q0, s_q1, s_q2, s_q3, s_bf, s_loud, dpair, dseg, drun, carry, ray_order, ray_queue, region_q, rstart, rcounters, counters,
       tile_first;
   uint32_t jac_tile_base = 0;
   int64_t n_inc = 0, n_pairs = 0, n_dperm = 0, n_dpairs = 0;
@@ -172,7 +173,7 @@ struct mrf_map {
     cudaGraphExec_t exec = nullptr;
     int version = -1;
     int64_t launches = 0;
-  } graphs[8];
+  } graphs[12];
 
   BpArrays bp() const {
     BpArrays a;
@@ -352,6 +353,12 @@ void rebuild(mrf_map* m) {
     }
     for (int c = 0; c < V; ++c) npre += nreal[c];
   }
+  // voxels with a dynamic incidence in any view ("loud"; the others are
+  // quiet, see enqueue_iteration)
+  m->s_loud.reserve((size_t)std::max<int64_t>(m->n_bricks * kBrickVox, 1), false, m->stream);
+  CK(cudaMemsetAsync(m->s_loud.p, 0, (size_t)std::max<int64_t>(m->n_bricks * kBrickVox, 1), m->stream));
+  CK(launch_loud_voxels(m->meta.as<RayMeta>(), npix, m->s_vox.as<uint32_t>(), m->s_loud.as<uint8_t>(),
+                        m->stream));
   // 4. pairs per view: sort the view's incidences by voxel (stable), one
   //    pair per run, then renumber the pairs brick-major by first visit
   //    (mrf_build.cu, k_pair_first) and regroup the incidences in the new
@@ -414,15 +421,17 @@ void rebuild(mrf_map* m) {
       CK(launch_pair_first(sg, np0, 0, m->s_v1.as<uint32_t>(), q0, m->stream));
       CK(launch_fill_u32(m->s_bf.as<uint32_t>(), m->n_bricks, 0xFFFFFFFFu, m->stream));
       CK(launch_brick_first(pv, q0, np0, m->s_bf.as<uint32_t>(), m->stream));
-      // order: by own first visit, then (stable) by the brick's first visit
+      // order: by own first visit, then (stable) by (quiet voxel, the
+      // brick's first visit)
       int ibits = 1;
-      while (ibits < 32 && ((uint64_t)1 << ibits) < (uint64_t)n) ++ibits;
-      size_t t4 = sort_temp_bytes(np0, ibits);
+      while (ibits < 31 && ((uint64_t)1 << ibits) < (uint64_t)n) ++ibits;
+      size_t t4 = std::max(sort_temp_bytes(np0, ibits), sort_temp_bytes(np0, ibits + 1));
       m->s_tmp.reserve(std::max(t4, t1), false, m->stream);
       CK(launch_iota(q2, np0, m->stream));
       CK(sort_pairs_u32(m->s_tmp.p, t4, q0, q1, q2, q3, np0, ibits, m->stream));  // q3: by own visit
-      CK(launch_brick_keys(q3, np0, pv, m->s_bf.as<uint32_t>(), q0, m->stream));
-      CK(sort_pairs_u32(m->s_tmp.p, t4, q0, q1, q3, q2, np0, ibits, m->stream));  // q2: new order
+      CK(launch_brick_keys(q3, np0, pv, m->s_bf.as<uint32_t>(), m->s_loud.as<uint8_t>(), ibits, q0,
+                           m->stream));
+      CK(sort_pairs_u32(m->s_tmp.p, t4, q0, q1, q3, q2, np0, ibits + 1, m->stream));  // q2: new order
       // new runs: lengths in the new order, their starts, the old -> new map
       CK(launch_new_lengths(q2, np0, sg, q0, q3, m->stream));
       CK(cudaMemsetAsync(q0 + np0, 0, 4, m->stream));
@@ -456,6 +465,10 @@ void rebuild(mrf_map* m) {
                                 m->pair_vox.as<uint32_t>(), m->pair_seg.as<uint32_t>(),
                                 m->inc_pair.as<uint32_t>(), m->stream));
     CK(launch_fill_u32(m->pair_seg.as<uint32_t>() + v.pair_base + np, 1, v.perm_base + nr, m->stream));
+    CK(cudaMemsetAsync(m->s_k1.p, 0, 4, m->stream));
+    CK(launch_count_loud(m->pair_vox.as<uint32_t>() + v.pair_base, np, m->s_loud.as<uint8_t>(),
+                         m->s_k1.as<uint32_t>(), m->stream));
+    v.n_loud = read1(m, m->s_k1.as<uint32_t>());
     m->s_recs.reserve((size_t)nr * 8, false, m->stream);
     CK(launch_gather_rec(m->s_v1.as<uint32_t>(), nr, v.inc_base, m->s_rec.as<float2>(),
                          m->s_recs.as<float2>(), m->stream));
@@ -838,16 +851,25 @@ void zero_counters(mrf_map* m) {
   CK(cudaMemsetAsync(m->rcounters.p, 0, (2 * V * m->nreg + V + 1) * 4, m->stream));
 }
 
-void enqueue_iteration(mrf_map* m, const BpArrays& a, bool jacobi, int fix, bool first,
+// phase 0: the first iteration of a call (static-pair updates); phase 1:
+// the second; phase 2: later ones.  From phase 2 on the ln q of a pair
+// whose voxel has no dynamic incidence in any view (a quiet voxel, whose
+// pairs are numbered after the others) cannot change: its total log-odds
+// moves only through static-pair updates, which happen in the first
+// iteration, and the second iteration's prepare has seen them all.  Those
+// pairs' ln q is then left as it is.
+void enqueue_iteration(mrf_map* m, const BpArrays& a, bool jacobi, int fix, int phase,
                        Profiler& prof, int64_t& launches) {
   const int V = (int)m->views.size();
+  const bool first = phase == 0;
   zero_counters(m);
   if (!jacobi) {
     for (int c = 0; c < V; ++c) {
       const View& v = m->views[c];
       if (v.n_inc == 0) continue;
       prof.begin(0);
-      CK(launch_pair_prepare(a, v.pair_base, v.pair_base + v.n_pairs, 0, m->stream));
+      CK(launch_pair_prepare(a, v.pair_base, v.pair_base + (phase >= 2 ? v.n_loud : v.n_pairs), 0,
+                             m->stream));
       prof.end();
       prof.begin(1);
       CK(launch_ray_bp(a, ray_work(m, c), fix, m->num_sms, m->ray_variant, m->stream));
@@ -892,9 +914,9 @@ void enqueue_iteration(mrf_map* m, const BpArrays& a, bool jacobi, int fix, bool
 
 // The iteration is captured once per incidence build and schedule into a
 // CUDA graph and replayed iters times.
-cudaGraphExec_t iteration_graph(mrf_map* m, const BpArrays& a, bool jacobi, int fix, bool first,
+cudaGraphExec_t iteration_graph(mrf_map* m, const BpArrays& a, bool jacobi, int fix, int phase,
                                 int64_t& launches_per_iter) {
-  int key = (jacobi ? 1 : 0) | (fix ? 2 : 0) | (first ? 4 : 0);
+  int key = (jacobi ? 1 : 0) | (fix ? 2 : 0) | (phase << 2);
   auto& slot = m->graphs[key];
   if (slot.exec && slot.version == m->built_version) {
     launches_per_iter = slot.launches;
@@ -909,7 +931,7 @@ cudaGraphExec_t iteration_graph(mrf_map* m, const BpArrays& a, bool jacobi, int 
   cudaGraph_t graph = nullptr;
   CK(cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal));
   try {
-    enqueue_iteration(m, a, jacobi, fix, first, off, launches);
+    enqueue_iteration(m, a, jacobi, fix, phase, off, launches);
   } catch (...) {
     cudaStreamEndCapture(m->stream, &graph);
     if (graph) cudaGraphDestroy(graph);
@@ -963,22 +985,21 @@ void run_infer(mrf_map* m, const int* ids, int n_ids, int iters, int flags, floa
   int done = 0;
   if (m->n_inc > 0) {
     const bool direct = prof.on || (flags & MRF_NO_GRAPH);
-    int64_t per0 = 0, per = 0;
-    cudaGraphExec_t exec0 = nullptr, exec = nullptr;
-    if (!direct) {
-      exec0 = iteration_graph(m, a, jacobi, fix, true, per0);
-      if (iters > 1) exec = iteration_graph(m, a, jacobi, fix, false, per);
-    }
+    int64_t per[3] = {0, 0, 0};
+    cudaGraphExec_t exec[3] = {nullptr, nullptr, nullptr};
+    if (!direct)
+      for (int ph = 0; ph < 3 && ph < iters; ++ph) exec[ph] = iteration_graph(m, a, jacobi, fix, ph, per[ph]);
     for (int it = 0; it < iters; ++it) {
       const bool check = conv && ((it + 1) % check_every == 0 || it + 1 == iters);
       if (check)
         CK(cudaMemcpyAsync(m->s_prev.p, m->d_belief.p, (size_t)nvox * 4, cudaMemcpyDeviceToDevice,
                            m->stream));
+      const int ph = std::min(it, 2);
       if (direct) {
-        enqueue_iteration(m, a, jacobi, fix, it == 0, prof, launches);
+        enqueue_iteration(m, a, jacobi, fix, ph, prof, launches);
       } else {
-        CK(cudaGraphLaunch(it == 0 ? exec0 : exec, m->stream));
-        launches += it == 0 ? per0 : per;
+        CK(cudaGraphLaunch(exec[ph], m->stream));
+        launches += per[ph];
       }
       done = it + 1;
       if (check) {
@@ -1070,7 +1091,7 @@ void destroy_bufs(mrf_map* m) {
                  &m->carry, &m->ray_order, &m->ray_queue, &m->region_q, &m->rstart, &m->rcounters, &m->counters, &m->tile_first,
                  &m->vseg, &m->vpairs, &m->vvox, &m->s_rec, &m->s_recs, &m->s_pf, &m->s_ps,
                  &m->s_flags, &m->s_ind, &m->s_scan,
-                 &m->s_q0, &m->s_q1, &m->s_q2, &m->s_q3, &m->s_bf,
+                 &m->s_q0, &m->s_q1, &m->s_q2, &m->s_q3, &m->s_bf, &m->s_loud,
                  &m->s_tmp, &m->s_counts, &m->s_offs, &m->s_vox, &m->s_k0, &m->s_k1, &m->s_v0,
                  &m->s_v1, &m->s_seg, &m->s_dense, &m->s_err, &m->s_depth_in, &m->s_depth,
                  &m->s_img, &m->s_part, &m->s_sum, &m->s_prev, &m->s_delta, &m->s_snap};
@@ -1516,7 +1537,7 @@ mrf_status mrf_autotune(mrf_map* m, int reps, double* ms_out, int cap, int* chos
         m->ray_variant = k;
         for (int r = 0; r <= reps; ++r) {
           if (r == 1) CK(cudaEventRecord(m->ev0, m->stream));
-          enqueue_iteration(m, a, false, 0, false, off, launches);
+          enqueue_iteration(m, a, false, 0, 2, off, launches);
         }
         CK(cudaEventRecord(m->ev1, m->stream));
         sync(m);

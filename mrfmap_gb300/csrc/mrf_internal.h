@@ -91,7 +91,13 @@ cudaError_t launch_pair_first(const uint32_t* seg, uint32_t np, uint32_t perm_ba
 cudaError_t launch_brick_first(const uint32_t* pair_vox, const uint32_t* key, uint32_t np, uint32_t* bfirst,
                                cudaStream_t s);
 cudaError_t launch_brick_keys(const uint32_t* order, uint32_t np, const uint32_t* pair_vox,
-                              const uint32_t* bfirst, uint32_t* key, cudaStream_t s);
+                              const uint32_t* bfirst, const uint8_t* loud, int bits, uint32_t* key,
+                              cudaStream_t s);
+// voxels with a dynamic incidence in any view, and the pairs on them
+cudaError_t launch_loud_voxels(const RayMeta* meta, int64_t npix, const uint32_t* vox, uint8_t* loud,
+                               cudaStream_t s);
+cudaError_t launch_count_loud(const uint32_t* pair_vox, uint32_t np, const uint8_t* loud, uint32_t* count,
+                              cudaStream_t s);
 cudaError_t launch_new_lengths(const uint32_t* order, uint32_t np, const uint32_t* seg, uint32_t* len,
                                uint32_t* slot_of, cudaStream_t s);
 cudaError_t launch_move_positions(const uint32_t* sidx, const uint32_t* flag, const uint32_t* scan,
