@@ -52,6 +52,8 @@ def parse():
     ap.add_argument("--policy", default="fullray", choices=["fullray", "endpoint"])
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--ray-variant", type=int, default=None,
+                    help="use this ray-kernel variant instead of autotuning (profiling runs)")
     ap.add_argument("--cpu-sample-views", type=int, default=2)
     ap.add_argument("--warm-scenes", type=int, default=4,
                     help="held-out 10x320x240 2 cm scenes for the warm-start comparison (0: skip)")
@@ -207,15 +209,16 @@ def run_reference(args):
 
 
 # bumped whenever k_ray_bp's memory traffic changes (profiles/ray_bp_traffic.json)
-RAY_KERNEL_VERSION = 4
+RAY_KERNEL_VERSION = 5
 
 
 def ray_kernel_bytes(st, iters):
-    """Algorithmic bytes of the ray-message kernel for one launch-sum: per
-    Pre incidence 12 B (pair id 4, length 4, ln q gather 4); per dynamic
+    """Algorithmic bytes of the ray-message kernel for one launch-sum, over
+    the rays it runs over (those with a dynamic incidence): per Pre
+    incidence 12 B (pair id 4, length 4, ln q gather 4); per dynamic
     incidence (from the ray's first non-zero potential on) +8 B (potential
     4, message write 4); per ray 16 B of metadata."""
-    return (12 * st["n_inc_pre"] + 8 * st["n_inc_dyn"] + 16 * st["n_rays"]) * iters
+    return (12 * st["n_inc_pre_bp"] + 8 * st["n_inc_dyn"] + 16 * st["n_rays_bp"]) * iters
 
 
 def run_ours(args):
@@ -241,7 +244,11 @@ def run_ours(args):
     m.infer(iters=1)  # builds the incidence lists
     # ray-kernel variant chosen by the autotuner on this workload (before the
     # timed region; variants are numerically identical)
-    tuned, tune_ms = m.autotune(reps=2)
+    if args.ray_variant is None:
+        tuned, tune_ms = m.autotune(reps=2)
+    else:
+        m.set_ray_variant(args.ray_variant)
+        tuned, tune_ms = args.ray_variant, []
     st = m.stats()
     n_upd_step = st["n_inc_post"] * iters
     stream = torch.cuda.ExternalStream(m.stream())
@@ -292,7 +299,7 @@ def run_ours(args):
             if t.get("kernel_version") == RAY_KERNEL_VERSION and t.get("activation") == args.policy:
                 # DRAM bytes per Pre incidence from a capture of the same
                 # kernel on a smaller case, scaled by this launch's incidences
-                traffic = t["dram_bytes_per_pre_incidence"] * prof["n_inc_pre"] * iters / k_n
+                traffic = t["dram_bytes_per_pre_incidence"] * prof["n_inc_pre_bp"] * iters / k_n
         except Exception:
             pass
     kernel_share = {n: round(v / max(sum(prof["kernel_ms"]), 1e-9), 4)
@@ -426,7 +433,8 @@ def run_ours(args):
                        "ray_variant": tuned, "ray_variant_ms": [round(x, 4) for x in tune_ms],
                        "static_messages": "exact constants (p = F_EPS before a ray's first non-zero "
                                           "potential), summed once per build",
-                       "n_rays": st["n_rays"], "n_bricks": st["n_bricks"],
+                       "n_rays": st["n_rays"], "n_rays_bp": st["n_rays_bp"],
+                       "n_inc_pre_bp_per_iter": st["n_inc_pre_bp"], "n_bricks": st["n_bricks"],
                        "l2": "inputs larger than L2 (no flush)",
                        "parallelism": f"replicas{ws}" if ws > 1 else "single"},
             "gpu_launches": launches_step * args.steps,

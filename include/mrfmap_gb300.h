@@ -89,6 +89,9 @@ typedef struct mrf_stats {
   int64_t n_inc_dyn;       /* Post incidences from the first non-zero potential
                               on: the messages recomputed every iteration */
   int64_t n_pairs_dyn;     /* pairs holding at least one of them */
+  int64_t n_rays_bp;       /* rays the ray kernel runs over: those with a dynamic
+                              incidence (the others' messages are all static) */
+  int64_t n_inc_pre_bp;    /* their Pre incidences */
 } mrf_stats;
 
 /* Map construction: GVDBInference(...) + GVDBMRFMap::gpuAllocate

@@ -514,8 +514,8 @@ __global__ void k_ray_keys(const RayMeta* __restrict__ meta, uint32_t n, uint32_
                            uint32_t* __restrict__ vals) {
   uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= n) return;
-  uint32_t len = meta[r].n_pre;
-  keys[r] = len ? 0xFFFFu - len : 0x10000u;  // empty rays sort last
+  const RayMeta me = meta[r];
+  keys[r] = ray_in_bp(me) ? 0xFFFFu - me.n_pre : 0x10000u;  // rays left out sort last
   vals[r] = r;
 }
 

@@ -335,7 +335,7 @@ void rebuild(mrf_map* m) {
   // per-view counters from the ray records
   std::vector<RayMeta> hm((size_t)npix);
   std::vector<int64_t> nreal(V, 0);
-  int64_t nrays = 0, npost = 0, npre = 0, ndyn = 0;
+  int64_t nrays = 0, npost = 0, npre = 0, ndyn = 0, nrays_bp = 0, npre_bp = 0;
   if (npix) {
     CK(cudaMemcpyAsync(hm.data(), m->meta.p, (size_t)npix * sizeof(RayMeta), cudaMemcpyDeviceToHost,
                        m->stream));
@@ -349,6 +349,10 @@ void rebuild(mrf_map* m) {
         nrays += r.n_pre > 0;
         npost += r.n_post;
         ndyn += r.n_post - std::min<int>(ray_kdyn(r), r.n_post);
+        if (ray_in_bp(r)) {
+          ++nrays_bp;
+          npre_bp += r.n_pre;
+        }
       }
     }
     for (int c = 0; c < V; ++c) npre += nreal[c];
@@ -525,7 +529,7 @@ void rebuild(mrf_map* m) {
       View& v = m->views[c];
       const int64_t hw = (int64_t)v.cam.rows * v.cam.cols;
       int64_t act = 0;
-      for (int64_t i = 0; i < hw; ++i) act += hm[(size_t)(v.pix_base + i)].n_pre > 0;
+      for (int64_t i = 0; i < hw; ++i) act += ray_in_bp(hm[(size_t)(v.pix_base + i)]);
       v.order_base = (uint32_t)base;
       v.n_active = (uint32_t)act;
       CK(launch_ray_keys(m->meta.as<RayMeta>() + v.pix_base, (uint32_t)hw, m->s_k0.as<uint32_t>(),
@@ -566,13 +570,14 @@ void rebuild(mrf_map* m) {
       std::vector<uint32_t> lcount(65536, 0u), reg((size_t)hw, 0u), bucket_off((size_t)R + 1, 0u);
       int64_t work = 0;
       for (int64_t i = 0; i < hw; ++i) {
+        if (!ray_in_bp(vm[i])) continue;
         work += vm[i].n_pre;
-        if (vm[i].n_pre) ++lcount[65535 - vm[i].n_pre];
+        ++lcount[65535 - vm[i].n_pre];
       }
       // region of each active pixel: equal shares of the view's work
       int64_t acc = 0;
       for (int64_t i = 0; i < hw; ++i) {
-        if (!vm[i].n_pre) continue;
+        if (!ray_in_bp(vm[i])) continue;
         const uint32_t r = (uint32_t)std::min<int64_t>(R - 1, acc * R / std::max<int64_t>(work, 1));
         reg[(size_t)i] = r;
         ++bucket_off[r + 1];
@@ -588,7 +593,7 @@ void rebuild(mrf_map* m) {
       }
       std::vector<uint32_t> lsorted(pos), buckets(pos), fill(bucket_off.begin(), bucket_off.end() - 1);
       for (int64_t i = 0; i < hw; ++i)
-        if (vm[i].n_pre) lsorted[lcount[65535 - vm[i].n_pre]++] = (uint32_t)i;
+        if (ray_in_bp(vm[i])) lsorted[lcount[65535 - vm[i].n_pre]++] = (uint32_t)i;
       for (uint32_t i : lsorted) buckets[fill[reg[i]]++] = i;
       // home = each region's longest rays up to kHomeShare of its work
       std::vector<uint8_t> is_home((size_t)hw, 0);
@@ -731,6 +736,8 @@ void rebuild(mrf_map* m) {
   m->stats.n_pairs = pair_total;
   m->stats.n_inc_dyn = ndyn;
   m->stats.n_pairs_dyn = dpair_total;
+  m->stats.n_rays_bp = nrays_bp;
+  m->stats.n_inc_pre_bp = npre_bp;
 }
 
 void build_jacobi_csr(mrf_map* m) {

@@ -56,6 +56,12 @@ static_assert(sizeof(RayMeta) == 16, "RayMeta layout");
 // mu1 = 0), so the outgoing probability is exactly the clamp floor F_EPS and
 // the message is F_EPS * l: static for the life of the incidence lists.
 __host__ __device__ __forceinline__ int ray_kdyn(const RayMeta& m) { return (int)(m.flags >> 16); }
+// rays the ray kernel runs over: those with a dynamic incidence.  A ray
+// whose Post messages are all static produces nothing (its messages are
+// build constants, summed into the pairs), so it is left out of the queues.
+__host__ __device__ __forceinline__ bool ray_in_bp(const RayMeta& m) {
+  return m.n_pre > 0 && ray_kdyn(m) < m.n_post;
+}
 
 
 constexpr int kMaxRayLen = 65532;        // n_pre fits uint16 after padding to 4

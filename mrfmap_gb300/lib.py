@@ -71,7 +71,9 @@ class mrf_stats(C.Structure):
                                                                 ("kernel_ms", C.c_double * 4),
                                                                 ("kernel_count", C.c_int64 * 4),
                                                                 ("n_inc_dyn", C.c_int64),
-                                                                ("n_pairs_dyn", C.c_int64)]
+                                                                ("n_pairs_dyn", C.c_int64),
+                                                                ("n_rays_bp", C.c_int64),
+                                                                ("n_inc_pre_bp", C.c_int64)]
 
 
 _lib = None
