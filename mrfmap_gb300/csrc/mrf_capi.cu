@@ -10,15 +10,19 @@
 //                  ray order (pixel-major, then along the ray), each ray
 //                  padded to a multiple of 4
 //   pairs          u32 voxel, fp32 m, fp32 cum_len, fp32 ln q, fp32 dm,
-//                  u32 seg   [N_cv], voxel order per view
-//   grouped        u32 incidence and u32 pair id per pair-grouped position
-//                  [N_pre] (the voxel-sorted permutation, CSR by pair)
+//                  u32 seg   [N_cv]; per view the pairs on voxels with a
+//                  dynamic incidence first, each part brick-major by first
+//                  visit along the rays (mrf_build.cu, k_pair_first)
+//   grouped        u32 incidence per pair-grouped position [N_pre] (CSR
+//                  by pair; the dynamic positions again in dperm)
+//   ray queues     RayMeta records in queue order: longest first, and the
+//                  SM-affine regions (home rays per region, leftovers)
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cmath>
 #include <mutex>
 #include <thread>
-#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <string>
