@@ -405,19 +405,32 @@ __global__ void k_new_lengths(const uint32_t* __restrict__ order, uint32_t np, c
   slot_of[p] = q;
 }
 
-// every sorted position k moves to its pair's new run: out_idx / out_key
-// (incidence index, voxel) in the new pair-grouped order
+// every sorted position k moves to its pair's new run (out_idx: incidence
+// index in the new pair-grouped order), and its incidence gets the new
+// pair id
 __global__ void k_move_positions(const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ flag,
                                  const uint32_t* __restrict__ scan, const uint32_t* __restrict__ seg,
-                                 const uint32_t* __restrict__ pair_vox, const uint32_t* __restrict__ slot_of,
-                                 const uint32_t* __restrict__ start, uint32_t n, uint32_t perm_base,
-                                 uint32_t* __restrict__ out_idx, uint32_t* __restrict__ out_key) {
+                                 const uint32_t* __restrict__ slot_of, const uint32_t* __restrict__ start,
+                                 uint32_t n, uint32_t inc_base, uint32_t pair_base,
+                                 uint32_t* __restrict__ out_idx, uint32_t* __restrict__ inc_pair) {
   uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
   const uint32_t p = scan[k] + flag[k] - 1;
-  const uint32_t dst = start[slot_of[p]] + (k - (seg[p] - perm_base));
-  out_idx[dst] = sidx[k];
-  out_key[dst] = pair_vox[p];
+  const uint32_t q = slot_of[p];
+  const uint32_t i = sidx[k];
+  out_idx[start[q] + (k - seg[p])] = i;
+  inc_pair[inc_base + i] = pair_base + q;
+}
+
+// the renumbered pairs: voxel and first pair-grouped position of new pair q
+__global__ void k_pairs_renumbered(const uint32_t* __restrict__ order, uint32_t np,
+                                   const uint32_t* __restrict__ vox_old, const uint32_t* __restrict__ start,
+                                   uint32_t pair_base, uint32_t perm_base, uint32_t* __restrict__ pair_vox,
+                                   uint32_t* __restrict__ seg) {
+  uint32_t q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q > np) return;
+  if (q < np) pair_vox[pair_base + q] = vox_old[order[q]];
+  seg[pair_base + q] = perm_base + start[q];  // start[np] = the view's position count
 }
 
 // build records in pair-grouped (sorted) order: one gather per position
@@ -685,12 +698,20 @@ cudaError_t launch_new_lengths(const uint32_t* order, uint32_t np, const uint32_
 }
 
 cudaError_t launch_move_positions(const uint32_t* sidx, const uint32_t* flag, const uint32_t* scan,
-                                  const uint32_t* seg, const uint32_t* pair_vox, const uint32_t* slot_of,
-                                  const uint32_t* start, uint32_t n, uint32_t perm_base, uint32_t* out_idx,
-                                  uint32_t* out_key, cudaStream_t s) {
+                                  const uint32_t* seg, const uint32_t* slot_of, const uint32_t* start, uint32_t n,
+                                  uint32_t inc_base, uint32_t pair_base, uint32_t* out_idx, uint32_t* inc_pair,
+                                  cudaStream_t s) {
   if (!n) return cudaSuccess;
-  k_move_positions<<<grid_for(n), kThreads, 0, s>>>(sidx, flag, scan, seg, pair_vox, slot_of, start, n,
-                                                    perm_base, out_idx, out_key);
+  k_move_positions<<<grid_for(n), kThreads, 0, s>>>(sidx, flag, scan, seg, slot_of, start, n, inc_base,
+                                                    pair_base, out_idx, inc_pair);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pairs_renumbered(const uint32_t* order, uint32_t np, const uint32_t* vox_old,
+                                    const uint32_t* start, uint32_t pair_base, uint32_t perm_base,
+                                    uint32_t* pair_vox, uint32_t* seg, cudaStream_t s) {
+  k_pairs_renumbered<<<grid_for((int64_t)np + 1), kThreads, 0, s>>>(order, np, vox_old, start, pair_base,
+                                                                  perm_base, pair_vox, seg);
   return cudaGetLastError();
 }
 

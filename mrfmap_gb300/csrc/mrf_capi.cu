@@ -156,7 +156,7 @@ struct mrf_map {
   std::vector<View> views;
   // arenas
   DBuf meta, inc_pair, inc_len, inc_mu, inc_pl, pair_vox, pair_m, pair_cum, pair_stat, pair_ndyn, pair_hit,
-      pair_q, pair_dm, pair_seg, dperm, s_q0, s_q1, s_q2, s_q3, s_bf, s_loud, dpair, dseg, drun, carry, ray_order, ray_queue, region_q, rstart, rcounters, counters,
+      pair_q, pair_dm, pair_seg, dperm, s_q0, s_q1, s_q2, s_q3, s_bf, s_loud, s_pv, s_sg, dpair, dseg, drun, carry, ray_order, ray_queue, region_q, rstart, rcounters, counters,
       tile_first;
   uint32_t jac_tile_base = 0;
   int64_t n_inc = 0, n_pairs = 0, n_dperm = 0, n_dpairs = 0;
@@ -399,24 +399,32 @@ void rebuild(mrf_map* m) {
                       m->s_v0.as<uint32_t>(), m->s_v1.as<uint32_t>(), n, bits, m->stream));
     size_t t1 = scan_temp_bytes(nr + 1);
     m->s_tmp.reserve(t1, false, m->stream);
+    // voxel-order pairs: runs of the sorted voxel keys
+    CK(launch_vox_heads(m->s_k1.as<uint32_t>(), nr, m->s_k0.as<uint32_t>(), m->stream));
+    CK(cudaMemsetAsync(m->s_k0.as<uint32_t>() + nr, 0, 4, m->stream));
+    CK(exclusive_scan_u32(m->s_tmp.p, t1, m->s_k0.as<uint32_t>(), m->s_v0.as<uint32_t>(), nr + 1,
+                          m->stream));
+    const uint32_t np = read1(m, m->s_v0.as<uint32_t>() + nr);
+    u32_checked(pair_total + np + 1, "pair count");
+    size_t pb = (size_t)(pair_total + np + 1);
+    m->pair_vox.reserve(pb * 4, true, m->stream);
+    m->pair_m.reserve(pb * 4, true, m->stream);
+    m->pair_cum.reserve(pb * 4, true, m->stream);
+    m->pair_stat.reserve(pb * 4, true, m->stream);
+    m->pair_ndyn.reserve(pb * 4, true, m->stream);
+    m->pair_hit.reserve(pb * 4, true, m->stream);
+    m->pair_seg.reserve(pb * 4, true, m->stream);
     {
-      // voxel-order pairs: runs of the sorted voxel keys (pair_vox and
-      // pair_seg hold them until the renumbered pairs overwrite them)
-      CK(launch_vox_heads(m->s_k1.as<uint32_t>(), nr, m->s_k0.as<uint32_t>(), m->stream));
-      CK(cudaMemsetAsync(m->s_k0.as<uint32_t>() + nr, 0, 4, m->stream));
-      CK(exclusive_scan_u32(m->s_tmp.p, t1, m->s_k0.as<uint32_t>(), m->s_v0.as<uint32_t>(), nr + 1,
-                            m->stream));
-      const uint32_t np0 = read1(m, m->s_v0.as<uint32_t>() + nr);
-      const size_t pb0 = (size_t)(pair_total + np0 + 1);
-      m->pair_vox.reserve(pb0 * 4, true, m->stream);
-      m->pair_seg.reserve(pb0 * 4, true, m->stream);
-      uint32_t* pv = m->pair_vox.as<uint32_t>() + v.pair_base;
-      uint32_t* sg = m->pair_seg.as<uint32_t>() + v.pair_base;
+      const uint32_t np0 = np;
+      const size_t q4 = (size_t)np0 * 4 + 4;
+      m->s_pv.reserve(q4, false, m->stream);
+      m->s_sg.reserve(q4, false, m->stream);
+      uint32_t* pv = m->s_pv.as<uint32_t>();
+      uint32_t* sg = m->s_sg.as<uint32_t>();
       CK(launch_pairs_from_sorted(m->s_k1.as<uint32_t>(), m->s_v1.as<uint32_t>(), m->s_k0.as<uint32_t>(),
                                   m->s_v0.as<uint32_t>(), nr, 0, 0, v.inc_base, pv, sg, nullptr, m->stream));
       CK(launch_fill_u32(sg + np0, 1, nr, m->stream));
       // first visits: of each pair, and of each brick (min over its pairs)
-      const size_t q4 = (size_t)np0 * 4 + 4;
       m->s_q0.reserve(q4, false, m->stream);
       m->s_q1.reserve(q4, false, m->stream);
       m->s_q2.reserve(q4, false, m->stream);
@@ -446,33 +454,17 @@ void rebuild(mrf_map* m) {
       size_t t5 = scan_temp_bytes(np0 + 1);
       m->s_tmp.reserve(t5, false, m->stream);
       CK(exclusive_scan_u32(m->s_tmp.p, t5, q0, q1, np0 + 1, m->stream));
-      // the sorted positions in the new pair order: incidence index and voxel
+      // the sorted positions in the new pair order (and each incidence's
+      // new pair id), the renumbered pairs' voxels and runs
       m->s_recs.reserve((size_t)nr * 8, false, m->stream);
       uint32_t* nidx = m->s_recs.as<uint32_t>();
-      CK(launch_move_positions(m->s_v1.as<uint32_t>(), m->s_k0.as<uint32_t>(), m->s_v0.as<uint32_t>(), sg, pv,
-                               q3, q1, nr, 0, nidx, m->s_k1.as<uint32_t>(), m->stream));
+      CK(launch_move_positions(m->s_v1.as<uint32_t>(), m->s_k0.as<uint32_t>(), m->s_v0.as<uint32_t>(), sg, q3,
+                               q1, nr, v.inc_base, v.pair_base, nidx, m->inc_pair.as<uint32_t>(), m->stream));
+      CK(launch_pairs_renumbered(q2, np0, pv, q1, v.pair_base, v.perm_base, m->pair_vox.as<uint32_t>(),
+                                 m->pair_seg.as<uint32_t>(), m->stream));
       std::swap(m->s_v1, m->s_recs);  // the moved positions become the sorted order
       m->s_v1.reserve((size_t)n * 4 + 4, true, m->stream);
     }
-    CK(launch_vox_heads(m->s_k1.as<uint32_t>(), nr, m->s_k0.as<uint32_t>(), m->stream));
-    CK(cudaMemsetAsync(m->s_k0.as<uint32_t>() + nr, 0, 4, m->stream));
-    CK(exclusive_scan_u32(m->s_tmp.p, t1, m->s_k0.as<uint32_t>(), m->s_v0.as<uint32_t>(), nr + 1,
-                          m->stream));
-    uint32_t np = read1(m, m->s_v0.as<uint32_t>() + nr);
-    u32_checked(pair_total + np + 1, "pair count");
-    size_t pb = (size_t)(pair_total + np + 1);
-    m->pair_vox.reserve(pb * 4, true, m->stream);
-    m->pair_m.reserve(pb * 4, true, m->stream);
-    m->pair_cum.reserve(pb * 4, true, m->stream);
-    m->pair_stat.reserve(pb * 4, true, m->stream);
-    m->pair_ndyn.reserve(pb * 4, true, m->stream);
-    m->pair_hit.reserve(pb * 4, true, m->stream);
-    m->pair_seg.reserve(pb * 4, true, m->stream);
-    CK(launch_pairs_from_sorted(m->s_k1.as<uint32_t>(), m->s_v1.as<uint32_t>(), m->s_k0.as<uint32_t>(),
-                                m->s_v0.as<uint32_t>(), nr, v.pair_base, v.perm_base, v.inc_base,
-                                m->pair_vox.as<uint32_t>(), m->pair_seg.as<uint32_t>(),
-                                m->inc_pair.as<uint32_t>(), m->stream));
-    CK(launch_fill_u32(m->pair_seg.as<uint32_t>() + v.pair_base + np, 1, v.perm_base + nr, m->stream));
     CK(cudaMemsetAsync(m->s_k1.p, 0, 4, m->stream));
     CK(launch_count_loud(m->pair_vox.as<uint32_t>() + v.pair_base, np, m->s_loud.as<uint8_t>(),
                          m->s_k1.as<uint32_t>(), m->stream));
@@ -1102,7 +1094,7 @@ void destroy_bufs(mrf_map* m) {
                  &m->carry, &m->ray_order, &m->ray_queue, &m->region_q, &m->rstart, &m->rcounters, &m->counters, &m->tile_first,
                  &m->vseg, &m->vpairs, &m->vvox, &m->s_rec, &m->s_recs, &m->s_pf, &m->s_ps,
                  &m->s_flags, &m->s_ind, &m->s_scan,
-                 &m->s_q0, &m->s_q1, &m->s_q2, &m->s_q3, &m->s_bf, &m->s_loud,
+                 &m->s_q0, &m->s_q1, &m->s_q2, &m->s_q3, &m->s_bf, &m->s_loud, &m->s_pv, &m->s_sg,
                  &m->s_tmp, &m->s_counts, &m->s_offs, &m->s_vox, &m->s_k0, &m->s_k1, &m->s_v0,
                  &m->s_v1, &m->s_seg, &m->s_dense, &m->s_err, &m->s_depth_in, &m->s_depth,
                  &m->s_img, &m->s_part, &m->s_sum, &m->s_prev, &m->s_delta, &m->s_snap};

@@ -107,9 +107,12 @@ cudaError_t launch_count_loud(const uint32_t* pair_vox, uint32_t np, const uint8
 cudaError_t launch_new_lengths(const uint32_t* order, uint32_t np, const uint32_t* seg, uint32_t* len,
                                uint32_t* slot_of, cudaStream_t s);
 cudaError_t launch_move_positions(const uint32_t* sidx, const uint32_t* flag, const uint32_t* scan,
-                                  const uint32_t* seg, const uint32_t* pair_vox, const uint32_t* slot_of,
-                                  const uint32_t* start, uint32_t n, uint32_t perm_base, uint32_t* out_idx,
-                                  uint32_t* out_key, cudaStream_t s);
+                                  const uint32_t* seg, const uint32_t* slot_of, const uint32_t* start, uint32_t n,
+                                  uint32_t inc_base, uint32_t pair_base, uint32_t* out_idx, uint32_t* inc_pair,
+                                  cudaStream_t s);
+cudaError_t launch_pairs_renumbered(const uint32_t* order, uint32_t np, const uint32_t* vox_old,
+                                    const uint32_t* start, uint32_t pair_base, uint32_t perm_base,
+                                    uint32_t* pair_vox, uint32_t* seg, cudaStream_t s);
 // pairs from the pair-grouped incidences: pair_vox, seg and (when given)
 // inc_pair
 cudaError_t launch_pairs_from_sorted(const uint32_t* sk, const uint32_t* sidx, const uint32_t* flag,
