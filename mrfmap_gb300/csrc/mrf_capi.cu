@@ -20,6 +20,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <mutex>
 #include <thread>
@@ -610,14 +611,19 @@ void rebuild(mrf_map* m) {
         if (!is_home[i]) out.left.push_back((uint32_t)(v.pix_base + i));
     };
     {
+      // at most one thread per host core; the views are taken in turn
+      const int nt = std::max(1, std::min<int>(V, (int)std::thread::hardware_concurrency()));
+      std::atomic<int> next{0};
       std::vector<std::thread> pool;
       std::vector<char> failed((size_t)V, 0);
-      for (int c = 0; c < V; ++c)
-        pool.emplace_back([&, c] {
-          try {
-            build_view(c);
-          } catch (...) {
-            failed[(size_t)c] = 1;
+      for (int t = 0; t < nt; ++t)
+        pool.emplace_back([&] {
+          for (int c = next++; c < V; c = next++) {
+            try {
+              build_view(c);
+            } catch (...) {
+              failed[(size_t)c] = 1;
+            }
           }
         });
       for (auto& t : pool) t.join();
