@@ -870,6 +870,42 @@ int orc_trace_pixel(const orc_map* m, const float* pose, int x, int y, int* vox,
   return n;
 }
 
+/* ---- standard log-odds ray insertion ------------------------------------
+ * The occupancy update of classic occupancy mapping (as OctoMap's
+ * insertPointCloud applies it: every voxel a ray crosses before its
+ * endpoint gets the miss log-odds, the voxel holding the endpoint the hit
+ * log-odds, each clamped), over the map's active voxels with the same
+ * traversal.  Not part of MRFMap: a CPU baseline for the insertion-style
+ * mapping the paper compares against (OctoMap itself is absent here).
+ * Single-threaded, in pixel order.  Returns the voxel updates made. */
+int64_t orc_insert_logodds(const orc_map* m, const float* pose, const float* depth, float l_hit,
+                           float l_miss, float l_min, float l_max, double* L) {
+  int64_t n = 0;
+  for (int y = 0; y < m->cam.rows; ++y)
+    for (int x = 0; x < m->cam.cols; ++x) {
+      const float d = depth[(int64_t)y * m->cam.cols + x];
+      if (!(d > 0.0f)) continue;
+      float o[3], dr[3], mult;
+      ray_setup(m, &m->cam, pose, x, y, o, dr, &mult);
+      dda_t r;
+      if (!dda_init(&r, m, o, dr)) continue;
+      int vv[3];
+      float l, tin, te;
+      while (dda_next(&r, vv, &l, &tin, &te)) {
+        int64_t lin;
+        const int id = vox_id(m, vv, &lin);
+        const int hit = te * mult >= d;
+        if (id >= 0) {
+          double v = L[id] + (hit ? l_hit : l_miss);
+          L[id] = v < l_min ? l_min : (v > l_max ? l_max : v);
+          ++n;
+        }
+        if (hit) break;
+      }
+    }
+  return n;
+}
+
 /* ---- likelihood (gvdbkernels.cu:183-293, 1246-1274) ---------------------- */
 static double like_pixel(const orc_map* m, const float* pose, int x, int y, float d) {
   const float* sg = lut_at(m, &m->cam, m->sigma_lut, x, y);

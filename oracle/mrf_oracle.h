@@ -104,6 +104,13 @@ double orc_likelihood(const orc_map* m, const float* pose, const float* depth,
 void orc_render(const orc_map* m, int mode, const float* pose, const float* depth, float thresh,
                 float* out_img, int64_t* counts);
 
+/* classic log-odds ray insertion of one depth image at a pose (miss along
+ * the ray, hit at the endpoint voxel, clamped) into L (one double per
+ * active voxel, slot*512+local); single-threaded.  A CPU baseline, not part
+ * of MRFMap.  Returns the voxel updates made. */
+int64_t orc_insert_logodds(const orc_map* m, const float* pose, const float* depth, float l_hit,
+                           float l_miss, float l_min, float l_max, double* L);
+
 /* counters from the last orc_infer: incidence-iterations of Post passes */
 int64_t orc_last_updates(const orc_map* m);
 

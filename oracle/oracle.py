@@ -78,6 +78,9 @@ def lib():
         L.orc_render.argtypes = [vp, C.c_int, fp, fp, C.c_float, fp, C.POINTER(C.c_int64)]
         L.orc_last_updates.argtypes = [vp]
         L.orc_last_updates.restype = C.c_int64
+        L.orc_insert_logodds.argtypes = [vp, fp, fp, C.c_float, C.c_float, C.c_float, C.c_float,
+                                         C.POINTER(C.c_double)]
+        L.orc_insert_logodds.restype = C.c_int64
         _lib = L
     return _lib
 
@@ -199,3 +202,15 @@ class OracleMap:
         img = np.zeros((self.params.rows, self.params.cols), np.float32)
         tot = self._L.orc_likelihood(self._h, _ptr(_f(pose)), _ptr(_f(depth)), _ptr(img))
         return tot, img
+
+    def insert_logodds(self, pose, depth, logodds=None, l_hit=0.85, l_miss=-0.4, l_min=-2.0, l_max=3.5):
+        """Classic log-odds ray insertion (miss along the ray, hit at the
+        endpoint voxel, clamped; OctoMap's default parameters) of one depth
+        image into ``logodds`` (one float64 per active voxel, updated in
+        place; zeros when None).  A CPU baseline, not part of MRFMap.
+        Returns (voxel updates, logodds)."""
+        if logodds is None:
+            logodds = np.zeros(self.num_bricks * 512, np.float64)
+        n = self._L.orc_insert_logodds(self._h, _ptr(_f(pose)), _ptr(_f(depth)), l_hit, l_miss, l_min,
+                                       l_max, _ptr(logodds, C.c_double))
+        return int(n), logodds

@@ -337,3 +337,40 @@ def test_render_single_ray_known_answers(oracle_lib):
     assert r(3, 20.0)[0] == -1.0
     v, cnt = r(3, 10.0)
     assert list(cnt) == [0, 0, 1, 0]
+
+
+def test_logodds_insertion_known_answer(oracle_lib):
+    """The classic log-odds insertion (the CPU insertion baseline) along one
+    ray: every active voxel the ray crosses before its endpoint gets the
+    miss log-odds, the voxel holding the endpoint the hit log-odds, and the
+    ray stops there; a second insertion adds again, clamped."""
+    from mrfmap_gb300 import synthetic
+    w = synthetic.small_room(3, n_frames=2, rows=45, cols=60)
+    m = O.OracleMap(w.params, threads=2)
+    for P, D in zip(w.poses, w.depths):
+        m.add_view(P, D, O.ACT_FULL_RAY)
+    P, D = w.poses[0], w.depths[0]
+    ys, xs = np.nonzero(D > 0)
+    y, x = int(ys[len(ys) // 2]), int(xs[len(xs) // 2])
+    one = np.zeros_like(D)
+    one[y, x] = D[y, x]
+    vox, _, s = m.trace_pixel(P, x, y)
+    hit = int(np.argmax(s >= one[y, x]))
+    assert s[hit] >= one[y, x] and (hit == 0 or s[hit - 1] < one[y, x])
+    n, L = m.insert_logodds(P, one, l_hit=0.85, l_miss=-0.4, l_min=-2.0, l_max=3.5)
+    assert n == hit + 1
+    expect = np.zeros_like(L)
+    for v in vox[:hit]:
+        expect[v] += float(np.float32(-0.4))  # the parameters pass as float
+    expect[vox[hit]] += float(np.float32(0.85))
+    np.testing.assert_allclose(L, expect, rtol=0, atol=1e-12)
+    for _ in range(9):
+        m.insert_logodds(P, one, logodds=L, l_hit=0.85, l_miss=-0.4, l_min=-2.0, l_max=3.5)
+    assert L.min() >= -2.0 and L.max() <= 3.5
+    np.testing.assert_allclose(L[vox[hit]], 3.5)
+    np.testing.assert_allclose(L[vox[:hit]], -2.0)
+    assert len(set(vox[:hit + 1].tolist())) == hit + 1  # a ray crosses a voxel once
+    # a whole image: every valid pixel's ray makes at least its endpoint update
+    n_all, L_all = m.insert_logodds(P, D)
+    assert n_all >= 1 and np.isfinite(L_all).all()
+    assert (L_all > 0).any() and (L_all < 0).any()
