@@ -205,6 +205,29 @@ def cpu_insertion_rate(w, policy, n_views):
     return upd / max(dt, 1e-9), rays / max(dt, 1e-9), upd, dt
 
 
+def cpu_baselines(w, policy, sample_views):
+    """The CPU baselines of the bench line on a bounded sample of the
+    workload: the FP64 oracle port (all host cores, one Gauss-Seidel
+    iteration) and the classic log-odds insertion (single-threaded)."""
+    threads = os.cpu_count() or 1
+    nv = min(sample_views, len(w.poses))
+    r, upd, dt = cpu_port_rate(w, policy, nv, 1, threads)
+    cpu = {"value": r, "unit": UNIT, "cores": threads, "kind": "port",
+           "sample": f"FP64 oracle, {nv} of {len(w.poses)} keyframes, 1 Gauss-Seidel iteration "
+                     f"({upd} updates in {dt:.1f} s)"}
+    cpu_ins = None
+    if not w.cams:
+        try:
+            ir, rr, iu, idt = cpu_insertion_rate(w, policy, nv)
+            cpu_ins = {"value": ir, "unit": "voxel updates/s", "rays_per_s": rr, "cores": 1,
+                       "kind": "classic log-odds ray insertion (OctoMap's update rule; OctoMap "
+                               "itself is absent), single-threaded",
+                       "sample": f"{nv} of {len(w.poses)} keyframes ({iu} voxel updates in {idt:.2f} s)"}
+        except Exception as e:  # a reported extra: never fails the bench line
+            cpu_ins = {"error": str(e)}
+    return cpu, cpu_ins
+
+
 def run_reference(args):
     rank, ws = dist_setup()
     if rank != 0:
@@ -440,25 +463,9 @@ def run_ours(args):
         except Exception as e:
             parity = {"error": str(e)}
 
-    cpu = None
-    cpu_ins = None
+    cpu, cpu_ins = None, None
     if rank == 0 and not args.no_cpu_baseline:
-        threads = os.cpu_count() or 1
-        nv = min(args.cpu_sample_views, len(w.poses))
-        r, upd, dt = cpu_port_rate(w, args.policy, nv, 1, threads)
-        cpu = {"value": r, "unit": UNIT, "cores": threads, "kind": "port",
-               "sample": f"FP64 oracle, {nv} of {len(w.poses)} keyframes, 1 Gauss-Seidel iteration "
-                         f"({upd} updates in {dt:.1f} s)"}
-        if not w.cams:
-            try:
-                ir, rr, iu, idt = cpu_insertion_rate(w, args.policy, nv)
-                cpu_ins = {"value": ir, "unit": "voxel updates/s", "rays_per_s": rr, "cores": 1,
-                           "kind": "classic log-odds ray insertion (OctoMap's update rule; OctoMap "
-                                   "itself is absent), single-threaded",
-                           "sample": f"{nv} of {len(w.poses)} keyframes ({iu} voxel updates in "
-                                     f"{idt:.2f} s)"}
-            except Exception as e:  # a reported extra: never fails the bench line
-                cpu_ins = {"error": str(e)}
+        cpu, cpu_ins = cpu_baselines(w, args.policy, args.cpu_sample_views)
 
     if rank == 0:
         line = {

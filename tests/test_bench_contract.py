@@ -33,3 +33,18 @@ def test_reference_arm_line():
     assert e["value"] == d["value"] and e["unit"] == d["unit"]
     assert e["h2d_bytes_per_step"] == 0 and e["d2h_bytes_per_step"] == 0
     assert d["config"]["workload"].startswith("small_room")
+
+
+def test_cpu_baselines_of_our_line():
+    """The cpu_baseline and cpu_insertion objects of our arm's line (the same
+    function runs inside bench.py's GPU arm)."""
+    sys.path.insert(0, ROOT)
+    import bench
+    w = bench.workload("small")
+    cpu, ins = bench.cpu_baselines(w, "fullray", 2)
+    assert "error" not in ins, ins
+    assert cpu["kind"] == "port" and cpu["unit"] == bench.UNIT and cpu["value"] > 0 and cpu["cores"] >= 1
+    assert "2 of 5 keyframes" in cpu["sample"]
+    assert ins["unit"] == "voxel updates/s" and ins["value"] > 0 and ins["rays_per_s"] > 0
+    assert "error" not in ins and ins["cores"] == 1
+    json.dumps({"cpu_baseline": cpu, "cpu_insertion": ins})
