@@ -11,8 +11,8 @@
 //   k_pair_update  : per pair, the length-weighted message average, new
 //                    log-odds message, total log-odds and belief
 //                    (gvdbkernels.cu:457-479); a segmented sum over the
-//                    voxel-sorted incidence permutation -- no atomics, fixed
-//                    summation order
+//                    pair-grouped permutation of the dynamic incidences --
+//                    no atomics, fixed summation order
 #include <algorithm>
 
 #include "mrf_internal.h"

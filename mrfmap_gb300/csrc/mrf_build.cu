@@ -307,10 +307,11 @@ __global__ void __launch_bounds__(kThreads, 4)
   }
 }
 
-// Pairs in voxel order.  The view's incidences are sorted by voxel id
-// (stable: increasing incidence index inside a voxel); each run of one voxel
-// is a (camera, voxel) pair.  perm[k] is the incidence at pair-grouped
-// position k; seg[p] the first position of pair p.
+// Pairs, first in voxel order.  The view's incidences are sorted by voxel
+// id (stable: increasing incidence index inside a voxel); each run of one
+// voxel is a (camera, voxel) pair.  perm[k] is the incidence at
+// pair-grouped position k; seg[p] the first position of pair p.  The pairs
+// are then renumbered (k_pair_first below) and the positions regrouped.
 __global__ void k_vox_heads(const uint32_t* __restrict__ sk, uint32_t n, uint32_t* __restrict__ flag) {
   uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
   if (k < n) flag[k] = (k == 0 || sk[k] != sk[k - 1]) ? 1u : 0u;

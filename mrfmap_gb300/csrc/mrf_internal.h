@@ -89,7 +89,7 @@ cudaError_t launch_trace_emit(const Geom& g, const Pose& P, const float* depth,
                               const uint32_t* pix_off, uint32_t inc_base, RayMeta* meta,
                               uint32_t* inc_vox, float* inc_len, float* inc_mu, float2* inc_rec,
                               int* err, cudaStream_t s);
-// pairs in voxel order and the pair-grouped positions
+// runs of the voxel-sorted incidences (the pairs before renumbering)
 cudaError_t launch_vox_heads(const uint32_t* sk, uint32_t n, uint32_t* flag, cudaStream_t s);
 // brick-major first-visit pair numbering (mrf_build.cu)
 cudaError_t launch_pair_first(const uint32_t* seg, uint32_t np, uint32_t perm_base, const uint32_t* sidx,
