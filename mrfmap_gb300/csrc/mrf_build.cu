@@ -29,13 +29,7 @@ __global__ void k_clean_depth(const float* __restrict__ in, float* __restrict__ 
                               int cols) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= rows * cols) return;
-  float d = in[i];
-  float v = isfinite(d) ? d : -1.0f;
-  if (rows == 480 && cols == 848) {
-    int x = i % cols, y = i / cols;
-    if (x < 24 || x >= cols - 24 || y < 20 || y >= rows - 20) v = -1.0f;
-  }
-  out[i] = v;
+  out[i] = clean_depth_value(in[i], i, rows, cols);
 }
 
 __device__ __forceinline__ int floordiv8(int v) { return v >= 0 ? v / 8 : -((-v + 7) / 8); }

@@ -19,6 +19,18 @@ __device__ __forceinline__ float fa(float a, float b) { return __fadd_rn(a, b); 
 __device__ __forceinline__ float fs(float a, float b) { return __fsub_rn(a, b); }
 __device__ __forceinline__ float fd(float a, float b) { return __fdiv_rn(a, b); }
 
+// depth clean-up of pixel i of a rows x cols image (src/GVDBImage.cpp:32-40):
+// a non-finite return becomes "no return" (-1), and 848x480 images lose a
+// 24-pixel left/right and a 20-pixel top/bottom border
+__device__ __forceinline__ float clean_depth_value(float d, int i, int rows, int cols) {
+  float v = isfinite(d) ? d : -1.0f;
+  if (rows == 480 && cols == 848) {
+    int x = i % cols, y = i / cols;
+    if (x < 24 || x >= cols - 24 || y < 20 || y >= rows - 20) v = -1.0f;
+  }
+  return v;
+}
+
 // sensor polynomial p0 + p1 z (+ p2 z^2): src/cuda/gvdbkernels.cu:46-55
 __device__ __forceinline__ float poly_f(const float* c, int n, float z) {
   if (n == 3) return fa(fa(fm(fm(z, z), c[2]), fm(z, c[1])), c[0]);

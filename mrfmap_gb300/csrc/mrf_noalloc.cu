@@ -19,14 +19,21 @@
 //    before reading them, so nothing has to start at zero.  Calls that
 //    overlap on the GPU (two streams, or two maps on one device) race on the
 //    array and must be serialized by the caller.
-//  * the first call on each device looks the array up with
-//    cudaGetSymbolAddress (the host-side name of a __device__ array is not a
-//    device address); make that first call before any stream capture.
+//  * the first call in each CUDA context (per device, and again after the
+//    caller's process tears the context down and a new one is created, e.g.
+//    after cudaDeviceReset) looks the array up with cudaGetSymbolAddress (the
+//    host-side name of a __device__ array is not a device address); make
+//    that first call before any stream capture.  The looked-up address is
+//    kept per device together with the id of the context it belongs to, so an
+//    address of a destroyed context is never reused.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <mutex>
+#include <string>
 
 #include "../../include/mrfmap_gb300.h"
+#include "mrf_geometry.cuh"
 #include "mrf_internal.h"
 #include "mrf_like_pixel.cuh"
 
@@ -40,11 +47,45 @@ constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) double g_noalloc_partials[kNoAllocMaxBlocks];
 
+// the array's device address per device, valid for the context whose id is
+// stored with it
+struct ScratchAddr {
+  unsigned long long ctx_id = 0;
+  double* ptr = nullptr;
+};
 std::mutex g_setup_mu;
-double* g_partials_addr[kMaxDevices] = {nullptr};
+ScratchAddr g_scratch[kMaxDevices];
 
-// raw depth in: non-finite -> no return, and the reference's 848x480 border
-// clip (src/GVDBImage.cpp:32-40) applied in place of a cleaned copy
+// driver entry points for the current context's id, looked up through the
+// runtime (the library does not link the driver library itself)
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
+
+// id of the calling thread's current context (0 on failure)
+unsigned long long current_context_id() {
+  if (!g_ctx_get_current || !g_ctx_get_id) {
+    void* f0 = nullptr;
+    void* f1 = nullptr;
+    cudaDriverEntryPointQueryResult q0 = cudaDriverEntryPointSymbolNotFound, q1 = q0;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f0, 12000, cudaEnableDefault, &q0) !=
+            cudaSuccess ||
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &f1, 12000, cudaEnableDefault, &q1) != cudaSuccess ||
+        q0 != cudaDriverEntryPointSuccess || q1 != cudaDriverEntryPointSuccess || !f0 || !f1)
+      return 0;
+    g_ctx_get_current = reinterpret_cast<CtxGetCurrentFn>(f0);
+    g_ctx_get_id = reinterpret_cast<CtxGetIdFn>(f1);
+  }
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (g_ctx_get_current(&ctx) != CUDA_SUCCESS || !ctx) return 0;
+  if (g_ctx_get_id(ctx, &id) != CUDA_SUCCESS) return 0;
+  return id;
+}
+
+// raw depth in, cleaned on the fly by the same rule as the regular path's
+// cleaned copy (clean_depth_value)
 __global__ void __launch_bounds__(kNoAllocThreads)
     k_likelihood_noalloc(Geom g, Pose P, const float* __restrict__ depth,
                          const float* __restrict__ belief, float* __restrict__ out_img,
@@ -52,12 +93,7 @@ __global__ void __launch_bounds__(kNoAllocThreads)
   int pix = blockIdx.x * blockDim.x + threadIdx.x;
   float val = 0.0f;
   if (pix < g.rows * g.cols) {
-    float d = depth[pix];
-    if (!isfinite(d)) d = -1.0f;
-    if (g.rows == 480 && g.cols == 848) {
-      int x = pix % g.cols, y = pix / g.cols;
-      if (x < 24 || x >= g.cols - 24 || y < 20 || y >= g.rows - 20) d = -1.0f;
-    }
+    const float d = clean_depth_value(depth[pix], pix, g.rows, g.cols);
     if (d > 0.0f) val = likelihood_pixel(g, P, belief, pix, d);
     if (out_img) out_img[pix] = val;
   }
@@ -97,7 +133,13 @@ extern "C" MRF_API mrf_status mrf_likelihood_device_noalloc(mrf_map* map, const 
   double* partials = nullptr;
   {
     std::lock_guard<std::mutex> lk(g_setup_mu);
-    if (!g_partials_addr[device]) {
+    const unsigned long long ctx = current_context_id();
+    if (ctx == 0) {
+      mrf_internal_set_error("mrf_likelihood_device_noalloc: no current CUDA context");
+      return MRF_ERR_CUDA;
+    }
+    ScratchAddr& a = g_scratch[device];
+    if (!a.ptr || a.ctx_id != ctx) {
       void* ptr = nullptr;
       cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_partials);
       if (e != cudaSuccess || !ptr) {
@@ -105,10 +147,15 @@ extern "C" MRF_API mrf_status mrf_likelihood_device_noalloc(mrf_map* map, const 
                                cudaGetErrorString(e));
         return MRF_ERR_CUDA;
       }
-      g_partials_addr[device] = static_cast<double*>(ptr);
+      a.ptr = static_cast<double*>(ptr);
+      a.ctx_id = ctx;
     }
-    partials = g_partials_addr[device];
+    partials = a.ptr;
   }
+  // a map without active bricks has no belief field; every brick-table probe
+  // then misses, so the kernel never reads through this (valid) pointer and
+  // the result is the regular entry point's n * ln(LIKE_EPS)
+  if (!belief) belief = reinterpret_cast<const float*>(partials);
   Pose P;
   for (int i = 0; i < 16; ++i) P.m[i] = pose[i];
   k_likelihood_noalloc<<<(unsigned)nblocks, kNoAllocThreads, 0, stream>>>(g, P, depth_dev, belief,
