@@ -7,7 +7,8 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
-REFERENCE = "/root/reference"
+# the reference source tree, when a test wants to read it directly (unset: skip)
+REFERENCE = os.environ.get("MRFMAP_REFERENCE_DIR")
 
 
 def pytest_configure(config):

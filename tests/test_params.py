@@ -77,9 +77,51 @@ def test_eigen_binary_reader(tmp_path):
     np.testing.assert_array_equal(read_eigen_binary(str(f)), a)
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference/data"), reason="reference fixtures absent")
+REFERENCE = os.environ.get("MRFMAP_REFERENCE_DIR")
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "coffin_world.npz")
+
+
+@pytest.mark.skipif(not REFERENCE or not os.path.isdir(os.path.join(REFERENCE or "", "data")),
+                    reason="MRFMAP_REFERENCE_DIR unset or without data/")
 def test_reference_fixture_shapes():
-    d = read_eigen_binary("/root/reference/data/depth_0.bin")
-    P = read_eigen_binary("/root/reference/data/pose_0.bin")
+    d = read_eigen_binary(os.path.join(REFERENCE, "data", "depth_0.bin"))
+    P = read_eigen_binary(os.path.join(REFERENCE, "data", "pose_0.bin"))
     assert d.shape == (480, 640) and P.shape == (4, 4)
     assert np.isnan(d).sum() == 69120
+
+
+@pytest.mark.skipif(not REFERENCE or not os.path.isdir(os.path.join(REFERENCE or "", "data")),
+                    reason="MRFMAP_REFERENCE_DIR unset or without data/")
+def test_golden_fixture_is_the_reference_data():
+    """tests/golden/coffin_world.npz holds the reference's frames unchanged
+    (row-major) and its body poses times cam_in_body."""
+    g = np.load(GOLDEN)
+    for k in (0, 7, 12):
+        d = read_eigen_binary(os.path.join(REFERENCE, "data", f"depth_{k}.bin"))
+        np.testing.assert_array_equal(g["depth"][k].view(np.uint32), d.view(np.uint32))
+        body = read_eigen_binary(os.path.join(REFERENCE, "data", f"pose_{k}.bin")).astype(np.float64)
+        np.testing.assert_allclose(g["pose"][k], body @ _cam_in_body(),
+                                   rtol=0, atol=1e-6)
+
+
+def _cam_in_body():
+    # config/coffin_world_640.yaml viewer_params_nodes.cam_in_body, row by row
+    return np.array([[0, 0, 1, 0], [-1, 0, 0, 0], [0, -1, 0, 0], [0, 0, 0, 1]], np.float64)
+
+
+def test_golden_fixture_loads_as_reference_config(tmp_path):
+    """The committed fixture's config parses to the reference's map and
+    sensor parameters (config/coffin_world_640.yaml:16-34)."""
+    g = np.load(GOLDEN)
+    f = tmp_path / "coffin_world_640.yaml"
+    f.write_text(str(g["yaml"]))
+    p = MapParams().load_from_file(str(f))
+    assert (p.rows, p.cols, p.res, p.dims, p.max_iters) == (480, 640, 0.02, (4.0, 4.0, 3.0), 3)
+    assert (p.fx, p.fy, p.cx, p.cy) == (381.36115025, 381.36115025, 319.5, 239.5)
+    assert p.use_polys is False and p.lookup_n == 3 and p.prior == pytest.approx(0.1)
+    np.testing.assert_array_equal(p.sigma_lut[:3], np.float32([0.05, 0.0, 0.0]))
+    assert g["depth"].shape == (13, 480, 640) and g["pose"].shape == (13, 4, 4)
+    assert np.isnan(g["depth"]).sum() == 13 * 69120
+    # camera z axis of frame 0 points from (3, 0, 2) m down towards the volume
+    np.testing.assert_allclose(g["pose"][0][:3, 3], [3.0, 0.0, 2.0], atol=1e-6)
+    assert g["pose"][0][2, 2] < 0
