@@ -102,6 +102,20 @@ MRF_API void mrf_destroy(mrf_map* map);
  * map; this returns the pooled blocks to the driver.  No reference
  * counterpart. */
 MRF_API mrf_status mrf_release_cached_memory(void);
+/* Bound on the device memory the maps of this process hold on one device
+ * (bytes, per device; 0 = no bound, the default).  A call that would grow
+ * a buffer past it fails with MRF_ERR_OOM before allocating; the map keeps
+ * its views and can be used again once the memory is there (a higher bound,
+ * other maps destroyed).  mrf_memory_in_use reports the bytes held on the
+ * current device (-1 without one).  No reference counterpart: GVDB's pool
+ * grows until the driver refuses. */
+MRF_API mrf_status mrf_set_memory_limit(int64_t bytes);
+MRF_API int64_t mrf_memory_in_use(void);
+/* Test hook, no reference counterpart: sets the map's device error flag from
+ * the host, as a traversal kernel does when a ray exceeds 65532 incidences.
+ * The next call that checks the flag (an incidence-list build) fails with
+ * MRF_ERR_DEVICE and clears it. */
+MRF_API mrf_status mrf_test_raise_device_error(mrf_map* map);
 /* Text of the last error raised on this thread. */
 MRF_API const char* mrf_last_error(void);
 
@@ -141,6 +155,16 @@ MRF_API mrf_status mrf_infer(mrf_map* map, const int* ids, int n_ids, int iters,
 MRF_API mrf_status mrf_infer_converge(mrf_map* map, const int* ids, int n_ids, int max_iters,
                                       float tol, int check_every, int flags, int* iters_done,
                                       float* last_delta);
+/* mrf_infer run until the map reaches a given belief field: iterations stop
+ * after the first one whose largest |belief - target| (over every voxel) is
+ * at most tol, checked every check_every iterations, max_iters the cap.
+ * target_dev is a device array of n_bricks x 512 floats (slot order, as
+ * mrf_read_bricks).  No reference counterpart: this is the clock of "time
+ * to the converged map" when the converged map is known (a tightly
+ * converged plain run).  iters_done and last_dist may be NULL. */
+MRF_API mrf_status mrf_infer_until(mrf_map* map, const int* ids, int n_ids, int max_iters,
+                                   const float* target_dev, float tol, int check_every, int flags,
+                                   int* iters_done, float* last_dist);
 /* Warm start (no reference counterpart).  From a predicted total log-odds
  * field logodds[n_bricks x 512] (slot order, as mrf_read_logodds): pairs
  * whose messages are build constants get them exactly, the other pairs of
@@ -229,10 +253,12 @@ MRF_API mrf_status mrf_likelihood_device(mrf_map* map, const float* pose, const 
  * device, hosts whose allocator owns all device memory).  The depth image
  * is cleaned on the fly; the only scratch is a fixed file-scope device array
  * of 4096 FP64 partial sums (32 KiB), so images are limited to 524,288
- * pixels (MRF_ERR_INVALID beyond; 640x480 and 848x480 fit).  All calls share that array: calls overlapping
- * on the GPU race and must be serialized.  The first call on each device
- * looks the array up with cudaGetSymbolAddress; make it before any stream
- * capture.  The map must have active bricks (MRF_ERR_STATE otherwise). */
+ * pixels (MRF_ERR_INVALID beyond; 640x480 and 848x480 fit).  All calls share
+ * that array: calls overlapping on the GPU race and must be serialized.  The
+ * first call in each CUDA context (per device, and again in a context created
+ * after the caller destroyed the previous one) looks the array up with
+ * cudaGetSymbolAddress; make it before any stream capture.  A map without
+ * active bricks scores n * ln(LIKE_EPS), as mrf_likelihood_device does. */
 MRF_API mrf_status mrf_likelihood_device_noalloc(mrf_map* map, const float* pose,
                                                  const float* depth_dev, float* out_img_dev,
                                                  float* out_sum_dev);

@@ -911,6 +911,27 @@ __global__ void k_scatter_const(const uint32_t* __restrict__ idx, uint32_t n, fl
   if (p < n) dense[idx[p]] = v;
 }
 
+// pairs past the length gate (the ones that ever update): counted, and
+// their voxels flagged
+__global__ void k_touch_pairs(const uint32_t* __restrict__ pair_vox, const float* __restrict__ cum,
+                              uint32_t np, uint8_t* __restrict__ flag,
+                              unsigned long long* __restrict__ n_active) {
+  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool act = p < np && cum[p] > kCumLenGate;
+  if (act) flag[pair_vox[p]] = 1;
+  const unsigned b = __ballot_sync(kFull, act);
+  if ((threadIdx.x & 31) == 0 && b) atomicAdd(n_active, (unsigned long long)__popc(b));
+}
+
+__global__ void k_count_flags(const uint8_t* __restrict__ flag, int64_t n, unsigned long long* __restrict__ out) {
+  unsigned c = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    c += flag[i] != 0;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(kFull, c, o);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, (unsigned long long)c);
+}
+
 inline unsigned blocks(int64_t n, int t) { return (unsigned)std::max<int64_t>(1, (n + t - 1) / t); }
 
 }  // namespace
@@ -1121,6 +1142,17 @@ cudaError_t launch_vassign(const uint32_t* sk, const uint32_t* flag, const uint3
                            uint32_t n, uint32_t* vvox, uint32_t* vseg, cudaStream_t s) {
   if (!n) return cudaSuccess;
   k_vassign<<<blocks(n, 256), 256, 0, s>>>(sk, flag, scan, n, vvox, vseg);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_touch_counts(const uint32_t* pair_vox, const float* cum, uint32_t np, uint8_t* flag,
+                                int64_t nvox, unsigned long long* out2, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(out2, 0, 16, s);
+  if (e == cudaSuccess && nvox > 0) e = cudaMemsetAsync(flag, 0, (size_t)nvox, s);
+  if (e != cudaSuccess) return e;
+  if (np) k_touch_pairs<<<blocks(np, 256), 256, 0, s>>>(pair_vox, cum, np, flag, out2);
+  if (nvox > 0)
+    k_count_flags<<<(unsigned)std::min<int64_t>(blocks(nvox, 256), 4096), 256, 0, s>>>(flag, nvox, out2 + 1);
   return cudaGetLastError();
 }
 

@@ -87,24 +87,51 @@ cudaMemPool_t map_pool() {
   return g_pools[dev];
 }
 
+// Bytes the maps of this process hold per device, and the optional bound
+// on them (mrf_set_memory_limit; 0 = none).  A buffer that would grow past
+// the bound fails with MRF_ERR_OOM before anything is allocated.
+std::atomic<int64_t> g_in_use[kMaxDevices];
+std::atomic<int64_t> g_limit{0};
+
 // growable device buffer (stream-ordered on the stream that last sized it)
 struct DBuf {
   void* p = nullptr;
   size_t cap = 0;
+  int dev = 0;
   cudaStream_t owner = nullptr;
   void reserve(size_t bytes, bool keep, cudaStream_t s) {
     if (bytes <= cap) return;
     size_t nc = std::max(bytes, cap + cap / 2);
+    int d = 0;
+    CK(cudaGetDevice(&d));
+    if (d < 0 || d >= kMaxDevices) fail(MRF_ERR_INVALID, "device index out of range");
+    const int64_t lim = g_limit.load();
+    if (lim > 0 && g_in_use[d].load() + (int64_t)nc > lim) {
+      // a buffer as large as the request itself may still fit where the
+      // growth margin does not
+      nc = bytes;
+      if (g_in_use[d].load() + (int64_t)nc > lim)
+        fail(MRF_ERR_OOM, "device memory limit reached (" + std::to_string(g_in_use[d].load()) + " + " +
+                              std::to_string(nc) + " bytes > " + std::to_string(lim) + ")");
+    }
     void* q = nullptr;
     CK(cudaMallocFromPoolAsync(&q, nc, map_pool(), s));
+    g_in_use[d] += (int64_t)nc;
     if (keep && p && cap) CK(cudaMemcpyAsync(q, p, cap, cudaMemcpyDeviceToDevice, s));
-    if (p) CK(cudaFreeAsync(p, s));
+    if (p) {
+      CK(cudaFreeAsync(p, s));
+      g_in_use[dev] -= (int64_t)cap;
+    }
     p = q;
     cap = nc;
+    dev = d;
     owner = s;
   }
   void release() {
-    if (p) cudaFreeAsync(p, owner);
+    if (p) {
+      cudaFreeAsync(p, owner);
+      g_in_use[dev] -= (int64_t)cap;
+    }
     p = nullptr;
     cap = 0;
   }
@@ -268,7 +295,55 @@ void activate_view(mrf_map* m, const View& v) {
 }
 
 // ---- incidence lists ---------------------------------------------------
+// the pairs and messages of the previous build, kept while a new build
+// runs so that every camera's messages move over to its new pairs
+struct OldPairs {
+  bool remap = false;
+  int64_t n_pairs = 0;
+  DBuf vox, m;
+  std::vector<View> views;  // pair_base / n_pairs of each view
+};
+
+void rebuild_lists(mrf_map* m, OldPairs& old);
+
+// A build that fails (device memory bound, device error flag) leaves the
+// previous pairs and messages in place, so the next build can still move
+// the messages over.
 void rebuild(mrf_map* m) {
+  OldPairs old;
+  old.remap = m->has_messages && m->n_pairs > 0;
+  old.n_pairs = m->n_pairs;
+  if (old.remap) {
+    old.vox = m->pair_vox;
+    old.m = m->pair_m;
+    m->pair_vox = DBuf{};
+    m->pair_m = DBuf{};
+    for (auto& v : m->views) {
+      View c;
+      c.pair_base = v.pair_base;
+      c.n_pairs = v.n_pairs;
+      old.views.push_back(std::move(c));
+    }
+  }
+  try {
+    rebuild_lists(m, old);
+  } catch (...) {
+    if (old.remap) {
+      m->pair_vox.release();
+      m->pair_m.release();
+      m->pair_vox = old.vox;
+      m->pair_m = old.m;
+      m->n_pairs = old.n_pairs;
+      for (size_t c = 0; c < old.views.size() && c < m->views.size(); ++c) {
+        m->views[c].pair_base = old.views[c].pair_base;
+        m->views[c].n_pairs = old.views[c].n_pairs;
+      }
+    }
+    throw;
+  }
+}
+
+void rebuild_lists(mrf_map* m, OldPairs& old) {
   const int V = (int)m->views.size();
   m->g.brick_slot = m->d_slot.as<int>();
   // per-pixel arrays of all views back to back (views may differ in size)
@@ -279,23 +354,10 @@ void rebuild(mrf_map* m) {
     npix += (int64_t)v.cam.rows * v.cam.cols;
   }
   CK(cudaEventRecord(m->ev0, m->stream));
-  // keep old pair arrays for message remapping
-  bool remap = m->has_messages && m->n_pairs > 0;
-  DBuf old_vox, old_m;
-  std::vector<View> old_views;
-  if (remap) {
-    old_vox = m->pair_vox;
-    old_m = m->pair_m;
-    m->pair_vox = DBuf{};
-    m->pair_m = DBuf{};
-    old_views = std::vector<View>();
-    for (auto& v : m->views) {
-      View c;
-      c.pair_base = v.pair_base;
-      c.n_pairs = v.n_pairs;
-      old_views.push_back(std::move(c));
-    }
-  }
+  const bool remap = old.remap;
+  DBuf& old_vox = old.vox;
+  DBuf& old_m = old.m;
+  const std::vector<View>& old_views = old.views;
   // 1. counts of every pixel of every view, one global scan -> offsets
   u32_checked(npix, "pixel count");
   m->s_counts.reserve((size_t)npix * 4 + 4, false, m->stream);
@@ -723,6 +785,7 @@ void rebuild(mrf_map* m) {
     sync(m);
     old_vox.release();
     old_m.release();
+    old.remap = false;  // the new pairs hold the messages from here on
   }
   CK(cudaEventRecord(m->ev1, m->stream));
   sync(m);
@@ -959,9 +1022,11 @@ cudaGraphExec_t iteration_graph(mrf_map* m, const BpArrays& a, bool jacobi, int 
 }
 
 // tol > 0: stop after the first iteration whose largest belief change is
-// below tol (checked every check_every iterations; iters is the cap)
+// below tol -- or, with a target field, whose largest distance to the
+// target is at most tol (checked every check_every iterations; iters is the
+// cap)
 void run_infer(mrf_map* m, const int* ids, int n_ids, int iters, int flags, float tol = -1.0f,
-               int check_every = 1, float* last_delta = nullptr) {
+               int check_every = 1, float* last_delta = nullptr, const float* target = nullptr) {
   ensure_built(m);
   const bool jacobi = flags & MRF_JACOBI;
   if (jacobi && m->jacobi_version != m->built_version) build_jacobi_csr(m);
@@ -1000,7 +1065,7 @@ void run_infer(mrf_map* m, const int* ids, int n_ids, int iters, int flags, floa
       for (int ph = 0; ph < 3 && ph < iters; ++ph) exec[ph] = iteration_graph(m, a, jacobi, fix, ph, per[ph]);
     for (int it = 0; it < iters; ++it) {
       const bool check = conv && ((it + 1) % check_every == 0 || it + 1 == iters);
-      if (check)
+      if (check && !target)
         CK(cudaMemcpyAsync(m->s_prev.p, m->d_belief.p, (size_t)nvox * 4, cudaMemcpyDeviceToDevice,
                            m->stream));
       const int ph = std::min(it, 2);
@@ -1012,14 +1077,14 @@ void run_infer(mrf_map* m, const int* ids, int n_ids, int iters, int flags, floa
       }
       done = it + 1;
       if (check) {
-        CK(launch_max_abs_diff(m->d_belief.as<float>(), m->s_prev.as<float>(), nvox,
+        CK(launch_max_abs_diff(m->d_belief.as<float>(), target ? target : m->s_prev.as<float>(), nvox,
                                m->s_delta.as<uint32_t>(), m->stream));
         ++launches;
         uint32_t bits = 0;
         CK(cudaMemcpyAsync(&bits, m->s_delta.p, 4, cudaMemcpyDeviceToHost, m->stream));
         sync(m);
         std::memcpy(&delta, &bits, 4);
-        if (delta < tol) break;
+        if (target ? delta <= tol : delta < tol) break;
       }
     }
   }
@@ -1139,13 +1204,11 @@ mrf_status mrf_internal_like_inputs(mrf_map* m, Geom* g, const float** belief, c
     set_err("cudaSetDevice failed");
     return MRF_ERR_CUDA;
   }
-  if (m->n_bricks == 0) {
-    set_err("the map has no active bricks");
-    return MRF_ERR_STATE;
-  }
   *g = m->g;
   g->brick_slot = m->d_slot.as<int>();
-  *belief = m->d_belief.as<float>();
+  // no belief field before the first active brick (every brick-table probe
+  // misses then, so the field is never read)
+  *belief = m->n_bricks ? m->d_belief.as<float>() : nullptr;
   *stream = m->stream;
   *device = m->device;
   return MRF_OK;
@@ -1247,6 +1310,30 @@ mrf_status mrf_release_cached_memory(void) {
     }
   }
   return MRF_OK;
+}
+
+mrf_status mrf_set_memory_limit(int64_t bytes) {
+  if (bytes < 0) {
+    set_err("negative memory limit");
+    return MRF_ERR_INVALID;
+  }
+  g_limit.store(bytes);
+  return MRF_OK;
+}
+
+int64_t mrf_memory_in_use(void) {
+  int d = 0;
+  if (cudaGetDevice(&d) != cudaSuccess || d < 0 || d >= kMaxDevices) return -1;
+  return g_in_use[d].load();
+}
+
+mrf_status mrf_test_raise_device_error(mrf_map* m) {
+  if (guard(m) != MRF_OK) return MRF_ERR_INVALID;
+  return wrap([&] {
+    const int one = 1;
+    CK(cudaMemcpyAsync(m->s_err.p, &one, sizeof(int), cudaMemcpyHostToDevice, m->stream));
+    sync(m);
+  });
 }
 
 static mrf_status add_view_impl(mrf_map* m, const float* pose, const float* depth, bool device,
@@ -1361,6 +1448,20 @@ mrf_status mrf_infer_converge(mrf_map* m, const int* ids, int n_ids, int max_ite
   }
   return wrap([&] {
     run_infer(m, ids, ids ? n_ids : 0, max_iters, flags, tol, check_every, last_delta);
+    if (iters_done) *iters_done = (int)m->stats.iters_done;
+  });
+}
+
+mrf_status mrf_infer_until(mrf_map* m, const int* ids, int n_ids, int max_iters, const float* target_dev,
+                           float tol, int check_every, int flags, int* iters_done, float* last_dist) {
+  if (guard(m) != MRF_OK) return MRF_ERR_INVALID;
+  if (n_ids < 0 || (n_ids > 0 && !ids) || !(tol >= 0.0f) || !target_dev) {
+    set_err("invalid ids, tolerance or target");
+    return MRF_ERR_INVALID;
+  }
+  return wrap([&] {
+    run_infer(m, ids, ids ? n_ids : 0, max_iters, flags, tol > 0.0f ? tol : 1e-30f, check_every, last_dist,
+              target_dev);
     if (iters_done) *iters_done = (int)m->stats.iters_done;
   });
 }
@@ -1840,9 +1941,9 @@ mrf_status mrf_load_map(mrf_map* m, const float* points, const float* occ, int64
     set_err("invalid points");
     return MRF_ERR_INVALID;
   }
-  return wrap([&] {
+  DBuf pts, oc;  // released on every exit, failures included
+  mrf_status st = wrap([&] {
     if (n == 0) return;
-    DBuf pts, oc;
     pts.reserve((size_t)n * 12, false, m->stream);
     oc.reserve((size_t)n * 4, false, m->stream);
     CK(cudaMemcpyAsync(pts.p, points, (size_t)n * 12, cudaMemcpyHostToDevice, m->stream));
@@ -1854,10 +1955,11 @@ mrf_status mrf_load_map(mrf_map* m, const float* points, const float* occ, int64
     m->g.brick_slot = m->d_slot.as<int>();
     CK(launch_set_points(m->g, pts.as<float>(), oc.as<float>(), n, m->d_belief.as<float>(), m->stream));
     sync(m);
-    pts.release();
-    oc.release();
     m->stats.n_bricks = m->n_bricks;
   });
+  pts.release();
+  oc.release();
+  return st;
 }
 
 mrf_status mrf_view_incidences(mrf_map* m, int view_id, int* meta, uint32_t* vox, float* len,
@@ -1924,25 +2026,17 @@ mrf_status mrf_stats_get(mrf_map* m, mrf_stats* out) {
   if (guard(m) != MRF_OK || !out) return MRF_ERR_INVALID;
   mrf_status st = wrap([&] {
     ensure_built(m);
-    // active pairs and touched voxels need a device pass: cheap host pass here
-    int64_t np = m->n_pairs;
-    std::vector<float> cum((size_t)np);
-    std::vector<uint32_t> vox((size_t)np);
-    if (np) {
-      CK(cudaMemcpyAsync(cum.data(), m->pair_cum.p, (size_t)np * 4, cudaMemcpyDeviceToHost, m->stream));
-      CK(cudaMemcpyAsync(vox.data(), m->pair_vox.p, (size_t)np * 4, cudaMemcpyDeviceToHost, m->stream));
-      sync(m);
-    }
-    int64_t act = 0;
-    std::vector<uint32_t> tv;
-    for (int64_t i = 0; i < np; ++i)
-      if (cum[i] > kCumLenGate) {
-        ++act;
-        tv.push_back(vox[i]);
-      }
-    std::sort(tv.begin(), tv.end());
-    m->stats.n_pairs_active = act;
-    m->stats.n_vox_touched = (int64_t)(std::unique(tv.begin(), tv.end()) - tv.begin());
+    // pairs past the length gate and the distinct voxels they reach
+    const int64_t nvox = m->n_bricks * kBrickVox;
+    m->s_loud.reserve((size_t)std::max<int64_t>(nvox, 1), false, m->stream);
+    m->s_delta.reserve(64, false, m->stream);
+    CK(launch_touch_counts(m->pair_vox.as<uint32_t>(), m->pair_cum.as<float>(), (uint32_t)m->n_pairs,
+                           m->s_loud.as<uint8_t>(), nvox, m->s_delta.as<unsigned long long>(), m->stream));
+    unsigned long long cnt[2] = {0, 0};
+    CK(cudaMemcpyAsync(cnt, m->s_delta.p, 16, cudaMemcpyDeviceToHost, m->stream));
+    sync(m);
+    m->stats.n_pairs_active = (int64_t)cnt[0];
+    m->stats.n_vox_touched = (int64_t)cnt[1];
     m->stats.n_views = (int64_t)m->views.size();
     m->stats.n_bricks = m->n_bricks;
   });

@@ -250,6 +250,10 @@ cudaError_t launch_fill_f32(float* p, int64_t n, float v, cudaStream_t s);
 cudaError_t launch_max_abs_diff(const float* a, const float* b, int64_t n, uint32_t* out,
                                 cudaStream_t s);
 cudaError_t launch_fill_u32(uint32_t* p, int64_t n, uint32_t v, cudaStream_t s);
+// out2[0] = pairs past the length gate, out2[1] = distinct voxels they
+// reach (flag: nvox bytes of scratch)
+cudaError_t launch_touch_counts(const uint32_t* pair_vox, const float* cum, uint32_t np, uint8_t* flag,
+                                int64_t nvox, unsigned long long* out2, cudaStream_t s);
 cudaError_t launch_vflag(const uint32_t* sk, uint32_t n, uint32_t* flag, cudaStream_t s);
 cudaError_t launch_vassign(const uint32_t* sk, const uint32_t* flag, const uint32_t* scan,
                            uint32_t n, uint32_t* vvox, uint32_t* vseg, cudaStream_t s);
@@ -272,8 +276,9 @@ cudaError_t launch_render(int mode, const Geom& g, const Pose& P, const float* d
                           cudaStream_t s);
 
 // Map state the likelihood needs, for entry points outside mrf_capi.cu: the
-// map's geometry (device brick table and sensor tables), its belief field,
-// stream and device.  Makes the map's device current.  Allocates nothing.
+// map's geometry (device brick table and sensor tables), its belief field
+// (NULL while the map has no active brick), stream and device.  Makes the
+// map's device current.  Allocates nothing.
 mrf_status mrf_internal_like_inputs(mrf_map* map, Geom* g, const float** belief,
                                     cudaStream_t* stream, int* device);
 void mrf_internal_set_error(const std::string& msg);

@@ -40,7 +40,8 @@ EXPORTS = ["mrf_create", "mrf_destroy", "mrf_release_cached_memory", "mrf_last_e
            "mrf_num_nodes", "mrf_read_nodes", "mrf_load_map", "mrf_view_incidences",
            "mrf_device_beliefs",
            "mrf_stats_get", "mrf_get_stream", "mrf_synchronize", "mrf_render", "mrf_render_view", "mrf_pixel_diagnostics", "mrf_add_view_camera",
-           "mrf_view_camera"]
+           "mrf_view_camera", "mrf_set_memory_limit", "mrf_memory_in_use", "mrf_test_raise_device_error",
+           "mrf_infer_until"]
 
 RENDER_EXPECTED_DEPTH = 0
 RENDER_ACCURACY = 1
@@ -138,6 +139,11 @@ def load(path: str | None = None):
         "mrf_add_view_camera": ([vp, fp, fp, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float,
                                  ip], C.c_int),
         "mrf_view_camera": ([vp, C.c_int, ip, ip, fp], C.c_int),
+        "mrf_set_memory_limit": ([C.c_int64], C.c_int),
+        "mrf_infer_until": ([vp, ip, C.c_int, C.c_int, C.c_void_p, C.c_float, C.c_int, C.c_int, ip, fp],
+                            C.c_int),
+        "mrf_memory_in_use": ([], C.c_int64),
+        "mrf_test_raise_device_error": ([vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)
@@ -261,6 +267,19 @@ class MRFMap:
             a = np.ascontiguousarray(ids, dtype=np.int32)
             _check(self._L.mrf_infer_converge(self._h, a.ctypes.data_as(C.POINTER(C.c_int)), len(a),
                                               max_iters, tol, check_every, flags, C.byref(n), C.byref(d)))
+        return n.value, d.value
+
+    def infer_until(self, target_dev_ptr: int, tol: float, max_iters: int = 0, ids=None, flags: int = 0,
+                    check_every: int = 1):
+        """Iterate until the largest |belief - target| is at most tol
+        (target: a device array of n_bricks x 512 floats); returns
+        (iterations run, last measured distance)."""
+        n = C.c_int()
+        d = C.c_float()
+        a = None if ids is None else np.ascontiguousarray(ids, dtype=np.int32)
+        _check(self._L.mrf_infer_until(self._h, None if a is None else a.ctypes.data_as(C.POINTER(C.c_int)),
+                                       0 if a is None else len(a), max_iters, C.c_void_p(target_dev_ptr),
+                                       tol, check_every, flags, C.byref(n), C.byref(d)))
         return n.value, d.value
 
     def warm_start(self, logodds, sweeps: int = 3):

@@ -324,3 +324,34 @@ def test_message_checkpoint_resume(native_lib, w):
     assert np.abs(m.beliefs() - b8).max() <= 1e-4
     with pytest.raises(L.MrfError):
         m.read_messages(len(w.poses))
+
+
+def test_infer_until_a_target_map(native_lib, w):
+    """mrf_infer_until stops at the first checked iteration within tol of a
+    target field; from the same start it takes no more iterations than the
+    plain run to that field, and it equals an mrf_infer of that many
+    iterations bit for bit."""
+    import torch
+    m = L.MRFMap(w.params, activation=L.ACT_FULL_RAY)
+    for P, D in zip(w.poses, w.depths):
+        m.add_view(P, D)
+    n_ref, d_ref = m.infer_converge(1e-6, max_iters=400)
+    assert d_ref < 1e-6
+    ref = m.beliefs()
+    target = torch.from_numpy(ref.reshape(-1)).cuda()
+    m.reset_state()
+    n, dist = m.infer_until(target.data_ptr(), 1e-3, max_iters=400)
+    assert 0 < n <= n_ref and dist <= 1e-3
+    got = m.beliefs()
+    assert np.abs(got - ref).max() <= 1e-3
+    m.reset_state()
+    m.infer(iters=n)
+    np.testing.assert_array_equal(m.beliefs(), got)
+    # a target out of reach: runs to the cap and reports the distance
+    far = torch.full_like(target, 0.5)
+    m.reset_state()
+    n2, d2 = m.infer_until(far.data_ptr(), 1e-3, max_iters=7)
+    assert n2 == 7 and d2 > 1e-3
+    with pytest.raises(L.MrfError):
+        m.infer_until(0, 1e-3)
+    m.close()
