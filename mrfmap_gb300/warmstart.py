@@ -211,14 +211,18 @@ def build_dataset(workloads, activation=L.ACT_FULL_RAY, bricks_per_scene: int = 
     return torch.cat(F), torch.cat(T), torch.cat(Wt)
 
 
-def evaluate(net, workloads, tol: float = 1e-3, max_iters: int = 300, sweeps: int = 0,
-             activation=L.ACT_FULL_RAY):
-    """Time to a converged map (largest belief change below tol): plain BP
-    from the prior against BP warm-started by the network and, as the
-    method without the network, by a prediction of the prior everywhere.
-    Times are device times of the whole procedure (features, network,
-    initial messages and BP iterations) with the incidence lists built
-    beforehand; each warm-started map is checked against the plain one."""
+def evaluate(net, workloads, accept_tol: float = 1e-3, ref_tol: float = 1e-5, ref_max_iters: int = 3000,
+             max_iters: int = 3000, sweeps: int = 0, activation=L.ACT_FULL_RAY):
+    """Time to the converged map, per scene.  The converged map is plain BP
+    from the prior run until its largest belief change is below ref_tol
+    (untimed).  Each method -- plain BP from the prior, BP warm-started by
+    the network, and BP warm-started by a prediction of the prior everywhere
+    (the method without the network) -- is then timed from its start until
+    its map is within accept_tol of the converged map (mrf_infer_until,
+    checked every iteration): the whole procedure (features, network,
+    initial messages, iterations) with the incidence lists built
+    beforehand.  One-time costs (the voxel CSR the warm start uses, the
+    network's workspace) are paid before the timed runs."""
     torch = _torch()
     rows = []
     for w in workloads:
@@ -226,39 +230,59 @@ def evaluate(net, workloads, tol: float = 1e-3, max_iters: int = 300, sweeps: in
         for P, D in zip(w.poses, w.depths):
             m.add_view(P, D)
         m.infer(iters=1)  # incidence lists
+        warm_start(m, net, sweeps)  # one-time costs, untimed
         m.reset_state()
+        n_ref, d_ref = m.infer_converge(ref_tol, max_iters=ref_max_iters)
+        Bref = m.beliefs()
+        ref_dev = torch.from_numpy(Bref.reshape(-1)).cuda()
+        rec = {"workload": w.name, "seed": w.seed, "ref_iters": n_ref, "ref_converged": d_ref < ref_tol}
         ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
-        torch.cuda.synchronize()
-        ev[0].record()
-        n_plain, _ = m.infer_converge(tol, max_iters=max_iters)
-        ev[1].record()
-        torch.cuda.synchronize()
-        t_plain = ev[0].elapsed_time(ev[1])
-        Bp = m.beliefs()
-        rec = {"workload": w.name, "seed": w.seed, "plain_iters": n_plain, "plain_ms": t_plain,
-               "plain_converged": n_plain < max_iters}
         lp = float(np.log(w.params.prior / (1 - w.params.prior)))
-        for label in ("learned", "prior"):
+        for label in ("plain", "learned", "prior"):
             m.reset_state()
             torch.cuda.synchronize()
             ev[0].record()
             if label == "learned":
                 warm_start(m, net, sweeps)
-            else:
+            elif label == "prior":
                 m.warm_start(np.full((m.num_bricks, 512), lp, np.float32), sweeps)
-            n, _ = m.infer_converge(tol, max_iters=max_iters, flags=L.INCREMENTAL)
+            n, dist = m.infer_until(ref_dev.data_ptr(), accept_tol, max_iters=max_iters,
+                                    flags=0 if label == "plain" else L.INCREMENTAL)
             ev[1].record()
             torch.cuda.synchronize()
-            Bw = m.beliefs()
-            touched = (Bp > 0) | (Bw > 0)
+            B = m.beliefs()
+            touched = (Bref > 0) | (B > 0)
             rec[label + "_iters"] = n
-            rec[label + "_converged"] = n < max_iters
             rec[label + "_ms"] = ev[0].elapsed_time(ev[1])
-            rec[label + "_max_err"] = float(np.abs(Bw - Bp).max())
-            rec[label + "_agree"] = float(((Bw > 0.5) == (Bp > 0.5))[touched].mean()) if touched.any() else 1.0
+            rec[label + "_reached"] = bool(dist <= accept_tol)
+            rec[label + "_max_err"] = float(np.abs(B - Bref).max())
+            rec[label + "_agree"] = float(((B > 0.5) == (Bref > 0.5))[touched].mean()) if touched.any() else 1.0
         rows.append(rec)
         m.close()
     return rows
+
+
+def summarize(rows, accept_tol: float = 1e-3, agree_min: float = 0.999):
+    """Speed-ups over the scenes whose converged map exists (the reference
+    run converged) and that every method reached (within accept_tol, class
+    agreement >= agree_min)."""
+    ok = [r for r in rows if r["ref_converged"] and all(
+        r[k + "_reached"] and r[k + "_max_err"] <= accept_tol and r[k + "_agree"] >= agree_min
+        for k in ("plain", "learned", "prior"))]
+    mean = lambda k: float(np.mean([r[k] for r in ok])) if ok else None
+    out = {"scenes": len(rows), "scenes_ref_converged": sum(r["ref_converged"] for r in rows),
+           "scenes_compared": len(ok)}
+    for k in ("plain", "learned", "prior"):
+        out[k + "_ms"] = mean(k + "_ms")
+        out[k + "_iters"] = mean(k + "_iters")
+    if ok:
+        out["speedup_learned_vs_plain"] = out["plain_ms"] / out["learned_ms"]
+        out["speedup_prior_vs_plain"] = out["plain_ms"] / out["prior_ms"]
+        out["speedup_learned_vs_prior"] = out["prior_ms"] / out["learned_ms"]
+        out["max_belief_err_vs_converged"] = {k: max(r[k + "_max_err"] for r in ok)
+                                             for k in ("plain", "learned", "prior")}
+        out["min_class_agreement"] = {k: min(r[k + "_agree"] for r in ok) for k in ("plain", "learned", "prior")}
+    return out
 
 
 def main(argv=None):

@@ -99,6 +99,8 @@ struct orc_map {
   double* lq;
   double* acc;
   int64_t scratch_vox;
+  double* pbuf; /* messages of one camera update (orc_update_camera) */
+  int64_t pbuf_cap;
 };
 
 static int g_threads = 1;
@@ -194,7 +196,7 @@ void orc_destroy(orc_map* m) {
   for (int i = 0; i < m->nviews; ++i) view_free(&m->views[i]);
   free(m->views); free(m->sigma_lut); free(m->bias_lut); free(m->brick_slot);
   free(m->brick_coord); free(m->L); free(m->belief);
-  free(m->q); free(m->lq); free(m->acc);
+  free(m->q); free(m->lq); free(m->acc); free(m->pbuf);
   free(m);
 }
 
@@ -828,6 +830,31 @@ void orc_infer(orc_map* m, const int* ids, int n_ids, int iters, int flags) {
     free(dL);
     free(hit);
   }
+}
+
+void orc_build_all(orc_map* m) {
+  /* views are independent: each build touches its own view only */
+#pragma omp parallel for schedule(dynamic, 1) num_threads(g_threads)
+  for (int c = 0; c < m->nviews; ++c) ensure_built(m, c);
+}
+
+int64_t orc_update_camera(orc_map* m, int c, int flags) {
+  if (c < 0 || c >= m->nviews) return -1;
+  ensure_built(m, c);
+  orc_view* v = &m->views[c];
+  if (v->ninc > m->pbuf_cap) {
+    free(m->pbuf);
+    m->pbuf = (double*)malloc((size_t)v->ninc * sizeof(double));
+    m->pbuf_cap = v->ninc;
+  }
+  /* the body of the Gauss-Seidel camera loop (src/GVDBInference.cpp:155-167) */
+  prepare_q(m, v);
+  ray_messages(m, v, (flags & ORC_FIX_PRE_RESET) != 0, m->pbuf);
+  accumulate(m, v, m->pbuf);
+  update_view(m, v, NULL);
+  int64_t n = 0;
+  for (int r = 0; r < v->nrays; ++r) n += v->meta[r * 5 + 1];
+  return n;
 }
 
 int64_t orc_last_updates(const orc_map* m) { return m->last_updates; }

@@ -111,6 +111,14 @@ void orc_render(const orc_map* m, int mode, const float* pose, const float* dept
 int64_t orc_insert_logodds(const orc_map* m, const float* pose, const float* depth, float l_hit,
                            float l_miss, float l_min, float l_max, double* L);
 
+/* builds the incidence lists of every view (views in parallel) */
+void orc_build_all(orc_map* m);
+/* one Gauss-Seidel camera update of camera c (the body of the reference's
+ * camera loop, src/GVDBInference.cpp:155-167) on the current state, its
+ * messages kept: the unit the CPU baseline is timed on.  Returns the Post
+ * incidences processed (-1 for a bad camera). */
+int64_t orc_update_camera(orc_map* m, int c, int flags);
+
 /* counters from the last orc_infer: incidence-iterations of Post passes */
 int64_t orc_last_updates(const orc_map* m);
 

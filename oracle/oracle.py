@@ -76,6 +76,9 @@ def lib():
         L.orc_likelihood.argtypes = [vp, fp, fp, fp]
         L.orc_likelihood.restype = C.c_double
         L.orc_render.argtypes = [vp, C.c_int, fp, fp, C.c_float, fp, C.POINTER(C.c_int64)]
+        L.orc_build_all.argtypes = [vp]
+        L.orc_update_camera.argtypes = [vp, C.c_int, C.c_int]
+        L.orc_update_camera.restype = C.c_int64
         L.orc_last_updates.argtypes = [vp]
         L.orc_last_updates.restype = C.c_int64
         L.orc_insert_logodds.argtypes = [vp, fp, fp, C.c_float, C.c_float, C.c_float, C.c_float,
@@ -147,6 +150,18 @@ class OracleMap:
         ids = np.arange(n, dtype=np.int32) if ids is None else np.asarray(ids, np.int32)
         iters = self.params.max_iters if iters is None else iters
         self._L.orc_infer(self._h, _ptr(ids, C.c_int), len(ids), iters, flags)
+
+    def build_all(self):
+        """Incidence lists of every view (views built in parallel)."""
+        self._L.orc_build_all(self._h)
+
+    def update_camera(self, view: int, flags: int = 0) -> int:
+        """One Gauss-Seidel camera update of ``view`` (messages kept);
+        returns the Post incidences it processed."""
+        n = self._L.orc_update_camera(self._h, view, flags)
+        if n < 0:
+            raise ValueError("bad view")
+        return n
 
     @property
     def last_updates(self) -> int:

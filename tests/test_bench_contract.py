@@ -33,6 +33,11 @@ def test_reference_arm_line():
     assert e["value"] == d["value"] and e["unit"] == d["unit"]
     assert e["h2d_bytes_per_step"] == 0 and e["d2h_bytes_per_step"] == 0
     assert d["config"]["workload"].startswith("small_room")
+    # the same config object as the GPU arm's line (same function, same args)
+    sys.path.insert(0, ROOT)
+    import bench
+    assert d["config"] == bench.workload_config(bench.workload("small"), "fullray", 1)
+    assert d["views_held"] == 5 and "camera update" in d["step"]
 
 
 def test_cpu_baselines_of_our_line():
@@ -44,7 +49,7 @@ def test_cpu_baselines_of_our_line():
     cpu, ins = bench.cpu_baselines(w, "fullray", 2)
     assert "error" not in ins, ins
     assert cpu["kind"] == "port" and cpu["unit"] == bench.UNIT and cpu["value"] > 0 and cpu["cores"] >= 1
-    assert "2 of 5 keyframes" in cpu["sample"]
+    assert "holding 5 of 5 keyframes" in cpu["sample"] and "sweep of 5 camera updates" in cpu["sample"]
     assert ins["unit"] == "voxel updates/s" and ins["value"] > 0 and ins["rays_per_s"] > 0
     assert "error" not in ins and ins["cores"] == 1
     json.dumps({"cpu_baseline": cpu, "cpu_insertion": ins})

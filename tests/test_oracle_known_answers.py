@@ -374,3 +374,25 @@ def test_logodds_insertion_known_answer(oracle_lib):
     n_all, L_all = m.insert_logodds(P, D)
     assert n_all >= 1 and np.isfinite(L_all).all()
     assert (L_all > 0).any() and (L_all < 0).any()
+
+
+def test_camera_updates_are_one_gauss_seidel_iteration(oracle_lib, small_room):
+    """orc_update_camera over every camera in order (the CPU baseline's unit)
+    is one Gauss-Seidel iteration of orc_infer, bit for bit."""
+    from oracle import oracle as O
+    w = small_room
+    a = O.OracleMap(w.params, threads=2)
+    b = O.OracleMap(w.params, threads=2)
+    for P, D in zip(w.poses, w.depths):
+        a.add_view(P, D, O.ACT_FULL_RAY)
+        b.add_view(P, D, O.ACT_FULL_RAY)
+    b.build_all()
+    for it in range(2):
+        a.infer(iters=1, flags=O.INCREMENTAL)
+        n = sum(b.update_camera(c) for c in range(len(w.poses)))
+        assert n == a.last_updates
+    np.testing.assert_array_equal(a.beliefs(), b.beliefs())
+    with pytest.raises(ValueError):
+        b.update_camera(len(w.poses))
+    a.close()
+    b.close()
