@@ -6,11 +6,20 @@
 #include <vector>
 
 #include "GVDBParams.h"
+#include "MatrixArgs.h"
 
 class GVDBImage {
  public:
   GVDBImage(const float* depth_rowmajor, int rows, int cols);
   GVDBImage(const float* depth_rowmajor, int rows, int cols, const gvdb_params_t& params);
+  // the reference's GVDBImage(const Eigen::MatrixXf&[, params]): any matrix
+  // type with rows(), cols() and m(i, j)
+  template <class M, class = mrf_shim::if_matrix<M>>
+  GVDBImage(const M& depth)
+      : GVDBImage(mrf_shim::rowmajor(depth).data(), (int)depth.rows(), (int)depth.cols()) {}
+  template <class M, class = mrf_shim::if_matrix<M>>
+  GVDBImage(const M& depth, const gvdb_params_t& params)
+      : GVDBImage(mrf_shim::rowmajor(depth).data(), (int)depth.rows(), (int)depth.cols(), params) {}
   const std::vector<float>& depth() const { return depth_; }
   int rows() const { return rows_; }
   int cols() const { return cols_; }

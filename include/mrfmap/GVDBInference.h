@@ -8,6 +8,7 @@
 #include "GVDBImage.h"
 #include "GVDBMRFMap.h"
 #include "GVDBParams.h"
+#include "MatrixArgs.h"
 
 class GVDBInference {
  public:
@@ -48,6 +49,67 @@ class GVDBInference {
   // extensions: BP schedule / message flags of mrf_infer, and counters
   int infer_flags = 0;
   mrf_stats stats() const;
+
+  // The reference's signatures with Eigen arguments (GVDBInference.h:87-102
+  // there): any matrix type with rows(), cols() and m(i, j) -- column-major
+  // Eigen::MatrixXf poses and images in, Eigen::Ref<MRow> images out.
+  // Output images have the camera's rows x cols (std::runtime_error else).
+  template <class P, class = mrf_shim::if_matrix<P>>
+  void add_camera(const P& pose, const std::shared_ptr<GVDBImage>& img) {
+    add_camera(mrf_shim::pose16(pose).data(), img);
+  }
+  template <class P, class D, class = mrf_shim::if_matrix<P>, class = mrf_shim::if_matrix<D>>
+  void add_camera_with_depth(const P& pose, const D& depth) {
+    const std::vector<float> d = mrf_shim::rowmajor(depth);
+    add_camera_with_depth(mrf_shim::pose16(pose).data(), d.data(), (int)depth.rows(), (int)depth.cols());
+  }
+  template <class P, class = mrf_shim::if_matrix<P>>
+  void set_pose(unsigned id, const P& pose) {
+    set_pose(id, mrf_shim::pose16(pose).data());
+  }
+  template <class O, class = mrf_shim::if_out_matrix<mrf_shim::plain<O>>>
+  float get_likelihood_image(unsigned id, O&& out) {
+    std::vector<float> b = mrf_shim::image_scratch(out, gvdb_params_.rows, gvdb_params_.cols);
+    const float s = get_likelihood_image(id, b.data());
+    mrf_shim::assign(out, b.data());
+    return s;
+  }
+  template <class P, class O, class = mrf_shim::if_matrix<P>, class = mrf_shim::if_out_matrix<mrf_shim::plain<O>>>
+  float get_likelihood_image_at_pose(const P& pose, const std::shared_ptr<GVDBImage>& img, O&& out) {
+    std::vector<float> b = mrf_shim::image_scratch(out, gvdb_params_.rows, gvdb_params_.cols);
+    const float s = get_likelihood_image_at_pose(mrf_shim::pose16(pose).data(), img, b.data());
+    mrf_shim::assign(out, b.data());
+    return s;
+  }
+  template <class O, class = mrf_shim::if_out_matrix<mrf_shim::plain<O>>>
+  void get_expected_depth_image(unsigned id, O&& out) {
+    std::vector<float> b = mrf_shim::image_scratch(out, gvdb_params_.rows, gvdb_params_.cols);
+    get_expected_depth_image(id, b.data());
+    mrf_shim::assign(out, b.data());
+  }
+  template <class P, class O, class = mrf_shim::if_matrix<P>, class = mrf_shim::if_out_matrix<mrf_shim::plain<O>>>
+  float get_accuracy_image_at_pose(const P& pose, const std::shared_ptr<GVDBImage>& img, O&& out) {
+    std::vector<float> b = mrf_shim::image_scratch(out, gvdb_params_.rows, gvdb_params_.cols);
+    const float s = get_accuracy_image_at_pose(mrf_shim::pose16(pose).data(), img, b.data());
+    mrf_shim::assign(out, b.data());
+    return s;
+  }
+  template <class O, class = mrf_shim::if_out_matrix<mrf_shim::plain<O>>>
+  void get_alphas(O&& out) {
+    map_->get_alphas(out);
+  }
+  template <class O, class = mrf_shim::if_out_matrix<mrf_shim::plain<O>>>
+  void get_diagnostic_image(unsigned id, O&& out, unsigned mode = 0) {
+    std::vector<float> b = mrf_shim::image_scratch(out, gvdb_params_.rows, gvdb_params_.cols);
+    get_diagnostic_image(id, b.data(), mode);
+    mrf_shim::assign(out, b.data());
+  }
+  template <class P, class O, class = mrf_shim::if_matrix<P>, class = mrf_shim::if_out_matrix<mrf_shim::plain<O>>>
+  void get_diagnostic_image_at_pose(const P& pose, const std::shared_ptr<GVDBImage>& img, O&& out) {
+    std::vector<float> b = mrf_shim::image_scratch(out, gvdb_params_.rows, gvdb_params_.cols);
+    get_diagnostic_image_at_pose(mrf_shim::pose16(pose).data(), img, b.data());
+    mrf_shim::assign(out, b.data());
+  }
 
  private:
   size_t n_cams_ = 0;

@@ -7,6 +7,7 @@
 
 #include "../mrfmap_gb300.h"
 #include "GVDBParams.h"
+#include "MatrixArgs.h"
 
 class GVDBMRFMap {
  public:
@@ -24,6 +25,20 @@ class GVDBMRFMap {
   void get_alphas(float* out, int64_t rows, int64_t cols) const;
   // [n_bricks x 16] int bitmask of belief >= threshold (GVDBMRFMap.cpp:210-263)
   void get_occupied_voxels_mask(int* out, int64_t rows, int64_t cols, float threshold) const;
+  // the same with the reference's Eigen::Ref arguments (any writable matrix
+  // type with rows(), cols() and m(i, j))
+  template <class O, class = mrf_shim::if_out_matrix<mrf_shim::plain<O>>>
+  void get_alphas(O&& out) const {
+    std::vector<float> b((size_t)((int64_t)out.rows() * (int64_t)out.cols()));
+    get_alphas(b.data(), (int64_t)out.rows(), (int64_t)out.cols());
+    mrf_shim::assign(out, b.data());
+  }
+  template <class O, class = mrf_shim::if_out_matrix<mrf_shim::plain<O>>>
+  void get_occupied_voxels_mask(O&& out, float threshold) const {
+    std::vector<int> b((size_t)((int64_t)out.rows() * (int64_t)out.cols()));
+    get_occupied_voxels_mask(b.data(), (int64_t)out.rows(), (int64_t)out.cols(), threshold);
+    mrf_shim::assign(out, b.data());
+  }
 
  private:
   mrf_map* map_ = nullptr;

@@ -7,6 +7,7 @@
 #include "GVDBImage.h"
 #include "GVDBMRFMap.h"
 #include "GVDBParams.h"
+#include "MatrixArgs.h"
 
 class GVDBMapLikelihoodEstimator {
  public:
@@ -46,6 +47,108 @@ class GVDBMapLikelihoodEstimator {
   void get_diagnostic_image_at_pose(const float* pose, const std::shared_ptr<GVDBImage>& img,
                                     float* out_rowmajor);
   void set_acc_thresh(float t) { params_.acc_thresh = t; }
+
+  // The reference's signatures with Eigen arguments
+  // (GVDBMapLikelihoodEstimator.h:97-117 there): any matrix type with
+  // rows(), cols() and m(i, j).  load_map takes points n x 3 (voxel units)
+  // and occupancies n x 1; output images have the camera's rows x cols.
+  template <class P, class = mrf_shim::if_matrix<P>>
+  void add_camera(const P& pose, const std::shared_ptr<GVDBImage>& img) {
+    add_camera(mrf_shim::pose16(pose).data(), img);
+  }
+  template <class P, class = mrf_shim::if_matrix<P>>
+  void set_pose(unsigned id, const P& pose) {
+    set_pose(id, mrf_shim::pose16(pose).data());
+  }
+  template <class C, class V, class = mrf_shim::if_matrix<C>, class = mrf_shim::if_matrix<V>>
+  bool load_map(const C& coords, const V& occupancies) {
+    if (coords.cols() != 3 || (int64_t)occupancies.rows() * occupancies.cols() != (int64_t)coords.rows())
+      throw std::runtime_error("load_map wants n x 3 points and n occupancies");
+    const std::vector<float> c = mrf_shim::rowmajor(coords), o = mrf_shim::rowmajor(occupancies);
+    return load_map(c.data(), o.data(), (int64_t)coords.rows());
+  }
+  template <class O, class = mrf_shim::if_out_matrix<mrf_shim::plain<O>>>
+  float get_likelihood_image(unsigned id, O&& out) {
+    std::vector<float> b = mrf_shim::image_scratch(out, params_.rows, params_.cols);
+    const float s = get_likelihood_image(id, b.data());
+    mrf_shim::assign(out, b.data());
+    return s;
+  }
+  template <class P, class O, class = mrf_shim::if_matrix<P>, class = mrf_shim::if_out_matrix<mrf_shim::plain<O>>>
+  float get_likelihood_image_at_pose(const P& pose, const std::shared_ptr<GVDBImage>& img, O&& out) {
+    std::vector<float> b = mrf_shim::image_scratch(out, params_.rows, params_.cols);
+    const float s = get_likelihood_image_at_pose(mrf_shim::pose16(pose).data(), img, b.data());
+    mrf_shim::assign(out, b.data());
+    return s;
+  }
+  template <class P, class D, class O, class = mrf_shim::if_matrix<P>, class = mrf_shim::if_matrix<D>,
+            class = mrf_shim::if_out_matrix<mrf_shim::plain<O>>>
+  float get_likelihood_image_at_pose_with_depth(const P& pose, const D& depth, O&& out) {
+    std::vector<float> b = mrf_shim::image_scratch(out, params_.rows, params_.cols);
+    const std::vector<float> d = mrf_shim::rowmajor(depth);
+    const float s = get_likelihood_image_at_pose_with_depth(mrf_shim::pose16(pose).data(), d.data(), b.data());
+    mrf_shim::assign(out, b.data());
+    return s;
+  }
+  template <class O, class = mrf_shim::if_out_matrix<mrf_shim::plain<O>>>
+  void get_accuracy_image(unsigned id, O&& out) {
+    std::vector<float> b = mrf_shim::image_scratch(out, params_.rows, params_.cols);
+    get_accuracy_image(id, b.data());
+    mrf_shim::assign(out, b.data());
+  }
+  template <class P, class O, class = mrf_shim::if_matrix<P>, class = mrf_shim::if_out_matrix<mrf_shim::plain<O>>>
+  float get_accuracy_image_at_pose(const P& pose, const std::shared_ptr<GVDBImage>& img, O&& out) {
+    std::vector<float> b = mrf_shim::image_scratch(out, params_.rows, params_.cols);
+    const float s = get_accuracy_image_at_pose(mrf_shim::pose16(pose).data(), img, b.data());
+    mrf_shim::assign(out, b.data());
+    return s;
+  }
+  template <class P, class D, class O, class = mrf_shim::if_matrix<P>, class = mrf_shim::if_matrix<D>,
+            class = mrf_shim::if_out_matrix<mrf_shim::plain<O>>>
+  float get_accuracy_image_at_pose_with_depth(const P& pose, const D& depth, O&& out) {
+    std::vector<float> b = mrf_shim::image_scratch(out, params_.rows, params_.cols);
+    const std::vector<float> d = mrf_shim::rowmajor(depth);
+    const float s = get_accuracy_image_at_pose_with_depth(mrf_shim::pose16(pose).data(), d.data(), b.data());
+    mrf_shim::assign(out, b.data());
+    return s;
+  }
+  template <class P, class = mrf_shim::if_matrix<P>>
+  float get_simple_accuracy_at_pose(const P& pose, const std::shared_ptr<GVDBImage>& img) {
+    return get_simple_accuracy_at_pose(mrf_shim::pose16(pose).data(), img);
+  }
+  template <class P, class D, class O, class = mrf_shim::if_matrix<P>, class = mrf_shim::if_matrix<D>,
+            class = mrf_shim::if_out_matrix<mrf_shim::plain<O>>>
+  float get_simple_accuracy_image_at_pose_with_depth(const P& pose, const D& depth, O&& out) {
+    std::vector<float> b = mrf_shim::image_scratch(out, params_.rows, params_.cols);
+    const std::vector<float> d = mrf_shim::rowmajor(depth);
+    const float s =
+        get_simple_accuracy_image_at_pose_with_depth(mrf_shim::pose16(pose).data(), d.data(), b.data());
+    mrf_shim::assign(out, b.data());
+    return s;
+  }
+  template <class P, class O, class = mrf_shim::if_matrix<P>, class = mrf_shim::if_out_matrix<mrf_shim::plain<O>>>
+  void get_occ_thresh_image_at_pose(const P& pose, const std::shared_ptr<GVDBImage>& img, O&& out,
+                                    float occ_thresh) {
+    std::vector<float> b = mrf_shim::image_scratch(out, params_.rows, params_.cols);
+    get_occ_thresh_image_at_pose(mrf_shim::pose16(pose).data(), img, b.data(), occ_thresh);
+    mrf_shim::assign(out, b.data());
+  }
+  template <class O, class = mrf_shim::if_out_matrix<mrf_shim::plain<O>>>
+  void get_alphas(O&& out) {
+    map_->get_alphas(out);
+  }
+  template <class O, class = mrf_shim::if_out_matrix<mrf_shim::plain<O>>>
+  void get_diagnostic_image(unsigned id, O&& out) {
+    std::vector<float> b = mrf_shim::image_scratch(out, params_.rows, params_.cols);
+    get_diagnostic_image(id, b.data());
+    mrf_shim::assign(out, b.data());
+  }
+  template <class P, class O, class = mrf_shim::if_matrix<P>, class = mrf_shim::if_out_matrix<mrf_shim::plain<O>>>
+  void get_diagnostic_image_at_pose(const P& pose, const std::shared_ptr<GVDBImage>& img, O&& out) {
+    std::vector<float> b = mrf_shim::image_scratch(out, params_.rows, params_.cols);
+    get_diagnostic_image_at_pose(mrf_shim::pose16(pose).data(), img, b.data());
+    mrf_shim::assign(out, b.data());
+  }
 
  private:
   std::vector<std::vector<float>> poses_;

@@ -102,7 +102,7 @@ def build_pymodule(force: bool = False) -> str:
     srcs = [os.path.join(CSRC, "shim", f) for f in ("GVDBShim.cpp", "GVDBPyModules.cpp", "KeyframeSelector.cpp")]
     hdrs = [os.path.join(ROOT, "include", "mrfmap", h) for h in
             ("GVDBParams.h", "GVDBImage.h", "GVDBInference.h", "GVDBMapLikelihoodEstimator.h",
-             "GVDBMRFMap.h")]
+             "GVDBMRFMap.h", "MatrixArgs.h")]
     out = pymodule_path()
     if not force and not _stale(out, srcs + hdrs + [lib]):
         return out

@@ -87,7 +87,10 @@ def test_device_error_flag_fails_the_next_build(native_lib):
     with pytest.raises(L.MrfError) as e:
         m.infer()
     assert e.value.status == DEVICE
-    m.infer()                              # flag cleared: the build runs
+    # flag cleared: the build runs (from the prior, as the fresh map below;
+    # mrf_infer alone would keep the log-odds of the two iterations above)
+    m.reset_state()
+    m.infer()
     ref = _map(w, range(5))
     ref.infer()
     np.testing.assert_array_equal(m.beliefs(), ref.beliefs())
