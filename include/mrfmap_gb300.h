@@ -142,6 +142,15 @@ MRF_API mrf_status mrf_view_camera(mrf_map* map, int view_id, int* rows, int* co
  * activates bricks for its new pose. */
 MRF_API mrf_status mrf_set_pose(mrf_map* map, int view_id, const float* pose);
 
+/* Takes a view out of the set BP iterates (no reference counterpart: the
+ * bounded keyframe window of a long incremental run, whose early keyframes'
+ * incidence lists would not fit in memory).  The view's current messages
+ * stay in the total log-odds for good; its incidence lists, pairs and depth
+ * image are dropped at the next build.  Its id stays reserved: mrf_infer
+ * passes over it and the per-view calls (likelihood, renders, messages,
+ * incidences, set_pose) fail with MRF_ERR_STATE.  mrf_reset_state forgets
+ * retired views' messages with everything else. */
+MRF_API mrf_status mrf_retire_view(mrf_map* map, int view_id);
 /* GVDBInference::perform_inference_ids (src/GVDBInference.cpp:100-178):
  * zeroes the messages of the cameras in ids (unless MRF_INCREMENTAL) and
  * runs iters BP iterations over every camera. ids == NULL -> all cameras. */

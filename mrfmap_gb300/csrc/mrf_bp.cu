@@ -537,8 +537,7 @@ constexpr uint32_t kOpenStart = 1u, kOpenEnd = 2u, kSingle = 4u;
 // Lo already loaded (the gate c > kCumLenGate already checked)
 __device__ __forceinline__ void apply_run_loaded(const uint4 r, float mo, float Lo, float acc_dyn,
                                                  float* __restrict__ m, float* __restrict__ L,
-                                                 float* __restrict__ belief, float* __restrict__ dm,
-                                                 int jacobi) {
+                                                 float* __restrict__ dm, int jacobi) {
   const uint32_t p = r.x, v = r.y;
   const float c = __uint_as_float(r.z);
   float a = clampf((__uint_as_float(r.w) + acc_dyn) / c, kFEps, 1.0f - kFEps);
@@ -548,16 +547,15 @@ __device__ __forceinline__ void apply_run_loaded(const uint4 r, float mo, float 
     dm[p] = mn - mo;
     return;
   }
-  float Lv = Lo + (mn - mo);
-  L[v] = Lv;
-  belief[v] = 1.0f - clampf(1.0f / (1.0f + expf(Lv)), kFEps, 1.0f - kFEps);
+  L[v] = Lo + (mn - mo);
 }
 
-// factor->voxel update of one pair (gvdbkernels.cu:457-479)
+// factor->voxel update of one pair (gvdbkernels.cu:457-479).  The belief
+// 1 - clamp(1 / (1 + e^L)) is not written here: k_belief_refresh derives it
+// from L once the iterations of a call are done.
 __device__ __forceinline__ void apply_pair(uint32_t p, float acc, const uint32_t* __restrict__ pair_vox,
                                            float* __restrict__ m, const float* __restrict__ cum,
-                                           float* __restrict__ L, float* __restrict__ belief,
-                                           float* __restrict__ dm, int jacobi) {
+                                           float* __restrict__ L, float* __restrict__ dm, int jacobi) {
   const float c = cum[p];
   const float mo = m[p];
   const uint32_t v = pair_vox[p];
@@ -569,21 +567,18 @@ __device__ __forceinline__ void apply_pair(uint32_t p, float acc, const uint32_t
     dm[p] = mn - mo;
     return;
   }
-  float Lv = L[v] + (mn - mo);
-  L[v] = Lv;
-  belief[v] = 1.0f - clampf(1.0f / (1.0f + expf(Lv)), kFEps, 1.0f - kFEps);
+  L[v] = L[v] + (mn - mo);
 }
 
 // the same for a dynamic run, whose pair id, voxel, cumulative length and
 // static-message sum are stored together (one 16-byte load; the voxel's L
 // gather does not wait on a pair-id lookup)
 __device__ __forceinline__ void apply_run(const uint4 r, float acc_dyn, float* __restrict__ m,
-                                          float* __restrict__ L, float* __restrict__ belief,
-                                          float* __restrict__ dm, int jacobi) {
+                                          float* __restrict__ L, float* __restrict__ dm, int jacobi) {
   const uint32_t p = r.x, v = r.y;
   const float c = __uint_as_float(r.z);
   if (!(c > kCumLenGate)) return;  // gvdbkernels.cu:408: the pair never updates
-  apply_run_loaded(r, m[p], jacobi ? 0.0f : L[v], acc_dyn, m, L, belief, dm, jacobi);
+  apply_run_loaded(r, m[p], jacobi ? 0.0f : L[v], acc_dyn, m, L, dm, jacobi);
 }
 
 __global__ void __launch_bounds__(kTileThreads, 8)
@@ -591,7 +586,7 @@ __global__ void __launch_bounds__(kTileThreads, 8)
                   const uint32_t* __restrict__ seg, const uint32_t* __restrict__ tile_first,
                   uint32_t k0, uint32_t k1, uint32_t p_end, TileCarry* __restrict__ carry,
                   const uint4* __restrict__ drun, float* __restrict__ m, float* __restrict__ L,
-                  float* __restrict__ belief, float* __restrict__ dm, int jacobi) {
+                  float* __restrict__ dm, int jacobi) {
   __shared__ float sv[kTile];
   __shared__ uint32_t sseg[kTile + 2];
   const int t = threadIdx.x;
@@ -628,9 +623,9 @@ __global__ void __launch_bounds__(kTileThreads, 8)
     const bool open_start = s0 < base, open_end = s1 > end;
     if (!open_start && !open_end) {
       if (q == t) {
-        if (gate0) apply_run_loaded(r0, mo0, Lo0, acc, m, L, belief, dm, jacobi);
+        if (gate0) apply_run_loaded(r0, mo0, Lo0, acc, m, L, dm, jacobi);
       } else {
-        apply_run(drun[pf + q], acc, m, L, belief, dm, jacobi);
+        apply_run(drun[pf + q], acc, m, L, dm, jacobi);
       }
       continue;
     }
@@ -683,8 +678,7 @@ __global__ void k_tile_first(const uint32_t* __restrict__ seg, uint32_t p0, uint
 // forward adding each following tile's partial, in tile order
 __global__ void k_pair_fixup(const TileCarry* __restrict__ carry, uint32_t ntiles,
                              const uint4* __restrict__ drun, float* __restrict__ m,
-                             float* __restrict__ L, float* __restrict__ belief, float* __restrict__ dm,
-                             int jacobi) {
+                             float* __restrict__ L, float* __restrict__ dm, int jacobi) {
   uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= ntiles) return;
   TileCarry c = carry[t];
@@ -698,7 +692,7 @@ __global__ void k_pair_fixup(const TileCarry* __restrict__ carry, uint32_t ntile
     if ((d.flags & kSingle) && (d.flags & kOpenEnd)) continue;
     break;
   }
-  apply_run(drun[key], sum, m, L, belief, dm, jacobi);
+  apply_run(drun[key], sum, m, L, dm, jacobi);
 }
 
 // per dynamic run: {pair id, voxel, cumulative length, static-message sum}
@@ -717,19 +711,17 @@ __global__ void k_drun(const uint32_t* __restrict__ dpair, uint32_t n, const uin
 __global__ void k_static_pairs(uint32_t p0, uint32_t p1, const uint32_t* __restrict__ ndyn,
                                const float* __restrict__ stat, const uint32_t* __restrict__ pair_vox,
                                float* __restrict__ m, const float* __restrict__ cum,
-                               float* __restrict__ L, float* __restrict__ belief,
-                               float* __restrict__ dm, int jacobi) {
+                               float* __restrict__ L, float* __restrict__ dm, int jacobi) {
   uint32_t p = p0 + blockIdx.x * blockDim.x + threadIdx.x;
   if (p >= p1 || ndyn[p]) return;
-  apply_pair(p, stat[p], pair_vox, m, cum, L, belief, dm, jacobi);
+  apply_pair(p, stat[p], pair_vox, m, cum, L, dm, jacobi);
 }
 
 // Jacobi: total log-odds of each voxel moves by the sum of its cameras'
 // message changes (pairs of a voxel grouped by a voxel-sorted CSR)
 __global__ void k_voxel_apply(const uint32_t* __restrict__ vseg, const uint32_t* __restrict__ vpairs,
                               const uint32_t* __restrict__ vvox, uint32_t nvox,
-                              const float* __restrict__ dm, float* __restrict__ L,
-                              float* __restrict__ belief) {
+                              const float* __restrict__ dm, float* __restrict__ L) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nvox) return;
   float s = 0.0f;
@@ -743,9 +735,17 @@ __global__ void k_voxel_apply(const uint32_t* __restrict__ vseg, const uint32_t*
   }
   if (!any) return;
   uint32_t v = vvox[i];
-  float Lv = L[v] + s;
-  L[v] = Lv;
-  belief[v] = 1.0f - clampf(1.0f / (1.0f + expf(Lv)), kFEps, 1.0f - kFEps);
+  L[v] = L[v] + s;
+}
+
+// beliefs of the voxels the iterations update (those with a pair past the
+// length gate in some camera), from their total log-odds: the per-voxel
+// belief of gvdbkernels.cu:474-477, written once per call instead of at
+// every message update
+__global__ void k_belief_refresh(const float* __restrict__ L, const uint8_t* __restrict__ active, int64_t n,
+                                 float* __restrict__ belief) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    if (active[i]) belief[i] = 1.0f - clampf(1.0f / (1.0f + expf(L[i])), kFEps, 1.0f - kFEps);
 }
 
 __global__ void k_max_abs_diff(const float* __restrict__ a, const float* __restrict__ b, int64_t n,
@@ -790,9 +790,9 @@ __global__ void k_voxel_rebuild(const uint32_t* __restrict__ vseg, const uint32_
 // gate keep 0 (they never update).
 __global__ void k_warm_split(const uint32_t* __restrict__ vseg, const uint32_t* __restrict__ vpairs,
                              const uint32_t* __restrict__ vvox, uint32_t nvox,
-                             const float* __restrict__ L_pred, float lp, const float* __restrict__ cum,
-                             const float* __restrict__ stat, const uint32_t* __restrict__ ndyn,
-                             float* __restrict__ m) {
+                             const float* __restrict__ L_pred, float lp, const float* __restrict__ base,
+                             const float* __restrict__ cum, const float* __restrict__ stat,
+                             const uint32_t* __restrict__ ndyn, float* __restrict__ m) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nvox) return;
   float fixed = 0.0f, dyn_len = 0.0f;
@@ -807,7 +807,7 @@ __global__ void k_warm_split(const uint32_t* __restrict__ vseg, const uint32_t* 
       fixed += logf(a) - logf(1.0f - a);
     }
   }
-  const float rest = L_pred[vvox[i]] - lp - fixed;
+  const float rest = L_pred[vvox[i]] - (base ? base[vvox[i]] : lp) - fixed;
   for (uint32_t k = vseg[i]; k < vseg[i + 1]; ++k) {
     const uint32_t p = vpairs[k];
     const float c = cum[p];
@@ -869,6 +869,14 @@ __global__ void k_remove_messages(const uint32_t* __restrict__ pair_vox, float* 
   m[p] = 0.0f;
 }
 
+// a retired camera's messages added to the base log-odds (one pair per
+// voxel within a camera: no two threads share a voxel)
+__global__ void k_fold_messages(const uint32_t* __restrict__ pv, const float* __restrict__ m, uint32_t n,
+                                float* __restrict__ base) {
+  uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < n && m[p] != 0.0f) base[pv[p]] += m[p];
+}
+
 __global__ void k_remap_scatter(const uint32_t* __restrict__ pv, const float* __restrict__ m,
                                 uint32_t n, float* __restrict__ dense) {
   uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
@@ -920,7 +928,7 @@ __global__ void k_touch_pairs(const uint32_t* __restrict__ pair_vox, const float
   const bool act = p < np && cum[p] > kCumLenGate;
   if (act) flag[pair_vox[p]] = 1;
   const unsigned b = __ballot_sync(kFull, act);
-  if ((threadIdx.x & 31) == 0 && b) atomicAdd(n_active, (unsigned long long)__popc(b));
+  if (n_active && (threadIdx.x & 31) == 0 && b) atomicAdd(n_active, (unsigned long long)__popc(b));
 }
 
 __global__ void k_count_flags(const uint8_t* __restrict__ flag, int64_t n, unsigned long long* __restrict__ out) {
@@ -1023,12 +1031,11 @@ cudaError_t launch_pair_update(const BpArrays& a, uint32_t k0, uint32_t k1, uint
   if (k1 <= k0) return cudaSuccess;
   uint32_t ntiles = (k1 - k0 + kTile - 1) / kTile;
   k_pair_reduce<<<ntiles, kTileThreads, 0, s>>>(a.dperm, a.inc_pl, a.dseg, tile_first, k0, k1, j1,
-                                                carry, a.drun, a.pair_m, a.L, a.belief, a.pair_dm,
-                                                jacobi);
+                                                carry, a.drun, a.pair_m, a.L, a.pair_dm, jacobi);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  k_pair_fixup<<<blocks(ntiles, 256), 256, 0, s>>>(carry, ntiles, a.drun, a.pair_m, a.L, a.belief,
-                                                   a.pair_dm, jacobi);
+  k_pair_fixup<<<blocks(ntiles, 256), 256, 0, s>>>(carry, ntiles, a.drun, a.pair_m, a.L, a.pair_dm,
+                                                   jacobi);
   return cudaGetLastError();
 }
 
@@ -1043,8 +1050,7 @@ cudaError_t launch_static_pairs(const BpArrays& a, uint32_t p0, uint32_t p1, int
                                 cudaStream_t s) {
   if (p1 <= p0) return cudaSuccess;
   k_static_pairs<<<blocks(p1 - p0, 256), 256, 0, s>>>(p0, p1, a.pair_ndyn, a.pair_stat, a.pair_vox,
-                                                      a.pair_m, a.pair_cum, a.L, a.belief, a.pair_dm,
-                                                      jacobi);
+                                                      a.pair_m, a.pair_cum, a.L, a.pair_dm, jacobi);
   return cudaGetLastError();
 }
 
@@ -1059,10 +1065,25 @@ cudaError_t launch_tile_first(const uint32_t* seg, uint32_t p0, uint32_t p1, uin
 uint32_t pair_update_tiles(uint32_t n) { return (n + kTile - 1) / kTile; }
 
 cudaError_t launch_voxel_apply(const uint32_t* vseg, const uint32_t* vpairs, const uint32_t* vvox,
-                               uint32_t nvox, const float* pair_dm, float* L, float* belief,
-                               cudaStream_t s) {
+                               uint32_t nvox, const float* pair_dm, float* L, cudaStream_t s) {
   if (!nvox) return cudaSuccess;
-  k_voxel_apply<<<blocks(nvox, 256), 256, 0, s>>>(vseg, vpairs, vvox, nvox, pair_dm, L, belief);
+  k_voxel_apply<<<blocks(nvox, 256), 256, 0, s>>>(vseg, vpairs, vvox, nvox, pair_dm, L);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_active_voxels(const uint32_t* pair_vox, const float* cum, uint32_t np, uint8_t* flag,
+                                 int64_t nvox, cudaStream_t s) {
+  if (nvox <= 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(flag, 0, (size_t)nvox, s);
+  if (e != cudaSuccess) return e;
+  if (np) k_touch_pairs<<<blocks(np, 256), 256, 0, s>>>(pair_vox, cum, np, flag, nullptr);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_belief_refresh(const float* L, const uint8_t* active, int64_t nvox, float* belief,
+                                  cudaStream_t s) {
+  if (nvox <= 0) return cudaSuccess;
+  k_belief_refresh<<<(unsigned)std::min<int64_t>(blocks(nvox, 256), 8192), 256, 0, s>>>(L, active, nvox, belief);
   return cudaGetLastError();
 }
 
@@ -1076,10 +1097,10 @@ cudaError_t launch_max_abs_diff(const float* a, const float* b, int64_t n, uint3
 }
 
 cudaError_t launch_warm_split(const uint32_t* vseg, const uint32_t* vpairs, const uint32_t* vvox,
-                              uint32_t nvox, const float* L_pred, float lp, const float* cum,
+                              uint32_t nvox, const float* L_pred, float lp, const float* base, const float* cum,
                               const float* stat, const uint32_t* ndyn, float* m, cudaStream_t s) {
   if (!nvox) return cudaSuccess;
-  k_warm_split<<<blocks(nvox, 256), 256, 0, s>>>(vseg, vpairs, vvox, nvox, L_pred, lp, cum, stat, ndyn, m);
+  k_warm_split<<<blocks(nvox, 256), 256, 0, s>>>(vseg, vpairs, vvox, nvox, L_pred, lp, base, cum, stat, ndyn, m);
   return cudaGetLastError();
 }
 
@@ -1103,6 +1124,13 @@ cudaError_t launch_voxel_rebuild(const uint32_t* vseg, const uint32_t* vpairs, c
 cudaError_t launch_remove_messages(const BpArrays& a, uint32_t p0, uint32_t p1, cudaStream_t s) {
   if (p1 <= p0) return cudaSuccess;
   k_remove_messages<<<blocks(p1 - p0, 256), 256, 0, s>>>(a.pair_vox, a.pair_m, p0, p1, a.L, a.belief);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_fold_messages(const uint32_t* pair_vox, const float* pair_m, uint32_t n, float* base,
+                                 cudaStream_t s) {
+  if (!n) return cudaSuccess;
+  k_fold_messages<<<blocks(n, 256), 256, 0, s>>>(pair_vox, pair_m, n, base);
   return cudaGetLastError();
 }
 

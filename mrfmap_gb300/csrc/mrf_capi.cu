@@ -155,7 +155,11 @@ struct View {
   uint32_t left_base = 0, n_left = 0;     // leftover queue of the SM-affine schedule
   uint32_t n_loud = 0;                    // pairs on voxels with a dynamic incidence (numbered first)
   uint32_t tile_base = 0;                 // first pair of each pair-update tile
+  bool retired = false;                   // out of the window: no lists, no pairs, no depth
 };
+
+// pixels a view contributes to the per-pixel arrays (none once retired)
+int64_t view_pixels(const View& v) { return v.retired ? 0 : (int64_t)v.cam.rows * v.cam.cols; }
 
 uint32_t u32_checked(int64_t v, const char* what) {
   if (v < 0 || v > (int64_t)0xFFFFFFF0ll) fail(MRF_ERR_CAPACITY, std::string(what) + " exceeds 32-bit range");
@@ -188,6 +192,12 @@ struct mrf_map {
       tile_first;
   uint32_t jac_tile_base = 0;
   int64_t n_inc = 0, n_pairs = 0, n_dperm = 0, n_dpairs = 0;
+  // voxels with a pair past the length gate (their beliefs follow L)
+  DBuf vox_active;
+  // logit(prior) + the messages of retired views, per voxel (kept once a view
+  // has been retired; the prior alone before that)
+  DBuf d_Lbase;
+  bool has_base = false;
   // jacobi voxel CSR
   DBuf vseg, vpairs, vvox;
   uint32_t n_vvox = 0;
@@ -276,6 +286,11 @@ void commit_new_bricks(mrf_map* m) {
   float lp = logf(m->prm.prior) - logf(1.0f - m->prm.prior);
   CK(launch_fill_new_voxels(m->d_L.as<float>(), m->d_belief.as<float>(), m->n_bricks * kBrickVox,
                             nb_new * kBrickVox, lp, m->stream));
+  if (m->has_base) {
+    m->d_Lbase.reserve((size_t)nb_new * kBrickVox * 4, true, m->stream);
+    CK(launch_fill_f32(m->d_Lbase.as<float>() + m->n_bricks * kBrickVox, add * (int64_t)kBrickVox, lp,
+                       m->stream));
+  }
   m->h_coord.resize((size_t)nb_new * 3);
   CK(cudaMemcpyAsync(m->h_coord.data() + m->n_bricks * 3, m->d_coord.as<int>() + m->n_bricks * 3,
                      (size_t)add * 12, cudaMemcpyDeviceToHost, m->stream));
@@ -351,7 +366,7 @@ void rebuild_lists(mrf_map* m, OldPairs& old) {
   for (View& v : m->views) {
     v.pix_base = npix;
     v.cam.brick_slot = m->g.brick_slot;
-    npix += (int64_t)v.cam.rows * v.cam.cols;
+    npix += view_pixels(v);
   }
   CK(cudaEventRecord(m->ev0, m->stream));
   const bool remap = old.remap;
@@ -363,8 +378,9 @@ void rebuild_lists(mrf_map* m, OldPairs& old) {
   m->s_counts.reserve((size_t)npix * 4 + 4, false, m->stream);
   m->s_offs.reserve((size_t)npix * 4 + 4, false, m->stream);
   for (int c = 0; c < V; ++c)
-    CK(launch_trace_count(m->views[c].cam, m->views[c].pose, m->views[c].depth.as<float>(),
-                          m->s_counts.as<uint32_t>() + m->views[c].pix_base, m->s_err.as<int>(), m->stream));
+    if (!m->views[c].retired)
+      CK(launch_trace_count(m->views[c].cam, m->views[c].pose, m->views[c].depth.as<float>(),
+                            m->s_counts.as<uint32_t>() + m->views[c].pix_base, m->s_err.as<int>(), m->stream));
   // sentinel 0 at the end so the scan yields the total
   CK(cudaMemsetAsync(m->s_counts.as<uint32_t>() + npix, 0, 4, m->stream));
   size_t tb = scan_temp_bytes((uint32_t)(npix + 1));
@@ -394,6 +410,7 @@ void rebuild_lists(mrf_map* m, OldPairs& old) {
     View& v = m->views[c];
     v.inc_base = bounds[c];
     v.n_inc = bounds[c + 1] - bounds[c];
+    if (v.retired) continue;
     CK(launch_trace_emit(v.cam, v.pose, v.depth.as<float>(), m->s_offs.as<uint32_t>() + v.pix_base, 0,
                          m->meta.as<RayMeta>() + v.pix_base, m->s_vox.as<uint32_t>(),
                          m->inc_len.as<float>(), m->inc_mu.as<float>(), m->s_rec.as<float2>(),
@@ -410,7 +427,7 @@ void rebuild_lists(mrf_map* m, OldPairs& old) {
     check_device_err(m);
     for (int c = 0; c < V; ++c) {
       const View& vc = m->views[c];
-      for (int64_t i = 0; i < (int64_t)vc.cam.rows * vc.cam.cols; ++i) {
+      for (int64_t i = 0; i < view_pixels(vc); ++i) {
         const RayMeta& r = hm[(size_t)(vc.pix_base + i)];
         nreal[c] += r.n_pre;
         nrays += r.n_pre > 0;
@@ -577,7 +594,7 @@ void rebuild_lists(mrf_map* m, OldPairs& old) {
   // ray queues: per view, the active rays longest first
   {
     int64_t hw_max = 0;
-    for (const View& v : m->views) hw_max = std::max<int64_t>(hw_max, (int64_t)v.cam.rows * v.cam.cols);
+    for (const View& v : m->views) hw_max = std::max<int64_t>(hw_max, view_pixels(v));
     m->ray_order.reserve((size_t)std::max<int64_t>(npix, 1) * 4, false, m->stream);
     m->ray_queue.reserve((size_t)std::max<int64_t>(npix, 1) * sizeof(RayMeta), false, m->stream);
     m->s_k0.reserve((size_t)hw_max * 4 + 4, false, m->stream);
@@ -586,11 +603,12 @@ void rebuild_lists(mrf_map* m, OldPairs& old) {
     int64_t base = 0;
     for (int c = 0; c < V; ++c) {
       View& v = m->views[c];
-      const int64_t hw = (int64_t)v.cam.rows * v.cam.cols;
+      const int64_t hw = view_pixels(v);
       int64_t act = 0;
       for (int64_t i = 0; i < hw; ++i) act += ray_in_bp(hm[(size_t)(v.pix_base + i)]);
       v.order_base = (uint32_t)base;
       v.n_active = (uint32_t)act;
+      if (hw == 0) continue;
       CK(launch_ray_keys(m->meta.as<RayMeta>() + v.pix_base, (uint32_t)hw, m->s_k0.as<uint32_t>(),
                          m->s_v0.as<uint32_t>(), m->stream));
       size_t t = sort_temp_bytes((uint32_t)hw, 17);
@@ -624,7 +642,7 @@ void rebuild_lists(mrf_map* m, OldPairs& old) {
     auto build_view = [&](int c) {
       const View& v = m->views[c];
       RegionLists& out = lists[(size_t)c];
-      const int64_t hw = (int64_t)v.cam.rows * v.cam.cols;
+      const int64_t hw = view_pixels(v);
       const RayMeta* vm = hm.data() + v.pix_base;
       std::vector<uint32_t> lcount(65536, 0u), reg((size_t)hw, 0u), bucket_off((size_t)R + 1, 0u);
       int64_t work = 0;
@@ -786,6 +804,12 @@ void rebuild_lists(mrf_map* m, OldPairs& old) {
     old_vox.release();
     old_m.release();
     old.remap = false;  // the new pairs hold the messages from here on
+  }
+  {
+    const int64_t nv = m->n_bricks * kBrickVox;
+    m->vox_active.reserve((size_t)std::max<int64_t>(nv, 1), false, m->stream);
+    CK(launch_active_voxels(m->pair_vox.as<uint32_t>(), m->pair_cum.as<float>(), (uint32_t)pair_total,
+                            m->vox_active.as<uint8_t>(), nv, m->stream));
   }
   CK(cudaEventRecord(m->ev1, m->stream));
   sync(m);
@@ -977,8 +1001,7 @@ void enqueue_iteration(mrf_map* m, const BpArrays& a, bool jacobi, int fix, int 
     prof.end();
     prof.begin(3);
     CK(launch_voxel_apply(m->vseg.as<uint32_t>(), m->vpairs.as<uint32_t>(), m->vvox.as<uint32_t>(),
-                          m->n_vvox, m->pair_dm.as<float>(), m->d_L.as<float>(),
-                          m->d_belief.as<float>(), m->stream));
+                          m->n_vvox, m->pair_dm.as<float>(), m->d_L.as<float>(), m->stream));
     prof.end();
     launches += 5 + (first ? 1 : 0);
   }
@@ -1019,6 +1042,12 @@ cudaGraphExec_t iteration_graph(mrf_map* m, const BpArrays& a, bool jacobi, int 
   slot.launches = launches;
   launches_per_iter = launches;
   return exec;
+}
+
+// beliefs of the voxels the iterations update, from their total log-odds
+void refresh_beliefs(mrf_map* m) {
+  CK(launch_belief_refresh(m->d_L.as<float>(), m->vox_active.as<uint8_t>(), m->n_bricks * kBrickVox,
+                           m->d_belief.as<float>(), m->stream));
 }
 
 // tol > 0: stop after the first iteration whose largest belief change is
@@ -1065,9 +1094,11 @@ void run_infer(mrf_map* m, const int* ids, int n_ids, int iters, int flags, floa
       for (int ph = 0; ph < 3 && ph < iters; ++ph) exec[ph] = iteration_graph(m, a, jacobi, fix, ph, per[ph]);
     for (int it = 0; it < iters; ++it) {
       const bool check = conv && ((it + 1) % check_every == 0 || it + 1 == iters);
-      if (check && !target)
+      if (check && !target) {
+        refresh_beliefs(m);
         CK(cudaMemcpyAsync(m->s_prev.p, m->d_belief.p, (size_t)nvox * 4, cudaMemcpyDeviceToDevice,
                            m->stream));
+      }
       const int ph = std::min(it, 2);
       if (direct) {
         enqueue_iteration(m, a, jacobi, fix, ph, prof, launches);
@@ -1077,6 +1108,7 @@ void run_infer(mrf_map* m, const int* ids, int n_ids, int iters, int flags, floa
       }
       done = it + 1;
       if (check) {
+        refresh_beliefs(m);
         CK(launch_max_abs_diff(m->d_belief.as<float>(), target ? target : m->s_prev.as<float>(), nvox,
                                m->s_delta.as<uint32_t>(), m->stream));
         ++launches;
@@ -1087,6 +1119,11 @@ void run_infer(mrf_map* m, const int* ids, int n_ids, int iters, int flags, floa
         if (target ? delta <= tol : delta < tol) break;
       }
     }
+  }
+  // the iteration kernels update L only; the beliefs follow once per call
+  if (done > 0) {
+    refresh_beliefs(m);
+    ++launches;
   }
   CK(cudaEventRecord(m->ev1, m->stream));
   m->has_messages = true;
@@ -1163,7 +1200,7 @@ void destroy_bufs(mrf_map* m) {
                  &m->pair_dm,
                  &m->pair_seg, &m->dperm, &m->dpair, &m->dseg, &m->drun,
                  &m->carry, &m->ray_order, &m->ray_queue, &m->region_q, &m->rstart, &m->rcounters, &m->counters, &m->tile_first,
-                 &m->vseg, &m->vpairs, &m->vvox, &m->s_rec, &m->s_recs, &m->s_pf, &m->s_ps,
+                 &m->vseg, &m->vpairs, &m->vvox, &m->vox_active, &m->d_Lbase, &m->s_rec, &m->s_recs, &m->s_pf, &m->s_ps,
                  &m->s_flags, &m->s_ind, &m->s_scan,
                  &m->s_q0, &m->s_q1, &m->s_q2, &m->s_q3, &m->s_bf, &m->s_loud, &m->s_pv, &m->s_sg,
                  &m->s_tmp, &m->s_counts, &m->s_offs, &m->s_vox, &m->s_k0, &m->s_k1, &m->s_v0,
@@ -1417,6 +1454,10 @@ mrf_status mrf_set_pose(mrf_map* m, int view_id, const float* pose) {
     set_err("invalid view id or pose");
     return MRF_ERR_INVALID;
   }
+  if (m->views[view_id].retired) {
+    set_err("view retired (mrf_retire_view)");
+    return MRF_ERR_STATE;
+  }
   return wrap([&] {
     // take the camera's messages out of the total log-odds before it moves
     // (src/GVDBInference.cpp:66-82 removes its ray contributions first)
@@ -1427,6 +1468,34 @@ mrf_status mrf_set_pose(mrf_map* m, int view_id, const float* pose) {
     activate_view(m, m->views[view_id]);
     m->version++;
     m->stats.n_bricks = m->n_bricks;
+  });
+}
+
+mrf_status mrf_retire_view(mrf_map* m, int view_id) {
+  if (guard(m) != MRF_OK) return MRF_ERR_INVALID;
+  if (view_id < 0 || view_id >= (int)m->views.size()) {
+    set_err("invalid view id");
+    return MRF_ERR_INVALID;
+  }
+  View& v = m->views[view_id];
+  if (v.retired) return MRF_OK;
+  return wrap([&] {
+    const int64_t nvox = m->n_bricks * kBrickVox;
+    if (!m->has_base && nvox) {
+      const float lp = logf(m->prm.prior) - logf(1.0f - m->prm.prior);
+      m->d_Lbase.reserve((size_t)nvox * 4, false, m->stream);
+      CK(launch_fill_f32(m->d_Lbase.as<float>(), nvox, lp, m->stream));
+      m->has_base = true;
+    }
+    // its messages stay in L; the base keeps them for the calls that rebuild
+    // L from the prior and the live views' messages
+    if (m->has_messages && v.n_pairs)
+      CK(launch_fold_messages(m->pair_vox.as<uint32_t>() + v.pair_base, m->pair_m.as<float>() + v.pair_base,
+                              v.n_pairs, m->d_Lbase.as<float>(), m->stream));
+    sync(m);
+    v.depth.release();
+    v.retired = true;
+    m->version++;  // the next build leaves its lists and pairs out
   });
 }
 
@@ -1466,6 +1535,18 @@ mrf_status mrf_infer_until(mrf_map* m, const int* ids, int n_ids, int max_iters,
   });
 }
 
+// The total log-odds without the live views' messages: the prior, plus the
+// messages of retired views once there are any (their beliefs, which only
+// those messages set, stay as they are).  Live views' messages are added
+// back by k_voxel_rebuild.
+static void start_logodds(mrf_map* m, float lp) {
+  const int64_t nvox = m->n_bricks * kBrickVox;
+  if (m->has_base)
+    CK(cudaMemcpyAsync(m->d_L.p, m->d_Lbase.p, (size_t)nvox * 4, cudaMemcpyDeviceToDevice, m->stream));
+  else
+    CK(launch_fill_new_voxels(m->d_L.as<float>(), m->d_belief.as<float>(), 0, nvox, lp, m->stream));
+}
+
 // Warm start.  The messages start from a split of the predicted field
 // L_pred: pairs without dynamic incidences get their exact (constant)
 // message, the dynamic pairs of a voxel share the rest of
@@ -1485,8 +1566,9 @@ static void warm_start_impl(mrf_map* m, const float* L_pred, bool device_ptr, in
   CK(cudaMemcpyAsync(m->d_L.p, L_pred, (size_t)nvox * 4,
                      device_ptr ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, m->stream));
   CK(launch_warm_split(m->vseg.as<uint32_t>(), m->vpairs.as<uint32_t>(), m->vvox.as<uint32_t>(), m->n_vvox,
-                       m->d_L.as<float>(), lp, m->pair_cum.as<float>(), m->pair_stat.as<float>(),
-                       m->pair_ndyn.as<uint32_t>(), m->pair_m.as<float>(), m->stream));
+                       m->d_L.as<float>(), lp, m->has_base ? m->d_Lbase.as<float>() : nullptr,
+                       m->pair_cum.as<float>(), m->pair_stat.as<float>(), m->pair_ndyn.as<uint32_t>(),
+                       m->pair_m.as<float>(), m->stream));
   BpArrays a = m->bp();
   const int V = (int)m->views.size();
   const uint32_t P = (uint32_t)m->n_pairs;
@@ -1498,7 +1580,7 @@ static void warm_start_impl(mrf_map* m, const float* L_pred, bool device_ptr, in
                           m->tile_first.as<uint32_t>() + m->jac_tile_base, m->carry.as<TileCarry>(),
                           1, m->stream));
   }
-  CK(launch_fill_new_voxels(m->d_L.as<float>(), m->d_belief.as<float>(), 0, nvox, lp, m->stream));
+  start_logodds(m, lp);
   CK(launch_voxel_rebuild(m->vseg.as<uint32_t>(), m->vpairs.as<uint32_t>(), m->vvox.as<uint32_t>(),
                           m->n_vvox, m->pair_m.as<float>(), m->pair_cum.as<float>(),
                           m->d_L.as<float>(), m->d_belief.as<float>(), m->stream));
@@ -1514,6 +1596,10 @@ mrf_status mrf_read_messages(mrf_map* m, int view_id, float* out_dense) {
   if (view_id < 0 || view_id >= (int)m->views.size() || !out_dense) {
     set_err("invalid view id or null argument");
     return MRF_ERR_INVALID;
+  }
+  if (m->views[view_id].retired) {
+    set_err("view retired (mrf_retire_view)");
+    return MRF_ERR_STATE;
   }
   return wrap([&] {
     ensure_built(m);
@@ -1534,6 +1620,10 @@ mrf_status mrf_write_messages(mrf_map* m, int view_id, const float* dense) {
   if (view_id < 0 || view_id >= (int)m->views.size() || !dense) {
     set_err("invalid view id or null argument");
     return MRF_ERR_INVALID;
+  }
+  if (m->views[view_id].retired) {
+    set_err("view retired (mrf_retire_view)");
+    return MRF_ERR_STATE;
   }
   return wrap([&] {
     ensure_built(m);
@@ -1557,7 +1647,7 @@ mrf_status mrf_rebuild_logodds(mrf_map* m) {
     const int64_t nvox = m->n_bricks * kBrickVox;
     if (nvox == 0) return;
     const float lp = logf(m->prm.prior) - logf(1.0f - m->prm.prior);
-    CK(launch_fill_new_voxels(m->d_L.as<float>(), m->d_belief.as<float>(), 0, nvox, lp, m->stream));
+    start_logodds(m, lp);
     CK(launch_voxel_rebuild(m->vseg.as<uint32_t>(), m->vpairs.as<uint32_t>(), m->vvox.as<uint32_t>(),
                             m->n_vvox, m->pair_m.as<float>(), m->pair_cum.as<float>(),
                             m->d_L.as<float>(), m->d_belief.as<float>(), m->stream));
@@ -1677,6 +1767,7 @@ mrf_status mrf_reset_state(mrf_map* m) {
     float lp = logf(m->prm.prior) - logf(1.0f - m->prm.prior);
     CK(launch_fill_new_voxels(m->d_L.as<float>(), m->d_belief.as<float>(), 0,
                               m->n_bricks * kBrickVox, lp, m->stream));
+    if (m->has_base) CK(launch_fill_f32(m->d_Lbase.as<float>(), m->n_bricks * kBrickVox, lp, m->stream));
     if (m->n_pairs) CK(launch_fill_f32(m->pair_m.as<float>(), m->n_pairs, 0.0f, m->stream));
   });
 }
@@ -1742,6 +1833,10 @@ mrf_status mrf_likelihood_view(mrf_map* m, int view_id, float* out_img, float* o
   if (view_id < 0 || view_id >= (int)m->views.size()) {
     set_err("invalid view id");
     return MRF_ERR_INVALID;
+  }
+  if (m->views[view_id].retired) {
+    set_err("view retired (mrf_retire_view)");
+    return MRF_ERR_STATE;
   }
   const View& v = m->views[view_id];
   return likelihood_host(m, v.pose, v.depth.as<float>(), out_img, out_sum, &v.cam);
@@ -1818,6 +1913,10 @@ mrf_status mrf_render_view(mrf_map* m, int mode, int view_id, float threshold, f
   if (view_id < 0 || view_id >= (int)m->views.size()) {
     set_err("invalid view id");
     return MRF_ERR_INVALID;
+  }
+  if (m->views[view_id].retired) {
+    set_err("view retired (mrf_retire_view)");
+    return MRF_ERR_STATE;
   }
   const View& v = m->views[view_id];
   return render_impl(m, mode, v.pose, v.depth.as<float>(), threshold, out_img, out_score, counts, &v.cam);
@@ -1968,6 +2067,10 @@ mrf_status mrf_view_incidences(mrf_map* m, int view_id, int* meta, uint32_t* vox
   if (view_id < 0 || view_id >= (int)m->views.size() || cap < 0) {
     set_err("invalid view id");
     return MRF_ERR_INVALID;
+  }
+  if (m->views[view_id].retired) {
+    set_err("view retired (mrf_retire_view)");
+    return MRF_ERR_STATE;
   }
   return wrap([&] {
     ensure_built(m);

@@ -129,8 +129,10 @@ cudaError_t launch_pair_stats(const uint32_t* seg, uint32_t p0, uint32_t np, uin
                               const float2* srec, float* cum, float* stat, uint32_t* ndyn, float* hit,
                               uint32_t* long_list, cudaStream_t s);
 // warm-start initial messages from a predicted log-odds field (voxel CSR)
+// (base: per-voxel log-odds without the live views' messages, or NULL for
+// the prior lp everywhere)
 cudaError_t launch_warm_split(const uint32_t* vseg, const uint32_t* vpairs, const uint32_t* vvox,
-                              uint32_t nvox, const float* L_pred, float lp, const float* cum,
+                              uint32_t nvox, const float* L_pred, float lp, const float* base, const float* cum,
                               const float* stat, const uint32_t* ndyn, float* m, cudaStream_t s);
 // warm-start features per voxel [nvox_slots][4] from the voxel CSR
 cudaError_t launch_voxel_features(const uint32_t* vseg, const uint32_t* vpairs, const uint32_t* vvox,
@@ -234,10 +236,19 @@ cudaError_t launch_static_pairs(const BpArrays& a, uint32_t p0, uint32_t p1, int
 cudaError_t launch_tile_first(const uint32_t* seg, uint32_t p0, uint32_t p1, uint32_t k0, uint32_t k1,
                               uint32_t* out, cudaStream_t s);
 cudaError_t launch_voxel_apply(const uint32_t* vseg, const uint32_t* vpairs, const uint32_t* vvox,
-                               uint32_t nvox, const float* pair_dm, float* L, float* belief,
-                               cudaStream_t s);
+                               uint32_t nvox, const float* pair_dm, float* L, cudaStream_t s);
+// flag[v] = 1 for the voxels with a pair past the length gate (the voxels
+// whose belief the iterations define), 0 elsewhere
+cudaError_t launch_active_voxels(const uint32_t* pair_vox, const float* cum, uint32_t np, uint8_t* flag,
+                                 int64_t nvox, cudaStream_t s);
+// belief[v] from L[v] where active[v]
+cudaError_t launch_belief_refresh(const float* L, const uint8_t* active, int64_t nvox, float* belief,
+                                  cudaStream_t s);
 cudaError_t launch_voxel_rebuild(const uint32_t* vseg, const uint32_t* vpairs, const uint32_t* vvox,
                                  uint32_t nvox, const float* m, const float* cum, float* L, float* belief,
+                                 cudaStream_t s);
+// base[pair_vox[p]] += pair_m[p] over one camera's pairs
+cudaError_t launch_fold_messages(const uint32_t* pair_vox, const float* pair_m, uint32_t n, float* base,
                                  cudaStream_t s);
 cudaError_t launch_remove_messages(const BpArrays& a, uint32_t p0, uint32_t p1, cudaStream_t s);
 cudaError_t launch_remap_scatter(const uint32_t* pair_vox, const float* pair_m, uint32_t n,

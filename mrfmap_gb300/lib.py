@@ -41,7 +41,7 @@ EXPORTS = ["mrf_create", "mrf_destroy", "mrf_release_cached_memory", "mrf_last_e
            "mrf_device_beliefs",
            "mrf_stats_get", "mrf_get_stream", "mrf_synchronize", "mrf_render", "mrf_render_view", "mrf_pixel_diagnostics", "mrf_add_view_camera",
            "mrf_view_camera", "mrf_set_memory_limit", "mrf_memory_in_use", "mrf_test_raise_device_error",
-           "mrf_infer_until"]
+           "mrf_infer_until", "mrf_retire_view"]
 
 RENDER_EXPECTED_DEPTH = 0
 RENDER_ACCURACY = 1
@@ -140,6 +140,7 @@ def load(path: str | None = None):
                                  ip], C.c_int),
         "mrf_view_camera": ([vp, C.c_int, ip, ip, fp], C.c_int),
         "mrf_set_memory_limit": ([C.c_int64], C.c_int),
+        "mrf_retire_view": ([vp, C.c_int], C.c_int),
         "mrf_infer_until": ([vp, ip, C.c_int, C.c_int, C.c_void_p, C.c_float, C.c_int, C.c_int, ip, fp],
                             C.c_int),
         "mrf_memory_in_use": ([], C.c_int64),
@@ -246,6 +247,10 @@ class MRFMap:
 
     def set_pose(self, view: int, pose):
         _check(self._L.mrf_set_pose(self._h, view, _fp(_f32(pose))))
+
+    def retire_view(self, view: int):
+        """Out of the iterated window; its messages stay in the log-odds."""
+        _check(self._L.mrf_retire_view(self._h, view))
 
     def infer(self, ids=None, iters: int = 0, flags: int = 0):
         if ids is None:

@@ -210,3 +210,108 @@ def mixed_room(seed: int = 2, n_frames: int = 12,
         cams.append((f, f, cols / 2, rows / 2))
     return Workload(f"mixed_room_{n_frames}x{len(sizes)}res_{int(round(res * 100))}cm", base.params, poses,
                     depths, seed, cams)
+
+
+# ---- the streamed large-map workload ---------------------------------------
+
+@dataclass
+class Walk:
+    """A camera walking through a room of boxes: the scene, the params and the
+    per-frame poses; depth frames are rendered on demand (render_frame /
+    render_frames_torch), since thousands of full-resolution frames do not
+    fit in host memory at once."""
+    name: str
+    params: MapParams
+    scene: Scene
+    poses: list
+    seed: int
+    max_range: float = 5.0
+
+
+def walk_room(seed: int = 5, n_frames: int = 2000, rows: int = 480, cols: int = 640, res: float = 0.02,
+              dims=(20.0, 20.0, 4.0), n_boxes: int = 150, step: float = 0.05) -> Walk:
+    """Seeded random walk through a dims-sized room holding n_boxes boxes on
+    the floor (footprints 0.2-1.5 m, heights 0.2-1.2 m): the camera moves
+    `step` metres per frame at 1.4-1.6 m height (above every box), its
+    heading turning by N(0, 0.15 rad) per frame and reflecting off a band
+    0.8 m inside the walls, looking 15 degrees down.  640x480 frames,
+    fx = fy = 525, principal point at the centre, max range 5 m, 2 cm voxels,
+    5 iterations per frame."""
+    rng = np.random.default_rng(seed)
+    f = 525.0 * cols / 640
+    p = MapParams(res=res, dims=tuple(dims), rows=rows, cols=cols, fx=f, fy=f, cx=cols / 2, cy=rows / 2,
+                  prior=0.1, max_iters=5)
+    sensor_params(p)
+    hx, hy, hz = dims[0] / 2, dims[1] / 2, dims[2]
+    eps = res / 2
+    room = np.array([-hx + eps, -hy + eps, eps, hx - eps, hy - eps, hz - eps])
+    boxes = []
+    while len(boxes) < n_boxes:
+        fx_, fy_ = rng.uniform(0.2, 1.5, 2)
+        h = rng.uniform(0.2, 1.2)
+        cx_, cy_ = rng.uniform(-hx + 1.0, hx - 1.0), rng.uniform(-hy + 1.0, hy - 1.0)
+        boxes.append([cx_ - fx_ / 2, cy_ - fy_ / 2, 0.0, cx_ + fx_ / 2, cy_ + fy_ / 2, h])
+    scene = Scene(room=room, boxes=np.array(boxes))
+    pos = np.array([rng.uniform(-hx / 2, hx / 2), rng.uniform(-hy / 2, hy / 2)])
+    head = rng.uniform(0, 2 * np.pi)
+    band = 0.8
+    poses = []
+    for k in range(n_frames):
+        head += rng.normal(0.0, 0.15)
+        nxt = pos + step * np.array([np.cos(head), np.sin(head)])
+        if abs(nxt[0]) > hx - band:
+            head = np.pi - head
+        if abs(nxt[1]) > hy - band:
+            head = -head
+        pos = pos + step * np.array([np.cos(head), np.sin(head)])
+        z = 1.5 + 0.1 * np.sin(0.01 * k)
+        eye = np.array([pos[0], pos[1], z])
+        target = eye + np.array([np.cos(head), np.sin(head), -np.tan(np.deg2rad(15.0))])
+        poses.append(look_at(eye, target))
+    return Walk(f"walk_room_{n_frames}x{cols}x{rows}_{int(round(res * 100))}cm", p, scene, poses, seed)
+
+
+def render_frame(walk: Walk, k: int) -> np.ndarray:
+    """Frame k of the walk on the host (numpy; seeded per frame)."""
+    rng = np.random.default_rng((walk.seed, k))
+    return add_noise(render_depth(walk.scene, walk.params, walk.poses[k]), rng, max_range=walk.max_range)
+
+
+def render_frames_torch(walk: Walk, frames, device="cuda"):
+    """Frames of the walk rendered with torch on `device` (the same scene,
+    camera and noise model as render_frame, a torch generator seeded per
+    frame): a list of (rows, cols) float32 tensors."""
+    import torch
+    p = walk.params
+    H, W = p.rows, p.cols
+    xs = (torch.arange(W, device=device, dtype=torch.float64) + 0.5 - p.cx) / p.fx
+    ys = (torch.arange(H, device=device, dtype=torch.float64) + 0.5 - p.cy) / p.fy
+    rc = torch.stack(torch.broadcast_tensors(xs[None, :], ys[:, None], torch.ones(H, W, device=device,
+                                                                                   dtype=torch.float64)), -1)
+    room = torch.tensor(walk.scene.room, device=device, dtype=torch.float64)
+    boxes = torch.tensor(walk.scene.boxes, device=device, dtype=torch.float64)
+    out = []
+    for k in frames:
+        P = torch.tensor(walk.poses[k], device=device, dtype=torch.float64)
+        d = (rc @ P[:3, :3].T).reshape(-1, 3)
+        o = P[:3, 3]
+        inv = 1.0 / d
+        lo = (room[:3] - o) * inv
+        hi = (room[3:] - o) * inv
+        t = torch.maximum(lo, hi).min(dim=1).values  # room seen from inside: its exit
+        bl = (boxes[None, :, :3] - o) * inv[:, None, :]
+        bh = (boxes[None, :, 3:] - o) * inv[:, None, :]
+        tn = torch.minimum(bl, bh).max(dim=2).values
+        tf = torch.maximum(bl, bh).min(dim=2).values
+        hit = (tn <= tf) & (tn > 0)
+        tb = torch.where(hit, tn, torch.full_like(tn, float("inf"))).min(dim=1).values
+        t = torch.minimum(t, tb).reshape(H, W)
+        g = torch.Generator(device=device)
+        g.manual_seed(int(walk.seed) * 100003 + int(k))
+        sig = 0.002 + 0.0012 * t * t
+        z = t + torch.randn(t.shape, generator=g, device=device, dtype=torch.float64) * sig
+        z = z.float()
+        z[torch.rand(t.shape, generator=g, device=device) < 0.02] = 0.0
+        z[z > walk.max_range] = 0.0
+        out.append(z.contiguous())
+    return out

@@ -211,7 +211,7 @@ def build_dataset(workloads, activation=L.ACT_FULL_RAY, bricks_per_scene: int = 
     return torch.cat(F), torch.cat(T), torch.cat(Wt)
 
 
-def evaluate(net, workloads, accept_tol: float = 1e-3, ref_tol: float = 1e-5, ref_max_iters: int = 3000,
+def evaluate(net, workloads, accept_tol: float = 1e-3, ref_tol: float = 1e-4, ref_max_iters: int = 3000,
              max_iters: int = 3000, sweeps: int = 0, activation=L.ACT_FULL_RAY):
     """Time to the converged map, per scene.  The converged map is plain BP
     from the prior run until its largest belief change is below ref_tol

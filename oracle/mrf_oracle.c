@@ -58,6 +58,7 @@ typedef struct {
   float* depth;
   int policy;
   int built_version;
+  int retired; /* out of the iterated window (orc_retire_view) */
   /* incidence lists (pixel-major, then along the ray) */
   int nrays;
   int* ray_pix;
@@ -649,7 +650,7 @@ static void build_view(orc_map* m, int c) {
 }
 
 static void ensure_built(orc_map* m, int c) {
-  if (m->views[c].built_version != m->version) build_view(m, c);
+  if (!m->views[c].retired && m->views[c].built_version != m->version) build_view(m, c);
 }
 
 int64_t orc_view_num_incidences(orc_map* m, int view) {
@@ -772,13 +773,14 @@ void orc_infer(orc_map* m, const int* ids, int n_ids, int iters, int flags) {
       int c = ids[k];
       if (c < 0 || c >= m->nviews) continue;
       orc_view* v = &m->views[c];
+      if (v->retired) continue;
       for (int64_t i = 0; i < v->nvox_alloc; ++i) v->m[i] = 0.0;
     }
   }
   int64_t maxinc = 1;
   for (int c = 0; c < m->nviews; ++c) {
     ensure_built(m, c);
-    if (m->views[c].ninc > maxinc) maxinc = m->views[c].ninc;
+    if (!m->views[c].retired && m->views[c].ninc > maxinc) maxinc = m->views[c].ninc;
   }
   int fix = (flags & ORC_FIX_PRE_RESET) != 0;
   int64_t nv = (int64_t)m->nbricks * BVOX;
@@ -789,6 +791,7 @@ void orc_infer(orc_map* m, const int* ids, int n_ids, int iters, int flags) {
     for (int it = 0; it < iters; ++it) {
       for (int c = 0; c < m->nviews; ++c) {
         orc_view* v = &m->views[c];
+        if (v->retired) continue;
         prepare_q(m, v);
         ray_messages(m, v, fix, p);
         accumulate(m, v, p);
@@ -805,11 +808,13 @@ void orc_infer(orc_map* m, const int* ids, int n_ids, int iters, int flags) {
       ps[c] = (double*)malloc((size_t)(m->views[c].ninc ? m->views[c].ninc : 1) * sizeof(double));
     for (int it = 0; it < iters; ++it) {
       for (int c = 0; c < m->nviews; ++c) {
+        if (m->views[c].retired) continue;
         prepare_q(m, &m->views[c]);
         ray_messages(m, &m->views[c], fix, ps[c]);
       }
       for (int c = 0; c < m->nviews; ++c) {
         orc_view* v = &m->views[c];
+        if (v->retired) continue;
         accumulate(m, v, ps[c]);
         update_view(m, v, dL);
         for (int64_t k = 0; k < v->ntouch; ++k)
@@ -830,6 +835,13 @@ void orc_infer(orc_map* m, const int* ids, int n_ids, int iters, int flags) {
     free(dL);
     free(hit);
   }
+}
+
+void orc_retire_view(orc_map* m, int c) {
+  if (c < 0 || c >= m->nviews) return;
+  /* its messages stay in L (L is only ever moved by message changes); the
+   * view is no longer traced or iterated */
+  m->views[c].retired = 1;
 }
 
 void orc_build_all(orc_map* m) {

@@ -111,6 +111,9 @@ void orc_render(const orc_map* m, int mode, const float* pose, const float* dept
 int64_t orc_insert_logodds(const orc_map* m, const float* pose, const float* depth, float l_hit,
                            float l_miss, float l_min, float l_max, double* L);
 
+/* takes a view out of the iterated set (a bounded keyframe window): its
+ * messages stay in the log-odds, it is no longer traced or iterated */
+void orc_retire_view(orc_map* m, int view);
 /* builds the incidence lists of every view (views in parallel) */
 void orc_build_all(orc_map* m);
 /* one Gauss-Seidel camera update of camera c (the body of the reference's

@@ -77,6 +77,7 @@ def lib():
         L.orc_likelihood.restype = C.c_double
         L.orc_render.argtypes = [vp, C.c_int, fp, fp, C.c_float, fp, C.POINTER(C.c_int64)]
         L.orc_build_all.argtypes = [vp]
+        L.orc_retire_view.argtypes = [vp, C.c_int]
         L.orc_update_camera.argtypes = [vp, C.c_int, C.c_int]
         L.orc_update_camera.restype = C.c_int64
         L.orc_last_updates.argtypes = [vp]
@@ -150,6 +151,10 @@ class OracleMap:
         ids = np.arange(n, dtype=np.int32) if ids is None else np.asarray(ids, np.int32)
         iters = self.params.max_iters if iters is None else iters
         self._L.orc_infer(self._h, _ptr(ids, C.c_int), len(ids), iters, flags)
+
+    def retire_view(self, view: int):
+        """Out of the iterated window; its messages stay in the log-odds."""
+        self._L.orc_retire_view(self._h, view)
 
     def build_all(self):
         """Incidence lists of every view (views built in parallel)."""

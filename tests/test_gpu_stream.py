@@ -1,0 +1,86 @@
+"""The bounded keyframe window of a long incremental run (the large-map
+workload's mode, scaled down): frames of a seeded random walk stream in, each
+is added, the view that leaves the window is retired (mrf_retire_view: its
+messages stay in the log-odds, its lists and pairs are dropped) and
+MRF_INCREMENTAL iterations run over the live window.  The loop of the
+reference's viewer (src/Viewer.cpp:44-61: add_camera, then
+perform_inference, for every keyframe) with consistent messages and a
+window.
+
+Compared with the FP64 oracle running the same loop (orc_retire_view):
+beliefs within 1e-3 with >= 99.9 % class agreement along the stream, the
+message-update count of the live window, and the total log-odds rebuilt from
+the prior, the retired views' messages and the live ones."""
+import numpy as np
+import pytest
+
+from mrfmap_gb300 import lib as L
+from mrfmap_gb300 import synthetic
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+WINDOW = 4
+ITERS = 5
+N_FRAMES = 20
+
+
+@pytest.fixture(scope="module")
+def walk():
+    w = synthetic.walk_room(7, n_frames=N_FRAMES, rows=120, cols=160, res=0.04, dims=(8.0, 8.0, 3.0),
+                            n_boxes=30, step=0.15)
+    return w, [synthetic.render_frame(w, k) for k in range(N_FRAMES)]
+
+
+def _compare(gb, ob):
+    gb = gb.astype(np.float64)
+    touched = (gb > 0) | (ob > 0)
+    return float(np.abs(gb - ob).max()), float(((gb > 0.5) == (ob > 0.5))[touched].mean())
+
+
+def test_windowed_incremental_stream_matches_oracle(native_lib, oracle_lib, walk):
+    w, depths = walk
+    gm = L.MRFMap(w.params, activation=L.ACT_FULL_RAY)
+    om = O.OracleMap(w.params, threads=8)
+    for k in range(N_FRAMES):
+        gm.add_view(w.poses[k], depths[k])
+        om.add_view(w.poses[k], depths[k], O.ACT_FULL_RAY)
+        if k >= WINDOW:
+            gm.retire_view(k - WINDOW)
+            om.retire_view(k - WINDOW)
+        gm.infer(iters=ITERS, flags=L.INCREMENTAL)
+        om.infer(iters=ITERS, flags=O.INCREMENTAL)
+        assert gm.num_bricks == om.num_bricks
+        assert gm.stats()["n_inc_post"] * ITERS == om.last_updates  # the live window only
+        if k in (WINDOW, N_FRAMES // 2, N_FRAMES - 1):
+            emax, agree = _compare(gm.beliefs(), om.beliefs())
+            assert emax <= 1e-3, f"frame {k}: max belief error {emax}"
+            assert agree >= 0.999, f"frame {k}: class agreement {agree}"
+    # the total log-odds is the prior + retired views' messages + live ones
+    lo = gm.logodds()
+    gm.rebuild_logodds()
+    np.testing.assert_allclose(gm.logodds(), lo, rtol=0, atol=2e-4)
+    np.testing.assert_allclose(lo, om.logodds(), rtol=1e-3, atol=1e-2)
+    gm.close()
+    om.close()
+
+
+def test_retired_views_refuse_per_view_calls(native_lib, walk):
+    w, depths = walk
+    m = L.MRFMap(w.params, activation=L.ACT_FULL_RAY)
+    for k in range(3):
+        m.add_view(w.poses[k], depths[k])
+    m.infer(iters=2, flags=L.INCREMENTAL)
+    m.retire_view(0)
+    m.retire_view(0)  # again: nothing to do
+    for call in (lambda: m.likelihood_view(0), lambda: m.read_messages(0), lambda: m.view_incidences(0),
+                 lambda: m.set_pose(0, w.poses[0])):
+        with pytest.raises(L.MrfError) as e:
+            call()
+        assert e.value.status == 6  # MRF_ERR_STATE
+    m.infer(iters=2, flags=L.INCREMENTAL)
+    s, img = m.likelihood_view(1)
+    assert np.isfinite(s) and img.shape == depths[1].shape
+    st = m.stats()
+    assert st["n_views"] == 3
+    m.close()
