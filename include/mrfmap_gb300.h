@@ -136,6 +136,18 @@ MRF_API mrf_status mrf_add_view_device(mrf_map* map, const float* pose, const fl
  * and mrf_view_incidences use the view's camera. */
 MRF_API mrf_status mrf_add_view_camera(mrf_map* map, const float* pose, const float* depth_host, int rows,
                                        int cols, float fx, float fy, float cx, float cy, int* view_id);
+/* A view with its own camera confined to a scene box (no counterpart in the
+ * reference): bricks [brick_lo, brick_hi) per axis of the map's brick grid
+ * (brick b spans voxels 8b .. 8b+7; voxel v spans metres (v - off) * res
+ * with off = dims/2/res for x, y and 0 for z).  The view's rays are traced
+ * and its bricks activated inside the box only, so several scenes placed in
+ * disjoint boxes of one map share its brick pool, its BP launches (one
+ * Jacobi ray launch covers every view of every scene) and its buffers
+ * without seeing one another.  A box outside the grid or empty is
+ * MRF_ERR_INVALID. */
+MRF_API mrf_status mrf_add_view_box(mrf_map* map, const float* pose, const float* depth_host, int rows, int cols,
+                                    float fx, float fy, float cx, float cy, const int brick_lo[3],
+                                    const int brick_hi[3], int* view_id);
 /* A view's camera: rows, cols, and fx, fy, cx, cy in k4 (any may be NULL). */
 MRF_API mrf_status mrf_view_camera(mrf_map* map, int view_id, int* rows, int* cols, float* k4);
 /* GVDBInference::set_pose (src/GVDBInference.cpp:66-82): moves a view and
@@ -239,6 +251,9 @@ MRF_API mrf_status mrf_net_adam(float* params, const float* grads, float* m1, fl
 MRF_API int mrf_ray_variants(void);
 MRF_API mrf_status mrf_set_ray_variant(mrf_map* map, int variant);
 MRF_API mrf_status mrf_autotune(mrf_map* map, int reps, double* ms_out, int cap, int* chosen);
+/* The same with the schedule of the timed iterations in flags (MRF_JACOBI:
+ * Jacobi iterations, one ray launch over every view; else Gauss-Seidel). */
+MRF_API mrf_status mrf_autotune_flags(mrf_map* map, int reps, int flags, double* ms_out, int cap, int* chosen);
 
 /* Extension: log-odds back to the prior, beliefs to 0, messages to 0. */
 MRF_API mrf_status mrf_reset_state(mrf_map* map);

@@ -41,8 +41,8 @@ __device__ __forceinline__ void mark_point(const Geom& g, float px, float py, fl
 #pragma unroll
   for (int a = 0; a < 3; ++a) {
     int vi = (int)floorf(pv[a]);
-    lo[a] = max(floordiv8(vi - 1), 0);
-    hi[a] = min(floordiv8(vi + 1), g.NB[a] - 1);
+    lo[a] = max(floordiv8(vi - 1), g.blo[a] / kBrick);
+    hi[a] = min(floordiv8(vi + 1), g.bhi[a] / kBrick - 1);
   }
   for (int bx = lo[0]; bx <= hi[0]; ++bx)
     for (int by = lo[1]; by <= hi[1]; ++by)
@@ -68,7 +68,7 @@ __global__ void k_activate(Geom g, Pose P, const float* __restrict__ depth, int 
     float pw = fa(fa(fa(fm(P.m[a * 4 + 0], X), fm(P.m[a * 4 + 1], Y)), fm(P.m[a * 4 + 2], d)),
                   P.m[a * 4 + 3]);
     pv[a] = fa(fm(pw, g.inv_res), g.off[a]);
-    if (!(pv[a] >= 0.0f && pv[a] < g.hi[a])) inside = false;
+    if (!(pv[a] >= g.glo[a] && pv[a] < g.hi[a])) inside = false;
   }
   if (inside) mark_point(g, pv[0], pv[1], pv[2], flags);
   if (policy == 1) {

@@ -1155,6 +1155,9 @@ Geom make_geom(const mrf_params& p) {
     int G = (int)ceilf(gg);
     g.NB[a] = (G + 1 + kBrick - 1) / kBrick;
     g.E[a] = kBrick * g.NB[a];
+    g.blo[a] = 0;
+    g.bhi[a] = g.E[a];
+    g.glo[a] = 0.0f;
   }
   g.off[0] = (p.dims[0] * 0.5f) / p.res;
   g.off[1] = (p.dims[1] * 0.5f) / p.res;
@@ -1374,12 +1377,19 @@ mrf_status mrf_test_raise_device_error(mrf_map* m) {
 }
 
 static mrf_status add_view_impl(mrf_map* m, const float* pose, const float* depth, bool device,
-                                int* view_id, const int* cam_size = nullptr, const float* cam_k = nullptr) {
+                                int* view_id, const int* cam_size = nullptr, const float* cam_k = nullptr,
+                                const int* box_lo = nullptr, const int* box_hi = nullptr) {
   if (guard(m) != MRF_OK) return MRF_ERR_INVALID;
   if (!pose || !depth) {
     set_err("null pose or depth");
     return MRF_ERR_INVALID;
   }
+  if (box_lo)
+    for (int a = 0; a < 3; ++a)
+      if (box_lo[a] < 0 || box_hi[a] > m->g.NB[a] || box_lo[a] >= box_hi[a]) {
+        set_err("scene box outside the brick grid or empty");
+        return MRF_ERR_INVALID;
+      }
   if (cam_size && (cam_size[0] < 1 || cam_size[1] < 1 || (int64_t)cam_size[0] * cam_size[1] > (1 << 26) ||
                    !(cam_k[0] > 0.0f) || !(cam_k[1] > 0.0f))) {
     set_err("invalid camera");
@@ -1397,6 +1407,13 @@ static mrf_status add_view_impl(mrf_map* m, const float* pose, const float* dept
       v.cam.cx = cam_k[2];
       v.cam.cy = cam_k[3];
     }
+    if (box_lo)
+      for (int a = 0; a < 3; ++a) {
+        v.cam.blo[a] = kBrick * box_lo[a];
+        v.cam.bhi[a] = kBrick * box_hi[a];
+        v.cam.glo[a] = (float)v.cam.blo[a];
+        v.cam.hi[a] = std::min(m->g.hi[a], (float)v.cam.bhi[a]);
+      }
     const int64_t HW = (int64_t)v.cam.rows * v.cam.cols;
     v.depth.reserve((size_t)HW * 4, false, m->stream);
     const float* src = depth;
@@ -1428,6 +1445,18 @@ mrf_status mrf_add_view_camera(mrf_map* m, const float* pose, const float* depth
   const int size[2] = {rows, cols};
   const float k[4] = {fx, fy, cx, cy};
   return add_view_impl(m, pose, depth_host, false, view_id, size, k);
+}
+
+mrf_status mrf_add_view_box(mrf_map* m, const float* pose, const float* depth_host, int rows, int cols, float fx,
+                            float fy, float cx, float cy, const int brick_lo[3], const int brick_hi[3],
+                            int* view_id) {
+  if (!brick_lo || !brick_hi) {
+    set_err("null scene box");
+    return MRF_ERR_INVALID;
+  }
+  const int size[2] = {rows, cols};
+  const float k[4] = {fx, fy, cx, cy};
+  return add_view_impl(m, pose, depth_host, false, view_id, size, k, brick_lo, brick_hi);
 }
 
 mrf_status mrf_view_camera(mrf_map* m, int view_id, int* rows, int* cols, float* k4) {
@@ -1709,13 +1738,19 @@ mrf_status mrf_set_ray_variant(mrf_map* m, int variant) {
 }
 
 mrf_status mrf_autotune(mrf_map* m, int reps, double* ms_out, int cap, int* chosen) {
+  return mrf_autotune_flags(m, reps, 0, ms_out, cap, chosen);
+}
+
+mrf_status mrf_autotune_flags(mrf_map* m, int reps, int flags, double* ms_out, int cap, int* chosen) {
   if (guard(m) != MRF_OK) return MRF_ERR_INVALID;
   if (reps < 1 || cap < 0 || (cap > 0 && !ms_out)) {
     set_err("invalid autotune arguments");
     return MRF_ERR_INVALID;
   }
+  const bool jacobi = (flags & MRF_JACOBI) != 0;
   return wrap([&] {
     ensure_built(m);
+    if (jacobi && m->jacobi_version != m->built_version) build_jacobi_csr(m);
     const int V = (int)m->views.size();
     const int NV = ray_bp_variants();
     BpArrays a = m->bp();
@@ -1737,7 +1772,7 @@ mrf_status mrf_autotune(mrf_map* m, int reps, double* ms_out, int cap, int* chos
         m->ray_variant = k;
         for (int r = 0; r <= reps; ++r) {
           if (r == 1) CK(cudaEventRecord(m->ev0, m->stream));
-          enqueue_iteration(m, a, false, 0, 2, off, launches);
+          enqueue_iteration(m, a, jacobi, 0, 2, off, launches);
         }
         CK(cudaEventRecord(m->ev1, m->stream));
         sync(m);

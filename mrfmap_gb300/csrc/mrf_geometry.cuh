@@ -93,7 +93,8 @@ __device__ __forceinline__ void ray_setup(const Geom& g, const Pose& P, int x, i
   r.mult = fm(g.res, fabsf(fa(fa(fm(P.m[2], r.d[0]), fm(P.m[6], r.d[1])), fm(P.m[10], r.d[2]))));
 }
 
-// Amanatides & Woo voxel DDA over the box [0, 8*NB) of the brick grid.  The
+// Amanatides & Woo voxel DDA over the box [blo, bhi) of the brick grid (the
+// whole grid [0, 8*NB) unless the view is confined to a scene box).  The
 // next boundary time of an axis is recomputed from the integer boundary each
 // step, (b - o) * (1/d), so no error accumulates along the ray.
 struct Dda {
@@ -104,25 +105,25 @@ struct Dda {
   bool alive;
 };
 
-__device__ __forceinline__ bool dda_axis(float o, float d, int E, float& inv, float& tn, float& tf) {
+__device__ __forceinline__ bool dda_axis(float o, float d, int lo, int hi, float& inv, float& tn, float& tf) {
   if (d > 0.0f || d < 0.0f) {
     inv = fd(1.0f, d);
-    float tA = fm(fs(0.0f, o), inv);
-    float tB = fm(fs((float)E, o), inv);
+    float tA = fm(fs((float)lo, o), inv);
+    float tB = fm(fs((float)hi, o), inv);
     tn = fminf(tA, tB);
     tf = fmaxf(tA, tB);
     return true;
   }
   inv = 0.0f;
-  if (o < 0.0f || o >= (float)E) return false;
+  if (o < (float)lo || o >= (float)hi) return false;
   tn = -INFINITY;
   tf = INFINITY;
   return true;
 }
 
-__device__ __forceinline__ int dda_start(float o, float t0, float d, int E) {
+__device__ __forceinline__ int dda_start(float o, float t0, float d, int lo, int hi) {
   int v = (int)floorf(fa(o, fm(t0, d)));
-  return v < 0 ? 0 : (v > E - 1 ? E - 1 : v);
+  return v < lo ? lo : (v > hi - 1 ? hi - 1 : v);
 }
 
 __device__ __forceinline__ float dda_tnext(int v, int s, float o, float inv) {
@@ -133,16 +134,16 @@ __device__ __forceinline__ float dda_tnext(int v, int s, float o, float inv) {
 
 __device__ __forceinline__ bool dda_init(Dda& r, const Geom& g, const Ray& ray) {
   float tn0, tf0, tn1, tf1, tn2, tf2;
-  if (!dda_axis(ray.o[0], ray.d[0], g.E[0], r.ix, tn0, tf0)) return false;
-  if (!dda_axis(ray.o[1], ray.d[1], g.E[1], r.iy, tn1, tf1)) return false;
-  if (!dda_axis(ray.o[2], ray.d[2], g.E[2], r.iz, tn2, tf2)) return false;
+  if (!dda_axis(ray.o[0], ray.d[0], g.blo[0], g.bhi[0], r.ix, tn0, tf0)) return false;
+  if (!dda_axis(ray.o[1], ray.d[1], g.blo[1], g.bhi[1], r.iy, tn1, tf1)) return false;
+  if (!dda_axis(ray.o[2], ray.d[2], g.blo[2], g.bhi[2], r.iz, tn2, tf2)) return false;
   float t0 = fmaxf(fmaxf(fmaxf(0.0f, tn0), tn1), tn2);
   float t1 = fminf(fminf(fminf(INFINITY, tf0), tf1), tf2);
   if (!(t0 < t1)) return false;
   r.ox = ray.o[0]; r.oy = ray.o[1]; r.oz = ray.o[2];
-  r.vx = dda_start(ray.o[0], t0, ray.d[0], g.E[0]);
-  r.vy = dda_start(ray.o[1], t0, ray.d[1], g.E[1]);
-  r.vz = dda_start(ray.o[2], t0, ray.d[2], g.E[2]);
+  r.vx = dda_start(ray.o[0], t0, ray.d[0], g.blo[0], g.bhi[0]);
+  r.vy = dda_start(ray.o[1], t0, ray.d[1], g.blo[1], g.bhi[1]);
+  r.vz = dda_start(ray.o[2], t0, ray.d[2], g.blo[2], g.bhi[2]);
   r.sx = ray.d[0] > 0.0f ? 1 : (ray.d[0] < 0.0f ? -1 : 0);
   r.sy = ray.d[1] > 0.0f ? 1 : (ray.d[1] < 0.0f ? -1 : 0);
   r.sz = ray.d[2] > 0.0f ? 1 : (ray.d[2] < 0.0f ? -1 : 0);
@@ -151,7 +152,7 @@ __device__ __forceinline__ bool dda_init(Dda& r, const Geom& g, const Ray& ray) 
   r.tz = dda_tnext(r.vz, r.sz, r.oz, r.iz);
   r.tprev = t0;
   r.alive = true;
-  r.guard = 2 * (g.E[0] + g.E[1] + g.E[2]) + 8;
+  r.guard = 2 * ((g.bhi[0] - g.blo[0]) + (g.bhi[1] - g.blo[1]) + (g.bhi[2] - g.blo[2])) + 8;
   return true;
 }
 
@@ -166,17 +167,17 @@ __device__ __forceinline__ bool dda_next(Dda& r, const Geom& g, int& vx, int& vy
   if (r.tx <= r.ty && r.tx <= r.tz) {
     te = r.tx;
     r.vx += r.sx;
-    if (r.vx < 0 || r.vx >= g.E[0]) r.alive = false;
+    if (r.vx < g.blo[0] || r.vx >= g.bhi[0]) r.alive = false;
     else r.tx = dda_tnext(r.vx, r.sx, r.ox, r.ix);
   } else if (r.ty <= r.tz) {
     te = r.ty;
     r.vy += r.sy;
-    if (r.vy < 0 || r.vy >= g.E[1]) r.alive = false;
+    if (r.vy < g.blo[1] || r.vy >= g.bhi[1]) r.alive = false;
     else r.ty = dda_tnext(r.vy, r.sy, r.oy, r.iy);
   } else {
     te = r.tz;
     r.vz += r.sz;
-    if (r.vz < 0 || r.vz >= g.E[2]) r.alive = false;
+    if (r.vz < g.blo[2] || r.vz >= g.bhi[2]) r.alive = false;
     else r.tz = dda_tnext(r.vz, r.sz, r.oz, r.iz);
   }
   float l = fs(te, tin);

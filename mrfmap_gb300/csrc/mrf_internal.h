@@ -28,7 +28,11 @@ struct Geom {
   float off[3];      // dims_xy/2/res, 0
   float hi[3];       // dims/res (activation gate)
   int NB[3];         // brick grid
-  int E[3];          // 8*NB, voxel box of the traversal
+  int E[3];          // 8*NB
+  int blo[3], bhi[3];  // voxel box of the traversal and activation: [0, E) for the
+                       // map's own camera; a view confined to a scene box
+                       // (mrf_add_view_box) has the box's brick-aligned bounds
+  float glo[3];      // lower gate of endpoint activation (0, or the box)
   int lookup_n, n_tiles_u, n_tiles_v;
   int lut_rows, lut_cols;  // image size the sensor tables are tiled for
   const float* sigma;   // device

@@ -41,7 +41,7 @@ EXPORTS = ["mrf_create", "mrf_destroy", "mrf_release_cached_memory", "mrf_last_e
            "mrf_device_beliefs",
            "mrf_stats_get", "mrf_get_stream", "mrf_synchronize", "mrf_render", "mrf_render_view", "mrf_pixel_diagnostics", "mrf_add_view_camera",
            "mrf_view_camera", "mrf_set_memory_limit", "mrf_memory_in_use", "mrf_test_raise_device_error",
-           "mrf_infer_until", "mrf_retire_view"]
+           "mrf_infer_until", "mrf_retire_view", "mrf_add_view_box", "mrf_autotune_flags"]
 
 RENDER_EXPECTED_DEPTH = 0
 RENDER_ACCURACY = 1
@@ -141,6 +141,9 @@ def load(path: str | None = None):
         "mrf_view_camera": ([vp, C.c_int, ip, ip, fp], C.c_int),
         "mrf_set_memory_limit": ([C.c_int64], C.c_int),
         "mrf_retire_view": ([vp, C.c_int], C.c_int),
+        "mrf_autotune_flags": ([vp, C.c_int, C.c_int, C.POINTER(C.c_double), C.c_int, ip], C.c_int),
+        "mrf_add_view_box": ([vp, fp, fp, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, ip, ip,
+                              ip], C.c_int),
         "mrf_infer_until": ([vp, ip, C.c_int, C.c_int, C.c_void_p, C.c_float, C.c_int, C.c_int, ip, fp],
                             C.c_int),
         "mrf_memory_in_use": ([], C.c_int64),
@@ -232,6 +235,18 @@ class MRFMap:
                                            cx, cy, C.byref(vid)))
         return vid.value
 
+    def add_view_box(self, pose, depth, fx: float, fy: float, cx: float, cy: float, brick_lo, brick_hi) -> int:
+        """A view with its own camera whose rays and bricks stay inside the
+        scene box of bricks [brick_lo, brick_hi)."""
+        vid = C.c_int()
+        d = _f32(depth)
+        lo = np.ascontiguousarray(brick_lo, dtype=np.int32)
+        hi = np.ascontiguousarray(brick_hi, dtype=np.int32)
+        _check(self._L.mrf_add_view_box(self._h, _fp(_f32(pose)), _fp(d), d.shape[0], d.shape[1], fx, fy, cx, cy,
+                                        lo.ctypes.data_as(C.POINTER(C.c_int)), hi.ctypes.data_as(C.POINTER(C.c_int)),
+                                        C.byref(vid)))
+        return vid.value
+
     def view_camera(self, view: int):
         """(rows, cols, (fx, fy, cx, cy)) of a view."""
         r, c = C.c_int(), C.c_int()
@@ -319,14 +334,15 @@ class MRFMap:
     def set_ray_variant(self, variant: int):
         _check(self._L.mrf_set_ray_variant(self._h, variant))
 
-    def autotune(self, reps: int = 3):
-        """Times every ray-kernel variant on this map; keeps the fastest.
+    def autotune(self, reps: int = 3, flags: int = 0):
+        """Times every ray-kernel variant on this map (iterations of the
+        schedule in flags: JACOBI or Gauss-Seidel); keeps the fastest.
         Returns (chosen variant, ms per pass of each variant)."""
         nv = self._L.mrf_ray_variants()
         ms = np.zeros(nv, np.float64)
         ch = C.c_int()
-        _check(self._L.mrf_autotune(self._h, reps, ms.ctypes.data_as(C.POINTER(C.c_double)), nv,
-                                    C.byref(ch)))
+        _check(self._L.mrf_autotune_flags(self._h, reps, flags, ms.ctypes.data_as(C.POINTER(C.c_double)), nv,
+                                          C.byref(ch)))
         return ch.value, ms
 
     def reset_state(self):

@@ -315,3 +315,139 @@ def render_frames_torch(walk: Walk, frames, device="cuda"):
         z[z > walk.max_range] = 0.0
         out.append(z.contiguous())
     return out
+
+
+# ---- the batched workload: several scenes in one map -------------------------
+
+@dataclass
+class Batch:
+    """Scenes placed side by side in one map, each in its own brick-aligned
+    box; every view belongs to one scene (box) and has its own camera."""
+    name: str
+    params: MapParams
+    scenes: list          # Scene per box (world coordinates of the map)
+    boxes: list           # (brick_lo[3], brick_hi[3]) per scene
+    poses: list
+    cams: list            # (rows, cols, fx, fy, cx, cy) per view
+    scene_of: list        # scene index per view
+    seed: int
+    max_range: float
+
+
+def batch_scenes(seed: int = 3, n_scenes: int = 8, views_per_scene: int = 32,
+                 sizes=((120, 160), (240, 320), (480, 640)), size_cycle=(0, 0, 0, 0, 1, 1, 1, 2),
+                 res: float = 0.02, max_range: float = 9.5, n_boxes: int = 20,
+                 room_range=(3.0, 7.0)) -> Batch:
+    """n_scenes seeded box rooms of different sizes (room_range metres wide
+    and deep, 2.5-4 m high), laid out along x with a one-brick gap,
+    views_per_scene views each on a seeded loop inside the room aimed at its
+    centre, image sizes taken from `sizes` in the order `size_cycle`
+    (f = 525 cols / 640, principal point at the centre).  The default mix
+    (half 160x120, three eighths 320x240, one eighth 640x480) keeps a map of
+    256 such views at 2 cm within 32-bit incidence indices.  Ray lengths run
+    from a few voxels to several hundred crossings: the range is capped
+    below the reference's 10 m Z_MAX."""
+    rng = np.random.default_rng(seed)
+    bsz = 8 * res
+    rooms = []
+    for s in range(n_scenes):
+        w = rng.uniform(*room_range)
+        dpt = rng.uniform(*room_range)
+        h = rng.uniform(2.5, 4.0)
+        rooms.append((w, dpt, h))
+    nbx = [int(np.ceil(w / bsz)) + 1 for (w, _, _) in rooms]
+    nby = max(int(np.ceil(d / bsz)) for (_, d, _) in rooms) + 1
+    nbz = max(int(np.ceil(h / bsz)) for (_, _, h) in rooms) + 1
+    NBx = sum(nbx) + (n_scenes - 1)
+    dims = (NBx * bsz - res, nby * bsz - res, nbz * bsz - res)  # brick grids of exactly NBx, nby, nbz
+    rows0, cols0 = sizes[-1]
+    f0 = 525.0 * cols0 / 640
+    p = MapParams(res=res, dims=dims, rows=rows0, cols=cols0, fx=f0, fy=f0, cx=cols0 / 2, cy=rows0 / 2,
+                  prior=0.1, max_iters=20)
+    sensor_params(p)
+    off = np.array([dims[0] / 2 / res, dims[1] / 2 / res, 0.0])
+    scenes, boxes, poses, cams, scene_of = [], [], [], [], []
+    bx0 = 0
+    for s, (w, dpt, h) in enumerate(rooms):
+        lo = np.array([bx0, 0, 0])
+        hi = np.array([bx0 + nbx[s], nby, nbz])
+        boxes.append((lo.tolist(), hi.tolist()))
+        # the room inside the box, in map world coordinates (metres)
+        wlo = (lo * 8 - off) * res
+        centre = np.array([wlo[0] + w / 2 + res, wlo[1] + dpt / 2 + res, 0.0])
+        eps = res / 2
+        room = np.array([centre[0] - w / 2 + eps, centre[1] - dpt / 2 + eps, eps,
+                         centre[0] + w / 2 - eps, centre[1] + dpt / 2 - eps, h - eps])
+        bxs = []
+        while len(bxs) < n_boxes:
+            side = rng.uniform(0.2, min(1.2, w / 4), 3)
+            side[2] = rng.uniform(0.2, h / 2)
+            c = np.array([rng.uniform(room[0] + 0.5, room[3] - 0.5), rng.uniform(room[1] + 0.5, room[4] - 0.5),
+                          side[2] / 2])
+            bxs.append(np.concatenate([c - side / 2, c + side / 2]))
+        scenes.append(Scene(room=room, boxes=np.array(bxs)))
+        target = np.array([centre[0], centre[1], h / 2])
+        a0 = rng.uniform(0, 2 * np.pi)
+        rad = 0.3 * min(w, dpt)
+        for k in range(views_per_scene):
+            a = a0 + 2 * np.pi * k / views_per_scene
+            eye = np.array([centre[0] + rad * np.cos(a), centre[1] + rad * np.sin(a),
+                            min(h - 0.3, 1.2 + rng.uniform(-0.2, 0.2))])
+            poses.append(look_at(eye, target, np.deg2rad(rng.uniform(-5, 5))))
+            rows, cols = sizes[size_cycle[k % len(size_cycle)]]
+            f = 525.0 * cols / 640
+            cams.append((rows, cols, f, f, cols / 2, rows / 2))
+            scene_of.append(s)
+        bx0 += nbx[s] + 1
+    n = n_scenes * views_per_scene
+    return Batch(f"batch_{n_scenes}scenes_{n}views_{int(round(res * 100))}cm", p, scenes, boxes, poses, cams,
+                 scene_of, seed, max_range)
+
+
+def render_batch_view(batch: Batch, k: int) -> np.ndarray:
+    """View k of the batch on the host (numpy; seeded per view)."""
+    rows, cols, fx, fy, cx, cy = batch.cams[k]
+    cp = MapParams(res=batch.params.res, dims=batch.params.dims, rows=rows, cols=cols, fx=fx, fy=fy, cx=cx,
+                   cy=cy, prior=0.1)
+    rng = np.random.default_rng((batch.seed, k))
+    return add_noise(render_depth(batch.scenes[batch.scene_of[k]], cp, batch.poses[k]), rng,
+                     max_range=batch.max_range)
+
+
+def render_batch_torch(batch: Batch, views, device="cuda"):
+    """Views of the batch rendered with torch on `device` (box scenes, the
+    noise model of add_noise, a generator seeded per view)."""
+    out = []
+    for k in views:
+        rows, cols, fx, fy, cx, cy = batch.cams[k]
+        out.append(_render_boxes_torch(batch.scenes[batch.scene_of[k]], rows, cols, fx, fy, cx, cy,
+                                       batch.poses[k], batch.seed * 100003 + k, batch.max_range, device))
+    return out
+
+
+def _render_boxes_torch(scene, rows, cols, fx, fy, cx, cy, pose, seed, max_range, device):
+    import torch
+    xs = (torch.arange(cols, device=device, dtype=torch.float64) + 0.5 - cx) / fx
+    ys = (torch.arange(rows, device=device, dtype=torch.float64) + 0.5 - cy) / fy
+    rc = torch.stack(torch.broadcast_tensors(xs[None, :], ys[:, None],
+                                             torch.ones(rows, cols, device=device, dtype=torch.float64)), -1)
+    room = torch.tensor(scene.room, device=device, dtype=torch.float64)
+    boxes = torch.tensor(scene.boxes, device=device, dtype=torch.float64)
+    P = torch.tensor(pose, device=device, dtype=torch.float64)
+    d = (rc @ P[:3, :3].T).reshape(-1, 3)
+    o = P[:3, 3]
+    inv = 1.0 / d
+    t = torch.maximum((room[:3] - o) * inv, (room[3:] - o) * inv).min(dim=1).values
+    bl = (boxes[None, :, :3] - o) * inv[:, None, :]
+    bh = (boxes[None, :, 3:] - o) * inv[:, None, :]
+    tn = torch.minimum(bl, bh).max(dim=2).values
+    tf = torch.maximum(bl, bh).min(dim=2).values
+    hit = (tn <= tf) & (tn > 0)
+    tb = torch.where(hit, tn, torch.full_like(tn, float("inf"))).min(dim=1).values
+    t = torch.minimum(t, tb).reshape(rows, cols)
+    g = torch.Generator(device=device)
+    g.manual_seed(int(seed))
+    z = (t + torch.randn(t.shape, generator=g, device=device, dtype=torch.float64) * (0.002 + 0.0012 * t * t)).float()
+    z[torch.rand(t.shape, generator=g, device=device) < 0.02] = 0.0
+    z[z > max_range] = 0.0
+    return z.contiguous()

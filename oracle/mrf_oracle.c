@@ -51,6 +51,10 @@
 typedef struct {
   int rows, cols;
   float fx, fy, cx, cy;
+  /* voxel box of the traversal and activation ([0, 8 NB) unless the view is
+   * confined to a scene box) and the endpoint-activation gate */
+  int blo[3], bhi[3];
+  float glo[3], ghi[3];
 } orc_cam;
 
 typedef struct {
@@ -102,6 +106,8 @@ struct orc_map {
   int64_t scratch_vox;
   double* pbuf; /* messages of one camera update (orc_update_camera) */
   int64_t pbuf_cap;
+  /* the scene box of the view being added (orc_add_view_box) */
+  int next_box, box_lo[3], box_hi[3];
 };
 
 static int g_threads = 1;
@@ -175,6 +181,10 @@ orc_map* orc_create(const orc_params* p) {
     m->hi[a] = g;
     m->G[a] = (int)ceilf(g);
     m->NB[a] = (m->G[a] + 1 + BRICK - 1) / BRICK;
+    m->cam.blo[a] = 0;
+    m->cam.bhi[a] = BRICK * m->NB[a];
+    m->cam.glo[a] = 0.0f;
+    m->cam.ghi[a] = g;
   }
   /* src/GVDBCamera.cpp:15-18 / 76-79: x,y centred, z not shifted */
   m->off[0] = (p->dims[0] * 0.5f) / p->res;
@@ -266,26 +276,28 @@ static void ray_setup(const orc_map* m, const orc_cam* cam, const float* pose, i
 /* ---- Amanatides-Woo voxel DDA over the brick-grid box ------------------- */
 typedef struct {
   float o[3], d[3], inv[3], tmax[3], tprev;
-  int v[3], step[3], E[3];
+  int v[3], step[3], lo[3], hi[3];
   int alive, guard;
 } dda_t;
 
-static int dda_init(dda_t* r, const orc_map* m, const float o[3], const float d[3]) {
+/* over the camera's voxel box [blo, bhi) */
+static int dda_init(dda_t* r, const orc_cam* cam, const float o[3], const float d[3]) {
   float t0 = 0.0f, t1 = INFINITY;
   for (int a = 0; a < 3; ++a) {
     r->o[a] = o[a]; r->d[a] = d[a];
-    r->E[a] = BRICK * m->NB[a];
-    float E = (float)r->E[a];
+    r->lo[a] = cam->blo[a];
+    r->hi[a] = cam->bhi[a];
+    float lo = (float)r->lo[a], E = (float)r->hi[a];
     float tn, tf;
     if (d[a] > 0.0f || d[a] < 0.0f) {
       r->inv[a] = 1.0f / d[a];
-      float tA = (0.0f - o[a]) * r->inv[a];
+      float tA = (lo - o[a]) * r->inv[a];
       float tB = (E - o[a]) * r->inv[a];
       tn = fminf(tA, tB);
       tf = fmaxf(tA, tB);
     } else {
       r->inv[a] = 0.0f;
-      if (o[a] < 0.0f || o[a] >= E) return 0;
+      if (o[a] < lo || o[a] >= E) return 0;
       tn = -INFINITY;
       tf = INFINITY;
     }
@@ -296,8 +308,8 @@ static int dda_init(dda_t* r, const orc_map* m, const float o[3], const float d[
   for (int a = 0; a < 3; ++a) {
     float pa = o[a] + t0 * d[a];
     int vi = (int)floorf(pa);
-    if (vi < 0) vi = 0;
-    if (vi > r->E[a] - 1) vi = r->E[a] - 1;
+    if (vi < r->lo[a]) vi = r->lo[a];
+    if (vi > r->hi[a] - 1) vi = r->hi[a] - 1;
     r->v[a] = vi;
     r->step[a] = d[a] > 0.0f ? 1 : (d[a] < 0.0f ? -1 : 0);
     if (r->step[a] > 0)
@@ -309,7 +321,7 @@ static int dda_init(dda_t* r, const orc_map* m, const float o[3], const float d[
   }
   r->tprev = t0;
   r->alive = 1;
-  r->guard = 2 * (r->E[0] + r->E[1] + r->E[2]) + 8;
+  r->guard = 2 * ((r->hi[0] - r->lo[0]) + (r->hi[1] - r->lo[1]) + (r->hi[2] - r->lo[2])) + 8;
   return 1;
 }
 
@@ -327,7 +339,7 @@ static int dda_next(dda_t* r, int vout[3], float* len, float* tin, float* texit)
   *texit = te;
   r->tprev = fmaxf(r->tprev, te);
   r->v[a] += r->step[a];
-  if (r->v[a] < 0 || r->v[a] >= r->E[a]) {
+  if (r->v[a] < r->lo[a] || r->v[a] >= r->hi[a]) {
     r->alive = 0;
   } else {
     float nb = r->step[a] > 0 ? (float)(r->v[a] + 1) : (float)r->v[a];
@@ -360,14 +372,14 @@ static void clean_depth(const orc_cam* cam, const float* in, float* out) {
 /* ---- activation (src/GVDBCamera.cpp:70-100; src/GVDBMRFMap.cpp:117-135) -- */
 static int floordiv8(int v) { return v >= 0 ? v / 8 : -((-v + 7) / 8); }
 
-static void mark_point_bricks(const orc_map* m, const float pv[3], unsigned char* flag) {
+static void mark_point_bricks(const orc_map* m, const orc_cam* cam, const float pv[3], unsigned char* flag) {
   int lo[3], hi[3];
   for (int a = 0; a < 3; ++a) {
     int vi = (int)floorf(pv[a]);
     lo[a] = floordiv8(vi - 1);
     hi[a] = floordiv8(vi + 1);
-    if (lo[a] < 0) lo[a] = 0;
-    if (hi[a] > m->NB[a] - 1) hi[a] = m->NB[a] - 1;
+    if (lo[a] < cam->blo[a] / BRICK) lo[a] = cam->blo[a] / BRICK;
+    if (hi[a] > cam->bhi[a] / BRICK - 1) hi[a] = cam->bhi[a] / BRICK - 1;
   }
   for (int bx = lo[0]; bx <= hi[0]; ++bx)
     for (int by = lo[1]; by <= hi[1]; ++by)
@@ -397,15 +409,15 @@ static void activate_view(orc_map* m, const orc_cam* cam, const float* pose, con
         float z = pose[a * 4 + 2] * Z;
         float pw = ((u + w) + z) + pose[a * 4 + 3];
         pv[a] = pw * m->inv_res + m->off[a];
-        if (!(pv[a] >= 0.0f && pv[a] < m->hi[a])) inside = 0;
+        if (!(pv[a] >= cam->glo[a] && pv[a] < cam->ghi[a])) inside = 0;
       }
-      if (inside) mark_point_bricks(m, pv, flag);
+      if (inside) mark_point_bricks(m, cam, pv, flag);
       if (policy == ORC_ACT_FULL_RAY) {
         float o[3], dr[3], mult;
         ray_setup(m, cam, pose, x, y, o, dr, &mult);
         float lim = d + 3.0f * poly_f(lut_at(m, cam, m->sigma_lut, x, y), m->p.lookup_n, d);
         dda_t r;
-        if (dda_init(&r, m, o, dr)) {
+        if (dda_init(&r, cam, o, dr)) {
           int v[3];
           float l, tin, te;
           while (dda_next(&r, v, &l, &tin, &te)) {
@@ -456,6 +468,22 @@ int orc_add_view_camera(orc_map* m, const float* pose, const float* depth, int p
   v->cam.fy = fy;
   v->cam.cx = cx;
   v->cam.cy = cy;
+  for (int a = 0; a < 3; ++a) {
+    v->cam.blo[a] = m->cam.blo[a];
+    v->cam.bhi[a] = m->cam.bhi[a];
+    v->cam.glo[a] = m->cam.glo[a];
+    v->cam.ghi[a] = m->cam.ghi[a];
+  }
+  if (m->next_box) {
+    /* a view confined to a scene box (orc_add_view_box) */
+    for (int a = 0; a < 3; ++a) {
+      v->cam.blo[a] = BRICK * m->box_lo[a];
+      v->cam.bhi[a] = BRICK * m->box_hi[a];
+      v->cam.glo[a] = (float)v->cam.blo[a];
+      v->cam.ghi[a] = fminf(m->hi[a], (float)v->cam.bhi[a]);
+    }
+    m->next_box = 0;
+  }
   v->depth = (float*)malloc((size_t)rows * cols * sizeof(float));
   clean_depth(&v->cam, depth, v->depth);
   v->policy = policy;
@@ -467,6 +495,17 @@ int orc_add_view_camera(orc_map* m, const float* pose, const float* depth, int p
   m->nviews++;
   activate_view(m, &v->cam, v->pose, v->depth, policy);
   return m->nviews - 1;
+}
+
+int orc_add_view_box(orc_map* m, const float* pose, const float* depth, int policy, int rows, int cols, float fx,
+                     float fy, float cx, float cy, const int brick_lo[3], const int brick_hi[3]) {
+  for (int a = 0; a < 3; ++a) {
+    if (brick_lo[a] < 0 || brick_hi[a] > m->NB[a] || brick_lo[a] >= brick_hi[a]) return -1;
+    m->box_lo[a] = brick_lo[a];
+    m->box_hi[a] = brick_hi[a];
+  }
+  m->next_box = 1;
+  return orc_add_view_camera(m, pose, depth, policy, rows, cols, fx, fy, cx, cy);
 }
 
 int orc_add_view(orc_map* m, const float* pose, const float* depth, int policy) {
@@ -532,7 +571,7 @@ static void build_ray(orc_map* m, orc_view* v, int x, int y, float d, int* meta)
   int64_t cur_lin = -1;
   float s_last = 0.0f;
   dda_t r;
-  if (dda_init(&r, m, o, dr)) {
+  if (dda_init(&r, &v->cam, o, dr)) {
     int vv[3];
     float l, tin, te;
     while (dda_next(&r, vv, &l, &tin, &te)) {
@@ -892,7 +931,7 @@ int orc_trace_pixel(const orc_map* m, const float* pose, int x, int y, int* vox,
   ray_setup(m, &m->cam, pose, x, y, o, dr, &mult);
   dda_t r;
   int n = 0;
-  if (!dda_init(&r, m, o, dr)) return 0;
+  if (!dda_init(&r, &m->cam, o, dr)) return 0;
   int vv[3];
   float l, tin, te;
   while (dda_next(&r, vv, &l, &tin, &te)) {
@@ -927,7 +966,7 @@ int64_t orc_insert_logodds(const orc_map* m, const float* pose, const float* dep
       float o[3], dr[3], mult;
       ray_setup(m, &m->cam, pose, x, y, o, dr, &mult);
       dda_t r;
-      if (!dda_init(&r, m, o, dr)) continue;
+      if (!dda_init(&r, &m->cam, o, dr)) continue;
       int vv[3];
       float l, tin, te;
       while (dda_next(&r, vv, &l, &tin, &te)) {
@@ -958,7 +997,7 @@ static double like_pixel(const orc_map* m, const float* pose, int x, int y, floa
   int64_t cur_lin = -1;
   float s_last = 0.0f;
   dda_t r;
-  if (dda_init(&r, m, o, dr)) {
+  if (dda_init(&r, &m->cam, o, dr)) {
     int vv[3];
     float l, tin, te;
     while (dda_next(&r, vv, &l, &tin, &te)) {
@@ -1046,7 +1085,7 @@ static float render_pixel(const orc_map* m, int mode, const float* pose, int x, 
   int64_t cur_lin = -1;
   int run_open = 0;
   dda_t r;
-  if (dda_init(&r, m, o, dr)) {
+  if (dda_init(&r, &m->cam, o, dr)) {
     int vv[3];
     float l, tin, te;
     while (dda_next(&r, vv, &l, &tin, &te)) {

@@ -58,6 +58,11 @@ int orc_add_view(orc_map* m, const float* pose, const float* depth, int policy);
  * are looked up at the pixel's position scaled into the params' image */
 int orc_add_view_camera(orc_map* m, const float* pose, const float* depth, int policy, int rows, int cols,
                         float fx, float fy, float cx, float cy);
+/* a view with its own camera confined to a scene box: bricks
+ * [brick_lo, brick_hi) per axis; its rays are traced and its bricks
+ * activated inside the box only.  Returns the view id, -1 for a bad box. */
+int orc_add_view_box(orc_map* m, const float* pose, const float* depth, int policy, int rows, int cols, float fx,
+                     float fy, float cx, float cy, const int brick_lo[3], const int brick_hi[3]);
 int orc_view_pixels(const orc_map* m, int view);
 int orc_set_pose(orc_map* m, int view, const float* pose, int policy);
 int orc_num_views(const orc_map* m);

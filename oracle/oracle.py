@@ -56,6 +56,9 @@ def lib():
         L.orc_add_view_camera.argtypes = [vp, fp, fp, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float,
                                           C.c_float, C.c_float]
         L.orc_add_view_camera.restype = C.c_int
+        L.orc_add_view_box.argtypes = [vp, fp, fp, C.c_int, C.c_int, C.c_int, C.c_float, C.c_float,
+                                       C.c_float, C.c_float, ip, ip]
+        L.orc_add_view_box.restype = C.c_int
         L.orc_view_pixels.argtypes = [vp, C.c_int]
         L.orc_view_pixels.restype = C.c_int
         L.orc_set_pose.argtypes = [vp, C.c_int, fp, C.c_int]
@@ -133,6 +136,17 @@ class OracleMap:
         d = _f(depth)
         assert d.size == rows * cols
         return self._L.orc_add_view_camera(self._h, _ptr(_f(pose)), _ptr(d), policy, rows, cols, fx, fy, cx, cy)
+
+    def add_view_box(self, pose, depth, rows, cols, fx, fy, cx, cy, brick_lo, brick_hi, policy=ACT_ENDPOINT) -> int:
+        d = _f(depth)
+        assert d.size == rows * cols
+        lo = np.ascontiguousarray(brick_lo, np.int32)
+        hi = np.ascontiguousarray(brick_hi, np.int32)
+        v = self._L.orc_add_view_box(self._h, _ptr(_f(pose)), _ptr(d), policy, rows, cols, fx, fy, cx, cy,
+                                     _ptr(lo, C.c_int), _ptr(hi, C.c_int))
+        if v < 0:
+            raise ValueError("bad scene box")
+        return v
 
     def set_pose(self, view, pose, policy=ACT_ENDPOINT):
         return self._L.orc_set_pose(self._h, view, _ptr(_f(pose)), policy)
