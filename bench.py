@@ -368,6 +368,11 @@ def parity_cut(w, act, policy):
             gm.add_view(w.poses[k], w.depths[k])
             om.add_view(w.poses[k], w.depths[k], pol)
     iters = w.params.max_iters
+    gm.set_precision(L.PRECISION_HALF_STREAMS)
+    gm.infer(iters=iters)
+    g16 = gm.beliefs().astype(np.float64).ravel()
+    gm.set_precision(L.PRECISION_FP32)
+    gm.reset_state()
     gm.infer(iters=iters)
     t0 = time.perf_counter()
     om.infer(iters=iters)
@@ -375,6 +380,7 @@ def parity_cut(w, act, policy):
     gb, ob = gm.beliefs().astype(np.float64).ravel(), om.beliefs().ravel()
     om.close()
     err = np.abs(gb - ob)
+    err16 = np.abs(g16 - ob)
     touched = (gb > 0) | (ob > 0)
     n_long, lv = 0, []
     for v in range(len(views)):
@@ -396,6 +402,8 @@ def parity_cut(w, act, policy):
     if len(lv):
         out["max_abs_belief_err_long_ray_voxels"] = float(err[lv].max())
         out["long_ray_voxels_checked"] = int(len(lv))
+    out["half_streams"] = {"max_abs_belief_err": float(err16.max()),
+                           "class_agreement_at_0.5": float(((g16 > 0.5) == (ob > 0.5))[touched].mean())}
     return out
 
 
@@ -449,6 +457,26 @@ def run_ours(args):
     torch.cuda.synchronize()
     barrier(ws)
     ms = e0.elapsed_time(e1)
+    # the same steps with 16-bit streams in the ray kernel (not the headline:
+    # reported beside it with its error against the FP64 oracle)
+    m.set_precision(L.PRECISION_HALF_STREAMS)
+    for _ in range(2):
+        m.reset_state()
+        m.infer(iters=iters, flags=L.ASYNC)
+    m.synchronize()
+    h0 = torch.cuda.Event(enable_timing=True)
+    h1 = torch.cuda.Event(enable_timing=True)
+    h0.record(stream)
+    for _ in range(args.steps):
+        m.reset_state()
+        m.infer(iters=iters, flags=L.ASYNC)
+    h1.record(stream)
+    m.synchronize()
+    ms_half = h0.elapsed_time(h1)
+    m.reset_state()
+    m.infer(iters=iters, flags=L.PROFILE)
+    prof_half = m.stats()
+    m.set_precision(L.PRECISION_FP32)
     # per-kernel device times of one profiled step (events on the map stream)
     m.reset_state()
     m.infer(iters=iters, flags=L.PROFILE)
@@ -596,6 +624,10 @@ def run_ours(args):
                                "static_messages": "exact constants (p = F_EPS before a ray's first "
                                                   "non-zero potential), summed once per build"},
             "dynamic_updates_per_s": st["n_inc_dyn"] * iters * args.steps / (ms / 1e3),
+            "half_streams": {"value": n_upd_step * args.steps / (ms_half / 1e3), "ms_per_step": ms_half / args.steps,
+                             "ray_kernel_ms_per_launch": prof_half["kernel_ms"][1] / max(prof_half["kernel_count"][1], 1),
+                             "note": "ray kernel reads segment lengths and gathers ln q as fp16; "
+                                     "error against the FP64 oracle in parity_vs_fp64.half_streams"},
             "gpu_launches": launches_step * args.steps,
             "roofline": {"bound": "hbm", "kernel": "k_ray_bp", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,

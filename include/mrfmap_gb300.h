@@ -255,6 +255,17 @@ MRF_API mrf_status mrf_autotune(mrf_map* map, int reps, double* ms_out, int cap,
  * Jacobi iterations, one ray launch over every view; else Gauss-Seidel). */
 MRF_API mrf_status mrf_autotune_flags(mrf_map* map, int reps, int flags, double* ms_out, int cap, int* chosen);
 
+/* Storage precision of the ray kernel's streams (no reference counterpart;
+ * the reference stores half2 channels, gvdbkernels.cu:975-978):
+ *   MRF_PRECISION_FP32         (default) segment lengths and ln q in fp32
+ *   MRF_PRECISION_HALF_STREAMS the ray kernel reads segment lengths and
+ *                              gathers ln q as fp16 (round to nearest);
+ *                              every product, prefix and sum stays fp32
+ *                              (fp64 on long rays), the messages fp32.
+ * Changing it keeps the map's state. */
+#define MRF_PRECISION_FP32 0
+#define MRF_PRECISION_HALF_STREAMS 1
+MRF_API mrf_status mrf_set_precision(mrf_map* map, int mode);
 /* Extension: log-odds back to the prior, beliefs to 0, messages to 0. */
 MRF_API mrf_status mrf_reset_state(mrf_map* map);
 

@@ -13,6 +13,8 @@
 //                    (gvdbkernels.cu:457-479); a segmented sum over the
 //                    pair-grouped permutation of the dynamic incidences --
 //                    no atomics, fixed summation order
+#include <cuda_fp16.h>
+
 #include <algorithm>
 
 #include "mrf_internal.h"
@@ -49,8 +51,8 @@ constexpr int kPrepPer = 4;
 
 __global__ void __launch_bounds__(kPrepThreads)
     k_pair_prepare(const uint32_t* __restrict__ pair_vox, const float* __restrict__ m,
-                   const float* __restrict__ L, float* __restrict__ lnq, float* __restrict__ dm, uint32_t p0,
-                   uint32_t p1) {
+                   const float* __restrict__ L, float* __restrict__ lnq, __half* __restrict__ lnq16,
+                   float* __restrict__ dm, uint32_t p0, uint32_t p1) {
   const uint32_t base = p0 + blockIdx.x * (kPrepThreads * kPrepPer) + threadIdx.x;
   float eta[kPrepPer];
 #pragma unroll
@@ -63,7 +65,10 @@ __global__ void __launch_bounds__(kPrepThreads)
     const uint32_t p = base + k * kPrepThreads;
     if (p >= p1) break;
     float qq = clampf(1.0f / (1.0f + expf(eta[k])), kFEps, 1.0f - kFEps);
-    lnq[p] = logf(qq);
+    if (lnq16)
+      lnq16[p] = __float2half_rn(logf(qq));  // 16-bit streams: the ray kernel gathers halves
+    else
+      lnq[p] = logf(qq);
     if (dm) dm[p] = __int_as_float(0x7fc00000);  // Jacobi: NaN until the pair updates
   }
 }
@@ -172,21 +177,43 @@ __device__ __forceinline__ void load_pids(uint32_t (&pid)[KE], uint32_t off, int
 
 // ln q of a lane's KE incidences (those >= n read as zero; kWhole: the
 // whole chunk lies inside the ray and nothing is checked)
-template <int KE, bool kWhole>
+__device__ __forceinline__ float to_f(float v) { return v; }
+__device__ __forceinline__ float to_f(__half v) { return __half2float(v); }
+
+template <int KE, bool kWhole, typename TQ>
 __device__ __forceinline__ void gather_lq(float (&lq)[KE], const uint32_t (&pid)[KE], int i0, int n,
-                                          const float* __restrict__ lnq) {
+                                          const TQ* __restrict__ lnq) {
 #pragma unroll
-  for (int j = 0; j < KE; ++j) lq[j] = (kWhole || i0 + j < n) ? __ldg(lnq + pid[j]) : 0.0f;
+  for (int j = 0; j < KE; ++j) lq[j] = (kWhole || i0 + j < n) ? to_f(__ldg(lnq + pid[j])) : 0.0f;
+}
+
+// VW lengths at element i of base (fp32: one 16-byte vector; fp16: one
+// 8-byte vector of four halves), zeros when !ok
+template <int VW, int kPol>
+__device__ __forceinline__ void ld_len(float (&out)[VW], const float* __restrict__ base, int i, bool ok) {
+  ld_vec<VW, kPol>(out, base, i, ok);
+}
+template <int VW, int kPol>
+__device__ __forceinline__ void ld_len(float (&out)[VW], const __half* __restrict__ base, int i, bool ok) {
+  static_assert(VW == 4, "fp16 lengths load four at a time");
+  uint2 u = make_uint2(0u, 0u);
+  if (ok) u = ld_stream<kPol>(reinterpret_cast<const uint2*>(base + i));
+  const float2 a = __half22float2(*reinterpret_cast<const __half2*>(&u.x));
+  const float2 b = __half22float2(*reinterpret_cast<const __half2*>(&u.y));
+  out[0] = a.x;
+  out[1] = a.y;
+  out[2] = b.x;
+  out[3] = b.y;
 }
 
 // with the lane's ln q gathered: loads lengths (and potentials at and after
 // kmu, a multiple of 4; below it they are known zeros), forms prefix
 // exponents from carryA; returns the chunk total of l ln q
 // (kLenIn: the lengths were loaded ahead into len_in)
-template <int KE, int kPol, bool kWhole, bool kLenIn = false>
+template <int KE, int kPol, bool kWhole, bool kLenIn = false, typename TL = float>
 __device__ __forceinline__ float slice_from_lq(Slice<KE>& s, const float (&lq)[KE], uint32_t off, int i0,
                                                int n, int kmu, float carryA, int lane,
-                                               const float* __restrict__ inc_len,
+                                               const TL* __restrict__ inc_len,
                                                const float* __restrict__ inc_mu,
                                                const float* len_in = nullptr) {
   constexpr int VW = KE % 4 == 0 ? 4 : KE;  // vector width
@@ -198,7 +225,7 @@ __device__ __forceinline__ float slice_from_lq(Slice<KE>& s, const float (&lq)[K
 #pragma unroll
       for (int j = 0; j < VW; ++j) l[j] = len_in[VW * v + j];
     } else {
-      ld_vec<VW, kPol>(l, inc_len + off, i, kWhole || i < n);
+      ld_len<VW, kPol>(l, inc_len + off, i, kWhole || i < n);
     }
     ld_vec<VW, kPol>(m, inc_mu + off, i, (kWhole || i < n) && i >= kmu);
 #pragma unroll
@@ -226,29 +253,30 @@ __device__ __forceinline__ float slice_from_lq(Slice<KE>& s, const float (&lq)[K
   return __shfl_sync(kFull, ex + run, 31);
 }
 
-template <int KE, int kPol, bool kWhole, bool kLenIn = false>
+template <int KE, int kPol, bool kWhole, bool kLenIn = false, typename TL = float, typename TQ = float>
 __device__ __forceinline__ float slice_from_pids(Slice<KE>& s, const uint32_t (&pid)[KE], uint32_t off,
                                                  int i0, int n, int kmu, float carryA, int lane,
-                                                 const float* __restrict__ inc_len,
+                                                 const TL* __restrict__ inc_len,
                                                  const float* __restrict__ inc_mu,
-                                                 const float* __restrict__ lnq,
+                                                 const TQ* __restrict__ lnq,
                                                  const float* len_in = nullptr) {
   float lq[KE];
   gather_lq<KE, kWhole>(lq, pid, i0, n, lnq);
-  return slice_from_lq<KE, kPol, kWhole, kLenIn>(s, lq, off, i0, n, kmu, carryA, lane, inc_len, inc_mu,
-                                                len_in);
+  return slice_from_lq<KE, kPol, kWhole, kLenIn, TL>(s, lq, off, i0, n, kmu, carryA, lane, inc_len, inc_mu,
+                                                    len_in);
 }
 
-template <int KE, int kPol, bool kWhole>
+template <int KE, int kPol, bool kWhole, typename TL, typename TQ>
 __device__ __forceinline__ float load_slice(Slice<KE>& s, uint32_t off, int i0, int n, int kmu,
                                             float carryA, int lane,
                                             const uint32_t* __restrict__ inc_pair,
-                                            const float* __restrict__ inc_len,
+                                            const TL* __restrict__ inc_len,
                                             const float* __restrict__ inc_mu,
-                                            const float* __restrict__ lnq) {
+                                            const TQ* __restrict__ lnq) {
   uint32_t pid[KE];
   load_pids<KE, kPol>(pid, off, i0, kWhole ? i0 + KE : n, inc_pair);
-  return slice_from_pids<KE, kPol, kWhole>(s, pid, off, i0, n, kmu, carryA, lane, inc_len, inc_mu, lnq);
+  return slice_from_pids<KE, kPol, kWhole, false, TL, TQ>(s, pid, off, i0, n, kmu, carryA, lane, inc_len,
+                                                          inc_mu, lnq);
 }
 
 // A at chunk-relative index idx (0 <= idx < 32 * KE), broadcast to the warp
@@ -341,11 +369,11 @@ __device__ __forceinline__ void pre_total(const Slice<KE>& s, int i0, int r0, fl
   ts = t;
 }
 
-template <typename Acc, int kPol, int kPf>
+template <typename Acc, int kPol, int kPf, typename TL, typename TQ>
 __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, const uint32_t* __restrict__ inc_pair,
-                                            const float* __restrict__ inc_len,
+                                            const TL* __restrict__ inc_len,
                                             const float* __restrict__ inc_mu,
-                                            const float* __restrict__ lnq, float* __restrict__ inc_pl,
+                                            const TQ* __restrict__ lnq, float* __restrict__ inc_pl,
                                             int fix_reset, int lane) {
   const int n_pre = me.n_pre, n_post = me.n_post;
   const int r0 = fix_reset ? 0 : me.r0;
@@ -368,7 +396,7 @@ __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, const uint32_t* _
     uint32_t pid_next[kE];
     float len_next[kE], len[kE];
     if (kPf) load_pids<kE, kPol>(pid_next, off, kE * lane, n_pre, inc_pair);
-    if (kPf == 2) ld_vec<kE, kPol>(len_next, inc_len + off, kE * lane, kE * lane < n_pre);
+    if (kPf == 2) ld_len<kE, kPol>(len_next, inc_len + off, kE * lane, kE * lane < n_pre);
     for (int base = 0; base < n_pre; base += kChunk) {
       const int i0 = base + kE * lane;
       uint32_t pid[kE];
@@ -381,7 +409,7 @@ __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, const uint32_t* _
         }
         if (base + kChunk < n_pre) {
           load_pids<kE, kPol>(pid_next, off, i0 + kChunk, n_pre, inc_pair);
-          if (kPf == 2) ld_vec<kE, kPol>(len_next, inc_len + off, i0 + kChunk, i0 + kChunk < n_pre);
+          if (kPf == 2) ld_len<kE, kPol>(len_next, inc_len + off, i0 + kChunk, i0 + kChunk < n_pre);
         }
       } else {
         load_pids<kE, kPol>(pid, off, i0, n_pre, inc_pair);
@@ -446,7 +474,7 @@ __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, const uint32_t* _
 // the SM's L1.  Which warp handles a ray does not change its result.  Variants differ only in register budget (kMinBlocks
 // resident blocks per SM), load policy and schedule: their arithmetic is
 // identical, so the autotuner's choice never changes a result.
-template <int kMinBlocks, int kPol, int kPf, bool kReg>
+template <int kMinBlocks, int kPol, int kPf, bool kReg, typename TL, typename TQ>
 __global__ void __launch_bounds__(kRayWarps * 32, kMinBlocks) k_ray_bp(const RayMeta* __restrict__ queue,
                                                            uint32_t n_rays,
                                                            const uint32_t* __restrict__ rstart,
@@ -456,17 +484,17 @@ __global__ void __launch_bounds__(kRayWarps * 32, kMinBlocks) k_ray_bp(const Ray
                                                            uint32_t* __restrict__ lcounter,
                                                            uint32_t* __restrict__ counter,
                                                            const uint32_t* __restrict__ inc_pair,
-                                                           const float* __restrict__ inc_len,
+                                                           const TL* __restrict__ inc_len,
                                                            const float* __restrict__ inc_mu,
-                                                           const float* __restrict__ lnq,
+                                                           const TQ* __restrict__ lnq,
                                                            float* __restrict__ inc_pl,
                                                            int fix_reset) {
   const int lane = threadIdx.x & 31;
   auto ray = [&](const RayMeta& me) {
     if (me.n_pre <= kLongRay)
-      ray_bp_warp<float, kPol, kPf>(me, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
+      ray_bp_warp<float, kPol, kPf, TL, TQ>(me, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
     else
-      ray_bp_warp<double, kPol, kPf>(me, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
+      ray_bp_warp<double, kPol, kPf, TL, TQ>(me, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
   };
   if constexpr (kReg) {
     // counter[r]: tickets of region r; rstart[r] .. rstart[r + 1] its home
@@ -948,7 +976,8 @@ cudaError_t launch_pair_prepare(const BpArrays& a, uint32_t p0, uint32_t p1, int
                                 cudaStream_t s) {
   if (p1 <= p0) return cudaSuccess;
   k_pair_prepare<<<blocks(p1 - p0, kPrepThreads * kPrepPer), kPrepThreads, 0, s>>>(
-      a.pair_vox, a.pair_m, a.L, a.pair_lnq, jacobi ? a.pair_dm : nullptr, p0, p1);
+      a.pair_vox, a.pair_m, a.L, a.pair_lnq, a.half_streams ? a.pair_lnq16 : nullptr,
+      jacobi ? a.pair_dm : nullptr, p0, p1);
   return cudaGetLastError();
 }
 
@@ -973,36 +1002,44 @@ int resident_of(K kernel) {
 }
 }  // namespace
 
-int ray_bp_resident_blocks(int variant) {
-  static int resident[kRayVariants] = {0};
+int ray_bp_resident_blocks(int variant, int half_streams) {
+  static int resident[2][kRayVariants] = {{0}};
   if (variant < 0 || variant >= kRayVariants) return 1;
-  if (!resident[variant]) {
+  const int h = half_streams ? 1 : 0;
+  if (!resident[h][variant]) {
     switch (variant) {
-#define X(id, mb, pol, pf, sc) \
-  case id:                     \
-    resident[variant] = resident_of(k_ray_bp<mb, pol, pf, (sc > 0)>); \
+#define X(id, mb, pol, pf, sc)                                                                        \
+  case id:                                                                                            \
+    resident[h][variant] = h ? resident_of(k_ray_bp<mb, pol, pf, (sc > 0), __half, __half>)          \
+                             : resident_of(k_ray_bp<mb, pol, pf, (sc > 0), float, float>);           \
     break;
       MRF_RAY_VARIANTS(X)
 #undef X
     }
   }
-  return resident[variant];
+  return resident[h][variant];
 }
 
 cudaError_t launch_ray_bp(const BpArrays& a, const RayWork& w, int fix_reset, int num_sms, int variant,
                           cudaStream_t s) {
   if (!w.n_rays) return cudaSuccess;
   if (variant < 0 || variant >= kRayVariants) return cudaErrorInvalidValue;
-  int64_t b = std::min<int64_t>((int64_t)num_sms * ray_bp_resident_blocks(variant),
+  int64_t b = std::min<int64_t>((int64_t)num_sms * ray_bp_resident_blocks(variant, a.half_streams),
                                 (w.n_rays + kRayWarps - 1) / kRayWarps);
   const unsigned grid = (unsigned)std::max<int64_t>(b, 1);
   switch (variant) {
 #define X(id, mb, pol, pf, sc)                                                                    \
   case id:                                                                                        \
-    k_ray_bp<mb, pol, pf, (sc > 0)><<<grid, kRayWarps * 32, 0, s>>>(                              \
-        sc == 0 ? w.queue : w.region, w.n_rays, w.rstart, w.nreg,                                 \
-        w.left, w.n_left, w.lcounter, sc == 0 ? w.counter : w.rcounter, a.inc_pair, a.inc_len,       \
-        a.inc_mu, a.pair_lnq, a.inc_pl, fix_reset);                                               \
+    if (a.half_streams)                                                                           \
+      k_ray_bp<mb, pol, pf, (sc > 0), __half, __half><<<grid, kRayWarps * 32, 0, s>>>(            \
+          sc == 0 ? w.queue : w.region, w.n_rays, w.rstart, w.nreg, w.left, w.n_left, w.lcounter,  \
+          sc == 0 ? w.counter : w.rcounter, a.inc_pair, a.inc_len16, a.inc_mu, a.pair_lnq16,        \
+          a.inc_pl, fix_reset);                                                                   \
+    else                                                                                          \
+      k_ray_bp<mb, pol, pf, (sc > 0), float, float><<<grid, kRayWarps * 32, 0, s>>>(              \
+          sc == 0 ? w.queue : w.region, w.n_rays, w.rstart, w.nreg, w.left, w.n_left, w.lcounter,  \
+          sc == 0 ? w.counter : w.rcounter, a.inc_pair, a.inc_len, a.inc_mu, a.pair_lnq, a.inc_pl,  \
+          fix_reset);                                                                             \
     break;
     MRF_RAY_VARIANTS(X)
 #undef X
@@ -1145,6 +1182,17 @@ cudaError_t launch_remap_gather(const uint32_t* pair_vox, float* pair_m, uint32_
                                 const float* dense, cudaStream_t s) {
   if (!n) return cudaSuccess;
   k_remap_gather<<<blocks(n, 256), 256, 0, s>>>(pair_vox, pair_m, n, dense);
+  return cudaGetLastError();
+}
+
+__global__ void k_to_half(const float* __restrict__ in, int64_t n, __half* __restrict__ out) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = __float2half_rn(in[i]);
+}
+
+cudaError_t launch_to_half(const float* in, int64_t n, __half* out, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_to_half<<<(unsigned)std::min<int64_t>(blocks(n, 256), 16384), 256, 0, s>>>(in, n, out);
   return cudaGetLastError();
 }
 

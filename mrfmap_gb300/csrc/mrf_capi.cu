@@ -194,6 +194,11 @@ struct mrf_map {
   int64_t n_inc = 0, n_pairs = 0, n_dperm = 0, n_dpairs = 0;
   // voxels with a pair past the length gate (their beliefs follow L)
   DBuf vox_active;
+  // MRF_PRECISION_HALF_STREAMS: fp16 copies of the segment lengths (per
+  // build) and of ln q (written by k_pair_prepare)
+  int precision = MRF_PRECISION_FP32;
+  DBuf inc_len16, pair_q16;
+  int len16_version = -1;
   // logit(prior) + the messages of retired views, per voxel (kept once a view
   // has been retired; the prior alone before that)
   DBuf d_Lbase;
@@ -237,6 +242,9 @@ struct mrf_map {
     a.pair_dm = pair_dm.as<float>();
     a.L = d_L.as<float>();
     a.belief = d_belief.as<float>();
+    a.half_streams = precision == MRF_PRECISION_HALF_STREAMS ? 1 : 0;
+    a.inc_len16 = inc_len16.as<__half>();
+    a.pair_lnq16 = pair_q16.as<__half>();
     return a;
   }
   int64_t hw() const { return (int64_t)prm.rows * prm.cols; }
@@ -867,6 +875,13 @@ void build_jacobi_csr(mrf_map* m) {
 
 void ensure_built(mrf_map* m) {
   if (m->built_version != m->version) rebuild(m);
+  // the fp16 streams of the current lists
+  if (m->precision == MRF_PRECISION_HALF_STREAMS && m->len16_version != m->built_version) {
+    m->inc_len16.reserve((size_t)std::max<int64_t>(m->n_inc, 1) * 2, false, m->stream);
+    m->pair_q16.reserve((size_t)std::max<int64_t>(m->n_pairs, 1) * 2, false, m->stream);
+    CK(launch_to_half(m->inc_len.as<float>(), m->n_inc, m->inc_len16.as<__half>(), m->stream));
+    m->len16_version = m->built_version;
+  }
 }
 
 struct Profiler {
@@ -1203,7 +1218,8 @@ void destroy_bufs(mrf_map* m) {
                  &m->pair_dm,
                  &m->pair_seg, &m->dperm, &m->dpair, &m->dseg, &m->drun,
                  &m->carry, &m->ray_order, &m->ray_queue, &m->region_q, &m->rstart, &m->rcounters, &m->counters, &m->tile_first,
-                 &m->vseg, &m->vpairs, &m->vvox, &m->vox_active, &m->d_Lbase, &m->s_rec, &m->s_recs, &m->s_pf, &m->s_ps,
+                 &m->vseg, &m->vpairs, &m->vvox, &m->vox_active, &m->d_Lbase, &m->inc_len16, &m->pair_q16,
+                 &m->s_rec, &m->s_recs, &m->s_pf, &m->s_ps,
                  &m->s_flags, &m->s_ind, &m->s_scan,
                  &m->s_q0, &m->s_q1, &m->s_q2, &m->s_q3, &m->s_bf, &m->s_loud, &m->s_pv, &m->s_sg,
                  &m->s_tmp, &m->s_counts, &m->s_offs, &m->s_vox, &m->s_k0, &m->s_k1, &m->s_v0,
@@ -1293,7 +1309,10 @@ mrf_status mrf_create(const mrf_params* params, mrf_map** out) {
     m->prm.bias_lut = m->bias.data();
     CK(cudaGetDevice(&m->device));
     CK(cudaDeviceGetAttribute(&m->num_sms, cudaDevAttrMultiProcessorCount, m->device));
-    for (int k = 0; k < ray_bp_variants(); ++k) ray_bp_resident_blocks(k);
+    for (int k = 0; k < ray_bp_variants(); ++k) {
+      ray_bp_resident_blocks(k, 0);
+      ray_bp_resident_blocks(k, 1);
+    }
     CK(cudaStreamCreateWithFlags(&m->stream, cudaStreamNonBlocking));
     CK(cudaEventCreate(&m->ev0));
     CK(cudaEventCreate(&m->ev1));
@@ -1724,6 +1743,20 @@ int mrf_ray_variants(void) { return ray_bp_variants(); }
 
 static void drop_graphs(mrf_map* m) {
   for (auto& g : m->graphs) g.version = -1;
+}
+
+mrf_status mrf_set_precision(mrf_map* m, int mode) {
+  if (guard(m) != MRF_OK) return MRF_ERR_INVALID;
+  if (mode != MRF_PRECISION_FP32 && mode != MRF_PRECISION_HALF_STREAMS) {
+    set_err("invalid precision mode");
+    return MRF_ERR_INVALID;
+  }
+  if (mode != m->precision) {
+    m->precision = mode;
+    m->len16_version = -1;
+    drop_graphs(m);
+  }
+  return MRF_OK;
 }
 
 mrf_status mrf_set_ray_variant(mrf_map* m, int variant) {

@@ -1,5 +1,6 @@
 // mrf_internal.h -- structures shared between the C-ABI layer and the kernels.
 #pragma once
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -186,6 +187,12 @@ struct BpArrays {
   float* pair_dm;
   float* L;
   float* belief;
+  // 16-bit streams (MRF_PRECISION_HALF_STREAMS): the ray kernel reads the
+  // segment lengths and gathers ln q as fp16; k_pair_prepare writes ln q as
+  // fp16 then
+  int half_streams;
+  const __half* inc_len16;
+  __half* pair_lnq16;
 };
 // per-tile partial sums of the pair-update segmented reduction
 struct TileCarry {
@@ -199,7 +206,9 @@ cudaError_t launch_pair_prepare(const BpArrays& a, uint32_t p0, uint32_t p1, int
 // ray-kernel variants (register budget x load policy; identical arithmetic)
 int ray_bp_variants();
 // resident blocks per SM of a variant of the persistent ray kernel (queried once)
-int ray_bp_resident_blocks(int variant);
+int ray_bp_resident_blocks(int variant, int half_streams);
+// fp32 -> fp16, round to nearest
+cudaError_t launch_to_half(const float* in, int64_t n, __half* out, cudaStream_t s);
 // the rays of one ray-kernel launch in its schedules: queue[0..n_rays)
 // longest first with one zeroed counter; the same rays as nreg regions of
 // consecutive pixels, region r's home rays (longest first) at positions

@@ -25,6 +25,8 @@ FIX_PRE_RESET = 4
 ASYNC = 8
 PROFILE = 16
 NO_GRAPH = 32
+PRECISION_FP32 = 0
+PRECISION_HALF_STREAMS = 1
 
 _STATUS = {0: "MRF_OK", 1: "MRF_ERR_INVALID", 2: "MRF_ERR_CUDA", 3: "MRF_ERR_OOM",
            4: "MRF_ERR_CAPACITY", 5: "MRF_ERR_DEVICE", 6: "MRF_ERR_STATE"}
@@ -41,7 +43,8 @@ EXPORTS = ["mrf_create", "mrf_destroy", "mrf_release_cached_memory", "mrf_last_e
            "mrf_device_beliefs",
            "mrf_stats_get", "mrf_get_stream", "mrf_synchronize", "mrf_render", "mrf_render_view", "mrf_pixel_diagnostics", "mrf_add_view_camera",
            "mrf_view_camera", "mrf_set_memory_limit", "mrf_memory_in_use", "mrf_test_raise_device_error",
-           "mrf_infer_until", "mrf_retire_view", "mrf_add_view_box", "mrf_autotune_flags"]
+           "mrf_infer_until", "mrf_retire_view", "mrf_add_view_box", "mrf_autotune_flags",
+           "mrf_set_precision"]
 
 RENDER_EXPECTED_DEPTH = 0
 RENDER_ACCURACY = 1
@@ -141,6 +144,7 @@ def load(path: str | None = None):
         "mrf_view_camera": ([vp, C.c_int, ip, ip, fp], C.c_int),
         "mrf_set_memory_limit": ([C.c_int64], C.c_int),
         "mrf_retire_view": ([vp, C.c_int], C.c_int),
+        "mrf_set_precision": ([vp, C.c_int], C.c_int),
         "mrf_autotune_flags": ([vp, C.c_int, C.c_int, C.POINTER(C.c_double), C.c_int, ip], C.c_int),
         "mrf_add_view_box": ([vp, fp, fp, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, ip, ip,
                               ip], C.c_int),
@@ -330,6 +334,11 @@ class MRFMap:
     def warm_features(self, feat_dev_ptr: int):
         """Writes [n_bricks, 512, 4] float features to a device buffer."""
         _check(self._L.mrf_warm_features(self._h, C.c_void_p(feat_dev_ptr)))
+
+    def set_precision(self, mode: int):
+        """PRECISION_FP32 (default) or PRECISION_HALF_STREAMS (fp16 lengths
+        and ln q gathers in the ray kernel)."""
+        _check(self._L.mrf_set_precision(self._h, mode))
 
     def set_ray_variant(self, variant: int):
         _check(self._L.mrf_set_ray_variant(self._h, variant))

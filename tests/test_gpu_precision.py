@@ -1,0 +1,45 @@
+"""16-bit streams (MRF_PRECISION_HALF_STREAMS): the ray kernel reads segment
+lengths and gathers ln q as fp16; products, prefixes and sums stay fp32
+(fp64 on long rays).  Measured against the FP64 oracle on the small room
+(Gauss-Seidel and Jacobi, 10 iterations); the fp32 default is unchanged by
+switching the mode back, bit for bit.  The error is printed for the record;
+the mode is accepted at the tests' belief tolerance (1e-3)."""
+import numpy as np
+import pytest
+
+from mrfmap_gb300 import lib as L
+from mrfmap_gb300 import synthetic
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("flags", [0, L.JACOBI], ids=["gauss-seidel", "jacobi"])
+def test_half_streams_against_oracle(native_lib, oracle_lib, small_room, flags):
+    w = small_room
+    gm = L.MRFMap(w.params, activation=L.ACT_FULL_RAY)
+    om = O.OracleMap(w.params, threads=8)
+    for P, D in zip(w.poses, w.depths):
+        gm.add_view(P, D)
+        om.add_view(P, D, O.ACT_FULL_RAY)
+    om.infer(flags=O.JACOBI if flags else 0)
+    ob = om.beliefs()
+    gm.infer(flags=flags)
+    b32 = gm.beliefs()
+    gm.set_precision(L.PRECISION_HALF_STREAMS)
+    gm.reset_state()
+    gm.infer(flags=flags)
+    b16 = gm.beliefs().astype(np.float64)
+    touched = (b16 > 0) | (ob > 0)
+    err = np.abs(b16 - ob).max()
+    agree = ((b16 > 0.5) == (ob > 0.5))[touched].mean()
+    print(f"fp16 streams: max belief error {err:.3e}, class agreement {agree:.6f}")
+    assert err <= 1e-3 and agree >= 0.999
+    gm.set_precision(L.PRECISION_FP32)
+    gm.reset_state()
+    gm.infer(flags=flags)
+    np.testing.assert_array_equal(gm.beliefs(), b32)
+    with pytest.raises(L.MrfError):
+        gm.set_precision(7)
+    gm.close()
+    om.close()
