@@ -959,6 +959,17 @@ __global__ void k_touch_pairs(const uint32_t* __restrict__ pair_vox, const float
   if (n_active && (threadIdx.x & 31) == 0 && b) atomicAdd(n_active, (unsigned long long)__popc(b));
 }
 
+// 64-bit total of n u32 counts (the incidence total of a build, checked
+// against the 32-bit index range before any offset is formed from it)
+__global__ void k_sum_u32(const uint32_t* __restrict__ v, int64_t n, unsigned long long* __restrict__ out) {
+  unsigned long long c = 0;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    c += v[i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(kFull, c, o);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
+}
+
 __global__ void k_count_flags(const uint8_t* __restrict__ flag, int64_t n, unsigned long long* __restrict__ out) {
   unsigned c = 0;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -1229,6 +1240,13 @@ cudaError_t launch_touch_counts(const uint32_t* pair_vox, const float* cum, uint
   if (np) k_touch_pairs<<<blocks(np, 256), 256, 0, s>>>(pair_vox, cum, np, flag, out2);
   if (nvox > 0)
     k_count_flags<<<(unsigned)std::min<int64_t>(blocks(nvox, 256), 4096), 256, 0, s>>>(flag, nvox, out2 + 1);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sum_u32(const uint32_t* v, int64_t n, unsigned long long* out, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(out, 0, 8, s);
+  if (e != cudaSuccess || n <= 0) return e;
+  k_sum_u32<<<(unsigned)std::min<int64_t>(blocks(n, 256), 4096), 256, 0, s>>>(v, n, out);
   return cudaGetLastError();
 }
 

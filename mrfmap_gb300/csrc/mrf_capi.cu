@@ -389,6 +389,17 @@ void rebuild_lists(mrf_map* m, OldPairs& old) {
     if (!m->views[c].retired)
       CK(launch_trace_count(m->views[c].cam, m->views[c].pose, m->views[c].depth.as<float>(),
                             m->s_counts.as<uint32_t>() + m->views[c].pix_base, m->s_err.as<int>(), m->stream));
+  // the total in 64 bits first: the u32 scan below wraps past 2^32, and a
+  // wrapped total would size the arenas too small for the emit pass
+  {
+    m->s_delta.reserve(64, false, m->stream);
+    CK(launch_sum_u32(m->s_counts.as<uint32_t>(), npix, m->s_delta.as<unsigned long long>(), m->stream));
+    const unsigned long long total = read1(m, m->s_delta.as<unsigned long long>());
+    check_device_err(m);
+    if (total > 0xFFFFFFF0ull)
+      fail(MRF_ERR_CAPACITY, "incidence count " + std::to_string(total) +
+                                 " exceeds the 32-bit incidence index range (fewer or smaller views per map)");
+  }
   // sentinel 0 at the end so the scan yields the total
   CK(cudaMemsetAsync(m->s_counts.as<uint32_t>() + npix, 0, 4, m->stream));
   size_t tb = scan_temp_bytes((uint32_t)(npix + 1));

@@ -335,7 +335,8 @@ class Batch:
 
 
 def batch_scenes(seed: int = 3, n_scenes: int = 8, views_per_scene: int = 32,
-                 sizes=((120, 160), (240, 320), (480, 640)), size_cycle=(0, 0, 0, 0, 1, 1, 1, 2),
+                 sizes=((120, 160), (240, 320), (480, 640)),
+                 size_cycle=(0, 0, 1, 0, 0, 1, 0, 0, 1, 0, 0, 1, 0, 0, 1, 2),
                  res: float = 0.02, max_range: float = 9.5, n_boxes: int = 20,
                  room_range=(3.0, 7.0)) -> Batch:
     """n_scenes seeded box rooms of different sizes (room_range metres wide
@@ -343,8 +344,9 @@ def batch_scenes(seed: int = 3, n_scenes: int = 8, views_per_scene: int = 32,
     views_per_scene views each on a seeded loop inside the room aimed at its
     centre, image sizes taken from `sizes` in the order `size_cycle`
     (f = 525 cols / 640, principal point at the centre).  The default mix
-    (half 160x120, three eighths 320x240, one eighth 640x480) keeps a map of
-    256 such views at 2 cm within 32-bit incidence indices.  Ray lengths run
+    (10 in 16 views 160x120, 5 in 16 320x240, 1 in 16 640x480: 160 / 80 / 16
+    of 256) keeps a map of such views at 2 cm near 3.2 G incidences, inside
+    the 32-bit incidence index range (4.29 G).  Ray lengths run
     from a few voxels to several hundred crossings: the range is capped
     below the reference's 10 m Z_MAX."""
     rng = np.random.default_rng(seed)

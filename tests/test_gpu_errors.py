@@ -116,3 +116,24 @@ def test_capacity_of_32_bit_voxel_ids(native_lib):
     m.load_map(np.array([[100.5, 100.5, 100.5]], np.float32), np.array([0.9], np.float32))
     assert m.num_bricks == 1
     m.close()
+
+
+def test_capacity_of_32_bit_incidence_indices(native_lib):
+    """44 copies of one 640x480 1 cm view hold ~4.6 G incidences: the build
+    counts them in 64 bits and refuses before forming any 32-bit offset
+    (only the per-pixel counts, ~54 MB, are allocated by then).  With the
+    copies retired the map builds and iterates normally."""
+    w = synthetic.full_room(1, n_frames=1)
+    m = L.MRFMap(w.params, activation=L.ACT_FULL_RAY)
+    for _ in range(44):
+        m.add_view(w.poses[0], w.depths[0])
+    with pytest.raises(L.MrfError) as e:
+        m.infer(iters=1)
+    assert e.value.status == CAPACITY and "32-bit incidence" in str(e.value)
+    for k in range(1, 44):
+        m.retire_view(k)
+    m.infer(iters=2)
+    st = m.stats()
+    assert 0 < st["n_inc_post"] < 2 ** 32 // 40
+    assert np.isfinite(m.beliefs()).all()
+    m.close()
