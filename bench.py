@@ -334,16 +334,18 @@ def run_reference(args):
 
 
 # bumped whenever k_ray_bp's memory traffic changes (profiles/ray_bp_traffic.json)
-RAY_KERNEL_VERSION = 5
+RAY_KERNEL_VERSION = 6
 
 
-def ray_kernel_bytes(st, iters):
+def ray_kernel_bytes(st, iters, half=True):
     """Algorithmic bytes of the ray-message kernel for one launch-sum, over
     the rays it runs over (those with a dynamic incidence): per Pre
-    incidence 12 B (pair id 4, length 4, ln q gather 4); per dynamic
+    incidence the pair id (4 B), the length and the ln q gather (2 B each
+    with the default 16-bit streams, 4 B each in fp32); per dynamic
     incidence (from the ray's first non-zero potential on) +8 B (potential
     4, message write 4); per ray 16 B of metadata."""
-    return (12 * st["n_inc_pre_bp"] + 8 * st["n_inc_dyn"] + 16 * st["n_rays_bp"]) * iters
+    per_pre = 8 if half else 12
+    return (per_pre * st["n_inc_pre_bp"] + 8 * st["n_inc_dyn"] + 16 * st["n_rays_bp"]) * iters
 
 
 LONG_RAY = 512  # Pre incidences above which the ray kernel sums in FP64
@@ -368,10 +370,10 @@ def parity_cut(w, act, policy):
             gm.add_view(w.poses[k], w.depths[k])
             om.add_view(w.poses[k], w.depths[k], pol)
     iters = w.params.max_iters
-    gm.set_precision(L.PRECISION_HALF_STREAMS)
-    gm.infer(iters=iters)
-    g16 = gm.beliefs().astype(np.float64).ravel()
     gm.set_precision(L.PRECISION_FP32)
+    gm.infer(iters=iters)
+    g32 = gm.beliefs().astype(np.float64).ravel()
+    gm.set_precision(L.PRECISION_HALF_STREAMS)
     gm.reset_state()
     gm.infer(iters=iters)
     t0 = time.perf_counter()
@@ -380,7 +382,7 @@ def parity_cut(w, act, policy):
     gb, ob = gm.beliefs().astype(np.float64).ravel(), om.beliefs().ravel()
     om.close()
     err = np.abs(gb - ob)
-    err16 = np.abs(g16 - ob)
+    err32 = np.abs(g32 - ob)
     touched = (gb > 0) | (ob > 0)
     n_long, lv = 0, []
     for v in range(len(views)):
@@ -402,8 +404,9 @@ def parity_cut(w, act, policy):
     if len(lv):
         out["max_abs_belief_err_long_ray_voxels"] = float(err[lv].max())
         out["long_ray_voxels_checked"] = int(len(lv))
-    out["half_streams"] = {"max_abs_belief_err": float(err16.max()),
-                           "class_agreement_at_0.5": float(((g16 > 0.5) == (ob > 0.5))[touched].mean())}
+    out["precision"] = "16-bit streams (the default)"
+    out["fp32_streams"] = {"max_abs_belief_err": float(err32.max()),
+                           "class_agreement_at_0.5": float(((g32 > 0.5) == (ob > 0.5))[touched].mean())}
     return out
 
 
@@ -457,9 +460,10 @@ def run_ours(args):
     torch.cuda.synchronize()
     barrier(ws)
     ms = e0.elapsed_time(e1)
-    # the same steps with 16-bit streams in the ray kernel (not the headline:
-    # reported beside it with its error against the FP64 oracle)
-    m.set_precision(L.PRECISION_HALF_STREAMS)
+    # the same steps with fp32 streams in the ray kernel (the default reads
+    # lengths and ln q as fp16; both are reported with their error against
+    # the FP64 oracle)
+    m.set_precision(L.PRECISION_FP32)
     for _ in range(2):
         m.reset_state()
         m.infer(iters=iters, flags=L.ASYNC)
@@ -476,7 +480,7 @@ def run_ours(args):
     m.reset_state()
     m.infer(iters=iters, flags=L.PROFILE)
     prof_half = m.stats()
-    m.set_precision(L.PRECISION_FP32)
+    m.set_precision(L.PRECISION_HALF_STREAMS)
     # per-kernel device times of one profiled step (events on the map stream)
     m.reset_state()
     m.infer(iters=iters, flags=L.PROFILE)
@@ -611,7 +615,7 @@ def run_ours(args):
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (fp64 sums on rays > 512)",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 on fp16 length/ln q streams (fp64 sums on rays > 512)",
             "data": "synthetic (seeded room scenes; no public dataset)",
             "config": workload_config(w, args.policy, ws),
             "workload_stats": {"n_inc_per_iter": st["n_inc_post"],
@@ -624,10 +628,12 @@ def run_ours(args):
                                "static_messages": "exact constants (p = F_EPS before a ray's first "
                                                   "non-zero potential), summed once per build"},
             "dynamic_updates_per_s": st["n_inc_dyn"] * iters * args.steps / (ms / 1e3),
-            "half_streams": {"value": n_upd_step * args.steps / (ms_half / 1e3), "ms_per_step": ms_half / args.steps,
+            "precision": "16-bit streams: the ray kernel reads segment lengths and gathers ln q as fp16; "
+                         "every product, prefix and sum fp32 (fp64 on rays > 512), messages fp32",
+            "fp32_streams": {"value": n_upd_step * args.steps / (ms_half / 1e3), "ms_per_step": ms_half / args.steps,
                              "ray_kernel_ms_per_launch": prof_half["kernel_ms"][1] / max(prof_half["kernel_count"][1], 1),
-                             "note": "ray kernel reads segment lengths and gathers ln q as fp16; "
-                                     "error against the FP64 oracle in parity_vs_fp64.half_streams"},
+                             "note": "the same steps with fp32 lengths and ln q; error against the FP64 oracle "
+                                     "in parity_vs_fp64.fp32_streams"},
             "gpu_launches": launches_step * args.steps,
             "roofline": {"bound": "hbm", "kernel": "k_ray_bp", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
@@ -724,7 +730,7 @@ def run_large(args):
         print(json.dumps({
             "metric": LARGE_METRIC, "value": sum_over_ranks(n, ws) / dt, "unit": "frames/s", "n_gpus": ws,
             "steps": n, "warmup": warm, "ms_per_step": 1e3 * dt / max(n, 1), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (fp64 sums on rays > 512)",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 on fp16 length/ln q streams (fp64 sums on rays > 512)",
             "data": "synthetic (seeded random walk; no public dataset)",
             "config": {"workload": walk.name, "frames": args.frames, "window": W, "iters_per_frame": iters,
                        "voxel_m": walk.params.res, "dims_m": list(walk.params.dims), "boxes": 150,
@@ -848,7 +854,7 @@ def run_batched(args):
         print(json.dumps({
             "metric": BATCH_METRIC, "value": sum_over_ranks(n_upd, ws) / (ms / 1e3), "unit": UNIT, "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (fp64 sums on rays > 512)",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 on fp16 length/ln q streams (fp64 sums on rays > 512)",
             "data": "synthetic (seeded box rooms; no public dataset)",
             "config": {"workload": b.name, "scenes": len(b.boxes), "views": len(b.poses), "view_sizes": sizes,
                        "voxel_m": b.params.res, "max_range_m": b.max_range, "activation": "fullray",

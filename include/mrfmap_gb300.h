@@ -92,6 +92,9 @@ typedef struct mrf_stats {
   int64_t n_rays_bp;       /* rays the ray kernel runs over: those with a dynamic
                               incidence (the others' messages are all static) */
   int64_t n_inc_pre_bp;    /* their Pre incidences */
+  int64_t builds_full;     /* incidence-list builds of every view so far */
+  int64_t builds_appended; /* builds that appended only the views added since
+                              the previous build (full-ray maps) */
 } mrf_stats;
 
 /* Map construction: GVDBInference(...) + GVDBMRFMap::gpuAllocate
@@ -257,11 +260,12 @@ MRF_API mrf_status mrf_autotune_flags(mrf_map* map, int reps, int flags, double*
 
 /* Storage precision of the ray kernel's streams (no reference counterpart;
  * the reference stores half2 channels, gvdbkernels.cu:975-978):
- *   MRF_PRECISION_FP32         (default) segment lengths and ln q in fp32
- *   MRF_PRECISION_HALF_STREAMS the ray kernel reads segment lengths and
- *                              gathers ln q as fp16 (round to nearest);
- *                              every product, prefix and sum stays fp32
- *                              (fp64 on long rays), the messages fp32.
+ *   MRF_PRECISION_HALF_STREAMS (default) the ray kernel reads segment
+ *                              lengths and gathers ln q as fp16 (round to
+ *                              nearest); every product, prefix and sum
+ *                              stays fp32 (fp64 on long rays), the messages
+ *                              fp32
+ *   MRF_PRECISION_FP32         segment lengths and ln q in fp32
  * Changing it keeps the map's state. */
 #define MRF_PRECISION_FP32 0
 #define MRF_PRECISION_HALF_STREAMS 1

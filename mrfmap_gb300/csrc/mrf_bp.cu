@@ -478,9 +478,10 @@ template <int kMinBlocks, int kPol, int kPf, bool kReg, typename TL, typename TQ
 __global__ void __launch_bounds__(kRayWarps * 32, kMinBlocks) k_ray_bp(const RayMeta* __restrict__ queue,
                                                            uint32_t n_rays,
                                                            const uint32_t* __restrict__ rstart,
-                                                           uint32_t nreg,
-                                                           const RayMeta* __restrict__ left,
-                                                           uint32_t n_left,
+                                                           uint32_t nreg, uint32_t rper,
+                                                           const uint32_t* __restrict__ lprefix,
+                                                           const uint32_t* __restrict__ lbase,
+                                                           uint32_t nlv,
                                                            uint32_t* __restrict__ lcounter,
                                                            uint32_t* __restrict__ counter,
                                                            const uint32_t* __restrict__ inc_pair,
@@ -497,12 +498,15 @@ __global__ void __launch_bounds__(kRayWarps * 32, kMinBlocks) k_ray_bp(const Ray
       ray_bp_warp<double, kPol, kPf, TL, TQ>(me, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
   };
   if constexpr (kReg) {
-    // counter[r]: tickets of region r; rstart[r] .. rstart[r + 1] its home
-    // rays.  Block b serves regions b mod G, + G, ... (G = min(grid,
-    // regions): every region has a home block).
+    // counter[r]: tickets of region r, whose home rays are positions
+    // rstart[q (rper + 1) + rr] .. rstart[q (rper + 1) + rr + 1] (view q =
+    // r / rper, rr = r % rper).  Block b serves regions b mod G, + G, ...
+    // (G = min(grid, regions): every region has a home block).
     const uint32_t G = min(gridDim.x, nreg);
     for (uint32_t r = blockIdx.x % G; r < nreg; r += G) {
-      const uint32_t a = rstart[r], nr = rstart[r + 1] - a;
+      const uint32_t q = r / rper;
+      const uint32_t* rs = rstart + (size_t)q * (rper + 1) + (r - q * rper);
+      const uint32_t a = rs[0], nr = rs[1] - a;
       for (;;) {
         uint32_t idx = 0;
         if (lane == 0) idx = atomicAdd(counter + r, 1u);
@@ -511,12 +515,27 @@ __global__ void __launch_bounds__(kRayWarps * 32, kMinBlocks) k_ray_bp(const Ray
         ray(queue[a + idx]);
       }
     }
+    // the views' leftovers, one ticket counter over all of them: ticket t
+    // is view q's (t - lprefix[q])-th leftover for the last q with
+    // lprefix[q] <= t
+    const uint32_t n_left = lprefix[nlv];
     for (;;) {
-      uint32_t idx = 0;
-      if (lane == 0) idx = atomicAdd(lcounter, 1u);
-      idx = __shfl_sync(kFull, idx, 0);
-      if (idx >= n_left) break;
-      ray(left[idx]);
+      uint32_t pos = 0xFFFFFFFFu;
+      if (lane == 0) {
+        const uint32_t t = atomicAdd(lcounter, 1u);
+        if (t < n_left) {
+          uint32_t lo = 0, hi = nlv;
+          while (hi - lo > 1) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (lprefix[mid] <= t) lo = mid;
+            else hi = mid;
+          }
+          pos = lbase[lo] + (t - lprefix[lo]);
+        }
+      }
+      pos = __shfl_sync(kFull, pos, 0);
+      if (pos == 0xFFFFFFFFu) break;
+      ray(queue[pos]);
     }
   } else {
     for (;;) {
@@ -1043,14 +1062,14 @@ cudaError_t launch_ray_bp(const BpArrays& a, const RayWork& w, int fix_reset, in
   case id:                                                                                        \
     if (a.half_streams)                                                                           \
       k_ray_bp<mb, pol, pf, (sc > 0), __half, __half><<<grid, kRayWarps * 32, 0, s>>>(            \
-          sc == 0 ? w.queue : w.region, w.n_rays, w.rstart, w.nreg, w.left, w.n_left, w.lcounter,  \
-          sc == 0 ? w.counter : w.rcounter, a.inc_pair, a.inc_len16, a.inc_mu, a.pair_lnq16,        \
-          a.inc_pl, fix_reset);                                                                   \
+          sc == 0 ? w.queue : w.region, w.n_rays, w.rstart, w.nreg, w.rper, w.lprefix, w.lbase,    \
+          w.nlv, w.lcounter, sc == 0 ? w.counter : w.rcounter, a.inc_pair, a.inc_len16, a.inc_mu,  \
+          a.pair_lnq16, a.inc_pl, fix_reset);                                                     \
     else                                                                                          \
       k_ray_bp<mb, pol, pf, (sc > 0), float, float><<<grid, kRayWarps * 32, 0, s>>>(              \
-          sc == 0 ? w.queue : w.region, w.n_rays, w.rstart, w.nreg, w.left, w.n_left, w.lcounter,  \
-          sc == 0 ? w.counter : w.rcounter, a.inc_pair, a.inc_len, a.inc_mu, a.pair_lnq, a.inc_pl,  \
-          fix_reset);                                                                             \
+          sc == 0 ? w.queue : w.region, w.n_rays, w.rstart, w.nreg, w.rper, w.lprefix, w.lbase,    \
+          w.nlv, w.lcounter, sc == 0 ? w.counter : w.rcounter, a.inc_pair, a.inc_len, a.inc_mu,    \
+          a.pair_lnq, a.inc_pl, fix_reset);                                                       \
     break;
     MRF_RAY_VARIANTS(X)
 #undef X
@@ -1125,6 +1144,13 @@ cudaError_t launch_active_voxels(const uint32_t* pair_vox, const float* cum, uin
   cudaError_t e = cudaMemsetAsync(flag, 0, (size_t)nvox, s);
   if (e != cudaSuccess) return e;
   if (np) k_touch_pairs<<<blocks(np, 256), 256, 0, s>>>(pair_vox, cum, np, flag, nullptr);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mark_active(const uint32_t* pair_vox, const float* cum, uint32_t np, uint8_t* flag,
+                               cudaStream_t s) {
+  if (!np) return cudaSuccess;
+  k_touch_pairs<<<blocks(np, 256), 256, 0, s>>>(pair_vox, cum, np, flag, nullptr);
   return cudaGetLastError();
 }
 

@@ -72,22 +72,29 @@ __global__ void k_activate(Geom g, Pose P, const float* __restrict__ depth, int 
   }
   if (inside) mark_point(g, pv[0], pv[1], pv[2], flags);
   if (policy == 1) {
+    // every brick the ray crosses up to the brick run where the Pre pass
+    // stops (the trace's test: at the exit s of a run's last voxel,
+    // s + bias(s) > d + 3 sigma(s)).  The trace then meets only bricks its
+    // own view activated before its stop, so bricks other views activate
+    // later never change this view's lists.
     const float* sg = lut_at(g, g.sigma, x, y);
-    float lim = fa(d, fm(3.0f, poly_f(sg, g.lookup_n, d)));
+    const float* bs = lut_at(g, g.bias, x, y);
+    const int n = g.lookup_n;
     Ray ray;
     ray_setup(g, P, x, y, ray);
     Dda r;
     if (dda_init(r, g, ray)) {
       int vx, vy, vz;
-      float l, tin, te;
+      float l, tin, te, s_last = 0.0f;
       int64_t cur = -1;
       while (dda_next(r, g, vx, vy, vz, l, tin, te)) {
-        if (fm(tin, ray.mult) >= lim) break;
         int64_t lin = brick_lin(g, vx, vy, vz);
         if (lin != cur) {
+          if (cur >= 0 && fa(s_last, poly_f(bs, n, s_last)) > fa(d, fm(3.0f, poly_f(sg, n, s_last)))) break;
           flags[lin] = 1;
           cur = lin;
         }
+        s_last = fm(te, ray.mult);
       }
     }
   }
@@ -282,6 +289,16 @@ __global__ void __launch_bounds__(kThreads, 4)
   const int padded = (n_pre + 3) & ~3;
   if (!EMIT) {
     counts[pix] = (uint32_t)padded;
+    if (meta) {
+      // the view's stored records: does this trace still give the same list?
+      const int kdyn = (kmu >= 0 && kmu < n_post) ? kmu : n_post;
+      const RayMeta o = meta[pix];
+      const uint32_t flags = (gate ? 1u : 0u) | ((uint32_t)kdyn << 16);
+      if (o.n_pre != (uint16_t)n_pre || o.n_post != (uint16_t)n_post ||
+          o.r0 != (uint16_t)(r0 >= 0 ? r0 : n_pre) || o.rinf != (uint16_t)(r0 >= 0 ? r0 : run_start) ||
+          o.flags != flags)
+        err[1] = 1;
+    }
   } else {
     // the last group, completed with padding (invalid voxel, zeros)
     if (count & 3) {
@@ -379,6 +396,15 @@ __global__ void k_loud_voxels(const RayMeta* __restrict__ meta, int64_t npix, co
   if (r >= npix) return;
   const RayMeta me = meta[r];
   for (int i = ray_kdyn(me); i < me.n_post; ++i) loud[vox[me.off + i]] = 1;
+}
+
+__global__ void k_loud_voxels_from_pairs(const RayMeta* __restrict__ meta, int64_t npix,
+                                         const uint32_t* __restrict__ inc_pair,
+                                         const uint32_t* __restrict__ pair_vox, uint8_t* __restrict__ loud) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= npix) return;
+  const RayMeta me = meta[r];
+  for (int i = ray_kdyn(me); i < me.n_post; ++i) loud[pair_vox[inc_pair[me.off + i]]] = 1;
 }
 
 // *count += number of pairs on loud voxels
@@ -618,9 +644,9 @@ cudaError_t launch_set_points(const Geom& g, const float* pts, const float* occ,
 }
 
 cudaError_t launch_trace_count(const Geom& g, const Pose& P, const float* depth, uint32_t* counts,
-                               int* err, cudaStream_t s) {
+                               int* err, cudaStream_t s, const RayMeta* check) {
   k_trace<false><<<grid_for((int64_t)g.rows * g.cols), kThreads, 0, s>>>(
-      g, P, depth, counts, nullptr, 0, nullptr, nullptr, nullptr, nullptr, nullptr, err);
+      g, P, depth, counts, nullptr, 0, const_cast<RayMeta*>(check), nullptr, nullptr, nullptr, nullptr, err);
   return cudaGetLastError();
 }
 
@@ -675,6 +701,13 @@ cudaError_t launch_loud_voxels(const RayMeta* meta, int64_t npix, const uint32_t
                                cudaStream_t s) {
   if (npix <= 0) return cudaSuccess;
   k_loud_voxels<<<grid_for(npix), kThreads, 0, s>>>(meta, npix, vox, loud);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_loud_voxels_from_pairs(const RayMeta* meta, int64_t npix, const uint32_t* inc_pair,
+                                          const uint32_t* pair_vox, uint8_t* loud, cudaStream_t s) {
+  if (npix <= 0) return cudaSuccess;
+  k_loud_voxels_from_pairs<<<grid_for(npix), kThreads, 0, s>>>(meta, npix, inc_pair, pair_vox, loud);
   return cudaGetLastError();
 }
 

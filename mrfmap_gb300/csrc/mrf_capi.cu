@@ -156,6 +156,9 @@ struct View {
   uint32_t n_loud = 0;                    // pairs on voxels with a dynamic incidence (numbered first)
   uint32_t tile_base = 0;                 // first pair of each pair-update tile
   bool retired = false;                   // out of the window: no lists, no pairs, no depth
+  // counters of the view's rays (incidences, rays, Post incidences, dynamic
+  // incidences, rays the ray kernel runs over and their Pre incidences)
+  int64_t c_npre = 0, c_nrays = 0, c_npost = 0, c_ndyn = 0, c_nrays_bp = 0, c_npre_bp = 0;
 };
 
 // pixels a view contributes to the per-pixel arrays (none once retired)
@@ -182,21 +185,30 @@ struct mrf_map {
   int ray_variant = 4;  // ray-kernel variant (mrf_autotune / mrf_set_ray_variant); 4: SM regions,
                         // pair-id prefetch, the fastest on the bench workloads
   uint32_t nreg = 1;    // SM regions per view of the region queues
-  uint32_t n_left_all = 0;
-  uint32_t region_home_n = 0;  // region_q: home rays of all regions, then the leftovers
+  // what the last build left: views with lists, per-pixel entries, the ends
+  // of the region blocks, the queues and the tiles, the bricks it saw
+  int built_views = 0;
+  int64_t npix_total = 0, queue_end = 0, tile_end = 0, carry_tiles = 0, vox_active_n = 0, n_perm_total = 0;
+  uint32_t region_end = 0;
+  int64_t bricks_at_build = -1;
+  // holes: retired views' lists still in the arenas; appended: lists added
+  // without a full build (the all-view structures of Jacobi are stale);
+  // needs_full: the next build must rebuild every view
+  bool holes = false, appended = false, needs_full = true;
+  int64_t dead_inc = 0;
   bool has_messages = false;
   std::vector<View> views;
   // arenas
   DBuf meta, inc_pair, inc_len, inc_mu, inc_pl, pair_vox, pair_m, pair_cum, pair_stat, pair_ndyn, pair_hit,
       pair_q, pair_dm, pair_seg, dperm, s_q0, s_q1, s_q2, s_q3, s_bf, s_loud, s_pv, s_sg, dpair, dseg, drun, carry, ray_order, ray_queue, region_q, rstart, rcounters, counters,
-      tile_first;
+      tile_first, lbase, lsingle, lprefix;
   uint32_t jac_tile_base = 0;
   int64_t n_inc = 0, n_pairs = 0, n_dperm = 0, n_dpairs = 0;
   // voxels with a pair past the length gate (their beliefs follow L)
   DBuf vox_active;
   // MRF_PRECISION_HALF_STREAMS: fp16 copies of the segment lengths (per
   // build) and of ln q (written by k_pair_prepare)
-  int precision = MRF_PRECISION_FP32;
+  int precision = MRF_PRECISION_HALF_STREAMS;
   DBuf inc_len16, pair_q16;
   int len16_version = -1;
   // logit(prior) + the messages of retired views, per voxel (kept once a view
@@ -366,126 +378,47 @@ void rebuild(mrf_map* m) {
   }
 }
 
-void rebuild_lists(mrf_map* m, OldPairs& old) {
-  const int V = (int)m->views.size();
-  m->g.brick_slot = m->d_slot.as<int>();
-  // per-pixel arrays of all views back to back (views may differ in size)
-  int64_t npix = 0;
-  for (View& v : m->views) {
-    v.pix_base = npix;
-    v.cam.brick_slot = m->g.brick_slot;
-    npix += view_pixels(v);
-  }
-  CK(cudaEventRecord(m->ev0, m->stream));
-  const bool remap = old.remap;
-  DBuf& old_vox = old.vox;
-  DBuf& old_m = old.m;
-  const std::vector<View>& old_views = old.views;
-  // 1. counts of every pixel of every view, one global scan -> offsets
-  u32_checked(npix, "pixel count");
-  m->s_counts.reserve((size_t)npix * 4 + 4, false, m->stream);
-  m->s_offs.reserve((size_t)npix * 4 + 4, false, m->stream);
-  for (int c = 0; c < V; ++c)
-    if (!m->views[c].retired)
-      CK(launch_trace_count(m->views[c].cam, m->views[c].pose, m->views[c].depth.as<float>(),
-                            m->s_counts.as<uint32_t>() + m->views[c].pix_base, m->s_err.as<int>(), m->stream));
-  // the total in 64 bits first: the u32 scan below wraps past 2^32, and a
-  // wrapped total would size the arenas too small for the emit pass
-  {
-    m->s_delta.reserve(64, false, m->stream);
-    CK(launch_sum_u32(m->s_counts.as<uint32_t>(), npix, m->s_delta.as<unsigned long long>(), m->stream));
-    const unsigned long long total = read1(m, m->s_delta.as<unsigned long long>());
-    check_device_err(m);
-    if (total > 0xFFFFFFF0ull)
-      fail(MRF_ERR_CAPACITY, "incidence count " + std::to_string(total) +
-                                 " exceeds the 32-bit incidence index range (fewer or smaller views per map)");
-  }
-  // sentinel 0 at the end so the scan yields the total
-  CK(cudaMemsetAsync(m->s_counts.as<uint32_t>() + npix, 0, 4, m->stream));
-  size_t tb = scan_temp_bytes((uint32_t)(npix + 1));
-  m->s_tmp.reserve(tb, false, m->stream);
-  CK(exclusive_scan_u32(m->s_tmp.p, tb, m->s_counts.as<uint32_t>(), m->s_offs.as<uint32_t>(),
-                        (uint32_t)(npix + 1), m->stream));
-  std::vector<uint32_t> bounds(V + 1);
-  for (int c = 0; c <= V; ++c)
-    CK(cudaMemcpyAsync(&bounds[c], m->s_offs.as<uint32_t>() + (c < V ? m->views[c].pix_base : npix), 4,
-                       cudaMemcpyDeviceToHost, m->stream));
-  sync(m);
-  check_device_err(m);
-  int64_t n_inc = bounds[V];
-  u32_checked(n_inc, "incidence count");
-  // 2. arenas
-  m->meta.reserve((size_t)npix * sizeof(RayMeta), false, m->stream);
-  size_t ib = (size_t)std::max<int64_t>(n_inc, 1) * 4;
-  m->inc_pair.reserve(ib, false, m->stream);
-  m->inc_len.reserve(ib, false, m->stream);
-  m->inc_mu.reserve(ib, false, m->stream);
-  m->dperm.reserve(ib, false, m->stream);
-  m->inc_pl.reserve(ib, false, m->stream);
-  m->s_vox.reserve(ib, false, m->stream);
-  m->s_rec.reserve(ib * 2, false, m->stream);
-  // 3. emit
-  for (int c = 0; c < V; ++c) {
-    View& v = m->views[c];
-    v.inc_base = bounds[c];
-    v.n_inc = bounds[c + 1] - bounds[c];
-    if (v.retired) continue;
-    CK(launch_trace_emit(v.cam, v.pose, v.depth.as<float>(), m->s_offs.as<uint32_t>() + v.pix_base, 0,
-                         m->meta.as<RayMeta>() + v.pix_base, m->s_vox.as<uint32_t>(),
-                         m->inc_len.as<float>(), m->inc_mu.as<float>(), m->s_rec.as<float2>(),
-                         m->s_err.as<int>(), m->stream));
-  }
-  // per-view counters from the ray records
-  std::vector<RayMeta> hm((size_t)npix);
-  std::vector<int64_t> nreal(V, 0);
-  int64_t nrays = 0, npost = 0, npre = 0, ndyn = 0, nrays_bp = 0, npre_bp = 0;
-  if (npix) {
-    CK(cudaMemcpyAsync(hm.data(), m->meta.p, (size_t)npix * sizeof(RayMeta), cudaMemcpyDeviceToHost,
-                       m->stream));
-    sync(m);
-    check_device_err(m);
-    for (int c = 0; c < V; ++c) {
-      const View& vc = m->views[c];
-      for (int64_t i = 0; i < view_pixels(vc); ++i) {
-        const RayMeta& r = hm[(size_t)(vc.pix_base + i)];
-        nreal[c] += r.n_pre;
-        nrays += r.n_pre > 0;
-        npost += r.n_post;
-        ndyn += r.n_post - std::min<int>(ray_kdyn(r), r.n_post);
-        if (ray_in_bp(r)) {
-          ++nrays_bp;
-          npre_bp += r.n_pre;
-        }
-      }
+// ---- per-view pieces of a build ------------------------------------------
+
+// counters of one view's rays (from its ray records on the host)
+void view_counters(View& v, const RayMeta* vm) {
+  v.c_npre = v.c_nrays = v.c_npost = v.c_ndyn = v.c_nrays_bp = v.c_npre_bp = 0;
+  const int64_t hw = view_pixels(v);
+  for (int64_t i = 0; i < hw; ++i) {
+    const RayMeta& r = vm[i];
+    v.c_npre += r.n_pre;
+    v.c_nrays += r.n_pre > 0;
+    v.c_npost += r.n_post;
+    v.c_ndyn += r.n_post - std::min<int>(ray_kdyn(r), r.n_post);
+    if (ray_in_bp(r)) {
+      ++v.c_nrays_bp;
+      v.c_npre_bp += r.n_pre;
     }
-    for (int c = 0; c < V; ++c) npre += nreal[c];
   }
-  // voxels with a dynamic incidence in any view ("loud"; the others are
-  // quiet, see enqueue_iteration)
-  m->s_loud.reserve((size_t)std::max<int64_t>(m->n_bricks * kBrickVox, 1), false, m->stream);
-  CK(cudaMemsetAsync(m->s_loud.p, 0, (size_t)std::max<int64_t>(m->n_bricks * kBrickVox, 1), m->stream));
-  CK(launch_loud_voxels(m->meta.as<RayMeta>(), npix, m->s_vox.as<uint32_t>(), m->s_loud.as<uint8_t>(),
-                        m->stream));
-  // 4. pairs per view: sort the view's incidences by voxel (stable), one
-  //    pair per run, then renumber the pairs brick-major by first visit
-  //    (mrf_build.cu, k_pair_first) and regroup the incidences in the new
-  //    pair order; pos[i] = pair-grouped position of i
-  int bits = 1;
-  while (bits < 32 && ((uint64_t)1 << bits) <= (uint64_t)(m->n_bricks * kBrickVox)) ++bits;
-  int64_t pair_total = 0, perm_total = 0, dperm_total = 0, dpair_total = 0;
-  for (int c = 0; c < V; ++c) {
-    View& v = m->views[c];
-    uint32_t n = v.n_inc;
-    uint32_t nr = (uint32_t)nreal[c];
-    v.pair_base = (uint32_t)pair_total;
-    v.perm_base = (uint32_t)perm_total;
-    v.dperm_base = (uint32_t)dperm_total;
-    v.dpair_base = (uint32_t)dpair_total;
-    v.n_pairs = 0;
-    v.n_perm = 0;
-    v.n_dperm = 0;
-    v.n_dpairs = 0;
-    if (nr == 0) continue;
+}
+
+// The pairs of view c: its incidences (at v.inc_base; voxel ids in s_vox and
+// build records in s_rec at the same positions) sorted by voxel (stable),
+// one pair per run, the pairs renumbered brick-major by first visit
+// (mrf_build.cu, k_pair_first; pairs on voxels flagged in s_loud first) and
+// the incidences regrouped in the new pair order; then the pair statistics
+// and the dynamic runs.  Numbered from the totals' current ends, which
+// advance.
+void view_pairs(mrf_map* m, int c, int bits, int64_t& pair_total, int64_t& perm_total, int64_t& dperm_total,
+                int64_t& dpair_total) {
+  View& v = m->views[c];
+  uint32_t n = v.n_inc;
+  uint32_t nr = (uint32_t)v.c_npre;
+  v.pair_base = (uint32_t)pair_total;
+  v.perm_base = (uint32_t)perm_total;
+  v.dperm_base = (uint32_t)dperm_total;
+  v.dpair_base = (uint32_t)dpair_total;
+  v.n_pairs = 0;
+  v.n_perm = 0;
+  v.n_dperm = 0;
+  v.n_dpairs = 0;
+  v.n_loud = 0;
+  if (nr == 0) return;
     m->s_k0.reserve((size_t)n * 4 + 4, false, m->stream);
     m->s_k1.reserve((size_t)n * 4 + 4, false, m->stream);
     m->s_v0.reserve((size_t)n * 4 + 4, false, m->stream);
@@ -609,161 +542,366 @@ void rebuild_lists(mrf_map* m, OldPairs& old) {
     perm_total += nr;
     dperm_total += nd;
     dpair_total += ndp;
+}
+
+// A view's rays in the SM-affine schedule: R regions of consecutive pixels
+// holding equal shares of the view's Pre incidences; a region's home rays
+// (its longest rays up to kHomeShare of its incidences, longest first) are
+// taken by the blocks homed on it, every region's remaining short rays go to
+// the view's leftover queue (longest first) that the blocks drain
+// afterwards, which evens out the regions' finishing times (home shares of
+// 60, 75 and 85 % measured: 75 % best on the bench workloads).  Built on
+// the host in linear time: a counting sort by length feeds the regions'
+// buckets in order, so each bucket is longest first.  Pixel indices are
+// absolute (v.pix_base + i); starts are positions in home.
+struct RegionLists {
+  std::vector<uint32_t> home, left, starts;
+};
+constexpr int64_t kHomeShare = 75;  // per cent of a region's incidences taken by its home blocks
+
+void region_lists(const View& v, const RayMeta* vm, int R, RegionLists& out) {
+  const int64_t hw = view_pixels(v);
+  std::vector<uint32_t> lcount(65536, 0u), reg((size_t)hw, 0u), bucket_off((size_t)R + 1, 0u);
+  int64_t work = 0;
+  for (int64_t i = 0; i < hw; ++i) {
+    if (!ray_in_bp(vm[i])) continue;
+    work += vm[i].n_pre;
+    ++lcount[65535 - vm[i].n_pre];
   }
-  // ray queues: per view, the active rays longest first
+  // region of each active pixel: equal shares of the view's work
+  int64_t acc = 0;
+  for (int64_t i = 0; i < hw; ++i) {
+    if (!ray_in_bp(vm[i])) continue;
+    const uint32_t r = (uint32_t)std::min<int64_t>(R - 1, acc * R / std::max<int64_t>(work, 1));
+    reg[(size_t)i] = r;
+    ++bucket_off[r + 1];
+    acc += vm[i].n_pre;
+  }
+  for (int r = 0; r < R; ++r) bucket_off[r + 1] += bucket_off[r];
+  // the view's active rays longest first (pixel order within a length)
+  uint32_t pos = 0;
+  for (int k = 0; k < 65536; ++k) {
+    const uint32_t c0 = lcount[k];
+    lcount[k] = pos;
+    pos += c0;
+  }
+  std::vector<uint32_t> lsorted(pos), buckets(pos), fill(bucket_off.begin(), bucket_off.end() - 1);
+  for (int64_t i = 0; i < hw; ++i)
+    if (ray_in_bp(vm[i])) lsorted[lcount[65535 - vm[i].n_pre]++] = (uint32_t)i;
+  for (uint32_t i : lsorted) buckets[fill[reg[i]]++] = i;
+  // home = each region's longest rays up to kHomeShare of its work
+  std::vector<uint8_t> is_home((size_t)hw, 0);
+  out.home.reserve(pos);
+  for (int r = 0; r < R; ++r) {
+    int64_t rw = 0, hwk = 0;
+    for (uint32_t k = bucket_off[r]; k < bucket_off[r + 1]; ++k) rw += vm[buckets[k]].n_pre;
+    out.starts.push_back((uint32_t)out.home.size());
+    for (uint32_t k = bucket_off[r]; k < bucket_off[r + 1] && hwk * 100 < rw * kHomeShare; ++k) {
+      const uint32_t i = buckets[k];
+      is_home[i] = 1;
+      hwk += vm[i].n_pre;
+      out.home.push_back((uint32_t)(v.pix_base + i));
+    }
+  }
+  // leftovers longest first
+  for (uint32_t i : lsorted)
+    if (!is_home[i]) out.left.push_back((uint32_t)(v.pix_base + i));
+}
+
+// region lists of several views in parallel host threads (at most one per
+// core, the views taken in turn); hm holds the ray records of every view in
+// `views` at their pix_base
+void region_lists_parallel(mrf_map* m, const std::vector<int>& views, const std::vector<RayMeta>& hm,
+                           int64_t hm_base, std::vector<RegionLists>& lists) {
+  const int R = std::max(1, m->num_sms);
+  const int nv = (int)views.size();
+  const int nt = std::max(1, std::min<int>(nv, (int)std::thread::hardware_concurrency()));
+  std::atomic<int> next{0};
+  std::vector<std::thread> pool;
+  std::vector<char> failed((size_t)nv, 0);
+  for (int t = 0; t < nt; ++t)
+    pool.emplace_back([&] {
+      for (int k = next++; k < nv; k = next++) {
+        try {
+          const View& v = m->views[views[k]];
+          region_lists(v, hm.data() + (v.pix_base - hm_base), R, lists[(size_t)views[k]]);
+        } catch (...) {
+          failed[(size_t)k] = 1;
+        }
+      }
+    });
+  for (auto& t : pool) t.join();
+  for (char f : failed)
+    if (f) fail(MRF_ERR_OOM, "host memory for the region queues");
+}
+
+// Per-view blocks [home rays][leftovers] of views (in that order) laid out
+// in region_q from position `at` on, their ray records gathered from meta;
+// per view: rstart row c*(R+1) (R region starts and the end of the home
+// block, absolute), lbase[c] (first leftover) and lsingle {0, n_left} at 2c.
+// Returns the end position.
+uint32_t region_blocks(mrf_map* m, const std::vector<int>& views, const std::vector<RegionLists>& lists,
+                       uint32_t at) {
+  const int R = std::max(1, m->num_sms);
+  const int V = (int)m->views.size();
+  m->rstart.reserve((size_t)V * (R + 1) * 4 + 4, true, m->stream);
+  m->lbase.reserve((size_t)V * 4 + 4, true, m->stream);
+  m->lsingle.reserve((size_t)V * 8 + 8, true, m->stream);
+  std::vector<uint32_t> pix;
+  for (int c : views) {
+    View& v = m->views[c];
+    const RegionLists& l = lists[(size_t)c];
+    std::vector<uint32_t> row((size_t)R + 1);
+    const uint32_t b = at + (uint32_t)pix.size();
+    for (int r = 0; r < R; ++r) row[(size_t)r] = b + (r < (int)l.starts.size() ? l.starts[(size_t)r] : 0u);
+    row[(size_t)R] = b + (uint32_t)l.home.size();
+    v.left_base = b + (uint32_t)l.home.size();
+    v.n_left = (uint32_t)l.left.size();
+    pix.insert(pix.end(), l.home.begin(), l.home.end());
+    pix.insert(pix.end(), l.left.begin(), l.left.end());
+    const uint32_t ls[2] = {0u, v.n_left};
+    CK(cudaMemcpyAsync(m->rstart.as<uint32_t>() + (size_t)c * (R + 1), row.data(), (size_t)(R + 1) * 4,
+                       cudaMemcpyHostToDevice, m->stream));
+    CK(cudaMemcpyAsync(m->lbase.as<uint32_t>() + c, &v.left_base, 4, cudaMemcpyHostToDevice, m->stream));
+    CK(cudaMemcpyAsync(m->lsingle.as<uint32_t>() + 2 * (size_t)c, ls, 8, cudaMemcpyHostToDevice, m->stream));
+    sync(m);  // row and ls are host temporaries
+  }
+  const uint32_t end = at + (uint32_t)pix.size();
+  m->region_q.reserve(std::max<size_t>(end, 1) * sizeof(RayMeta), true, m->stream);
+  if (!pix.empty()) {
+    m->ray_order.reserve(pix.size() * 4, false, m->stream);
+    CK(cudaMemcpyAsync(m->ray_order.p, pix.data(), pix.size() * 4, cudaMemcpyHostToDevice, m->stream));
+    CK(launch_ray_queue(m->meta.as<RayMeta>(), m->ray_order.as<uint32_t>(), (uint32_t)pix.size(),
+                        m->region_q.as<RayMeta>() + at, m->stream));
+    sync(m);  // the host vector goes out of scope
+  }
+  return end;
+}
+
+// the leftover prefix of every view (V + 1 entries) for a launch over all
+// views (Jacobi)
+void leftover_prefix(mrf_map* m) {
+  const int V = (int)m->views.size();
+  std::vector<uint32_t> pre((size_t)V + 1, 0u);
+  for (int c = 0; c < V; ++c) pre[(size_t)c + 1] = pre[(size_t)c] + m->views[c].n_left;
+  m->lprefix.reserve(pre.size() * 4, false, m->stream);
+  CK(cudaMemcpyAsync(m->lprefix.p, pre.data(), pre.size() * 4, cudaMemcpyHostToDevice, m->stream));
+  sync(m);
+}
+
+// view c's active rays longest first (17-bit key radix sort on the GPU),
+// their records copied into queue order at ray_queue + v.order_base
+void view_ray_queue(mrf_map* m, int c, const RayMeta* vm) {
+  View& v = m->views[c];
+  const int64_t hw = view_pixels(v);
+  int64_t act = 0;
+  for (int64_t i = 0; i < hw; ++i) act += ray_in_bp(vm[i]);
+  v.n_active = (uint32_t)act;
+  if (hw == 0) return;
+  m->s_k0.reserve((size_t)hw * 4 + 4, false, m->stream);
+  m->s_k1.reserve((size_t)hw * 4 + 4, false, m->stream);
+  m->s_v0.reserve((size_t)hw * 4 + 4, false, m->stream);
+  m->s_v1.reserve((size_t)hw * 4 + 4, false, m->stream);
+  CK(launch_ray_keys(m->meta.as<RayMeta>() + v.pix_base, (uint32_t)hw, m->s_k0.as<uint32_t>(),
+                     m->s_v0.as<uint32_t>(), m->stream));
+  size_t t = sort_temp_bytes((uint32_t)hw, 17);
+  m->s_tmp.reserve(t, false, m->stream);
+  CK(sort_pairs_u32(m->s_tmp.p, t, m->s_k0.as<uint32_t>(), m->s_k1.as<uint32_t>(), m->s_v0.as<uint32_t>(),
+                    m->s_v1.as<uint32_t>(), (uint32_t)hw, 17, m->stream));
+  CK(launch_ray_queue(m->meta.as<RayMeta>() + v.pix_base, m->s_v1.as<uint32_t>(), (uint32_t)act,
+                      m->ray_queue.as<RayMeta>() + v.order_base, m->stream));
+}
+
+// the statistics of the live views
+void stats_from_views(mrf_map* m) {
+  int64_t nrays = 0, npre = 0, npost = 0, ndyn = 0, nrays_bp = 0, npre_bp = 0, np = 0, ndp = 0;
+  for (const View& v : m->views) {
+    if (v.retired) continue;
+    nrays += v.c_nrays;
+    npre += v.c_npre;
+    npost += v.c_npost;
+    ndyn += v.c_ndyn;
+    nrays_bp += v.c_nrays_bp;
+    npre_bp += v.c_npre_bp;
+    np += v.n_pairs;
+    ndp += v.n_dpairs;
+  }
+  m->stats.n_rays = nrays;
+  m->stats.n_inc_pre = npre;
+  m->stats.n_inc_post = npost;
+  m->stats.n_pairs = np;
+  m->stats.n_inc_dyn = ndyn;
+  m->stats.n_pairs_dyn = ndp;
+  m->stats.n_rays_bp = nrays_bp;
+  m->stats.n_inc_pre_bp = npre_bp;
+}
+
+int voxel_id_bits(const mrf_map* m) {
+  int bits = 1;
+  while (bits < 32 && ((uint64_t)1 << bits) <= (uint64_t)(m->n_bricks * kBrickVox)) ++bits;
+  return bits;
+}
+
+// Incidence counts of the given views: view k's pixel counts at
+// s_counts + coff[k] (its hw entries and a sentinel) and their exclusive scan
+// at s_offs + coff[k]; each view's total is summed in 64 bits and the running
+// total (from `before` incidences already in the arenas) checked against the
+// 32-bit index range before any offset is used.  Returns the views' counts.
+std::vector<uint32_t> count_views(mrf_map* m, const std::vector<int>& views, int64_t before,
+                                  std::vector<int64_t>& coff) {
+  int64_t tot_px = 0;
+  coff.assign(views.size(), 0);
+  for (size_t k = 0; k < views.size(); ++k) {
+    coff[k] = tot_px;
+    tot_px += view_pixels(m->views[views[k]]) + 1;
+  }
+  m->s_counts.reserve((size_t)std::max<int64_t>(tot_px, 1) * 4, false, m->stream);
+  m->s_offs.reserve((size_t)std::max<int64_t>(tot_px, 1) * 4, false, m->stream);
+  m->s_delta.reserve(64, false, m->stream);
+  std::vector<uint32_t> n(views.size(), 0u);
+  unsigned long long run = (unsigned long long)before;
+  for (size_t k = 0; k < views.size(); ++k) {
+    const View& v = m->views[views[k]];
+    const int64_t hw = view_pixels(v);
+    uint32_t* cnt = m->s_counts.as<uint32_t>() + coff[k];
+    if (hw) CK(launch_trace_count(v.cam, v.pose, v.depth.as<float>(), cnt, m->s_err.as<int>(), m->stream));
+    CK(launch_sum_u32(cnt, hw, m->s_delta.as<unsigned long long>(), m->stream));
+    const unsigned long long total = read1(m, m->s_delta.as<unsigned long long>());
+    run += total;
+    if (run > 0xFFFFFFF0ull)
+      fail(MRF_ERR_CAPACITY, "incidence count " + std::to_string(run) +
+                                 " exceeds the 32-bit incidence index range (fewer or smaller views per map)");
+    CK(cudaMemsetAsync(cnt + hw, 0, 4, m->stream));
+    size_t tb = scan_temp_bytes((uint32_t)(hw + 1));
+    m->s_tmp.reserve(tb, false, m->stream);
+    CK(exclusive_scan_u32(m->s_tmp.p, tb, cnt, m->s_offs.as<uint32_t>() + coff[k], (uint32_t)(hw + 1),
+                          m->stream));
+    n[k] = (uint32_t)total;
+  }
+  check_device_err(m);
+  return n;
+}
+
+// the emit pass of view c at v.inc_base (pix_off: its scanned counts)
+void emit_view(mrf_map* m, int c, const uint32_t* pix_off) {
+  View& v = m->views[c];
+  CK(launch_trace_emit(v.cam, v.pose, v.depth.as<float>(), pix_off, v.inc_base,
+                       m->meta.as<RayMeta>() + v.pix_base, m->s_vox.as<uint32_t>() + v.inc_base,
+                       m->inc_len.as<float>() + v.inc_base, m->inc_mu.as<float>() + v.inc_base,
+                       m->s_rec.as<float2>() + v.inc_base, m->s_err.as<int>(), m->stream));
+}
+
+// tiles of view c's pair update, from position tb of tile_first
+void view_tiles(mrf_map* m, int c, uint32_t tb) {
+  View& v = m->views[c];
+  v.tile_base = tb;
+  CK(launch_tile_first(m->dseg.as<uint32_t>(), v.dpair_base, v.dpair_base + v.n_dpairs, v.dperm_base,
+                       v.dperm_base + v.n_dperm, m->tile_first.as<uint32_t>() + tb, m->stream));
+}
+
+void rebuild_lists(mrf_map* m, OldPairs& old) {
+  const int V = (int)m->views.size();
+  m->g.brick_slot = m->d_slot.as<int>();
+  // per-pixel arrays of all live views back to back (views may differ in size)
+  int64_t npix = 0;
+  for (View& v : m->views) {
+    v.pix_base = npix;
+    v.cam.brick_slot = m->g.brick_slot;
+    npix += view_pixels(v);
+  }
+  u32_checked(npix, "pixel count");
+  CK(cudaEventRecord(m->ev0, m->stream));
+  const bool remap = old.remap;
+  DBuf& old_vox = old.vox;
+  DBuf& old_m = old.m;
+  const std::vector<View>& old_views = old.views;
+  // 1. counts of every pixel of every live view, one scan per view ->
+  //    offsets (totals in 64 bits: a wrapped total would size the arenas
+  //    too small for the emit pass)
+  std::vector<int> live;
+  for (int c = 0; c < V; ++c) {
+    m->views[c].n_inc = 0;
+    if (!m->views[c].retired) live.push_back(c);
+  }
+  std::vector<int64_t> coff;
+  const std::vector<uint32_t> cnt = count_views(m, live, 0, coff);
+  int64_t n_inc = 0;
+  for (int c = 0; c < V; ++c) {
+    View& v = m->views[c];
+    v.inc_base = (uint32_t)n_inc;
+    const auto it = std::find(live.begin(), live.end(), c);
+    if (it != live.end()) {
+      v.n_inc = cnt[(size_t)(it - live.begin())];
+      n_inc += v.n_inc;
+    }
+  }
+  // 2. arenas
   {
-    int64_t hw_max = 0;
-    for (const View& v : m->views) hw_max = std::max<int64_t>(hw_max, view_pixels(v));
-    m->ray_order.reserve((size_t)std::max<int64_t>(npix, 1) * 4, false, m->stream);
+    const size_t ib = (size_t)std::max<int64_t>(n_inc, 1) * 4;
+    m->meta.reserve((size_t)std::max<int64_t>(npix, 1) * sizeof(RayMeta), false, m->stream);
+    m->inc_pair.reserve(ib, false, m->stream);
+    m->inc_len.reserve(ib, false, m->stream);
+    m->inc_mu.reserve(ib, false, m->stream);
+    m->dperm.reserve(ib, false, m->stream);
+    m->inc_pl.reserve(ib, false, m->stream);
+    m->s_vox.reserve(ib, false, m->stream);
+    m->s_rec.reserve(ib * 2, false, m->stream);
+  }
+  // 3. emit
+  for (size_t k = 0; k < live.size(); ++k) emit_view(m, live[k], m->s_offs.as<uint32_t>() + coff[k]);
+  // per-view counters from the ray records
+  std::vector<RayMeta> hm((size_t)npix);
+  if (npix) {
+    CK(cudaMemcpyAsync(hm.data(), m->meta.p, (size_t)npix * sizeof(RayMeta), cudaMemcpyDeviceToHost,
+                       m->stream));
+    sync(m);
+    check_device_err(m);
+  }
+  for (View& v : m->views) view_counters(v, hm.data() + v.pix_base);
+  // voxels with a dynamic incidence in any view ("loud"; the others are
+  // quiet, see enqueue_iteration)
+  m->s_loud.reserve((size_t)std::max<int64_t>(m->n_bricks * kBrickVox, 1), false, m->stream);
+  CK(cudaMemsetAsync(m->s_loud.p, 0, (size_t)std::max<int64_t>(m->n_bricks * kBrickVox, 1), m->stream));
+  CK(launch_loud_voxels(m->meta.as<RayMeta>(), npix, m->s_vox.as<uint32_t>(), m->s_loud.as<uint8_t>(),
+                        m->stream));
+  // 4. pairs per view
+  const int bits = voxel_id_bits(m);
+  int64_t pair_total = 0, perm_total = 0, dperm_total = 0, dpair_total = 0;
+  for (int c = 0; c < V; ++c) view_pairs(m, c, bits, pair_total, perm_total, dperm_total, dpair_total);
+  // 5. ray queues: per view the active rays longest first, and the
+  //    SM-affine region blocks
+  {
     m->ray_queue.reserve((size_t)std::max<int64_t>(npix, 1) * sizeof(RayMeta), false, m->stream);
-    m->s_k0.reserve((size_t)hw_max * 4 + 4, false, m->stream);
-    m->s_k1.reserve((size_t)hw_max * 4 + 4, false, m->stream);
-    m->s_v0.reserve((size_t)hw_max * 4 + 4, false, m->stream);
     int64_t base = 0;
     for (int c = 0; c < V; ++c) {
       View& v = m->views[c];
-      const int64_t hw = view_pixels(v);
-      int64_t act = 0;
-      for (int64_t i = 0; i < hw; ++i) act += ray_in_bp(hm[(size_t)(v.pix_base + i)]);
       v.order_base = (uint32_t)base;
-      v.n_active = (uint32_t)act;
-      if (hw == 0) continue;
-      CK(launch_ray_keys(m->meta.as<RayMeta>() + v.pix_base, (uint32_t)hw, m->s_k0.as<uint32_t>(),
-                         m->s_v0.as<uint32_t>(), m->stream));
-      size_t t = sort_temp_bytes((uint32_t)hw, 17);
-      m->s_tmp.reserve(t, false, m->stream);
-      CK(sort_pairs_u32(m->s_tmp.p, t, m->s_k0.as<uint32_t>(), m->s_k1.as<uint32_t>(),
-                        m->s_v0.as<uint32_t>(), m->ray_order.as<uint32_t>() + base, (uint32_t)hw, 17,
-                        m->stream));
-      // queue records in queue order
-      CK(launch_ray_queue(m->meta.as<RayMeta>() + v.pix_base, m->ray_order.as<uint32_t>() + base,
-                          (uint32_t)act, m->ray_queue.as<RayMeta>() + base, m->stream));
-      base += act;
+      view_ray_queue(m, c, hm.data() + v.pix_base);
+      base += v.n_active;
     }
+    m->queue_end = base;
     m->counters.reserve((size_t)(V + 1) * 4, false, m->stream);
-    // SM-affine region queues: per view, R = SM count regions of
-    // consecutive pixels holding equal shares of the view's Pre incidences.
-    // A region's home rays (its longest rays up to kHomeShare of its
-    // incidences, longest first) are taken by the blocks homed on it; every region's remaining short rays go to one leftover
-    // queue of the view (longest first) that the blocks drain afterwards,
-    // which evens out the regions' finishing times (home shares of 60, 75
-    // and 85 % measured: 75 % best on the bench workloads).  rstart (flat over the views,
-    // V * R + 1 entries) holds each region's first home position.
     const int R = std::max(1, m->num_sms);
-    constexpr int64_t kHomeShare = 75;  // per cent of a region's incidences taken by its home blocks
-    // per view, in parallel host threads, in linear time: a counting sort
-    // by length (longest first) feeds the regions' buckets in order, so each
-    // bucket is longest first
-    struct RegionLists {
-      std::vector<uint32_t> home, left, starts;  // starts: view-local home positions
-    };
+    m->nreg = (uint32_t)R;
+    m->rcounters.reserve(((size_t)2 * V * R + 2 * (size_t)V + 2) * 4, false, m->stream);
     std::vector<RegionLists> lists((size_t)V);
-    auto build_view = [&](int c) {
-      const View& v = m->views[c];
-      RegionLists& out = lists[(size_t)c];
-      const int64_t hw = view_pixels(v);
-      const RayMeta* vm = hm.data() + v.pix_base;
-      std::vector<uint32_t> lcount(65536, 0u), reg((size_t)hw, 0u), bucket_off((size_t)R + 1, 0u);
-      int64_t work = 0;
-      for (int64_t i = 0; i < hw; ++i) {
-        if (!ray_in_bp(vm[i])) continue;
-        work += vm[i].n_pre;
-        ++lcount[65535 - vm[i].n_pre];
-      }
-      // region of each active pixel: equal shares of the view's work
-      int64_t acc = 0;
-      for (int64_t i = 0; i < hw; ++i) {
-        if (!ray_in_bp(vm[i])) continue;
-        const uint32_t r = (uint32_t)std::min<int64_t>(R - 1, acc * R / std::max<int64_t>(work, 1));
-        reg[(size_t)i] = r;
-        ++bucket_off[r + 1];
-        acc += vm[i].n_pre;
-      }
-      for (int r = 0; r < R; ++r) bucket_off[r + 1] += bucket_off[r];
-      // the view's active rays longest first (pixel order within a length)
-      uint32_t pos = 0;
-      for (int k = 0; k < 65536; ++k) {
-        const uint32_t c0 = lcount[k];
-        lcount[k] = pos;
-        pos += c0;
-      }
-      std::vector<uint32_t> lsorted(pos), buckets(pos), fill(bucket_off.begin(), bucket_off.end() - 1);
-      for (int64_t i = 0; i < hw; ++i)
-        if (ray_in_bp(vm[i])) lsorted[lcount[65535 - vm[i].n_pre]++] = (uint32_t)i;
-      for (uint32_t i : lsorted) buckets[fill[reg[i]]++] = i;
-      // home = each region's longest rays up to kHomeShare of its work
-      std::vector<uint8_t> is_home((size_t)hw, 0);
-      out.home.reserve(pos);
-      for (int r = 0; r < R; ++r) {
-        int64_t rw = 0, hwk = 0;
-        for (uint32_t k = bucket_off[r]; k < bucket_off[r + 1]; ++k) rw += vm[buckets[k]].n_pre;
-        out.starts.push_back((uint32_t)out.home.size());
-        for (uint32_t k = bucket_off[r]; k < bucket_off[r + 1] && hwk * 100 < rw * kHomeShare; ++k) {
-          const uint32_t i = buckets[k];
-          is_home[i] = 1;
-          hwk += vm[i].n_pre;
-          out.home.push_back((uint32_t)(v.pix_base + i));
-        }
-      }
-      // leftovers longest first
-      for (uint32_t i : lsorted)
-        if (!is_home[i]) out.left.push_back((uint32_t)(v.pix_base + i));
-    };
-    {
-      // at most one thread per host core; the views are taken in turn
-      const int nt = std::max(1, std::min<int>(V, (int)std::thread::hardware_concurrency()));
-      std::atomic<int> next{0};
-      std::vector<std::thread> pool;
-      std::vector<char> failed((size_t)V, 0);
-      for (int t = 0; t < nt; ++t)
-        pool.emplace_back([&] {
-          for (int c = next++; c < V; c = next++) {
-            try {
-              build_view(c);
-            } catch (...) {
-              failed[(size_t)c] = 1;
-            }
-          }
-        });
-      for (auto& t : pool) t.join();
-      for (char f : failed)
-        if (f) fail(MRF_ERR_OOM, "host memory for the region queues");
-    }
-    std::vector<uint32_t> rq_long, rq_left, rst;
-    rq_long.reserve((size_t)base);
-    rq_left.reserve((size_t)base);
-    rst.reserve((size_t)V * R + 1);
+    region_lists_parallel(m, live, hm, 0, lists);
+    // retired views: empty rows
     for (int c = 0; c < V; ++c) {
       View& v = m->views[c];
-      const RegionLists& l = lists[(size_t)c];
-      for (uint32_t st : l.starts) rst.push_back((uint32_t)rq_long.size() + st);
-      rq_long.insert(rq_long.end(), l.home.begin(), l.home.end());
-      v.left_base = (uint32_t)rq_left.size();
-      v.n_left = (uint32_t)l.left.size();
-      rq_left.insert(rq_left.end(), l.left.begin(), l.left.end());
+      if (v.retired) {
+        v.n_left = 0;
+        v.left_base = 0;
+      }
     }
-    rst.push_back((uint32_t)rq_long.size());
-    m->rstart.reserve(rst.size() * 4, false, m->stream);
-    m->rcounters.reserve(((size_t)2 * V * R + 2 * (size_t)V + 2) * 4, false, m->stream);
-    m->nreg = (uint32_t)R;
-    m->n_left_all = (uint32_t)rq_left.size();
-    CK(cudaMemcpyAsync(m->rstart.p, rst.data(), rst.size() * 4, cudaMemcpyHostToDevice, m->stream));
-    // home rays and leftovers in one array: one upload of the pixel
-    // indices (into ray_order, free again once the longest-first queues are
-    // gathered) and one gather of their records
-    m->region_home_n = (uint32_t)rq_long.size();
-    rq_long.insert(rq_long.end(), rq_left.begin(), rq_left.end());
-    m->region_q.reserve(std::max<size_t>(rq_long.size(), 1) * sizeof(RayMeta), false, m->stream);
-    if (!rq_long.empty()) {
-      CK(cudaMemcpyAsync(m->ray_order.p, rq_long.data(), rq_long.size() * 4, cudaMemcpyHostToDevice,
-                         m->stream));
-      CK(launch_ray_queue(m->meta.as<RayMeta>(), m->ray_order.as<uint32_t>(), (uint32_t)rq_long.size(),
-                          m->region_q.as<RayMeta>(), m->stream));
-      sync(m);  // the host vector goes out of scope
-    }
+    std::vector<int> all;
+    for (int c = 0; c < V; ++c) all.push_back(c);
+    m->region_end = region_blocks(m, all, lists, 0u);
+    leftover_prefix(m);
   }
   m->n_inc = n_inc;
   m->n_pairs = pair_total;
+  m->n_perm_total = perm_total;
   m->n_dperm = dperm_total;
   m->n_dpairs = dpair_total;
   size_t pb = (size_t)std::max<int64_t>(pair_total + 1, 1);
@@ -788,22 +926,20 @@ void rebuild_lists(mrf_map* m, OldPairs& old) {
     // first pair of every tile, per view (Gauss-Seidel) and over all views
     // (Jacobi)
     int64_t tiles = (int64_t)pair_update_tiles((uint32_t)std::min<int64_t>(dperm_total, 0xFFFFFFF0ll)) + V + 1;
+    m->carry_tiles = tiles;
     m->carry.reserve((size_t)tiles * sizeof(TileCarry), false, m->stream);
     m->tile_first.reserve((size_t)(2 * tiles + 2) * 4, false, m->stream);
     uint32_t tb = 0;
     for (int c = 0; c < V; ++c) {
-      View& v = m->views[c];
-      v.tile_base = tb;
-      CK(launch_tile_first(m->dseg.as<uint32_t>(), v.dpair_base, v.dpair_base + v.n_dpairs,
-                           v.dperm_base, v.dperm_base + v.n_dperm, m->tile_first.as<uint32_t>() + tb,
-                           m->stream));
-      tb += pair_update_tiles(v.n_dperm);
+      view_tiles(m, c, tb);
+      tb += pair_update_tiles(m->views[c].n_dperm);
     }
     m->jac_tile_base = tb;
     CK(launch_tile_first(m->dseg.as<uint32_t>(), 0, (uint32_t)dpair_total, 0, (uint32_t)dperm_total,
                          m->tile_first.as<uint32_t>() + tb, m->stream));
+    m->tile_end = tb + pair_update_tiles((uint32_t)std::min<int64_t>(dperm_total, 0xFFFFFFF0ll)) + 1;
   }
-  // 5. carry messages of every camera over to its new pairs
+  // 6. carry messages of every camera over to its new pairs
   if (remap) {
     int64_t nv = m->n_bricks * kBrickVox;
     m->s_dense.reserve((size_t)nv * 4, false, m->stream);
@@ -829,6 +965,7 @@ void rebuild_lists(mrf_map* m, OldPairs& old) {
     m->vox_active.reserve((size_t)std::max<int64_t>(nv, 1), false, m->stream);
     CK(launch_active_voxels(m->pair_vox.as<uint32_t>(), m->pair_cum.as<float>(), (uint32_t)pair_total,
                             m->vox_active.as<uint8_t>(), nv, m->stream));
+    m->vox_active_n = nv;
   }
   CK(cudaEventRecord(m->ev1, m->stream));
   sync(m);
@@ -838,14 +975,210 @@ void rebuild_lists(mrf_map* m, OldPairs& old) {
   m->stats.build_ms = ms;
   m->built_version = m->version;
   m->jacobi_version = -1;
-  m->stats.n_rays = nrays;
-  m->stats.n_inc_pre = npre;
-  m->stats.n_inc_post = npost;
-  m->stats.n_pairs = pair_total;
-  m->stats.n_inc_dyn = ndyn;
-  m->stats.n_pairs_dyn = dpair_total;
-  m->stats.n_rays_bp = nrays_bp;
-  m->stats.n_inc_pre_bp = npre_bp;
+  m->built_views = V;
+  m->npix_total = npix;
+  m->bricks_at_build = m->n_bricks;
+  m->holes = false;
+  m->needs_full = false;
+  m->dead_inc = 0;
+  stats_from_views(m);
+}
+
+// Appends the lists of the views added since the last build (a full-ray
+// map only; see ensure_built), leaving the other views' lists, pairs and
+// messages as they are: every brick a full-ray view's rays cross before
+// their stop was activated by the view itself, so bricks activated later
+// change no old list -- which a count pass over the old views, compared
+// with their stored ray records, confirms whenever the brick set grew.
+// Returns false (nothing changed) when a full build is needed instead.
+bool append_lists(mrf_map* m) {
+  const int V = (int)m->views.size();
+  CK(cudaEventRecord(m->ev0, m->stream));
+  m->g.brick_slot = m->d_slot.as<int>();
+  for (View& v : m->views) v.cam.brick_slot = m->g.brick_slot;
+  if (m->n_bricks != m->bricks_at_build) {
+    CK(cudaMemsetAsync(m->s_err.p, 0, 8, m->stream));
+    for (int c = 0; c < m->built_views; ++c) {
+      const View& v = m->views[c];
+      const int64_t hw = view_pixels(v);
+      if (!hw) continue;
+      m->s_counts.reserve((size_t)hw * 4 + 4, false, m->stream);
+      CK(launch_trace_count(v.cam, v.pose, v.depth.as<float>(), m->s_counts.as<uint32_t>(), m->s_err.as<int>(),
+                            m->stream, m->meta.as<RayMeta>() + v.pix_base));
+    }
+    int flags[2] = {0, 0};
+    CK(cudaMemcpyAsync(flags, m->s_err.p, 8, cudaMemcpyDeviceToHost, m->stream));
+    sync(m);
+    if (flags[1]) {
+      CK(cudaMemsetAsync(m->s_err.p, 0, 8, m->stream));
+      return false;
+    }
+    check_device_err(m);
+  }
+  std::vector<int> added;
+  for (int c = m->built_views; c < V; ++c)
+    if (!m->views[c].retired) added.push_back(c);
+  // 1-3. counts, arenas (kept), emit of the new views
+  int64_t npix = m->npix_total, n_inc = m->n_inc;
+  for (int c = m->built_views; c < V; ++c) {
+    View& v = m->views[c];
+    v.pix_base = npix;
+    v.inc_base = (uint32_t)n_inc;
+    v.n_inc = 0;
+    npix += view_pixels(v);
+  }
+  u32_checked(npix, "pixel count");
+  std::vector<int64_t> coff;
+  const std::vector<uint32_t> cnt = count_views(m, added, n_inc, coff);
+  for (size_t k = 0; k < added.size(); ++k) {
+    View& v = m->views[added[k]];
+    v.inc_base = (uint32_t)n_inc;
+    v.n_inc = cnt[k];
+    n_inc += cnt[k];
+  }
+  for (int c = m->built_views; c < V; ++c)
+    if (m->views[c].retired) m->views[c].inc_base = (uint32_t)n_inc;
+  {
+    const size_t ib = (size_t)std::max<int64_t>(n_inc, 1) * 4;
+    m->meta.reserve((size_t)std::max<int64_t>(npix, 1) * sizeof(RayMeta), true, m->stream);
+    m->inc_len.reserve(ib, true, m->stream);
+    m->inc_mu.reserve(ib, true, m->stream);
+    m->inc_pair.reserve(ib, true, m->stream);
+    m->inc_pl.reserve(ib, true, m->stream);
+    m->dperm.reserve((size_t)(m->n_dperm + (n_inc - m->n_inc)) * 4 + 4, true, m->stream);
+    // scratch of the build: only the new views' parts are written and read
+    m->s_vox.reserve(ib, false, m->stream);
+    m->s_rec.reserve(ib * 2, false, m->stream);
+  }
+  for (size_t k = 0; k < added.size(); ++k) emit_view(m, added[k], m->s_offs.as<uint32_t>() + coff[k]);
+  std::vector<RayMeta> hm;
+  // the new views' ray records on the host
+  const int64_t hw_new = npix - m->npix_total;
+  hm.resize((size_t)std::max<int64_t>(hw_new, 0));
+  if (hw_new > 0) {
+    CK(cudaMemcpyAsync(hm.data(), m->meta.as<RayMeta>() + m->npix_total, (size_t)hw_new * sizeof(RayMeta),
+                       cudaMemcpyDeviceToHost, m->stream));
+    sync(m);
+    check_device_err(m);
+  }
+  for (int c : added) view_counters(m->views[c], hm.data() + (m->views[c].pix_base - m->npix_total));
+  // loud voxels of every live view: the old views' from their pairs, the
+  // new ones' from the voxel ids of the emit pass
+  const int64_t nvox = m->n_bricks * kBrickVox;
+  m->s_loud.reserve((size_t)std::max<int64_t>(nvox, 1), false, m->stream);
+  CK(cudaMemsetAsync(m->s_loud.p, 0, (size_t)std::max<int64_t>(nvox, 1), m->stream));
+  for (int c = 0; c < m->built_views; ++c) {
+    const View& v = m->views[c];
+    if (v.retired || !v.n_inc) continue;
+    CK(launch_loud_voxels_from_pairs(m->meta.as<RayMeta>() + v.pix_base, view_pixels(v), m->inc_pair.as<uint32_t>(),
+                                     m->pair_vox.as<uint32_t>(), m->s_loud.as<uint8_t>(), m->stream));
+  }
+  for (int c : added)
+    CK(launch_loud_voxels(m->meta.as<RayMeta>() + m->views[c].pix_base, view_pixels(m->views[c]),
+                          m->s_vox.as<uint32_t>(), m->s_loud.as<uint8_t>(), m->stream));
+  // an old view's quiet pairs (numbered after its loud ones) must all stay
+  // quiet: where one became loud, the view prepares every pair
+  m->s_k1.reserve(64, false, m->stream);
+  for (int c = 0; c < m->built_views; ++c) {
+    View& v = m->views[c];
+    if (v.retired || v.n_loud >= v.n_pairs) continue;
+    CK(cudaMemsetAsync(m->s_k1.p, 0, 4, m->stream));
+    CK(launch_count_loud(m->pair_vox.as<uint32_t>() + v.pair_base + v.n_loud, v.n_pairs - v.n_loud,
+                         m->s_loud.as<uint8_t>(), m->s_k1.as<uint32_t>(), m->stream));
+    if (read1(m, m->s_k1.as<uint32_t>())) v.n_loud = v.n_pairs;
+  }
+  // 4. pairs of the new views, numbered after the existing ones
+  const int bits = voxel_id_bits(m);
+  int64_t pair_total = m->n_pairs, perm_total = m->n_perm_total, dperm_total = m->n_dperm,
+          dpair_total = m->n_dpairs;
+  const int64_t pair0 = pair_total, dpair0 = dpair_total;
+  for (int c : added) view_pairs(m, c, bits, pair_total, perm_total, dperm_total, dpair_total);
+  // 5. ray queues and region blocks of the new views
+  {
+    int64_t base = 0;
+    for (int c = 0; c < m->built_views; ++c) base = std::max<int64_t>(base, (int64_t)m->views[c].order_base + m->views[c].n_active);
+    base = std::max<int64_t>(base, m->queue_end);
+    m->ray_queue.reserve((size_t)std::max<int64_t>(base + hw_new, 1) * sizeof(RayMeta), true, m->stream);
+    for (int c = m->built_views; c < V; ++c) {
+      View& v = m->views[c];
+      v.order_base = (uint32_t)base;
+      view_ray_queue(m, c, hm.data() + (v.pix_base - m->npix_total));
+      base += v.n_active;
+    }
+    m->queue_end = base;
+    const int R = std::max(1, m->num_sms);
+    m->counters.reserve((size_t)(V + 1) * 4, false, m->stream);
+    m->rcounters.reserve(((size_t)2 * V * R + 2 * (size_t)V + 2) * 4, false, m->stream);
+    std::vector<RegionLists> lists((size_t)V);
+    region_lists_parallel(m, added, hm, m->npix_total, lists);
+    std::vector<int> newv;
+    for (int c = m->built_views; c < V; ++c) {
+      if (m->views[c].retired) {
+        m->views[c].n_left = 0;
+        m->views[c].left_base = 0;
+      }
+      newv.push_back(c);
+    }
+    m->region_end = region_blocks(m, newv, lists, m->region_end);
+  }
+  m->n_inc = n_inc;
+  m->n_pairs = pair_total;
+  m->n_perm_total = perm_total;
+  m->n_dperm = dperm_total;
+  m->n_dpairs = dpair_total;
+  const size_t pb = (size_t)std::max<int64_t>(pair_total + 1, 1);
+  m->pair_vox.reserve(pb * 4, true, m->stream);
+  m->pair_m.reserve(pb * 4, true, m->stream);
+  m->pair_cum.reserve(pb * 4, true, m->stream);
+  m->pair_stat.reserve(pb * 4, true, m->stream);
+  m->pair_ndyn.reserve(pb * 4, true, m->stream);
+  m->pair_hit.reserve(pb * 4, true, m->stream);
+  m->pair_seg.reserve(pb * 4, true, m->stream);
+  m->dpair.reserve((size_t)(dpair_total + 1) * 4, true, m->stream);
+  m->dseg.reserve((size_t)(dpair_total + 1) * 4, true, m->stream);
+  m->drun.reserve((size_t)(dpair_total + 1) * 16, true, m->stream);
+  CK(launch_drun(m->dpair.as<uint32_t>() + dpair0, (uint32_t)(dpair_total - dpair0), m->pair_vox.as<uint32_t>(),
+                 m->pair_cum.as<float>(), m->pair_stat.as<float>(), m->drun.as<uint4>() + dpair0, m->stream));
+  m->pair_q.reserve(pb * 4, false, m->stream);
+  m->pair_dm.reserve(pb * 4, false, m->stream);
+  CK(launch_fill_f32(m->pair_m.as<float>() + pair0, pair_total - pair0, 0.0f, m->stream));
+  // tiles of the new views at the end of tile_first; the carries sized for
+  // the largest launch
+  {
+    int64_t need = m->tile_end;
+    for (int c = m->built_views; c < V; ++c) need += pair_update_tiles(m->views[c].n_dperm) + 1;
+    m->tile_first.reserve((size_t)(need + 2) * 4, true, m->stream);
+    uint32_t tb = (uint32_t)m->tile_end;
+    int64_t most = m->carry_tiles;
+    for (int c = m->built_views; c < V; ++c) {
+      view_tiles(m, c, tb);
+      tb += pair_update_tiles(m->views[c].n_dperm) + 1;
+      most = std::max<int64_t>(most, (int64_t)pair_update_tiles(m->views[c].n_dperm) + 1);
+    }
+    m->tile_end = tb;
+    m->carry_tiles = most;
+    m->carry.reserve((size_t)most * sizeof(TileCarry), false, m->stream);
+  }
+  // active voxels: the new bricks' voxels start at 0, the new pairs add theirs
+  m->vox_active.reserve((size_t)std::max<int64_t>(nvox, 1), true, m->stream);
+  if (nvox > m->vox_active_n)
+    CK(cudaMemsetAsync(m->vox_active.as<uint8_t>() + m->vox_active_n, 0, (size_t)(nvox - m->vox_active_n), m->stream));
+  m->vox_active_n = nvox;
+  CK(launch_mark_active(m->pair_vox.as<uint32_t>() + pair0, m->pair_cum.as<float>() + pair0,
+                        (uint32_t)(pair_total - pair0), m->vox_active.as<uint8_t>(), m->stream));
+  CK(cudaEventRecord(m->ev1, m->stream));
+  sync(m);
+  check_device_err(m);
+  float ms = 0.0f;
+  cudaEventElapsedTime(&ms, m->ev0, m->ev1);
+  m->stats.build_ms = ms;
+  m->built_version = m->version;
+  m->jacobi_version = -1;
+  m->built_views = V;
+  m->npix_total = npix;
+  m->bricks_at_build = m->n_bricks;
+  stats_from_views(m);
+  return true;
 }
 
 void build_jacobi_csr(mrf_map* m) {
@@ -884,8 +1217,48 @@ void build_jacobi_csr(mrf_map* m) {
   m->jacobi_version = m->built_version;
 }
 
+// Lists of views added since the last build are appended when that is exact
+// (full-ray activation: see append_lists) and the arenas are not mostly
+// retired views' data; otherwise, and after set_pose or load_map, every
+// view is rebuilt (which also drops the retired views' data).
+void ensure_built(mrf_map* m);
+
+// the all-view structures (Jacobi queues and tiles, the voxel CSR) need
+// one full build with no retired views' data in the arenas
+void ensure_compact(mrf_map* m) {
+  if (m->holes || m->appended) {
+    m->needs_full = true;
+    m->version++;
+  }
+  ensure_built(m);
+}
+
 void ensure_built(mrf_map* m) {
-  if (m->built_version != m->version) rebuild(m);
+  if (m->built_version != m->version) {
+    const bool can_append = !m->needs_full && m->built_version >= 0 &&
+                            m->prm.activation == MRF_ACT_FULL_RAY && m->built_views <= (int)m->views.size() &&
+                            m->dead_inc * 2 <= m->n_inc;
+    bool done = false;
+    if (can_append) {
+      try {
+        done = append_lists(m);
+      } catch (...) {
+        m->needs_full = true;  // a part-done append: the next build starts over
+        throw;
+      }
+      if (done) {
+        m->appended = true;
+        m->len16_version = -1;
+        ++m->stats.builds_appended;
+      }
+    }
+    if (!done) {
+      rebuild(m);
+      m->appended = false;
+      m->len16_version = -1;
+      ++m->stats.builds_full;
+    }
+  }
   // the fp16 streams of the current lists
   if (m->precision == MRF_PRECISION_HALF_STREAMS && m->len16_version != m->built_version) {
     m->inc_len16.reserve((size_t)std::max<int64_t>(m->n_inc, 1) * 2, false, m->stream);
@@ -941,17 +1314,19 @@ RayWork ray_work(mrf_map* m, int c) {
   const uint32_t R = m->nreg;
   RayWork w{};
   w.region = m->region_q.as<RayMeta>();
+  w.rper = R;
   uint32_t* lc = m->rcounters.as<uint32_t>() + (size_t)2 * V * R;  // leftover counters
   if (c >= 0) {
     const View& v = m->views[c];
     w.queue = m->ray_queue.as<RayMeta>() + v.order_base;
     w.n_rays = v.n_active;
     w.counter = m->counters.as<uint32_t>() + c;
-    w.rstart = m->rstart.as<uint32_t>() + (size_t)c * R;
+    w.rstart = m->rstart.as<uint32_t>() + (size_t)c * (R + 1);
     w.nreg = R;
     w.rcounter = m->rcounters.as<uint32_t>() + (size_t)c * R;
-    w.left = m->region_q.as<RayMeta>() + m->region_home_n + v.left_base;
-    w.n_left = v.n_left;
+    w.lprefix = m->lsingle.as<uint32_t>() + 2 * (size_t)c;
+    w.lbase = m->lbase.as<uint32_t>() + c;
+    w.nlv = 1;
     w.lcounter = lc + c;
   } else {
     w.queue = m->ray_queue.as<RayMeta>();
@@ -960,8 +1335,9 @@ RayWork ray_work(mrf_map* m, int c) {
     w.rstart = m->rstart.as<uint32_t>();
     w.nreg = (uint32_t)V * R;
     w.rcounter = m->rcounters.as<uint32_t>() + (size_t)V * R;
-    w.left = m->region_q.as<RayMeta>() + m->region_home_n;
-    w.n_left = m->n_left_all;
+    w.lprefix = m->lprefix.as<uint32_t>();
+    w.lbase = m->lbase.as<uint32_t>();
+    w.nlv = (uint32_t)V;
     w.lcounter = lc + V;
   }
   return w;
@@ -1082,8 +1458,11 @@ void refresh_beliefs(mrf_map* m) {
 // cap)
 void run_infer(mrf_map* m, const int* ids, int n_ids, int iters, int flags, float tol = -1.0f,
                int check_every = 1, float* last_delta = nullptr, const float* target = nullptr) {
-  ensure_built(m);
   const bool jacobi = flags & MRF_JACOBI;
+  if (jacobi)
+    ensure_compact(m);
+  else
+    ensure_built(m);
   if (jacobi && m->jacobi_version != m->built_version) build_jacobi_csr(m);
   const int V = (int)m->views.size();
   if (iters <= 0) iters = m->prm.max_iters > 0 ? m->prm.max_iters : 1;
@@ -1229,6 +1608,7 @@ void destroy_bufs(mrf_map* m) {
                  &m->pair_dm,
                  &m->pair_seg, &m->dperm, &m->dpair, &m->dseg, &m->drun,
                  &m->carry, &m->ray_order, &m->ray_queue, &m->region_q, &m->rstart, &m->rcounters, &m->counters, &m->tile_first,
+                 &m->lbase, &m->lsingle, &m->lprefix,
                  &m->vseg, &m->vpairs, &m->vvox, &m->vox_active, &m->d_Lbase, &m->inc_len16, &m->pair_q16,
                  &m->s_rec, &m->s_recs, &m->s_pf, &m->s_ps,
                  &m->s_flags, &m->s_ind, &m->s_scan,
@@ -1526,6 +1906,7 @@ mrf_status mrf_set_pose(mrf_map* m, int view_id, const float* pose) {
     set_pose(m->views[view_id].pose, pose);
     activate_view(m, m->views[view_id]);
     m->version++;
+    m->needs_full = true;  // the moved view's lists are traced anew
     m->stats.n_bricks = m->n_bricks;
   });
 }
@@ -1554,7 +1935,12 @@ mrf_status mrf_retire_view(mrf_map* m, int view_id) {
     sync(m);
     v.depth.release();
     v.retired = true;
-    m->version++;  // the next build leaves its lists and pairs out
+    // its lists and pairs are out of every launch from now on; their space
+    // in the arenas is reclaimed by the next full build
+    if (v.n_inc) m->holes = true;
+    m->dead_inc += v.n_inc;
+    v.n_inc = v.n_pairs = v.n_perm = v.n_dperm = v.n_dpairs = v.n_active = v.n_left = v.n_loud = 0;
+    m->version++;
   });
 }
 
@@ -1616,7 +2002,7 @@ static void start_logodds(mrf_map* m, float lp) {
 // L = logit(prior) + sum m, so the state is a consistent BP state: the
 // equations and their fixed point are those of the plain start.
 static void warm_start_impl(mrf_map* m, const float* L_pred, bool device_ptr, int sweeps) {
-  ensure_built(m);
+  ensure_compact(m);
   if (m->jacobi_version != m->built_version) build_jacobi_csr(m);
   const int64_t nvox = m->n_bricks * kBrickVox;
   if (nvox == 0 || m->n_inc == 0) return;
@@ -1701,7 +2087,7 @@ mrf_status mrf_write_messages(mrf_map* m, int view_id, const float* dense) {
 mrf_status mrf_rebuild_logodds(mrf_map* m) {
   if (guard(m) != MRF_OK) return MRF_ERR_INVALID;
   return wrap([&] {
-    ensure_built(m);
+    ensure_compact(m);
     if (m->jacobi_version != m->built_version) build_jacobi_csr(m);
     const int64_t nvox = m->n_bricks * kBrickVox;
     if (nvox == 0) return;
@@ -1721,7 +2107,7 @@ mrf_status mrf_warm_features(mrf_map* m, float* feat_dev) {
     return MRF_ERR_INVALID;
   }
   return wrap([&] {
-    ensure_built(m);
+    ensure_compact(m);
     if (m->jacobi_version != m->built_version) build_jacobi_csr(m);
     const int64_t nvox = m->n_bricks * kBrickVox;
     CK(launch_voxel_features(m->vseg.as<uint32_t>(), m->vpairs.as<uint32_t>(), m->vvox.as<uint32_t>(),
@@ -1793,7 +2179,10 @@ mrf_status mrf_autotune_flags(mrf_map* m, int reps, int flags, double* ms_out, i
   }
   const bool jacobi = (flags & MRF_JACOBI) != 0;
   return wrap([&] {
-    ensure_built(m);
+    if (jacobi)
+      ensure_compact(m);
+    else
+      ensure_built(m);
     if (jacobi && m->jacobi_version != m->built_version) build_jacobi_csr(m);
     const int V = (int)m->views.size();
     const int NV = ray_bp_variants();
@@ -2130,6 +2519,7 @@ mrf_status mrf_load_map(mrf_map* m, const float* points, const float* occ, int64
     m->g.brick_slot = m->d_slot.as<int>();
     CK(launch_activate_points(m->g, pts.as<float>(), n, m->s_flags.as<uint8_t>(), m->stream));
     commit_new_bricks(m);
+    m->needs_full = true;
     m->g.brick_slot = m->d_slot.as<int>();
     CK(launch_set_points(m->g, pts.as<float>(), oc.as<float>(), n, m->d_belief.as<float>(), m->stream));
     sync(m);

@@ -87,9 +87,11 @@ cudaError_t launch_fill_new_voxels(float* L, float* belief, int64_t v0, int64_t 
 cudaError_t launch_set_points(const Geom& g, const float* pts, const float* occ, int64_t n,
                               float* belief, cudaStream_t s);
 
-// traversal: count pass then emit pass
+// traversal: count pass then emit pass.  With check (the view's stored ray
+// records) the count pass also sets err[1] when any ray's record would
+// differ from the stored one (err holds two ints).
 cudaError_t launch_trace_count(const Geom& g, const Pose& P, const float* depth, uint32_t* counts,
-                               int* err, cudaStream_t s);
+                               int* err, cudaStream_t s, const RayMeta* check = nullptr);
 cudaError_t launch_trace_emit(const Geom& g, const Pose& P, const float* depth,
                               const uint32_t* pix_off, uint32_t inc_base, RayMeta* meta,
                               uint32_t* inc_vox, float* inc_len, float* inc_mu, float2* inc_rec,
@@ -106,6 +108,12 @@ cudaError_t launch_brick_keys(const uint32_t* order, uint32_t np, const uint32_t
                               cudaStream_t s);
 // voxels with a dynamic incidence in any view, and the pairs on them
 cudaError_t launch_loud_voxels(const RayMeta* meta, int64_t npix, const uint32_t* vox, uint8_t* loud,
+                               cudaStream_t s);
+// the same with each incidence's voxel from its pair (vox = pair_vox[inc_pair])
+cudaError_t launch_loud_voxels_from_pairs(const RayMeta* meta, int64_t npix, const uint32_t* inc_pair,
+                                          const uint32_t* pair_vox, uint8_t* loud, cudaStream_t s);
+// flag[v] = 1 for the voxels of the given pairs past the length gate (no reset)
+cudaError_t launch_mark_active(const uint32_t* pair_vox, const float* cum, uint32_t np, uint8_t* flag,
                                cudaStream_t s);
 cudaError_t launch_count_loud(const uint32_t* pair_vox, uint32_t np, const uint8_t* loud, uint32_t* count,
                               cudaStream_t s);
@@ -211,20 +219,23 @@ int ray_bp_resident_blocks(int variant, int half_streams);
 cudaError_t launch_to_half(const float* in, int64_t n, __half* out, cudaStream_t s);
 // the rays of one ray-kernel launch in its schedules: queue[0..n_rays)
 // longest first with one zeroed counter; the same rays as nreg regions of
-// consecutive pixels, region r's home rays (longest first) at positions
-// rstart[r] .. rstart[r + 1] of region (nreg zeroed counters) and the
-// regions' remaining short rays in left[0..n_left) (longest first; one
-// zeroed counter)
+// consecutive pixels, rper regions per view: region r = (view q = r / rper,
+// rr = r % rper) has its home rays (longest first) at positions
+// rstart[q (rper + 1) + rr] .. rstart[q (rper + 1) + rr + 1] of region (nreg
+// zeroed counters), and the views' remaining short rays (longest first):
+// view q's lprefix[q + 1] - lprefix[q] leftovers from region[lbase[q]] on,
+// nlv views, one zeroed counter
 struct RayWork {
   const RayMeta* queue;
   uint32_t n_rays;
   uint32_t* counter;
   const RayMeta* region;
   const uint32_t* rstart;
-  uint32_t nreg;
+  uint32_t nreg, rper;
   uint32_t* rcounter;
-  const RayMeta* left;
-  uint32_t n_left;
+  const uint32_t* lprefix;
+  const uint32_t* lbase;
+  uint32_t nlv;
   uint32_t* lcounter;
 };
 cudaError_t launch_ray_bp(const BpArrays& a, const RayWork& w, int fix_reset, int num_sms, int variant,

@@ -77,7 +77,9 @@ class mrf_stats(C.Structure):
                                                                 ("n_inc_dyn", C.c_int64),
                                                                 ("n_pairs_dyn", C.c_int64),
                                                                 ("n_rays_bp", C.c_int64),
-                                                                ("n_inc_pre_bp", C.c_int64)]
+                                                                ("n_inc_pre_bp", C.c_int64),
+                                                                ("builds_full", C.c_int64),
+                                                                ("builds_appended", C.c_int64)]
 
 
 _lib = None
@@ -336,8 +338,8 @@ class MRFMap:
         _check(self._L.mrf_warm_features(self._h, C.c_void_p(feat_dev_ptr)))
 
     def set_precision(self, mode: int):
-        """PRECISION_FP32 (default) or PRECISION_HALF_STREAMS (fp16 lengths
-        and ln q gathers in the ray kernel)."""
+        """PRECISION_HALF_STREAMS (default: fp16 lengths and ln q gathers
+        in the ray kernel) or PRECISION_FP32."""
         _check(self._L.mrf_set_precision(self._h, mode))
 
     def set_ray_variant(self, variant: int):

@@ -413,16 +413,31 @@ static void activate_view(orc_map* m, const orc_cam* cam, const float* pose, con
       }
       if (inside) mark_point_bricks(m, cam, pv, flag);
       if (policy == ORC_ACT_FULL_RAY) {
+        /* every brick the ray crosses up to the brick run where the Pre
+         * pass stops: at the exit s of a run's last voxel,
+         * s + bias(s) > d + 3 sigma(s) (the stop test of build_ray) */
         float o[3], dr[3], mult;
         ray_setup(m, cam, pose, x, y, o, dr, &mult);
-        float lim = d + 3.0f * poly_f(lut_at(m, cam, m->sigma_lut, x, y), m->p.lookup_n, d);
+        const float* sg = lut_at(m, cam, m->sigma_lut, x, y);
+        const float* bs = lut_at(m, cam, m->bias_lut, x, y);
+        const int n = m->p.lookup_n;
         dda_t r;
         if (dda_init(&r, cam, o, dr)) {
           int v[3];
-          float l, tin, te;
+          float l, tin, te, s_last = 0.0f;
+          int64_t cur = -1;
           while (dda_next(&r, v, &l, &tin, &te)) {
-            if (tin * mult >= lim) break;
-            flag[blin(m, v[0] >> 3, v[1] >> 3, v[2] >> 3)] = 1;
+            int64_t lin = blin(m, v[0] >> 3, v[1] >> 3, v[2] >> 3);
+            if (lin != cur) {
+              if (cur >= 0) {
+                float lhs = s_last + poly_f(bs, n, s_last);
+                float rhs = d + 3.0f * poly_f(sg, n, s_last);
+                if (lhs > rhs) break;
+              }
+              flag[lin] = 1;
+              cur = lin;
+            }
+            s_last = te * mult;
           }
         }
       }

@@ -119,21 +119,25 @@ def test_capacity_of_32_bit_voxel_ids(native_lib):
 
 
 def test_capacity_of_32_bit_incidence_indices(native_lib):
-    """44 copies of one 640x480 1 cm view hold ~4.6 G incidences: the build
-    counts them in 64 bits and refuses before forming any 32-bit offset
-    (only the per-pixel counts, ~54 MB, are allocated by then).  With the
+    """Copies of one 640x480 1 cm view, enough for ~4.4 G incidences: the
+    build counts them in 64 bits and refuses before forming any 32-bit
+    offset (only the per-pixel counts are allocated by then).  With the
     copies retired the map builds and iterates normally."""
     w = synthetic.full_room(1, n_frames=1)
     m = L.MRFMap(w.params, activation=L.ACT_FULL_RAY)
-    for _ in range(44):
+    m.add_view(w.poses[0], w.depths[0])
+    m.infer(iters=1)
+    per_view = m.stats()["n_inc_pre"]
+    copies = int(4.4e9 // per_view) + 2
+    for _ in range(copies - 1):
         m.add_view(w.poses[0], w.depths[0])
     with pytest.raises(L.MrfError) as e:
         m.infer(iters=1)
     assert e.value.status == CAPACITY and "32-bit incidence" in str(e.value)
-    for k in range(1, 44):
+    for k in range(1, copies):
         m.retire_view(k)
     m.infer(iters=2)
     st = m.stats()
-    assert 0 < st["n_inc_post"] < 2 ** 32 // 40
+    assert st["n_inc_pre"] == per_view
     assert np.isfinite(m.beliefs()).all()
     m.close()

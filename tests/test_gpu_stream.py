@@ -84,3 +84,52 @@ def test_retired_views_refuse_per_view_calls(native_lib, walk):
     st = m.stats()
     assert st["n_views"] == 3
     m.close()
+
+
+def test_appended_lists_equal_a_full_build(native_lib, walk):
+    """Frames added one at a time to a full-ray map, each followed by a build,
+    append only the new view's lists; they are those a single build of all
+    the views gives, bit for bit, and BP from the prior reaches the same
+    beliefs.  After retiring a view and appending more, a Jacobi run (which
+    needs the all-view structures: a full build first) matches a map built
+    directly from the live views."""
+    w, depths = walk
+    a = L.MRFMap(w.params, activation=L.ACT_FULL_RAY)
+    for k in range(8):
+        a.add_view(w.poses[k], depths[k])
+        a.infer(iters=1, flags=L.INCREMENTAL)
+    st = a.stats()
+    assert st["builds_appended"] == 7 and st["builds_full"] == 1
+    b = L.MRFMap(w.params, activation=L.ACT_FULL_RAY)
+    for k in range(8):
+        b.add_view(w.poses[k], depths[k])
+    b.infer(iters=1)
+    np.testing.assert_array_equal(a.brick_coords(), b.brick_coords())
+    for v in range(8):
+        for x, y in zip(a.view_incidences(v), b.view_incidences(v)):
+            np.testing.assert_array_equal(x, y)
+    assert a.stats()["n_inc_post"] == b.stats()["n_inc_post"]
+    a.reset_state()
+    b.reset_state()
+    a.infer(iters=5)
+    b.infer(iters=5)
+    np.testing.assert_allclose(a.beliefs(), b.beliefs(), rtol=0, atol=1e-6)
+    # a window step: retire, append, then Jacobi
+    a.retire_view(0)
+    for k in (8, 9):
+        a.add_view(w.poses[k], depths[k])
+        a.infer(iters=1, flags=L.INCREMENTAL)
+    assert a.stats()["builds_appended"] == 9
+    c = L.MRFMap(w.params, activation=L.ACT_FULL_RAY)
+    for k in range(10):
+        c.add_view(w.poses[k], depths[k])
+    c.retire_view(0)
+    a.reset_state()
+    c.reset_state()
+    a.infer(iters=4, flags=L.JACOBI)
+    c.infer(iters=4, flags=L.JACOBI)
+    assert a.stats()["builds_full"] == 2
+    np.testing.assert_array_equal(a.brick_coords(), c.brick_coords())
+    np.testing.assert_allclose(a.beliefs(), c.beliefs(), rtol=0, atol=1e-6)
+    for m in (a, b, c):
+        m.close()
