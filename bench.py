@@ -337,11 +337,11 @@ def run_reference(args):
 RAY_KERNEL_VERSION = 6
 
 
-def ray_kernel_bytes(st, iters, half=True):
+def ray_kernel_bytes(st, iters, half=False):
     """Algorithmic bytes of the ray-message kernel for one launch-sum, over
     the rays it runs over (those with a dynamic incidence): per Pre
-    incidence the pair id (4 B), the length and the ln q gather (2 B each
-    with the default 16-bit streams, 4 B each in fp32); per dynamic
+    incidence the pair id (4 B), the length and the ln q gather (4 B each
+    with the default fp32 streams, 2 B each with 16-bit streams); per dynamic
     incidence (from the ray's first non-zero potential on) +8 B (potential
     4, message write 4); per ray 16 B of metadata."""
     per_pre = 8 if half else 12
@@ -370,10 +370,10 @@ def parity_cut(w, act, policy):
             gm.add_view(w.poses[k], w.depths[k])
             om.add_view(w.poses[k], w.depths[k], pol)
     iters = w.params.max_iters
-    gm.set_precision(L.PRECISION_FP32)
-    gm.infer(iters=iters)
-    g32 = gm.beliefs().astype(np.float64).ravel()
     gm.set_precision(L.PRECISION_HALF_STREAMS)
+    gm.infer(iters=iters)
+    g16 = gm.beliefs().astype(np.float64).ravel()
+    gm.set_precision(L.PRECISION_FP32)
     gm.reset_state()
     gm.infer(iters=iters)
     t0 = time.perf_counter()
@@ -382,7 +382,7 @@ def parity_cut(w, act, policy):
     gb, ob = gm.beliefs().astype(np.float64).ravel(), om.beliefs().ravel()
     om.close()
     err = np.abs(gb - ob)
-    err32 = np.abs(g32 - ob)
+    err16 = np.abs(g16 - ob)
     touched = (gb > 0) | (ob > 0)
     n_long, lv = 0, []
     for v in range(len(views)):
@@ -404,9 +404,8 @@ def parity_cut(w, act, policy):
     if len(lv):
         out["max_abs_belief_err_long_ray_voxels"] = float(err[lv].max())
         out["long_ray_voxels_checked"] = int(len(lv))
-    out["precision"] = "16-bit streams (the default)"
-    out["fp32_streams"] = {"max_abs_belief_err": float(err32.max()),
-                           "class_agreement_at_0.5": float(((g32 > 0.5) == (ob > 0.5))[touched].mean())}
+    out["half_streams"] = {"max_abs_belief_err": float(err16.max()),
+                           "class_agreement_at_0.5": float(((g16 > 0.5) == (ob > 0.5))[touched].mean())}
     return out
 
 
@@ -460,10 +459,10 @@ def run_ours(args):
     torch.cuda.synchronize()
     barrier(ws)
     ms = e0.elapsed_time(e1)
-    # the same steps with fp32 streams in the ray kernel (the default reads
-    # lengths and ln q as fp16; both are reported with their error against
-    # the FP64 oracle)
-    m.set_precision(L.PRECISION_FP32)
+    # the same steps with 16-bit streams in the ray kernel (fp16 lengths and
+    # ln q; reported beside the fp32 default with its error against the
+    # FP64 oracle)
+    m.set_precision(L.PRECISION_HALF_STREAMS)
     for _ in range(2):
         m.reset_state()
         m.infer(iters=iters, flags=L.ASYNC)
@@ -480,7 +479,7 @@ def run_ours(args):
     m.reset_state()
     m.infer(iters=iters, flags=L.PROFILE)
     prof_half = m.stats()
-    m.set_precision(L.PRECISION_HALF_STREAMS)
+    m.set_precision(L.PRECISION_FP32)
     # per-kernel device times of one profiled step (events on the map stream)
     m.reset_state()
     m.infer(iters=iters, flags=L.PROFILE)
@@ -527,7 +526,7 @@ def run_ours(args):
     # e2e through the C ABI with host buffers (pinned), create -> read-back
     pinned = [torch.from_numpy(np.ascontiguousarray(d)).pin_memory() for d in w.depths]
     h2d = sum(p.numel() * 4 for p in pinned) + 16 * 4 * len(w.poses)
-    e2e_times, d2h = [], 0
+    e2e_times, d2h, phases = [], 0, []
     for step in range(args.e2e_steps + 1 if args.e2e_steps > 0 else 0):
         torch.cuda.synchronize()
         barrier(ws)
@@ -538,13 +537,20 @@ def run_ours(args):
                 mm.add_view_camera(P, D.numpy(), *w.cams[k])
             else:
                 mm.add_view(P, D.numpy())
+        t1 = time.perf_counter()
         mm.infer(iters=iters)
+        t2 = time.perf_counter()
         cen, bel = mm.read_bricks()
+        t3 = time.perf_counter()
+        est = mm.stats()
         mm.close()
         dt = time.perf_counter() - t0
         d2h = cen.nbytes + bel.nbytes
         if step > 0:  # first pass warms allocator and host paths
             e2e_times.append(dt)
+            phases.append({"create_and_add_views_s": t1 - t0, "infer_s": t2 - t1,
+                           "build_device_ms": est["build_ms"], "iterations_device_ms": est["infer_ms"],
+                           "read_back_s": t3 - t2})
     if e2e_times:
         e2e_t = max_over_ranks(float(np.mean(e2e_times)), ws)
         e2e_val = sum_over_ranks(n_upd_step, ws) / e2e_t
@@ -615,7 +621,7 @@ def run_ours(args):
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32 on fp16 length/ln q streams (fp64 sums on rays > 512)",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (fp64 sums on rays > 512)",
             "data": "synthetic (seeded room scenes; no public dataset)",
             "config": workload_config(w, args.policy, ws),
             "workload_stats": {"n_inc_per_iter": st["n_inc_post"],
@@ -628,12 +634,11 @@ def run_ours(args):
                                "static_messages": "exact constants (p = F_EPS before a ray's first "
                                                   "non-zero potential), summed once per build"},
             "dynamic_updates_per_s": st["n_inc_dyn"] * iters * args.steps / (ms / 1e3),
-            "precision": "16-bit streams: the ray kernel reads segment lengths and gathers ln q as fp16; "
-                         "every product, prefix and sum fp32 (fp64 on rays > 512), messages fp32",
-            "fp32_streams": {"value": n_upd_step * args.steps / (ms_half / 1e3), "ms_per_step": ms_half / args.steps,
+            "half_streams": {"value": n_upd_step * args.steps / (ms_half / 1e3), "ms_per_step": ms_half / args.steps,
                              "ray_kernel_ms_per_launch": prof_half["kernel_ms"][1] / max(prof_half["kernel_count"][1], 1),
-                             "note": "the same steps with fp32 lengths and ln q; error against the FP64 oracle "
-                                     "in parity_vs_fp64.fp32_streams"},
+                             "note": "the same steps with fp16 segment lengths and ln q gathers in the ray kernel "
+                                     "(MRF_PRECISION_HALF_STREAMS); error against the FP64 oracle in "
+                                     "parity_vs_fp64.half_streams"},
             "gpu_launches": launches_step * args.steps,
             "roofline": {"bound": "hbm", "kernel": "k_ray_bp", "achieved": achieved, "peak": peak,
                          "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
@@ -651,7 +656,9 @@ def run_ours(args):
             "kernel_share": kernel_share,
             "clocks": clk,
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                    "d2h_bytes_per_step": d2h, "s_per_step": e2e_t},
+                    "d2h_bytes_per_step": d2h, "s_per_step": e2e_t,
+                    "phases": {k: round(float(np.mean([p[k] for p in phases])), 4) for k in phases[0]}
+                    if phases else None},
             "cpu_baseline": cpu,
             "cpu_insertion": cpu_ins,
             "likelihood": like,
@@ -730,7 +737,7 @@ def run_large(args):
         print(json.dumps({
             "metric": LARGE_METRIC, "value": sum_over_ranks(n, ws) / dt, "unit": "frames/s", "n_gpus": ws,
             "steps": n, "warmup": warm, "ms_per_step": 1e3 * dt / max(n, 1), "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32 on fp16 length/ln q streams (fp64 sums on rays > 512)",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (fp64 sums on rays > 512)",
             "data": "synthetic (seeded random walk; no public dataset)",
             "config": {"workload": walk.name, "frames": args.frames, "window": W, "iters_per_frame": iters,
                        "voxel_m": walk.params.res, "dims_m": list(walk.params.dims), "boxes": 150,
@@ -854,7 +861,7 @@ def run_batched(args):
         print(json.dumps({
             "metric": BATCH_METRIC, "value": sum_over_ranks(n_upd, ws) / (ms / 1e3), "unit": UNIT, "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f32 on fp16 length/ln q streams (fp64 sums on rays > 512)",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (fp64 sums on rays > 512)",
             "data": "synthetic (seeded box rooms; no public dataset)",
             "config": {"workload": b.name, "scenes": len(b.boxes), "views": len(b.poses), "view_sizes": sizes,
                        "voxel_m": b.params.res, "max_range_m": b.max_range, "activation": "fullray",

@@ -254,6 +254,13 @@ __global__ void __launch_bounds__(kThreads, 4)
         }
         float s = fm(te, ray.mult);
         if (!run_open) run_start = count;
+        if (!EMIT && meta && (r0 < 0 || kmu < 0)) {
+          // a checking count pass: the visibility-reset and dynamic starts
+          // of the record it compares against
+          const bool z = potential_is_zero(sg, bs, n, s, d);
+          if (r0 < 0 && !z) r0 = run_start;
+          if (kmu < 0 && !z) kmu = count;
+        }
         if (EMIT) {
           const bool z = potential_is_zero(sg, bs, n, s, d);
           const float mu = z ? 0.0f : potential(sg, bs, n, s, d);

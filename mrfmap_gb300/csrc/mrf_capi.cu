@@ -208,7 +208,7 @@ struct mrf_map {
   DBuf vox_active;
   // MRF_PRECISION_HALF_STREAMS: fp16 copies of the segment lengths (per
   // build) and of ln q (written by k_pair_prepare)
-  int precision = MRF_PRECISION_HALF_STREAMS;
+  int precision = MRF_PRECISION_FP32;
   DBuf inc_len16, pair_q16;
   int len16_version = -1;
   // logit(prior) + the messages of retired views, per voxel (kept once a view
@@ -864,10 +864,28 @@ void rebuild_lists(mrf_map* m, OldPairs& old) {
   CK(cudaMemsetAsync(m->s_loud.p, 0, (size_t)std::max<int64_t>(m->n_bricks * kBrickVox, 1), m->stream));
   CK(launch_loud_voxels(m->meta.as<RayMeta>(), npix, m->s_vox.as<uint32_t>(), m->s_loud.as<uint8_t>(),
                         m->stream));
+  // the region lists of the SM-affine schedule are host work on the ray
+  // records alone: built on host threads while the GPU builds the pairs
+  std::vector<RegionLists> lists((size_t)V);
+  bool lists_failed = false;
+  std::thread lists_thread([&] {
+    try {
+      region_lists_parallel(m, live, hm, 0, lists);
+    } catch (...) {
+      lists_failed = true;
+    }
+  });
   // 4. pairs per view
   const int bits = voxel_id_bits(m);
   int64_t pair_total = 0, perm_total = 0, dperm_total = 0, dpair_total = 0;
-  for (int c = 0; c < V; ++c) view_pairs(m, c, bits, pair_total, perm_total, dperm_total, dpair_total);
+  try {
+    for (int c = 0; c < V; ++c) view_pairs(m, c, bits, pair_total, perm_total, dperm_total, dpair_total);
+  } catch (...) {
+    lists_thread.join();
+    throw;
+  }
+  lists_thread.join();
+  if (lists_failed) fail(MRF_ERR_OOM, "host memory for the region queues");
   // 5. ray queues: per view the active rays longest first, and the
   //    SM-affine region blocks
   {
@@ -884,8 +902,6 @@ void rebuild_lists(mrf_map* m, OldPairs& old) {
     const int R = std::max(1, m->num_sms);
     m->nreg = (uint32_t)R;
     m->rcounters.reserve(((size_t)2 * V * R + 2 * (size_t)V + 2) * 4, false, m->stream);
-    std::vector<RegionLists> lists((size_t)V);
-    region_lists_parallel(m, live, hm, 0, lists);
     // retired views: empty rows
     for (int c = 0; c < V; ++c) {
       View& v = m->views[c];

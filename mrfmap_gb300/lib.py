@@ -338,8 +338,8 @@ class MRFMap:
         _check(self._L.mrf_warm_features(self._h, C.c_void_p(feat_dev_ptr)))
 
     def set_precision(self, mode: int):
-        """PRECISION_HALF_STREAMS (default: fp16 lengths and ln q gathers
-        in the ray kernel) or PRECISION_FP32."""
+        """PRECISION_FP32 (default) or PRECISION_HALF_STREAMS (fp16 lengths
+        and ln q gathers in the ray kernel)."""
         _check(self._L.mrf_set_precision(self._h, mode))
 
     def set_ray_variant(self, variant: int):

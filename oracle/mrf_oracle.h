@@ -38,7 +38,7 @@ typedef struct {
 
 /* activation policies */
 #define ORC_ACT_ENDPOINT 0   /* bricks around measured endpoints (reference) */
-#define ORC_ACT_FULL_RAY 1   /* + every brick the ray crosses up to d+3sigma */
+#define ORC_ACT_FULL_RAY 1   /* + every brick the ray crosses up to its Pre stop */
 
 /* inference flags */
 #define ORC_JACOBI        1  /* all cameras from one snapshot per iteration */
