@@ -747,6 +747,7 @@ def run_large(args):
             "per_frame_ms": {"build": build_ms / max(n, 1), "bp": infer_ms / max(n, 1),
                              "other": 1e3 * dt / max(n, 1) - (build_ms + infer_ms) / max(n, 1)},
             "device_bytes_peak": peak, "n_bricks_final": nb,
+            "list_builds": {"full": st["builds_full"], "appended": st["builds_appended"]},
             "occupied_voxels_final": int((bel > 0.5).sum()),
             "clocks": clk,
             "e2e": {"value": sum_over_ranks(n, ws) / dt, "unit": "frames/s",
