@@ -334,7 +334,7 @@ def run_reference(args):
 
 
 # bumped whenever k_ray_bp's memory traffic changes (profiles/ray_bp_traffic.json)
-RAY_KERNEL_VERSION = 6
+RAY_KERNEL_VERSION = 7
 
 
 def ray_kernel_bytes(st, iters, half=False):
@@ -342,10 +342,11 @@ def ray_kernel_bytes(st, iters, half=False):
     the rays it runs over (those with a dynamic incidence): per Pre
     incidence the pair id (4 B), the length and the ln q gather (4 B each
     with the default fp32 streams, 2 B each with 16-bit streams); per dynamic
-    incidence (from the ray's first non-zero potential on) +8 B (potential
-    4, message write 4); per ray 16 B of metadata."""
+    incidence (from the ray's first non-zero potential on) +12 B (potential
+    4, the message's pair-grouped slot 4, message write 4); per ray 16 B of
+    metadata."""
     per_pre = 8 if half else 12
-    return (per_pre * st["n_inc_pre_bp"] + 8 * st["n_inc_dyn"] + 16 * st["n_rays_bp"]) * iters
+    return (per_pre * st["n_inc_pre_bp"] + 12 * st["n_inc_dyn"] + 16 * st["n_rays_bp"]) * iters
 
 
 LONG_RAY = 512  # Pre incidences above which the ray kernel sums in FP64

@@ -14,7 +14,10 @@
 //                  dynamic incidence first, each part brick-major by first
 //                  visit along the rays (mrf_build.cu, k_pair_first)
 //   grouped        u32 incidence per pair-grouped position [N_pre] (CSR
-//                  by pair; the dynamic positions again in dperm)
+//                  by pair); per dynamic incidence its position in the
+//                  pair-grouped order of the dynamic ones (dslot, indexed
+//                  by incidence), and the messages at those positions
+//                  (dmsg, written by the ray kernel)
 //   ray queues     RayMeta records in queue order: longest first, and the
 //                  SM-affine regions (home rays per region, leftovers)
 #include <cuda_runtime.h>
@@ -199,8 +202,8 @@ struct mrf_map {
   bool has_messages = false;
   std::vector<View> views;
   // arenas
-  DBuf meta, inc_pair, inc_len, inc_mu, inc_pl, pair_vox, pair_m, pair_cum, pair_stat, pair_ndyn, pair_hit,
-      pair_q, pair_dm, pair_seg, dperm, s_q0, s_q1, s_q2, s_q3, s_bf, s_loud, s_pv, s_sg, dpair, dseg, drun, carry, ray_order, ray_queue, region_q, rstart, rcounters, counters,
+  DBuf meta, inc_pair, inc_len, inc_mu, inc_dslot, pair_vox, pair_m, pair_cum, pair_stat, pair_ndyn, pair_hit,
+      pair_q, pair_dm, pair_seg, dmsg, s_q0, s_q1, s_q2, s_q3, s_bf, s_loud, s_pv, s_sg, dpair, dseg, drun, carry, ray_order, ray_queue, region_q, rstart, rcounters, counters,
       tile_first, lbase, lsingle, lprefix;
   uint32_t jac_tile_base = 0;
   int64_t n_inc = 0, n_pairs = 0, n_dperm = 0, n_dpairs = 0;
@@ -240,8 +243,8 @@ struct mrf_map {
     a.inc_pair = inc_pair.as<uint32_t>();
     a.inc_len = inc_len.as<float>();
     a.inc_mu = inc_mu.as<float>();
-    a.inc_pl = inc_pl.as<float>();
-    a.dperm = dperm.as<uint32_t>();
+    a.inc_dslot = inc_dslot.as<uint32_t>();
+    a.dmsg = dmsg.as<float>();
     a.dpair = dpair.as<uint32_t>();
     a.dseg = dseg.as<uint32_t>();
     a.drun = drun.as<uint4>();
@@ -516,7 +519,7 @@ void view_pairs(mrf_map* m, int c, int bits, int64_t& pair_total, int64_t& perm_
                           m->stream));
     uint32_t nd = read1(m, m->s_v0.as<uint32_t>() + nr);
     CK(launch_dyn_scatter(m->s_v1.as<uint32_t>(), m->s_k0.as<uint32_t>(), m->s_v0.as<uint32_t>(), nr,
-                          v.inc_base, v.dperm_base, m->dperm.as<uint32_t>(), m->stream));
+                          v.inc_base, v.dperm_base, m->inc_dslot.as<uint32_t>(), m->stream));
     m->s_pf.reserve((size_t)np * 4 + 4, false, m->stream);
     m->s_ps.reserve((size_t)np * 4 + 4, false, m->stream);
     CK(launch_dpair_flags(m->pair_ndyn.as<uint32_t>(), v.pair_base, np, m->s_pf.as<uint32_t>(),
@@ -842,8 +845,8 @@ void rebuild_lists(mrf_map* m, OldPairs& old) {
     m->inc_pair.reserve(ib, false, m->stream);
     m->inc_len.reserve(ib, false, m->stream);
     m->inc_mu.reserve(ib, false, m->stream);
-    m->dperm.reserve(ib, false, m->stream);
-    m->inc_pl.reserve(ib, false, m->stream);
+    m->dmsg.reserve(ib, false, m->stream);
+    m->inc_dslot.reserve(ib, false, m->stream);
     m->s_vox.reserve(ib, false, m->stream);
     m->s_rec.reserve(ib * 2, false, m->stream);
   }
@@ -1060,8 +1063,8 @@ bool append_lists(mrf_map* m) {
     m->inc_len.reserve(ib, true, m->stream);
     m->inc_mu.reserve(ib, true, m->stream);
     m->inc_pair.reserve(ib, true, m->stream);
-    m->inc_pl.reserve(ib, true, m->stream);
-    m->dperm.reserve((size_t)(m->n_dperm + (n_inc - m->n_inc)) * 4 + 4, true, m->stream);
+    m->inc_dslot.reserve(ib, true, m->stream);
+    m->dmsg.reserve((size_t)(m->n_dperm + (n_inc - m->n_inc)) * 4 + 4, true, m->stream);
     // scratch of the build: only the new views' parts are written and read
     m->s_vox.reserve(ib, false, m->stream);
     m->s_rec.reserve(ib * 2, false, m->stream);
@@ -1619,10 +1622,10 @@ mrf_status wrap(F&& f) {
 
 void destroy_bufs(mrf_map* m) {
   DBuf* all[] = {&m->d_sigma, &m->d_bias, &m->d_slot, &m->d_coord, &m->d_L, &m->d_belief,
-                 &m->meta, &m->inc_pair, &m->inc_len, &m->inc_mu, &m->inc_pl, &m->pair_vox,
+                 &m->meta, &m->inc_pair, &m->inc_len, &m->inc_mu, &m->inc_dslot, &m->pair_vox,
                  &m->pair_m, &m->pair_cum, &m->pair_stat, &m->pair_ndyn, &m->pair_hit, &m->pair_q,
                  &m->pair_dm,
-                 &m->pair_seg, &m->dperm, &m->dpair, &m->dseg, &m->drun,
+                 &m->pair_seg, &m->dmsg, &m->dpair, &m->dseg, &m->drun,
                  &m->carry, &m->ray_order, &m->ray_queue, &m->region_q, &m->rstart, &m->rcounters, &m->counters, &m->tile_first,
                  &m->lbase, &m->lsingle, &m->lprefix,
                  &m->vseg, &m->vpairs, &m->vvox, &m->vox_active, &m->d_Lbase, &m->inc_len16, &m->pair_q16,
