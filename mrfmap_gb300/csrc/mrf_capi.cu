@@ -1016,7 +1016,9 @@ bool append_lists(mrf_map* m) {
   m->g.brick_slot = m->d_slot.as<int>();
   for (View& v : m->views) v.cam.brick_slot = m->g.brick_slot;
   if (m->n_bricks != m->bricks_at_build) {
-    CK(cudaMemsetAsync(m->s_err.p, 0, 8, m->stream));
+    // err[1]: the count pass's mismatch flag (err[0], the kernels' error
+    // flag, is left as it is and checked below)
+    CK(cudaMemsetAsync(m->s_err.as<int>() + 1, 0, 4, m->stream));
     for (int c = 0; c < m->built_views; ++c) {
       const View& v = m->views[c];
       const int64_t hw = view_pixels(v);
@@ -1028,11 +1030,11 @@ bool append_lists(mrf_map* m) {
     int flags[2] = {0, 0};
     CK(cudaMemcpyAsync(flags, m->s_err.p, 8, cudaMemcpyDeviceToHost, m->stream));
     sync(m);
+    check_device_err(m);
     if (flags[1]) {
-      CK(cudaMemsetAsync(m->s_err.p, 0, 8, m->stream));
+      CK(cudaMemsetAsync(m->s_err.as<int>() + 1, 0, 4, m->stream));
       return false;
     }
-    check_device_err(m);
   }
   std::vector<int> added;
   for (int c = m->built_views; c < V; ++c)
