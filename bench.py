@@ -334,7 +334,10 @@ def run_reference(args):
 
 
 # bumped whenever k_ray_bp's memory traffic changes (profiles/ray_bp_traffic.json)
-RAY_KERNEL_VERSION = 7
+RAY_KERNEL_VERSION = 6
+
+
+HOME_SHARES = (60, 75, 90)  # per cent of an SM region's work on its home blocks, tried by the autotuner
 
 
 def ray_kernel_bytes(st, iters, half=False):
@@ -342,11 +345,10 @@ def ray_kernel_bytes(st, iters, half=False):
     the rays it runs over (those with a dynamic incidence): per Pre
     incidence the pair id (4 B), the length and the ln q gather (4 B each
     with the default fp32 streams, 2 B each with 16-bit streams); per dynamic
-    incidence (from the ray's first non-zero potential on) +12 B (potential
-    4, the message's pair-grouped slot 4, message write 4); per ray 16 B of
-    metadata."""
+    incidence (from the ray's first non-zero potential on) +8 B (potential
+    4, message write 4); per ray 16 B of metadata."""
     per_pre = 8 if half else 12
-    return (per_pre * st["n_inc_pre_bp"] + 12 * st["n_inc_dyn"] + 16 * st["n_rays_bp"]) * iters
+    return (per_pre * st["n_inc_pre_bp"] + 8 * st["n_inc_dyn"] + 16 * st["n_rays_bp"]) * iters
 
 
 LONG_RAY = 512  # Pre incidences above which the ray kernel sums in FP64
@@ -438,6 +440,10 @@ def run_ours(args):
     else:
         m.set_ray_variant(args.ray_variant)
         tuned, tune_ms = args.ray_variant, []
+    # the SM-region schedule's home share, likewise (moves rays, not results)
+    share_ms = []
+    if args.ray_variant is None:
+        _, share_ms = m.autotune_home_share(HOME_SHARES, reps=2)
     st = m.stats()
     n_upd_step = st["n_inc_post"] * iters
     stream = torch.cuda.ExternalStream(m.stream())
@@ -632,6 +638,8 @@ def run_ours(args):
                                "n_rays": st["n_rays"], "n_rays_bp": st["n_rays_bp"],
                                "n_inc_pre_bp_per_iter": st["n_inc_pre_bp"], "n_bricks": st["n_bricks"],
                                "ray_variant": tuned, "ray_variant_ms": [round(x, 4) for x in tune_ms],
+                               "home_share": m.tuning()[1], "home_share_ms": dict(zip(HOME_SHARES[:len(share_ms)],
+                                                                                     [round(float(x), 4) for x in share_ms])),
                                "static_messages": "exact constants (p = F_EPS before a ray's first "
                                                   "non-zero potential), summed once per build"},
             "dynamic_updates_per_s": st["n_inc_dyn"] * iters * args.steps / (ms / 1e3),
@@ -814,6 +822,7 @@ def run_batched(args):
     m.infer(iters=1, flags=L.JACOBI)  # incidence lists, voxel CSR
     build_s = time.perf_counter() - t0
     tuned, tune_ms = m.autotune(reps=2, flags=L.JACOBI)
+    _, share_ms = m.autotune_home_share(HOME_SHARES, reps=2, flags=L.JACOBI)
     st = m.stats()
     stream = torch.cuda.ExternalStream(m.stream())
     for _ in range(args.warmup):
@@ -839,6 +848,7 @@ def run_batched(args):
     m.reset_state()
     m.infer(iters=iters, flags=L.JACOBI | L.PROFILE)
     prof = m.stats()
+    share_choice = m.tuning()[1]
     m.close()
     peaks = {}
     try:
@@ -873,7 +883,9 @@ def run_batched(args):
             "workload_stats": {"n_inc_per_iter": st["n_inc_post"], "n_inc_dyn_per_iter": st["n_inc_dyn"],
                                "n_pairs": st["n_pairs"], "n_rays": st["n_rays"], "n_bricks": st["n_bricks"],
                                "build_s": round(build_s, 3), "ray_variant": tuned,
-                               "ray_variant_ms": [round(x, 4) for x in tune_ms]},
+                               "ray_variant_ms": [round(x, 4) for x in tune_ms],
+                               "home_share": share_choice,
+                               "home_share_ms": dict(zip(HOME_SHARES, [round(float(x), 4) for x in share_ms]))},
             "ray_launches_per_iter": k_n / iters,
             "kernel_share": {n: round(v / max(sum(prof["kernel_ms"]), 1e-9), 4)
                              for n, v in zip(("pair_prepare", "ray_bp", "pair_update", "voxel_apply"),

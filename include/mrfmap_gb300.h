@@ -244,9 +244,11 @@ MRF_API mrf_status mrf_net_adam(float* params, const float* grads, float* m1, fl
                                 float lr, float beta1, float beta2, float eps, int step, void* stream);
 
 /* Autotuner (no reference counterpart).  The ray-message kernel comes in
- * variants that differ in the cache policy of its streamed loads and in
- * whether a chunk's pair ids are requested one chunk ahead; their
- * arithmetic is identical, so the choice never changes a result.
+ * variants that differ in the cache policy of its streamed loads, in
+ * whether a chunk's pair ids are requested one chunk ahead, in the ray
+ * schedule (longest first or SM regions) and in the register budget (a
+ * 12-block-per-SM target caps a thread at 40 registers); their arithmetic
+ * is identical, so the choice never changes a result.
  * mrf_autotune times every variant on this map's own incidence lists (reps
  * timed Gauss-Seidel iterations after one warm-up, the map state saved
  * before and restored after each variant), keeps the fastest and returns
@@ -258,6 +260,23 @@ MRF_API mrf_status mrf_autotune(mrf_map* map, int reps, double* ms_out, int cap,
 /* The same with the schedule of the timed iterations in flags (MRF_JACOBI:
  * Jacobi iterations, one ray launch over every view; else Gauss-Seidel). */
 MRF_API mrf_status mrf_autotune_flags(mrf_map* map, int reps, int flags, double* ms_out, int cap, int* chosen);
+
+/* SM-region schedule of the ray kernel (no reference counterpart): each
+ * SM's region hands its longest rays, up to `percent` of the region's
+ * incidences, to the blocks homed on that SM; the rest go to the view's
+ * shared leftover queue.  Default 75.  It only moves rays between warps, so
+ * results do not change.  mrf_autotune_home_share times `n` shares
+ * (1..100) on this map's lists (reps iterations each after a warm-up, the
+ * map state restored after each), keeps the fastest, and returns the
+ * per-share milliseconds per iteration in ms_out[0..n) (may be NULL).
+ * The pair-update tile and the ray chunk are not tuned: both change the
+ * order of floating-point sums, and a choice made from timings would make
+ * results differ from run to run.  mrf_get_tuning reports the current
+ * ray-kernel variant and home share. */
+MRF_API mrf_status mrf_set_home_share(mrf_map* map, int percent);
+MRF_API mrf_status mrf_autotune_home_share(mrf_map* map, int reps, int flags, const int* shares, int n,
+                                           double* ms_out, int* chosen);
+MRF_API mrf_status mrf_get_tuning(mrf_map* map, int* ray_variant, int* home_share);
 
 /* Storage precision of the ray kernel's streams (no reference counterpart;
  * the reference stores half2 channels, gvdbkernels.cu:975-978):

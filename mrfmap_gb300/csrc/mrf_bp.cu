@@ -290,19 +290,15 @@ __device__ __forceinline__ float slice_value(const Slice<KE>& s, int idx) {
   return __shfl_sync(kFull, mine, idx / KE);
 }
 
-// pass 2 on one lane's slice: messages p*l for positions i0..i0+KE-1; each
-// dynamic one (kdyn <= i < n_post) is written to its pair-grouped position
-// (slot, loaded by the caller for the vectors starting inside [k4, n_post),
-// k4 = kdyn rounded down to 4), where the pair update reads the messages
-// of a pair contiguously.  cF is F at the chunk start and D = T - cF, formed
-// in the ray's accumulation type by the caller; returns the chunk's total
-// of tau.
+// pass 2 on one lane's slice: messages p*l for positions i0..i0+KE-1; the
+// vectors starting inside [k4, n_post) are written (k4 a multiple of 4).
+// cF is F at the chunk start and D = T - cF, formed in the ray's
+// accumulation type by the caller; returns the chunk's total of tau.
 template <int KE, bool kWhole>
 __device__ __forceinline__ float emit_slice(const float (&vmu)[KE], const float (&q)[KE],
-                                            const float (&len)[KE], int i0, int kdyn, int n_post,
-                                            float cF, float D, int lane, const uint4 (&slot)[KE / 4],
-                                            float* __restrict__ dmsg) {
-  static_assert(KE % 4 == 0, "slices are whole 16-byte vectors");
+                                            const float (&len)[KE], int i0, int k4, int n_post,
+                                            float cF, float D, int lane, uint32_t off,
+                                            float* __restrict__ inc_pl) {
   float tau[KE], eloc[KE];
   float run = 0.0f;
 #pragma unroll
@@ -323,13 +319,17 @@ __device__ __forceinline__ float emit_slice(const float (&vmu)[KE], const float 
     float p = clampf(__fdividef(mu1, mu1 + mu0 + 1e-7f), kFEps, 1.0f - kFEps);
     out[j] = (kWhole || i0 + j < n_post) ? p * len[j] : 0.0f;
   }
+  constexpr int VW = KE % 4 == 0 ? 4 : KE;
 #pragma unroll
-  for (int v = 0; v < KE / 4; ++v) {
-    const int i = i0 + 4 * v;
-    const uint32_t sl[4] = {slot[v].x, slot[v].y, slot[v].z, slot[v].w};
-#pragma unroll
-    for (int e = 0; e < 4; ++e)
-      if (i + e >= kdyn && (kWhole || i + e < n_post)) dmsg[sl[e]] = out[4 * v + e];
+  for (int v = 0; v < KE / VW; ++v) {
+    const int i = i0 + VW * v;
+    if (i >= k4 && (kWhole || i < n_post)) {
+      if constexpr (VW == 4)
+        *reinterpret_cast<float4*>(inc_pl + off + i) =
+            make_float4(out[4 * v], out[4 * v + 1], out[4 * v + 2], out[4 * v + 3]);
+      else
+        *reinterpret_cast<float2*>(inc_pl + off + i) = make_float2(out[2 * v], out[2 * v + 1]);
+    }
   }
   return __shfl_sync(kFull, ex + run, 31);
 }
@@ -373,9 +373,8 @@ template <typename Acc, int kPol, int kPf, typename TL, typename TQ>
 __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, const uint32_t* __restrict__ inc_pair,
                                             const TL* __restrict__ inc_len,
                                             const float* __restrict__ inc_mu,
-                                            const TQ* __restrict__ lnq,
-                                            const uint32_t* __restrict__ inc_dslot,
-                                            float* __restrict__ dmsg, int fix_reset, int lane) {
+                                            const TQ* __restrict__ lnq, float* __restrict__ inc_pl,
+                                            int fix_reset, int lane) {
   const int n_pre = me.n_pre, n_post = me.n_post;
   const int r0 = fix_reset ? 0 : me.r0;
   const int rinf = fix_reset ? 0 : me.rinf;
@@ -441,15 +440,6 @@ __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, const uint32_t* _
   for (int base = k4; base < n_post; base += kChunk) {
     const int i0 = base + kE * lane;
     const bool full = base + kChunk <= n_post;
-    // the slots of this lane's messages, requested before the slice's loads
-    uint4 slot[kE / 4];
-#pragma unroll
-    for (int v = 0; v < kE / 4; ++v) {
-      const int i = i0 + 4 * v;
-      slot[v] = (i >= k4 && (full || i < n_post))
-                    ? ld_stream<kPol>(reinterpret_cast<const uint4*>(inc_dslot + off + i))
-                    : make_uint4(0u, 0u, 0u, 0u);
-    }
     const float tot2 =
         full ? load_slice<kE, kPol, true>(s, off, i0, n_post, k4, carryA2, lane, inc_pair, inc_len, inc_mu,
                                           lnq)
@@ -463,8 +453,8 @@ __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, const uint32_t* _
       q[j] = __expf(s.lq[j]);
     }
     const float D = (float)Dd;
-    const float ct = full ? emit_slice<kE, true>(vmu, q, s.len, i0, kdyn, n_post, cF, D, lane, slot, dmsg)
-                          : emit_slice<kE, false>(vmu, q, s.len, i0, kdyn, n_post, cF, D, lane, slot, dmsg);
+    const float ct = full ? emit_slice<kE, true>(vmu, q, s.len, i0, k4, n_post, cF, D, lane, off, inc_pl)
+                          : emit_slice<kE, false>(vmu, q, s.len, i0, k4, n_post, cF, D, lane, off, inc_pl);
     Dd -= (Acc)ct;
     cF += ct;
   }
@@ -498,17 +488,14 @@ __global__ void __launch_bounds__(kRayWarps * 32, kMinBlocks) k_ray_bp(const Ray
                                                            const TL* __restrict__ inc_len,
                                                            const float* __restrict__ inc_mu,
                                                            const TQ* __restrict__ lnq,
-                                                           const uint32_t* __restrict__ inc_dslot,
-                                                           float* __restrict__ dmsg,
+                                                           float* __restrict__ inc_pl,
                                                            int fix_reset) {
   const int lane = threadIdx.x & 31;
   auto ray = [&](const RayMeta& me) {
     if (me.n_pre <= kLongRay)
-      ray_bp_warp<float, kPol, kPf, TL, TQ>(me, inc_pair, inc_len, inc_mu, lnq, inc_dslot, dmsg, fix_reset,
-                                            lane);
+      ray_bp_warp<float, kPol, kPf, TL, TQ>(me, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
     else
-      ray_bp_warp<double, kPol, kPf, TL, TQ>(me, inc_pair, inc_len, inc_mu, lnq, inc_dslot, dmsg, fix_reset,
-                                             lane);
+      ray_bp_warp<double, kPol, kPf, TL, TQ>(me, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
   };
   if constexpr (kReg) {
     // counter[r]: tickets of region r, whose home rays are positions
@@ -579,12 +566,12 @@ __global__ void k_ray_keys(const RayMeta* __restrict__ meta, uint32_t n, uint32_
   vals[r] = r;
 }
 
-// Pair update: a load-balanced segmented reduction over the dynamic
-// messages, which the ray kernel wrote in pair-grouped order, fused with the
-// per-pair update.  One block takes a tile of kTile consecutive positions:
-// it loads the tile's messages into shared memory (coalesced) together with
-// the segment bounds of the pairs the tile touches; each thread then sums
-// whole pairs sequentially from shared memory
+// Pair update: a load-balanced segmented reduction over the pair-grouped
+// permutation of the messages, fused with the per-pair update.  One block
+// takes a tile of kTile consecutive positions: it gathers the tile's messages
+// into shared memory (coalesced permutation reads, kTile independent gathers
+// in flight) together with the segment bounds of the pairs the tile
+// touches; each thread then sums whole pairs sequentially from shared memory
 // (a fixed order) and updates the pairs that lie inside the tile.  Segments
 // that cross tile edges leave partial sums that k_pair_fixup adds in tile
 // order.  Any segment length balances: voxels next to the camera are crossed
@@ -642,7 +629,8 @@ __device__ __forceinline__ void apply_run(const uint4 r, float acc_dyn, float* _
 }
 
 __global__ void __launch_bounds__(kTileThreads, 8)
-    k_pair_reduce(const float* __restrict__ pl, const uint32_t* __restrict__ seg, const uint32_t* __restrict__ tile_first,
+    k_pair_reduce(const uint32_t* __restrict__ perm, const float* __restrict__ pl,
+                  const uint32_t* __restrict__ seg, const uint32_t* __restrict__ tile_first,
                   uint32_t k0, uint32_t k1, uint32_t p_end, TileCarry* __restrict__ carry,
                   const uint4* __restrict__ drun, float* __restrict__ m, float* __restrict__ L,
                   float* __restrict__ dm, int jacobi) {
@@ -665,7 +653,7 @@ __global__ void __launch_bounds__(kTileThreads, 8)
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
     uint32_t i = j * kTileThreads + t;
-    if (i < n) sv[i] = pl[base + i];
+    if (i < n) sv[i] = pl[perm[base + i]];
   }
   for (uint32_t q = t; q < nseg; q += kTileThreads) sseg[q] = seg[pf + q];
   const bool gate0 = pre && __uint_as_float(r0.z) > kCumLenGate;
@@ -1027,8 +1015,9 @@ cudaError_t launch_pair_prepare(const BpArrays& a, uint32_t p0, uint32_t p1, int
 // ray-kernel variants: (id, resident-block target, load policy, chunk
 // prefetch, schedule: 0 longest first, 1 SM regions)
 #define MRF_RAY_VARIANTS(X) \
-  X(0, 0, 0, 0, 0) X(1, 0, 0, 1, 0) X(2, 0, 0, 2, 0) X(3, 0, 0, 0, 1) X(4, 0, 0, 1, 1) X(5, 0, 0, 2, 1)
-constexpr int kRayVariants = 6;
+  X(0, 0, 0, 0, 0) X(1, 0, 0, 1, 0) X(2, 0, 0, 2, 0) X(3, 0, 0, 0, 1) X(4, 0, 0, 1, 1) X(5, 0, 0, 2, 1) \
+  X(6, 12, 0, 1, 1) X(7, 12, 1, 1, 1)
+constexpr int kRayVariants = 8;
 
 int ray_bp_variants() { return kRayVariants; }
 
@@ -1076,12 +1065,12 @@ cudaError_t launch_ray_bp(const BpArrays& a, const RayWork& w, int fix_reset, in
       k_ray_bp<mb, pol, pf, (sc > 0), __half, __half><<<grid, kRayWarps * 32, 0, s>>>(            \
           sc == 0 ? w.queue : w.region, w.n_rays, w.rstart, w.nreg, w.rper, w.lprefix, w.lbase,    \
           w.nlv, w.lcounter, sc == 0 ? w.counter : w.rcounter, a.inc_pair, a.inc_len16, a.inc_mu,  \
-          a.pair_lnq16, a.inc_dslot, a.dmsg, fix_reset);                                          \
+          a.pair_lnq16, a.inc_pl, fix_reset);                                                     \
     else                                                                                          \
       k_ray_bp<mb, pol, pf, (sc > 0), float, float><<<grid, kRayWarps * 32, 0, s>>>(              \
           sc == 0 ? w.queue : w.region, w.n_rays, w.rstart, w.nreg, w.rper, w.lprefix, w.lbase,    \
           w.nlv, w.lcounter, sc == 0 ? w.counter : w.rcounter, a.inc_pair, a.inc_len, a.inc_mu,    \
-          a.pair_lnq, a.inc_dslot, a.dmsg, fix_reset);                                            \
+          a.pair_lnq, a.inc_pl, fix_reset);                                                       \
     break;
     MRF_RAY_VARIANTS(X)
 #undef X
@@ -1109,7 +1098,7 @@ cudaError_t launch_pair_update(const BpArrays& a, uint32_t k0, uint32_t k1, uint
   (void)j0;
   if (k1 <= k0) return cudaSuccess;
   uint32_t ntiles = (k1 - k0 + kTile - 1) / kTile;
-  k_pair_reduce<<<ntiles, kTileThreads, 0, s>>>(a.dmsg, a.dseg, tile_first, k0, k1, j1,
+  k_pair_reduce<<<ntiles, kTileThreads, 0, s>>>(a.dperm, a.inc_pl, a.dseg, tile_first, k0, k1, j1,
                                                 carry, a.drun, a.pair_m, a.L, a.pair_dm, jacobi);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;

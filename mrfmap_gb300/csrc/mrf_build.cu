@@ -573,14 +573,11 @@ __global__ void k_dyn_flags(const float2* __restrict__ srec, uint32_t n, uint32_
   if (k < n) flag[k] = signbit(srec[k].y) ? 1u : 0u;
 }
 
-// the pair-grouped position of each dynamic incidence (the ray kernel
-// writes the incidence's message there); other incidences' slots are left
-// as they are and never read
 __global__ void k_dyn_scatter(const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ flag,
                               const uint32_t* __restrict__ scan, uint32_t n, uint32_t inc_base,
-                              uint32_t dperm_base, uint32_t* __restrict__ dslot) {
+                              uint32_t dperm_base, uint32_t* __restrict__ dperm) {
   uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k < n && flag[k]) dslot[inc_base + sidx[k]] = dperm_base + scan[k];
+  if (k < n && flag[k]) dperm[dperm_base + scan[k]] = inc_base + sidx[k];
 }
 
 __global__ void k_dpair_flags(const uint32_t* __restrict__ ndyn, uint32_t p0, uint32_t np,
@@ -781,10 +778,10 @@ cudaError_t launch_dyn_flags(const float2* srec, uint32_t n, uint32_t* flag, cud
 }
 
 cudaError_t launch_dyn_scatter(const uint32_t* sidx, const uint32_t* flag, const uint32_t* scan,
-                               uint32_t n, uint32_t inc_base, uint32_t dperm_base, uint32_t* dslot,
+                               uint32_t n, uint32_t inc_base, uint32_t dperm_base, uint32_t* dperm,
                                cudaStream_t s) {
   if (!n) return cudaSuccess;
-  k_dyn_scatter<<<grid_for(n), kThreads, 0, s>>>(sidx, flag, scan, n, inc_base, dperm_base, dslot);
+  k_dyn_scatter<<<grid_for(n), kThreads, 0, s>>>(sidx, flag, scan, n, inc_base, dperm_base, dperm);
   return cudaGetLastError();
 }
 

@@ -14,10 +14,7 @@
 //                  dynamic incidence first, each part brick-major by first
 //                  visit along the rays (mrf_build.cu, k_pair_first)
 //   grouped        u32 incidence per pair-grouped position [N_pre] (CSR
-//                  by pair); per dynamic incidence its position in the
-//                  pair-grouped order of the dynamic ones (dslot, indexed
-//                  by incidence), and the messages at those positions
-//                  (dmsg, written by the ray kernel)
+//                  by pair; the dynamic positions again in dperm)
 //   ray queues     RayMeta records in queue order: longest first, and the
 //                  SM-affine regions (home rays per region, leftovers)
 #include <cuda_runtime.h>
@@ -174,6 +171,8 @@ uint32_t u32_checked(int64_t v, const char* what) {
 
 }  // namespace
 
+constexpr int kHomeShare = 75;  // default per cent of a region's incidences taken by its home blocks
+
 struct mrf_map {
   mrf_params prm;
   std::vector<float> sigma, bias;
@@ -202,8 +201,8 @@ struct mrf_map {
   bool has_messages = false;
   std::vector<View> views;
   // arenas
-  DBuf meta, inc_pair, inc_len, inc_mu, inc_dslot, pair_vox, pair_m, pair_cum, pair_stat, pair_ndyn, pair_hit,
-      pair_q, pair_dm, pair_seg, dmsg, s_q0, s_q1, s_q2, s_q3, s_bf, s_loud, s_pv, s_sg, dpair, dseg, drun, carry, ray_order, ray_queue, region_q, rstart, rcounters, counters,
+  DBuf meta, inc_pair, inc_len, inc_mu, inc_pl, pair_vox, pair_m, pair_cum, pair_stat, pair_ndyn, pair_hit,
+      pair_q, pair_dm, pair_seg, dperm, s_q0, s_q1, s_q2, s_q3, s_bf, s_loud, s_pv, s_sg, dpair, dseg, drun, carry, ray_order, ray_queue, region_q, rstart, rcounters, counters,
       tile_first, lbase, lsingle, lprefix;
   uint32_t jac_tile_base = 0;
   int64_t n_inc = 0, n_pairs = 0, n_dperm = 0, n_dpairs = 0;
@@ -212,6 +211,7 @@ struct mrf_map {
   // MRF_PRECISION_HALF_STREAMS: fp16 copies of the segment lengths (per
   // build) and of ln q (written by k_pair_prepare)
   int precision = MRF_PRECISION_FP32;
+  int home_share = kHomeShare;  // SM-region schedule: per cent of a region's work on its home blocks
   DBuf inc_len16, pair_q16;
   int len16_version = -1;
   // logit(prior) + the messages of retired views, per voxel (kept once a view
@@ -243,8 +243,8 @@ struct mrf_map {
     a.inc_pair = inc_pair.as<uint32_t>();
     a.inc_len = inc_len.as<float>();
     a.inc_mu = inc_mu.as<float>();
-    a.inc_dslot = inc_dslot.as<uint32_t>();
-    a.dmsg = dmsg.as<float>();
+    a.inc_pl = inc_pl.as<float>();
+    a.dperm = dperm.as<uint32_t>();
     a.dpair = dpair.as<uint32_t>();
     a.dseg = dseg.as<uint32_t>();
     a.drun = drun.as<uint4>();
@@ -519,7 +519,7 @@ void view_pairs(mrf_map* m, int c, int bits, int64_t& pair_total, int64_t& perm_
                           m->stream));
     uint32_t nd = read1(m, m->s_v0.as<uint32_t>() + nr);
     CK(launch_dyn_scatter(m->s_v1.as<uint32_t>(), m->s_k0.as<uint32_t>(), m->s_v0.as<uint32_t>(), nr,
-                          v.inc_base, v.dperm_base, m->inc_dslot.as<uint32_t>(), m->stream));
+                          v.inc_base, v.dperm_base, m->dperm.as<uint32_t>(), m->stream));
     m->s_pf.reserve((size_t)np * 4 + 4, false, m->stream);
     m->s_ps.reserve((size_t)np * 4 + 4, false, m->stream);
     CK(launch_dpair_flags(m->pair_ndyn.as<uint32_t>(), v.pair_base, np, m->s_pf.as<uint32_t>(),
@@ -552,17 +552,16 @@ void view_pairs(mrf_map* m, int c, int bits, int64_t& pair_total, int64_t& perm_
 // (its longest rays up to kHomeShare of its incidences, longest first) are
 // taken by the blocks homed on it, every region's remaining short rays go to
 // the view's leftover queue (longest first) that the blocks drain
-// afterwards, which evens out the regions' finishing times (home shares of
-// 60, 75 and 85 % measured: 75 % best on the bench workloads).  Built on
+// afterwards, which evens out the regions' finishing times (the home share,
+// 75 % unless mrf_set_home_share or mrf_autotune_home_share chose another;
+// it moves rays between warps only, never a result).  Built on
 // the host in linear time: a counting sort by length feeds the regions'
 // buckets in order, so each bucket is longest first.  Pixel indices are
 // absolute (v.pix_base + i); starts are positions in home.
 struct RegionLists {
   std::vector<uint32_t> home, left, starts;
 };
-constexpr int64_t kHomeShare = 75;  // per cent of a region's incidences taken by its home blocks
-
-void region_lists(const View& v, const RayMeta* vm, int R, RegionLists& out) {
+void region_lists(const View& v, const RayMeta* vm, int R, int64_t share, RegionLists& out) {
   const int64_t hw = view_pixels(v);
   std::vector<uint32_t> lcount(65536, 0u), reg((size_t)hw, 0u), bucket_off((size_t)R + 1, 0u);
   int64_t work = 0;
@@ -592,14 +591,14 @@ void region_lists(const View& v, const RayMeta* vm, int R, RegionLists& out) {
   for (int64_t i = 0; i < hw; ++i)
     if (ray_in_bp(vm[i])) lsorted[lcount[65535 - vm[i].n_pre]++] = (uint32_t)i;
   for (uint32_t i : lsorted) buckets[fill[reg[i]]++] = i;
-  // home = each region's longest rays up to kHomeShare of its work
+  // home = each region's longest rays up to `share` per cent of its work
   std::vector<uint8_t> is_home((size_t)hw, 0);
   out.home.reserve(pos);
   for (int r = 0; r < R; ++r) {
     int64_t rw = 0, hwk = 0;
     for (uint32_t k = bucket_off[r]; k < bucket_off[r + 1]; ++k) rw += vm[buckets[k]].n_pre;
     out.starts.push_back((uint32_t)out.home.size());
-    for (uint32_t k = bucket_off[r]; k < bucket_off[r + 1] && hwk * 100 < rw * kHomeShare; ++k) {
+    for (uint32_t k = bucket_off[r]; k < bucket_off[r + 1] && hwk * 100 < rw * share; ++k) {
       const uint32_t i = buckets[k];
       is_home[i] = 1;
       hwk += vm[i].n_pre;
@@ -627,7 +626,7 @@ void region_lists_parallel(mrf_map* m, const std::vector<int>& views, const std:
       for (int k = next++; k < nv; k = next++) {
         try {
           const View& v = m->views[views[k]];
-          region_lists(v, hm.data() + (v.pix_base - hm_base), R, lists[(size_t)views[k]]);
+          region_lists(v, hm.data() + (v.pix_base - hm_base), R, m->home_share, lists[(size_t)views[k]]);
         } catch (...) {
           failed[(size_t)k] = 1;
         }
@@ -690,6 +689,31 @@ void leftover_prefix(mrf_map* m) {
   m->lprefix.reserve(pre.size() * 4, false, m->stream);
   CK(cudaMemcpyAsync(m->lprefix.p, pre.data(), pre.size() * 4, cudaMemcpyHostToDevice, m->stream));
   sync(m);
+}
+
+// the region blocks of every built view again, from their ray records (the
+// home share changed); the incidence lists stay as they are.  The caller
+// drops the captured graphs.
+void rebuild_regions(mrf_map* m) {
+  const int B = m->built_views;
+  if (m->built_version < 0 || B == 0 || m->npix_total == 0) return;
+  std::vector<RayMeta> hm((size_t)m->npix_total);
+  CK(cudaMemcpyAsync(hm.data(), m->meta.p, hm.size() * sizeof(RayMeta), cudaMemcpyDeviceToHost, m->stream));
+  sync(m);
+  std::vector<int> live, built;
+  for (int c = 0; c < B; ++c) {
+    built.push_back(c);
+    if (!m->views[c].retired) live.push_back(c);
+  }
+  std::vector<RegionLists> lists(m->views.size());
+  region_lists_parallel(m, live, hm, 0, lists);
+  for (int c : built)
+    if (m->views[c].retired) {
+      m->views[c].n_left = 0;
+      m->views[c].left_base = 0;
+    }
+  m->region_end = region_blocks(m, built, lists, 0u);
+  leftover_prefix(m);
 }
 
 // view c's active rays longest first (17-bit key radix sort on the GPU),
@@ -845,8 +869,8 @@ void rebuild_lists(mrf_map* m, OldPairs& old) {
     m->inc_pair.reserve(ib, false, m->stream);
     m->inc_len.reserve(ib, false, m->stream);
     m->inc_mu.reserve(ib, false, m->stream);
-    m->dmsg.reserve(ib, false, m->stream);
-    m->inc_dslot.reserve(ib, false, m->stream);
+    m->dperm.reserve(ib, false, m->stream);
+    m->inc_pl.reserve(ib, false, m->stream);
     m->s_vox.reserve(ib, false, m->stream);
     m->s_rec.reserve(ib * 2, false, m->stream);
   }
@@ -1065,8 +1089,8 @@ bool append_lists(mrf_map* m) {
     m->inc_len.reserve(ib, true, m->stream);
     m->inc_mu.reserve(ib, true, m->stream);
     m->inc_pair.reserve(ib, true, m->stream);
-    m->inc_dslot.reserve(ib, true, m->stream);
-    m->dmsg.reserve((size_t)(m->n_dperm + (n_inc - m->n_inc)) * 4 + 4, true, m->stream);
+    m->inc_pl.reserve(ib, true, m->stream);
+    m->dperm.reserve((size_t)(m->n_dperm + (n_inc - m->n_inc)) * 4 + 4, true, m->stream);
     // scratch of the build: only the new views' parts are written and read
     m->s_vox.reserve(ib, false, m->stream);
     m->s_rec.reserve(ib * 2, false, m->stream);
@@ -1624,10 +1648,10 @@ mrf_status wrap(F&& f) {
 
 void destroy_bufs(mrf_map* m) {
   DBuf* all[] = {&m->d_sigma, &m->d_bias, &m->d_slot, &m->d_coord, &m->d_L, &m->d_belief,
-                 &m->meta, &m->inc_pair, &m->inc_len, &m->inc_mu, &m->inc_dslot, &m->pair_vox,
+                 &m->meta, &m->inc_pair, &m->inc_len, &m->inc_mu, &m->inc_pl, &m->pair_vox,
                  &m->pair_m, &m->pair_cum, &m->pair_stat, &m->pair_ndyn, &m->pair_hit, &m->pair_q,
                  &m->pair_dm,
-                 &m->pair_seg, &m->dmsg, &m->dpair, &m->dseg, &m->drun,
+                 &m->pair_seg, &m->dperm, &m->dpair, &m->dseg, &m->drun,
                  &m->carry, &m->ray_order, &m->ray_queue, &m->region_q, &m->rstart, &m->rcounters, &m->counters, &m->tile_first,
                  &m->lbase, &m->lsingle, &m->lprefix,
                  &m->vseg, &m->vpairs, &m->vvox, &m->vox_active, &m->d_Lbase, &m->inc_len16, &m->pair_q16,
@@ -2186,6 +2210,93 @@ mrf_status mrf_set_ray_variant(mrf_map* m, int variant) {
   m->ray_variant = variant;
   drop_graphs(m);
   return MRF_OK;
+}
+
+// reps timed iterations (after one warm-up) of the map's current schedule,
+// the BP state saved before and restored after: milliseconds per iteration
+static double time_schedule(mrf_map* m, bool jacobi, int reps) {
+  if (m->n_inc <= 0) return 0.0;
+  BpArrays a = m->bp();
+  const size_t nv = (size_t)m->n_bricks * kBrickVox * 4, npb = (size_t)m->n_pairs * 4;
+  m->s_snap.reserve(2 * nv + npb, false, m->stream);
+  char* snap = static_cast<char*>(m->s_snap.p);
+  CK(cudaMemcpyAsync(snap, m->d_L.p, nv, cudaMemcpyDeviceToDevice, m->stream));
+  CK(cudaMemcpyAsync(snap + nv, m->d_belief.p, nv, cudaMemcpyDeviceToDevice, m->stream));
+  CK(cudaMemcpyAsync(snap + 2 * nv, m->pair_m.p, npb, cudaMemcpyDeviceToDevice, m->stream));
+  Profiler off{m, false};
+  int64_t launches = 0;
+  for (int r = 0; r <= reps; ++r) {
+    if (r == 1) CK(cudaEventRecord(m->ev0, m->stream));
+    enqueue_iteration(m, a, jacobi, 0, 2, off, launches);
+  }
+  CK(cudaEventRecord(m->ev1, m->stream));
+  sync(m);
+  float t = 0.0f;
+  CK(cudaEventElapsedTime(&t, m->ev0, m->ev1));
+  CK(cudaMemcpyAsync(m->d_L.p, snap, nv, cudaMemcpyDeviceToDevice, m->stream));
+  CK(cudaMemcpyAsync(m->d_belief.p, snap + nv, nv, cudaMemcpyDeviceToDevice, m->stream));
+  CK(cudaMemcpyAsync(m->pair_m.p, snap + 2 * nv, npb, cudaMemcpyDeviceToDevice, m->stream));
+  sync(m);
+  return t / reps;
+}
+
+mrf_status mrf_set_home_share(mrf_map* m, int percent) {
+  if (guard(m) != MRF_OK) return MRF_ERR_INVALID;
+  if (percent < 1 || percent > 100) {
+    set_err("home share must be 1..100 per cent");
+    return MRF_ERR_INVALID;
+  }
+  if (percent == m->home_share) return MRF_OK;
+  return wrap([&] {
+    m->home_share = percent;
+    rebuild_regions(m);
+    drop_graphs(m);
+  });
+}
+
+mrf_status mrf_get_tuning(mrf_map* m, int* ray_variant, int* home_share) {
+  if (guard(m) != MRF_OK) return MRF_ERR_INVALID;
+  if (ray_variant) *ray_variant = m->ray_variant;
+  if (home_share) *home_share = m->home_share;
+  return MRF_OK;
+}
+
+mrf_status mrf_autotune_home_share(mrf_map* m, int reps, int flags, const int* shares, int n, double* ms_out,
+                                   int* chosen) {
+  if (guard(m) != MRF_OK) return MRF_ERR_INVALID;
+  if (reps < 1 || n < 1 || !shares) {
+    set_err("invalid autotune arguments");
+    return MRF_ERR_INVALID;
+  }
+  for (int k = 0; k < n; ++k)
+    if (shares[k] < 1 || shares[k] > 100) {
+      set_err("home share must be 1..100 per cent");
+      return MRF_ERR_INVALID;
+    }
+  const bool jacobi = (flags & MRF_JACOBI) != 0;
+  return wrap([&] {
+    if (jacobi)
+      ensure_compact(m);
+    else
+      ensure_built(m);
+    if (jacobi && m->jacobi_version != m->built_version) build_jacobi_csr(m);
+    std::vector<double> ms((size_t)n, 0.0);
+    for (int k = 0; k < n; ++k) {
+      m->home_share = shares[k];
+      rebuild_regions(m);
+      drop_graphs(m);
+      ms[(size_t)k] = time_schedule(m, jacobi, reps);
+    }
+    int best = 0;
+    for (int k = 1; k < n; ++k)
+      if (ms[(size_t)k] < ms[(size_t)best]) best = k;
+    m->home_share = shares[best];
+    rebuild_regions(m);
+    drop_graphs(m);
+    if (ms_out)
+      for (int k = 0; k < n; ++k) ms_out[k] = ms[(size_t)k];
+    if (chosen) *chosen = shares[best];
+  });
 }
 
 mrf_status mrf_autotune(mrf_map* m, int reps, double* ms_out, int cap, int* chosen) {

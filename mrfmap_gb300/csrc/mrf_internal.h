@@ -151,12 +151,11 @@ cudaError_t launch_warm_split(const uint32_t* vseg, const uint32_t* vpairs, cons
 cudaError_t launch_voxel_features(const uint32_t* vseg, const uint32_t* vpairs, const uint32_t* vvox,
                                   uint32_t nvox, const float* cum, const float* stat, const float* hit,
                                   const float* belief, int64_t n_slots_vox, float* feat, cudaStream_t s);
-// dynamic incidences of a view in pair-grouped order: each dynamic
-// incidence's position in that order (dslot, indexed by incidence) and the
-// pairs that own the positions (dpair, with their first position dseg)
+// dynamic incidences of a view in pair-grouped order (dperm) and the pairs
+// that own them (dpair, with their first position dseg)
 cudaError_t launch_dyn_flags(const float2* srec, uint32_t n, uint32_t* flag, cudaStream_t s);
 cudaError_t launch_dyn_scatter(const uint32_t* sidx, const uint32_t* flag, const uint32_t* scan,
-                               uint32_t n, uint32_t inc_base, uint32_t dperm_base, uint32_t* dslot,
+                               uint32_t n, uint32_t inc_base, uint32_t dperm_base, uint32_t* dperm,
                                cudaStream_t s);
 cudaError_t launch_dpair_flags(const uint32_t* ndyn, uint32_t p0, uint32_t np, uint32_t* flag,
                                cudaStream_t s);
@@ -182,8 +181,8 @@ struct BpArrays {
   const uint32_t* inc_pair;
   const float* inc_len;
   const float* inc_mu;
-  const uint32_t* inc_dslot;  // per dynamic incidence: its pair-grouped position
-  float* dmsg;                // p*l at each pair-grouped dynamic position
+  float* inc_pl;           // p*l per incidence, ray order (dynamic ones only)
+  const uint32_t* dperm;   // dynamic incidence at each pair-grouped position
   const uint32_t* dpair;   // pair owning each dynamic run
   const uint32_t* dseg;    // first dynamic position of each run
   const uint4* drun;       // per run: pair id, voxel, cumulative length, static sum

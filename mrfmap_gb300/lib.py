@@ -44,7 +44,7 @@ EXPORTS = ["mrf_create", "mrf_destroy", "mrf_release_cached_memory", "mrf_last_e
            "mrf_stats_get", "mrf_get_stream", "mrf_synchronize", "mrf_render", "mrf_render_view", "mrf_pixel_diagnostics", "mrf_add_view_camera",
            "mrf_view_camera", "mrf_set_memory_limit", "mrf_memory_in_use", "mrf_test_raise_device_error",
            "mrf_infer_until", "mrf_retire_view", "mrf_add_view_box", "mrf_autotune_flags",
-           "mrf_set_precision"]
+           "mrf_set_precision", "mrf_set_home_share", "mrf_autotune_home_share", "mrf_get_tuning"]
 
 RENDER_EXPECTED_DEPTH = 0
 RENDER_ACCURACY = 1
@@ -148,6 +148,9 @@ def load(path: str | None = None):
         "mrf_retire_view": ([vp, C.c_int], C.c_int),
         "mrf_set_precision": ([vp, C.c_int], C.c_int),
         "mrf_autotune_flags": ([vp, C.c_int, C.c_int, C.POINTER(C.c_double), C.c_int, ip], C.c_int),
+        "mrf_set_home_share": ([vp, C.c_int], C.c_int),
+        "mrf_autotune_home_share": ([vp, C.c_int, C.c_int, ip, C.c_int, C.POINTER(C.c_double), ip], C.c_int),
+        "mrf_get_tuning": ([vp, ip, ip], C.c_int),
         "mrf_add_view_box": ([vp, fp, fp, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, ip, ip,
                               ip], C.c_int),
         "mrf_infer_until": ([vp, ip, C.c_int, C.c_int, C.c_void_p, C.c_float, C.c_int, C.c_int, ip, fp],
@@ -355,6 +358,28 @@ class MRFMap:
         _check(self._L.mrf_autotune_flags(self._h, reps, flags, ms.ctypes.data_as(C.POINTER(C.c_double)), nv,
                                           C.byref(ch)))
         return ch.value, ms
+
+    def set_home_share(self, percent: int):
+        """Per cent of an SM region's incidences taken by its home blocks in
+        the SM-region schedule (default 75); results do not change."""
+        _check(self._L.mrf_set_home_share(self._h, percent))
+
+    def autotune_home_share(self, shares=(60, 75, 90), reps: int = 3, flags: int = 0):
+        """Times each home share on this map; keeps the fastest.  Returns
+        (chosen share, ms per iteration of each share)."""
+        sh = np.ascontiguousarray(shares, np.int32)
+        ms = np.zeros(len(sh), np.float64)
+        ch = C.c_int()
+        _check(self._L.mrf_autotune_home_share(self._h, reps, flags, sh.ctypes.data_as(C.POINTER(C.c_int)),
+                                               len(sh), ms.ctypes.data_as(C.POINTER(C.c_double)),
+                                               C.byref(ch)))
+        return ch.value, ms
+
+    def tuning(self):
+        """(ray-kernel variant, home share) in use."""
+        v, h = C.c_int(), C.c_int()
+        _check(self._L.mrf_get_tuning(self._h, C.byref(v), C.byref(h)))
+        return v.value, h.value
 
     def reset_state(self):
         _check(self._L.mrf_reset_state(self._h))

@@ -262,6 +262,39 @@ def test_ray_variants_identical_and_autotune(native_lib, w):
         m.set_ray_variant(99)
 
 
+def test_home_share_moves_rays_not_results(native_lib, w):
+    """The SM-region schedule's home share only moves rays between warps:
+    every share gives the same bits, in Gauss-Seidel and Jacobi; its
+    autotuner picks one of the shares it timed and leaves the state as it
+    was."""
+    for flags in (0, L.JACOBI):
+        out = []
+        for share in (40, 75, 100):
+            m = L.MRFMap(w.params, activation=L.ACT_FULL_RAY)
+            for P, D in zip(w.poses, w.depths):
+                m.add_view(P, D)
+            m.set_ray_variant(4)
+            m.infer(iters=1, flags=flags)
+            m.set_home_share(share)
+            assert m.tuning() == (4, share)
+            m.infer(iters=3, flags=flags | L.INCREMENTAL)
+            out.append(m.beliefs())
+            if share == 75:
+                before = (m.beliefs(), m.logodds())
+                best, ms = m.autotune_home_share((50, 90), reps=2, flags=flags)
+                assert best in (50, 90) and (ms > 0).all() and m.tuning()[1] == best
+                np.testing.assert_array_equal(m.beliefs(), before[0])
+                np.testing.assert_array_equal(m.logodds(), before[1])
+            m.close()
+        for b in out[1:]:
+            np.testing.assert_array_equal(b, out[0])
+    m = L.MRFMap(w.params)
+    for bad in (0, 101):
+        with pytest.raises(L.MrfError):
+            m.set_home_share(bad)
+    m.close()
+
+
 def test_ray_variants_identical_jacobi(native_lib, w):
     """The Jacobi schedule runs one ray launch over all views' queues (the
     SM-region schedule then has regions of every view and one leftover
