@@ -10,8 +10,11 @@
 //                  ray order (pixel-major, then along the ray), each ray
 //                  padded to a multiple of 4
 //   pairs          u32 voxel, fp32 m, fp32 cum_len, fp32 ln q, fp32 dm,
-//                  u32 seg   [N_cv]; per view the pairs on voxels with a
-//                  dynamic incidence first, each part brick-major by first
+//                  u32 seg   [N_cv]; per view the pairs with a dynamic
+//                  incidence in the view first (so the pair update's
+//                  message reads and writes are contiguous), then the other
+//                  pairs on voxels with a dynamic incidence in any view,
+//                  then the quiet ones, each part brick-major by first
 //                  visit along the rays (mrf_build.cu, k_pair_first)
 //   grouped        u32 incidence per pair-grouped position [N_pre] (CSR
 //                  by pair; the dynamic positions again in dperm)
@@ -403,7 +406,8 @@ void view_counters(View& v, const RayMeta* vm) {
 // The pairs of view c: its incidences (at v.inc_base; voxel ids in s_vox and
 // build records in s_rec at the same positions) sorted by voxel (stable),
 // one pair per run, the pairs renumbered brick-major by first visit
-// (mrf_build.cu, k_pair_first; pairs on voxels flagged in s_loud first) and
+// (mrf_build.cu, k_pair_first; the view's dynamic pairs first, then the
+// other pairs on voxels flagged in s_loud, then the quiet ones) and
 // the incidences regrouped in the new pair order; then the pair statistics
 // and the dynamic runs.  Numbered from the totals' current ends, which
 // advance.
@@ -472,17 +476,23 @@ void view_pairs(mrf_map* m, int c, int bits, int64_t& pair_total, int64_t& perm_
       CK(launch_pair_first(sg, np0, 0, m->s_v1.as<uint32_t>(), q0, m->stream));
       CK(launch_fill_u32(m->s_bf.as<uint32_t>(), m->n_bricks, 0xFFFFFFFFu, m->stream));
       CK(launch_brick_first(pv, q0, np0, m->s_bf.as<uint32_t>(), m->stream));
-      // order: by own first visit, then (stable) by (quiet voxel, the
-      // brick's first visit)
+      // order: by own first visit, then (stable) by (class: dynamic in this
+      // view, loud, quiet; the brick's first visit)
       int ibits = 1;
       while (ibits < 31 && ((uint64_t)1 << ibits) < (uint64_t)n) ++ibits;
-      size_t t4 = std::max(sort_temp_bytes(np0, ibits), sort_temp_bytes(np0, ibits + 1));
+      if (ibits > 30) fail(MRF_ERR_CAPACITY, "more than 2^30 incidences in one view");
+      size_t t4 = std::max(sort_temp_bytes(np0, ibits), sort_temp_bytes(np0, ibits + 2));
       m->s_tmp.reserve(std::max(t4, t1), false, m->stream);
       CK(launch_iota(q2, np0, m->stream));
       CK(sort_pairs_u32(m->s_tmp.p, t4, q0, q1, q2, q3, np0, ibits, m->stream));  // q3: by own visit
+      // the view's own dynamic voxels marked 3 while its keys are formed
+      CK(launch_loud_voxels(m->meta.as<RayMeta>() + v.pix_base, view_pixels(v), m->s_vox.as<uint32_t>(),
+                            m->s_loud.as<uint8_t>(), m->stream, 3));
       CK(launch_brick_keys(q3, np0, pv, m->s_bf.as<uint32_t>(), m->s_loud.as<uint8_t>(), ibits, q0,
                            m->stream));
-      CK(sort_pairs_u32(m->s_tmp.p, t4, q0, q1, q3, q2, np0, ibits + 1, m->stream));  // q2: new order
+      CK(launch_loud_voxels(m->meta.as<RayMeta>() + v.pix_base, view_pixels(v), m->s_vox.as<uint32_t>(),
+                            m->s_loud.as<uint8_t>(), m->stream, 1));
+      CK(sort_pairs_u32(m->s_tmp.p, t4, q0, q1, q3, q2, np0, ibits + 2, m->stream));  // q2: new order
       // new runs: lengths in the new order, their starts, the old -> new map
       CK(launch_new_lengths(q2, np0, sg, q0, q3, m->stream));
       CK(cudaMemsetAsync(q0 + np0, 0, 4, m->stream));
