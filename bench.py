@@ -638,6 +638,7 @@ def run_ours(args):
                                "n_rays": st["n_rays"], "n_rays_bp": st["n_rays_bp"],
                                "n_inc_pre_bp_per_iter": st["n_inc_pre_bp"], "n_bricks": st["n_bricks"],
                                "ray_variant": tuned, "ray_variant_ms": [round(x, 4) for x in tune_ms],
+                               "pair_variant": m.tuning()[2],
                                "home_share": m.tuning()[1], "home_share_ms": dict(zip(HOME_SHARES[:len(share_ms)],
                                                                                      [round(float(x), 4) for x in share_ms])),
                                "static_messages": "exact constants (p = F_EPS before a ray's first "

@@ -249,6 +249,10 @@ MRF_API mrf_status mrf_net_adam(float* params, const float* grads, float* m1, fl
  * schedule (longest first or SM regions) and in the register budget (a
  * 12-block-per-SM target caps a thread at 40 registers); their arithmetic
  * is identical, so the choice never changes a result.
+ * The pair reduction has two variants as well (one or two pairs' records
+ * requested ahead per thread, at 8 or 5 resident blocks per SM), with the
+ * same arithmetic; mrf_autotune times both after choosing the ray variant
+ * and keeps the faster (mrf_get_tuning reports it).
  * mrf_autotune times every variant on this map's own incidence lists (reps
  * timed Gauss-Seidel iterations after one warm-up, the map state saved
  * before and restored after each variant), keeps the fastest and returns
@@ -272,11 +276,12 @@ MRF_API mrf_status mrf_autotune_flags(mrf_map* map, int reps, int flags, double*
  * The pair-update tile and the ray chunk are not tuned: both change the
  * order of floating-point sums, and a choice made from timings would make
  * results differ from run to run.  mrf_get_tuning reports the current
- * ray-kernel variant and home share. */
+ * ray-kernel variant, home share and pair-reduction variant. */
 MRF_API mrf_status mrf_set_home_share(mrf_map* map, int percent);
 MRF_API mrf_status mrf_autotune_home_share(mrf_map* map, int reps, int flags, const int* shares, int n,
                                            double* ms_out, int* chosen);
-MRF_API mrf_status mrf_get_tuning(mrf_map* map, int* ray_variant, int* home_share);
+MRF_API mrf_status mrf_get_tuning(mrf_map* map, int* ray_variant, int* home_share, int* pair_variant);
+MRF_API mrf_status mrf_set_pair_variant(mrf_map* map, int variant);  /* 0 or 1 */
 
 /* Storage precision of the ray kernel's streams (no reference counterpart;
  * the reference stores half2 channels, gvdbkernels.cu:975-978):

@@ -628,7 +628,10 @@ __device__ __forceinline__ void apply_run(const uint4 r, float acc_dyn, float* _
   apply_run_loaded(r, m[p], jacobi ? 0.0f : L[v], acc_dyn, m, L, dm, jacobi);
 }
 
-__global__ void __launch_bounds__(kTileThreads, 8)
+// kTwo false: one prefetched pair per thread, 32 registers (8 blocks per
+// SM); true: two, 48 registers (5 blocks per SM).  Same arithmetic.
+template <bool kTwo>
+__global__ void __launch_bounds__(kTileThreads, kTwo ? 5 : 8)
     k_pair_reduce(const uint32_t* __restrict__ perm, const float* __restrict__ pl,
                   const uint32_t* __restrict__ seg, const uint32_t* __restrict__ tile_first,
                   uint32_t k0, uint32_t k1, uint32_t p_end, TileCarry* __restrict__ carry,
@@ -643,13 +646,18 @@ __global__ void __launch_bounds__(kTileThreads, 8)
   const uint32_t pf = tile_first[blockIdx.x];
   // a tile touches at most n pairs: their starts and the next pair's start
   const uint32_t nseg = min(n + 1, p_end - pf) + 1;
-  // the run record of this thread's first pair, and that pair's message and
-  // voxel total, are requested before the message gathers so that neither
-  // dependent load waits after the barrier
-  uint4 r0 = make_uint4(0u, 0u, 0u, 0u);
-  float mo0 = 0.0f, Lo0 = 0.0f;
+  // the run records of this thread's first two pairs (q = t, t + 256; a
+  // tile of 1024 positions holds about 340 pairs), and those pairs' messages
+  // and voxel totals, are requested before the message gathers so that no
+  // dependent load waits after the barrier.  The tile's pairs end at the
+  // next tile's first pair.
+  const uint32_t last = blockIdx.x + 1 < gridDim.x ? tile_first[blockIdx.x + 1] : p_end - 1;
+  uint4 r0 = make_uint4(0u, 0u, 0u, 0u), r1 = make_uint4(0u, 0u, 0u, 0u);
+  float mo0 = 0.0f, Lo0 = 0.0f, mo1 = 0.0f, Lo1 = 0.0f;
   const bool pre = t < n && pf + t < p_end;
+  const bool pre1 = kTwo && t + kTileThreads < n && pf + t + kTileThreads <= min(last, p_end - 1);
   if (pre) r0 = drun[pf + t];
+  if (pre1) r1 = drun[pf + t + kTileThreads];
 #pragma unroll
   for (int j = 0; j < 4; ++j) {
     uint32_t i = j * kTileThreads + t;
@@ -661,6 +669,11 @@ __global__ void __launch_bounds__(kTileThreads, 8)
     mo0 = m[r0.x];
     if (!jacobi) Lo0 = L[r0.y];
   }
+  const bool gate1 = pre1 && __uint_as_float(r1.z) > kCumLenGate;
+  if (gate1) {
+    mo1 = m[r1.x];
+    if (!jacobi) Lo1 = L[r1.y];
+  }
   __syncthreads();
   for (uint32_t q = t; q < n && pf + q < p_end && sseg[q] < end; q += kTileThreads) {
     const uint32_t s0 = sseg[q], s1 = sseg[q + 1];
@@ -671,6 +684,8 @@ __global__ void __launch_bounds__(kTileThreads, 8)
     if (!open_start && !open_end) {
       if (q == t) {
         if (gate0) apply_run_loaded(r0, mo0, Lo0, acc, m, L, dm, jacobi);
+      } else if (q == t + kTileThreads && pre1) {
+        if (gate1) apply_run_loaded(r1, mo1, Lo1, acc, m, L, dm, jacobi);
       } else {
         apply_run(drun[pf + q], acc, m, L, dm, jacobi);
       }
@@ -1098,8 +1113,12 @@ cudaError_t launch_pair_update(const BpArrays& a, uint32_t k0, uint32_t k1, uint
   (void)j0;
   if (k1 <= k0) return cudaSuccess;
   uint32_t ntiles = (k1 - k0 + kTile - 1) / kTile;
-  k_pair_reduce<<<ntiles, kTileThreads, 0, s>>>(a.dperm, a.inc_pl, a.dseg, tile_first, k0, k1, j1,
-                                                carry, a.drun, a.pair_m, a.L, a.pair_dm, jacobi);
+  if (a.pair_variant)
+    k_pair_reduce<true><<<ntiles, kTileThreads, 0, s>>>(a.dperm, a.inc_pl, a.dseg, tile_first, k0, k1, j1,
+                                                        carry, a.drun, a.pair_m, a.L, a.pair_dm, jacobi);
+  else
+    k_pair_reduce<false><<<ntiles, kTileThreads, 0, s>>>(a.dperm, a.inc_pl, a.dseg, tile_first, k0, k1, j1,
+                                                         carry, a.drun, a.pair_m, a.L, a.pair_dm, jacobi);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   k_pair_fixup<<<blocks(ntiles, 256), 256, 0, s>>>(carry, ntiles, a.drun, a.pair_m, a.L, a.pair_dm,

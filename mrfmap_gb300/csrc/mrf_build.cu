@@ -384,28 +384,25 @@ __global__ void k_brick_first(const uint32_t* __restrict__ pair_vox, const uint3
   if (ok && (threadIdx.x & 31) == (unsigned)(__ffs(same) - 1)) atomicMin(bfirst + b, m);
 }
 
-// second sort key of a pair: its class above bit `bits` -- 0 a dynamic incidence in this
-// view (loud[v] bit 1), 1 another pair on a loud voxel, 2 a quiet voxel's --
-// and its brick's first visit below
+// second sort key: pairs on quiet voxels last (bit `bits` set), then the
+// brick's first visit
 __global__ void k_brick_keys(const uint32_t* __restrict__ order, uint32_t np,
                              const uint32_t* __restrict__ pair_vox, const uint32_t* __restrict__ bfirst,
                              const uint8_t* __restrict__ loud, int bits, uint32_t* __restrict__ key) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= np) return;
   const uint32_t v = pair_vox[order[i]];
-  const uint8_t l = loud[v];
-  const uint32_t cls = (l & 2u) ? 0u : (l ? 1u : 2u);
-  key[i] = bfirst[v / kBrickVox] | (cls << bits);
+  key[i] = bfirst[v / kBrickVox] | (loud[v] ? 0u : (1u << bits));
 }
 
-// loud[v] = value for every voxel with a dynamic incidence in the given
-// rays: one thread per ray walks its dynamic range [k_dyn, n_post)
+// loud[v] = 1 for every voxel with a dynamic incidence (any view): one
+// thread per ray walks its dynamic range [k_dyn, n_post)
 __global__ void k_loud_voxels(const RayMeta* __restrict__ meta, int64_t npix, const uint32_t* __restrict__ vox,
-                              uint8_t* __restrict__ loud, uint8_t value) {
+                              uint8_t* __restrict__ loud) {
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= npix) return;
   const RayMeta me = meta[r];
-  for (int i = ray_kdyn(me); i < me.n_post; ++i) loud[vox[me.off + i]] = value;
+  for (int i = ray_kdyn(me); i < me.n_post; ++i) loud[vox[me.off + i]] = 1;
 }
 
 __global__ void k_loud_voxels_from_pairs(const RayMeta* __restrict__ meta, int64_t npix,
@@ -708,9 +705,9 @@ cudaError_t launch_brick_keys(const uint32_t* order, uint32_t np, const uint32_t
 }
 
 cudaError_t launch_loud_voxels(const RayMeta* meta, int64_t npix, const uint32_t* vox, uint8_t* loud,
-                               cudaStream_t s, uint8_t value) {
+                               cudaStream_t s) {
   if (npix <= 0) return cudaSuccess;
-  k_loud_voxels<<<grid_for(npix), kThreads, 0, s>>>(meta, npix, vox, loud, value);
+  k_loud_voxels<<<grid_for(npix), kThreads, 0, s>>>(meta, npix, vox, loud);
   return cudaGetLastError();
 }
 

@@ -10,11 +10,8 @@
 //                  ray order (pixel-major, then along the ray), each ray
 //                  padded to a multiple of 4
 //   pairs          u32 voxel, fp32 m, fp32 cum_len, fp32 ln q, fp32 dm,
-//                  u32 seg   [N_cv]; per view the pairs with a dynamic
-//                  incidence in the view first (so the pair update's
-//                  message reads and writes are contiguous), then the other
-//                  pairs on voxels with a dynamic incidence in any view,
-//                  then the quiet ones, each part brick-major by first
+//                  u32 seg   [N_cv]; per view the pairs on voxels with a
+//                  dynamic incidence first, each part brick-major by first
 //                  visit along the rays (mrf_build.cu, k_pair_first)
 //   grouped        u32 incidence per pair-grouped position [N_pre] (CSR
 //                  by pair; the dynamic positions again in dperm)
@@ -215,6 +212,7 @@ struct mrf_map {
   // build) and of ln q (written by k_pair_prepare)
   int precision = MRF_PRECISION_FP32;
   int home_share = kHomeShare;  // SM-region schedule: per cent of a region's work on its home blocks
+  int pair_variant = 0;  // pair reduction variant (mrf_autotune_flags); same results
   DBuf inc_len16, pair_q16;
   int len16_version = -1;
   // logit(prior) + the messages of retired views, per voxel (kept once a view
@@ -261,6 +259,7 @@ struct mrf_map {
     a.L = d_L.as<float>();
     a.belief = d_belief.as<float>();
     a.half_streams = precision == MRF_PRECISION_HALF_STREAMS ? 1 : 0;
+    a.pair_variant = pair_variant;
     a.inc_len16 = inc_len16.as<__half>();
     a.pair_lnq16 = pair_q16.as<__half>();
     return a;
@@ -406,8 +405,7 @@ void view_counters(View& v, const RayMeta* vm) {
 // The pairs of view c: its incidences (at v.inc_base; voxel ids in s_vox and
 // build records in s_rec at the same positions) sorted by voxel (stable),
 // one pair per run, the pairs renumbered brick-major by first visit
-// (mrf_build.cu, k_pair_first; the view's dynamic pairs first, then the
-// other pairs on voxels flagged in s_loud, then the quiet ones) and
+// (mrf_build.cu, k_pair_first; pairs on voxels flagged in s_loud first) and
 // the incidences regrouped in the new pair order; then the pair statistics
 // and the dynamic runs.  Numbered from the totals' current ends, which
 // advance.
@@ -476,23 +474,17 @@ void view_pairs(mrf_map* m, int c, int bits, int64_t& pair_total, int64_t& perm_
       CK(launch_pair_first(sg, np0, 0, m->s_v1.as<uint32_t>(), q0, m->stream));
       CK(launch_fill_u32(m->s_bf.as<uint32_t>(), m->n_bricks, 0xFFFFFFFFu, m->stream));
       CK(launch_brick_first(pv, q0, np0, m->s_bf.as<uint32_t>(), m->stream));
-      // order: by own first visit, then (stable) by (class: dynamic in this
-      // view, loud, quiet; the brick's first visit)
+      // order: by own first visit, then (stable) by (quiet voxel, the
+      // brick's first visit)
       int ibits = 1;
       while (ibits < 31 && ((uint64_t)1 << ibits) < (uint64_t)n) ++ibits;
-      if (ibits > 30) fail(MRF_ERR_CAPACITY, "more than 2^30 incidences in one view");
-      size_t t4 = std::max(sort_temp_bytes(np0, ibits), sort_temp_bytes(np0, ibits + 2));
+      size_t t4 = std::max(sort_temp_bytes(np0, ibits), sort_temp_bytes(np0, ibits + 1));
       m->s_tmp.reserve(std::max(t4, t1), false, m->stream);
       CK(launch_iota(q2, np0, m->stream));
       CK(sort_pairs_u32(m->s_tmp.p, t4, q0, q1, q2, q3, np0, ibits, m->stream));  // q3: by own visit
-      // the view's own dynamic voxels marked 3 while its keys are formed
-      CK(launch_loud_voxels(m->meta.as<RayMeta>() + v.pix_base, view_pixels(v), m->s_vox.as<uint32_t>(),
-                            m->s_loud.as<uint8_t>(), m->stream, 3));
       CK(launch_brick_keys(q3, np0, pv, m->s_bf.as<uint32_t>(), m->s_loud.as<uint8_t>(), ibits, q0,
                            m->stream));
-      CK(launch_loud_voxels(m->meta.as<RayMeta>() + v.pix_base, view_pixels(v), m->s_vox.as<uint32_t>(),
-                            m->s_loud.as<uint8_t>(), m->stream, 1));
-      CK(sort_pairs_u32(m->s_tmp.p, t4, q0, q1, q3, q2, np0, ibits + 2, m->stream));  // q2: new order
+      CK(sort_pairs_u32(m->s_tmp.p, t4, q0, q1, q3, q2, np0, ibits + 1, m->stream));  // q2: new order
       // new runs: lengths in the new order, their starts, the old -> new map
       CK(launch_new_lengths(q2, np0, sg, q0, q3, m->stream));
       CK(cudaMemsetAsync(q0 + np0, 0, 4, m->stream));
@@ -1292,7 +1284,7 @@ void ensure_built(mrf_map* m) {
   if (m->built_version != m->version) {
     const bool can_append = !m->needs_full && m->built_version >= 0 &&
                             m->prm.activation == MRF_ACT_FULL_RAY && m->built_views <= (int)m->views.size() &&
-                            m->dead_inc * 2 <= m->n_inc;
+                            m->dead_inc * 3 <= m->n_inc * 2;  // retired lists at most twice the live ones
     bool done = false;
     if (can_append) {
       try {
@@ -2264,10 +2256,22 @@ mrf_status mrf_set_home_share(mrf_map* m, int percent) {
   });
 }
 
-mrf_status mrf_get_tuning(mrf_map* m, int* ray_variant, int* home_share) {
+mrf_status mrf_set_pair_variant(mrf_map* m, int variant) {
+  if (guard(m) != MRF_OK) return MRF_ERR_INVALID;
+  if (variant < 0 || variant > 1) {
+    set_err("invalid pair-reduction variant");
+    return MRF_ERR_INVALID;
+  }
+  m->pair_variant = variant;
+  drop_graphs(m);
+  return MRF_OK;
+}
+
+mrf_status mrf_get_tuning(mrf_map* m, int* ray_variant, int* home_share, int* pair_variant) {
   if (guard(m) != MRF_OK) return MRF_ERR_INVALID;
   if (ray_variant) *ray_variant = m->ray_variant;
   if (home_share) *home_share = m->home_share;
+  if (pair_variant) *pair_variant = m->pair_variant;
   return MRF_OK;
 }
 
@@ -2367,6 +2371,17 @@ mrf_status mrf_autotune_flags(mrf_map* m, int reps, int flags, double* ms_out, i
     for (int k = 0; k < NV && k < cap; ++k) ms_out[k] = ms[k];
     m->ray_variant = best;
     drop_graphs(m);
+    // then the pair reduction's variant with that ray kernel
+    if (m->n_inc > 0) {
+      double pms[2];
+      for (int k = 0; k < 2; ++k) {
+        m->pair_variant = k;
+        drop_graphs(m);
+        pms[k] = time_schedule(m, jacobi, reps);
+      }
+      m->pair_variant = pms[1] < pms[0] ? 1 : 0;
+      drop_graphs(m);
+    }
     if (chosen) *chosen = best;
   });
 }

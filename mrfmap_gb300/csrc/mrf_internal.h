@@ -107,10 +107,8 @@ cudaError_t launch_brick_keys(const uint32_t* order, uint32_t np, const uint32_t
                               const uint32_t* bfirst, const uint8_t* loud, int bits, uint32_t* key,
                               cudaStream_t s);
 // voxels with a dynamic incidence in any view, and the pairs on them
-// (loud[v] = value: 1 loud; 3 while one view's pairs are numbered, its own
-// dynamic voxels)
 cudaError_t launch_loud_voxels(const RayMeta* meta, int64_t npix, const uint32_t* vox, uint8_t* loud,
-                               cudaStream_t s, uint8_t value = 1);
+                               cudaStream_t s);
 // the same with each incidence's voxel from its pair (vox = pair_vox[inc_pair])
 cudaError_t launch_loud_voxels_from_pairs(const RayMeta* meta, int64_t npix, const uint32_t* inc_pair,
                                           const uint32_t* pair_vox, uint8_t* loud, cudaStream_t s);
@@ -201,6 +199,7 @@ struct BpArrays {
   // segment lengths and gathers ln q as fp16; k_pair_prepare writes ln q as
   // fp16 then
   int half_streams;
+  int pair_variant;  // pair reduction: 0 one prefetched pair per thread, 1 two
   const __half* inc_len16;
   __half* pair_lnq16;
 };

@@ -44,7 +44,8 @@ EXPORTS = ["mrf_create", "mrf_destroy", "mrf_release_cached_memory", "mrf_last_e
            "mrf_stats_get", "mrf_get_stream", "mrf_synchronize", "mrf_render", "mrf_render_view", "mrf_pixel_diagnostics", "mrf_add_view_camera",
            "mrf_view_camera", "mrf_set_memory_limit", "mrf_memory_in_use", "mrf_test_raise_device_error",
            "mrf_infer_until", "mrf_retire_view", "mrf_add_view_box", "mrf_autotune_flags",
-           "mrf_set_precision", "mrf_set_home_share", "mrf_autotune_home_share", "mrf_get_tuning"]
+           "mrf_set_precision", "mrf_set_home_share", "mrf_autotune_home_share", "mrf_get_tuning",
+           "mrf_set_pair_variant"]
 
 RENDER_EXPECTED_DEPTH = 0
 RENDER_ACCURACY = 1
@@ -150,7 +151,8 @@ def load(path: str | None = None):
         "mrf_autotune_flags": ([vp, C.c_int, C.c_int, C.POINTER(C.c_double), C.c_int, ip], C.c_int),
         "mrf_set_home_share": ([vp, C.c_int], C.c_int),
         "mrf_autotune_home_share": ([vp, C.c_int, C.c_int, ip, C.c_int, C.POINTER(C.c_double), ip], C.c_int),
-        "mrf_get_tuning": ([vp, ip, ip], C.c_int),
+        "mrf_get_tuning": ([vp, ip, ip, ip], C.c_int),
+        "mrf_set_pair_variant": ([vp, C.c_int], C.c_int),
         "mrf_add_view_box": ([vp, fp, fp, C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, ip, ip,
                               ip], C.c_int),
         "mrf_infer_until": ([vp, ip, C.c_int, C.c_int, C.c_void_p, C.c_float, C.c_int, C.c_int, ip, fp],
@@ -375,11 +377,15 @@ class MRFMap:
                                                C.byref(ch)))
         return ch.value, ms
 
+    def set_pair_variant(self, variant: int):
+        """Pair-reduction variant (0 or 1; the same results)."""
+        _check(self._L.mrf_set_pair_variant(self._h, variant))
+
     def tuning(self):
-        """(ray-kernel variant, home share) in use."""
-        v, h = C.c_int(), C.c_int()
-        _check(self._L.mrf_get_tuning(self._h, C.byref(v), C.byref(h)))
-        return v.value, h.value
+        """(ray-kernel variant, home share, pair-reduction variant) in use."""
+        v, h, p = C.c_int(), C.c_int(), C.c_int()
+        _check(self._L.mrf_get_tuning(self._h, C.byref(v), C.byref(h), C.byref(p)))
+        return v.value, h.value, p.value
 
     def reset_state(self):
         _check(self._L.mrf_reset_state(self._h))

@@ -255,11 +255,28 @@ def test_ray_variants_identical_and_autotune(native_lib, w):
             np.testing.assert_array_equal(m.beliefs(), before[0])
             np.testing.assert_array_equal(m.logodds(), before[1])
         m.close()
+    # the pair reduction's two variants, Gauss-Seidel and Jacobi
+    for flags in (0, L.JACOBI):
+        res = []
+        for pv in (0, 1):
+            m = L.MRFMap(w.params, activation=L.ACT_FULL_RAY)
+            for P, D in zip(w.poses, w.depths):
+                m.add_view(P, D)
+            m.set_pair_variant(pv)
+            m.infer(iters=3, flags=flags)
+            assert m.tuning()[2] == pv
+            res.append(m.beliefs())
+            m.close()
+        np.testing.assert_array_equal(res[1], res[0])
+        if flags == 0:
+            np.testing.assert_array_equal(res[0], out[0])
     for b in out[1:]:
         np.testing.assert_array_equal(b, out[0])
     m = L.MRFMap(w.params)
     with pytest.raises(L.MrfError):
         m.set_ray_variant(99)
+    with pytest.raises(L.MrfError):
+        m.set_pair_variant(2)
 
 
 def test_home_share_moves_rays_not_results(native_lib, w):
@@ -276,7 +293,7 @@ def test_home_share_moves_rays_not_results(native_lib, w):
             m.set_ray_variant(4)
             m.infer(iters=1, flags=flags)
             m.set_home_share(share)
-            assert m.tuning() == (4, share)
+            assert m.tuning()[:2] == (4, share)
             m.infer(iters=3, flags=flags | L.INCREMENTAL)
             out.append(m.beliefs())
             if share == 75:
