@@ -260,6 +260,18 @@ def evaluate(net, workloads, accept_tol: float = 1e-3, ref_tol: float = 1e-4, re
             rec[label + "_reached"] = bool(dist <= accept_tol)
             rec[label + "_max_err"] = float(np.abs(B - Bref).max())
             rec[label + "_agree"] = float(((B > 0.5) == (Bref > 0.5))[touched].mean()) if touched.any() else 1.0
+        # the network's three convolutions alone (mean of 5 calls on this
+        # scene's features), and the bricks they cover
+        feat = map_features(m)
+        net.predict(feat)
+        torch.cuda.synchronize()
+        ev[0].record()
+        for _ in range(5):
+            net.predict(feat)
+        ev[1].record()
+        torch.cuda.synchronize()
+        rec["net_forward_ms"] = ev[0].elapsed_time(ev[1]) / 5
+        rec["n_bricks"] = int(m.num_bricks)
         rows.append(rec)
         m.close()
     return rows
@@ -278,6 +290,12 @@ def summarize(rows, accept_tol: float = 1e-3, agree_min: float = 0.999):
     for k in ("plain", "learned", "prior"):
         out[k + "_ms"] = mean(k + "_ms")
         out[k + "_start_ms"] = mean(k + "_start_ms")
+    if rows and "net_forward_ms" in rows[0]:
+        # the convolutions' rate: 9072 multiply-adds per voxel (27 taps x
+        # (4x16 + 16x16 + 16x1)), 512 voxels per brick
+        out["net_forward_ms"] = float(np.mean([r["net_forward_ms"] for r in rows]))
+        out["net_forward_tflops"] = float(np.mean([2 * 9072 * 512 * r["n_bricks"] / (r["net_forward_ms"] * 1e9)
+                                                   for r in rows]))
         out[k + "_iters"] = mean(k + "_iters")
     if ok:
         out["speedup_learned_vs_plain"] = out["plain_ms"] / out["learned_ms"]
