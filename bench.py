@@ -334,21 +334,36 @@ def run_reference(args):
 
 
 # bumped whenever k_ray_bp's memory traffic changes (profiles/ray_bp_traffic.json)
-RAY_KERNEL_VERSION = 6
+RAY_KERNEL_VERSION = 7
 
 
 HOME_SHARES = (60, 75, 90)  # per cent of an SM region's work on its home blocks, tried by the autotuner
 
 
 def ray_kernel_bytes(st, iters, half=False):
-    """Algorithmic bytes of the ray-message kernel for one launch-sum, over
-    the rays it runs over (those with a dynamic incidence): per Pre
-    incidence the pair id (4 B), the length and the ln q gather (4 B each
-    with the default fp32 streams, 2 B each with 16-bit streams); per dynamic
-    incidence (from the ray's first non-zero potential on) +8 B (potential
-    4, message write 4); per ray 16 B of metadata."""
-    per_pre = 8 if half else 12
-    return (per_pre * st["n_inc_pre_bp"] + 8 * st["n_inc_dyn"] + 16 * st["n_rays_bp"]) * iters
+    """Algorithmic bytes of the ray-message work of one mrf_infer call of
+    `iters` iterations, over the rays it runs over (those with a dynamic
+    incidence).  Gather width g and length width l: 4 B each with the
+    default fp32 streams, 2 B each with 16-bit streams.
+      the first two iterations (full path): per Pre incidence the pair id
+        (4 B), length and ln q gather (l + g); per dynamic incidence +8 B
+        (potential 4, message write 4); per ray 16 B of metadata;
+      once per call, the quiet sums of the static prefixes [0, k4): per
+        incidence pair id, fp32 length and gather (8 + g); per ray 16 B;
+      every later iteration (fast path): per incidence from k4 on 4 + l + g;
+        per loud prefix incidence pair id, fp32 length, position and gather
+        (10 + g); per dynamic incidence +8 B; per ray 36 B (metadata 16,
+        ray index 4, quiet sums 8, list bounds 8)."""
+    g = 2 if half else 4
+    ln = 2 if half else 4
+    pre, k4, loud = st["n_inc_pre_bp"], st["n_inc_from_k4"], st["n_loud_prefix"]
+    dyn, rays = st["n_inc_dyn"], st["n_rays_bp"]
+    full = (4 + ln + g) * pre + 8 * dyn + 16 * rays
+    if iters < 3:
+        return full * iters
+    quiet = (8 + g) * (pre - k4) + 16 * rays
+    fast = (4 + ln + g) * k4 + (10 + g) * loud + 8 * dyn + 36 * rays
+    return 2 * full + quiet + (iters - 2) * fast
 
 
 LONG_RAY = 512  # Pre incidences above which the ray kernel sums in FP64
@@ -513,9 +528,9 @@ def run_ours(args):
         try:
             t = json.load(open(tfile))
             if t.get("kernel_version") == RAY_KERNEL_VERSION and t.get("activation") == args.policy:
-                # DRAM bytes per Pre incidence from a capture of the same
-                # kernel on a smaller case, scaled by this launch's incidences
-                traffic = t["dram_bytes_per_pre_incidence"] * prof["n_inc_pre_bp"] * iters / k_n
+                # DRAM bytes over algorithmic bytes from a capture of the same
+                # kernel on a smaller case, applied to this launch's bytes
+                traffic = t["dram_over_algorithmic"] * per_launch_bytes
         except Exception:
             pass
     kernel_share = {n: round(v / max(sum(prof["kernel_ms"]), 1e-9), 4)
@@ -637,6 +652,7 @@ def run_ours(args):
                                "n_vox_touched": st["n_vox_touched"],
                                "n_rays": st["n_rays"], "n_rays_bp": st["n_rays_bp"],
                                "n_inc_pre_bp_per_iter": st["n_inc_pre_bp"], "n_bricks": st["n_bricks"],
+                               "n_inc_from_k4": st["n_inc_from_k4"], "n_loud_prefix": st["n_loud_prefix"],
                                "ray_variant": tuned, "ray_variant_ms": [round(x, 4) for x in tune_ms],
                                "pair_variant": m.tuning()[2],
                                "home_share": m.tuning()[1], "home_share_ms": dict(zip(HOME_SHARES[:len(share_ms)],
@@ -662,7 +678,11 @@ def run_ours(args):
                              "step_achieved": step_gbs,
                              "step_frac_survey_bytes": step_gbs / peak,
                              "widths": "per incidence 12 B in the ray kernel (slot 4, length 2, L 4, "
-                                       "message 2); per iteration 16 N_inc + 12 N_cv + 8 N_vox"}},
+                                       "message 2); per iteration 16 N_inc + 12 N_cv + 8 N_vox",
+                             "note": "bytes of the schedule that reads every incidence every iteration; "
+                                     "from the third iteration of a call on the ray kernel reads the static "
+                                     "prefixes' loud incidences only (the quiet ones' sums are formed once "
+                                     "per call), so these are effective rates, not DRAM bandwidths"}},
             "kernel_share": kernel_share,
             "clocks": clk,
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d,

@@ -96,6 +96,13 @@ typedef struct mrf_stats {
   int64_t builds_full;     /* incidence-list builds of every view so far */
   int64_t builds_appended; /* builds that appended only the views added since
                               the previous build (full-ray maps) */
+  int64_t n_inc_from_k4;   /* Pre incidences of those rays from k4 (their first
+                              dynamic incidence rounded down to 4) on: what the
+                              ray kernel reads in full from the third
+                              iteration of a call on */
+  int64_t n_loud_prefix;   /* incidences before k4 on voxels with a dynamic
+                              incidence in some view: the rest of the static
+                              prefixes is summed once per call */
 } mrf_stats;
 
 /* Map construction: GVDBInference(...) + GVDBMRFMap::gpuAllocate

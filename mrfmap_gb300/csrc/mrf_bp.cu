@@ -370,7 +370,8 @@ __device__ __forceinline__ void pre_total(const Slice<KE>& s, int i0, int r0, fl
 }
 
 template <typename Acc, int kPol, int kPf, typename TL, typename TQ>
-__device__ __forceinline__ void ray_bp_warp(const RayMeta& me, const uint32_t* __restrict__ inc_pair,
+__device__ __forceinline__ void ray_bp_warp(const RayMeta& me, uint32_t rid, const QuietPrefix& qp,
+                                            const uint32_t* __restrict__ inc_pair,
                                             const TL* __restrict__ inc_len,
                                             const float* __restrict__ inc_mu,
                                             const TQ* __restrict__ lnq, float* __restrict__ inc_pl,
@@ -382,6 +383,32 @@ __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, const uint32_t* _
   const int k4 = kdyn & ~3;
   const uint32_t off = me.off;
   float carryA = 0.0f, Ar0 = 0.0f, Arinf = 0.0f, Ak = 0.0f;
+  // ---- the static prefix [0, k4) from its quiet sums --------------------
+  // Its quiet incidences (pairs on voxels without a dynamic incidence in
+  // any view) keep their ln q from the third iteration of a call on, so
+  // their sums up to r0 and up to k4 were formed once (k_quiet_prefix);
+  // only the prefix's loud incidences are gathered here.  A ray in the
+  // queues has a non-zero potential, so its rinf equals r0.
+  int start = 0;
+  if (qp.q) {
+    const float2 qv = qp.q[rid];
+    const uint32_t e0 = qp.loff[rid], e1 = qp.loff[rid + 1];
+    float la = 0.0f, lk = 0.0f;
+    for (uint32_t e = e0 + lane; e < e1; e += 32) {
+      const float c = qp.llen[e] * to_f(__ldg(lnq + qp.lpid[e]));
+      lk += c;
+      if ((int)qp.lpos[e] < r0) la += c;
+    }
+    lk = warp_sum(lk);
+    la = warp_sum(la);
+    carryA = qv.y + lk;
+    Ak = carryA;
+    if (!fix_reset && r0 <= k4) {
+      Ar0 = qv.x + la;
+      Arinf = Ar0;
+    }
+    start = k4;
+  }
   // ---- pass 1: prefixes, Pre total ---------------------------------------
   // Chunks of 128 (a chunk costs the same instructions however many of its
   // lanes hold incidences: measured against 256-incidence chunks and against
@@ -395,9 +422,9 @@ __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, const uint32_t* _
   {
     uint32_t pid_next[kE];
     float len_next[kE], len[kE];
-    if (kPf) load_pids<kE, kPol>(pid_next, off, kE * lane, n_pre, inc_pair);
-    if (kPf == 2) ld_len<kE, kPol>(len_next, inc_len + off, kE * lane, kE * lane < n_pre);
-    for (int base = 0; base < n_pre; base += kChunk) {
+    if (kPf) load_pids<kE, kPol>(pid_next, off, start + kE * lane, n_pre, inc_pair);
+    if (kPf == 2) ld_len<kE, kPol>(len_next, inc_len + off, start + kE * lane, start + kE * lane < n_pre);
+    for (int base = start; base < n_pre; base += kChunk) {
       const int i0 = base + kE * lane;
       uint32_t pid[kE];
       if (kPf) {
@@ -489,13 +516,18 @@ __global__ void __launch_bounds__(kRayWarps * 32, kMinBlocks) k_ray_bp(const Ray
                                                            const float* __restrict__ inc_mu,
                                                            const TQ* __restrict__ lnq,
                                                            float* __restrict__ inc_pl,
-                                                           int fix_reset) {
+                                                           const uint32_t* __restrict__ ids,
+                                                           QuietPrefix qp, int fix_reset) {
   const int lane = threadIdx.x & 31;
-  auto ray = [&](const RayMeta& me) {
+  auto ray_at = [&](uint32_t i) {
+    const RayMeta me = queue[i];
+    const uint32_t rid = qp.q ? ids[i] : 0u;
     if (me.n_pre <= kLongRay)
-      ray_bp_warp<float, kPol, kPf, TL, TQ>(me, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
+      ray_bp_warp<float, kPol, kPf, TL, TQ>(me, rid, qp, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset,
+                                            lane);
     else
-      ray_bp_warp<double, kPol, kPf, TL, TQ>(me, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset, lane);
+      ray_bp_warp<double, kPol, kPf, TL, TQ>(me, rid, qp, inc_pair, inc_len, inc_mu, lnq, inc_pl, fix_reset,
+                                             lane);
   };
   if constexpr (kReg) {
     // counter[r]: tickets of region r, whose home rays are positions
@@ -512,7 +544,7 @@ __global__ void __launch_bounds__(kRayWarps * 32, kMinBlocks) k_ray_bp(const Ray
         if (lane == 0) idx = atomicAdd(counter + r, 1u);
         idx = __shfl_sync(kFull, idx, 0);
         if (idx >= nr) break;
-        ray(queue[a + idx]);
+        ray_at(a + idx);
       }
     }
     // the views' leftovers, one ticket counter over all of them: ticket t
@@ -535,7 +567,7 @@ __global__ void __launch_bounds__(kRayWarps * 32, kMinBlocks) k_ray_bp(const Ray
       }
       pos = __shfl_sync(kFull, pos, 0);
       if (pos == 0xFFFFFFFFu) break;
-      ray(queue[pos]);
+      ray_at(pos);
     }
   } else {
     for (;;) {
@@ -543,7 +575,7 @@ __global__ void __launch_bounds__(kRayWarps * 32, kMinBlocks) k_ray_bp(const Ray
       if (lane == 0) idx = atomicAdd(counter, 1u);
       idx = __shfl_sync(kFull, idx, 0);
       if (idx >= n_rays) break;
-      ray(queue[idx]);
+      ray_at(idx);
     }
   }
 }
@@ -551,9 +583,83 @@ __global__ void __launch_bounds__(kRayWarps * 32, kMinBlocks) k_ray_bp(const Ray
 // queue records: queue[i] = meta[base + order[i]] (order: view-local ray
 // indices, longest first)
 __global__ void k_ray_queue(const RayMeta* __restrict__ meta, const uint32_t* __restrict__ order,
-                            uint32_t n, RayMeta* __restrict__ queue) {
+                            uint32_t n, RayMeta* __restrict__ queue, uint32_t* __restrict__ ids,
+                            uint32_t id_base) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) queue[i] = meta[order[i]];
+  if (i < n) {
+    queue[i] = meta[order[i]];
+    ids[i] = id_base + order[i];
+  }
+}
+
+// The static prefix of each queued ray of one view (rays r0..r0+n of the
+// pixel arrays; a warp per ray): the loud incidences in [0, k4) -- those
+// whose pair is among the view's first n_loud, the pairs on voxels with a
+// dynamic incidence in any view -- counted (emit false) or listed at
+// loff[r] (emit true: pair id, length, position), in ray order.
+template <bool kEmit>
+__global__ void k_loud_prefix(const RayMeta* __restrict__ meta, uint32_t r_first, uint32_t n,
+                              const uint32_t* __restrict__ inc_pair, const float* __restrict__ inc_len,
+                              uint32_t pair_base, uint32_t n_loud, uint32_t* __restrict__ loff,
+                              uint32_t* __restrict__ lpid, float* __restrict__ llen,
+                              uint16_t* __restrict__ lpos) {
+  const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (w >= n) return;
+  const uint32_t r = r_first + w;
+  const RayMeta me = meta[r];
+  uint32_t cnt = 0;
+  uint32_t at = kEmit ? loff[r] : 0u;
+  if (ray_in_bp(me)) {
+    const int k4 = ray_kdyn(me) & ~3;
+    for (int b = 0; b < k4; b += 32) {
+      const int j = b + lane;
+      const uint32_t p = j < k4 ? inc_pair[me.off + j] : 0u;
+      const bool loud = j < k4 && p - pair_base < n_loud;
+      const unsigned m = __ballot_sync(kFull, loud);
+      if (kEmit && loud) {
+        const uint32_t e = at + (uint32_t)__popc(m & ((1u << lane) - 1u));
+        lpid[e] = p;
+        llen[e] = inc_len[me.off + j];
+        lpos[e] = (uint16_t)j;
+      }
+      at += (uint32_t)__popc(m);
+      cnt += (uint32_t)__popc(m);
+    }
+  }
+  if (!kEmit && lane == 0) loff[r] = cnt;
+}
+
+// The quiet sums of the static prefix of each queued ray of one view (a
+// warp per ray): sum of l ln q over the quiet incidences j < min(r0, k4)
+// and j < k4, written to q[r] -- valid while the quiet pairs' ln q stay
+// fixed, from the third iteration of a call on.  Lane-strided partial
+// sums and a butterfly warp sum: a fixed order.
+template <typename TQ>
+__global__ void k_quiet_prefix(const RayMeta* __restrict__ meta, uint32_t r_first, uint32_t n,
+                               const uint32_t* __restrict__ inc_pair, const float* __restrict__ inc_len,
+                               const TQ* __restrict__ lnq, uint32_t pair_base, uint32_t n_loud,
+                               float2* __restrict__ q) {
+  const uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (w >= n) return;
+  const uint32_t r = r_first + w;
+  const RayMeta me = meta[r];
+  if (!ray_in_bp(me)) return;
+  const int k4 = ray_kdyn(me) & ~3;
+  const int ra = min((int)me.r0, k4);
+  float qa = 0.0f, qk = 0.0f;
+  for (int j = lane; j < k4; j += 32) {
+    const uint32_t p = inc_pair[me.off + j];
+    if (p - pair_base >= n_loud) {
+      const float c = inc_len[me.off + j] * to_f(__ldg(lnq + p));
+      qk += c;
+      if (j < ra) qa += c;
+    }
+  }
+  qa = warp_sum(qa);
+  qk = warp_sum(qk);
+  if (lane == 0) q[r] = make_float2(qa, qk);
 }
 
 // ray queue of one build: active rays sorted by decreasing length
@@ -1067,8 +1173,16 @@ int ray_bp_resident_blocks(int variant, int half_streams) {
 }
 
 cudaError_t launch_ray_bp(const BpArrays& a, const RayWork& w, int fix_reset, int num_sms, int variant,
-                          cudaStream_t s) {
+                          bool quiet, cudaStream_t s) {
   if (!w.n_rays) return cudaSuccess;
+  QuietPrefix qp{};
+  if (quiet) {
+    qp.q = a.quiet_q;
+    qp.loff = a.loud_off;
+    qp.lpid = a.loud_pid;
+    qp.llen = a.loud_len;
+    qp.lpos = a.loud_pos;
+  }
   if (variant < 0 || variant >= kRayVariants) return cudaErrorInvalidValue;
   int64_t b = std::min<int64_t>((int64_t)num_sms * ray_bp_resident_blocks(variant, a.half_streams),
                                 (w.n_rays + kRayWarps - 1) / kRayWarps);
@@ -1080,12 +1194,12 @@ cudaError_t launch_ray_bp(const BpArrays& a, const RayWork& w, int fix_reset, in
       k_ray_bp<mb, pol, pf, (sc > 0), __half, __half><<<grid, kRayWarps * 32, 0, s>>>(            \
           sc == 0 ? w.queue : w.region, w.n_rays, w.rstart, w.nreg, w.rper, w.lprefix, w.lbase,    \
           w.nlv, w.lcounter, sc == 0 ? w.counter : w.rcounter, a.inc_pair, a.inc_len16, a.inc_mu,  \
-          a.pair_lnq16, a.inc_pl, fix_reset);                                                     \
+          a.pair_lnq16, a.inc_pl, sc == 0 ? w.queue_ids : w.region_ids, qp, fix_reset);            \
     else                                                                                          \
       k_ray_bp<mb, pol, pf, (sc > 0), float, float><<<grid, kRayWarps * 32, 0, s>>>(              \
           sc == 0 ? w.queue : w.region, w.n_rays, w.rstart, w.nreg, w.rper, w.lprefix, w.lbase,    \
           w.nlv, w.lcounter, sc == 0 ? w.counter : w.rcounter, a.inc_pair, a.inc_len, a.inc_mu,    \
-          a.pair_lnq, a.inc_pl, fix_reset);                                                       \
+          a.pair_lnq, a.inc_pl, sc == 0 ? w.queue_ids : w.region_ids, qp, fix_reset);              \
     break;
     MRF_RAY_VARIANTS(X)
 #undef X
@@ -1101,9 +1215,36 @@ cudaError_t launch_ray_keys(const RayMeta* meta, uint32_t n, uint32_t* keys, uin
 }
 
 cudaError_t launch_ray_queue(const RayMeta* meta, const uint32_t* order, uint32_t n, RayMeta* queue,
-                             cudaStream_t s) {
+                             uint32_t* ids, uint32_t id_base, cudaStream_t s) {
   if (!n) return cudaSuccess;
-  k_ray_queue<<<blocks(n, 256), 256, 0, s>>>(meta, order, n, queue);
+  k_ray_queue<<<blocks(n, 256), 256, 0, s>>>(meta, order, n, queue, ids, id_base);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_loud_prefix(const RayMeta* meta, uint32_t r_first, uint32_t n, const uint32_t* inc_pair,
+                               const float* inc_len, uint32_t pair_base, uint32_t n_loud, uint32_t* loff,
+                               uint32_t* lpid, float* llen, uint16_t* lpos, bool emit, cudaStream_t s) {
+  if (!n) return cudaSuccess;
+  const unsigned g = blocks((uint64_t)n * 32, 256);
+  if (emit)
+    k_loud_prefix<true><<<g, 256, 0, s>>>(meta, r_first, n, inc_pair, inc_len, pair_base, n_loud, loff, lpid,
+                                          llen, lpos);
+  else
+    k_loud_prefix<false><<<g, 256, 0, s>>>(meta, r_first, n, inc_pair, inc_len, pair_base, n_loud, loff,
+                                           lpid, llen, lpos);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_quiet_prefix(const BpArrays& a, uint32_t r_first, uint32_t n, uint32_t pair_base,
+                                uint32_t n_loud, float2* q, cudaStream_t s) {
+  if (!n) return cudaSuccess;
+  const unsigned g = blocks((uint64_t)n * 32, 256);
+  if (a.half_streams)
+    k_quiet_prefix<__half><<<g, 256, 0, s>>>(a.meta, r_first, n, a.inc_pair, a.inc_len, a.pair_lnq16, pair_base,
+                                             n_loud, q);
+  else
+    k_quiet_prefix<float><<<g, 256, 0, s>>>(a.meta, r_first, n, a.inc_pair, a.inc_len, a.pair_lnq, pair_base,
+                                            n_loud, q);
   return cudaGetLastError();
 }
 

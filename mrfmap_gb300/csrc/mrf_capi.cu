@@ -158,7 +158,7 @@ struct View {
   bool retired = false;                   // out of the window: no lists, no pairs, no depth
   // counters of the view's rays (incidences, rays, Post incidences, dynamic
   // incidences, rays the ray kernel runs over and their Pre incidences)
-  int64_t c_npre = 0, c_nrays = 0, c_npost = 0, c_ndyn = 0, c_nrays_bp = 0, c_npre_bp = 0;
+  int64_t c_npre = 0, c_nrays = 0, c_npost = 0, c_ndyn = 0, c_nrays_bp = 0, c_npre_bp = 0, c_nfast_bp = 0;
 };
 
 // pixels a view contributes to the per-pixel arrays (none once retired)
@@ -191,6 +191,7 @@ struct mrf_map {
   // of the region blocks, the queues and the tiles, the bricks it saw
   int built_views = 0;
   int64_t npix_total = 0, queue_end = 0, tile_end = 0, carry_tiles = 0, vox_active_n = 0, n_perm_total = 0;
+  int64_t n_loud_prefix = 0;  // entries of the static prefixes' loud lists
   uint32_t region_end = 0;
   int64_t bricks_at_build = -1;
   // holes: retired views' lists still in the arenas; appended: lists added
@@ -203,7 +204,8 @@ struct mrf_map {
   // arenas
   DBuf meta, inc_pair, inc_len, inc_mu, inc_pl, pair_vox, pair_m, pair_cum, pair_stat, pair_ndyn, pair_hit,
       pair_q, pair_dm, pair_seg, dperm, s_q0, s_q1, s_q2, s_q3, s_bf, s_loud, s_pv, s_sg, dpair, dseg, drun, carry, ray_order, ray_queue, region_q, rstart, rcounters, counters,
-      tile_first, lbase, lsingle, lprefix;
+      tile_first, lbase, lsingle, lprefix, queue_ids, region_ids, loud_off, loud_pid, loud_len, loud_pos,
+      quiet_q;
   uint32_t jac_tile_base = 0;
   int64_t n_inc = 0, n_pairs = 0, n_dperm = 0, n_dpairs = 0;
   // voxels with a pair past the length gate (their beliefs follow L)
@@ -260,6 +262,11 @@ struct mrf_map {
     a.belief = d_belief.as<float>();
     a.half_streams = precision == MRF_PRECISION_HALF_STREAMS ? 1 : 0;
     a.pair_variant = pair_variant;
+    a.quiet_q = quiet_q.as<float2>();
+    a.loud_off = loud_off.as<uint32_t>();
+    a.loud_pid = loud_pid.as<uint32_t>();
+    a.loud_len = loud_len.as<float>();
+    a.loud_pos = loud_pos.as<uint16_t>();
     a.inc_len16 = inc_len16.as<__half>();
     a.pair_lnq16 = pair_q16.as<__half>();
     return a;
@@ -387,7 +394,7 @@ void rebuild(mrf_map* m) {
 
 // counters of one view's rays (from its ray records on the host)
 void view_counters(View& v, const RayMeta* vm) {
-  v.c_npre = v.c_nrays = v.c_npost = v.c_ndyn = v.c_nrays_bp = v.c_npre_bp = 0;
+  v.c_npre = v.c_nrays = v.c_npost = v.c_ndyn = v.c_nrays_bp = v.c_npre_bp = v.c_nfast_bp = 0;
   const int64_t hw = view_pixels(v);
   for (int64_t i = 0; i < hw; ++i) {
     const RayMeta& r = vm[i];
@@ -398,6 +405,7 @@ void view_counters(View& v, const RayMeta* vm) {
     if (ray_in_bp(r)) {
       ++v.c_nrays_bp;
       v.c_npre_bp += r.n_pre;
+      v.c_nfast_bp += r.n_pre - (ray_kdyn(r) & ~3);
     }
   }
 }
@@ -672,11 +680,12 @@ uint32_t region_blocks(mrf_map* m, const std::vector<int>& views, const std::vec
   }
   const uint32_t end = at + (uint32_t)pix.size();
   m->region_q.reserve(std::max<size_t>(end, 1) * sizeof(RayMeta), true, m->stream);
+  m->region_ids.reserve(std::max<size_t>(end, 1) * 4, true, m->stream);
   if (!pix.empty()) {
     m->ray_order.reserve(pix.size() * 4, false, m->stream);
     CK(cudaMemcpyAsync(m->ray_order.p, pix.data(), pix.size() * 4, cudaMemcpyHostToDevice, m->stream));
     CK(launch_ray_queue(m->meta.as<RayMeta>(), m->ray_order.as<uint32_t>(), (uint32_t)pix.size(),
-                        m->region_q.as<RayMeta>() + at, m->stream));
+                        m->region_q.as<RayMeta>() + at, m->region_ids.as<uint32_t>() + at, 0u, m->stream));
     sync(m);  // the host vector goes out of scope
   }
   return end;
@@ -738,12 +747,13 @@ void view_ray_queue(mrf_map* m, int c, const RayMeta* vm) {
   CK(sort_pairs_u32(m->s_tmp.p, t, m->s_k0.as<uint32_t>(), m->s_k1.as<uint32_t>(), m->s_v0.as<uint32_t>(),
                     m->s_v1.as<uint32_t>(), (uint32_t)hw, 17, m->stream));
   CK(launch_ray_queue(m->meta.as<RayMeta>() + v.pix_base, m->s_v1.as<uint32_t>(), (uint32_t)act,
-                      m->ray_queue.as<RayMeta>() + v.order_base, m->stream));
+                      m->ray_queue.as<RayMeta>() + v.order_base, m->queue_ids.as<uint32_t>() + v.order_base,
+                      (uint32_t)v.pix_base, m->stream));
 }
 
 // the statistics of the live views
 void stats_from_views(mrf_map* m) {
-  int64_t nrays = 0, npre = 0, npost = 0, ndyn = 0, nrays_bp = 0, npre_bp = 0, np = 0, ndp = 0;
+  int64_t nrays = 0, npre = 0, npost = 0, ndyn = 0, nrays_bp = 0, npre_bp = 0, np = 0, ndp = 0, nfast = 0;
   for (const View& v : m->views) {
     if (v.retired) continue;
     nrays += v.c_nrays;
@@ -752,6 +762,7 @@ void stats_from_views(mrf_map* m) {
     ndyn += v.c_ndyn;
     nrays_bp += v.c_nrays_bp;
     npre_bp += v.c_npre_bp;
+    nfast += v.c_nfast_bp;
     np += v.n_pairs;
     ndp += v.n_dpairs;
   }
@@ -763,6 +774,8 @@ void stats_from_views(mrf_map* m) {
   m->stats.n_pairs_dyn = ndp;
   m->stats.n_rays_bp = nrays_bp;
   m->stats.n_inc_pre_bp = npre_bp;
+  m->stats.n_inc_from_k4 = nfast;
+  m->stats.n_loud_prefix = m->n_loud_prefix;
 }
 
 int voxel_id_bits(const mrf_map* m) {
@@ -826,6 +839,52 @@ void view_tiles(mrf_map* m, int c, uint32_t tb) {
   v.tile_base = tb;
   CK(launch_tile_first(m->dseg.as<uint32_t>(), v.dpair_base, v.dpair_base + v.n_dpairs, v.dperm_base,
                        v.dperm_base + v.n_dperm, m->tile_first.as<uint32_t>() + tb, m->stream));
+}
+
+// The loud lists of the static prefixes of every live view's queued rays
+// (npix pixel records in meta): counts per ray, one scan over all pixels,
+// then the lists (pair id, length, position) -- the data the ray kernel's
+// fast path gathers every iteration, and room for the quiet sums.
+void build_loud_lists(mrf_map* m, int64_t npix) {
+  m->loud_off.reserve((size_t)(npix + 1) * 4, false, m->stream);
+  m->quiet_q.reserve((size_t)std::max<int64_t>(npix, 1) * 8, false, m->stream);
+  CK(cudaMemsetAsync(m->loud_off.p, 0, (size_t)(npix + 1) * 4, m->stream));
+  const RayMeta* meta = m->meta.as<RayMeta>();
+  for (const View& v : m->views) {
+    if (v.retired || v.n_inc == 0) continue;
+    CK(launch_loud_prefix(meta, (uint32_t)v.pix_base, (uint32_t)view_pixels(v), m->inc_pair.as<uint32_t>(),
+                          m->inc_len.as<float>(), v.pair_base, v.n_loud, m->loud_off.as<uint32_t>(), nullptr,
+                          nullptr, nullptr, false, m->stream));
+  }
+  m->s_offs.reserve((size_t)(npix + 1) * 4, false, m->stream);
+  const size_t t = scan_temp_bytes((uint32_t)(npix + 1));
+  m->s_tmp.reserve(t, false, m->stream);
+  CK(exclusive_scan_u32(m->s_tmp.p, t, m->loud_off.as<uint32_t>(), m->s_offs.as<uint32_t>(), (uint32_t)(npix + 1),
+                        m->stream));
+  std::swap(m->loud_off, m->s_offs);
+  const uint32_t total = read1(m, m->loud_off.as<uint32_t>() + npix);
+  m->loud_pid.reserve((size_t)std::max<uint32_t>(total, 1) * 4, false, m->stream);
+  m->loud_len.reserve((size_t)std::max<uint32_t>(total, 1) * 4, false, m->stream);
+  m->loud_pos.reserve((size_t)std::max<uint32_t>(total, 1) * 2, false, m->stream);
+  for (const View& v : m->views) {
+    if (v.retired || v.n_inc == 0) continue;
+    CK(launch_loud_prefix(meta, (uint32_t)v.pix_base, (uint32_t)view_pixels(v), m->inc_pair.as<uint32_t>(),
+                          m->inc_len.as<float>(), v.pair_base, v.n_loud, m->loud_off.as<uint32_t>(),
+                          m->loud_pid.as<uint32_t>(), m->loud_len.as<float>(), m->loud_pos.as<uint16_t>(), true,
+                          m->stream));
+  }
+  m->n_loud_prefix = total;
+}
+
+// the quiet sums of every live view's static prefixes from the current
+// ln q (valid from the third iteration of a call on, when the quiet pairs'
+// ln q no longer change)
+void quiet_prefix_all(mrf_map* m, const BpArrays& a) {
+  for (const View& v : m->views) {
+    if (v.retired || v.n_inc == 0) continue;
+    CK(launch_quiet_prefix(a, (uint32_t)v.pix_base, (uint32_t)view_pixels(v), v.pair_base, v.n_loud,
+                           m->quiet_q.as<float2>(), m->stream));
+  }
 }
 
 void rebuild_lists(mrf_map* m, OldPairs& old) {
@@ -919,6 +978,7 @@ void rebuild_lists(mrf_map* m, OldPairs& old) {
   //    SM-affine region blocks
   {
     m->ray_queue.reserve((size_t)std::max<int64_t>(npix, 1) * sizeof(RayMeta), false, m->stream);
+    m->queue_ids.reserve((size_t)std::max<int64_t>(npix, 1) * 4, false, m->stream);
     int64_t base = 0;
     for (int c = 0; c < V; ++c) {
       View& v = m->views[c];
@@ -1012,6 +1072,7 @@ void rebuild_lists(mrf_map* m, OldPairs& old) {
                             m->vox_active.as<uint8_t>(), nv, m->stream));
     m->vox_active_n = nv;
   }
+  build_loud_lists(m, npix);
   CK(cudaEventRecord(m->ev1, m->stream));
   sync(m);
   check_device_err(m);
@@ -1146,6 +1207,7 @@ bool append_lists(mrf_map* m) {
     for (int c = 0; c < m->built_views; ++c) base = std::max<int64_t>(base, (int64_t)m->views[c].order_base + m->views[c].n_active);
     base = std::max<int64_t>(base, m->queue_end);
     m->ray_queue.reserve((size_t)std::max<int64_t>(base + hw_new, 1) * sizeof(RayMeta), true, m->stream);
+    m->queue_ids.reserve((size_t)std::max<int64_t>(base + hw_new, 1) * 4, true, m->stream);
     for (int c = m->built_views; c < V; ++c) {
       View& v = m->views[c];
       v.order_base = (uint32_t)base;
@@ -1213,6 +1275,7 @@ bool append_lists(mrf_map* m) {
   m->vox_active_n = nvox;
   CK(launch_mark_active(m->pair_vox.as<uint32_t>() + pair0, m->pair_cum.as<float>() + pair0,
                         (uint32_t)(pair_total - pair0), m->vox_active.as<uint8_t>(), m->stream));
+  build_loud_lists(m, npix);
   CK(cudaEventRecord(m->ev1, m->stream));
   sync(m);
   check_device_err(m);
@@ -1361,11 +1424,13 @@ RayWork ray_work(mrf_map* m, int c) {
   const uint32_t R = m->nreg;
   RayWork w{};
   w.region = m->region_q.as<RayMeta>();
+  w.region_ids = m->region_ids.as<uint32_t>();
   w.rper = R;
   uint32_t* lc = m->rcounters.as<uint32_t>() + (size_t)2 * V * R;  // leftover counters
   if (c >= 0) {
     const View& v = m->views[c];
     w.queue = m->ray_queue.as<RayMeta>() + v.order_base;
+    w.queue_ids = m->queue_ids.as<uint32_t>() + v.order_base;
     w.n_rays = v.n_active;
     w.counter = m->counters.as<uint32_t>() + c;
     w.rstart = m->rstart.as<uint32_t>() + (size_t)c * (R + 1);
@@ -1377,6 +1442,7 @@ RayWork ray_work(mrf_map* m, int c) {
     w.lcounter = lc + c;
   } else {
     w.queue = m->ray_queue.as<RayMeta>();
+    w.queue_ids = m->queue_ids.as<uint32_t>();
     for (const View& v : m->views) w.n_rays += v.n_active;
     w.counter = m->counters.as<uint32_t>() + V;
     w.rstart = m->rstart.as<uint32_t>();
@@ -1417,7 +1483,7 @@ void enqueue_iteration(mrf_map* m, const BpArrays& a, bool jacobi, int fix, int 
                              m->stream));
       prof.end();
       prof.begin(1);
-      CK(launch_ray_bp(a, ray_work(m, c), fix, m->num_sms, m->ray_variant, m->stream));
+      CK(launch_ray_bp(a, ray_work(m, c), fix, m->num_sms, m->ray_variant, phase >= 2, m->stream));
       prof.end();
       prof.begin(2);
       if (v.n_dperm) {
@@ -1440,7 +1506,7 @@ void enqueue_iteration(mrf_map* m, const BpArrays& a, bool jacobi, int fix, int 
     prof.end();
     prof.begin(1);
     // the queues of all views are contiguous: one launch over all rays
-    CK(launch_ray_bp(a, ray_work(m, -1), fix, m->num_sms, m->ray_variant, m->stream));
+    CK(launch_ray_bp(a, ray_work(m, -1), fix, m->num_sms, m->ray_variant, phase >= 2, m->stream));
     prof.end();
     prof.begin(2);
     CK(launch_pair_update(a, 0, (uint32_t)m->n_dperm, 0, (uint32_t)m->n_dpairs,
@@ -1552,6 +1618,13 @@ void run_infer(mrf_map* m, const int* ids, int n_ids, int iters, int flags, floa
                            m->stream));
       }
       const int ph = std::min(it, 2);
+      if (it == 2) {
+        // from here on the ray kernel takes the static prefixes from
+        // their quiet sums
+        prof.begin(1);
+        quiet_prefix_all(m, a);
+        prof.end();
+      }
       if (direct) {
         enqueue_iteration(m, a, jacobi, fix, ph, prof, launches);
       } else {
@@ -1655,7 +1728,8 @@ void destroy_bufs(mrf_map* m) {
                  &m->pair_dm,
                  &m->pair_seg, &m->dperm, &m->dpair, &m->dseg, &m->drun,
                  &m->carry, &m->ray_order, &m->ray_queue, &m->region_q, &m->rstart, &m->rcounters, &m->counters, &m->tile_first,
-                 &m->lbase, &m->lsingle, &m->lprefix,
+                 &m->lbase, &m->lsingle, &m->lprefix, &m->queue_ids, &m->region_ids, &m->loud_off,
+                 &m->loud_pid, &m->loud_len, &m->loud_pos, &m->quiet_q,
                  &m->vseg, &m->vpairs, &m->vvox, &m->vox_active, &m->d_Lbase, &m->inc_len16, &m->pair_q16,
                  &m->s_rec, &m->s_recs, &m->s_pf, &m->s_ps,
                  &m->s_flags, &m->s_ind, &m->s_scan,
@@ -2067,7 +2141,7 @@ static void warm_start_impl(mrf_map* m, const float* L_pred, bool device_ptr, in
   for (int k = 0; k < sweeps; ++k) {
     zero_counters(m);
     CK(launch_pair_prepare(a, 0, P, 1, m->stream));
-    CK(launch_ray_bp(a, ray_work(m, -1), 0, m->num_sms, m->ray_variant, m->stream));
+    CK(launch_ray_bp(a, ray_work(m, -1), 0, m->num_sms, m->ray_variant, false, m->stream));
     CK(launch_pair_update(a, 0, (uint32_t)m->n_dperm, 0, (uint32_t)m->n_dpairs,
                           m->tile_first.as<uint32_t>() + m->jac_tile_base, m->carry.as<TileCarry>(),
                           1, m->stream));
@@ -2227,6 +2301,7 @@ static double time_schedule(mrf_map* m, bool jacobi, int reps) {
   CK(cudaMemcpyAsync(snap + 2 * nv, m->pair_m.p, npb, cudaMemcpyDeviceToDevice, m->stream));
   Profiler off{m, false};
   int64_t launches = 0;
+  quiet_prefix_all(m, a);
   for (int r = 0; r <= reps; ++r) {
     if (r == 1) CK(cudaEventRecord(m->ev0, m->stream));
     enqueue_iteration(m, a, jacobi, 0, 2, off, launches);
@@ -2347,6 +2422,7 @@ mrf_status mrf_autotune_flags(mrf_map* m, int reps, int flags, double* ms_out, i
       const int keep = m->ray_variant;
       Profiler off{m, false};
       int64_t launches = 0;
+      quiet_prefix_all(m, a);
       for (int k = 0; k < NV; ++k) {
         m->ray_variant = k;
         for (int r = 0; r <= reps; ++r) {

@@ -200,6 +200,11 @@ struct BpArrays {
   // fp16 then
   int half_streams;
   int pair_variant;  // pair reduction: 0 one prefetched pair per thread, 1 two
+  const float2* quiet_q;     // per ray: quiet sums of the static prefix
+  const uint32_t* loud_off;  // per ray: first entry of its loud list (and the next ray's)
+  const uint32_t* loud_pid;
+  const float* loud_len;
+  const uint16_t* loud_pos;
   const __half* inc_len16;
   __half* pair_lnq16;
 };
@@ -226,11 +231,24 @@ cudaError_t launch_to_half(const float* in, int64_t n, __half* out, cudaStream_t
 // zeroed counters), and the views' remaining short rays (longest first):
 // view q's lprefix[q + 1] - lprefix[q] leftovers from region[lbase[q]] on,
 // nlv views, one zeroed counter
+// the static-prefix data of the ray kernel's fast path (iterations from the
+// third of a call on): per ray (pixel index) the quiet sums up to r0 and up
+// to k4, and the list of the prefix's loud incidences at loff[r]..loff[r+1]
+struct QuietPrefix {
+  const float2* q;
+  const uint32_t* loff;
+  const uint32_t* lpid;
+  const float* llen;
+  const uint16_t* lpos;
+};
+
 struct RayWork {
   const RayMeta* queue;
+  const uint32_t* queue_ids;   // pixel index of each queue record
   uint32_t n_rays;
   uint32_t* counter;
   const RayMeta* region;
+  const uint32_t* region_ids;
   const uint32_t* rstart;
   uint32_t nreg, rper;
   uint32_t* rcounter;
@@ -239,13 +257,23 @@ struct RayWork {
   uint32_t nlv;
   uint32_t* lcounter;
 };
+// quiet: the static prefix from the quiet sums (a.quiet_q and the loud
+// lists must be current)
 cudaError_t launch_ray_bp(const BpArrays& a, const RayWork& w, int fix_reset, int num_sms, int variant,
-                          cudaStream_t s);
+                          bool quiet, cudaStream_t s);
+// loud incidences of the static prefixes of rays r_first..r_first+n of one
+// view: counts to loff[r] (emit false), or the lists at loff[r] (emit true)
+cudaError_t launch_loud_prefix(const RayMeta* meta, uint32_t r_first, uint32_t n, const uint32_t* inc_pair,
+                               const float* inc_len, uint32_t pair_base, uint32_t n_loud, uint32_t* loff,
+                               uint32_t* lpid, float* llen, uint16_t* lpos, bool emit, cudaStream_t s);
+// quiet sums of the static prefixes of rays r_first..r_first+n of one view
+cudaError_t launch_quiet_prefix(const BpArrays& a, uint32_t r_first, uint32_t n, uint32_t pair_base,
+                                uint32_t n_loud, float2* q, cudaStream_t s);
 cudaError_t launch_ray_keys(const RayMeta* meta, uint32_t n, uint32_t* keys, uint32_t* vals,
                             cudaStream_t s);
-// queue[i] = meta[order[i]], i < n
+// queue[i] = meta[order[i]], ids[i] = id_base + order[i], i < n
 cudaError_t launch_ray_queue(const RayMeta* meta, const uint32_t* order, uint32_t n, RayMeta* queue,
-                             cudaStream_t s);
+                             uint32_t* ids, uint32_t id_base, cudaStream_t s);
 // dynamic positions k0..k1 hold the runs j0..j1 (dpair/dseg indices);
 // tile_first from launch_tile_first over dseg
 cudaError_t launch_pair_update(const BpArrays& a, uint32_t k0, uint32_t k1, uint32_t j0, uint32_t j1,

@@ -80,7 +80,9 @@ class mrf_stats(C.Structure):
                                                                 ("n_rays_bp", C.c_int64),
                                                                 ("n_inc_pre_bp", C.c_int64),
                                                                 ("builds_full", C.c_int64),
-                                                                ("builds_appended", C.c_int64)]
+                                                                ("builds_appended", C.c_int64),
+                                                                ("n_inc_from_k4", C.c_int64),
+                                                                ("n_loud_prefix", C.c_int64)]
 
 
 _lib = None
