@@ -389,15 +389,28 @@ __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, uint32_t rid, con
   // their sums up to r0 and up to k4 were formed once (k_quiet_prefix);
   // only the prefix's loud incidences are gathered here.  A ray in the
   // queues has a non-zero potential, so its rinf equals r0.
-  int start = 0;
+  const int start = qp.q ? k4 : 0;
+  // kPf >= 1: the first chunk's pair ids are requested before the static
+  // prefix's loads, so the two chains of dependent loads overlap
+  uint32_t pid_next[kE];
+  float len_next[kE];
+  if (kPf) load_pids<kE, kPol>(pid_next, off, start + kE * lane, n_pre, inc_pair);
+  if (kPf == 2) ld_len<kE, kPol>(len_next, inc_len + off, start + kE * lane, start + kE * lane < n_pre);
   if (qp.q) {
     const float2 qv = qp.q[rid];
     const uint32_t e0 = qp.loff[rid], e1 = qp.loff[rid + 1];
     float la = 0.0f, lk = 0.0f;
-    for (uint32_t e = e0 + lane; e < e1; e += 32) {
-      const float c = qp.llen[e] * to_f(__ldg(lnq + qp.lpid[e]));
-      lk += c;
-      if ((int)qp.lpos[e] < r0) la += c;
+    // two entries per lane in flight (a ray's list holds ~40 on average)
+    for (uint32_t e = e0 + lane; e < e1; e += 64) {
+      const bool two = e + 32 < e1;
+      const uint32_t p0 = qp.lpid[e], p1 = two ? qp.lpid[e + 32] : p0;
+      const float l0 = qp.llen[e], l1 = two ? qp.llen[e + 32] : 0.0f;
+      const int j0 = qp.lpos[e], j1 = two ? (int)qp.lpos[e + 32] : 0x7FFFFFFF;
+      const float c0 = l0 * to_f(__ldg(lnq + p0)), c1 = l1 * to_f(__ldg(lnq + p1));
+      lk += c0;
+      if (j0 < r0) la += c0;
+      lk += c1;
+      if (j1 < r0) la += c1;
     }
     lk = warp_sum(lk);
     la = warp_sum(la);
@@ -407,7 +420,6 @@ __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, uint32_t rid, con
       Ar0 = qv.x + la;
       Arinf = Ar0;
     }
-    start = k4;
   }
   // ---- pass 1: prefixes, Pre total ---------------------------------------
   // Chunks of 128 (a chunk costs the same instructions however many of its
@@ -420,10 +432,7 @@ __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, uint32_t rid, con
   float ts = 0.0f, tc = 0.0f;
   Slice<kE> s;
   {
-    uint32_t pid_next[kE];
-    float len_next[kE], len[kE];
-    if (kPf) load_pids<kE, kPol>(pid_next, off, start + kE * lane, n_pre, inc_pair);
-    if (kPf == 2) ld_len<kE, kPol>(len_next, inc_len + off, start + kE * lane, start + kE * lane < n_pre);
+    float len[kE];
     for (int base = start; base < n_pre; base += kChunk) {
       const int i0 = base + kE * lane;
       uint32_t pid[kE];
@@ -539,19 +548,23 @@ __global__ void __launch_bounds__(kRayWarps * 32, kMinBlocks) k_ray_bp(const Ray
       const uint32_t q = r / rper;
       const uint32_t* rs = rstart + (size_t)q * (rper + 1) + (r - q * rper);
       const uint32_t a = rs[0], nr = rs[1] - a;
-      for (;;) {
-        uint32_t idx = 0;
+      // the next ticket is taken before the current ray runs, so its
+      // atomic's latency hides behind the ray's work
+      uint32_t idx = 0;
+      if (lane == 0) idx = atomicAdd(counter + r, 1u);
+      idx = __shfl_sync(kFull, idx, 0);
+      while (idx < nr) {
+        const uint32_t cur = a + idx;
         if (lane == 0) idx = atomicAdd(counter + r, 1u);
         idx = __shfl_sync(kFull, idx, 0);
-        if (idx >= nr) break;
-        ray_at(a + idx);
+        ray_at(cur);
       }
     }
     // the views' leftovers, one ticket counter over all of them: ticket t
     // is view q's (t - lprefix[q])-th leftover for the last q with
     // lprefix[q] <= t
     const uint32_t n_left = lprefix[nlv];
-    for (;;) {
+    auto leftover = [&]() {
       uint32_t pos = 0xFFFFFFFFu;
       if (lane == 0) {
         const uint32_t t = atomicAdd(lcounter, 1u);
@@ -565,17 +578,23 @@ __global__ void __launch_bounds__(kRayWarps * 32, kMinBlocks) k_ray_bp(const Ray
           pos = lbase[lo] + (t - lprefix[lo]);
         }
       }
-      pos = __shfl_sync(kFull, pos, 0);
-      if (pos == 0xFFFFFFFFu) break;
-      ray_at(pos);
+      return __shfl_sync(kFull, pos, 0);
+    };
+    uint32_t pos = leftover();
+    while (pos != 0xFFFFFFFFu) {
+      const uint32_t cur = pos;
+      pos = leftover();
+      ray_at(cur);
     }
   } else {
-    for (;;) {
-      uint32_t idx = 0;
+    uint32_t idx = 0;
+    if (lane == 0) idx = atomicAdd(counter, 1u);
+    idx = __shfl_sync(kFull, idx, 0);
+    while (idx < n_rays) {
+      const uint32_t cur = idx;
       if (lane == 0) idx = atomicAdd(counter, 1u);
       idx = __shfl_sync(kFull, idx, 0);
-      if (idx >= n_rays) break;
-      ray_at(idx);
+      ray_at(cur);
     }
   }
 }

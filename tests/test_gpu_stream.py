@@ -90,7 +90,10 @@ def test_appended_lists_equal_a_full_build(native_lib, walk):
     """Frames added one at a time to a full-ray map, each followed by a build,
     append only the new view's lists; they are those a single build of all
     the views gives, bit for bit, and BP from the prior reaches the same
-    beliefs.  After retiring a view and appending more, a Jacobi run (which
+    beliefs within 1e-5 (from the third iteration the ray kernel sums each
+    static prefix as a quiet part and a loud part, and an appended view
+    whose quiet pair turned loud counts all its pairs as loud until the
+    next full build, so the two maps round those sums differently).  After retiring a view and appending more, a Jacobi run (which
     needs the all-view structures: a full build first) matches a map built
     directly from the live views."""
     w, depths = walk
@@ -113,7 +116,7 @@ def test_appended_lists_equal_a_full_build(native_lib, walk):
     b.reset_state()
     a.infer(iters=5)
     b.infer(iters=5)
-    np.testing.assert_allclose(a.beliefs(), b.beliefs(), rtol=0, atol=1e-6)
+    np.testing.assert_allclose(a.beliefs(), b.beliefs(), rtol=0, atol=1e-5)
     # a window step: retire, append, then Jacobi
     a.retire_view(0)
     for k in (8, 9):
