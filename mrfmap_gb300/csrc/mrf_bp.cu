@@ -400,17 +400,10 @@ __device__ __forceinline__ void ray_bp_warp(const RayMeta& me, uint32_t rid, con
     const float2 qv = qp.q[rid];
     const uint32_t e0 = qp.loff[rid], e1 = qp.loff[rid + 1];
     float la = 0.0f, lk = 0.0f;
-    // two entries per lane in flight (a ray's list holds ~40 on average)
-    for (uint32_t e = e0 + lane; e < e1; e += 64) {
-      const bool two = e + 32 < e1;
-      const uint32_t p0 = qp.lpid[e], p1 = two ? qp.lpid[e + 32] : p0;
-      const float l0 = qp.llen[e], l1 = two ? qp.llen[e + 32] : 0.0f;
-      const int j0 = qp.lpos[e], j1 = two ? (int)qp.lpos[e + 32] : 0x7FFFFFFF;
-      const float c0 = l0 * to_f(__ldg(lnq + p0)), c1 = l1 * to_f(__ldg(lnq + p1));
-      lk += c0;
-      if (j0 < r0) la += c0;
-      lk += c1;
-      if (j1 < r0) la += c1;
+    for (uint32_t e = e0 + lane; e < e1; e += 32) {
+      const float c = qp.llen[e] * to_f(__ldg(lnq + qp.lpid[e]));
+      lk += c;
+      if ((int)qp.lpos[e] < r0) la += c;
     }
     lk = warp_sum(lk);
     la = warp_sum(la);
