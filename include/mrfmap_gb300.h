@@ -297,7 +297,8 @@ MRF_API mrf_status mrf_set_pair_variant(mrf_map* map, int variant);  /* 0 or 1 *
  *                              gathers ln q as fp16 (round to nearest);
  *                              every product, prefix and sum stays fp32
  *                              (fp64 on long rays), the messages fp32.
- *                              About 3 % faster; belief error against the
+ *                              No faster on the bench map (the ray kernel
+ *                              is latency-bound); belief error against the
  *                              FP64 oracle 1.5e-6 on a converged 1 cm map,
  *                              but 2.8e-3 in the transient of an incremental
  *                              schedule, so not the default.
