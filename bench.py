@@ -343,7 +343,7 @@ HOME_SHARES = (60, 75, 90)  # per cent of an SM region's work on its home blocks
 def ray_kernel_bytes(st, iters, half=False):
     """Algorithmic bytes of the ray-message work of one mrf_infer call of
     `iters` iterations, over the rays it runs over (those with a dynamic
-    incidence).  Gather width g and length width l: 4 B each with the
+    incidence); the call's stats say whether it took the fast path.  Gather width g and length width l: 4 B each with the
     default fp32 streams, 2 B each with 16-bit streams.
       the first two iterations (full path): per Pre incidence the pair id
         (4 B), length and ln q gather (l + g); per dynamic incidence +8 B
@@ -359,7 +359,7 @@ def ray_kernel_bytes(st, iters, half=False):
     pre, k4, loud = st["n_inc_pre_bp"], st["n_inc_from_k4"], st["n_loud_prefix"]
     dyn, rays = st["n_inc_dyn"], st["n_rays_bp"]
     full = (4 + ln + g) * pre + 8 * dyn + 16 * rays
-    if iters < 3:
+    if iters < 3 or not st.get("quiet_prefix_used"):
         return full * iters
     quiet = (8 + g) * (pre - k4) + 16 * rays
     fast = (4 + ln + g) * k4 + (10 + g) * loud + 8 * dyn + 36 * rays

@@ -49,6 +49,13 @@ typedef enum {
 #define MRF_PROFILE 16      /* time every kernel with CUDA events (mrf_stats) */
 #define MRF_NO_GRAPH 32     /* launch kernels one by one instead of replaying the
                                captured CUDA graph of one iteration */
+#define MRF_FULL_RAYS 64    /* read every ray's whole Pre range in every iteration
+                               (no static prefixes from their quiet sums; by default
+                               a call of 4 or more iterations takes them from the
+                               third iteration on when the quiet incidences are at
+                               least half of the Pre incidences) */
+#define MRF_QUIET_PREFIX 128 /* take the static prefixes from their quiet sums from
+                                the third iteration on whatever their share */
 
 /* Mirrors gvdb_params_t (include/mrfmap/GVDBParams.h:11-28). */
 typedef struct mrf_params {
@@ -102,7 +109,10 @@ typedef struct mrf_stats {
                               iteration of a call on */
   int64_t n_loud_prefix;   /* incidences before k4 on voxels with a dynamic
                               incidence in some view: the rest of the static
-                              prefixes is summed once per call */
+                              prefixes is summed once per call (0 until the
+                              first call of 4 or more iterations counts them) */
+  int64_t quiet_prefix_used; /* 1 if the last mrf_infer took the static
+                                prefixes from their quiet sums */
 } mrf_stats;
 
 /* Map construction: GVDBInference(...) + GVDBMRFMap::gpuAllocate

@@ -192,6 +192,7 @@ struct mrf_map {
   int built_views = 0;
   int64_t npix_total = 0, queue_end = 0, tile_end = 0, carry_tiles = 0, vox_active_n = 0, n_perm_total = 0;
   int64_t n_loud_prefix = 0;  // entries of the static prefixes' loud lists
+  int64_t loud_count_version = -1, loud_list_version = -1;  // builds the loud lists were counted / made for
   uint32_t region_end = 0;
   int64_t bricks_at_build = -1;
   // holes: retired views' lists still in the arenas; appended: lists added
@@ -232,13 +233,13 @@ struct mrf_map {
   // MRF_PROFILE event pool
   std::vector<cudaEvent_t> prof_ev;
   std::vector<int> prof_cat;
-  // captured BP iteration per schedule (Jacobi bit, fixed-reset bit, first
-  // iteration of an mrf_infer call bit)
+  // captured BP iteration per schedule (Jacobi bit, fixed-reset bit, the
+  // phase of the iteration in its call (two bits), quiet-prefix bit)
   struct GraphSlot {
     cudaGraphExec_t exec = nullptr;
     int version = -1;
     int64_t launches = 0;
-  } graphs[12];
+  } graphs[32];
 
   BpArrays bp() const {
     BpArrays a;
@@ -775,7 +776,7 @@ void stats_from_views(mrf_map* m) {
   m->stats.n_rays_bp = nrays_bp;
   m->stats.n_inc_pre_bp = npre_bp;
   m->stats.n_inc_from_k4 = nfast;
-  m->stats.n_loud_prefix = m->n_loud_prefix;
+  m->stats.n_loud_prefix = m->loud_count_version == m->built_version ? m->n_loud_prefix : 0;
 }
 
 int voxel_id_bits(const mrf_map* m) {
@@ -845,9 +846,9 @@ void view_tiles(mrf_map* m, int c, uint32_t tb) {
 // (npix pixel records in meta): counts per ray, one scan over all pixels,
 // then the lists (pair id, length, position) -- the data the ray kernel's
 // fast path gathers every iteration, and room for the quiet sums.
-void build_loud_lists(mrf_map* m, int64_t npix) {
+void count_loud_lists(mrf_map* m) {
+  const int64_t npix = m->npix_total;
   m->loud_off.reserve((size_t)(npix + 1) * 4, false, m->stream);
-  m->quiet_q.reserve((size_t)std::max<int64_t>(npix, 1) * 8, false, m->stream);
   CK(cudaMemsetAsync(m->loud_off.p, 0, (size_t)(npix + 1) * 4, m->stream));
   const RayMeta* meta = m->meta.as<RayMeta>();
   for (const View& v : m->views) {
@@ -862,7 +863,15 @@ void build_loud_lists(mrf_map* m, int64_t npix) {
   CK(exclusive_scan_u32(m->s_tmp.p, t, m->loud_off.as<uint32_t>(), m->s_offs.as<uint32_t>(), (uint32_t)(npix + 1),
                         m->stream));
   std::swap(m->loud_off, m->s_offs);
-  const uint32_t total = read1(m, m->loud_off.as<uint32_t>() + npix);
+  m->n_loud_prefix = read1(m, m->loud_off.as<uint32_t>() + npix);
+  m->stats.n_loud_prefix = m->n_loud_prefix;
+}
+
+void emit_loud_lists(mrf_map* m) {
+  const int64_t npix = m->npix_total;
+  const uint32_t total = (uint32_t)m->n_loud_prefix;
+  const RayMeta* meta = m->meta.as<RayMeta>();
+  m->quiet_q.reserve((size_t)std::max<int64_t>(npix, 1) * 8, false, m->stream);
   m->loud_pid.reserve((size_t)std::max<uint32_t>(total, 1) * 4, false, m->stream);
   m->loud_len.reserve((size_t)std::max<uint32_t>(total, 1) * 4, false, m->stream);
   m->loud_pos.reserve((size_t)std::max<uint32_t>(total, 1) * 2, false, m->stream);
@@ -873,7 +882,30 @@ void build_loud_lists(mrf_map* m, int64_t npix) {
                           m->loud_pid.as<uint32_t>(), m->loud_len.as<float>(), m->loud_pos.as<uint16_t>(), true,
                           m->stream));
   }
-  m->n_loud_prefix = total;
+}
+
+// Whether a call of `iters` iterations takes the static prefixes from
+// their quiet sums from its third iteration on: only when at least two
+// iterations use them (the quiet sums cost about one pass over the static
+// prefixes) and the quiet incidences are at least half of the Pre
+// incidences (else the per-ray overhead outweighs the saved gathers; maps
+// of short rays near many surfaces).  Counts the loud lists of the current
+// build when needed and makes them when the answer is yes.
+bool quiet_path(mrf_map* m, int64_t iters, int flags) {
+  const bool force = (flags & MRF_QUIET_PREFIX) != 0;
+  if (iters < (force ? 3 : 4) || (flags & MRF_FULL_RAYS) || m->n_inc <= 0 || m->npix_total <= 0) return false;
+  if (m->loud_count_version != m->built_version) {
+    count_loud_lists(m);
+    m->loud_count_version = m->built_version;
+    m->loud_list_version = -1;
+  }
+  const int64_t pre = m->stats.n_inc_pre_bp, k4 = m->stats.n_inc_from_k4;
+  if (!force && (pre - k4 - m->n_loud_prefix) * 2 < pre) return false;
+  if (m->loud_list_version != m->built_version) {
+    emit_loud_lists(m);
+    m->loud_list_version = m->built_version;
+  }
+  return true;
 }
 
 // the quiet sums of every live view's static prefixes from the current
@@ -1072,7 +1104,6 @@ void rebuild_lists(mrf_map* m, OldPairs& old) {
                             m->vox_active.as<uint8_t>(), nv, m->stream));
     m->vox_active_n = nv;
   }
-  build_loud_lists(m, npix);
   CK(cudaEventRecord(m->ev1, m->stream));
   sync(m);
   check_device_err(m);
@@ -1275,7 +1306,6 @@ bool append_lists(mrf_map* m) {
   m->vox_active_n = nvox;
   CK(launch_mark_active(m->pair_vox.as<uint32_t>() + pair0, m->pair_cum.as<float>() + pair0,
                         (uint32_t)(pair_total - pair0), m->vox_active.as<uint8_t>(), m->stream));
-  build_loud_lists(m, npix);
   CK(cudaEventRecord(m->ev1, m->stream));
   sync(m);
   check_device_err(m);
@@ -1469,7 +1499,7 @@ void zero_counters(mrf_map* m) {
 // moves only through static-pair updates, which happen in the first
 // iteration, and the second iteration's prepare has seen them all.  Those
 // pairs' ln q is then left as it is.
-void enqueue_iteration(mrf_map* m, const BpArrays& a, bool jacobi, int fix, int phase,
+void enqueue_iteration(mrf_map* m, const BpArrays& a, bool jacobi, int fix, int phase, bool quiet,
                        Profiler& prof, int64_t& launches) {
   const int V = (int)m->views.size();
   const bool first = phase == 0;
@@ -1483,7 +1513,7 @@ void enqueue_iteration(mrf_map* m, const BpArrays& a, bool jacobi, int fix, int 
                              m->stream));
       prof.end();
       prof.begin(1);
-      CK(launch_ray_bp(a, ray_work(m, c), fix, m->num_sms, m->ray_variant, phase >= 2, m->stream));
+      CK(launch_ray_bp(a, ray_work(m, c), fix, m->num_sms, m->ray_variant, quiet && phase >= 2, m->stream));
       prof.end();
       prof.begin(2);
       if (v.n_dperm) {
@@ -1506,7 +1536,7 @@ void enqueue_iteration(mrf_map* m, const BpArrays& a, bool jacobi, int fix, int 
     prof.end();
     prof.begin(1);
     // the queues of all views are contiguous: one launch over all rays
-    CK(launch_ray_bp(a, ray_work(m, -1), fix, m->num_sms, m->ray_variant, phase >= 2, m->stream));
+    CK(launch_ray_bp(a, ray_work(m, -1), fix, m->num_sms, m->ray_variant, quiet && phase >= 2, m->stream));
     prof.end();
     prof.begin(2);
     CK(launch_pair_update(a, 0, (uint32_t)m->n_dperm, 0, (uint32_t)m->n_dpairs,
@@ -1524,9 +1554,9 @@ void enqueue_iteration(mrf_map* m, const BpArrays& a, bool jacobi, int fix, int 
 
 // The iteration is captured once per incidence build and schedule into a
 // CUDA graph and replayed iters times.
-cudaGraphExec_t iteration_graph(mrf_map* m, const BpArrays& a, bool jacobi, int fix, int phase,
+cudaGraphExec_t iteration_graph(mrf_map* m, const BpArrays& a, bool jacobi, int fix, int phase, bool quiet,
                                 int64_t& launches_per_iter) {
-  int key = (jacobi ? 1 : 0) | (fix ? 2 : 0) | (phase << 2);
+  int key = (jacobi ? 1 : 0) | (fix ? 2 : 0) | (phase << 2) | (quiet ? 16 : 0);
   auto& slot = m->graphs[key];
   if (slot.exec && slot.version == m->built_version) {
     launches_per_iter = slot.launches;
@@ -1541,7 +1571,7 @@ cudaGraphExec_t iteration_graph(mrf_map* m, const BpArrays& a, bool jacobi, int 
   cudaGraph_t graph = nullptr;
   CK(cudaStreamBeginCapture(m->stream, cudaStreamCaptureModeThreadLocal));
   try {
-    enqueue_iteration(m, a, jacobi, fix, phase, off, launches);
+    enqueue_iteration(m, a, jacobi, fix, phase, quiet, off, launches);
   } catch (...) {
     cudaStreamEndCapture(m->stream, &graph);
     if (graph) cudaGraphDestroy(graph);
@@ -1580,6 +1610,8 @@ void run_infer(mrf_map* m, const int* ids, int n_ids, int iters, int flags, floa
   const int V = (int)m->views.size();
   if (iters <= 0) iters = m->prm.max_iters > 0 ? m->prm.max_iters : 1;
   if (check_every < 1) check_every = 1;
+  const bool quiet = quiet_path(m, iters, flags);  // before bp(): it may allocate the loud lists
+  m->stats.quiet_prefix_used = quiet ? 1 : 0;
   BpArrays a = m->bp();
   int64_t launches = 0;
   Profiler prof{m, (flags & MRF_PROFILE) != 0};
@@ -1609,7 +1641,8 @@ void run_infer(mrf_map* m, const int* ids, int n_ids, int iters, int flags, floa
     int64_t per[3] = {0, 0, 0};
     cudaGraphExec_t exec[3] = {nullptr, nullptr, nullptr};
     if (!direct)
-      for (int ph = 0; ph < 3 && ph < iters; ++ph) exec[ph] = iteration_graph(m, a, jacobi, fix, ph, per[ph]);
+      for (int ph = 0; ph < 3 && ph < iters; ++ph)
+        exec[ph] = iteration_graph(m, a, jacobi, fix, ph, quiet, per[ph]);
     for (int it = 0; it < iters; ++it) {
       const bool check = conv && ((it + 1) % check_every == 0 || it + 1 == iters);
       if (check && !target) {
@@ -1618,7 +1651,7 @@ void run_infer(mrf_map* m, const int* ids, int n_ids, int iters, int flags, floa
                            m->stream));
       }
       const int ph = std::min(it, 2);
-      if (it == 2) {
+      if (it == 2 && quiet) {
         // from here on the ray kernel takes the static prefixes from
         // their quiet sums
         prof.begin(1);
@@ -1626,7 +1659,7 @@ void run_infer(mrf_map* m, const int* ids, int n_ids, int iters, int flags, floa
         prof.end();
       }
       if (direct) {
-        enqueue_iteration(m, a, jacobi, fix, ph, prof, launches);
+        enqueue_iteration(m, a, jacobi, fix, ph, quiet, prof, launches);
       } else {
         CK(cudaGraphLaunch(exec[ph], m->stream));
         launches += per[ph];
@@ -2292,6 +2325,8 @@ mrf_status mrf_set_ray_variant(mrf_map* m, int variant) {
 // the BP state saved before and restored after: milliseconds per iteration
 static double time_schedule(mrf_map* m, bool jacobi, int reps) {
   if (m->n_inc <= 0) return 0.0;
+  // the iterations of a long call (the third on)
+  const bool quiet = quiet_path(m, 1 << 30, jacobi ? MRF_JACOBI : 0);
   BpArrays a = m->bp();
   const size_t nv = (size_t)m->n_bricks * kBrickVox * 4, npb = (size_t)m->n_pairs * 4;
   m->s_snap.reserve(2 * nv + npb, false, m->stream);
@@ -2301,10 +2336,10 @@ static double time_schedule(mrf_map* m, bool jacobi, int reps) {
   CK(cudaMemcpyAsync(snap + 2 * nv, m->pair_m.p, npb, cudaMemcpyDeviceToDevice, m->stream));
   Profiler off{m, false};
   int64_t launches = 0;
-  quiet_prefix_all(m, a);
+  if (quiet) quiet_prefix_all(m, a);
   for (int r = 0; r <= reps; ++r) {
     if (r == 1) CK(cudaEventRecord(m->ev0, m->stream));
-    enqueue_iteration(m, a, jacobi, 0, 2, off, launches);
+    enqueue_iteration(m, a, jacobi, 0, 2, quiet, off, launches);
   }
   CK(cudaEventRecord(m->ev1, m->stream));
   sync(m);
@@ -2407,6 +2442,7 @@ mrf_status mrf_autotune_flags(mrf_map* m, int reps, int flags, double* ms_out, i
     if (jacobi && m->jacobi_version != m->built_version) build_jacobi_csr(m);
     const int V = (int)m->views.size();
     const int NV = ray_bp_variants();
+    const bool quiet = quiet_path(m, 1 << 30, flags);  // the iterations of a long call
     BpArrays a = m->bp();
     std::vector<double> ms(NV, 0.0);
     if (m->n_inc > 0) {
@@ -2422,12 +2458,12 @@ mrf_status mrf_autotune_flags(mrf_map* m, int reps, int flags, double* ms_out, i
       const int keep = m->ray_variant;
       Profiler off{m, false};
       int64_t launches = 0;
-      quiet_prefix_all(m, a);
+      if (quiet) quiet_prefix_all(m, a);
       for (int k = 0; k < NV; ++k) {
         m->ray_variant = k;
         for (int r = 0; r <= reps; ++r) {
           if (r == 1) CK(cudaEventRecord(m->ev0, m->stream));
-          enqueue_iteration(m, a, jacobi, 0, 2, off, launches);
+          enqueue_iteration(m, a, jacobi, 0, 2, quiet, off, launches);
         }
         CK(cudaEventRecord(m->ev1, m->stream));
         sync(m);

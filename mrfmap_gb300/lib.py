@@ -25,6 +25,8 @@ FIX_PRE_RESET = 4
 ASYNC = 8
 PROFILE = 16
 NO_GRAPH = 32
+FULL_RAYS = 64
+QUIET_PREFIX = 128
 PRECISION_FP32 = 0
 PRECISION_HALF_STREAMS = 1
 
@@ -82,7 +84,8 @@ class mrf_stats(C.Structure):
                                                                 ("builds_full", C.c_int64),
                                                                 ("builds_appended", C.c_int64),
                                                                 ("n_inc_from_k4", C.c_int64),
-                                                                ("n_loud_prefix", C.c_int64)]
+                                                                ("n_loud_prefix", C.c_int64),
+                                                                ("quiet_prefix_used", C.c_int64)]
 
 
 _lib = None

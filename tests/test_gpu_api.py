@@ -279,6 +279,37 @@ def test_ray_variants_identical_and_autotune(native_lib, w):
         m.set_pair_variant(2)
 
 
+@pytest.mark.parametrize("flags", [0, L.JACOBI, L.FIX_PRE_RESET], ids=["gauss-seidel", "jacobi", "fix-reset"])
+def test_quiet_prefix_paths(native_lib, oracle_lib, w, flags):
+    """From the third iteration of a call the ray kernel may take each ray's
+    static prefix from its quiet sums (formed once per call) plus its loud
+    incidences.  Forced on and forced off, both paths agree with the FP64
+    oracle at the tests' tolerance and with each other to FP32 rounding of
+    the regrouped sums, and the stats say which path ran."""
+    om = O.OracleMap(w.params, threads=8)
+    for P, D in zip(w.poses, w.depths):
+        om.add_view(P, D, O.ACT_FULL_RAY)
+    om.infer(iters=10, flags=(O.JACOBI if flags & L.JACOBI else 0) | (O.FIX_PRE_RESET if flags & L.FIX_PRE_RESET else 0))
+    ob = om.beliefs()
+    om.close()
+    out = {}
+    for name, extra in (("fast", L.QUIET_PREFIX), ("full", L.FULL_RAYS)):
+        m = L.MRFMap(w.params, activation=L.ACT_FULL_RAY)
+        for P, D in zip(w.poses, w.depths):
+            m.add_view(P, D)
+        m.infer(iters=10, flags=flags | extra)
+        st = m.stats()
+        assert st["quiet_prefix_used"] == (1 if name == "fast" else 0)
+        assert st["n_loud_prefix"] >= 0
+        b = m.beliefs().astype(np.float64)
+        touched = (b > 0) | (ob > 0)
+        assert np.abs(b - ob).max() <= 1e-3
+        assert ((b > 0.5) == (ob > 0.5))[touched].mean() >= 0.999
+        out[name] = b
+        m.close()
+    np.testing.assert_allclose(out["fast"], out["full"], rtol=0, atol=1e-5)
+
+
 def test_home_share_moves_rays_not_results(native_lib, w):
     """The SM-region schedule's home share only moves rays between warps:
     every share gives the same bits, in Gauss-Seidel and Jacobi; its
