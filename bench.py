@@ -652,7 +652,8 @@ def run_ours(args):
                                "n_vox_touched": st["n_vox_touched"],
                                "n_rays": st["n_rays"], "n_rays_bp": st["n_rays_bp"],
                                "n_inc_pre_bp_per_iter": st["n_inc_pre_bp"], "n_bricks": st["n_bricks"],
-                               "n_inc_from_k4": st["n_inc_from_k4"], "n_loud_prefix": st["n_loud_prefix"],
+                               "n_inc_from_k4": st["n_inc_from_k4"], "n_loud_prefix": prof["n_loud_prefix"],
+                               "quiet_prefix_used": prof["quiet_prefix_used"],
                                "ray_variant": tuned, "ray_variant_ms": [round(x, 4) for x in tune_ms],
                                "pair_variant": m.tuning()[2],
                                "home_share": m.tuning()[1], "home_share_ms": dict(zip(HOME_SHARES[:len(share_ms)],
@@ -778,6 +779,7 @@ def run_large(args):
                              "other": 1e3 * dt / max(n, 1) - (build_ms + infer_ms) / max(n, 1)},
             "device_bytes_peak": peak, "n_bricks_final": nb,
             "list_builds": {"full": st["builds_full"], "appended": st["builds_appended"]},
+            "quiet_prefix_used": st["quiet_prefix_used"],
             "occupied_voxels_final": int((bel > 0.5).sum()),
             "clocks": clk,
             "e2e": {"value": sum_over_ranks(n, ws) / dt, "unit": "frames/s",
@@ -904,6 +906,8 @@ def run_batched(args):
             "workload_stats": {"n_inc_per_iter": st["n_inc_post"], "n_inc_dyn_per_iter": st["n_inc_dyn"],
                                "n_pairs": st["n_pairs"], "n_rays": st["n_rays"], "n_bricks": st["n_bricks"],
                                "build_s": round(build_s, 3), "ray_variant": tuned,
+                               "quiet_prefix_used": prof["quiet_prefix_used"],
+                               "n_inc_from_k4": prof["n_inc_from_k4"], "n_loud_prefix": prof["n_loud_prefix"],
                                "ray_variant_ms": [round(x, 4) for x in tune_ms],
                                "home_share": share_choice,
                                "home_share_ms": dict(zip(HOME_SHARES, [round(float(x), 4) for x in share_ms]))},

@@ -53,7 +53,8 @@ typedef enum {
                                (no static prefixes from their quiet sums; by default
                                a call of 4 or more iterations takes them from the
                                third iteration on when the quiet incidences are at
-                               least half of the Pre incidences) */
+                               least half of the Pre incidences and average at
+                               least 256 per ray) */
 #define MRF_QUIET_PREFIX 128 /* take the static prefixes from their quiet sums from
                                 the third iteration on whatever their share */
 

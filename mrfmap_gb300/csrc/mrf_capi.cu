@@ -887,20 +887,24 @@ void emit_loud_lists(mrf_map* m) {
 // Whether a call of `iters` iterations takes the static prefixes from
 // their quiet sums from its third iteration on: only when at least two
 // iterations use them (the quiet sums cost about one pass over the static
-// prefixes) and the quiet incidences are at least half of the Pre
-// incidences (else the per-ray overhead outweighs the saved gathers; maps
-// of short rays near many surfaces).  Counts the loud lists of the current
-// build when needed and makes them when the answer is yes.
+// prefixes), the quiet incidences are at least half of the Pre incidences
+// and they average at least two 128-incidence chunks per ray (else the
+// per-ray overhead outweighs the saved gathers: maps of short rays, or of
+// rays near many surfaces).  Counts the loud lists of the current build
+// when needed and makes them when the answer is yes.
+constexpr int64_t kQuietPerRay = 256;
 bool quiet_path(mrf_map* m, int64_t iters, int flags) {
   const bool force = (flags & MRF_QUIET_PREFIX) != 0;
   if (iters < (force ? 3 : 4) || (flags & MRF_FULL_RAYS) || m->n_inc <= 0 || m->npix_total <= 0) return false;
+  const int64_t pre = m->stats.n_inc_pre_bp, k4 = m->stats.n_inc_from_k4, rays = m->stats.n_rays_bp;
+  if (!force && (rays <= 0 || pre - k4 < kQuietPerRay * rays)) return false;  // no count needed
   if (m->loud_count_version != m->built_version) {
     count_loud_lists(m);
     m->loud_count_version = m->built_version;
     m->loud_list_version = -1;
   }
-  const int64_t pre = m->stats.n_inc_pre_bp, k4 = m->stats.n_inc_from_k4;
-  if (!force && (pre - k4 - m->n_loud_prefix) * 2 < pre) return false;
+  const int64_t quiet = pre - k4 - m->n_loud_prefix;
+  if (!force && (quiet * 2 < pre || quiet < kQuietPerRay * rays)) return false;
   if (m->loud_list_version != m->built_version) {
     emit_loud_lists(m);
     m->loud_list_version = m->built_version;
