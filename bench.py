@@ -568,6 +568,7 @@ def run_ours(args):
     pinned = [torch.from_numpy(np.ascontiguousarray(d)).pin_memory() for d in w.depths]
     h2d = sum(p.numel() * 4 for p in pinned) + 16 * 4 * len(w.poses)
     e2e_times, d2h, phases = [], 0, []
+    out = None  # pinned read-back buffers, allocated once from the warm-up pass's brick count
     for step in range(args.e2e_steps + 1 if args.e2e_steps > 0 else 0):
         torch.cuda.synchronize()
         barrier(ws)
@@ -581,8 +582,16 @@ def run_ours(args):
         t1 = time.perf_counter()
         mm.infer(iters=iters)
         t2 = time.perf_counter()
-        cen, bel = mm.read_bricks()
+        if out is not None and out[1].shape[0] == mm.num_bricks:
+            cen, bel = mm.read_bricks(out[0], out[1])
+        else:
+            cen, bel = mm.read_bricks()
         t3 = time.perf_counter()
+        if out is None:
+            nb = mm.num_bricks
+            out_t = (torch.empty((nb, 3), dtype=torch.float32).pin_memory(),
+                     torch.empty((nb, 512), dtype=torch.float32).pin_memory())
+            out = (out_t[0].numpy(), out_t[1].numpy())
         est = mm.stats()
         mm.close()
         dt = time.perf_counter() - t0

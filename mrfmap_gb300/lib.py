@@ -404,10 +404,16 @@ class MRFMap:
         _check(self._L.mrf_num_bricks(self._h, C.byref(n)))
         return n.value
 
-    def read_bricks(self):
+    def read_bricks(self, centres=None, beliefs=None):
+        """Brick centres (n, 3) and beliefs (n, 512); pass preallocated
+        float32 arrays (pinned host memory, e.g. numpy views of pinned
+        torch tensors, makes the device-to-host copy run at full speed)."""
         n = self.num_bricks
-        cen = np.zeros((n, 3), np.float32)
-        bel = np.zeros((n, 512), np.float32)
+        cen = np.zeros((n, 3), np.float32) if centres is None else centres
+        bel = np.zeros((n, 512), np.float32) if beliefs is None else beliefs
+        if cen.shape != (n, 3) or bel.shape != (n, 512) or cen.dtype != np.float32 or bel.dtype != np.float32 \
+                or not cen.flags.c_contiguous or not bel.flags.c_contiguous:
+            raise ValueError("read_bricks: outputs must be C-contiguous float32 of shapes (n, 3) and (n, 512)")
         _check(self._L.mrf_read_bricks(self._h, _fp(cen), _fp(bel), n))
         return cen, bel
 
