@@ -463,9 +463,13 @@ __global__ void k_pairs_renumbered(const uint32_t* __restrict__ order, uint32_t 
 
 // build records in pair-grouped (sorted) order: one gather per position
 __global__ void k_gather_rec(const uint32_t* __restrict__ sidx, uint32_t n, uint32_t inc_base,
-                             const float2* __restrict__ rec, float2* __restrict__ out) {
+                             const float2* __restrict__ rec, float2* __restrict__ out,
+                             uint32_t* __restrict__ dflag) {
   uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k < n) out[k] = rec[inc_base + sidx[k]];
+  if (k >= n) return;
+  const float2 r = rec[inc_base + sidx[k]];
+  out[k] = r;
+  dflag[k] = signbit(r.y) ? 1u : 0u;  // a dynamic incidence (the record's class bit)
 }
 
 // Per pair: cumulative length, the sum of its static messages F_EPS * l
@@ -566,11 +570,6 @@ __global__ void __launch_bounds__(kStatThreads)
     if (threadIdx.x == 0) store_sums(p, sc[0], sst[0], sh[0], snd[0], cum, stat, ndyn, hit);
     __syncthreads();
   }
-}
-
-__global__ void k_dyn_flags(const float2* __restrict__ srec, uint32_t n, uint32_t* __restrict__ flag) {
-  uint32_t k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k < n) flag[k] = signbit(srec[k].y) ? 1u : 0u;
 }
 
 __global__ void k_dyn_scatter(const uint32_t* __restrict__ sidx, const uint32_t* __restrict__ flag,
@@ -751,9 +750,9 @@ cudaError_t launch_pairs_renumbered(const uint32_t* order, uint32_t np, const ui
 }
 
 cudaError_t launch_gather_rec(const uint32_t* sidx, uint32_t n, uint32_t inc_base, const float2* rec,
-                              float2* out, cudaStream_t s) {
+                              float2* out, uint32_t* dflag, cudaStream_t s) {
   if (!n) return cudaSuccess;
-  k_gather_rec<<<grid_for(n), kThreads, 0, s>>>(sidx, n, inc_base, rec, out);
+  k_gather_rec<<<grid_for(n), kThreads, 0, s>>>(sidx, n, inc_base, rec, out, dflag);
   return cudaGetLastError();
 }
 
@@ -768,12 +767,6 @@ cudaError_t launch_pair_stats(const uint32_t* seg, uint32_t p0, uint32_t np, uin
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   k_pair_stats_long<<<1024, kStatThreads, 0, s>>>(seg, perm_base, srec, long_list, cum, stat, ndyn, hit);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_dyn_flags(const float2* srec, uint32_t n, uint32_t* flag, cudaStream_t s) {
-  if (!n) return cudaSuccess;
-  k_dyn_flags<<<grid_for(n), kThreads, 0, s>>>(srec, n, flag);
   return cudaGetLastError();
 }
 

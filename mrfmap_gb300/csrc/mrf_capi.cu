@@ -517,14 +517,13 @@ void view_pairs(mrf_map* m, int c, int bits, int64_t& pair_total, int64_t& perm_
     v.n_loud = read1(m, m->s_k1.as<uint32_t>());
     m->s_recs.reserve((size_t)nr * 8, false, m->stream);
     CK(launch_gather_rec(m->s_v1.as<uint32_t>(), nr, v.inc_base, m->s_rec.as<float2>(),
-                         m->s_recs.as<float2>(), m->stream));
+                         m->s_recs.as<float2>(), m->s_k0.as<uint32_t>(), m->stream));
     m->s_pf.reserve((size_t)np * 4 + 4, false, m->stream);
     CK(launch_pair_stats(m->pair_seg.as<uint32_t>(), v.pair_base, np, v.perm_base, m->s_recs.as<float2>(),
                          m->pair_cum.as<float>(), m->pair_stat.as<float>(), m->pair_ndyn.as<uint32_t>(),
                          m->pair_hit.as<float>(), m->s_pf.as<uint32_t>(), m->stream));
     // dynamic incidences in pair-grouped order (a stable compaction of the
     // sorted positions) and the run of each pair that has any
-    CK(launch_dyn_flags(m->s_recs.as<float2>(), nr, m->s_k0.as<uint32_t>(), m->stream));
     CK(cudaMemsetAsync(m->s_k0.as<uint32_t>() + nr, 0, 4, m->stream));
     CK(exclusive_scan_u32(m->s_tmp.p, t1, m->s_k0.as<uint32_t>(), m->s_v0.as<uint32_t>(), nr + 1,
                           m->stream));

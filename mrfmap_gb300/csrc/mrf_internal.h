@@ -133,8 +133,9 @@ cudaError_t launch_pairs_from_sorted(const uint32_t* sk, const uint32_t* sidx, c
                                      uint32_t perm_base, uint32_t inc_base, uint32_t* pair_vox,
                                      uint32_t* seg, uint32_t* inc_pair, cudaStream_t s);
 // build records (post length, -(mu l) on dynamic incidences) in sorted order
+// build records in pair-grouped order, and each position's dynamic flag
 cudaError_t launch_gather_rec(const uint32_t* sidx, uint32_t n, uint32_t inc_base, const float2* rec,
-                              float2* out, cudaStream_t s);
+                              float2* out, uint32_t* dflag, cudaStream_t s);
 // per pair: cumulative length, summed static messages, dynamic incidences,
 // potential mass (from the sorted records)
 // long_list: scratch of 1 + np u32 (count, then the pairs with long runs)
@@ -153,7 +154,6 @@ cudaError_t launch_voxel_features(const uint32_t* vseg, const uint32_t* vpairs, 
                                   const float* belief, int64_t n_slots_vox, float* feat, cudaStream_t s);
 // dynamic incidences of a view in pair-grouped order (dperm) and the pairs
 // that own them (dpair, with their first position dseg)
-cudaError_t launch_dyn_flags(const float2* srec, uint32_t n, uint32_t* flag, cudaStream_t s);
 cudaError_t launch_dyn_scatter(const uint32_t* sidx, const uint32_t* flag, const uint32_t* scan,
                                uint32_t n, uint32_t inc_base, uint32_t dperm_base, uint32_t* dperm,
                                cudaStream_t s);
