@@ -138,6 +138,12 @@ MRF_API int64_t mrf_memory_in_use(void);
  * The next call that checks the flag (an incidence-list build) fails with
  * MRF_ERR_DEVICE and clears it. */
 MRF_API mrf_status mrf_test_raise_device_error(mrf_map* map);
+/* Test hook, no reference counterpart: the pixels of built view view_id
+ * whose rays may cross a brick in slots b0..b1 -- the footprint an appended
+ * build re-checks after bricks were activated -- as mask[rows*cols] (0/1,
+ * host) and *all (1: the footprint covers the whole image). */
+MRF_API mrf_status mrf_test_brick_footprint(mrf_map* map, int view_id, int64_t b0, int64_t b1,
+                                            uint8_t* mask, int* all);
 /* Text of the last error raised on this thread. */
 MRF_API const char* mrf_last_error(void);
 

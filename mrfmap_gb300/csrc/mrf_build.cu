@@ -172,9 +172,12 @@ __global__ void __launch_bounds__(kThreads, 4)
             const uint32_t* __restrict__ pix_off, uint32_t inc_base, RayMeta* __restrict__ meta,
             uint32_t* __restrict__ inc_vox, float* __restrict__ inc_len,
             float* __restrict__ inc_mu, float2* __restrict__ inc_rec,
-            int* __restrict__ err) {
+            int* __restrict__ err, const uint8_t* __restrict__ only, const int* __restrict__ only_all) {
   int pix = blockIdx.x * blockDim.x + threadIdx.x;
   if (pix >= g.rows * g.cols) return;
+  // a checking count pass may be limited to the pixels marked in `only`
+  // (unless *only_all is set)
+  if (only && !*only_all && !only[pix]) return;
   float d = depth[pix];
   int count = 0, n_pre = -1, n_post = -1, r0 = -1, run_start = 0, kmu = -1;
   bool gate = false;
@@ -650,9 +653,65 @@ cudaError_t launch_set_points(const Geom& g, const float* pts, const float* occ,
 }
 
 cudaError_t launch_trace_count(const Geom& g, const Pose& P, const float* depth, uint32_t* counts,
-                               int* err, cudaStream_t s, const RayMeta* check) {
+                               int* err, cudaStream_t s, const RayMeta* check, const uint8_t* only,
+                               const int* only_all) {
   k_trace<false><<<grid_for((int64_t)g.rows * g.cols), kThreads, 0, s>>>(
-      g, P, depth, counts, nullptr, 0, const_cast<RayMeta*>(check), nullptr, nullptr, nullptr, nullptr, err);
+      g, P, depth, counts, nullptr, 0, const_cast<RayMeta*>(check), nullptr, nullptr, nullptr, nullptr, err, only,
+      only_all);
+  return cudaGetLastError();
+}
+
+// The pixels of a view whose rays may cross one of the bricks in slots
+// b0..b1 (bricks activated after the view's lists were built): each brick's
+// eight corners projected through the view's camera (the inverse of
+// ray_setup: a pixel's ray projects onto that pixel), the box of the
+// projections widened by a pixel against rounding, marked in mask.  A brick
+// with a corner at or behind the camera plane, or whose box covers more
+// than a quarter of the image, sets *all instead (every pixel is checked).
+__global__ void k_brick_footprint(Geom g, Pose P, const int* __restrict__ coord, uint32_t b0, uint32_t b1,
+                                  uint8_t* __restrict__ mask, int* __restrict__ all) {
+  const uint32_t b = b0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= b1) return;
+  const float o0 = fa(fd(P.m[3], g.res), g.off[0]);
+  const float o1 = fa(fd(P.m[7], g.res), g.off[1]);
+  const float o2 = fa(fd(P.m[11], g.res), g.off[2]);
+  const float kx = g.fx / g.cx, ky = g.fy / g.cy;
+  float x_lo = 3.0e38f, x_hi = -3.0e38f, y_lo = 3.0e38f, y_hi = -3.0e38f;
+  for (int k = 0; k < 8; ++k) {
+    const float v0 = (float)(kBrick * (coord[3 * b + 0] + (k & 1))) - o0;
+    const float v1 = (float)(kBrick * (coord[3 * b + 1] + ((k >> 1) & 1))) - o1;
+    const float v2 = (float)(kBrick * (coord[3 * b + 2] + ((k >> 2) & 1))) - o2;
+    const float xc = P.m[0] * v0 + P.m[4] * v1 + P.m[8] * v2;
+    const float yc = P.m[1] * v0 + P.m[5] * v1 + P.m[9] * v2;
+    const float zc = P.m[2] * v0 + P.m[6] * v1 + P.m[10] * v2;
+    if (!(zc > 1e-3f)) {
+      atomicExch(all, 1);
+      return;
+    }
+    const float px = (xc / zc * kx + 1.0f) * 0.5f * (float)g.cols - 0.5f;
+    const float py = (yc / zc * ky + 1.0f) * 0.5f * (float)g.rows - 0.5f;
+    x_lo = fminf(x_lo, px);
+    x_hi = fmaxf(x_hi, px);
+    y_lo = fminf(y_lo, py);
+    y_hi = fmaxf(y_hi, py);
+  }
+  const int x0 = max(0, (int)floorf(fmaxf(x_lo, -4.0f)) - 1);
+  const int x1 = min(g.cols - 1, (int)ceilf(fminf(x_hi, (float)g.cols + 4.0f)) + 1);
+  const int y0 = max(0, (int)floorf(fmaxf(y_lo, -4.0f)) - 1);
+  const int y1 = min(g.rows - 1, (int)ceilf(fminf(y_hi, (float)g.rows + 4.0f)) + 1);
+  if (x0 > x1 || y0 > y1) return;
+  if ((int64_t)(x1 - x0 + 1) * (y1 - y0 + 1) * 4 > (int64_t)g.rows * g.cols) {
+    atomicExch(all, 1);
+    return;
+  }
+  for (int y = y0; y <= y1; ++y)
+    for (int x = x0; x <= x1; ++x) mask[y * g.cols + x] = 1;
+}
+
+cudaError_t launch_brick_footprint(const Geom& g, const Pose& P, const int* coord, uint32_t b0, uint32_t b1,
+                                   uint8_t* mask, int* all, cudaStream_t s) {
+  if (b1 <= b0) return cudaSuccess;
+  k_brick_footprint<<<grid_for(b1 - b0), kThreads, 0, s>>>(g, P, coord, b0, b1, mask, all);
   return cudaGetLastError();
 }
 
@@ -661,7 +720,7 @@ cudaError_t launch_trace_emit(const Geom& g, const Pose& P, const float* depth,
                               uint32_t* inc_vox, float* inc_len, float* inc_mu, float2* inc_rec,
                               int* err, cudaStream_t s) {
   k_trace<true><<<grid_for((int64_t)g.rows * g.cols), kThreads, 0, s>>>(
-      g, P, depth, nullptr, pix_off, inc_base, meta, inc_vox, inc_len, inc_mu, inc_rec, err);
+      g, P, depth, nullptr, pix_off, inc_base, meta, inc_vox, inc_len, inc_mu, inc_rec, err, nullptr, nullptr);
   return cudaGetLastError();
 }
 

@@ -1138,15 +1138,25 @@ bool append_lists(mrf_map* m) {
   for (View& v : m->views) v.cam.brick_slot = m->g.brick_slot;
   if (m->n_bricks != m->bricks_at_build) {
     // err[1]: the count pass's mismatch flag (err[0], the kernels' error
-    // flag, is left as it is and checked below)
+    // flag, is left as it is and checked below).  Only the pixels whose
+    // rays may cross a brick activated since the last build are traced
+    // again (their footprint through each view's camera); err[2] tells the
+    // pass to check every pixel of the view.
     CK(cudaMemsetAsync(m->s_err.as<int>() + 1, 0, 4, m->stream));
+    const uint32_t b0 = (uint32_t)std::max<int64_t>(m->bricks_at_build, 0), b1 = (uint32_t)m->n_bricks;
     for (int c = 0; c < m->built_views; ++c) {
       const View& v = m->views[c];
       const int64_t hw = view_pixels(v);
       if (!hw) continue;
       m->s_counts.reserve((size_t)hw * 4 + 4, false, m->stream);
+      m->s_dense.reserve((size_t)hw + 16, false, m->stream);
+      CK(cudaMemsetAsync(m->s_dense.p, 0, (size_t)hw, m->stream));
+      CK(cudaMemsetAsync(m->s_err.as<int>() + 2, 0, 4, m->stream));
+      CK(launch_brick_footprint(v.cam, v.pose, m->d_coord.as<int>(), b0, b1, m->s_dense.as<uint8_t>(),
+                                m->s_err.as<int>() + 2, m->stream));
       CK(launch_trace_count(v.cam, v.pose, v.depth.as<float>(), m->s_counts.as<uint32_t>(), m->s_err.as<int>(),
-                            m->stream, m->meta.as<RayMeta>() + v.pix_base));
+                            m->stream, m->meta.as<RayMeta>() + v.pix_base, m->s_dense.as<uint8_t>(),
+                            m->s_err.as<int>() + 2));
     }
     int flags[2] = {0, 0};
     CK(cudaMemcpyAsync(flags, m->s_err.p, 8, cudaMemcpyDeviceToHost, m->stream));
@@ -1932,6 +1942,27 @@ int64_t mrf_memory_in_use(void) {
   int d = 0;
   if (cudaGetDevice(&d) != cudaSuccess || d < 0 || d >= kMaxDevices) return -1;
   return g_in_use[d].load();
+}
+
+mrf_status mrf_test_brick_footprint(mrf_map* m, int view_id, int64_t b0, int64_t b1, uint8_t* mask, int* all) {
+  if (guard(m) != MRF_OK) return MRF_ERR_INVALID;
+  if (view_id < 0 || view_id >= (int)m->views.size() || !mask || !all || b0 < 0 || b1 < b0 || b1 > m->n_bricks) {
+    set_err("invalid footprint arguments");
+    return MRF_ERR_INVALID;
+  }
+  return wrap([&] {
+    const View& v = m->views[view_id];
+    if (v.retired) fail(MRF_ERR_STATE, "view retired");
+    const int64_t hw = (int64_t)v.cam.rows * v.cam.cols;
+    m->s_dense.reserve((size_t)hw + 16, false, m->stream);
+    CK(cudaMemsetAsync(m->s_dense.p, 0, (size_t)hw, m->stream));
+    CK(cudaMemsetAsync(m->s_err.as<int>() + 2, 0, 4, m->stream));
+    CK(launch_brick_footprint(v.cam, v.pose, m->d_coord.as<int>(), (uint32_t)b0, (uint32_t)b1,
+                              m->s_dense.as<uint8_t>(), m->s_err.as<int>() + 2, m->stream));
+    CK(cudaMemcpyAsync(mask, m->s_dense.p, (size_t)hw, cudaMemcpyDeviceToHost, m->stream));
+    CK(cudaMemcpyAsync(all, m->s_err.as<int>() + 2, 4, cudaMemcpyDeviceToHost, m->stream));
+    sync(m);
+  });
 }
 
 mrf_status mrf_test_raise_device_error(mrf_map* m) {

@@ -91,7 +91,12 @@ cudaError_t launch_set_points(const Geom& g, const float* pts, const float* occ,
 // records) the count pass also sets err[1] when any ray's record would
 // differ from the stored one (err holds two ints).
 cudaError_t launch_trace_count(const Geom& g, const Pose& P, const float* depth, uint32_t* counts,
-                               int* err, cudaStream_t s, const RayMeta* check = nullptr);
+                               int* err, cudaStream_t s, const RayMeta* check = nullptr,
+                               const uint8_t* only = nullptr, const int* only_all = nullptr);
+// pixels of a view whose rays may cross one of the bricks in slots b0..b1
+// (mask[pix] = 1; *all = 1 when every pixel must be checked)
+cudaError_t launch_brick_footprint(const Geom& g, const Pose& P, const int* coord, uint32_t b0, uint32_t b1,
+                                   uint8_t* mask, int* all, cudaStream_t s);
 cudaError_t launch_trace_emit(const Geom& g, const Pose& P, const float* depth,
                               const uint32_t* pix_off, uint32_t inc_base, RayMeta* meta,
                               uint32_t* inc_vox, float* inc_len, float* inc_mu, float2* inc_rec,

@@ -11,6 +11,8 @@ Compared with the FP64 oracle running the same loop (orc_retire_view):
 beliefs within 1e-3 with >= 99.9 % class agreement along the stream, the
 message-update count of the live window, and the total log-odds rebuilt from
 the prior, the retired views' messages and the live ones."""
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -136,3 +138,47 @@ def test_appended_lists_equal_a_full_build(native_lib, walk):
     np.testing.assert_allclose(a.beliefs(), c.beliefs(), rtol=0, atol=1e-6)
     for m in (a, b, c):
         m.close()
+
+
+def test_brick_footprint_covers_every_crossing_ray(native_lib, walk):
+    """After bricks are activated, an appended build re-traces only the
+    pixels of each old view whose rays may cross one of the new bricks (the
+    bricks' projected footprint).  Every pixel whose incidence list holds a
+    voxel of a brick in the range must be in that footprint: checked
+    against the oracle's own lists for every view, over slices of the
+    brick range."""
+    w, depths = walk
+    nv = 4
+    m = L.MRFMap(w.params, activation=L.ACT_FULL_RAY)
+    om = O.OracleMap(w.params, threads=8)
+    for k in range(nv):
+        m.add_view(w.poses[k], depths[k])
+        om.add_view(w.poses[k], depths[k], O.ACT_FULL_RAY)
+    m.infer(iters=1)
+    om.build_all()
+    nb = m.num_bricks
+    assert nb == om.num_bricks
+    lib = L.load()
+    rows, cols = w.params.rows, w.params.cols
+    checked = 0
+    for v in range(nv):
+        tr = om.view_trace(v)
+        pix, off, meta, vox = tr["pix"], tr["off"], tr["meta"], tr["vox"]
+        for b0, b1 in ((0, nb // 3), (nb // 3, 2 * nb // 3), (2 * nb // 3, nb), (nb - 5, nb)):
+            mask = np.zeros(rows * cols, np.uint8)
+            allf = C.c_int(0)
+            assert lib.mrf_test_brick_footprint(m.handle, v, b0, b1,
+                                                mask.ctypes.data_as(C.POINTER(C.c_uint8)), C.byref(allf)) == 0
+            if allf.value:
+                continue
+            for r in range(len(pix)):
+                n = meta[r, 0]
+                if n == 0:
+                    continue
+                bricks = vox[off[r]:off[r] + n] // 512
+                if np.any((bricks >= b0) & (bricks < b1)):
+                    assert mask[pix[r]] == 1, (v, r, b0, b1)
+                    checked += 1
+    assert checked > 0
+    m.close()
+    om.close()
