@@ -521,6 +521,13 @@ def run_ours(args):
     m.infer(iters=iters, flags=L.PROFILE)
     prof_half = m.stats()
     m.set_precision(L.PRECISION_FP32)
+    # the same steps reading every ray's whole Pre range in every iteration
+    # (MRF_FULL_RAYS: no static prefixes from their quiet sums), profiled
+    # once: the ray kernel's roofline on the full path
+    m.reset_state()
+    m.infer(iters=iters, flags=L.FULL_RAYS | L.PROFILE)
+    prof_full = m.stats()
+    ms_full = prof_full["infer_ms"]
     # per-kernel device times of one profiled step (events on the map stream)
     m.reset_state()
     m.infer(iters=iters, flags=L.PROFILE)
@@ -689,6 +696,14 @@ def run_ours(args):
                                "static_messages": "exact constants (p = F_EPS before a ray's first "
                                                   "non-zero potential), summed once per build"},
             "dynamic_updates_per_s": st["n_inc_dyn"] * iters * args.steps / (ms / 1e3),
+            "full_ray_path": {"ms_per_step_profiled": ms_full,
+                              "ray_kernel_ms_per_launch": prof_full["kernel_ms"][1] / max(prof_full["kernel_count"][1], 1),
+                              "ray_kernel_bytes_per_launch": ray_kernel_bytes(prof_full, iters)
+                              / max(prof_full["kernel_count"][1], 1),
+                              "ray_kernel_frac": ray_kernel_bytes(prof_full, iters) / (prof_full["kernel_ms"][1] / 1e3)
+                              / 1e9 / peak,
+                              "note": "one profiled step with MRF_FULL_RAYS (every iteration reads every ray's whole "
+                                      "Pre range); the headline value uses the default choice"},
             "half_streams": {"value": n_upd_step * args.steps / (ms_half / 1e3), "ms_per_step": ms_half / args.steps,
                              "ray_kernel_ms_per_launch": prof_half["kernel_ms"][1] / max(prof_half["kernel_count"][1], 1),
                              "note": "the same steps with fp16 segment lengths and ln q gathers in the ray kernel "
