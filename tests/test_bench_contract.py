@@ -53,3 +53,21 @@ def test_cpu_baselines_of_our_line():
     assert ins["unit"] == "voxel updates/s" and ins["value"] > 0 and ins["rays_per_s"] > 0
     assert "error" not in ins and ins["cores"] == 1
     json.dumps({"cpu_baseline": cpu, "cpu_insertion": ins})
+
+
+def test_ray_kernel_bytes_of_both_paths():
+    """The ray kernel's algorithmic bytes per call: every iteration over the
+    whole Pre ranges on the full path; two such iterations, the quiet sums
+    and the fast iterations (from k4 plus the loud prefix entries) when the
+    call took the fast path."""
+    import bench
+    st = {"n_inc_pre_bp": 1000, "n_inc_from_k4": 200, "n_loud_prefix": 50, "n_inc_dyn": 150,
+          "n_rays_bp": 10, "quiet_prefix_used": 0}
+    full = 12 * 1000 + 8 * 150 + 16 * 10
+    assert bench.ray_kernel_bytes(st, 20) == 20 * full
+    assert bench.ray_kernel_bytes(st, 20, half=True) == 20 * (8 * 1000 + 8 * 150 + 16 * 10)
+    st["quiet_prefix_used"] = 1
+    quiet = 12 * 800 + 16 * 10
+    fast = 12 * 200 + 14 * 50 + 8 * 150 + 36 * 10
+    assert bench.ray_kernel_bytes(st, 20) == 2 * full + quiet + 18 * fast
+    assert bench.ray_kernel_bytes(st, 2) == 2 * full
