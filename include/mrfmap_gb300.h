@@ -152,7 +152,10 @@ MRF_API const char* mrf_last_error(void);
  * activates bricks (src/GVDBCamera.cpp:70-112). */
 MRF_API mrf_status mrf_add_view(mrf_map* map, const float* pose, const float* depth_host,
                         int* view_id);
-/* Same, with the depth image already in device memory. */
+/* Same, with the depth image already in device memory: depth_dev must hold
+ * params.rows x params.cols floats (the map camera's image; the library
+ * cannot check the size of a device buffer).  Views of other sizes go
+ * through mrf_add_view_camera. */
 MRF_API mrf_status mrf_add_view_device(mrf_map* map, const float* pose, const float* depth_dev,
                                int* view_id);
 /* A view with its own pinhole camera (no counterpart in the reference, whose
