@@ -272,6 +272,9 @@ class MRFMap:
         return r.value, c.value, tuple(float(x) for x in k)
 
     def add_view_device(self, pose, depth_dev_ptr: int) -> int:
+        """A view whose depth image is already on the device: depth_dev_ptr
+        must point at params.rows x params.cols floats (the map camera's
+        image); views of other sizes go through add_view_camera."""
         vid = C.c_int()
         _check(self._L.mrf_add_view_device(self._h, _fp(_f32(pose)), C.c_void_p(depth_dev_ptr),
                                            C.byref(vid)))
