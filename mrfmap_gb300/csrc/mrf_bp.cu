@@ -1122,6 +1122,35 @@ __global__ void k_sum_u32(const uint32_t* __restrict__ v, int64_t n, unsigned lo
   if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
 }
 
+// the per-view counters of a view's ray records, kRayCounters 64-bit totals:
+// Pre incidences, rays with any, Post incidences, dynamic Post incidences
+// (those from k_dyn on), rays in BP, their Pre incidences, and their Pre
+// incidences from the quiet-prefix boundary (k_dyn rounded down to 4) on.
+// Integer sums: the totals do not depend on the order of the atomics.
+__global__ void k_ray_counters(const RayMeta* __restrict__ meta, int64_t n, unsigned long long* __restrict__ out) {
+  unsigned long long c[kRayCounters] = {};
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const RayMeta r = meta[i];
+    const int kd = ray_kdyn(r);
+    c[0] += r.n_pre;
+    c[1] += r.n_pre > 0;
+    c[2] += r.n_post;
+    c[3] += (unsigned)(r.n_post - min(kd, (int)r.n_post));
+    if (ray_in_bp(r)) {
+      c[4] += 1;
+      c[5] += r.n_pre;
+      c[6] += (unsigned long long)(long long)((int)r.n_pre - (kd & ~3));  // two's complement: a signed total
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < kRayCounters; ++k) {
+    unsigned long long v = c[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+    if ((threadIdx.x & 31) == 0 && v) atomicAdd(out + k, v);
+  }
+}
+
 __global__ void k_count_flags(const uint8_t* __restrict__ flag, int64_t n, unsigned long long* __restrict__ out) {
   unsigned c = 0;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -1446,6 +1475,13 @@ cudaError_t launch_sum_u32(const uint32_t* v, int64_t n, unsigned long long* out
   cudaError_t e = cudaMemsetAsync(out, 0, 8, s);
   if (e != cudaSuccess || n <= 0) return e;
   k_sum_u32<<<(unsigned)std::min<int64_t>(blocks(n, 256), 4096), 256, 0, s>>>(v, n, out);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_ray_counters(const RayMeta* meta, int64_t n, unsigned long long* out, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(out, 0, kRayCounters * sizeof(unsigned long long), s);
+  if (e != cudaSuccess || n <= 0) return e;
+  k_ray_counters<<<(unsigned)std::min<int64_t>(blocks(n, 256), 1024), 256, 0, s>>>(meta, n, out);
   return cudaGetLastError();
 }
 

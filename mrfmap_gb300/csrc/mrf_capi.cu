@@ -228,7 +228,7 @@ struct mrf_map {
   int jacobi_version = -1;
   // scratch
   DBuf s_rec, s_recs, s_pf, s_ps, s_flags, s_ind, s_scan, s_tmp, s_counts, s_offs, s_vox, s_k0, s_k1, s_v0, s_v1,
-      s_seg, s_dense, s_err, s_depth_in, s_depth, s_img, s_part, s_sum, s_prev, s_delta, s_snap;
+      s_seg, s_dense, s_err, s_depth_in, s_depth, s_img, s_part, s_sum, s_prev, s_delta, s_snap, s_vcnt;
   mrf_stats stats{};
   // MRF_PROFILE event pool
   std::vector<cudaEvent_t> prof_ev;
@@ -393,21 +393,36 @@ void rebuild(mrf_map* m) {
 
 // ---- per-view pieces of a build ------------------------------------------
 
-// counters of one view's rays (from its ray records on the host)
-void view_counters(View& v, const RayMeta* vm) {
-  v.c_npre = v.c_nrays = v.c_npost = v.c_ndyn = v.c_nrays_bp = v.c_npre_bp = v.c_nfast_bp = 0;
-  const int64_t hw = view_pixels(v);
-  for (int64_t i = 0; i < hw; ++i) {
-    const RayMeta& r = vm[i];
-    v.c_npre += r.n_pre;
-    v.c_nrays += r.n_pre > 0;
-    v.c_npost += r.n_post;
-    v.c_ndyn += r.n_post - std::min<int>(ray_kdyn(r), r.n_post);
-    if (ray_in_bp(r)) {
-      ++v.c_nrays_bp;
-      v.c_npre_bp += r.n_pre;
-      v.c_nfast_bp += r.n_pre - (ray_kdyn(r) & ~3);
-    }
+// The counters of the given views' rays, summed on the device from their ray
+// records (k_ray_counters), and the records of pixels [hm_base, hm_base +
+// hm.size()) copied to the host for the region lists: one synchronisation.
+void ray_records_and_counters(mrf_map* m, const std::vector<int>& views, int64_t hm_base,
+                              std::vector<RayMeta>& hm) {
+  const size_t K = (size_t)kRayCounters;
+  m->s_vcnt.reserve(std::max<size_t>(views.size(), 1) * K * 8, false, m->stream);
+  unsigned long long* dc = m->s_vcnt.as<unsigned long long>();
+  for (size_t k = 0; k < views.size(); ++k) {
+    const View& v = m->views[(size_t)views[k]];
+    CK(launch_ray_counters(m->meta.as<RayMeta>() + v.pix_base, view_pixels(v), dc + k * K, m->stream));
+  }
+  std::vector<unsigned long long> hc(views.size() * K, 0ull);
+  if (!hc.empty())
+    CK(cudaMemcpyAsync(hc.data(), dc, hc.size() * 8, cudaMemcpyDeviceToHost, m->stream));
+  if (!hm.empty())
+    CK(cudaMemcpyAsync(hm.data(), m->meta.as<RayMeta>() + hm_base, hm.size() * sizeof(RayMeta),
+                       cudaMemcpyDeviceToHost, m->stream));
+  sync(m);
+  check_device_err(m);
+  for (size_t k = 0; k < views.size(); ++k) {
+    View& v = m->views[(size_t)views[k]];
+    const unsigned long long* c = hc.data() + k * K;
+    v.c_npre = (int64_t)c[0];
+    v.c_nrays = (int64_t)c[1];
+    v.c_npost = (int64_t)c[2];
+    v.c_ndyn = (int64_t)c[3];
+    v.c_nrays_bp = (int64_t)c[4];
+    v.c_npre_bp = (int64_t)c[5];
+    v.c_nfast_bp = (int64_t)c[6];
   }
 }
 
@@ -660,23 +675,30 @@ uint32_t region_blocks(mrf_map* m, const std::vector<int>& views, const std::vec
   m->lbase.reserve((size_t)V * 4 + 4, true, m->stream);
   m->lsingle.reserve((size_t)V * 8 + 8, true, m->stream);
   std::vector<uint32_t> pix;
-  for (int c : views) {
+  // each view's row of region starts, leftover base and leftover counter
+  // pair, staged on the host until the synchronisation below
+  const size_t nv = views.size();
+  std::vector<uint32_t> rows(nv * ((size_t)R + 1)), lbs(nv), lss(2 * nv);
+  for (size_t k = 0; k < nv; ++k) {
+    const int c = views[k];
     View& v = m->views[c];
     const RegionLists& l = lists[(size_t)c];
-    std::vector<uint32_t> row((size_t)R + 1);
+    uint32_t* row = rows.data() + k * ((size_t)R + 1);
     const uint32_t b = at + (uint32_t)pix.size();
-    for (int r = 0; r < R; ++r) row[(size_t)r] = b + (r < (int)l.starts.size() ? l.starts[(size_t)r] : 0u);
-    row[(size_t)R] = b + (uint32_t)l.home.size();
+    for (int r = 0; r < R; ++r) row[r] = b + (r < (int)l.starts.size() ? l.starts[(size_t)r] : 0u);
+    row[R] = b + (uint32_t)l.home.size();
     v.left_base = b + (uint32_t)l.home.size();
     v.n_left = (uint32_t)l.left.size();
     pix.insert(pix.end(), l.home.begin(), l.home.end());
     pix.insert(pix.end(), l.left.begin(), l.left.end());
-    const uint32_t ls[2] = {0u, v.n_left};
-    CK(cudaMemcpyAsync(m->rstart.as<uint32_t>() + (size_t)c * (R + 1), row.data(), (size_t)(R + 1) * 4,
+    lbs[k] = v.left_base;
+    lss[2 * k] = 0u;
+    lss[2 * k + 1] = v.n_left;
+    CK(cudaMemcpyAsync(m->rstart.as<uint32_t>() + (size_t)c * (R + 1), row, (size_t)(R + 1) * 4,
                        cudaMemcpyHostToDevice, m->stream));
-    CK(cudaMemcpyAsync(m->lbase.as<uint32_t>() + c, &v.left_base, 4, cudaMemcpyHostToDevice, m->stream));
-    CK(cudaMemcpyAsync(m->lsingle.as<uint32_t>() + 2 * (size_t)c, ls, 8, cudaMemcpyHostToDevice, m->stream));
-    sync(m);  // row and ls are host temporaries
+    CK(cudaMemcpyAsync(m->lbase.as<uint32_t>() + c, &lbs[k], 4, cudaMemcpyHostToDevice, m->stream));
+    CK(cudaMemcpyAsync(m->lsingle.as<uint32_t>() + 2 * (size_t)c, &lss[2 * k], 8, cudaMemcpyHostToDevice,
+                       m->stream));
   }
   const uint32_t end = at + (uint32_t)pix.size();
   m->region_q.reserve(std::max<size_t>(end, 1) * sizeof(RayMeta), true, m->stream);
@@ -686,8 +708,8 @@ uint32_t region_blocks(mrf_map* m, const std::vector<int>& views, const std::vec
     CK(cudaMemcpyAsync(m->ray_order.p, pix.data(), pix.size() * 4, cudaMemcpyHostToDevice, m->stream));
     CK(launch_ray_queue(m->meta.as<RayMeta>(), m->ray_order.as<uint32_t>(), (uint32_t)pix.size(),
                         m->region_q.as<RayMeta>() + at, m->region_ids.as<uint32_t>() + at, 0u, m->stream));
-    sync(m);  // the host vector goes out of scope
   }
+  sync(m);  // the host staging vectors go out of scope
   return end;
 }
 
@@ -729,11 +751,10 @@ void rebuild_regions(mrf_map* m) {
 
 // view c's active rays longest first (17-bit key radix sort on the GPU),
 // their records copied into queue order at ray_queue + v.order_base
-void view_ray_queue(mrf_map* m, int c, const RayMeta* vm) {
+void view_ray_queue(mrf_map* m, int c) {
   View& v = m->views[c];
   const int64_t hw = view_pixels(v);
-  int64_t act = 0;
-  for (int64_t i = 0; i < hw; ++i) act += ray_in_bp(vm[i]);
+  const int64_t act = hw ? v.c_nrays_bp : 0;  // the rays in BP (ray_in_bp)
   v.n_active = (uint32_t)act;
   if (hw == 0) return;
   m->s_k0.reserve((size_t)hw * 4 + 4, false, m->stream);
@@ -974,13 +995,11 @@ void rebuild_lists(mrf_map* m, OldPairs& old) {
   for (size_t k = 0; k < live.size(); ++k) emit_view(m, live[k], m->s_offs.as<uint32_t>() + coff[k]);
   // per-view counters from the ray records
   std::vector<RayMeta> hm((size_t)npix);
-  if (npix) {
-    CK(cudaMemcpyAsync(hm.data(), m->meta.p, (size_t)npix * sizeof(RayMeta), cudaMemcpyDeviceToHost,
-                       m->stream));
-    sync(m);
-    check_device_err(m);
+  {
+    std::vector<int> all_views((size_t)V);
+    for (int c = 0; c < V; ++c) all_views[(size_t)c] = c;
+    ray_records_and_counters(m, all_views, 0, hm);
   }
-  for (View& v : m->views) view_counters(v, hm.data() + v.pix_base);
   // voxels with a dynamic incidence in any view ("loud"; the others are
   // quiet, see enqueue_iteration)
   m->s_loud.reserve((size_t)std::max<int64_t>(m->n_bricks * kBrickVox, 1), false, m->stream);
@@ -1018,7 +1037,7 @@ void rebuild_lists(mrf_map* m, OldPairs& old) {
     for (int c = 0; c < V; ++c) {
       View& v = m->views[c];
       v.order_base = (uint32_t)base;
-      view_ray_queue(m, c, hm.data() + v.pix_base);
+      view_ray_queue(m, c);
       base += v.n_active;
     }
     m->queue_end = base;
@@ -1203,17 +1222,27 @@ bool append_lists(mrf_map* m) {
     m->s_rec.reserve(ib * 2, false, m->stream);
   }
   for (size_t k = 0; k < added.size(); ++k) emit_view(m, added[k], m->s_offs.as<uint32_t>() + coff[k]);
-  std::vector<RayMeta> hm;
-  // the new views' ray records on the host
+  // the new views' ray records on the host, and their counters
   const int64_t hw_new = npix - m->npix_total;
-  hm.resize((size_t)std::max<int64_t>(hw_new, 0));
-  if (hw_new > 0) {
-    CK(cudaMemcpyAsync(hm.data(), m->meta.as<RayMeta>() + m->npix_total, (size_t)hw_new * sizeof(RayMeta),
-                       cudaMemcpyDeviceToHost, m->stream));
-    sync(m);
-    check_device_err(m);
-  }
-  for (int c : added) view_counters(m->views[c], hm.data() + (m->views[c].pix_base - m->npix_total));
+  std::vector<RayMeta> hm((size_t)std::max<int64_t>(hw_new, 0));
+  ray_records_and_counters(m, added, m->npix_total, hm);
+  // the new views' region lists: host work on their ray records, on host
+  // threads while the GPU builds their pairs
+  std::vector<RegionLists> lists((size_t)V);
+  bool lists_failed = false;
+  std::thread lists_thread([&] {
+    try {
+      region_lists_parallel(m, added, hm, m->npix_total, lists);
+    } catch (...) {
+      lists_failed = true;
+    }
+  });
+  struct Joiner {
+    std::thread& t;
+    ~Joiner() {
+      if (t.joinable()) t.join();
+    }
+  } joiner{lists_thread};
   // loud voxels of every live view: the old views' from their pairs, the
   // new ones' from the voxel ids of the emit pass
   const int64_t nvox = m->n_bricks * kBrickVox;
@@ -1255,15 +1284,15 @@ bool append_lists(mrf_map* m) {
     for (int c = m->built_views; c < V; ++c) {
       View& v = m->views[c];
       v.order_base = (uint32_t)base;
-      view_ray_queue(m, c, hm.data() + (v.pix_base - m->npix_total));
+      view_ray_queue(m, c);
       base += v.n_active;
     }
     m->queue_end = base;
     const int R = std::max(1, m->num_sms);
     m->counters.reserve((size_t)(V + 1) * 4, false, m->stream);
     m->rcounters.reserve(((size_t)2 * V * R + 2 * (size_t)V + 2) * 4, false, m->stream);
-    std::vector<RegionLists> lists((size_t)V);
-    region_lists_parallel(m, added, hm, m->npix_total, lists);
+    lists_thread.join();
+    if (lists_failed) fail(MRF_ERR_OOM, "host memory for the region queues");
     std::vector<int> newv;
     for (int c = m->built_views; c < V; ++c) {
       if (m->views[c].retired) {
@@ -1782,7 +1811,7 @@ void destroy_bufs(mrf_map* m) {
                  &m->s_q0, &m->s_q1, &m->s_q2, &m->s_q3, &m->s_bf, &m->s_loud, &m->s_pv, &m->s_sg,
                  &m->s_tmp, &m->s_counts, &m->s_offs, &m->s_vox, &m->s_k0, &m->s_k1, &m->s_v0,
                  &m->s_v1, &m->s_seg, &m->s_dense, &m->s_err, &m->s_depth_in, &m->s_depth,
-                 &m->s_img, &m->s_part, &m->s_sum, &m->s_prev, &m->s_delta, &m->s_snap};
+                 &m->s_img, &m->s_part, &m->s_sum, &m->s_prev, &m->s_delta, &m->s_snap, &m->s_vcnt};
   for (DBuf* b : all) b->release();
   for (auto& v : m->views) v.depth.release();
 }

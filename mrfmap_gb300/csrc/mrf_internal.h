@@ -321,6 +321,10 @@ cudaError_t launch_max_abs_diff(const float* a, const float* b, int64_t n, uint3
 cudaError_t launch_fill_u32(uint32_t* p, int64_t n, uint32_t v, cudaStream_t s);
 // *out = sum of n u32 values, in 64 bits
 cudaError_t launch_sum_u32(const uint32_t* v, int64_t n, unsigned long long* out, cudaStream_t s);
+// per-view ray-record counters (k_ray_counters): out[0..kRayCounters) zeroed
+// on the stream, then summed over meta[0..n)
+constexpr int kRayCounters = 7;
+cudaError_t launch_ray_counters(const RayMeta* meta, int64_t n, unsigned long long* out, cudaStream_t s);
 // out2[0] = pairs past the length gate, out2[1] = distinct voxels they
 // reach (flag: nvox bytes of scratch)
 cudaError_t launch_touch_counts(const uint32_t* pair_vox, const float* cum, uint32_t np, uint8_t* flag,
