@@ -114,6 +114,9 @@ typedef struct mrf_stats {
                               first call of 4 or more iterations counts them) */
   int64_t quiet_prefix_used; /* 1 if the last mrf_infer took the static
                                 prefixes from their quiet sums */
+  int64_t builds_oom_fallback; /* full builds run because appending the new
+                                  views' lists ran out of device memory (the
+                                  full build drops the retired views' lists) */
 } mrf_stats;
 
 /* Map construction: GVDBInference(...) + GVDBMRFMap::gpuAllocate
@@ -144,6 +147,13 @@ MRF_API mrf_status mrf_test_raise_device_error(mrf_map* map);
  * host) and *all (1: the footprint covers the whole image). */
 MRF_API mrf_status mrf_test_brick_footprint(mrf_map* map, int view_id, int64_t b0, int64_t b1,
                                             uint8_t* mask, int* all);
+/* Test hook, no reference counterpart: the next build that appends new
+ * views' lists fails with `status` once their pairs are built (a host-side
+ * stand-in for a failing allocation or CUDA call part-way through).  An
+ * MRF_ERR_OOM failure makes that build a full one (stats
+ * builds_oom_fallback); any other fails the call, and the next build is a
+ * full one. */
+MRF_API mrf_status mrf_test_fail_next_append(mrf_map* map, mrf_status status);
 /* Text of the last error raised on this thread. */
 MRF_API const char* mrf_last_error(void);
 

@@ -199,6 +199,9 @@ struct mrf_map {
   // without a full build (the all-view structures of Jacobi are stale);
   // needs_full: the next build must rebuild every view
   bool holes = false, appended = false, needs_full = true;
+  // test hook: the next append fails with this status once its pairs are
+  // built (0: none)
+  int test_append_fail = 0;
   int64_t dead_inc = 0;
   bool has_messages = false;
   std::vector<View> views;
@@ -1274,6 +1277,11 @@ bool append_lists(mrf_map* m) {
           dpair_total = m->n_dpairs;
   const int64_t pair0 = pair_total, dpair0 = dpair_total;
   for (int c : added) view_pairs(m, c, bits, pair_total, perm_total, dperm_total, dpair_total);
+  if (m->test_append_fail) {
+    const mrf_status st = (mrf_status)m->test_append_fail;
+    m->test_append_fail = 0;
+    fail(st, "append of the new views' lists: injected failure (mrf_test_fail_next_append)");
+  }
   // 5. ray queues and region blocks of the new views
   {
     int64_t base = 0;
@@ -1415,17 +1423,38 @@ void ensure_compact(mrf_map* m) {
   ensure_built(m);
 }
 
+// Retired views' lists stay in the arenas until they reach kDeadRatio times
+// the live ones; the next build is then a full one, which drops them.  Only
+// memory grows with them: no per-frame pass reads a retired view's data.
+constexpr int64_t kDeadRatio = 4;
+
 void ensure_built(mrf_map* m) {
   if (m->built_version != m->version) {
     const bool can_append = !m->needs_full && m->built_version >= 0 &&
                             m->prm.activation == MRF_ACT_FULL_RAY && m->built_views <= (int)m->views.size() &&
-                            m->dead_inc * 3 <= m->n_inc * 2;  // retired lists at most twice the live ones
+                            m->dead_inc * (kDeadRatio + 1) <= m->n_inc * kDeadRatio;
     bool done = false;
     if (can_append) {
+      // a part-done append: the next build starts over, and the views it
+      // was adding carry no pairs (their message range was never written)
+      // into that build's message remap
+      auto abandon = [&] {
+        m->needs_full = true;
+        for (size_t c = (size_t)std::max(m->built_views, 0); c < m->views.size(); ++c) {
+          m->views[c].pair_base = 0;
+          m->views[c].n_pairs = 0;
+        }
+      };
       try {
         done = append_lists(m);
+      } catch (const Fail& e) {
+        abandon();
+        // out of memory: the retired views' lists fill it, and the full
+        // build below drops them and reuses the buffers
+        if (e.st != MRF_ERR_OOM) throw;
+        ++m->stats.builds_oom_fallback;
       } catch (...) {
-        m->needs_full = true;  // a part-done append: the next build starts over
+        abandon();
         throw;
       }
       if (done) {
@@ -2001,6 +2030,16 @@ mrf_status mrf_test_raise_device_error(mrf_map* m) {
     CK(cudaMemcpyAsync(m->s_err.p, &one, sizeof(int), cudaMemcpyHostToDevice, m->stream));
     sync(m);
   });
+}
+
+mrf_status mrf_test_fail_next_append(mrf_map* m, mrf_status status) {
+  if (guard(m) != MRF_OK) return MRF_ERR_INVALID;
+  if (status == MRF_OK) {
+    set_err("mrf_test_fail_next_append: a failure status is needed");
+    return MRF_ERR_INVALID;
+  }
+  m->test_append_fail = (int)status;
+  return MRF_OK;
 }
 
 static mrf_status add_view_impl(mrf_map* m, const float* pose, const float* depth, bool device,

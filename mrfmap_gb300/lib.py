@@ -47,7 +47,7 @@ EXPORTS = ["mrf_create", "mrf_destroy", "mrf_release_cached_memory", "mrf_last_e
            "mrf_view_camera", "mrf_set_memory_limit", "mrf_memory_in_use", "mrf_test_raise_device_error",
            "mrf_infer_until", "mrf_retire_view", "mrf_add_view_box", "mrf_autotune_flags",
            "mrf_set_precision", "mrf_set_home_share", "mrf_autotune_home_share", "mrf_get_tuning",
-           "mrf_set_pair_variant", "mrf_test_brick_footprint"]
+           "mrf_set_pair_variant", "mrf_test_brick_footprint", "mrf_test_fail_next_append"]
 
 RENDER_EXPECTED_DEPTH = 0
 RENDER_ACCURACY = 1
@@ -85,7 +85,8 @@ class mrf_stats(C.Structure):
                                                                 ("builds_appended", C.c_int64),
                                                                 ("n_inc_from_k4", C.c_int64),
                                                                 ("n_loud_prefix", C.c_int64),
-                                                                ("quiet_prefix_used", C.c_int64)]
+                                                                ("quiet_prefix_used", C.c_int64),
+                                                                ("builds_oom_fallback", C.c_int64)]
 
 
 _lib = None
@@ -164,6 +165,7 @@ def load(path: str | None = None):
                             C.c_int),
         "mrf_memory_in_use": ([], C.c_int64),
         "mrf_test_raise_device_error": ([vp], C.c_int),
+        "mrf_test_fail_next_append": ([vp, C.c_int], C.c_int),
         "mrf_test_brick_footprint": ([vp, C.c_int, C.c_int64, C.c_int64, C.POINTER(C.c_uint8), ip], C.c_int),
     }
     for name, (args, res) in sig.items():

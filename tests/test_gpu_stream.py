@@ -182,3 +182,80 @@ def test_brick_footprint_covers_every_crossing_ray(native_lib, walk):
     assert checked > 0
     m.close()
     om.close()
+
+
+def test_failed_append_falls_back_to_a_full_build(native_lib, oracle_lib, walk):
+    """A build that appends a new view's lists and fails part-way (injected
+    on the host, mrf_test_fail_next_append, once the new view's pairs are
+    built): out of device memory, the same call makes a full build instead
+    (which drops the retired views' lists); any other failure fails the call
+    and the next call's build is a full one.  The messages carried into the
+    full build are the built views' only, so both streams go on to the
+    oracle's beliefs, identical to each other and within 1e-4 of a stream
+    that appended throughout (a full and an appended build round the static
+    prefixes' sums differently)."""
+    w, depths = walk
+    lib = L.load()
+    n = 14
+    # the frames whose build appends (a build is a full one when new bricks
+    # change an older view's rays): the same stream, run once beforehand
+    # (the stats are read after each frame's infer only: reading them builds
+    # the lists of views added since the last build)
+    probe = L.MRFMap(w.params, activation=L.ACT_FULL_RAY)
+    appends, count = [], 0
+    for k in range(n):
+        probe.add_view(w.poses[k], depths[k])
+        if k >= WINDOW:
+            probe.retire_view(k - WINDOW)
+        probe.infer(iters=ITERS, flags=L.INCREMENTAL)
+        if probe.stats()["builds_appended"] > count:
+            appends.append(k)
+        count = probe.stats()["builds_appended"]
+    probe.close()
+    later = [k for k in appends if k > WINDOW]  # with retired views' lists in the arenas
+    assert later, f"no appended build after frame {WINDOW}: {appends}"
+    fail_at = later[0]
+    om = O.OracleMap(w.params, threads=8)
+    maps = {name: L.MRFMap(w.params, activation=L.ACT_FULL_RAY) for name in ("plain", "oom", "cuda")}
+    last = {}
+    for k in range(n):
+        om.add_view(w.poses[k], depths[k], O.ACT_FULL_RAY)
+        for m in maps.values():
+            m.add_view(w.poses[k], depths[k])
+        if k >= WINDOW:
+            om.retire_view(k - WINDOW)
+            for m in maps.values():
+                m.retire_view(k - WINDOW)
+        om.infer(iters=ITERS, flags=O.INCREMENTAL)
+        if k == fail_at:
+            before = last
+            assert lib.mrf_test_fail_next_append(maps["oom"].handle, 3) == 0   # MRF_ERR_OOM
+            assert lib.mrf_test_fail_next_append(maps["cuda"].handle, 2) == 0  # MRF_ERR_CUDA
+            maps["oom"].infer(iters=ITERS, flags=L.INCREMENTAL)
+            st = maps["oom"].stats()
+            assert st["builds_oom_fallback"] == 1
+            assert st["builds_full"] == before["oom"]["builds_full"] + 1
+            with pytest.raises(L.MrfError, match="MRF_ERR_CUDA"):
+                maps["cuda"].infer(iters=ITERS, flags=L.INCREMENTAL)
+            maps["cuda"].infer(iters=ITERS, flags=L.INCREMENTAL)
+            st = maps["cuda"].stats()
+            assert st["builds_oom_fallback"] == 0
+            assert st["builds_full"] == before["cuda"]["builds_full"] + 1
+            maps["plain"].infer(iters=ITERS, flags=L.INCREMENTAL)
+        else:
+            for m in maps.values():
+                m.infer(iters=ITERS, flags=L.INCREMENTAL)
+        last = {name: m.stats() for name, m in maps.items()}
+        if k in (fail_at, n - 1):
+            ob = om.beliefs()
+            bel = {name: m.beliefs() for name, m in maps.items()}
+            for name, gb in bel.items():
+                emax, agree = _compare(gb, ob)
+                assert emax <= 1e-3, f"{name}, frame {k}: max belief error {emax}"
+                assert agree >= 0.999, f"{name}, frame {k}: class agreement {agree}"
+            np.testing.assert_array_equal(bel["oom"], bel["cuda"])
+            np.testing.assert_allclose(bel["oom"], bel["plain"], rtol=0, atol=1e-4)
+    assert maps["plain"].stats()["builds_oom_fallback"] == 0
+    for m in maps.values():
+        m.close()
+    om.close()
