@@ -399,13 +399,14 @@ __global__ void k_brick_keys(const uint32_t* __restrict__ order, uint32_t np,
 }
 
 // loud[v] = 1 for every voxel with a dynamic incidence (any view): one
-// thread per ray walks its dynamic range [k_dyn, n_post)
+// thread per ray walks its dynamic range [k_dyn, n_post); vox[k] holds the
+// voxel of incidence vox_base + k
 __global__ void k_loud_voxels(const RayMeta* __restrict__ meta, int64_t npix, const uint32_t* __restrict__ vox,
-                              uint8_t* __restrict__ loud) {
+                              uint32_t vox_base, uint8_t* __restrict__ loud) {
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= npix) return;
   const RayMeta me = meta[r];
-  for (int i = ray_kdyn(me); i < me.n_post; ++i) loud[vox[me.off + i]] = 1;
+  for (int i = ray_kdyn(me); i < me.n_post; ++i) loud[vox[me.off - vox_base + i]] = 1;
 }
 
 __global__ void k_loud_voxels_from_pairs(const RayMeta* __restrict__ meta, int64_t npix,
@@ -762,10 +763,10 @@ cudaError_t launch_brick_keys(const uint32_t* order, uint32_t np, const uint32_t
   return cudaGetLastError();
 }
 
-cudaError_t launch_loud_voxels(const RayMeta* meta, int64_t npix, const uint32_t* vox, uint8_t* loud,
-                               cudaStream_t s) {
+cudaError_t launch_loud_voxels(const RayMeta* meta, int64_t npix, const uint32_t* vox, uint32_t vox_base,
+                               uint8_t* loud, cudaStream_t s) {
   if (npix <= 0) return cudaSuccess;
-  k_loud_voxels<<<grid_for(npix), kThreads, 0, s>>>(meta, npix, vox, loud);
+  k_loud_voxels<<<grid_for(npix), kThreads, 0, s>>>(meta, npix, vox, vox_base, loud);
   return cudaGetLastError();
 }
 

@@ -202,6 +202,10 @@ struct mrf_map {
   // test hook: the next append fails with this status once its pairs are
   // built (0: none)
   int test_append_fail = 0;
+  // the build scratch s_vox / s_rec holds the incidences from this index on
+  // (0 in a full build; an appended build's first new incidence, so the
+  // scratch holds the new views only, not the arenas' retired lists)
+  uint32_t scratch_base = 0;
   int64_t dead_inc = 0;
   bool has_messages = false;
   std::vector<View> views;
@@ -459,7 +463,7 @@ void view_pairs(mrf_map* m, int c, int bits, int64_t& pair_total, int64_t& perm_
     size_t t2 = sort_temp_bytes(n, bits);
     m->s_tmp.reserve(t2, false, m->stream);
     // padding incidences carry kNoVoxel, whose low bits exceed every voxel id
-    CK(sort_pairs_u32(m->s_tmp.p, t2, m->s_vox.as<uint32_t>() + v.inc_base, m->s_k1.as<uint32_t>(),
+    CK(sort_pairs_u32(m->s_tmp.p, t2, m->s_vox.as<uint32_t>() + (v.inc_base - m->scratch_base), m->s_k1.as<uint32_t>(),
                       m->s_v0.as<uint32_t>(), m->s_v1.as<uint32_t>(), n, bits, m->stream));
     size_t t1 = scan_temp_bytes(nr + 1);
     m->s_tmp.reserve(t1, false, m->stream);
@@ -534,7 +538,7 @@ void view_pairs(mrf_map* m, int c, int bits, int64_t& pair_total, int64_t& perm_
                          m->s_k1.as<uint32_t>(), m->stream));
     v.n_loud = read1(m, m->s_k1.as<uint32_t>());
     m->s_recs.reserve((size_t)nr * 8, false, m->stream);
-    CK(launch_gather_rec(m->s_v1.as<uint32_t>(), nr, v.inc_base, m->s_rec.as<float2>(),
+    CK(launch_gather_rec(m->s_v1.as<uint32_t>(), nr, v.inc_base - m->scratch_base, m->s_rec.as<float2>(),
                          m->s_recs.as<float2>(), m->s_k0.as<uint32_t>(), m->stream));
     m->s_pf.reserve((size_t)np * 4 + 4, false, m->stream);
     CK(launch_pair_stats(m->pair_seg.as<uint32_t>(), v.pair_base, np, v.perm_base, m->s_recs.as<float2>(),
@@ -852,9 +856,9 @@ std::vector<uint32_t> count_views(mrf_map* m, const std::vector<int>& views, int
 void emit_view(mrf_map* m, int c, const uint32_t* pix_off) {
   View& v = m->views[c];
   CK(launch_trace_emit(v.cam, v.pose, v.depth.as<float>(), pix_off, v.inc_base,
-                       m->meta.as<RayMeta>() + v.pix_base, m->s_vox.as<uint32_t>() + v.inc_base,
+                       m->meta.as<RayMeta>() + v.pix_base, m->s_vox.as<uint32_t>() + (v.inc_base - m->scratch_base),
                        m->inc_len.as<float>() + v.inc_base, m->inc_mu.as<float>() + v.inc_base,
-                       m->s_rec.as<float2>() + v.inc_base, m->s_err.as<int>(), m->stream));
+                       m->s_rec.as<float2>() + (v.inc_base - m->scratch_base), m->s_err.as<int>(), m->stream));
 }
 
 // tiles of view c's pair update, from position tb of tile_first
@@ -993,6 +997,7 @@ void rebuild_lists(mrf_map* m, OldPairs& old) {
     m->inc_pl.reserve(ib, false, m->stream);
     m->s_vox.reserve(ib, false, m->stream);
     m->s_rec.reserve(ib * 2, false, m->stream);
+    m->scratch_base = 0;
   }
   // 3. emit
   for (size_t k = 0; k < live.size(); ++k) emit_view(m, live[k], m->s_offs.as<uint32_t>() + coff[k]);
@@ -1007,7 +1012,7 @@ void rebuild_lists(mrf_map* m, OldPairs& old) {
   // quiet, see enqueue_iteration)
   m->s_loud.reserve((size_t)std::max<int64_t>(m->n_bricks * kBrickVox, 1), false, m->stream);
   CK(cudaMemsetAsync(m->s_loud.p, 0, (size_t)std::max<int64_t>(m->n_bricks * kBrickVox, 1), m->stream));
-  CK(launch_loud_voxels(m->meta.as<RayMeta>(), npix, m->s_vox.as<uint32_t>(), m->s_loud.as<uint8_t>(),
+  CK(launch_loud_voxels(m->meta.as<RayMeta>(), npix, m->s_vox.as<uint32_t>(), 0u, m->s_loud.as<uint8_t>(),
                         m->stream));
   // the region lists of the SM-affine schedule are host work on the ray
   // records alone: built on host threads while the GPU builds the pairs
@@ -1220,9 +1225,12 @@ bool append_lists(mrf_map* m) {
     m->inc_pair.reserve(ib, true, m->stream);
     m->inc_pl.reserve(ib, true, m->stream);
     m->dperm.reserve((size_t)(m->n_dperm + (n_inc - m->n_inc)) * 4 + 4, true, m->stream);
-    // scratch of the build: only the new views' parts are written and read
-    m->s_vox.reserve(ib, false, m->stream);
-    m->s_rec.reserve(ib * 2, false, m->stream);
+    // scratch of the build: the new views' incidences only, from the first
+    // new one on (the arenas' retired lists need none)
+    m->scratch_base = (uint32_t)m->n_inc;
+    const size_t sb = (size_t)std::max<int64_t>(n_inc - m->n_inc, 1) * 4;
+    m->s_vox.reserve(sb, false, m->stream);
+    m->s_rec.reserve(sb * 2, false, m->stream);
   }
   for (size_t k = 0; k < added.size(); ++k) emit_view(m, added[k], m->s_offs.as<uint32_t>() + coff[k]);
   // the new views' ray records on the host, and their counters
@@ -1259,7 +1267,7 @@ bool append_lists(mrf_map* m) {
   }
   for (int c : added)
     CK(launch_loud_voxels(m->meta.as<RayMeta>() + m->views[c].pix_base, view_pixels(m->views[c]),
-                          m->s_vox.as<uint32_t>(), m->s_loud.as<uint8_t>(), m->stream));
+                          m->s_vox.as<uint32_t>(), m->scratch_base, m->s_loud.as<uint8_t>(), m->stream));
   // an old view's quiet pairs (numbered after its loud ones) must all stay
   // quiet: where one became loud, the view prepares every pair
   m->s_k1.reserve(64, false, m->stream);
@@ -1426,7 +1434,7 @@ void ensure_compact(mrf_map* m) {
 // Retired views' lists stay in the arenas until they reach kDeadRatio times
 // the live ones; the next build is then a full one, which drops them.  Only
 // memory grows with them: no per-frame pass reads a retired view's data.
-constexpr int64_t kDeadRatio = 4;
+constexpr int64_t kDeadRatio = 8;
 
 void ensure_built(mrf_map* m) {
   if (m->built_version != m->version) {

@@ -111,9 +111,10 @@ cudaError_t launch_brick_first(const uint32_t* pair_vox, const uint32_t* key, ui
 cudaError_t launch_brick_keys(const uint32_t* order, uint32_t np, const uint32_t* pair_vox,
                               const uint32_t* bfirst, const uint8_t* loud, int bits, uint32_t* key,
                               cudaStream_t s);
-// voxels with a dynamic incidence in any view, and the pairs on them
-cudaError_t launch_loud_voxels(const RayMeta* meta, int64_t npix, const uint32_t* vox, uint8_t* loud,
-                               cudaStream_t s);
+// voxels with a dynamic incidence in any view (vox[k]: the voxel of
+// incidence vox_base + k), and the pairs on them
+cudaError_t launch_loud_voxels(const RayMeta* meta, int64_t npix, const uint32_t* vox, uint32_t vox_base,
+                               uint8_t* loud, cudaStream_t s);
 // the same with each incidence's voxel from its pair (vox = pair_vox[inc_pair])
 cudaError_t launch_loud_voxels_from_pairs(const RayMeta* meta, int64_t npix, const uint32_t* inc_pair,
                                           const uint32_t* pair_vox, uint8_t* loud, cudaStream_t s);
