@@ -7,8 +7,8 @@ Everything numeric runs in the library's own kernels through the C ABI
 (features ``mrf_warm_features``; network forward, gradients and Adam
 ``mrf_net_*``, BF16 tensor-core convolutions with FP32 accumulation).  torch
 only provides device buffers and the stream.  Plain BP from the prior stays
-the judge: a warm-started map is accepted only when its converged beliefs
-match the plain run's.
+the reference result: a warm-started map is accepted only when its
+converged beliefs match the plain run's.
 """
 from __future__ import annotations
 

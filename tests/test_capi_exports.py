@@ -50,3 +50,32 @@ def test_create_rejects_bad_params(native_lib):
     assert native_lib.mrf_create(C.byref(s), C.byref(h)) == 1
     assert b"invalid" in native_lib.mrf_last_error()
     assert native_lib.mrf_infer(None, None, 0, 1, 0) == 1
+
+
+def test_ctypes_structs_match_the_header(tmp_path):
+    """lib.py's ctypes mirrors of mrf_params and mrf_stats have the header's
+    layout: a C compiler reports every field's offset and each struct's
+    size, which must equal ctypes' (a field added to one side only moves an
+    offset or the size)."""
+    import ctypes as C
+
+    from mrfmap_gb300 import lib
+    structs = (("mrf_params", lib.mrf_params), ("mrf_stats", lib.mrf_stats))
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "mrfmap_gb300.h"', "int main(void) {"]
+    for cname, cls in structs:
+        lines.append(f'printf("{cname} sizeof %zu\\n", sizeof({cname}));')
+        for fname, _ in cls._fields_:
+            lines.append(f'printf("{cname} {fname} %zu\\n", offsetof({cname}, {fname}));')
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = {}
+    for line in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.splitlines():
+        cname, fname, v = line.split()
+        got[(cname, fname)] = int(v)
+    for cname, cls in structs:
+        assert got[(cname, "sizeof")] == C.sizeof(cls), cname
+        for fname, _ in cls._fields_:
+            assert got[(cname, fname)] == getattr(cls, fname).offset, f"{cname}.{fname}"

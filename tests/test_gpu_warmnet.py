@@ -1,7 +1,7 @@
 """The learned warm start on the GPU: the network's forward pass and
 gradients against the CPU reference (oracle/warmnet.py), training on the
 project's own kernels, the features, and the warm-started BP against plain
-BP (the judge)."""
+BP (whose converged map is the reference result)."""
 import numpy as np
 import pytest
 
