@@ -198,8 +198,12 @@ MRF_API mrf_status mrf_set_pose(mrf_map* map, int view_id, const float* pose);
 /* Takes a view out of the set BP iterates (no reference counterpart: the
  * bounded keyframe window of a long incremental run, whose early keyframes'
  * incidence lists would not fit in memory).  The view's current messages
- * stay in the total log-odds for good; its incidence lists, pairs and depth
- * image are dropped at the next build.  Its id stays reserved: mrf_infer
+ * stay in the total log-odds for good and its depth image is released.  Its
+ * incidence lists and pairs leave every launch at once; their memory is
+ * reclaimed by the next full build, which runs once the retired views'
+ * lists reach eight times the live ones, when appending new views runs out
+ * of device memory, or before a call that needs every view's structures
+ * (Jacobi, warm start).  Its id stays reserved: mrf_infer
  * passes over it and the per-view calls (likelihood, renders, messages,
  * incidences, set_pose) fail with MRF_ERR_STATE.  mrf_reset_state forgets
  * retired views' messages with everything else. */
