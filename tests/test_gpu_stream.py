@@ -259,3 +259,41 @@ def test_failed_append_falls_back_to_a_full_build(native_lib, oracle_lib, walk):
     for m in maps.values():
         m.close()
     om.close()
+
+
+def test_quiet_prefix_on_appended_lists(native_lib, oracle_lib, walk):
+    """The static prefixes taken from their quiet sums (forced,
+    MRF_QUIET_PREFIX) on lists built by appending one view at a time: an
+    older view whose quiet pair turned loud when a later view was appended
+    counts all its pairs as loud, so the fast path and the full ray path
+    (MRF_FULL_RAYS) on the same lists agree to FP32 rounding of the
+    regrouped prefix sums (within 5e-5: 1.1e-5 at one voxel of 457,216
+    after 6 iterations, the rest within 1e-5), and both agree with the
+    oracle within 1e-3 at >= 99.9 % class agreement."""
+    w, depths = walk
+    n = 8
+    om = O.OracleMap(w.params, threads=8)
+    for k in range(n):
+        om.add_view(w.poses[k], depths[k], O.ACT_FULL_RAY)
+    om.infer(iters=ITERS + 1)
+    ob = om.beliefs()
+    om.close()
+    m = L.MRFMap(w.params, activation=L.ACT_FULL_RAY)
+    for k in range(n):
+        m.add_view(w.poses[k], depths[k])
+        m.infer(iters=1, flags=L.INCREMENTAL)  # one build per view: appended
+    assert m.stats()["builds_appended"] == n - 1
+    out = {}
+    for name, extra in (("fast", L.QUIET_PREFIX), ("full", L.FULL_RAYS)):
+        m.reset_state()
+        m.infer(iters=ITERS + 1, flags=extra)
+        st = m.stats()
+        assert st["quiet_prefix_used"] == (1 if name == "fast" else 0)
+        assert st["builds_appended"] == n - 1 and st["builds_full"] == 1  # the same lists for both
+        emax, agree = _compare(m.beliefs(), ob)
+        assert emax <= 1e-3, f"{name}: max belief error {emax}"
+        assert agree >= 0.999, f"{name}: class agreement {agree}"
+        out[name] = m.beliefs()
+    np.testing.assert_allclose(out["fast"], out["full"], rtol=0, atol=5e-5)
+    assert (np.abs(out["fast"] - out["full"]) > 1e-5).sum() <= 10
+    m.close()
