@@ -147,6 +147,20 @@ MRF_API mrf_status mrf_test_raise_device_error(mrf_map* map);
  * host) and *all (1: the footprint covers the whole image). */
 MRF_API mrf_status mrf_test_brick_footprint(mrf_map* map, int view_id, int64_t b0, int64_t b1,
                                             uint8_t* mask, int* all);
+/* Test hook, no reference counterpart (host only: no device call, no map):
+ * the SM-affine schedule of one view's rays as an incidence build makes it
+ * from the view's ray records.  records: n_pix triples {n_pre, n_post,
+ * k_dyn} in pixel order (each in [0, 65535]); the rays in BP are those with
+ * n_pre > 0 and k_dyn < n_post.  The view's pixels are cut into `regions`
+ * runs of consecutive pixels holding equal shares of the BP rays' Pre
+ * incidences; region r's home rays, its longest ones up to `share` per cent
+ * of its incidences, are home[starts[r] .. starts[r+1]) (longest first,
+ * pixel order within a length; starts has regions + 1 entries); the other
+ * BP rays are left[0 .. *n_left), longest first.  home and left must hold
+ * n_pix entries. */
+MRF_API mrf_status mrf_test_region_lists(const int32_t* records, int64_t n_pix, int regions, int share,
+                                         uint32_t* home, int64_t* n_home, uint32_t* starts, uint32_t* left,
+                                         int64_t* n_left);
 /* Test hook, no reference counterpart: the next build that appends new
  * views' lists fails with `status` once their pairs are built (a host-side
  * stand-in for a failing allocation or CUDA call part-way through).  An

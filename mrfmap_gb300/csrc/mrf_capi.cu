@@ -2040,6 +2040,41 @@ mrf_status mrf_test_raise_device_error(mrf_map* m) {
   });
 }
 
+mrf_status mrf_test_region_lists(const int32_t* records, int64_t n_pix, int regions, int share, uint32_t* home,
+                                 int64_t* n_home, uint32_t* starts, uint32_t* left, int64_t* n_left) {
+  if (!records || n_pix < 0 || n_pix > (int64_t)0x7FFFFFFF || regions < 1 || share < 0 || share > 100 || !home ||
+      !n_home || !starts || !left || !n_left) {
+    set_err("mrf_test_region_lists: invalid arguments");
+    return MRF_ERR_INVALID;
+  }
+  return wrap([&] {
+    std::vector<RayMeta> hm((size_t)n_pix);
+    for (int64_t i = 0; i < n_pix; ++i) {
+      const int32_t* r = records + 3 * i;
+      for (int k = 0; k < 3; ++k)
+        if (r[k] < 0 || r[k] > 65535) fail(MRF_ERR_INVALID, "mrf_test_region_lists: fields must lie in [0, 65535]");
+      RayMeta me{};
+      me.n_pre = (uint16_t)r[0];
+      me.n_post = (uint16_t)r[1];
+      me.flags = (uint32_t)r[2] << 16;
+      hm[(size_t)i] = me;
+    }
+    View v;
+    v.cam.rows = 1;
+    v.cam.cols = (int)n_pix;
+    v.pix_base = 0;
+    v.retired = false;
+    RegionLists l;
+    region_lists(v, hm.data(), regions, share, l);
+    std::copy(l.home.begin(), l.home.end(), home);
+    std::copy(l.left.begin(), l.left.end(), left);
+    for (int r = 0; r < regions; ++r) starts[r] = r < (int)l.starts.size() ? l.starts[(size_t)r] : 0u;
+    starts[regions] = (uint32_t)l.home.size();
+    *n_home = (int64_t)l.home.size();
+    *n_left = (int64_t)l.left.size();
+  });
+}
+
 mrf_status mrf_test_fail_next_append(mrf_map* m, mrf_status status) {
   if (guard(m) != MRF_OK) return MRF_ERR_INVALID;
   if (status == MRF_OK) {

@@ -47,7 +47,8 @@ EXPORTS = ["mrf_create", "mrf_destroy", "mrf_release_cached_memory", "mrf_last_e
            "mrf_view_camera", "mrf_set_memory_limit", "mrf_memory_in_use", "mrf_test_raise_device_error",
            "mrf_infer_until", "mrf_retire_view", "mrf_add_view_box", "mrf_autotune_flags",
            "mrf_set_precision", "mrf_set_home_share", "mrf_autotune_home_share", "mrf_get_tuning",
-           "mrf_set_pair_variant", "mrf_test_brick_footprint", "mrf_test_fail_next_append"]
+           "mrf_set_pair_variant", "mrf_test_brick_footprint", "mrf_test_fail_next_append",
+           "mrf_test_region_lists"]
 
 RENDER_EXPECTED_DEPTH = 0
 RENDER_ACCURACY = 1
@@ -166,6 +167,8 @@ def load(path: str | None = None):
         "mrf_memory_in_use": ([], C.c_int64),
         "mrf_test_raise_device_error": ([vp], C.c_int),
         "mrf_test_fail_next_append": ([vp, C.c_int], C.c_int),
+        "mrf_test_region_lists": ([C.POINTER(C.c_int32), C.c_int64, C.c_int, C.c_int, C.POINTER(C.c_uint32),
+                                   i64p, C.POINTER(C.c_uint32), C.POINTER(C.c_uint32), i64p], C.c_int),
         "mrf_test_brick_footprint": ([vp, C.c_int, C.c_int64, C.c_int64, C.POINTER(C.c_uint8), ip], C.c_int),
     }
     for name, (args, res) in sig.items():
