@@ -290,13 +290,13 @@ def summarize(rows, accept_tol: float = 1e-3, agree_min: float = 0.999):
     for k in ("plain", "learned", "prior"):
         out[k + "_ms"] = mean(k + "_ms")
         out[k + "_start_ms"] = mean(k + "_start_ms")
+        out[k + "_iters"] = mean(k + "_iters")
     if rows and "net_forward_ms" in rows[0]:
         # the convolutions' rate: 9072 multiply-adds per voxel (27 taps x
         # (4x16 + 16x16 + 16x1)), 512 voxels per brick
         out["net_forward_ms"] = float(np.mean([r["net_forward_ms"] for r in rows]))
         out["net_forward_tflops"] = float(np.mean([2 * 9072 * 512 * r["n_bricks"] / (r["net_forward_ms"] * 1e9)
                                                    for r in rows]))
-        out[k + "_iters"] = mean(k + "_iters")
     if ok:
         out["speedup_learned_vs_plain"] = out["plain_ms"] / out["learned_ms"]
         out["speedup_prior_vs_plain"] = out["plain_ms"] / out["prior_ms"]
